@@ -1,0 +1,160 @@
+"""ctypes binding of the CPU restatement (awg_oracle.cpp).
+
+Test infrastructure: imported only by tests/, __graft_entry__.smoke() and bench.py's CPU
+leg, as the checker the CUDA path is compared against. It never feeds the product path.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "liboracle.so")
+_lib = None
+
+
+class OracleProblem(C.Structure):
+    _fields_ = [("ntrees", C.c_int), ("nnodes", C.c_int), ("ntimes", C.c_int),
+                ("nseqs", C.c_int), ("seqlen", C.c_int), ("internal", C.c_int),
+                ("start_coord", C.c_int), ("minage", C.c_int),
+                ("ptrees", C.c_void_p), ("ages", C.c_void_p), ("sprs", C.c_void_p),
+                ("blocklens", C.c_void_p), ("mapping", C.c_void_p),
+                ("root_child0", C.c_void_p), ("times", C.c_void_p),
+                ("popsizes", C.c_void_p), ("rho", C.c_double), ("mu", C.c_double),
+                ("seqs", C.c_void_p)]
+
+
+def build() -> str:
+    subprocess.run(["make", "-s", "-C", HERE, "oracle"], check=True)
+    return LIB
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        lib = C.CDLL(LIB)
+        P = C.POINTER(OracleProblem)
+        for name, args in [("oracle_nstates", [P, C.c_void_p]),
+                           ("oracle_forward", [P, C.c_void_p, C.c_void_p]),
+                           ("oracle_traceback", [P, C.c_void_p, C.c_void_p, C.c_void_p]),
+                           ("oracle_backward", [P, C.c_void_p]),
+                           ("oracle_posterior", [P, C.c_void_p, C.c_void_p, C.c_void_p]),
+                           ("oracle_block_terms", [P, C.c_void_p, C.c_void_p]),
+                           ("oracle_emissions", [P, C.c_void_p])]:
+            fn = getattr(lib, name)
+            fn.restype = C.c_int
+            fn.argtypes = args
+        lib.oracle_cells.restype = C.c_longlong
+        lib.oracle_cells.argtypes = [P]
+        _lib = lib
+    return _lib
+
+
+class Bound:
+    """A problem pinned in memory with its C view."""
+
+    def __init__(self, prob):
+        self.p = prob.normalized()
+        p = self.p
+        ptr = lambda a: None if a is None else a.ctypes.data
+        self.c = OracleProblem(p.ntrees, p.nnodes, p.ntimes, p.nseqs, p.seqlen,
+                               int(p.internal), p.start_coord, 0,
+                               ptr(p.ptrees), ptr(p.ages), ptr(p.sprs), ptr(p.blocklens),
+                               ptr(p.mapping), ptr(p.root_child0), ptr(p.times),
+                               ptr(p.popsizes), p.rho, p.mu, ptr(p.seqs))
+
+    @property
+    def ref(self):
+        return C.byref(self.c)
+
+
+def _check(rc, what):
+    if rc != 0:
+        raise ValueError(f"oracle {what} rejected the problem (code {rc})")
+
+
+def nstates(prob) -> np.ndarray:
+    b = Bound(prob)
+    out = np.zeros(prob.seqlen, dtype=np.int32)
+    _check(load().oracle_nstates(b.ref, out.ctypes.data), "nstates")
+    return out
+
+
+def offsets(ns: np.ndarray) -> np.ndarray:
+    off = np.zeros(ns.shape[0] + 1, dtype=np.int64)
+    np.cumsum(np.maximum(ns, 1), out=off[1:])
+    return off
+
+
+def forward(prob):
+    """Packed forward table and the log-likelihood from the column norms."""
+    b = Bound(prob)
+    lib = load()
+    ncells = lib.oracle_cells(b.ref)
+    if ncells < 0:
+        raise ValueError("oracle rejected the problem")
+    fw = np.zeros(ncells, dtype=np.float64)
+    lnl = C.c_double(0.0)
+    _check(lib.oracle_forward(b.ref, fw.ctypes.data, C.addressof(lnl)), "forward")
+    return fw, lnl.value
+
+
+def traceback(prob, fw: np.ndarray, u: np.ndarray) -> np.ndarray:
+    b = Bound(prob)
+    fw = np.ascontiguousarray(fw, dtype=np.float64)
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    path = np.zeros(prob.seqlen, dtype=np.int32)
+    _check(load().oracle_traceback(b.ref, fw.ctypes.data, u.ctypes.data, path.ctypes.data),
+           "traceback")
+    return path
+
+
+def backward(prob) -> np.ndarray:
+    b = Bound(prob)
+    lib = load()
+    bw = np.zeros(lib.oracle_cells(b.ref), dtype=np.float64)
+    _check(lib.oracle_backward(b.ref, bw.ctypes.data), "backward")
+    return bw
+
+
+def posterior(prob, fw: np.ndarray, bw: np.ndarray) -> np.ndarray:
+    b = Bound(prob)
+    post = np.zeros_like(fw)
+    _check(load().oracle_posterior(b.ref, np.ascontiguousarray(fw).ctypes.data,
+                                   np.ascontiguousarray(bw).ctypes.data, post.ctypes.data),
+           "posterior")
+    return post
+
+
+def block_terms(prob):
+    b = Bound(prob)
+    T = prob.ntimes
+    out = np.zeros((prob.ntrees, 9, T), dtype=np.float64)
+    minage = np.zeros(prob.ntrees, dtype=np.int32)
+    _check(load().oracle_block_terms(b.ref, out.ctypes.data, minage.ctypes.data), "terms")
+    return out, minage
+
+
+def emissions(prob) -> np.ndarray:
+    b = Bound(prob)
+    lib = load()
+    out = np.zeros(lib.oracle_cells(b.ref), dtype=np.float64)
+    _check(lib.oracle_emissions(b.ref, out.ctypes.data), "emissions")
+    return out
+
+
+def rand_uniforms(seed: int, n: int) -> np.ndarray:
+    """The uniforms the reference's traceback draws after srand(seed): rand()/RAND_MAX,
+    one per column, last column first (sample_thread.cpp:537, common.h:103-110).
+    Returned indexed by column."""
+    libc = C.CDLL(None)
+    libc.srand(C.c_uint(seed))
+    rmax = 2147483647.0  # glibc RAND_MAX
+    draws = np.array([libc.rand() / rmax for _ in range(n)], dtype=np.float64)
+    return draws[::-1].copy()

@@ -1,0 +1,407 @@
+// Fixture harness around the compiled reference library (oracle/_ref/libargweaver.a).
+//
+// Test infrastructure only, run where the reference checkout exists. It reads a
+// problem file (format below, written by argweaver_gb300/problem.py), runs the
+// reference's own C++ threading HMM on it and writes the results as golden data:
+//
+//   forward <problem> <out> <seed>   forward table (arghmm_forward_alg, sample_thread.cpp:394)
+//                                    + stochastic_traceback (sample_thread.cpp:522) after
+//                                    srand(seed); per-column nstates (states.cpp:209)
+//   tables  <problem> <out>          per-block TransMatrix terms (trans.cpp:26),
+//                                    TransMatrixSwitch (trans.cpp:538), emissions (emit.cpp:650)
+//   dense   <problem> <out>          single-block problems: the reference's dense log-space
+//                                    backward_alg (hmm.cpp:48) on calc_transition_probs
+//                                    (trans.cpp:136) + calc_emissions, for the backward oracle
+//   sim1    <sites> <smc> <c> <out>  reads a sites file + SMC ARG the way arg-sample does
+//                                    (arg-sample.cpp:996-1155), removes the last sequence's
+//                                    thread (thread.cpp:425) and writes the external problem
+//   cut     <problem> <seed> <out>   samples a uniform removal path (thread.h:130) and cuts it
+//                                    (remove_arg_thread_path, thread.h:43): internal problem
+//
+// Problem file (little endian): "AWGPROB1"; int32 ntrees,nnodes,ntimes,nseqs,seqlen,
+// internal,start_coord,pad; f64 rho,mu; f64 times[T]; f64 popsizes[T];
+// i32 ptrees[ntrees*nnodes]; i32 ages[ntrees*nnodes]; i32 sprs[ntrees*4];
+// i32 blocklens[ntrees]; u8 seqs[nseqs*seqlen]. The header's last int32 holds flags:
+// bit 0: i32 mapping[ntrees*nnodes] follows: LocalTreeSpr::mapping (previous tree node ->
+//        this tree node, -1 for the broken node; row 0 unused). Without it the mapping is
+//        the reference's make_node_mapping (local_tree.h:767).
+// bit 1: i32 root_child0[ntrees] follows: child[0] of each tree's root. The reference
+//        names the cut subtree of an internal-branch tree child[0] of the virtual root
+//        (states.cpp:121); parent arrays alone order children by index
+//        (local_tree.h:216-229), which cannot express every cut.
+
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "argweaver/common.h"
+#include "argweaver/compress.h"
+#include "argweaver/emit.h"
+#include "argweaver/hmm.h"
+#include "argweaver/local_tree.h"
+#include "argweaver/matrices.h"
+#include "argweaver/model.h"
+#include "argweaver/sample_thread.h"
+#include "argweaver/sequences.h"
+#include "argweaver/states.h"
+#include "argweaver/thread.h"
+#include "argweaver/trans.h"
+
+using namespace argweaver;
+using std::vector;
+
+// extern "C" entry points the reference defines without a header declaration
+namespace argweaver {
+extern "C" {
+void get_local_trees_ptrees(LocalTrees *trees, int **ptrees, int **ages, int **sprs,
+                            int *blocklens);          // local_tree.cpp:1846
+void arghmm_get_nstates(LocalTrees *trees, int ntimes, bool internal,
+                        int *nstates);                // states.cpp:209
+}
+}
+
+struct Problem {
+    int ntrees = 0, nnodes = 0, ntimes = 0, nseqs = 0, seqlen = 0;
+    int internal = 0, start_coord = 0;
+    double rho = 0, mu = 0;
+    vector<double> times, popsizes;
+    vector<int> ptrees, ages, sprs, blocklens;
+    vector<char> seqs;
+    vector<int> mapping;      // empty: make_node_mapping default
+    vector<int> root_child0;  // empty: children ordered by index
+};
+
+static void die(const char *msg) { fprintf(stderr, "ref_harness: %s\n", msg); exit(1); }
+
+template <class T> static void rd(FILE *f, T *p, size_t n) {
+    if (n && fread(p, sizeof(T), n, f) != n) die("short read");
+}
+template <class T> static void wr(FILE *f, const T *p, size_t n) {
+    if (n && fwrite(p, sizeof(T), n, f) != n) die("short write");
+}
+
+static Problem read_problem(const char *path) {
+    FILE *f = fopen(path, "rb");
+    if (!f) die("cannot open problem");
+    char magic[8];
+    rd(f, magic, 8);
+    if (memcmp(magic, "AWGPROB1", 8) != 0) die("bad problem magic");
+    Problem p;
+    int hdr[8];
+    rd(f, hdr, 8);
+    p.ntrees = hdr[0]; p.nnodes = hdr[1]; p.ntimes = hdr[2]; p.nseqs = hdr[3];
+    p.seqlen = hdr[4]; p.internal = hdr[5]; p.start_coord = hdr[6];
+    rd(f, &p.rho, 1); rd(f, &p.mu, 1);
+    p.times.resize(p.ntimes); p.popsizes.resize(p.ntimes);
+    rd(f, p.times.data(), p.ntimes); rd(f, p.popsizes.data(), p.ntimes);
+    size_t tn = (size_t)p.ntrees * p.nnodes;
+    p.ptrees.resize(tn); p.ages.resize(tn); p.sprs.resize(p.ntrees * 4);
+    p.blocklens.resize(p.ntrees);
+    rd(f, p.ptrees.data(), tn); rd(f, p.ages.data(), tn);
+    rd(f, p.sprs.data(), p.sprs.size()); rd(f, p.blocklens.data(), p.ntrees);
+    p.seqs.resize((size_t)p.nseqs * p.seqlen);
+    rd(f, p.seqs.data(), p.seqs.size());
+    if (hdr[7] & 1) {
+        p.mapping.resize(tn);
+        rd(f, p.mapping.data(), tn);
+    }
+    if (hdr[7] & 2) {
+        p.root_child0.resize(p.ntrees);
+        rd(f, p.root_child0.data(), p.ntrees);
+    }
+    fclose(f);
+    return p;
+}
+
+static void write_problem(const char *path, const Problem &p) {
+    FILE *f = fopen(path, "wb");
+    if (!f) die("cannot write problem");
+    wr(f, "AWGPROB1", 8);
+    int hdr[8] = {p.ntrees, p.nnodes, p.ntimes, p.nseqs, p.seqlen, p.internal,
+                  p.start_coord,
+                  (p.mapping.empty() ? 0 : 1) | (p.root_child0.empty() ? 0 : 2)};
+    wr(f, hdr, 8);
+    wr(f, &p.rho, 1); wr(f, &p.mu, 1);
+    wr(f, p.times.data(), p.ntimes); wr(f, p.popsizes.data(), p.ntimes);
+    wr(f, p.ptrees.data(), p.ptrees.size()); wr(f, p.ages.data(), p.ages.size());
+    wr(f, p.sprs.data(), p.sprs.size()); wr(f, p.blocklens.data(), p.blocklens.size());
+    wr(f, p.seqs.data(), p.seqs.size());
+    if (!p.mapping.empty()) wr(f, p.mapping.data(), p.mapping.size());
+    if (!p.root_child0.empty()) wr(f, p.root_child0.data(), p.root_child0.size());
+    fclose(f);
+}
+
+// Build the reference's LocalTrees from the flat arrays (local_tree.cpp:321).
+static LocalTrees *make_trees(Problem &p) {
+    vector<int *> pt(p.ntrees), ag(p.ntrees), sp(p.ntrees);
+    for (int i = 0; i < p.ntrees; i++) {
+        pt[i] = &p.ptrees[(size_t)i * p.nnodes];
+        ag[i] = &p.ages[(size_t)i * p.nnodes];
+        sp[i] = &p.sprs[(size_t)i * 4];
+    }
+    LocalTrees *trees = new LocalTrees(pt.data(), ag.data(), sp.data(), p.blocklens.data(),
+                                       p.ntrees, p.nnodes, -1, p.start_coord);
+    if (!p.mapping.empty()) {
+        int i = 0;
+        for (LocalTrees::iterator it = trees->begin(); it != trees->end(); ++it, ++i)
+            if (it->mapping)
+                for (int j = 0; j < p.nnodes; j++)
+                    it->mapping[j] = p.mapping[(size_t)i * p.nnodes + j];
+    }
+    if (!p.root_child0.empty()) {
+        int i = 0;
+        for (LocalTrees::iterator it = trees->begin(); it != trees->end(); ++it, ++i) {
+            LocalNode &r = it->tree->nodes[it->tree->root];
+            if (r.child[0] != p.root_child0[i]) std::swap(r.child[0], r.child[1]);
+        }
+    }
+    return trees;
+}
+
+// Flatten a LocalTrees back to arrays (get_local_trees_ptrees, local_tree.cpp:1846).
+static void trees_to_problem(LocalTrees *trees, Problem &p) {
+    p.ntrees = trees->get_num_trees();
+    p.nnodes = trees->nnodes;
+    p.start_coord = trees->start_coord;
+    size_t tn = (size_t)p.ntrees * p.nnodes;
+    p.ptrees.assign(tn, 0); p.ages.assign(tn, 0);
+    p.sprs.assign(p.ntrees * 4, 0); p.blocklens.assign(p.ntrees, 0);
+    vector<int *> pt(p.ntrees), ag(p.ntrees), sp(p.ntrees);
+    for (int i = 0; i < p.ntrees; i++) {
+        pt[i] = &p.ptrees[(size_t)i * p.nnodes];
+        ag[i] = &p.ages[(size_t)i * p.nnodes];
+        sp[i] = &p.sprs[(size_t)i * 4];
+    }
+    get_local_trees_ptrees(trees, pt.data(), ag.data(), sp.data(), p.blocklens.data());
+    // mappings, in the same leaf permutation get_local_trees_ptrees applies
+    const int nleaves = trees->get_num_leaves();
+    vector<int> perm(p.nnodes);
+    for (int j = 0; j < p.nnodes; j++) perm[j] = j < nleaves ? trees->seqids[j] : j;
+    p.mapping.assign(tn, -1);
+    int i = 0;
+    for (LocalTrees::iterator it = trees->begin(); it != trees->end(); ++it, ++i)
+        if (it->mapping)
+            for (int j = 0; j < p.nnodes; j++) {
+                int m = it->mapping[j];
+                p.mapping[(size_t)i * p.nnodes + perm[j]] = m == -1 ? -1 : perm[m];
+            }
+    p.root_child0.assign(p.ntrees, -1);
+    i = 0;
+    for (LocalTrees::iterator it = trees->begin(); it != trees->end(); ++it, ++i) {
+        LocalTree *t = it->tree;
+        int c0 = t->nodes[t->root].child[0];
+        p.root_child0[i] = c0 == -1 ? -1 : perm[c0];
+    }
+}
+
+static vector<char *> seq_ptrs(Problem &p) {
+    vector<char *> s(p.nseqs);
+    for (int i = 0; i < p.nseqs; i++) s[i] = &p.seqs[(size_t)i * p.seqlen];
+    return s;
+}
+
+static int cmd_forward(const char *in, const char *out, int seed) {
+    Problem p = read_problem(in);
+    LocalTrees *trees = make_trees(p);
+    ArgModel model(p.ntimes, p.times.data(), p.popsizes.data(), p.rho, p.mu);
+    vector<char *> sp = seq_ptrs(p);
+    Sequences sequences(sp.data(), p.nseqs, p.seqlen);
+    const bool internal = p.internal != 0;
+
+    ArgHmmMatrixList matrix_list(&model, &sequences, trees);
+    matrix_list.set_internal(internal);
+    matrix_list.setup();
+    ArgHmmForwardTable forward(trees->start_coord, trees->length());
+    arghmm_forward_alg(trees, &model, &sequences, &matrix_list, &forward, NULL,
+                       false, internal, false);
+    double **fw = forward.get_table();
+
+    vector<int> nstates(p.seqlen);
+    arghmm_get_nstates(trees, p.ntimes, internal, nstates.data());
+
+    srand(seed);
+    vector<int> path(p.seqlen);
+    stochastic_traceback(trees, &model, &matrix_list, fw, path.data() - trees->start_coord,
+                         false, internal);
+
+    FILE *f = fopen(out, "wb");
+    if (!f) die("cannot write output");
+    wr(f, "AWGREF01", 8);
+    long long ncells = 0;
+    for (int i = 0; i < p.seqlen; i++) ncells += std::max(nstates[i], 1);
+    int hdr[2] = {p.seqlen, 0};
+    wr(f, hdr, 2);
+    wr(f, &ncells, 1);
+    wr(f, nstates.data(), p.seqlen);
+    for (int i = 0; i < p.seqlen; i++)
+        wr(f, fw[trees->start_coord + i], std::max(nstates[i], 1));
+    wr(f, path.data(), p.seqlen);
+    fclose(f);
+    delete trees;
+    return 0;
+}
+
+static int cmd_tables(const char *in, const char *out) {
+    Problem p = read_problem(in);
+    LocalTrees *trees = make_trees(p);
+    ArgModel model(p.ntimes, p.times.data(), p.popsizes.data(), p.rho, p.mu);
+    vector<char *> sp = seq_ptrs(p);
+    Sequences sequences(sp.data(), p.nseqs, p.seqlen);
+    const bool internal = p.internal != 0;
+    const int T = p.ntimes;
+
+    ArgHmmMatrixList matrix_list(&model, &sequences, trees);
+    matrix_list.set_internal(internal);
+    matrix_list.setup();
+
+    FILE *f = fopen(out, "wb");
+    if (!f) die("cannot write output");
+    wr(f, "AWGTAB01", 8);
+    int nblocks = 0;
+    for (matrix_list.begin(); matrix_list.more(); matrix_list.next()) nblocks++;
+    wr(f, &nblocks, 1);
+    for (matrix_list.begin(); matrix_list.more(); matrix_list.next()) {
+        ArgHmmMatrices &m = matrix_list.ref_matrices();
+        int hdr[6] = {matrix_list.get_block_start(), m.blocklen, m.nstates1, m.nstates2,
+                      m.transmat_switch ? 1 : 0, m.transmat->minage};
+        wr(f, hdr, 6);
+        const TransMatrix *tm = m.transmat;
+        // entries [0, T-2] are the ones calc_transition_probs writes
+        const double *arrs[9] = {tm->D, tm->E, tm->lnB, tm->lnE2, tm->lnNegG1,
+                                 tm->G2, tm->G3, tm->lnG4, tm->norecombs};
+        for (int a = 0; a < 9; a++) wr(f, arrs[a], T - 1);
+        if (m.transmat_switch) {
+            const TransMatrixSwitch *sw = m.transmat_switch;
+            int n1 = std::max(sw->nstates1, 1), n2 = std::max(sw->nstates2, 1);
+            int src[2] = {sw->recombsrc, sw->recoalsrc};
+            wr(f, src, 2);
+            wr(f, sw->determ, n1);
+            wr(f, sw->determprob, n1);
+            // rows are only defined when their source exists
+            vector<double> zero(n2, 0.0);
+            wr(f, sw->recombsrc != -1 ? sw->recombrow : zero.data(), n2);
+            wr(f, sw->recoalsrc != -1 ? sw->recoalrow : zero.data(), n2);
+        }
+        int S = std::max(m.nstates2, 1);
+        for (int i = 0; i < m.blocklen; i++) wr(f, m.emit[i], S);
+    }
+    fclose(f);
+    delete trees;
+    return 0;
+}
+
+// Dense log-space backward of the reference's generic HMM on one block.
+static int cmd_dense(const char *in, const char *out) {
+    Problem p = read_problem(in);
+    if (p.ntrees != 1 || p.internal) die("dense: single external tree only");
+    LocalTrees *trees = make_trees(p);
+    ArgModel model(p.ntimes, p.times.data(), p.popsizes.data(), p.rho, p.mu);
+    LocalTree *tree = trees->front().tree;
+    States states;
+    get_coal_states(tree, p.ntimes, states, false);
+    int S = states.size();
+    LineageCounts lineages(p.ntimes);
+    lineages.count(tree);
+    double **trans = new_matrix<double>(S, S);
+    calc_transition_probs(tree, &model, states, &lineages, trans);  // log values
+    double **emit = new_matrix<double>(p.seqlen, S);
+    vector<char *> sp = seq_ptrs(p);
+    calc_emissions_external(states, tree, sp.data(), p.nseqs, p.seqlen, &model, emit, NULL);
+    for (int i = 0; i < p.seqlen; i++)
+        for (int k = 0; k < S; k++) emit[i][k] = log(emit[i][k]);
+    double **bw = new_matrix<double>(p.seqlen, S);
+    for (int k = 0; k < S; k++) bw[p.seqlen - 1][k] = 0.0;
+    backward_alg(p.seqlen, S, trans, emit, bw);
+    FILE *f = fopen(out, "wb");
+    if (!f) die("cannot write output");
+    wr(f, "AWGDNS02", 8);
+    int hdr[2] = {p.seqlen, S};
+    wr(f, hdr, 2);
+    for (int i = 0; i < p.seqlen; i++) wr(f, bw[i], S);
+    for (int i = 0; i < S; i++) wr(f, trans[i], S);      // log transition matrix
+    for (int i = 0; i < p.seqlen; i++) wr(f, emit[i], S); // log emissions
+    fclose(f);
+    delete_matrix(trans, S); delete_matrix(emit, p.seqlen); delete_matrix(bw, p.seqlen);
+    delete trees;
+    return 0;
+}
+
+static int cmd_sim1(const char *sites_file, const char *smc_file, int compress,
+                    const char *out) {
+    const int ntimes = 20;
+    const double maxtime = 200e3, popsize = 1e4, rho = 1.6e-8, mu = 1.8e-8;
+    Sites sites;
+    CompressStream stream(sites_file);
+    if (!stream.stream || !read_sites(stream.stream, &sites, -1, -1)) die("cannot read sites");
+    stream.close();
+    SitesMapping mapping;
+    if (!find_compress_cols(&sites, compress, &mapping)) die("cannot compress");
+    compress_sites(&sites, &mapping);
+    Sequences sequences;
+    make_sequences_from_sites(&sites, &sequences);
+
+    ArgModel model(ntimes, maxtime, popsize, rho, mu);
+    LocalTrees *trees = new LocalTrees();
+    vector<std::string> seqnames;
+    CompressStream smc(smc_file, "r");
+    if (!smc.stream || !read_local_trees(smc.stream, model.times, model.ntimes, trees, seqnames))
+        die("cannot read smc");
+    if (!trees->set_seqids(seqnames, sequences.names)) die("seqids");
+    compress_local_trees(trees, &mapping, true);
+
+    // remove the thread of the last sequence (the one to re-thread)
+    const int nseqs = sequences.get_num_seqs();
+    remove_arg_thread(trees, nseqs - 1);
+
+    Problem p;
+    p.ntimes = ntimes;
+    p.rho = rho * compress;
+    p.mu = mu * compress;
+    p.times.assign(model.times, model.times + ntimes);
+    p.popsizes.assign(model.popsizes, model.popsizes + ntimes);
+    p.internal = 0;
+    trees_to_problem(trees, p);
+    // sequences in leaf order (seqids) followed by the new sequence
+    const int nleaves = trees->get_num_leaves();
+    p.nseqs = nleaves + 1;
+    p.seqlen = sequences.length();
+    p.seqs.resize((size_t)p.nseqs * p.seqlen);
+    // get_local_trees_ptrees writes leaf j at position seqids[j], so problem row r is
+    // sequence r; the re-threaded sequence comes last
+    for (int r = 0; r < nleaves; r++)
+        memcpy(&p.seqs[(size_t)r * p.seqlen], sequences.seqs[r], p.seqlen);
+    memcpy(&p.seqs[(size_t)nleaves * p.seqlen], sequences.seqs[nseqs - 1], p.seqlen);
+    write_problem(out, p);
+    delete trees;
+    return 0;
+}
+
+static int cmd_cut(const char *in, int seed, const char *out) {
+    Problem p = read_problem(in);
+    if (p.internal) die("cut: input must be a full (external-format) ARG");
+    LocalTrees *trees = make_trees(p);
+    srand(seed);
+    vector<int> path(trees->get_num_trees());
+    sample_arg_removal_path_uniform(trees, path.data());
+    remove_arg_thread_path(trees, path.data(), p.ntimes + 1);
+    Problem q = p;
+    q.internal = 1;
+    trees_to_problem(trees, q);
+    write_problem(out, q);
+    delete trees;
+    return 0;
+}
+
+int main(int argc, char **argv) {
+    if (argc < 2) die("usage: ref_harness forward|tables|dense|sim1|cut ...");
+    std::string cmd = argv[1];
+    if (cmd == "forward" && argc == 5) return cmd_forward(argv[2], argv[3], atoi(argv[4]));
+    if (cmd == "tables" && argc == 4) return cmd_tables(argv[2], argv[3]);
+    if (cmd == "dense" && argc == 4) return cmd_dense(argv[2], argv[3]);
+    if (cmd == "sim1" && argc == 6) return cmd_sim1(argv[2], argv[3], atoi(argv[4]), argv[5]);
+    if (cmd == "cut" && argc == 5) return cmd_cut(argv[2], atoi(argv[3]), argv[4]);
+    die("bad arguments");
+    return 1;
+}

@@ -1,0 +1,174 @@
+"""Generate the golden fixtures in tests/golden/ from the compiled reference.
+
+Run where the reference checkout exists (default /root/reference, or $AWG_REFERENCE):
+
+    python tests/golden/make_golden.py
+
+It builds the reference from its own sources (oracle/Makefile target ``ref``), writes
+each problem as an AWGPROB1 file and runs the reference's threading HMM on it through
+oracle/ref_harness.cpp. Each ``<name>.npz`` then holds, from the reference:
+
+  nstates      int32 [L]    states per column (arghmm_get_nstates, states.cpp:209)
+  colsum       f64   [L]    sum of each forward column
+  colwsum      f64   [L]    sum of fw[i][k] * w_k, w_k = 1 + ((k * 2654435761) % 1000) / 1000
+  rows         int32 [R]    sampled columns (every 32nd and the last)
+  rowvals      f64   [..]   those forward columns, packed
+  seed         int          srand seed of the traceback
+  uniforms     f64   [L]    rand()/RAND_MAX the traceback drew, indexed by column
+  path         int32 [L]    sampled state path (stochastic_traceback, sample_thread.cpp:522)
+and for single-tree problems the reference's dense log-space backward (hmm.cpp:48) with
+the log transition matrix (calc_transition_probs, trans.cpp:136) and log emissions it ran on:
+  dense_bw     f64   [L, S]
+  dense_trans  f64   [S, S]
+  dense_emit   f64   [L, S]
+
+Sources of the problems: examples/sim1 (the reference's bundled data, converted by
+the harness the way arg-sample reads it), the seeded DSMC generator of this project
+(argweaver_gb300/csrc/sim.cpp), and internal-branch cuts made by the reference's own
+removal-path code (remove_arg_thread_path) on simulated full ARGs.
+"""
+
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+from argweaver_gb300.problem import Problem  # noqa: E402
+from argweaver_gb300.sim import simulate  # noqa: E402
+import pyoracle  # noqa: E402
+
+REF = os.environ.get("AWG_REFERENCE", "/root/reference")
+HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
+
+
+def weights(n: int) -> np.ndarray:
+    k = np.arange(n, dtype=np.int64)
+    return 1.0 + ((k * 2654435761) % 1000) / 1000.0
+
+
+def read_ref(path: str):
+    d = open(path, "rb").read()
+    assert d[:8] == b"AWGREF01"
+    L = int(np.frombuffer(d, np.int32, 1, 8)[0])
+    ncells = int(np.frombuffer(d, np.int64, 1, 16)[0])
+    off = 24
+    ns = np.frombuffer(d, np.int32, L, off).copy(); off += 4 * L
+    fw = np.frombuffer(d, np.float64, ncells, off).copy(); off += 8 * ncells
+    path = np.frombuffer(d, np.int32, L, off).copy()
+    return ns, fw, path
+
+
+def read_dense(path: str):
+    d = open(path, "rb").read()
+    assert d[:8] == b"AWGDNS02"
+    L, S = (int(x) for x in np.frombuffer(d, np.int32, 2, 8))
+    off = 16
+    bw = np.frombuffer(d, np.float64, L * S, off).reshape(L, S).copy(); off += 8 * L * S
+    trans = np.frombuffer(d, np.float64, S * S, off).reshape(S, S).copy(); off += 8 * S * S
+    emit = np.frombuffer(d, np.float64, L * S, off).reshape(L, S).copy()
+    return bw, trans, emit
+
+
+def summarize(ns, fw):
+    off = pyoracle.offsets(ns)
+    L = ns.shape[0]
+    colsum = np.zeros(L)
+    colwsum = np.zeros(L)
+    for i in range(L):
+        col = fw[off[i]:off[i + 1]]
+        colsum[i] = col.sum()
+        colwsum[i] = (col * weights(col.shape[0])).sum()
+    rows = np.unique(np.concatenate([np.arange(0, L, 32), [L - 1]])).astype(np.int32)
+    rowvals = np.concatenate([fw[off[i]:off[i + 1]] for i in rows])
+    return colsum, colwsum, rows, rowvals
+
+
+def run(*args):
+    subprocess.run([HARNESS] + [str(a) for a in args], check=True)
+
+
+def make(name: str, prob_path: str, seed: int, tmp: str, dense: bool = False):
+    prob = Problem.load(prob_path)
+    out = os.path.join(tmp, name + ".ref")
+    run("forward", prob_path, out, seed)
+    ns, fw, path = read_ref(out)
+    colsum, colwsum, rows, rowvals = summarize(ns, fw)
+    extra = {}
+    if dense:
+        dout = os.path.join(tmp, name + ".dense")
+        run("dense", prob_path, dout)
+        extra["dense_bw"], extra["dense_trans"], extra["dense_emit"] = read_dense(dout)
+    u = pyoracle.rand_uniforms(seed, prob.seqlen)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), nstates=ns, colsum=colsum,
+                        colwsum=colwsum, rows=rows, rowvals=rowvals, seed=seed,
+                        uniforms=u, path=path, **extra)
+    dst = os.path.join(HERE, name + ".prob")
+    if os.path.abspath(prob_path) != dst:
+        prob.save(dst)
+    print(f"{name}: L={prob.seqlen} trees={prob.ntrees} cells={fw.size} "
+          f"internal={prob.internal}")
+
+
+def first_tree(prob: Problem) -> Problem:
+    """The problem restricted to its first local tree (single-block HMM)."""
+    L = int(prob.blocklens[0])
+    return Problem(times=prob.times, popsizes=prob.popsizes, rho=prob.rho, mu=prob.mu,
+                   ptrees=prob.ptrees[:1].copy(), ages=prob.ages[:1].copy(),
+                   sprs=prob.sprs[:1].copy(), blocklens=prob.blocklens[:1].copy(),
+                   seqs=prob.seqs[:, :L].copy(), internal=prob.internal)
+
+
+def main():
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={REF}"],
+                   check=True)
+    pyoracle.build()
+    with tempfile.TemporaryDirectory() as tmp:
+        # the reference's bundled example, re-threading its last sequence (k=8, 100 kb)
+        p = os.path.join(HERE, "sim1_c20.prob")
+        run("sim1", os.path.join(REF, "examples/sim1/sim1.sites"),
+            os.path.join(REF, "examples/sim1/sim1.sample/out.100.smc.gz"), 20, p)
+        make("sim1_c20", p, 7, tmp)
+
+        # config-0 shape (k=8: 7 leaves + 1 threaded), shortened
+        for seed in (11, 12):
+            prob = simulate(7, 4000, seed)
+            p = os.path.join(tmp, "p.prob"); prob.save(p)
+            make(f"dsmc_k8_s{seed}", p, 100 + seed, tmp)
+
+        # missing data and a larger tree
+        prob = simulate(16, 2000, 21, missing=0.02)
+        p = os.path.join(tmp, "p.prob"); prob.save(p)
+        make("dsmc_k17_missing", p, 121, tmp)
+
+        # ntimes 16 and 32
+        for T, seed in ((16, 31), (32, 32)):
+            prob = simulate(9, 1500, seed, ntimes=T)
+            p = os.path.join(tmp, "p.prob"); prob.save(p)
+            make(f"dsmc_k10_T{T}", p, 100 + seed, tmp)
+
+        # internal-branch cuts by the reference's uniform removal path
+        for seed in (3, 8, 17, 24):
+            full = simulate(10, 2000, 200 + seed, add_thread=False)
+            pf = os.path.join(tmp, "full.prob"); full.save(pf)
+            pc = os.path.join(tmp, "cut.prob")
+            run("cut", pf, seed, pc)
+            make(f"cut_k10_s{seed}", pc, 500 + seed, tmp)
+
+        # single-tree problems with the reference's dense backward
+        for seed in (41, 43):
+            prob = first_tree(simulate(6, 400, seed))
+            p = os.path.join(tmp, "p.prob"); prob.save(p)
+            make(f"single_k7_s{seed}", p, seed, tmp, dense=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,113 @@
+"""The CPU restatement (oracle/) against the compiled reference's outputs.
+
+The fixtures in tests/golden/ were produced by the reference's own threading HMM
+(tests/golden/make_golden.py). The forward table must match them to 1e-13 relative
+(bit-identical on the host that made them) and the sampled path exactly.
+
+The backward pass is new (the reference has none for the threading HMM). On single-tree
+problems it must equal, to 1e-12, the exact dense backward recursion over the reference's
+own dense transition matrix and emissions (trans.cpp:136, emit.cpp:650), and track the
+reference's log-space backward_alg (hmm.cpp:48) to 2e-3: backward_alg sums with logsum
+(common.h:182-202), which drops terms more than e^-15 below the largest, so its error
+grows by about S*e^-15 per column.
+"""
+
+import os
+
+import numpy as np
+import pytest
+
+import pyoracle
+from argweaver_gb300.problem import Problem
+from conftest import GOLDEN, golden_names
+
+NAMES = golden_names()
+
+
+def load(name):
+    prob = Problem.load(os.path.join(GOLDEN, name + ".prob"))
+    gold = np.load(os.path.join(GOLDEN, name + ".npz"))
+    return prob, gold
+
+
+def weights(n):
+    k = np.arange(n, dtype=np.int64)
+    return 1.0 + ((k * 2654435761) % 1000) / 1000.0
+
+
+def column_checks(ns, fw, gold, rtol):
+    off = pyoracle.offsets(ns)
+    L = ns.shape[0]
+    colsum = np.array([fw[off[i]:off[i + 1]].sum() for i in range(L)])
+    colwsum = np.array([(fw[off[i]:off[i + 1]] * weights(off[i + 1] - off[i])).sum()
+                        for i in range(L)])
+    np.testing.assert_allclose(colsum, gold["colsum"], rtol=rtol, atol=0)
+    np.testing.assert_allclose(colwsum, gold["colwsum"], rtol=rtol, atol=0)
+    rows = np.concatenate([fw[off[i]:off[i + 1]] for i in gold["rows"]])
+    np.testing.assert_allclose(rows, gold["rowvals"], rtol=rtol, atol=1e-300)
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_nstates(name):
+    prob, gold = load(name)
+    np.testing.assert_array_equal(pyoracle.nstates(prob), gold["nstates"])
+    np.testing.assert_array_equal(prob.nstates_per_column(), gold["nstates"])
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_forward_matches_reference(name):
+    prob, gold = load(name)
+    fw, lnl = pyoracle.forward(prob)
+    column_checks(gold["nstates"], fw, gold, rtol=1e-13)
+    assert np.isfinite(lnl) and lnl < 0
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_traceback_matches_reference(name):
+    prob, gold = load(name)
+    fw, _ = pyoracle.forward(prob)
+    path = pyoracle.traceback(prob, fw, gold["uniforms"])
+    np.testing.assert_array_equal(path, gold["path"])
+
+
+def test_rand_uniforms_match_fixture():
+    # glibc's rand() after srand(seed) gives the uniforms stored with each fixture
+    prob, gold = load(NAMES[0])
+    u = pyoracle.rand_uniforms(int(gold["seed"]), prob.seqlen)
+    np.testing.assert_array_equal(u, gold["uniforms"])
+
+
+@pytest.mark.parametrize("name", [n for n in NAMES if n.startswith("single_")])
+def test_backward_matches_dense_reference(name):
+    prob, gold = load(name)
+    bw = pyoracle.backward(prob)
+    ns = gold["nstates"]
+    off = pyoracle.offsets(ns)
+    P = np.exp(gold["dense_trans"])
+    E = np.exp(gold["dense_emit"])
+    L = prob.seqlen
+    exact = np.full(P.shape[0], 1.0 / P.shape[0])
+    for i in range(L - 1, -1, -1):
+        if i < L - 1:
+            exact = P @ (E[i + 1] * exact)
+            exact /= exact.sum()
+        np.testing.assert_allclose(bw[off[i]:off[i + 1]], exact, rtol=1e-12, atol=0)
+        d = np.exp(gold["dense_bw"][i] - gold["dense_bw"][i].max())
+        d /= d.sum()
+        np.testing.assert_allclose(bw[off[i]:off[i + 1]], d, rtol=2e-3, atol=0)
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_posterior_properties(name):
+    prob, gold = load(name)
+    fw, _ = pyoracle.forward(prob)
+    bw = pyoracle.backward(prob)
+    post = pyoracle.posterior(prob, fw, bw)
+    ns = gold["nstates"]
+    off = pyoracle.offsets(ns)
+    sums = np.add.reduceat(post, off[:-1])
+    np.testing.assert_allclose(sums, 1.0, rtol=1e-12)
+    assert np.all(post >= 0)
+    # at the last column the backward is flat, so the posterior is the forward column
+    L = prob.seqlen
+    np.testing.assert_allclose(post[off[L - 1]:], fw[off[L - 1]:], rtol=1e-12, atol=1e-300)

@@ -1,0 +1,147 @@
+"""NumPy-level host API of the GPU threading HMM.
+
+  forward(problem)                -> packed forward table (FP64) and log-likelihood
+  sample_path(problem, uniforms)  -> sampled state index per column
+  posterior(problem)              -> posterior marginals (forward-backward)
+  run_batch(problems, ...)        -> many problems in one launch sequence
+
+The reference-compatible calls (arghmm_forward_alg and friends) live in
+:mod:`argweaver_gb300.refapi`. Tables are packed column after column with max(nstates,1)
+entries per column, the rows of the reference's forward table laid end to end.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+from . import capi
+from .problem import Problem
+
+
+class GpuError(RuntimeError):
+    pass
+
+
+class _Bound:
+    """Problem arrays pinned for the duration of a call, with their C view."""
+
+    def __init__(self, prob: Problem):
+        self.p = prob.normalized()
+        p = self.p
+        ptr = lambda a: None if a is None else a.ctypes.data
+        self.c = capi.AwgProblem(p.ntrees, p.nnodes, p.ntimes, p.nseqs, p.seqlen,
+                                 int(p.internal), p.start_coord, 0, ptr(p.ptrees),
+                                 ptr(p.ages), ptr(p.sprs), ptr(p.blocklens), ptr(p.mapping),
+                                 ptr(p.root_child0), ptr(p.times), ptr(p.popsizes), p.rho,
+                                 p.mu, ptr(p.seqs))
+
+
+def cells(prob: Problem) -> int:
+    lib = capi.load()
+    b = _Bound(prob)
+    n = lib.awg_problem_cells(C.byref(b.c))
+    if n < 0:
+        raise ValueError(capi.last_error())
+    return int(n)
+
+
+def offsets(nstates: np.ndarray) -> np.ndarray:
+    off = np.zeros(nstates.shape[0] + 1, dtype=np.int64)
+    np.cumsum(np.maximum(nstates, 1), out=off[1:])
+    return off
+
+
+@dataclass
+class Result:
+    forward: Optional[np.ndarray] = None
+    posterior: Optional[np.ndarray] = None
+    path: Optional[np.ndarray] = None
+    loglik: float = float("nan")
+
+
+def run_batch(problems: Sequence[Problem], *, precision: str = "fp64",
+              want_forward: bool = True, want_path: bool = False,
+              want_posterior: bool = False,
+              uniforms: Optional[Sequence[Optional[np.ndarray]]] = None) -> List[Result]:
+    """Run forward (+ traceback, + backward/posterior) for a batch of problems."""
+    lib = capi.load()
+    fp32 = precision == "fp32"
+    if precision not in ("fp32", "fp64"):
+        raise ValueError("precision must be 'fp64' or 'fp32'")
+    n = len(problems)
+    bound = [_Bound(p) for p in problems]
+    probs = (capi.AwgProblem * n)(*[b.c for b in bound])
+    outs = (capi.AwgOutputs * n)()
+    results, keep = [], []
+    for q, b in enumerate(bound):
+        r = Result()
+        ncell = lib.awg_problem_cells(C.byref(b.c))
+        if ncell < 0:
+            raise ValueError(capi.last_error())
+        o = outs[q]
+        if want_forward:
+            r.forward = np.empty(ncell, dtype=np.float32 if fp32 else np.float64)
+            if fp32:
+                o.forward32 = r.forward.ctypes.data
+            else:
+                o.forward = r.forward.ctypes.data
+        if want_posterior:
+            r.posterior = np.empty(ncell, dtype=np.float64)
+            o.posterior = r.posterior.ctypes.data
+        if want_path:
+            r.path = np.empty(b.p.seqlen, dtype=np.int32)
+            o.path = r.path.ctypes.data
+            if uniforms is not None and uniforms[q] is not None:
+                u = np.ascontiguousarray(uniforms[q], dtype=np.float64)
+                if u.shape[0] != b.p.seqlen:
+                    raise ValueError("uniforms must have one entry per column")
+                keep.append(u)
+                o.uniforms = u.ctypes.data
+        ll = np.zeros(1, dtype=np.float64)
+        keep.append(ll)
+        o.loglik = ll.ctypes.data
+        results.append((r, ll))
+    rc = lib.awg_run_batch(probs, outs, n, capi.AWG_FP32 if fp32 else capi.AWG_FP64)
+    if rc != 0:
+        raise GpuError(f"awg_run_batch failed ({rc}): {capi.last_error()}")
+    out = []
+    for r, ll in results:
+        r.loglik = float(ll[0])
+        out.append(r)
+    return out
+
+
+def forward(prob: Problem, precision: str = "fp64"):
+    r = run_batch([prob], precision=precision)[0]
+    return r.forward, r.loglik
+
+
+def sample_path(prob: Problem, uniforms: Optional[np.ndarray] = None,
+                precision: str = "fp64") -> np.ndarray:
+    r = run_batch([prob], precision=precision, want_forward=False, want_path=True,
+                  uniforms=[uniforms])[0]
+    return r.path
+
+
+def posterior(prob: Problem, precision: str = "fp64") -> np.ndarray:
+    return run_batch([prob], precision=precision, want_forward=False,
+                     want_posterior=True)[0].posterior
+
+
+def kernel_launches() -> int:
+    return int(capi.load().awg_kernel_launches())
+
+
+def set_timing(on: bool) -> None:
+    capi.load().awg_set_timing(1 if on else 0)
+
+
+def last_timings() -> dict:
+    out = np.zeros(7, dtype=np.float64)
+    capi.load().awg_last_timings(out.ctypes.data_as(capi.c_double_p))
+    keys = ["h2d", "tables", "emit", "forward", "traceback", "backward", "d2h"]
+    return {k: float(v) for k, v in zip(keys, out)}

@@ -101,9 +101,7 @@ def build_cuda(verbose: bool = False) -> str:
         key = _digest([path] + headers, NVCC_FLAGS)
         if os.path.exists(obj) and os.path.exists(stamp) and open(stamp).read() == key:
             continue
-        cmd = [nvcc] + NVCC_FLAGS + ["-dc" if src.endswith(".cu") else "-c", "-o", obj, path]
-        if src.endswith(".cpp"):
-            cmd = [nvcc] + NVCC_FLAGS + ["-x", "c++", "-c", "-o", obj, path]
+        cmd = [nvcc] + NVCC_FLAGS + ["-c", "-o", obj, path]
         jobs.append((src, cmd))
         if verbose:
             print(" ".join(cmd), file=sys.stderr)

@@ -1,0 +1,115 @@
+"""ctypes binding of libargweaver_gb300.so (include/argweaver_gb300.h).
+
+The reference-compatible prototypes mirror the reference's own ctypes declarations
+(argweaver/argweaverc.py:133-167) so Python callers of the reference keep their calls;
+the awg_* prototypes expose the flat batch API. Loading fails loudly when the library is
+missing: there is no CPU fallback.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+from . import build
+
+_lock = threading.Lock()
+_lib = None
+
+c_int_p = C.POINTER(C.c_int)
+c_int_pp = C.POINTER(c_int_p)
+c_double_p = C.POINTER(C.c_double)
+c_double_pp = C.POINTER(c_double_p)
+c_char_pp = C.POINTER(C.c_char_p)
+
+
+class AwgProblem(C.Structure):
+    _fields_ = [("ntrees", C.c_int), ("nnodes", C.c_int), ("ntimes", C.c_int),
+                ("nseqs", C.c_int), ("seqlen", C.c_int), ("internal", C.c_int),
+                ("start_coord", C.c_int), ("minage", C.c_int),
+                ("ptrees", C.c_void_p), ("ages", C.c_void_p), ("sprs", C.c_void_p),
+                ("blocklens", C.c_void_p), ("mapping", C.c_void_p),
+                ("root_child0", C.c_void_p), ("times", C.c_void_p),
+                ("popsizes", C.c_void_p), ("rho", C.c_double), ("mu", C.c_double),
+                ("seqs", C.c_void_p)]
+
+
+class AwgOutputs(C.Structure):
+    _fields_ = [("forward", C.c_void_p), ("forward32", C.c_void_p),
+                ("posterior", C.c_void_p), ("path", C.c_void_p), ("loglik", C.c_void_p),
+                ("uniforms", C.c_void_p)]
+
+
+AWG_FP64 = 0
+AWG_FP32 = 1
+
+# (name, restype, argtypes) of every export declared in include/argweaver_gb300.h
+PROTOTYPES = [
+    ("arghmm_new_trees", C.c_void_p,
+     [c_int_pp, c_int_pp, c_int_pp, c_int_p, C.c_int, C.c_int, C.c_int]),
+    ("delete_local_trees", None, [C.c_void_p]),
+    ("get_local_trees_ntrees", C.c_int, [C.c_void_p]),
+    ("get_local_trees_nnodes", C.c_int, [C.c_void_p]),
+    ("arghmm_get_nstates", None, [C.c_void_p, C.c_int, C.c_bool, c_int_p]),
+    ("arghmm_forward_alg", c_double_pp,
+     [C.c_void_p, c_double_p, C.c_int, c_double_p, C.c_double, C.c_double, c_char_pp,
+      C.c_int, C.c_int, C.c_bool, c_double_p, C.c_bool, C.c_bool]),
+    ("arghmm_backward_alg", c_double_pp,
+     [C.c_void_p, c_double_p, C.c_int, c_double_p, C.c_double, C.c_double, c_char_pp,
+      C.c_int, C.c_int, C.c_bool]),
+    ("arghmm_posterior_marginals", c_double_pp,
+     [C.c_void_p, c_double_p, C.c_int, c_double_p, C.c_double, C.c_double, c_char_pp,
+      C.c_int, C.c_int, C.c_bool]),
+    ("arghmm_sample_posterior", c_int_p,
+     [c_int_pp, c_int_pp, c_int_pp, c_int_p, C.c_int, C.c_int, c_double_p, C.c_int,
+      c_double_p, C.c_double, C.c_double, c_char_pp, C.c_int, C.c_int, C.c_void_p]),
+    ("arghmm_sample_arg_thread_internal", None,
+     [C.c_void_p, c_double_p, C.c_int, c_double_p, C.c_double, C.c_double, c_char_pp,
+      C.c_int, C.c_int, c_int_p]),
+    ("delete_path", None, [c_int_p]),
+    ("delete_double_matrix", None, [c_double_pp, C.c_int]),
+    ("delete_forward_matrix", None, [c_double_pp, C.c_int]),
+    ("awg_problem_cells", C.c_longlong, [C.POINTER(AwgProblem)]),
+    ("awg_run_batch", C.c_int, [C.POINTER(AwgProblem), C.POINTER(AwgOutputs), C.c_int,
+                                C.c_int]),
+    ("awg_last_error", C.c_char_p, []),
+    ("awg_device_name", C.c_int, [C.c_char_p, C.c_int]),
+    ("awg_kernel_launches", C.c_longlong, []),
+]
+
+# helpers exported beside the header's API (timing of the last batch)
+EXTRA = [
+    ("awg_debug_tables", C.c_int, [C.POINTER(AwgProblem), C.c_void_p, C.c_void_p, C.c_void_p,
+                                   C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("awg_set_timing", None, [C.c_int]),
+    ("awg_last_timings", None, [c_double_p]),
+]
+
+
+def library_path() -> str:
+    return build.CUDA_LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load the library (building it in-tree when missing)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            path = library_path()
+            if not os.path.exists(path):
+                if not build_if_missing:
+                    raise RuntimeError(f"{path} is missing: run argweaver_gb300.build first")
+                build.build_cuda()
+            lib = C.CDLL(path)
+            for name, res, args in PROTOTYPES + EXTRA:
+                fn = getattr(lib, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = lib
+    return _lib
+
+
+def last_error() -> str:
+    msg = load().awg_last_error()
+    return msg.decode() if msg else ""

@@ -1,0 +1,228 @@
+// K5: backward pass fused with the posterior marginals, one CTA per instance.
+//
+// The reference has no backward pass for the threading HMM. This one uses the forward
+// pass's transition semantics (TransMatrix::get, trans.h:64-83; TransMatrixSwitch::get,
+// trans.h:207-219) transposed, over the same structure:
+//   g[k]     = e_{i+1}[k] * bw_{i+1}[k]
+//   G[b]     = sum of g over states of time b
+//   bw_i[j]  = sum_b tmatrix[a_j][b] * G[b] + sum over states k of j's node of
+//              tmatrix2[a_j][k] * g[k]
+// normalised per column. At a tree boundary bw of the previous tree's last column is
+// gathered through the switch matrix. Posterior marginals are fw[i] * bw[i] renormalised;
+// the backward column never leaves shared memory unless the caller asks for the table.
+
+#include <cuda_runtime.h>
+
+#include "kernels.h"
+
+namespace awg {
+
+namespace {
+
+template <typename F> struct BTab;
+template <> struct BTab<double> {
+    const double *tm, *inv, *var, *dprob, *rrow, *crow, *gts, *fw;
+    __device__ explicit BTab(const BatchDev &d)
+        : tm(d.tm), inv(d.inv_lk), var(d.varemit), dprob(d.determprob), rrow(d.recombrow),
+          crow(d.recoalrow), gts(d.gts), fw(d.fw64) {}
+    __device__ double t2(long long t2_0, int off, int y, double tmab) const {
+        return gts[t2_0 + off + y] - tmab;
+    }
+};
+template <> struct BTab<float> {
+    const float *tm, *inv, *var, *dprob, *rrow, *crow, *t2d, *fw;
+    __device__ explicit BTab(const BatchDev &d)
+        : tm(d.tm32), inv(d.inv32), var(d.var32), dprob(d.determprob32), rrow(d.recombrow32),
+          crow(d.recoalrow32), t2d(d.t2d32), fw(d.fw32) {}
+    __device__ float t2(long long t2_0, int off, int y, float) const { return t2d[t2_0 + off + y]; }
+};
+
+template <typename F>
+__device__ __forceinline__ F warp_sum(F v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+struct Meta {
+    int time, j1, m, off;
+};
+
+// Block-wide sum in a fixed order; every thread gets the result.
+template <typename F>
+__device__ F block_sum(F part, F *red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    part = warp_sum(part);
+    __syncthreads();
+    if (lane == 0) red[warp] = part;
+    __syncthreads();
+    F s = 0;
+    for (int w = 0; w < nw; w++) s += red[w];
+    return s;
+}
+
+template <typename F>
+__global__ void k_backward(BatchDev d, int maxS, double *bw_out) {
+    extern __shared__ double dyn_d[];
+    const BTab<F> tab(d);
+    const InstDev I = d.inst[blockIdx.x];
+    const int T = I.T;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nwarps = blockDim.x >> 5;
+
+    F *bwA = (F *)dyn_d;
+    F *bwB = bwA + maxS;
+    F *g = bwB + maxS;
+    Meta *meta = (Meta *)(g + maxS + (maxS & 1));
+    int *perm = (int *)(meta + maxS);
+    __shared__ F tm[MAXT * MAXT];
+    __shared__ F G[MAXT], H[MAXT], red[32];
+    __shared__ int bptr[MAXT + 1];
+
+    F *cur = bwA, *nxt = bwB;  // cur: bw of column i+1, nxt: bw of column i
+    {
+        const BlockDev &B = d.blocks[I.block0 + I.ntrees - 1];
+        const int Sm = imax(B.S, 1);
+        for (int k = tid; k < Sm; k += blockDim.x) cur[k] = F(1) / F(Sm);
+    }
+    __syncthreads();
+
+    for (int bi = I.ntrees - 1; bi >= 0; bi--) {
+        const BlockDev &B = d.blocks[I.block0 + bi];
+        const int S = B.S, Sm = imax(S, 1);
+        for (int k = tid; k < S; k += blockDim.x) {
+            const StateInfo si = d.sinfo[B.state0 + k];
+            meta[k] = Meta{si.time, si.j1, si.m, d.t2off[B.state0 + k]};
+            perm[k] = d.bt_perm[B.state0 + k];
+        }
+        const F *tmg = tab.tm + (size_t)(I.block0 + bi) * MAXT * MAXT;
+        for (int e = tid; e < (T - 1) * MAXT; e += blockDim.x) tm[e] = tmg[e];
+        for (int a = tid; a <= MAXT; a += blockDim.x)
+            bptr[a] = d.bt_ptr[(size_t)(I.block0 + bi) * (MAXT + 1) + a];
+        const uint8_t *cls = d.colclass + I.col0 + B.start;
+        const int *cvar = d.colvar + I.col0 + B.start;
+        const F *inv = tab.inv + B.state0;
+        const F *var = tab.var + B.var0;
+        const F *fw = tab.fw + B.cell0;
+        __syncthreads();
+
+        auto emit = [&](int i, int k) -> F {
+            const uint8_t c = cls[i];
+            if (c == COL_MASKED || S == 0) return F(1);
+            if (c == COL_INVARIANT) return inv[k];
+            return var[(size_t)cvar[i] * S + k];
+        };
+        // posterior of one column from its bw (in `bw`) and fw
+        auto posterior = [&](int i, const F *bw) {
+            const F *f = fw + (size_t)i * Sm;
+            F part = 0;
+            for (int k = tid; k < Sm; k += blockDim.x) part += f[k] * bw[k];
+            const F z = block_sum(part, red);
+            const long long c0 = B.cell0 + (long long)i * Sm;
+            for (int k = tid; k < Sm; k += blockDim.x) {
+                if (d.post) d.post[c0 + k] = (double)(f[k] * bw[k] / z);
+                if (bw_out) bw_out[c0 + k] = (double)bw[k];
+            }
+        };
+
+        posterior(B.len - 1, cur);
+        for (int i = B.len - 2; i >= 0; i--) {
+            for (int k = tid; k < Sm; k += blockDim.x) g[k] = emit(i + 1, k) * cur[k];
+            __syncthreads();
+            if (S == 0) {
+                if (tid == 0) nxt[0] = g[0];
+            } else {
+                for (int a = warp; a < T - 1; a += nwarps) {
+                    F s = 0;
+                    for (int p = bptr[a] + lane; p < bptr[a + 1]; p += 32) s += g[perm[p]];
+                    s = warp_sum(s);
+                    if (lane == 0) G[a] = s;
+                }
+                __syncthreads();
+                if (warp == 0 && lane < T - 1) {
+                    F s = 0;
+                    for (int b = 0; b < T - 1; b++) s += tm[lane * MAXT + b] * G[b];
+                    H[lane] = s;
+                }
+                __syncthreads();
+                for (int j = tid; j < S; j += blockDim.x) {
+                    const Meta mj = meta[j];
+                    const int y = j - mj.j1;  // position of j's time among its node's times
+                    const int a = mj.time;
+                    const int a0 = a - y;
+                    F s = H[a];
+                    for (int x = 0; x < mj.m; x++) {
+                        const int k = mj.j1 + x;  // target on the same node, time a0 + x
+                        s += tab.t2(B.t2_0, meta[k].off, y, tm[a * MAXT + a0 + x]) * g[k];
+                    }
+                    nxt[j] = s;
+                }
+            }
+            F part = 0;
+            for (int k = tid; k < Sm; k += blockDim.x) part += nxt[k];
+            const F z = block_sum(part, red);
+            for (int k = tid; k < Sm; k += blockDim.x) nxt[k] /= z;
+            __syncthreads();
+            posterior(i, nxt);
+            F *t = cur; cur = nxt; nxt = t;
+        }
+        if (bi > 0) {
+            // into the previous tree's last column through the switch matrix
+            const BlockDev &P = d.blocks[I.block0 + bi - 1];
+            const int n1 = imax(B.S1, 1);
+            for (int k = tid; k < Sm; k += blockDim.x) g[k] = emit(0, k) * cur[k];
+            __syncthreads();
+            const int2 src = d.srcs[I.block0 + bi];
+            const int *determ = d.determ + B.prev_state0;
+            const F *dp = tab.dprob + B.prev_state0;
+            const F *rr = tab.rrow + B.state0;
+            const F *cr = tab.crow + B.state0;
+            for (int j = tid; j < n1; j += blockDim.x) {
+                F s = 0;
+                if (j == src.y || j == src.x) {
+                    const F *row = (j == src.y) ? cr : rr;
+                    for (int k = 0; k < Sm; k++)
+                        if (row[k] > F(0)) s += row[k] * g[k];
+                } else if (determ[j] >= 0) {
+                    s = dp[j] * g[determ[j]];
+                }
+                nxt[j] = s;
+            }
+            F part = 0;
+            for (int k = tid; k < n1; k += blockDim.x) part += nxt[k];
+            const F z = block_sum(part, red);
+            for (int k = tid; k < n1; k += blockDim.x) nxt[k] /= z;
+            __syncthreads();
+            (void)P;
+            F *t = cur; cur = nxt; nxt = t;
+        }
+    }
+}
+
+int backward_threads(int maxS) {
+    if (maxS > 768) return 512;
+    if (maxS > 256) return 256;
+    return 128;
+}
+
+template <typename F>
+void launch(const BatchDev &d, double *bw_out, cudaStream_t s) {
+    const int maxS = imax(d.maxS, 1);
+    const size_t smem = 3 * (size_t)maxS * sizeof(F) + 8 + (size_t)maxS * (sizeof(Meta) + sizeof(int));
+    static size_t configured = 0;
+    if (smem > 48 * 1024 && smem > configured) {
+        cudaFuncSetAttribute(k_backward<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        configured = smem;
+    }
+    k_backward<F><<<d.ninst, backward_threads(maxS), smem, s>>>(d, maxS, bw_out);
+    note_launch();
+}
+
+}  // namespace
+
+void launch_backward(const BatchDev &d, bool fp32, double *bw_out, cudaStream_t s) {
+    if (fp32) launch<float>(d, bw_out, s);
+    else launch<double>(d, bw_out, s);
+}
+
+}  // namespace awg

@@ -1,0 +1,318 @@
+// The C ABI: the reference's threading-HMM entry points (sample_thread.cpp:883-1046,
+// states.cpp:209, local_tree.cpp:1817-1895) re-hosted on the GPU engine, and the flat
+// batch API. Results of the reference-compatible calls are host memory allocated with
+// new[], as the reference's are, and are freed by this library's delete_* exports.
+
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "argweaver_gb300.h"
+#include "engine.h"
+#include "kernels.h"
+#include "plan.h"
+
+struct awg_local_trees {
+    int ntrees = 0, nnodes = 0, start_coord = 0;
+    std::vector<int> ptrees, ages, sprs, blocklens, mapping;
+};
+
+namespace {
+
+thread_local std::string g_err;
+
+void set_error(const std::string &msg) {
+    g_err = msg;
+    fprintf(stderr, "argweaver_gb300: %s\n", msg.c_str());
+}
+
+// Trees + model + sequences of a reference-style call as one awg_problem.
+struct ProblemView {
+    awg_problem p;
+    std::vector<char> seqs;
+};
+
+bool make_view(const awg_local_trees *t, double *times, int ntimes, double *popsizes,
+               double rho, double mu, char **seqs, int nseqs, int seqlen, bool internal,
+               ProblemView &v) {
+    if (!t || !times || !popsizes || !seqs) { set_error("NULL argument"); return false; }
+    v.seqs.resize((size_t)nseqs * seqlen);
+    for (int i = 0; i < nseqs; i++) memcpy(&v.seqs[(size_t)i * seqlen], seqs[i], seqlen);
+    awg_problem &p = v.p;
+    memset(&p, 0, sizeof(p));
+    p.ntrees = t->ntrees; p.nnodes = t->nnodes; p.ntimes = ntimes; p.nseqs = nseqs;
+    p.seqlen = seqlen; p.internal = internal ? 1 : 0; p.start_coord = t->start_coord;
+    p.minage = 0;
+    p.ptrees = t->ptrees.data(); p.ages = t->ages.data(); p.sprs = t->sprs.data();
+    p.blocklens = t->blocklens.data();
+    p.mapping = t->mapping.empty() ? nullptr : t->mapping.data();
+    p.root_child0 = nullptr;
+    p.times = times; p.popsizes = popsizes; p.rho = rho; p.mu = mu;
+    p.seqs = v.seqs.data();
+    return true;
+}
+
+// seqlen rows of max(nstates,1) doubles over one new[] block; the block pointer is kept in
+// a hidden slot before the row array so delete_forward_matrix can free it.
+double **make_rows(const std::vector<int> &nstates, double **block_out) {
+    const int L = (int)nstates.size();
+    long long cells = 0;
+    for (int i = 0; i < L; i++) cells += std::max(nstates[i], 1);
+    double *block = new double[std::max(cells, 1LL)];
+    double **rows = new double *[L + 1];
+    rows[0] = block;
+    long long off = 0;
+    for (int i = 0; i < L; i++) {
+        rows[i + 1] = block + off;
+        off += std::max(nstates[i], 1);
+    }
+    *block_out = block;
+    return rows + 1;
+}
+
+std::vector<int> column_nstates(const awg_problem &p) {
+    std::vector<int> ns(p.seqlen, 0);
+    int pos = 0;
+    for (int b = 0; b < p.ntrees; b++) {
+        int S = awg::count_states(p.ptrees + (size_t)b * p.nnodes, p.ages + (size_t)b * p.nnodes,
+                                  p.nnodes, p.ntimes, p.internal != 0, p.minage,
+                                  p.root_child0 ? p.root_child0[b] : -1, nullptr);
+        for (int i = 0; i < p.blocklens[b]; i++) ns[pos + i] = S;
+        pos += p.blocklens[b];
+    }
+    return ns;
+}
+
+double **table_call(awg_local_trees *trees, double *times, int ntimes, double *popsizes,
+                    double rho, double mu, char **seqs, int nseqs, int seqlen, bool internal,
+                    const double *prior, int kind) {
+    g_err.clear();
+    ProblemView v;
+    if (!make_view(trees, times, ntimes, popsizes, rho, mu, seqs, nseqs, seqlen, internal, v))
+        return nullptr;
+    if (awg_problem_cells(&v.p) < 0) return nullptr;
+    std::vector<int> ns = column_nstates(v.p);
+    double *block = nullptr;
+    double **rows = make_rows(ns, &block);
+    awg_outputs o;
+    memset(&o, 0, sizeof(o));
+    awg::RunOptions opt;
+    opt.precision = AWG_FP64;
+    const double *priors[1] = {prior};
+    double *bws[1] = {block};
+    if (kind == 0) o.forward = block;
+    if (kind == 1) { opt.backward = bws; }
+    if (kind == 2) o.posterior = block;
+    if (prior) opt.priors = priors;
+    std::string err;
+    if (awg::run_batch(&v.p, &o, 1, opt, err) != 0) {
+        set_error(err);
+        delete[] block;
+        delete[] (rows - 1);
+        return nullptr;
+    }
+    return rows;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *awg_last_error(void) { return g_err.c_str(); }
+
+long long awg_kernel_launches(void) { return awg::kernel_launch_count(); }
+
+int awg_device_name(char *buf, int len) {
+    int dev = 0;
+    cudaDeviceProp prop;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaGetDeviceProperties(&prop, dev) != cudaSuccess)
+        return -1;
+    snprintf(buf, len, "%s", prop.name);
+    return 0;
+}
+
+long long awg_problem_cells(const awg_problem *p) {
+    g_err.clear();
+    awg::HostPlan plan;
+    std::string err;
+    if (!p || !awg::build_plan(p, 1, plan, err)) {
+        set_error(err.empty() ? "NULL problem" : err);
+        return -1;
+    }
+    return plan.total_cells;
+}
+
+int awg_run_batch(const awg_problem *problems, awg_outputs *outputs, int n, int precision) {
+    g_err.clear();
+    if (!problems || !outputs || n <= 0) { set_error("empty batch"); return -1; }
+    awg::RunOptions opt;
+    opt.precision = precision;
+    std::string err;
+    int rc = awg::run_batch(problems, outputs, n, opt, err);
+    if (rc != 0) set_error(err);
+    return rc;
+}
+
+awg_local_trees *arghmm_new_trees(int **ptrees, int **ages, int **sprs, int *blocklens,
+                                  int ntrees, int nnodes, int start_coord) {
+    if (!ptrees || !ages || !sprs || !blocklens || ntrees < 1 || nnodes < 1) {
+        set_error("arghmm_new_trees: bad arguments");
+        return nullptr;
+    }
+    awg_local_trees *t = new awg_local_trees();
+    t->ntrees = ntrees; t->nnodes = nnodes; t->start_coord = start_coord;
+    t->ptrees.resize((size_t)ntrees * nnodes);
+    t->ages.resize((size_t)ntrees * nnodes);
+    t->sprs.resize((size_t)ntrees * 4);
+    t->blocklens.assign(blocklens, blocklens + ntrees);
+    for (int i = 0; i < ntrees; i++) {
+        memcpy(&t->ptrees[(size_t)i * nnodes], ptrees[i], sizeof(int) * nnodes);
+        memcpy(&t->ages[(size_t)i * nnodes], ages[i], sizeof(int) * nnodes);
+        memcpy(&t->sprs[(size_t)i * 4], sprs[i], sizeof(int) * 4);
+    }
+    return t;
+}
+
+void delete_local_trees(awg_local_trees *trees) { delete trees; }
+int get_local_trees_ntrees(awg_local_trees *trees) { return trees ? trees->ntrees : 0; }
+int get_local_trees_nnodes(awg_local_trees *trees) { return trees ? trees->nnodes : 0; }
+
+void arghmm_get_nstates(awg_local_trees *trees, int ntimes, bool internal, int *nstates) {
+    if (!trees || !nstates) return;
+    int pos = 0;
+    for (int b = 0; b < trees->ntrees; b++) {
+        int S = awg::count_states(&trees->ptrees[(size_t)b * trees->nnodes],
+                                  &trees->ages[(size_t)b * trees->nnodes], trees->nnodes,
+                                  ntimes, internal, 0, -1, nullptr);
+        for (int i = 0; i < trees->blocklens[b]; i++) nstates[pos + i] = S;
+        pos += trees->blocklens[b];
+    }
+}
+
+double **arghmm_forward_alg(awg_local_trees *trees, double *times, int ntimes,
+                            double *popsizes, double rho, double mu, char **seqs, int nseqs,
+                            int seqlen, bool prior_given, double *prior, bool internal,
+                            bool slow) {
+    (void)slow;  // the dense step (sample_thread.cpp:303-338) computes the same table
+    return table_call(trees, times, ntimes, popsizes, rho, mu, seqs, nseqs, seqlen, internal,
+                      prior_given ? prior : nullptr, 0);
+}
+
+double **arghmm_backward_alg(awg_local_trees *trees, double *times, int ntimes,
+                             double *popsizes, double rho, double mu, char **seqs, int nseqs,
+                             int seqlen, bool internal) {
+    return table_call(trees, times, ntimes, popsizes, rho, mu, seqs, nseqs, seqlen, internal,
+                      nullptr, 1);
+}
+
+double **arghmm_posterior_marginals(awg_local_trees *trees, double *times, int ntimes,
+                                    double *popsizes, double rho, double mu, char **seqs,
+                                    int nseqs, int seqlen, bool internal) {
+    return table_call(trees, times, ntimes, popsizes, rho, mu, seqs, nseqs, seqlen, internal,
+                      nullptr, 2);
+}
+
+awg_intstate *arghmm_sample_posterior(int **ptrees, int **ages, int **sprs, int *blocklens,
+                                      int ntrees, int nnodes, double *times, int ntimes,
+                                      double *popsizes, double rho, double mu, char **seqs,
+                                      int nseqs, int seqlen, awg_intstate *path) {
+    g_err.clear();
+    awg_local_trees *t = arghmm_new_trees(ptrees, ages, sprs, blocklens, ntrees, nnodes, 0);
+    if (!t) return nullptr;
+    ProblemView v;
+    if (!make_view(t, times, ntimes, popsizes, rho, mu, seqs, nseqs, seqlen, false, v)) {
+        delete t;
+        return nullptr;
+    }
+    std::vector<int> ipath(seqlen);
+    awg_outputs o;
+    memset(&o, 0, sizeof(o));
+    o.path = ipath.data();
+    awg::RunOptions opt;
+    std::string err;
+    if (awg::run_batch(&v.p, &o, 1, opt, err) != 0) {
+        set_error(err);
+        delete t;
+        return nullptr;
+    }
+    if (!path) path = (awg_intstate *)new int[2 * (size_t)seqlen];
+    // state index -> (node, time) with each column's own state space (states.cpp:53-74)
+    int pos = 0;
+    for (int b = 0; b < ntrees; b++) {
+        const int *par = &t->ptrees[(size_t)b * nnodes];
+        const int *age = &t->ages[(size_t)b * nnodes];
+        std::vector<int> first(nnodes), t0(nnodes);
+        int S = 0;
+        for (int v2 = 0; v2 < nnodes; v2++) {
+            const int top = par[v2] == -1 ? ntimes - 2 : age[par[v2]];
+            first[v2] = S;
+            t0[v2] = age[v2];
+            S += std::max(0, top - age[v2] + 1);
+        }
+        for (int i = pos; i < pos + blocklens[b]; i++) {
+            const int k = ipath[i];
+            int node = nnodes - 1;
+            for (int v2 = 0; v2 < nnodes; v2++)
+                if (first[v2] <= k && (v2 + 1 == nnodes || k < first[v2 + 1])) { node = v2; break; }
+            path[i][0] = node;
+            path[i][1] = t0[node] + (k - first[node]);
+        }
+        pos += blocklens[b];
+    }
+    delete t;
+    return path;
+}
+
+void arghmm_sample_arg_thread_internal(awg_local_trees *trees, double *times, int ntimes,
+                                       double *popsizes, double rho, double mu, char **seqs,
+                                       int nseqs, int seqlen, int *thread_path) {
+    g_err.clear();
+    ProblemView v;
+    if (!make_view(trees, times, ntimes, popsizes, rho, mu, seqs, nseqs, seqlen, true, v)) return;
+    awg_outputs o;
+    memset(&o, 0, sizeof(o));
+    o.path = thread_path;
+    awg::RunOptions opt;
+    std::string err;
+    if (awg::run_batch(&v.p, &o, 1, opt, err) != 0) set_error(err);
+}
+
+void delete_path(int *path) { delete[] path; }
+
+// Debug export: the FP64 tables the table kernel builds for one problem (layouts in
+// engine.h). Returns 0 or a negative code.
+int awg_debug_tables(const awg_problem *p, double *tm, double *gts, double *inv, double *prior,
+                     int *btptr, int *btperm) {
+    g_err.clear();
+    awg_outputs o;
+    memset(&o, 0, sizeof(o));
+    awg::RunOptions opt;
+    opt.tables_only = true;
+    opt.dbg_tm = tm; opt.dbg_gts = gts; opt.dbg_inv = inv; opt.dbg_prior = prior;
+    opt.dbg_btptr = btptr; opt.dbg_btperm = btperm;
+    std::string err;
+    int rc = awg::run_batch(p, &o, 1, opt, err);
+    if (rc != 0) set_error(err);
+    return rc;
+}
+
+void delete_double_matrix(double **mat, int nrows) {
+    (void)nrows;
+    if (!mat) return;
+    delete[] mat[0];
+    delete[] mat;
+}
+
+void delete_forward_matrix(double **mat, int nrows) {
+    (void)nrows;
+    if (!mat) return;
+    double **base = mat - 1;
+    delete[] base[0];
+    delete[] base;
+}
+
+}  // extern "C"

@@ -1,0 +1,331 @@
+// Host plan of a batch of threading problems.
+//
+// The host does only O(nodes) work per local tree and one pass over the sequences:
+// validation, child arrays (the reference's set_ptree, local_tree.h:190-230), state-space
+// sizes (states.cpp:53-199) for the memory layout, node mappings (make_node_mapping,
+// local_tree.h:767), the model's time grid (model.h:322-333, model.cpp:9-23) and the
+// column classes of the emission step (emit.cpp:30-58). Everything numeric runs on the GPU.
+
+#include "plan.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <thread>
+
+namespace awg {
+
+namespace {
+
+bool valid_base(char c) {
+    switch (c) {
+        case 'A': case 'C': case 'G': case 'T': case 'N':
+        case 'a': case 'c': case 'g': case 't':
+            return true;
+        default:
+            return false;
+    }
+}
+
+struct TreeScratch {
+    std::vector<int> c0, c1;
+    std::vector<char> ignore;
+};
+
+// Children in index order (set_ptree), root, optional child[0] override of the root.
+bool make_children(const int *parent, int n, int rc0, TreeScratch &ts, int &root) {
+    ts.c0.assign(n, -1);
+    ts.c1.assign(n, -1);
+    root = -1;
+    for (int i = 0; i < n; i++) {
+        int p = parent[i];
+        if (p < -1 || p >= n) return false;
+        if (p == -1) {
+            if (root != -1) return false;
+            root = i;
+        } else if (ts.c0[p] == -1) {
+            ts.c0[p] = i;
+        } else if (ts.c1[p] == -1) {
+            ts.c1[p] = i;
+        } else {
+            return false;
+        }
+    }
+    if (root < 0) return false;
+    if (rc0 != -1 && ts.c0[root] != rc0) {
+        if (ts.c1[root] != rc0) return false;
+        std::swap(ts.c0[root], ts.c1[root]);
+    }
+    return true;
+}
+
+}  // namespace
+
+int count_states(const int *parent, const int *age, int n, int T, bool internal, int minage,
+                 int root_child0, int *M_out) {
+    TreeScratch ts;
+    int root;
+    if (!make_children(parent, n, root_child0, ts, root)) return -1;
+    long long S = 0, M = 0;
+    if (!internal) {
+        for (int i = 0; i < n; i++) {
+            int top = parent[i] == -1 ? T - 2 : age[parent[i]];
+            int m = std::max(0, top - age[i] + 1);
+            S += m;
+            M += (long long)m * m;
+        }
+    } else {
+        if (age[root] < T) {
+            if (M_out) *M_out = 0;
+            return 0;
+        }
+        const int sub = ts.c0[root];
+        minage = std::max(minage, age[sub]);
+        for (int i = 0; i < n; i++) {
+            if (i == root) continue;
+            bool in_sub = false;
+            for (int v = i; v != -1; v = parent[v])
+                if (v == sub) { in_sub = true; break; }
+            if (in_sub) continue;
+            int t0 = std::max(age[i], minage);
+            int top = parent[i] == root ? T - 2 : age[parent[i]];
+            int m = std::max(0, top - t0 + 1);
+            S += m;
+            M += (long long)m * m;
+        }
+    }
+    if (M_out) *M_out = (int)M;
+    return (int)S;
+}
+
+bool build_plan(const awg_problem *probs, int n, HostPlan &plan, std::string &err) {
+    plan = HostPlan();
+    if (n <= 0) { err = "empty batch"; return false; }
+    plan.ninst = n;
+    plan.inst.resize(n);
+
+    // pass 1: validation and sizes
+    std::vector<std::vector<int>> S_of(n), M_of(n);
+    long long nblocks = 0;
+    for (int q = 0; q < n; q++) {
+        const awg_problem &p = probs[q];
+        char buf[256];
+        auto fail = [&](const char *what) {
+            snprintf(buf, sizeof(buf), "problem %d: %s", q, what);
+            err = buf;
+            return false;
+        };
+        if (p.ntrees < 1) return fail("ntrees < 1");
+        if (p.nnodes < 1 || p.nnodes > MAXNODES) return fail("nnodes out of range [1, 1024]");
+        if (p.ntimes < 3 || p.ntimes > MAXT) return fail("ntimes out of range [3, 32]");
+        if (!p.ptrees || !p.ages || !p.sprs || !p.blocklens || !p.times || !p.popsizes || !p.seqs)
+            return fail("missing input array");
+        const int nleaves = (p.nnodes + 1) / 2;
+        const int nemit = p.internal ? nleaves : nleaves + 1;
+        if (p.nseqs < nemit) return fail("fewer sequences than leaves (+1 when external)");
+        if (p.minage < 0) return fail("negative minage");
+        long long L = 0;
+        for (int b = 0; b < p.ntrees; b++) {
+            if (p.blocklens[b] < 1) return fail("block length < 1");
+            L += p.blocklens[b];
+        }
+        if (L != p.seqlen) return fail("block lengths do not add up to seqlen");
+        if (p.seqlen < 1) return fail("seqlen < 1");
+        for (int i = 0; i < p.ntimes; i++)
+            if (!(p.times[i] >= 0) || !(p.popsizes[i] > 0)) return fail("bad times or popsizes");
+        for (int i = 1; i < p.ntimes; i++)
+            if (!(p.times[i] > p.times[i - 1])) return fail("times not increasing");
+        S_of[q].resize(p.ntrees);
+        M_of[q].resize(p.ntrees);
+        for (int b = 0; b < p.ntrees; b++) {
+            const int *par = p.ptrees + (size_t)b * p.nnodes;
+            const int *age = p.ages + (size_t)b * p.nnodes;
+            for (int i = 0; i < p.nnodes; i++) {
+                const int maxage = p.internal ? p.ntimes + 1 : p.ntimes - 2;
+                if (age[i] < 0 || age[i] > maxage) return fail("node age out of range");
+            }
+            int M = 0;
+            int rc0 = p.root_child0 ? p.root_child0[b] : -1;
+            int S = count_states(par, age, p.nnodes, p.ntimes, p.internal != 0, p.minage, rc0, &M);
+            if (S < 0) return fail("malformed tree (parents/children)");
+            if (!p.internal && S == 0) return fail("external tree with no states");
+            S_of[q][b] = S;
+            M_of[q][b] = M;
+            plan.maxS = std::max(plan.maxS, S);
+            if (b > 0) {
+                const int *s = p.sprs + (size_t)b * 4;
+                if (s[0] < 0 || s[0] >= p.nnodes || s[2] < 0 || s[2] >= p.nnodes)
+                    return fail("SPR nodes out of range");
+                if (s[1] < 0 || s[1] >= p.ntimes || s[3] < 0 || s[3] >= p.ntimes)
+                    return fail("SPR times out of range");
+                const int *prev = p.ptrees + (size_t)(b - 1) * p.nnodes;
+                if (prev[s[0]] < 0) return fail("SPR recombines the root");
+            }
+        }
+        for (long long c = 0; c < (long long)nemit * p.seqlen; c++)
+            if (!valid_base(p.seqs[c])) return fail("sequence byte outside A,C,G,T,N");
+        nblocks += p.ntrees;
+        plan.maxnodes = std::max(plan.maxnodes, p.nnodes);
+        plan.maxT = std::max(plan.maxT, p.ntimes);
+    }
+    plan.nblocks = (int)nblocks;
+    plan.blocks.resize(nblocks);
+    plan.model.assign((size_t)n * MODEL_STRIDE, 0.0);
+
+    // pass 2: offsets
+    long long cell = 0, col = 0, st = 0, t2 = 0, nodes = 0, map = 0, seq = 0;
+    int blk = 0;
+    for (int q = 0; q < n; q++) {
+        const awg_problem &p = probs[q];
+        const int nleaves = (p.nnodes + 1) / 2;
+        const int nemit = p.internal ? nleaves : nleaves + 1;
+        InstDev &I = plan.inst[q];
+        I.T = p.ntimes; I.internal = p.internal ? 1 : 0; I.minage = p.minage;
+        I.nleaves = nleaves; I.nnodes = p.nnodes; I.nseqs = nemit; I.seqlen = p.seqlen;
+        I.ntrees = p.ntrees; I.block0 = blk; I.pad = 0;
+        I.cell0 = cell; I.col0 = col; I.seq0 = seq; I.model0 = (long long)q * MODEL_STRIDE;
+
+        // model (model.h:322-333, model.cpp:9-23)
+        double *m = &plan.model[(size_t)q * MODEL_STRIDE];
+        const int T = p.ntimes;
+        for (int i = 0; i < T; i++) {
+            m[M_TIMES + i] = p.times[i];
+            m[M_POPSIZES + i] = p.popsizes[i];
+        }
+        for (int i = 0; i < T - 1; i++) m[M_TIMESTEPS + i] = p.times[i + 1] - p.times[i];
+        m[M_TIMESTEPS + T - 1] = INFINITY;
+        std::vector<double> times2(2 * T + 1, 0.0);
+        for (int i = 0; i < T - 1; i++) {
+            times2[2 * i] = p.times[i];
+            times2[2 * i + 1] = std::sqrt((p.times[i + 1] + 1.0) * (p.times[i] + 1.0));
+        }
+        times2[2 * T - 2] = times2[2 * T - 1] = times2[2 * T] = p.times[T - 1];
+        for (int i = 0; i < 2 * T - 2; i++)
+            m[M_COALSTEPS + i] = times2[std::min(i + 1, 2 * T)] - times2[i];
+        m[M_COALSTEPS + 2 * T - 2] = INFINITY;
+        m[M_COALSTEPS + 2 * T - 1] = INFINITY;
+        m[M_CONST + 0] = p.rho;
+        m[M_CONST + 1] = p.mu;
+        m[M_CONST + 2] = p.times[1] * .1;
+
+        int pos = 0;
+        for (int b = 0; b < p.ntrees; b++, blk++) {
+            BlockDev &B = plan.blocks[blk];
+            memset(&B, 0, sizeof(B));
+            B.inst = q; B.b = b; B.start = pos; B.len = p.blocklens[b];
+            B.S = S_of[q][b];
+            B.S1 = b > 0 ? S_of[q][b - 1] : 0;
+            B.nodes0 = (int)nodes;
+            B.prev_nodes0 = b > 0 ? (int)(nodes - p.nnodes) : -1;
+            const int *s = p.sprs + (size_t)b * 4;
+            for (int k = 0; k < 4; k++) B.spr[k] = b > 0 ? s[k] : -1;
+            B.map0 = b > 0 ? (int)map : -1;
+            B.M = M_of[q][b];
+            B.cell0 = cell;
+            B.state0 = st;
+            B.prev_state0 = b > 0 ? plan.blocks[blk - 1].state0 : -1;
+            B.gptr0 = st + blk;
+            B.t2_0 = t2;
+            plan.maxlen = std::max(plan.maxlen, B.len);
+            cell += (long long)B.len * std::max(B.S, 1);
+            st += std::max(B.S, 1);  // a zero-state space still takes one slot
+            t2 += B.M;
+            nodes += p.nnodes;
+            if (b > 0) map += p.nnodes;
+            pos += B.len;
+        }
+        col += p.seqlen;
+        seq += (long long)p.seqlen * nemit;
+    }
+    plan.total_cells = cell; plan.total_cols = col; plan.total_states = st;
+    plan.total_M = t2; plan.total_nodes = nodes; plan.total_map = map; plan.total_seq = seq;
+
+    // pass 3: arrays (instances in parallel)
+    plan.nodes.assign((size_t)nodes * 4, -1);
+    plan.mapping.assign((size_t)std::max(map, 1LL), -1);
+    plan.seqT.assign((size_t)std::max(seq, 1LL), 'N');
+    plan.colclass.assign((size_t)col, COL_INVARIANT);
+    plan.colvar.assign((size_t)col, -1);
+    std::vector<std::string> errs(n);
+
+    auto fill = [&](int q) {
+        const awg_problem &p = probs[q];
+        const InstDev &I = plan.inst[q];
+        TreeScratch ts;
+        for (int b = 0; b < p.ntrees; b++) {
+            BlockDev &B = plan.blocks[I.block0 + b];
+            const int *par = p.ptrees + (size_t)b * p.nnodes;
+            const int *age = p.ages + (size_t)b * p.nnodes;
+            int root;
+            int rc0 = p.root_child0 ? p.root_child0[b] : -1;
+            make_children(par, p.nnodes, rc0, ts, root);
+            B.root = root;
+            int *nd = &plan.nodes[(size_t)B.nodes0 * 4];
+            for (int i = 0; i < p.nnodes; i++) {
+                nd[4 * i + 0] = par[i];
+                nd[4 * i + 1] = ts.c0[i];
+                nd[4 * i + 2] = ts.c1[i];
+                nd[4 * i + 3] = age[i];
+            }
+            if (b > 0) {
+                B.prev_root = plan.blocks[I.block0 + b - 1].root;
+                int *mp = &plan.mapping[B.map0];
+                if (p.mapping) {
+                    memcpy(mp, p.mapping + (size_t)b * p.nnodes, sizeof(int) * p.nnodes);
+                } else {
+                    const int *prev = p.ptrees + (size_t)(b - 1) * p.nnodes;
+                    for (int j = 0; j < p.nnodes; j++) mp[j] = j;
+                    mp[prev[B.spr[0]]] = -1;
+                }
+            } else {
+                B.prev_root = -1;
+            }
+        }
+        // column-major sequences and column classes
+        const int ns = I.nseqs, L = p.seqlen;
+        uint8_t *dst = &plan.seqT[I.seq0];
+        for (int r = 0; r < ns; r++) {
+            const char *row = p.seqs + (size_t)r * L;
+            for (int i = 0; i < L; i++) dst[(size_t)i * ns + r] = (uint8_t)row[i];
+        }
+        uint8_t *cls = &plan.colclass[I.col0];
+        int *cv = &plan.colvar[I.col0];
+        for (int b = 0; b < p.ntrees; b++) {
+            BlockDev &B = plan.blocks[I.block0 + b];
+            int nv = 0;
+            for (int i = B.start; i < B.start + B.len; i++) {
+                const uint8_t *c = dst + (size_t)i * ns;
+                bool inv = true;
+                for (int r = 1; r < ns; r++)
+                    if (c[r] != c[0]) { inv = false; break; }
+                if (inv) {
+                    cls[i] = (c[0] == 'N') ? COL_MASKED : COL_INVARIANT;
+                } else {
+                    cls[i] = COL_VARIANT;
+                    cv[i] = nv++;
+                }
+            }
+            B.nvar = nv;
+        }
+    };
+    const int nthreads = std::max(1, std::min<int>(n, (int)std::thread::hardware_concurrency()));
+    if (nthreads <= 1 || n < 4) {
+        for (int q = 0; q < n; q++) fill(q);
+    } else {
+        std::vector<std::thread> pool;
+        for (int t = 0; t < nthreads; t++)
+            pool.emplace_back([&, t]() {
+                for (int q = t; q < n; q += nthreads) fill(q);
+            });
+        for (auto &th : pool) th.join();
+    }
+    long long var = 0;
+    for (auto &B : plan.blocks) {
+        B.var0 = var;
+        var += (long long)B.nvar * std::max(B.S, 1);
+    }
+    plan.total_var = var;
+    return true;
+}
+
+}  // namespace awg

@@ -1,0 +1,26 @@
+// Kernel launchers (all asynchronous on the given stream).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "awg_internal.h"
+
+namespace awg {
+
+// K1: per-block tables (states, transition matrix, same-branch rows, switch matrix,
+// priors into forward column 0, invariant emissions); one CTA per local tree.
+void launch_tables(const BatchDev &d, bool want32, cudaStream_t s);
+// K2: emissions of variant columns (Felsenstein pruning); one CTA per local tree.
+void launch_varemit(const BatchDev &d, bool want32, cudaStream_t s);
+// K3: forward pass, one CTA per instance.
+void launch_forward(const BatchDev &d, bool fp32, cudaStream_t s);
+// K4: stochastic traceback, one warp per instance.
+void launch_traceback(const BatchDev &d, bool fp32, cudaStream_t s);
+// K5: backward pass fused with the posterior marginals, one CTA per instance.
+void launch_backward(const BatchDev &d, bool fp32, double *bw_out, cudaStream_t s);
+
+// Count of kernels launched by this library (process-wide).
+long long kernel_launch_count();
+void note_launch();
+
+}  // namespace awg

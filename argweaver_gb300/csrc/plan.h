@@ -1,0 +1,39 @@
+// Host-side plan of a batch: validated inputs packed into the flat arrays the kernels read.
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "argweaver_gb300.h"
+#include "awg_internal.h"
+
+namespace awg {
+
+struct HostPlan {
+    int ninst = 0, nblocks = 0, maxS = 1, maxnodes = 1, maxT = 0, maxlen = 1;
+    long long total_states = 0;  // sum of S over blocks
+    long long total_cells = 0;   // forward-table cells of the batch
+    long long total_cols = 0;    // columns of the batch
+    long long total_M = 0;       // same-branch row entries
+    long long total_var = 0;     // variant emission cells
+    long long total_nodes = 0;   // tree nodes (int4 each)
+    long long total_map = 0;     // mapping ints
+    long long total_seq = 0;     // sequence bytes
+    std::vector<InstDev> inst;
+    std::vector<BlockDev> blocks;
+    std::vector<double> model;
+    std::vector<int> nodes;      // 4 ints per node
+    std::vector<int> mapping;
+    std::vector<uint8_t> seqT;
+    std::vector<uint8_t> colclass;
+    std::vector<int> colvar;
+};
+
+// Validates the problems and fills the plan; returns false with a message on bad input.
+bool build_plan(const awg_problem *probs, int n, HostPlan &plan, std::string &err);
+
+// Number of states of a local tree given by parent/age arrays (states.cpp:53-199).
+int count_states(const int *parent, const int *age, int n, int T, bool internal, int minage,
+                 int root_child0, int *M_out);
+
+}  // namespace awg

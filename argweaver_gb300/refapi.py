@@ -1,0 +1,162 @@
+"""The reference's Python-facing threading-HMM calls, in Python 3, over this library.
+
+Mirrors argweaver/argweaverc.py: ``argweaver_forward_algorithm`` (argweaverc.py:529-572),
+``sample_posterior`` (the commented-out wrapper at argweaverc.py:611-649, here live) and
+the raw prototypes, taking the same tree arrays the reference's ``get_treeset`` builds
+(ptrees, ages, sprs, blocklens). Randomness follows the reference: libc rand(), seeded
+with ``srand`` (argweaverc.py:347-354).
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from typing import List, Sequence
+
+import numpy as np
+
+from . import capi
+from .problem import Problem
+
+_libc = C.CDLL(None)
+
+
+def srand(seed: int) -> None:
+    """Seed libc's rand(), the generator the samplers draw from (common.h:103-110)."""
+    _libc.srand(C.c_uint(seed))
+
+
+def _int_matrix(a: np.ndarray):
+    a = np.ascontiguousarray(a, dtype=np.int32)
+    rows = (capi.c_int_p * a.shape[0])(*[a[i].ctypes.data_as(capi.c_int_p)
+                                        for i in range(a.shape[0])])
+    return rows, a
+
+
+def _char_pp(seqs: np.ndarray):
+    seqs = np.ascontiguousarray(seqs, dtype=np.uint8)
+    rows = (C.c_char_p * seqs.shape[0])(*[bytes(seqs[i]) for i in range(seqs.shape[0])])
+    return C.cast(rows, capi.c_char_pp), rows
+
+
+class LocalTrees:
+    """Handle from arghmm_new_trees (local_tree.cpp:1817); freed on close/delete."""
+
+    def __init__(self, prob: Problem):
+        lib = capi.load()
+        p = prob.normalized()
+        self._pt = _int_matrix(p.ptrees)
+        self._ag = _int_matrix(p.ages)
+        self._sp = _int_matrix(p.sprs)
+        self._bl = p.blocklens
+        self.handle = lib.arghmm_new_trees(self._pt[0], self._ag[0], self._sp[0],
+                                           p.blocklens.ctypes.data_as(capi.c_int_p),
+                                           p.ntrees, p.nnodes, p.start_coord)
+        if not self.handle:
+            raise ValueError(capi.last_error())
+
+    def close(self):
+        if self.handle:
+            capi.load().delete_local_trees(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def get_nstates(trees: LocalTrees, ntimes: int, internal: bool, seqlen: int) -> np.ndarray:
+    out = np.zeros(seqlen, dtype=np.int32)
+    capi.load().arghmm_get_nstates(trees.handle, ntimes, internal,
+                                   out.ctypes.data_as(capi.c_int_p))
+    return out
+
+
+def _rows_to_list(mat, nstates: np.ndarray) -> List[np.ndarray]:
+    return [np.ctypeslib.as_array(mat[i], shape=(max(int(n), 1),)).copy()
+            for i, n in enumerate(nstates)]
+
+
+def arghmm_forward_alg(prob: Problem, prior: Sequence[float] = (), slow: bool = False
+                       ) -> List[np.ndarray]:
+    """Forward table as a list of per-column arrays, like argweaver_forward_algorithm."""
+    lib = capi.load()
+    p = prob.normalized()
+    trees = LocalTrees(p)
+    seqs, _keep = _char_pp(p.seqs)
+    prior_arr = np.ascontiguousarray(prior, dtype=np.float64)
+    fw = lib.arghmm_forward_alg(trees.handle, p.times.ctypes.data_as(capi.c_double_p),
+                                p.ntimes, p.popsizes.ctypes.data_as(capi.c_double_p), p.rho,
+                                p.mu, seqs, p.nseqs, p.seqlen, len(prior_arr) > 0,
+                                prior_arr.ctypes.data_as(capi.c_double_p), p.internal, slow)
+    if not fw:
+        raise RuntimeError(capi.last_error())
+    nstates = get_nstates(trees, p.ntimes, p.internal, p.seqlen)
+    probs = _rows_to_list(fw, nstates)
+    lib.delete_forward_matrix(fw, p.seqlen)
+    trees.close()
+    return probs
+
+
+def _table_call(name: str, prob: Problem) -> List[np.ndarray]:
+    lib = capi.load()
+    p = prob.normalized()
+    trees = LocalTrees(p)
+    seqs, _keep = _char_pp(p.seqs)
+    mat = getattr(lib, name)(trees.handle, p.times.ctypes.data_as(capi.c_double_p), p.ntimes,
+                             p.popsizes.ctypes.data_as(capi.c_double_p), p.rho, p.mu, seqs,
+                             p.nseqs, p.seqlen, p.internal)
+    if not mat:
+        raise RuntimeError(capi.last_error())
+    nstates = get_nstates(trees, p.ntimes, p.internal, p.seqlen)
+    out = _rows_to_list(mat, nstates)
+    lib.delete_forward_matrix(mat, p.seqlen)
+    trees.close()
+    return out
+
+
+def arghmm_backward_alg(prob: Problem) -> List[np.ndarray]:
+    return _table_call("arghmm_backward_alg", prob)
+
+
+def arghmm_posterior_marginals(prob: Problem) -> List[np.ndarray]:
+    return _table_call("arghmm_posterior_marginals", prob)
+
+
+def arghmm_sample_posterior(prob: Problem) -> np.ndarray:
+    """(node, time) of the sampled thread per column (arghmm_sample_posterior)."""
+    lib = capi.load()
+    p = prob.normalized()
+    pt, _a = _int_matrix(p.ptrees)
+    ag, _b = _int_matrix(p.ages)
+    sp, _c = _int_matrix(p.sprs)
+    seqs, _keep = _char_pp(p.seqs)
+    path = lib.arghmm_sample_posterior(pt, ag, sp, p.blocklens.ctypes.data_as(capi.c_int_p),
+                                       p.ntrees, p.nnodes,
+                                       p.times.ctypes.data_as(capi.c_double_p), p.ntimes,
+                                       p.popsizes.ctypes.data_as(capi.c_double_p), p.rho, p.mu,
+                                       seqs, p.nseqs, p.seqlen, None)
+    if not path:
+        raise RuntimeError(capi.last_error())
+    out = np.ctypeslib.as_array(path, shape=(2 * p.seqlen,)).reshape(p.seqlen, 2).copy()
+    lib.delete_path(path)
+    return out
+
+
+def arghmm_sample_arg_thread_internal(prob: Problem) -> np.ndarray:
+    """State index per column of a sampled internal-branch thread."""
+    lib = capi.load()
+    p = prob.normalized()
+    trees = LocalTrees(p)
+    seqs, _keep = _char_pp(p.seqs)
+    out = np.zeros(p.seqlen, dtype=np.int32)
+    lib.arghmm_sample_arg_thread_internal(trees.handle, p.times.ctypes.data_as(capi.c_double_p),
+                                          p.ntimes, p.popsizes.ctypes.data_as(capi.c_double_p),
+                                          p.rho, p.mu, seqs, p.nseqs, p.seqlen,
+                                          out.ctypes.data_as(capi.c_int_p))
+    err = capi.last_error()
+    trees.close()
+    if err:
+        raise RuntimeError(err)
+    return out

@@ -1,0 +1,283 @@
+#!/usr/bin/env python3
+"""Benchmark: batched threading HMM, forward + stochastic traceback, state-cells/s.
+
+Workload (the headline configuration): 256 independent threading problems, each a seeded
+DSMC ARG with k ~ U{8..64} haplotypes (k-1 in the ARG, one re-threaded), L ~ U[100 kb,
+1 Mb] at 10 bp per column, ntimes=20, N=1e4, r=1.6e-8, mu=1.8e-8, 0.5% missing calls.
+One step = forward + traceback of the whole batch in FP32 (log scales in FP64).
+
+  value     cells / device time of the step's kernels, inputs resident in HBM
+  e2e       cells / wall time of the public call awg_run_batch with host buffers: host
+            plan, host->device copy of the inputs, kernels, device->host copy of the paths
+  roofline  forward+traceback kernels: 8 B per cell (FP32 write + read) over their time,
+            against the measured HBM copy bandwidth
+  cpu_baseline  the CPU port of the reference's algorithm (oracle/) on the host cores,
+            one problem per thread, on a bounded sample of the same problems
+
+Flags: --gpus N --steps K --warmup W [--impl reference] [--instances n] [--seed s]
+Multi-GPU: replicas (each rank threads its own 256 problems; weak scaling).
+"""
+
+from __future__ import annotations
+
+import argparse
+import concurrent.futures as cf
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "HMM state-cells/s fwd+traceback, batched FP32 vs plain FP64 @<=1e-5 err; p50/p99"
+UNIT = "state-cells/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--instances", type=int, default=256)
+    ap.add_argument("--seed", type=int, default=20261203)
+    ap.add_argument("--cpu-sample-seconds", type=float, default=15.0)
+    return ap.parse_args()
+
+
+def make_workload(n: int, seed: int, rank: int = 0):
+    from argweaver_gb300.sim import simulate
+
+    rng = np.random.default_rng(seed + 7919 * rank)
+    ks = rng.integers(8, 65, size=n)                # haplotypes incl. the re-threaded one
+    bps = rng.uniform(1e5, 1e6, size=n)
+    seeds = rng.integers(1, 2**62, size=n)
+    specs = [(int(k) - 1, int(bp // 10), int(s)) for k, bp, s in zip(ks, bps, seeds)]
+
+    def one(spec):
+        nl, L, s = spec
+        return simulate(nl, L, s, compress=10, ntimes=20, maxtime=200e3, popsize=1e4,
+                        rho=1.6e-8, mu=1.8e-8, missing=0.005)
+
+    with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        return list(ex.map(one, specs))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0],
+                 f"--query-gpu={self.Q}", "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        sm = [float(r[0]) for r in self.rows if r and r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if len(r) > 1 and r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4)
+                          if len(r) > 2 + i and r[2 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(sm)}
+
+
+def cpu_reference(problems, seconds: float, threads: int):
+    """Time the oracle's forward+traceback (the reference's algorithm, ported to C) on
+    problems, one per thread, until about `seconds` of wall time; returns cells/s."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+
+    pyoracle.load()
+    done_cells = [0]
+    lock = threading.Lock()
+    order = sorted(range(len(problems)), key=lambda i: problems[i].cells())
+    t0 = time.perf_counter()
+    deadline = t0 + seconds
+
+    def work(i):
+        if time.perf_counter() > deadline:
+            return
+        p = problems[i]
+        fw, _ = pyoracle.forward(p)
+        u = np.random.default_rng(i).random(p.seqlen)
+        pyoracle.traceback(p, fw, u)
+        with lock:
+            done_cells[0] += fw.size
+
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        list(ex.map(work, order))
+    dt = time.perf_counter() - t0
+    return done_cells[0] / dt, done_cells[0], dt
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    threads = os.cpu_count() or 1
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        problems = make_workload(args.instances, args.seed)
+        for _ in range(args.warmup):
+            cpu_reference(problems, min(2.0, args.cpu_sample_seconds), threads)
+        vals = []
+        cells_total, t_total = 0, 0.0
+        for _ in range(args.steps):
+            v, c, dt = cpu_reference(problems, args.cpu_sample_seconds, threads)
+            vals.append(v)
+            cells_total += c
+            t_total += dt
+        v = cells_total / t_total
+        print(json.dumps({
+            "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded DSMC ARGs)",
+            "config": {"workload": "batched threading, 256 problems, k~U{8..64}, "
+                                   "L~U[1e4,1e5] columns, ntimes=20, 0.5% missing",
+                       "sample": "problems in ascending size until the time budget"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{args.cpu_sample_seconds:.0f} s per step of the same "
+                                       "problems, smallest first, one per thread"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }))
+        return
+
+    import torch
+
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+    from argweaver_gb300 import api
+
+    problems = make_workload(args.instances, args.seed, rank)
+    cells = sum(p.cells() for p in problems)
+    h2d = sum(p.ptrees.nbytes + p.ages.nbytes + p.sprs.nbytes + p.blocklens.nbytes +
+              p.seqs.nbytes for p in problems)
+    d2h = sum(4 * p.seqlen + 8 for p in problems)
+    rng = np.random.default_rng(args.seed)
+    uniforms = [rng.random(p.seqlen) for p in problems]
+
+    def step():
+        return api.run_batch(problems, precision="fp32", want_forward=False, want_path=True,
+                             uniforms=uniforms)
+
+    api.set_timing(True)
+    for _ in range(max(args.warmup, 3)):
+        step()
+    launches0 = api.kernel_launches()
+    sampler = ClockSampler()
+    sampler.start()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    dev_ms, fwd_ms, tb_ms, wall = [], [], [], []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        step()
+        wall.append(time.perf_counter() - t0)
+        t = api.last_timings()
+        dev_ms.append(t["tables"] + t["emit"] + t["forward"] + t["traceback"])
+        fwd_ms.append(t["forward"])
+        tb_ms.append(t["traceback"])
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = sampler.stop()
+    launches = api.kernel_launches() - launches0
+
+    dev_s = sum(dev_ms) / 1e3
+    wall_s = sum(wall)
+    if world > 1:
+        t = torch.tensor([dev_s, wall_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        dev_s, wall_s = float(t[0]), float(t[1])
+    value = world * cells * args.steps / dev_s
+    e2e = world * cells * args.steps / wall_s
+
+    # error report outside the timed region: FP32 vs FP64 posteriors on a few problems
+    sample = sorted(problems, key=lambda p: p.cells())[:4]
+    errs = []
+    for p in sample:
+        a = api.run_batch([p], precision="fp32", want_forward=False, want_posterior=True)[0]
+        b = api.run_batch([p], precision="fp64", want_forward=False, want_posterior=True)[0]
+        errs.append(float(np.max(np.abs(a.posterior - b.posterior))))
+
+    if rank != 0:
+        return
+    hbm, src = peaks()
+    achieved = cells * 8 / ((sum(fwd_ms) + sum(tb_ms)) / args.steps / 1e3) / 1e9
+    cpu_v, cpu_cells, cpu_dt = cpu_reference(problems, args.cpu_sample_seconds, os.cpu_count() or 1)
+    per_inst = sorted(p.cells() for p in problems)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded DSMC ARGs, simulated in-process)",
+        "config": {"workload": f"batched threading, {args.instances} problems, k~U{{8..64}}, "
+                               "L~U[1e4,1e5] columns (10 bp), ntimes=20, 0.5% missing, "
+                               "FP32 forward + traceback, log scales in FP64",
+                   "cells_per_step": cells, "instances": args.instances,
+                   "cells_per_instance_p50": per_inst[len(per_inst) // 2],
+                   "l2": "inputs and tables larger than L2 (129 MB)",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * wall_s / args.steps},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": None,
+                     "peak_source": src,
+                     "kernels": "forward+traceback, 8 B per cell (FP32 write + read)"},
+        "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                         "sample": f"{cpu_cells} cells in {cpu_dt:.1f} s: the same problems, "
+                                   "smallest first, one per thread"},
+        "fp32_vs_fp64_posterior_max_abs_err": max(errs),
+        "gpu_launches": launches,
+        "clocks": clocks,
+        "phase_ms": api.last_timings(),
+    }
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

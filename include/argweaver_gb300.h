@@ -1,0 +1,152 @@
+/* argweaver_gb300 — the chromosome-threading HMM of ARGweaver on one GB300 (sm_103a).
+ *
+ * Two groups of entry points:
+ *
+ *  1. The reference's C ABI for the threading HMM, same names, signatures and ownership
+ *     rules (libargweaver.so, declared by the reference's ctypes prototypes in
+ *     argweaver/argweaverc.py:133-167). A ctypes or C caller of the reference switches
+ *     libraries without code changes. Results are host memory allocated with new[], freed
+ *     by the matching delete_* export of this library.
+ *
+ *  2. A flat batch API (awg_*) over plain arrays: many problems per call, FP64 or FP32
+ *     compute, explicit uniforms, device-resident sessions for serving.
+ *
+ * Threading and randomness: as in the reference, the C-ABI samplers draw their uniforms
+ * from libc rand() (one per column, last column first: common.h:103-110,
+ * sample_thread.cpp:522-569), so srand(seed) reproduces the reference's draws. Calls are
+ * synchronous. Errors: the reference returns no codes (it asserts); these entry points
+ * log to stderr and return NULL / leave outputs untouched, and awg_last_error() holds the
+ * message. Nothing here traps the device.
+ */
+#ifndef ARGWEAVER_GB300_H
+#define ARGWEAVER_GB300_H
+
+#include <stdbool.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------------------------
+ * Reference-compatible C ABI
+ * --------------------------------------------------------------------------------- */
+
+/* A (node, time) state, as the reference's intstate (states.h:135). */
+typedef int awg_intstate[2];
+
+/* Opaque local-tree set. Replaces LocalTrees* (local_tree.h:504) on the C-ABI surface. */
+typedef struct awg_local_trees awg_local_trees;
+
+/* arghmm_new_trees (local_tree.cpp:1817): trees from parent arrays (leaves first), age
+ * indices, SPRs (recomb_node, recomb_time, coal_node, coal_time) and block lengths; node
+ * mappings follow make_node_mapping (local_tree.h:767). */
+awg_local_trees *arghmm_new_trees(int **ptrees, int **ages, int **sprs, int *blocklens,
+                                  int ntrees, int nnodes, int start_coord);
+/* delete_local_trees (local_tree.cpp:1895) */
+void delete_local_trees(awg_local_trees *trees);
+/* get_local_trees_ntrees / _nnodes (local_tree.cpp:1838-1847) */
+int get_local_trees_ntrees(awg_local_trees *trees);
+int get_local_trees_nnodes(awg_local_trees *trees);
+
+/* arghmm_get_nstates (states.cpp:209): states of every column. */
+void arghmm_get_nstates(awg_local_trees *trees, int ntimes, bool internal, int *nstates);
+
+/* arghmm_forward_alg (sample_thread.cpp:887-926): FP64 forward table, seqlen rows of
+ * max(nstates,1) doubles; free with delete_forward_matrix. `slow` is accepted for ABI
+ * compatibility (the dense step gives the same table). */
+double **arghmm_forward_alg(awg_local_trees *trees, double *times, int ntimes,
+                            double *popsizes, double rho, double mu, char **seqs, int nseqs,
+                            int seqlen, bool prior_given, double *prior, bool internal,
+                            bool slow);
+
+/* arghmm_backward_alg: NEW (the reference has no backward pass for the threading HMM).
+ * Same arguments as arghmm_forward_alg minus prior/slow; table layout as the forward
+ * table, each column normalised to sum 1; free with delete_forward_matrix. */
+double **arghmm_backward_alg(awg_local_trees *trees, double *times, int ntimes,
+                             double *popsizes, double rho, double mu, char **seqs, int nseqs,
+                             int seqlen, bool internal);
+
+/* arghmm_posterior_marginals: NEW. Posterior state marginals P(state at column i | data)
+ * from forward-backward, layout as the forward table; free with delete_forward_matrix. */
+double **arghmm_posterior_marginals(awg_local_trees *trees, double *times, int ntimes,
+                                    double *popsizes, double rho, double mu, char **seqs,
+                                    int nseqs, int seqlen, bool internal);
+
+/* arghmm_sample_posterior (sample_thread.cpp:930-977): forward + stochastic traceback on
+ * trees given as arrays; returns (node, time) per column (allocated when path == NULL).
+ * The reference converts every block over [start, start+blocklen) of the block start
+ * (an inner `end` shadows the outer one, sample_thread.cpp:959-962); this export converts
+ * each column with its own block's state space. Free with delete_path. */
+awg_intstate *arghmm_sample_posterior(int **ptrees, int **ages, int **sprs, int *blocklens,
+                                      int ntrees, int nnodes, double *times, int ntimes,
+                                      double *popsizes, double rho, double mu, char **seqs,
+                                      int nseqs, int seqlen, awg_intstate *path);
+
+/* arghmm_sample_arg_thread_internal (sample_thread.cpp:981-1006): forward + traceback for
+ * an internal branch; writes the state index of every column into thread_path[seqlen]. */
+void arghmm_sample_arg_thread_internal(awg_local_trees *trees, double *times, int ntimes,
+                                       double *popsizes, double rho, double mu, char **seqs,
+                                       int nseqs, int seqlen, int *thread_path);
+
+/* delete_path / delete_double_matrix / delete_forward_matrix (sample_thread.cpp:1026-1042) */
+void delete_path(int *path);
+void delete_double_matrix(double **mat, int nrows);
+void delete_forward_matrix(double **mat, int nrows);
+
+/* ---------------------------------------------------------------------------------
+ * Flat batch API
+ * --------------------------------------------------------------------------------- */
+
+/* One threading problem over plain arrays (the arrays arghmm_new_trees takes). */
+typedef struct {
+    int ntrees, nnodes, ntimes, nseqs, seqlen, internal, start_coord, minage;
+    const int *ptrees;      /* [ntrees*nnodes] parent (-1 for the root), leaves first */
+    const int *ages;        /* [ntrees*nnodes] age as a time index */
+    const int *sprs;        /* [ntrees*4] SPR to the left of each tree (row 0 unused) */
+    const int *blocklens;   /* [ntrees] columns of each tree */
+    const int *mapping;     /* [ntrees*nnodes] node map from the previous tree, or NULL */
+    const int *root_child0; /* [ntrees] child[0] of each root, or NULL (index order);
+                               internal-branch trees name their cut subtree there */
+    const double *times;    /* [ntimes] time points */
+    const double *popsizes; /* [ntimes] population sizes (diploid N, as the reference) */
+    double rho, mu;         /* per column */
+    const char *seqs;       /* [nseqs*seqlen] rows: leaves in leaf order, then (external)
+                               the sequence being threaded; bytes A,C,G,T (either case), N */
+} awg_problem;
+
+enum { AWG_FP64 = 0, AWG_FP32 = 1 };
+
+/* Outputs of one problem in a batch. Any pointer may be NULL (not wanted). Tables are
+ * packed column after column, max(nstates,1) entries per column. */
+typedef struct {
+    double *forward;        /* [cells] forward table (FP64 compute) */
+    float *forward32;       /* [cells] forward table (FP32 compute) */
+    double *posterior;      /* [cells] posterior marginals */
+    int *path;              /* [seqlen] sampled state index per column */
+    double *loglik;         /* [1] sum over columns i>=1 of log(column norm) */
+    const double *uniforms; /* [seqlen] input: u[i] drives the draw at column i; NULL
+                               draws from libc rand() in the reference's order */
+} awg_outputs;
+
+/* Number of forward-table cells of a problem (sum over columns of max(nstates,1)),
+ * or -1 when the problem is invalid. */
+long long awg_problem_cells(const awg_problem *p);
+
+/* Run forward (+ traceback when path is wanted, + backward when posterior is wanted) for
+ * n problems in one batch on the current device. precision: AWG_FP64 or AWG_FP32.
+ * Returns 0 on success, a negative code on error (awg_last_error() has the message). */
+int awg_run_batch(const awg_problem *problems, awg_outputs *outputs, int n, int precision);
+
+/* Message of the last error on this thread ("" when none). */
+const char *awg_last_error(void);
+
+/* Device and library information: device name and the number of kernels launched by
+ * this process so far (every kernel of this library counts). */
+int awg_device_name(char *buf, int len);
+long long awg_kernel_launches(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ARGWEAVER_GB300_H */

@@ -1423,6 +1423,50 @@ int oracle_block_terms(const oracle_problem *p, double *out_terms, int *out_mina
     return 0;
 }
 
+int oracle_debug_tables(const oracle_problem *p, double *tm_out, double *gts_out,
+                        double *inv_out, double *prior_out) {
+    Hmm h;
+    if (!setup(p, h)) return -1;
+    const int T = h.m.T;
+    long long goff = 0, ioff = 0;
+    BlockSteps bs;
+    for (size_t b = 0; b < h.arg.trees.size(); b++) {
+        Block blk;
+        if (!make_block(h, (int)b, blk, false)) return -2;
+        const Tree &t = h.arg.trees[b];
+        block_steps(t, T, blk.states, blk.tm, h.internal, bs);
+        for (int a = 0; a < T - 1; a++)
+            for (int c = 0; c < T - 1; c++)
+                tm_out[(b * (T - 1) + a) * (T - 1) + c] = bs.tmatrix[a * T + c];
+        const int S = blk.states.size();
+        // rows in node order: node v's states j1..j1+m-1, each row over the node's times
+        int k = 0;
+        while (k < S) {
+            const int v = blk.states.node[k];
+            int m = 0;
+            while (k + m < S && blk.states.node[k + m] == v) m++;
+            const int t0 = blk.states.time[k];
+            for (int x = 0; x < m; x++)
+                for (int y = 0; y < m; y++)
+                    gts_out[goff++] = blk.tm.get_time(t0 + y, t0 + x, t.age[v], blk.tm.minage, true);
+            k += m;
+        }
+        // invariant-site emission per state: the emission of an all-equal column
+        vector<double> emit;
+        Block one = blk;
+        one.len = 1;
+        vector<char> col(h.nseqs_emit, 'A');
+        vector<const char *> rows(h.nseqs_emit);
+        for (int i = 0; i < h.nseqs_emit; i++) rows[i] = &col[i];
+        vector<double> e(std::max(S, 1));
+        calc_emissions(blk.states, t, rows.data(), h.nseqs_emit, 1, h.m, h.internal, e.data());
+        for (int j = 0; j < std::max(S, 1); j++) inv_out[ioff + j] = e[j];
+        ioff += std::max(S, 1);
+        if (b == 0) calc_state_priors(blk.states, blk.lineages, h.m, prior_out, h.minage);
+    }
+    return 0;
+}
+
 int oracle_emissions(const oracle_problem *p, double *emit_out) {
     Hmm h;
     if (!setup(p, h)) return -1;

@@ -57,6 +57,13 @@ int oracle_block_terms(const oracle_problem *p, double *out_terms, int *out_mina
 /* Emissions of every column, packed like the forward table. */
 int oracle_emissions(const oracle_problem *p, double *emit);
 
+/* The tables of the GPU table kernel, same layouts (for kernel-level checks): tmatrix
+ * [ntrees][T-1][T-1]; same-branch rows get_time(a, b_k, c_k, minage, true) for a over the
+ * times of k's node, nodes in index order, [sum over trees of sum over nodes of m^2];
+ * invariant-site emissions [sum over trees of max(S,1)]; column-0 prior [max(S0,1)]. */
+int oracle_debug_tables(const oracle_problem *p, double *tm, double *gts, double *inv,
+                        double *prior);
+
 /* Total cells: sum over columns of max(nstates,1). */
 long long oracle_cells(const oracle_problem *p);
 

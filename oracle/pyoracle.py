@@ -46,7 +46,9 @@ def load():
                            ("oracle_backward", [P, C.c_void_p]),
                            ("oracle_posterior", [P, C.c_void_p, C.c_void_p, C.c_void_p]),
                            ("oracle_block_terms", [P, C.c_void_p, C.c_void_p]),
-                           ("oracle_emissions", [P, C.c_void_p])]:
+                           ("oracle_emissions", [P, C.c_void_p]),
+                           ("oracle_debug_tables", [P, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                    C.c_void_p])]:
             fn = getattr(lib, name)
             fn.restype = C.c_int
             fn.argtypes = args
@@ -147,6 +149,42 @@ def emissions(prob) -> np.ndarray:
     out = np.zeros(lib.oracle_cells(b.ref), dtype=np.float64)
     _check(lib.oracle_emissions(b.ref, out.ctypes.data), "emissions")
     return out
+
+
+def debug_tables(prob):
+    """tmatrix, same-branch rows, invariant emissions and prior, GPU table-kernel layout."""
+    b = Bound(prob)
+    T = prob.ntimes
+    S = prob.nstates_per_tree()
+    M = 0
+    for t in range(prob.ntrees):
+        par, age = prob.ptrees[t], prob.ages[t]
+    tm = np.zeros(prob.ntrees * (T - 1) * (T - 1))
+    # sizes from the host-side state spaces
+    Mtot = _total_M(prob)
+    gts = np.zeros(max(Mtot, 1))
+    inv = np.zeros(int(np.maximum(S, 1).sum()))
+    prior = np.zeros(max(int(S[0]), 1))
+    _check(load().oracle_debug_tables(b.ref, tm.ctypes.data, gts.ctypes.data, inv.ctypes.data,
+                                      prior.ctypes.data), "debug tables")
+    return tm.reshape(prob.ntrees, T - 1, T - 1), gts[:Mtot], inv, prior
+
+
+def _total_M(prob) -> int:
+    ns = nstates(prob)
+    del ns
+    T = prob.ntimes
+    tot = 0
+    for t in range(prob.ntrees):
+        par, age = prob.ptrees[t], prob.ages[t]
+        if not prob.internal:
+            for v in range(prob.nnodes):
+                top = T - 2 if par[v] == -1 else age[par[v]]
+                m = max(0, top - age[v] + 1)
+                tot += m * m
+        else:
+            raise NotImplementedError("debug tables: external problems only")
+    return tot
 
 
 def rand_uniforms(seed: int, n: int) -> np.ndarray:

@@ -1,0 +1,226 @@
+"""Parity of the CUDA path with the oracle and the reference (GPU only).
+
+Bars:
+  FP64 forward table        <= 1e-12 relative to the oracle, per cell, and to the
+                             reference's column checksums in tests/golden
+  sampled path (FP64)       identical to the reference's, given the same uniforms
+  posterior marginals FP64  <= 1e-10 relative to the oracle's forward-backward
+  log-likelihood            <= 1e-12 relative to the oracle
+  FP32 posterior            <= 1e-5 absolute (max over cells) of the FP64 posterior
+The reference-compatible entry points (arghmm_forward_alg, arghmm_sample_posterior, ...)
+are exercised through the same ctypes prototypes the reference declares.
+"""
+
+import os
+
+import numpy as np
+import pytest
+
+import pyoracle
+from argweaver_gb300 import api, refapi
+from argweaver_gb300.problem import Problem
+from argweaver_gb300.sim import simulate
+from conftest import GOLDEN, golden_names
+
+pytestmark = pytest.mark.gpu
+
+NAMES = golden_names()
+EXTERNAL_DEFAULT_MAP = [n for n in NAMES if n.startswith(("dsmc_", "single_"))]
+
+
+def load(name):
+    return (Problem.load(os.path.join(GOLDEN, name + ".prob")),
+            np.load(os.path.join(GOLDEN, name + ".npz")))
+
+
+def weights(n):
+    k = np.arange(n, dtype=np.int64)
+    return 1.0 + ((k * 2654435761) % 1000) / 1000.0
+
+
+def max_rel(a, b, floor=1e-300):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), floor)))
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_forward_fp64_matches_oracle_and_reference(name):
+    prob, gold = load(name)
+    r = api.run_batch([prob])[0]
+    fw_o, lnl_o = pyoracle.forward(prob)
+    assert r.forward.shape == fw_o.shape
+    assert max_rel(r.forward, fw_o) <= 1e-12
+    assert abs(r.loglik - lnl_o) <= 1e-12 * abs(lnl_o)
+    ns = gold["nstates"]
+    off = pyoracle.offsets(ns)
+    colsum = np.add.reduceat(r.forward, off[:-1])
+    np.testing.assert_allclose(colsum, gold["colsum"], rtol=1e-12)
+    colw = np.array([(r.forward[off[i]:off[i + 1]] * weights(off[i + 1] - off[i])).sum()
+                     for i in range(prob.seqlen)])
+    np.testing.assert_allclose(colw, gold["colwsum"], rtol=1e-12)
+    rows = np.concatenate([r.forward[off[i]:off[i + 1]] for i in gold["rows"]])
+    np.testing.assert_allclose(rows, gold["rowvals"], rtol=1e-12, atol=1e-300)
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_sampled_path_matches_reference(name):
+    prob, gold = load(name)
+    path = api.sample_path(prob, uniforms=gold["uniforms"])
+    np.testing.assert_array_equal(path, gold["path"])
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_posterior_fp64_matches_oracle(name):
+    prob, _ = load(name)
+    post = api.posterior(prob)
+    fw, _ = pyoracle.forward(prob)
+    bw = pyoracle.backward(prob)
+    ref = pyoracle.posterior(prob, fw, bw)
+    big = ref > 1e-200
+    assert max_rel(post[big], ref[big]) <= 1e-10
+    assert np.max(np.abs(post - ref)) <= 1e-14
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_fp32_close_to_fp64(name):
+    prob, _ = load(name)
+    r32, r64 = (api.run_batch([prob], precision=p, want_posterior=True)[0]
+                for p in ("fp32", "fp64"))
+    assert np.max(np.abs(r32.posterior - r64.posterior)) <= 1e-5
+    assert abs(r32.loglik - r64.loglik) <= 1e-5 * abs(r64.loglik)
+
+
+@pytest.mark.parametrize("name", EXTERNAL_DEFAULT_MAP)
+def test_c_abi_forward_alg(name):
+    prob, gold = load(name)
+    rows = refapi.arghmm_forward_alg(prob)
+    fw_o, _ = pyoracle.forward(prob)
+    assert max_rel(np.concatenate(rows), fw_o) <= 1e-12
+    np.testing.assert_array_equal([len(r) for r in rows], np.maximum(gold["nstates"], 1))
+
+
+def test_c_abi_forward_alg_given_prior():
+    prob, gold = load("dsmc_k8_s11")
+    S0 = int(gold["nstates"][0])
+    prior = np.random.default_rng(3).random(S0)
+    rows = refapi.arghmm_forward_alg(prob, prior=prior)
+    np.testing.assert_array_equal(rows[0], prior)
+
+
+@pytest.mark.parametrize("name", EXTERNAL_DEFAULT_MAP)
+def test_c_abi_sample_posterior_with_srand(name):
+    prob, gold = load(name)
+    refapi.srand(int(gold["seed"]))
+    path = refapi.arghmm_sample_posterior(prob)
+    # expected (node, time) from the reference's state index path, column by column
+    exp = np.zeros((prob.seqlen, 2), dtype=np.int64)
+    pos = 0
+    for b in range(prob.ntrees):
+        par, age = prob.ptrees[b], prob.ages[b]
+        states = []
+        for v in range(prob.nnodes):
+            top = prob.ntimes - 2 if par[v] == -1 else age[par[v]]
+            states += [(v, t) for t in range(age[v], top + 1)]
+        for i in range(pos, pos + prob.blocklens[b]):
+            exp[i] = states[gold["path"][i]]
+        pos += prob.blocklens[b]
+    np.testing.assert_array_equal(path, exp)
+
+
+@pytest.mark.parametrize("name", EXTERNAL_DEFAULT_MAP[:3])
+def test_c_abi_backward_and_posterior(name):
+    prob, _ = load(name)
+    bw = np.concatenate(refapi.arghmm_backward_alg(prob))
+    bw_o = pyoracle.backward(prob)
+    assert max_rel(bw, bw_o) <= 1e-10
+    post = np.concatenate(refapi.arghmm_posterior_marginals(prob))
+    fw_o, _ = pyoracle.forward(prob)
+    ref = pyoracle.posterior(prob, fw_o, bw_o)
+    assert np.max(np.abs(post - ref)) <= 1e-14
+
+
+def test_internal_c_abi_sample_thread():
+    # leaf cut: a single-leaf subtree (index order of the virtual root's children holds)
+    full = simulate(8, 1200, 77, add_thread=False)
+    prob = _leaf_cut(full)
+    refapi.srand(5)
+    path = refapi.arghmm_sample_arg_thread_internal(prob)
+    fw, _ = pyoracle.forward(prob)
+    u = pyoracle.rand_uniforms(5, prob.seqlen)
+    np.testing.assert_array_equal(path, pyoracle.traceback(prob, fw, u))
+
+
+def _leaf_cut(full: Problem) -> Problem:
+    """Cut leaf 0's branch in every tree: its parent becomes the virtual root (age
+    ntimes+1) with children (leaf 0, rest of the tree), as remove_arg_thread_path leaves
+    a leaf removal (thread.cpp:1481). Only trees whose SPRs avoid leaf 0 and its parent are
+    kept, so the SPRs stay valid."""
+    T = full.ntimes
+    keep = []
+    for b in range(full.ntrees):
+        if b > 0:
+            rn, cn = full.sprs[b, 0], full.sprs[b, 2]
+            p0 = full.ptrees[b - 1, 0]
+            if rn in (0, p0) or cn in (0, p0) or full.ptrees[b - 1, rn] == p0:
+                break
+        keep.append(b)
+    B = len(keep)
+    ptrees = full.ptrees[:B].copy()
+    ages = full.ages[:B].copy()
+    for b in range(B):
+        par = ptrees[b]
+        p = par[0]
+        sib = [v for v in range(full.nnodes) if par[v] == p and v != 0][0]
+        gp = par[p]
+        par[sib] = gp
+        if gp == -1:
+            main = sib
+        else:
+            main = int(np.nonzero(par == -1)[0][0])
+        par[p] = -1
+        par[main] = p
+        ages[b, p] = T + 1
+    L = int(full.blocklens[:B].sum())
+    sprs = full.sprs[:B].copy()
+    return Problem(times=full.times, popsizes=full.popsizes, rho=full.rho, mu=full.mu,
+                   ptrees=ptrees, ages=ages, sprs=sprs, blocklens=full.blocklens[:B].copy(),
+                   seqs=full.seqs[:, :L].copy(), internal=True)
+
+
+def test_batch_matches_single_runs():
+    probs = [load(n)[0] for n in NAMES]
+    batch = api.run_batch(probs, want_posterior=True)
+    for p, rb in zip(probs, batch):
+        r1 = api.run_batch([p], want_posterior=True)[0]
+        np.testing.assert_array_equal(rb.forward, r1.forward)
+        np.testing.assert_array_equal(rb.posterior, r1.posterior)
+        assert rb.loglik == r1.loglik
+
+
+def test_edge_cases_single_column_blocks_and_tiny_problems():
+    # every block one column long; a one-column problem
+    prob = simulate(5, 300, 9)
+    bl = np.ones(prob.ntrees, dtype=np.int32)
+    tiny = Problem(times=prob.times, popsizes=prob.popsizes, rho=prob.rho, mu=prob.mu,
+                   ptrees=prob.ptrees, ages=prob.ages, sprs=prob.sprs, blocklens=bl,
+                   seqs=prob.seqs[:, :prob.ntrees].copy())
+    one = Problem(times=prob.times, popsizes=prob.popsizes, rho=prob.rho, mu=prob.mu,
+                  ptrees=prob.ptrees[:1], ages=prob.ages[:1], sprs=prob.sprs[:1],
+                  blocklens=np.array([1], np.int32), seqs=prob.seqs[:, :1].copy())
+    for p in (tiny, one):
+        r = api.run_batch([p], want_path=True, want_posterior=True,
+                          uniforms=[np.full(p.seqlen, 0.5)])[0]
+        fw_o, _ = pyoracle.forward(p)
+        assert max_rel(r.forward, fw_o) <= 1e-12
+        np.testing.assert_array_equal(r.path, pyoracle.traceback(p, fw_o, np.full(p.seqlen, 0.5)))
+
+
+def test_all_missing_column_data_is_prior():
+    # every call 'N': emissions are 1, the posterior is the prior chain's marginal
+    prob = simulate(6, 500, 12)
+    prob.seqs[:] = ord("N")
+    r = api.run_batch([prob], want_posterior=True)[0]
+    fw_o, lnl_o = pyoracle.forward(prob)
+    assert max_rel(r.forward, fw_o) <= 1e-12
+    assert abs(r.loglik - lnl_o) <= 1e-9

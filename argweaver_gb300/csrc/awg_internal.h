@@ -70,7 +70,7 @@ struct StateInfo {
 
 // Device views of a batch (all pointers are device memory).
 struct BatchDev {
-    int ninst, nblocks, maxS, maxT, maxnodes;
+    int ninst, nblocks, maxS, maxT, maxnodes, maxM;
     const InstDev *inst;
     BlockDev *blocks;
     const double *model;         // [ninst * MODEL_STRIDE]
@@ -96,8 +96,14 @@ struct BatchDev {
     int *gidx;                   // [total states] gather sources (prev-tree state indices)
     double *varemit;             // [total variant cells] emissions of variant columns
 
-    // FP32 copies of the per-column hot tables (FP32 path only)
-    float *tm32, *t2d32, *inv32, *var32, *determprob32, *recombrow32, *recoalrow32;
+    // FP32 tables of the chosen path. Quantities next to 1 are stored as their complements,
+    // computed with expm1 in FP64, so FP32 keeps their information:
+    //   t2d32    tmatrix2 without the no-recombination term of the diagonal
+    //   rstay32  [nblocks * MAXT] 1 - norecombs[b]
+    //   inv32    1 - e_k / e_ref for invariant sites, e_ref the block's largest emission
+    //   lneref   [nblocks] log(e_ref), added to the log-likelihood per invariant column
+    float *tm32, *t2d32, *inv32, *var32, *determprob32, *recombrow32, *recoalrow32, *rstay32;
+    double *lneref;
 
     // outputs
     double *fw64;                // forward table (FP64 path)

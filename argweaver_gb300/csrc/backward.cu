@@ -21,6 +21,8 @@ namespace {
 
 template <typename F> struct BTab;
 template <> struct BTab<double> {
+    static constexpr bool split = false;
+    const float *rstay = nullptr;
     const double *tm, *inv, *var, *dprob, *rrow, *crow, *gts, *fw;
     __device__ explicit BTab(const BatchDev &d)
         : tm(d.tm), inv(d.inv_lk), var(d.varemit), dprob(d.determprob), rrow(d.recombrow),
@@ -30,10 +32,13 @@ template <> struct BTab<double> {
     }
 };
 template <> struct BTab<float> {
+    // complements of the stay probability and of the invariant emissions, as in the forward
+    static constexpr bool split = true;
+    const float *rstay;
     const float *tm, *inv, *var, *dprob, *rrow, *crow, *t2d, *fw;
     __device__ explicit BTab(const BatchDev &d)
-        : tm(d.tm32), inv(d.inv32), var(d.var32), dprob(d.determprob32), rrow(d.recombrow32),
-          crow(d.recoalrow32), t2d(d.t2d32), fw(d.fw32) {}
+        : rstay(d.rstay32), tm(d.tm32), inv(d.inv32), var(d.var32), dprob(d.determprob32),
+          rrow(d.recombrow32), crow(d.recoalrow32), t2d(d.t2d32), fw(d.fw32) {}
     __device__ float t2(long long t2_0, int off, int y, float) const { return t2d[t2_0 + off + y]; }
 };
 
@@ -76,7 +81,7 @@ __global__ void k_backward(BatchDev d, int maxS, double *bw_out) {
     Meta *meta = (Meta *)(g + maxS + (maxS & 1));
     int *perm = (int *)(meta + maxS);
     __shared__ F tm[MAXT * MAXT];
-    __shared__ F G[MAXT], H[MAXT], red[32];
+    __shared__ F G[MAXT], H[MAXT], red[32], rS[MAXT];
     __shared__ int bptr[MAXT + 1];
 
     F *cur = bwA, *nxt = bwB;  // cur: bw of column i+1, nxt: bw of column i
@@ -99,6 +104,9 @@ __global__ void k_backward(BatchDev d, int maxS, double *bw_out) {
         for (int e = tid; e < (T - 1) * MAXT; e += blockDim.x) tm[e] = tmg[e];
         for (int a = tid; a <= MAXT; a += blockDim.x)
             bptr[a] = d.bt_ptr[(size_t)(I.block0 + bi) * (MAXT + 1) + a];
+        if (BTab<F>::split)
+            for (int a = tid; a < MAXT; a += blockDim.x)
+                rS[a] = tab.rstay[(size_t)(I.block0 + bi) * MAXT + a];
         const uint8_t *cls = d.colclass + I.col0 + B.start;
         const int *cvar = d.colvar + I.col0 + B.start;
         const F *inv = tab.inv + B.state0;
@@ -106,11 +114,12 @@ __global__ void k_backward(BatchDev d, int maxS, double *bw_out) {
         const F *fw = tab.fw + B.cell0;
         __syncthreads();
 
-        auto emit = [&](int i, int k) -> F {
+        // emission times a backward value (the common factor e_ref dropped in FP32)
+        auto emitx = [&](int i, int k, F x) -> F {
             const uint8_t c = cls[i];
-            if (c == COL_MASKED || S == 0) return F(1);
-            if (c == COL_INVARIANT) return inv[k];
-            return var[(size_t)cvar[i] * S + k];
+            if (c == COL_MASKED || S == 0) return x;
+            if (c == COL_INVARIANT) return BTab<F>::split ? x - x * inv[k] : x * inv[k];
+            return x * var[(size_t)cvar[i] * S + k];
         };
         // posterior of one column from its bw (in `bw`) and fw
         auto posterior = [&](int i, const F *bw) {
@@ -127,7 +136,7 @@ __global__ void k_backward(BatchDev d, int maxS, double *bw_out) {
 
         posterior(B.len - 1, cur);
         for (int i = B.len - 2; i >= 0; i--) {
-            for (int k = tid; k < Sm; k += blockDim.x) g[k] = emit(i + 1, k) * cur[k];
+            for (int k = tid; k < Sm; k += blockDim.x) g[k] = emitx(i + 1, k, cur[k]);
             __syncthreads();
             if (S == 0) {
                 if (tid == 0) nxt[0] = g[0];
@@ -155,6 +164,7 @@ __global__ void k_backward(BatchDev d, int maxS, double *bw_out) {
                         const int k = mj.j1 + x;  // target on the same node, time a0 + x
                         s += tab.t2(B.t2_0, meta[k].off, y, tm[a * MAXT + a0 + x]) * g[k];
                     }
+                    if (BTab<F>::split) s = g[j] + (s - rS[a] * g[j]);  // stay term apart
                     nxt[j] = s;
                 }
             }
@@ -170,7 +180,7 @@ __global__ void k_backward(BatchDev d, int maxS, double *bw_out) {
             // into the previous tree's last column through the switch matrix
             const BlockDev &P = d.blocks[I.block0 + bi - 1];
             const int n1 = imax(B.S1, 1);
-            for (int k = tid; k < Sm; k += blockDim.x) g[k] = emit(0, k) * cur[k];
+            for (int k = tid; k < Sm; k += blockDim.x) g[k] = emitx(0, k, cur[k]);
             __syncthreads();
             const int2 src = d.srcs[I.block0 + bi];
             const int *determ = d.determ + B.prev_state0;
@@ -210,8 +220,8 @@ void launch(const BatchDev &d, double *bw_out, cudaStream_t s) {
     const int maxS = imax(d.maxS, 1);
     const size_t smem = 3 * (size_t)maxS * sizeof(F) + 8 + (size_t)maxS * (sizeof(Meta) + sizeof(int));
     static size_t configured = 0;
-    if (smem > 48 * 1024 && smem > configured) {
-        cudaFuncSetAttribute(k_backward<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (smem > configured) {  // opt in; static shared memory counts against 48 KB too
+        if (cudaFuncSetAttribute(k_backward<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return;
         configured = smem;
     }
     k_backward<F><<<d.ninst, backward_threads(maxS), smem, s>>>(d, maxS, bw_out);

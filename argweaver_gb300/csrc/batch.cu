@@ -58,6 +58,18 @@ Engine &engine() {
         }                                                                             \
     } while (0)
 
+#define CKL(what)                                                                     \
+    do {                                                                              \
+        cudaError_t rc_ = cudaGetLastError();                                         \
+        if (rc_ != cudaSuccess) {                                                     \
+            char b_[256];                                                             \
+            snprintf(b_, sizeof(b_), "%s launch (maxS %d, maxM %d, nodes %d): %s", what, \
+                     plan.maxS, plan.maxM, plan.maxnodes, cudaGetErrorString(rc_));   \
+            err = b_;                                                                 \
+            return -3;                                                                \
+        }                                                                             \
+    } while (0)
+
 struct Layout {
     size_t total = 0;
     size_t add(size_t bytes) {
@@ -137,7 +149,7 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
     const size_t o_gidx = w.add(sizeof(int) * ST);
     const size_t o_var = w.add(sizeof(double) * std::max(plan.total_var, 1LL));
     size_t o_tm32 = 0, o_t2d32 = 0, o_inv32 = 0, o_var32 = 0, o_detp32 = 0, o_rrow32 = 0,
-           o_crow32 = 0;
+           o_crow32 = 0, o_rstay32 = 0, o_lneref = 0;
     if (fp32) {
         o_tm32 = w.add(sizeof(float) * (size_t)plan.nblocks * MAXT * MAXT);
         o_t2d32 = w.add(sizeof(float) * std::max(plan.total_M, 1LL));
@@ -146,6 +158,8 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
         o_detp32 = w.add(sizeof(float) * ST);
         o_rrow32 = w.add(sizeof(float) * ST);
         o_crow32 = w.add(sizeof(float) * ST);
+        o_rstay32 = w.add(sizeof(float) * (size_t)plan.nblocks * MAXT);
+        o_lneref = w.add(sizeof(double) * plan.nblocks);
     }
     const size_t o_fw = w.add((fp32 ? sizeof(float) : sizeof(double)) * CELLS);
     const size_t o_lnl = w.add(sizeof(double) * plan.ninst);
@@ -200,6 +214,7 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
     char *D = E.dev;
     d.ninst = plan.ninst; d.nblocks = plan.nblocks; d.maxS = plan.maxS; d.maxT = plan.maxT;
     d.maxnodes = plan.maxnodes;
+    d.maxM = plan.maxM;
     d.inst = (const InstDev *)(D + o_inst);
     d.blocks = (BlockDev *)(D + o_blocks);
     d.model = (const double *)(D + o_model);
@@ -231,6 +246,8 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
         d.determprob32 = (float *)(D + o_detp32);
         d.recombrow32 = (float *)(D + o_rrow32);
         d.recoalrow32 = (float *)(D + o_crow32);
+        d.rstay32 = (float *)(D + o_rstay32);
+        d.lneref = (double *)(D + o_lneref);
         d.fw32 = (float *)(D + o_fw);
     } else {
         d.fw64 = (double *)(D + o_fw);
@@ -247,7 +264,7 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
     CK(cudaMemsetAsync(d.err, 0, 4 * sizeof(int), s));
     if (T) CK(cudaEventRecord(E.ev[1], s));
     launch_tables(d, fp32, s);
-    CK(cudaGetLastError());
+    CKL("table kernel");
     if (opt.priors) {
         for (int q = 0; q < n; q++) {
             if (!opt.priors[q]) continue;
@@ -298,19 +315,19 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
     }
     if (T) CK(cudaEventRecord(E.ev[2], s));
     launch_varemit(d, fp32, s);
-    CK(cudaGetLastError());
+    CKL("emission kernel");
     if (T) CK(cudaEventRecord(E.ev[3], s));
     launch_forward(d, fp32, s);
-    CK(cudaGetLastError());
+    CKL("forward kernel");
     if (T) CK(cudaEventRecord(E.ev[4], s));
     if (want_path) {
         launch_traceback(d, fp32, s);
-        CK(cudaGetLastError());
+        CKL("traceback kernel");
     }
     if (T) CK(cudaEventRecord(E.ev[5], s));
     if (want_post) {
         launch_backward(d, fp32, want_bw ? (double *)(D + o_bw) : nullptr, s);
-        CK(cudaGetLastError());
+        CKL("backward kernel");
     }
     if (T) CK(cudaEventRecord(E.ev[6], s));
 

@@ -7,12 +7,26 @@
 //   col2      /= sum(col2)
 // At a local-tree boundary the first column comes from the switch matrix
 // (arghmm_forward_switch, sample_thread.cpp:345-389), gathered per target state.
-// All reductions use a fixed order (per-warp shuffle trees combined in warp order), so a
-// result is the same in every run and in every batch composition.
 //
-// FP64 (plain path): tmatrix2 is formed as gts - tmatrix, the reference's own subtraction.
-// FP32 (chosen path): tables were rounded to FP32 by the table kernels; the column is
-// rescaled every column as above and log(norm) is accumulated in FP64.
+// Schedule: one CTA barrier per column. Column values stay unnormalised in shared memory;
+// after the barrier every warp sums the time bins of the previous column (a fixed order per
+// bin), which also gives that column's norm, forms tf with shuffles, and then each thread
+//   - writes its entries of the previous column, now divided by that norm, to HBM, and
+//   - computes its entries of the new column, scaled by 1/norm (the reference's
+//     normalise-then-step, reordered; the normalised values are the same).
+// Reductions have a fixed order, so results do not depend on the run or the batch.
+// log(norm) goes into an FP64 mantissa product plus an integer exponent (one FP64 log
+// every 64 columns instead of one per column).
+//
+// FP64 (plain path): tmatrix2 = gts - tmatrix, the reference's own subtraction, formed when
+// the block's rows are staged. FP32 (chosen path): tables rounded to FP32 by the table
+// kernels; columns rescaled every column; the log-likelihood accumulates in FP64. Values
+// next to 1 keep their information as complements (built with expm1 in FP64):
+//   stay:     x_k * norecombs[b]   ->  x_k - rstay[b] * x_k
+//   emission: x_k * e_k            ->  (x_k - inv32[k] * x_k) * e_ref, e_ref into the FP64
+//                                      log-likelihood once per invariant column
+// so the moving probability mass and the emission contrasts, not their rounding, drive
+// the chain over thousands of columns.
 
 #include <cuda_runtime.h>
 
@@ -25,24 +39,28 @@ namespace {
 template <typename F> struct Tab;
 
 template <> struct Tab<double> {
+    static constexpr bool split = false;
     const double *tm, *inv, *var, *dprob, *rrow, *crow, *gts;
+    const float *rstay = nullptr;
+    const double *lneref = nullptr;
     double *fw;
     __device__ explicit Tab(const BatchDev &d)
         : tm(d.tm), inv(d.inv_lk), var(d.varemit), dprob(d.determprob), rrow(d.recombrow),
           crow(d.recoalrow), gts(d.gts), fw(d.fw64) {}
     // tmatrix2[a][k] (sample_thread.cpp:223-224)
-    __device__ double t2(long long t2_0, int off, int y, double tmab) const {
-        return gts[t2_0 + off + y] - tmab;
-    }
+    __device__ double t2(long long idx, double tmab) const { return gts[idx] - tmab; }
 };
 
 template <> struct Tab<float> {
+    static constexpr bool split = true;
     const float *tm, *inv, *var, *dprob, *rrow, *crow, *t2d;
+    const float *rstay;
+    const double *lneref;
     float *fw;
     __device__ explicit Tab(const BatchDev &d)
         : tm(d.tm32), inv(d.inv32), var(d.var32), dprob(d.determprob32), rrow(d.recombrow32),
-          crow(d.recoalrow32), t2d(d.t2d32), fw(d.fw32) {}
-    __device__ float t2(long long t2_0, int off, int y, float) const { return t2d[t2_0 + off + y]; }
+          crow(d.recoalrow32), t2d(d.t2d32), rstay(d.rstay32), lneref(d.lneref), fw(d.fw32) {}
+    __device__ float t2(long long idx, float) const { return t2d[idx]; }
 };
 
 template <typename F>
@@ -52,189 +70,291 @@ __device__ __forceinline__ F warp_sum(F v) {
     return v;
 }
 
-struct Meta {  // per-state metadata in shared memory
+// Running sum of log(norm): mantissa product in FP64 and binary exponent in an integer.
+struct LogAcc {
+    double prod = 1.0;
+    long long e = 0;
+    int n = 0;
+    double lnl = 0.0;
+    double extra = 0.0;  // log(e_ref) of invariant columns (FP32 path)
+    __device__ void add(double norm) {
+        int ex;
+        prod *= frexp(norm, &ex);
+        e += ex;
+        if (++n == 64) flush();
+    }
+    __device__ void flush() {
+        lnl += extra;
+        extra = 0.0;
+        if (n) {
+            lnl += log(prod) + (double)e * 0.69314718055994530942;
+            prod = 1.0;
+            e = 0;
+            n = 0;
+        }
+    }
+};
+
+struct Meta {
     int time, j1, m, off;
 };
 
 template <typename F>
-__global__ void k_forward(BatchDev d, int maxS) {
+__global__ void __launch_bounds__(512) k_forward(BatchDev d, int maxS, int maxM, int t2_in_smem) {
     extern __shared__ double dyn_d[];
     const Tab<F> tab(d);
     const InstDev I = d.inst[blockIdx.x];
     const int T = I.T;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int nwarps = blockDim.x >> 5;
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int NT = blockDim.x;
 
-    F *colA = (F *)dyn_d;
-    F *colB = colA + maxS;
-    Meta *meta = (Meta *)(colB + maxS + (maxS & 1));
-    int *perm = (int *)(meta + maxS);
-    __shared__ F tm[MAXT * MAXT];
-    __shared__ F fg[MAXT], tf[MAXT], red[32];
+    F *col = (F *)dyn_d;                       // [2][maxS]
+    F *t2s = col + 2 * maxS;                   // [maxM] tmatrix2 rows of the block
+    Meta *meta = (Meta *)(t2s + maxM + ((2 * maxS + maxM) & 1));
+    int *perm = (int *)(meta + maxS);          // states grouped by time
+    F *invS = (F *)(perm + maxS + (maxS & 1)); // invariant-site emission per state
+    __shared__ F tmS[MAXT * MAXT];
+    __shared__ F rS[MAXT];
     __shared__ int bptr[MAXT + 1];
 
-    F *cur = colA, *nxt = colB;
-    double lnl = 0.0;
-    int prevS = 0;
+    F tmcol[MAXT - 1];                         // lane b: tmatrix[a][b] for every a
+    LogAcc acc;
+    int c = 0;                                 // buffer holding the current column
 
     for (int bi = 0; bi < I.ntrees; bi++) {
-        const BlockDev &B = d.blocks[I.block0 + bi];
+        const int blk = I.block0 + bi;
+        const BlockDev &B = d.blocks[blk];
         const int S = B.S, Sm = imax(S, 1);
-        const bool empty = (S == 0);  // fully specified internal tree: one state of prob 1
-        // block tables
-        for (int k = tid; k < S; k += blockDim.x) {
+        F *fw = tab.fw + B.cell0;
+
+        if (S == 0) {
+            // fully specified tree: one state that carries over (sample_thread.cpp:201-206)
+            F v;
+            if (bi == 0) {
+                v = fw[0];
+                if (tid == 0) col[c * maxS] = v;
+            } else {
+                // switch into the single state: every source maps to it
+                const int2 src = d.srcs[blk];
+                const int *gp = d.gptr + B.gptr0;
+                const int *gi = d.gidx + B.prev_state0;
+                const F *dp = tab.dprob + B.prev_state0;
+                const F *rr = tab.rrow + B.state0;
+                const F *cr = tab.crow + B.state0;
+                F part = 0;
+                if (tid < 32) {
+                    for (int p = gp[0] + lane; p < gp[1]; p += 32) part += col[c * maxS + gi[p]] * dp[gi[p]];
+                    part = warp_sum(part);
+                }
+                if (tid == 0) {
+                    if (src.x != -1 && rr[0] > F(0)) part += col[c * maxS + src.x] * rr[0];
+                    if (src.y != -1 && cr[0] > F(0)) part += col[c * maxS + src.y] * cr[0];
+                    acc.add((double)part);
+                    col[c * maxS] = F(1);
+                    fw[0] = F(1);
+                }
+                v = F(1);
+            }
+            for (int i = 1 + tid; i < B.len; i += NT) fw[i] = v;
+            __syncthreads();
+            continue;
+        }
+
+        // ---- stage the block's tables
+        for (int k = tid; k < S; k += NT) {
             const StateInfo si = d.sinfo[B.state0 + k];
             meta[k] = Meta{si.time, si.j1, si.m, d.t2off[B.state0 + k]};
             perm[k] = d.bt_perm[B.state0 + k];
+            invS[k] = tab.inv[B.state0 + k];
         }
-        const F *tmg = tab.tm + (size_t)(I.block0 + bi) * MAXT * MAXT;
-        for (int e = tid; e < (T - 1) * MAXT; e += blockDim.x) tm[e] = tmg[e];
-        for (int a = tid; a <= MAXT; a += blockDim.x)
-            bptr[a] = d.bt_ptr[(size_t)(I.block0 + bi) * (MAXT + 1) + a];
+        const F *tmg = tab.tm + (size_t)blk * MAXT * MAXT;
+        for (int e = tid; e < (T - 1) * MAXT; e += NT) tmS[e] = tmg[e];
+        for (int a = tid; a <= MAXT; a += NT) bptr[a] = d.bt_ptr[(size_t)blk * (MAXT + 1) + a];
+        if (Tab<F>::split)
+            for (int a = tid; a < MAXT; a += NT) rS[a] = tab.rstay[(size_t)blk * MAXT + a];
+        __syncthreads();
+        if (t2_in_smem)
+            for (int k = tid; k < S; k += NT) {  // same-branch rows, one per state
+                const Meta mk = meta[k];
+                const int a0 = mk.time - (k - mk.j1);
+                for (int y = 0; y < mk.m; y++)
+                    t2s[mk.off + y] = tab.t2(B.t2_0 + mk.off + y, tmS[(a0 + y) * MAXT + mk.time]);
+            }
+        const double lner = Tab<F>::split ? tab.lneref[blk] : 0.0;
+#pragma unroll
+        for (int a = 0; a < MAXT - 1; a++)
+            tmcol[a] = (a < T - 1 && lane < T - 1) ? tmS[a * MAXT + lane] : F(0);
         const uint8_t *cls = d.colclass + I.col0 + B.start;
         const int *cvar = d.colvar + I.col0 + B.start;
-        const F *inv = tab.inv + B.state0;
+        const F *inv = invS;
         const F *var = tab.var + B.var0;
-        F *fw = tab.fw + B.cell0;
-        __syncthreads();
-
-        auto emit = [&](int i, int k) -> F {
-            const uint8_t c = cls[i];
-            if (c == COL_MASKED) return F(1);
-            if (c == COL_INVARIANT) return inv[k];
-            return var[(size_t)cvar[i] * S + k];
+        // column classes and variant rows, 32 columns per load, read back by shuffles
+        int ccache = 0, vcache = 0, cbase = -32;
+        auto colinfo = [&](int i, uint8_t &ci, int &vi) {
+            if (i - cbase >= 32) {
+                cbase = i;
+                const int q = i + lane;
+                ccache = q < B.len ? cls[q] : 0;
+                vcache = q < B.len ? cvar[q] : 0;
+            }
+            ci = (uint8_t)__shfl_sync(0xffffffffu, ccache, i - cbase);
+            vi = __shfl_sync(0xffffffffu, vcache, i - cbase);
         };
 
-        // first column of the block
+        // ---- first column of the block
         if (bi == 0) {
-            for (int k = tid; k < Sm; k += blockDim.x) cur[k] = fw[k];  // priors (K1)
-            __syncthreads();  // the first step reads every thread's entries
+            for (int k = tid; k < S; k += NT) col[c * maxS + k] = fw[k];  // priors (K1)
         } else {
-            const int2 src = d.srcs[I.block0 + bi];
+            // previous column is normalised in col[c] (S1 entries)
+            const int2 src = d.srcs[blk];
             const int *gp = d.gptr + B.gptr0;
             const int *gi = d.gidx + B.prev_state0;
             const F *dp = tab.dprob + B.prev_state0;
             const F *rr = tab.rrow + B.state0;
             const F *cr = tab.crow + B.state0;
-            F part = 0;
-            for (int k = tid; k < Sm; k += blockDim.x) {
+            uint8_t c0;
+            int v0;
+            colinfo(0, c0, v0);
+            const F *prev = col + c * maxS;
+            for (int k = tid; k < S; k += NT) {
                 F s = 0;
                 for (int p = gp[k]; p < gp[k + 1]; p++) {
                     const int j = gi[p];
-                    s += cur[j] * dp[j];
+                    s += prev[j] * dp[j];
                 }
-                if (src.x != -1 && rr[k] > F(0)) s += cur[src.x] * rr[k];
-                if (src.y != -1 && cr[k] > F(0)) s += cur[src.y] * cr[k];
-                s *= empty ? F(1) : emit(0, k);
-                nxt[k] = s;
-                part += s;
+                if (src.x != -1 && rr[k] > F(0)) s += prev[src.x] * rr[k];
+                if (src.y != -1 && cr[k] > F(0)) s += prev[src.y] * cr[k];
+                F v;
+                if (c0 == COL_MASKED) v = s;
+                else if (c0 == COL_INVARIANT) v = Tab<F>::split ? s - s * inv[k] : s * inv[k];
+                else v = s * var[(size_t)v0 * S + k];
+                col[(c ^ 1) * maxS + k] = v;
             }
-            part = warp_sum(part);
-            if (lane == 0) red[warp] = part;
-            __syncthreads();
-            F norm = 0;
-            for (int w = 0; w < nwarps; w++) norm += red[w];
-            for (int k = tid; k < Sm; k += blockDim.x) {
-                const F v = nxt[k] / norm;
-                nxt[k] = v;
-                fw[k] = v;
-            }
-            if (tid == 0) {
-                lnl += log((double)norm);
-                if (!(norm > F(0))) report_error(d.err, ERR_ZERO_NORM, blockIdx.x, bi, B.start);
-            }
-            F *t = cur; cur = nxt; nxt = t;
-            __syncthreads();
-        }
-        (void)prevS;
-        prevS = S;
-
-        if (empty) {
-            // fully specified tree: the single state carries over (sample_thread.cpp:201-206)
-            for (int i = 1; i < B.len; i++)
-                if (tid == 0) fw[(size_t)i] = cur[0];
-            __syncthreads();
-            continue;
+            if (Tab<F>::split && tid == 0 && c0 == COL_INVARIANT) acc.extra += lner;
+            c ^= 1;
         }
 
-        for (int i = 1; i < B.len; i++) {
-            // fgroups
-            for (int a = warp; a < T - 1; a += nwarps) {
-                F s = 0;
-                for (int p = bptr[a] + lane; p < bptr[a + 1]; p += 32) s += cur[perm[p]];
-                s = warp_sum(s);
-                if (lane == 0) fg[a] = s;
-            }
+        // ---- remaining columns; iteration i also finalises column i-1
+        for (int i = 1; i <= B.len; i++) {
             __syncthreads();
-            if (warp == 0 && lane < T - 1) {
-                F s = 0;
-                for (int a = 0; a < T - 1; a++) s += tm[a * MAXT + lane] * fg[a];
-                tf[lane] = s;
+            const F *cur = col + c * maxS;
+            // time bins of column i-1 (lane a), its norm, tf (lane b)
+            F fg = 0;
+            if (lane < T - 1) {
+                F s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+                int p = bptr[lane];
+                const int pe = bptr[lane + 1];
+                for (; p + 3 < pe; p += 4) {
+                    s0 += cur[perm[p]]; s1 += cur[perm[p + 1]];
+                    s2 += cur[perm[p + 2]]; s3 += cur[perm[p + 3]];
+                }
+                for (; p < pe; p++) s0 += cur[perm[p]];
+                fg = (s0 + s1) + (s2 + s3);
             }
-            __syncthreads();
-            F part = 0;
-            for (int k = tid; k < S; k += blockDim.x) {
-                const Meta mk = meta[k];
-                const int a0 = mk.time - (k - mk.j1);
-                F s = tf[mk.time];
-                for (int y = 0; y < mk.m; y++)
-                    s += tab.t2(B.t2_0, mk.off, y, tm[(a0 + y) * MAXT + mk.time]) * cur[mk.j1 + y];
-                s *= emit(i, k);
-                nxt[k] = s;
-                part += s;
-            }
-            part = warp_sum(part);
-            if (lane == 0) red[warp] = part;
-            __syncthreads();
-            F norm = 0;
-            for (int w = 0; w < nwarps; w++) norm += red[w];
-            F *out = fw + (size_t)i * S;
-            for (int k = tid; k < S; k += blockDim.x) {
-                const F v = nxt[k] / norm;
-                nxt[k] = v;
-                out[k] = v;
+            const F norm = warp_sum(fg);
+            const F inv_norm = F(1) / norm;
+            F tf = 0;
+#pragma unroll
+            for (int a = 0; a < MAXT - 1; a++) {
+                const F f = __shfl_sync(0xffffffffu, fg, a);
+                tf += tmcol[a] * f;
             }
             if (tid == 0) {
-                lnl += log((double)norm);
-                if (!(norm > F(0)))
-                    report_error(d.err, ERR_ZERO_NORM, blockIdx.x, bi, B.start + i);
+                acc.add((double)norm);
+                if (!(norm > F(0))) report_error(d.err, ERR_ZERO_NORM, blockIdx.x, bi, B.start + i - 1);
             }
-            F *t = cur; cur = nxt; nxt = t;
-            __syncthreads();
+            // finalise column i-1: normalised into the table (the instance's column 0
+            // keeps the unnormalised prior, as the reference's table does)
+            const bool write_prev = !(bi == 0 && i == 1);
+            F *outp = fw + (size_t)(i - 1) * S;
+            if (i == B.len) {
+                for (int k = tid; k < S; k += NT) {
+                    const F v = cur[k] * inv_norm;
+                    if (write_prev) outp[k] = v;
+                    col[c * maxS + k] = v;  // normalised, for the next switch
+                }
+                break;
+            }
+            uint8_t ci;
+            int vrow;
+            colinfo(i, ci, vrow);
+            F *nxt = col + (c ^ 1) * maxS;
+            if (Tab<F>::split && tid == 0 && ci == COL_INVARIANT) acc.extra += lner;
+            for (int k0 = 0; k0 < S; k0 += NT) {
+                const int k = k0 + tid;
+                const bool valid = k < S;
+                const Meta mk = meta[valid ? k : 0];
+                const F tfb = __shfl_sync(0xffffffffu, tf, mk.time);
+                if (valid) {
+                    const F xk = cur[k];
+                    if (write_prev) outp[k] = xk * inv_norm;
+                    const F *nb = cur + mk.j1;
+                    F s = tfb;
+                    if (t2_in_smem) {
+                        const F *row = t2s + mk.off;
+                        for (int y = 0; y < mk.m; y++) s += row[y] * nb[y];
+                    } else {
+                        const int a0 = mk.time - (k - mk.j1);
+                        for (int y = 0; y < mk.m; y++)
+                            s += tab.t2(B.t2_0 + mk.off + y, tmS[(a0 + y) * MAXT + mk.time]) * nb[y];
+                    }
+                    F v;
+                    if (Tab<F>::split) {
+                        s = xk + (s - rS[mk.time] * xk);  // stay term apart
+                        if (ci == COL_MASKED) v = s;
+                        else if (ci == COL_INVARIANT) v = s - s * inv[k];
+                        else v = s * var[(size_t)vrow * S + k];
+                    } else {
+                        const F e = ci == COL_MASKED ? F(1)
+                                  : ci == COL_INVARIANT ? inv[k] : var[(size_t)vrow * S + k];
+                        v = s * e;
+                    }
+                    nxt[k] = v * inv_norm;
+                }
+            }
+            c ^= 1;
         }
+        __syncthreads();
     }
-    if (tid == 0 && d.lnl) d.lnl[blockIdx.x] = lnl;
+    if (tid == 0 && d.lnl) {
+        acc.flush();
+        d.lnl[blockIdx.x] = acc.lnl;
+    }
 }
 
 int forward_threads(int maxS) {
-    if (maxS > 768) return 512;
+    if (maxS > 1024) return 512;
     if (maxS > 256) return 256;
     return 128;
 }
 
 template <typename F>
-size_t forward_smem(int maxS) {
-    return 2 * (size_t)maxS * sizeof(F) + 8 + (size_t)maxS * (sizeof(Meta) + sizeof(int));
+size_t forward_smem(int maxS, int maxM) {
+    return (size_t)(3 * maxS + maxM + 2) * sizeof(F) + (size_t)maxS * (sizeof(Meta) + sizeof(int)) + 16;
 }
 
 template <typename F>
-void launch(const BatchDev &d, cudaStream_t s) {
+void launch(const BatchDev &d, int maxM, cudaStream_t s) {
     const int maxS = imax(d.maxS, 1);
-    const size_t smem = forward_smem<F>(maxS);
+    maxM = imax(maxM, 1);
+    // stage the same-branch rows in shared memory when they fit, else read them from L1/L2
+    int t2_in_smem = forward_smem<F>(maxS, maxM) <= 200 * 1024;
+    if (!t2_in_smem) maxM = 1;
+    const size_t smem = forward_smem<F>(maxS, maxM);
     static size_t configured = 0;
-    if (smem > 48 * 1024 && smem > configured) {
-        cudaFuncSetAttribute(k_forward<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (smem > configured) {  // opt in; static shared memory counts against 48 KB too
+        if (cudaFuncSetAttribute(k_forward<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return;
         configured = smem;
     }
-    k_forward<F><<<d.ninst, forward_threads(maxS), smem, s>>>(d, maxS);
+    k_forward<F><<<d.ninst, forward_threads(maxS), smem, s>>>(d, maxS, maxM, t2_in_smem);
     note_launch();
 }
 
 }  // namespace
 
 void launch_forward(const BatchDev &d, bool fp32, cudaStream_t s) {
-    if (fp32) launch<float>(d, s);
-    else launch<double>(d, s);
+    if (fp32) launch<float>(d, d.maxM, s);
+    else launch<double>(d, d.maxM, s);
 }
 
 }  // namespace awg

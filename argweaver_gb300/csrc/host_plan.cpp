@@ -152,6 +152,7 @@ bool build_plan(const awg_problem *probs, int n, HostPlan &plan, std::string &er
             S_of[q][b] = S;
             M_of[q][b] = M;
             plan.maxS = std::max(plan.maxS, S);
+            plan.maxM = std::max(plan.maxM, M);
             if (b > 0) {
                 const int *s = p.sprs + (size_t)b * 4;
                 if (s[0] < 0 || s[0] >= p.nnodes || s[2] < 0 || s[2] >= p.nnodes)

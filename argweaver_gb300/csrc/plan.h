@@ -10,7 +10,7 @@
 namespace awg {
 
 struct HostPlan {
-    int ninst = 0, nblocks = 0, maxS = 1, maxnodes = 1, maxT = 0, maxlen = 1;
+    int ninst = 0, nblocks = 0, maxS = 1, maxnodes = 1, maxT = 0, maxlen = 1, maxM = 1;
     long long total_states = 0;  // sum of S over blocks
     long long total_cells = 0;   // forward-table cells of the batch
     long long total_cols = 0;    // columns of the batch

@@ -31,24 +31,40 @@ constexpr int TAB_THREADS = 128;
 struct Terms {
     double D[MAXT], E[MAXT], lnB[MAXT], lnE2[MAXT], lnNegG1[MAXT], G2[MAXT], G3[MAXT],
         lnG4[MAXT], norecombs[MAXT];
+    // the exponentials get_time needs, each evaluated once per tree:
+    double EB[MAXT];              // exp(lnE2[b] + lnB[b-1]), b > 0
+    double E2B[MAXT][MAXT];       // [a][b] exp(lnE2[b] + lnB[a])
+    double E2N[MAXT][MAXT];       // [a][b] exp(lnE2[b] + lnNegG1[a])
+    double CT[MAXT][MAXT];        // [b][c] exp(lnG4[b] + lnB[c-1]), c > 0
 };
 
-// TransMatrix::get_time (trans.h:89-128)
+// Fill the exponential tables (the same arguments get_time exponentiates).
+__device__ void exp_tables(Terms &t, int T) {
+    for (int e = threadIdx.x; e < (T - 1) * (T - 1); e += blockDim.x) {
+        const int a = e / (T - 1), b = e % (T - 1);
+        t.E2B[a][b] = exp(t.lnE2[b] + t.lnB[a]);
+        t.E2N[a][b] = exp(t.lnE2[b] + t.lnNegG1[a]);
+        t.CT[a][b + 1] = exp(t.lnG4[a] + t.lnB[b]);  // [b=a][c=b+1]
+    }
+    for (int b = threadIdx.x; b < T - 1; b += blockDim.x)
+        t.EB[b] = b > 0 ? exp(t.lnE2[b] + t.lnB[b - 1]) : 0.0;
+}
+
+// TransMatrix::get_time (trans.h:89-128) over the precomputed exponentials: every value is
+// the one the reference computes, in the same order.
 __device__ double get_time(const Terms &t, int a, int b, int c, int minage, bool same_node) {
     if (a < minage || b < minage) return 0.0;
     double term1 = __dmul_rn(t.D[a], t.E[b]);
     double minage_term = 0.0;
-    if (minage > 0) minage_term = exp(t.lnG4[b] + t.lnB[minage - 1]);
-    const double eb = (b > 0 ? exp(t.lnE2[b] + t.lnB[b - 1]) : 0.0);
+    if (minage > 0) minage_term = t.CT[b][minage];
+    const double eb = t.EB[b];
     if (!same_node) {
-        if (a < b) return term1 * (exp(t.lnE2[b] + t.lnB[a]) - exp(t.lnE2[b] + t.lnNegG1[a]) - minage_term);
+        if (a < b) return term1 * (t.E2B[a][b] - t.E2N[a][b] - minage_term);
         if (a == b) return term1 * (eb + t.G3[b] - minage_term);
         return term1 * (eb + t.G2[b] - minage_term);
     }
-    double c_term = (c > 0 ? exp(t.lnG4[b] + t.lnB[c - 1]) : 0.0);
-    if (a < b)
-        return term1 * (2 * (exp(t.lnE2[b] + t.lnB[a]) - exp(t.lnE2[b] + t.lnNegG1[a])) - c_term -
-                        minage_term);
+    double c_term = (c > 0 ? t.CT[b][c] : 0.0);
+    if (a < b) return term1 * (2 * (t.E2B[a][b] - t.E2N[a][b]) - c_term - minage_term);
     if (a == b) return term1 * ((2 * (eb + t.G3[b])) - c_term - minage_term) + t.norecombs[a];
     return term1 * ((2 * (eb + t.G2[b])) - c_term - minage_term);
 }
@@ -296,7 +312,8 @@ __global__ void __launch_bounds__(TAB_THREADS) k_tables(BatchDev d, int want32) 
     __shared__ Terms tr;
     __shared__ int nb[MAXT], nr[MAXT], nc[MAXT], pnb[MAXT], pnr[MAXT], pnc[MAXT];
     __shared__ double sums2[2 * MAXT + 1], recoals[MAXT];
-    __shared__ double sh_treelen, sh_sums, sh_maintreelen, sh_subtreelen;
+    __shared__ double sh_treelen, sh_sums, sh_maintreelen, sh_subtreelen, sh_tlmin;
+    __shared__ double wmin[TAB_THREADS / 32];
     __shared__ int sh_S, sh_S1, sh_minage, sh_rootage, sh_src[2];
 
     const double *model = d.model + I.model0;
@@ -405,6 +422,7 @@ __global__ void __launch_bounds__(TAB_THREADS) k_tables(BatchDev d, int want32) 
             tr.D[b] = (1.0 - exp(-rho * treelen2)) / treelen2_b;
             tr.E[b] = 1.0 / nc[b];
             tr.norecombs[b] = exp(-fmax(rho * treelen2, rho));
+            if (want32) d.rstay32[(size_t)blk * MAXT + b] = (float)(-expm1(-fmax(rho * treelen2, rho)));
         }
     }
     __syncthreads();
@@ -413,6 +431,8 @@ __global__ void __launch_bounds__(TAB_THREADS) k_tables(BatchDev d, int want32) 
         for (int b = 1; b < T - 1; b++) tr.lnB[b] = logadd(tr.lnB[b - 1], lnBterm[b]);
         tr.E[T - 2] = 1.0 / nc[T - 2];
     }
+    __syncthreads();
+    exp_tables(tr, T);
     __syncthreads();
 
     // tmatrix[a][b] = get_time(a, b, 0, minage, false) (sample_thread.cpp:212-216)
@@ -435,7 +455,9 @@ __global__ void __launch_bounds__(TAB_THREADS) k_tables(BatchDev d, int want32) 
             const int a = t0[si.node] + y;
             const double g = get_time(tr, a, b, c, minage, true);
             gts[base + y] = g;
-            if (want32) d.t2d32[B.t2_0 + base + y] = (float)(g - tm[a * MAXT + b]);
+            if (want32)  // the moving part: the diagonal's no-recombination term is apart
+                d.t2d32[B.t2_0 + base + y] =
+                    (float)(g - tm[a * MAXT + b] - (a == b ? tr.norecombs[a] : 0.0));
         }
     }
 
@@ -503,7 +525,8 @@ __global__ void __launch_bounds__(TAB_THREADS) k_tables(BatchDev d, int want32) 
         const int mainr = internal ? cur[root].z : root;
         const int node1 = internal ? cur[root].y : 0;
         const double time1 = internal ? times[cur[node1].w] : 0.0;
-        for (int k = tid; k < S; k += blockDim.x) {
+        // tree length seen by each state (emit.cpp:807-816), floored at mintime
+        auto tlen = [&](int k) {
             const StateInfo si = sinfo[k];
             const double coal_time = times[si.time];
             double treelen;
@@ -512,13 +535,31 @@ __global__ void __launch_bounds__(TAB_THREADS) k_tables(BatchDev d, int want32) 
                           fmax(coal_time - times[cur[mainr].w], mintime);
             else
                 treelen = sh_maintreelen + sh_subtreelen + fmax(coal_time - time1, mintime);
-            const double v = .25 * exp(-mu * fmax(treelen, mintime));
-            inv[k] = v;
-            if (want32) d.inv32[B.state0 + k] = (float)v;
+            return fmax(treelen, mintime);
+        };
+        double lmin = INFINITY;
+        for (int k = tid; k < S; k += blockDim.x) {
+            const double tl = tlen(k);
+            inv[k] = .25 * exp(-mu * tl);
+            lmin = fmin(lmin, tl);
+        }
+        if (want32) {
+            for (int o = 16; o > 0; o >>= 1) lmin = fmin(lmin, __shfl_xor_sync(0xffffffffu, lmin, o));
+            if ((tid & 31) == 0) wmin[tid >> 5] = lmin;
+            __syncthreads();
+            if (tid == 0) {
+                double m = INFINITY;
+                for (int w = 0; w < (int)(blockDim.x >> 5); w++) m = fmin(m, wmin[w]);
+                sh_tlmin = m;
+                d.lneref[blk] = S == 0 ? 0.0 : log(.25) - mu * m;
+            }
+            __syncthreads();
+            for (int k = tid; k < S; k += blockDim.x)
+                d.inv32[B.state0 + k] = (float)(-expm1(-mu * (tlen(k) - sh_tlmin)));
         }
         if (S == 0 && tid == 0) {
             inv[0] = 1.0;
-            if (want32) d.inv32[B.state0] = 1.0f;
+            if (want32) d.inv32[B.state0] = 0.0f;
         }
     }
 
@@ -762,8 +803,15 @@ __global__ void __launch_bounds__(TAB_THREADS) k_tables(BatchDev d, int want32) 
 
 // ---------------------------------------------------------------------------------------
 // K2: emissions of variant columns (calc_emissions' non-invariant branch, emit.cpp:822-844)
+//
+// One CTA per local tree. The per-state branch factors (prob_branch of the three split
+// branches, emit.cpp:787-805) are computed once per tree in FP64; each warp then takes
+// every nwarps-th variant column of the tree: lane 0 runs the inner (postorder) and outer
+// (preorder) partial likelihoods, the warp evaluates calc_emit for all states. F is the
+// arithmetic type of the partials and emissions (FP64 plain path / FP32 chosen path).
 
-__global__ void k_varemit(BatchDev d, int want32, int nwarps) {
+template <typename F>
+__global__ void k_varemit(BatchDev d, int nwarps, int maxS) {
     extern __shared__ int4 dyn[];
     const int blk = blockIdx.x;
     const BlockDev B = d.blocks[blk];
@@ -772,14 +820,20 @@ __global__ void k_varemit(BatchDev d, int want32, int nwarps) {
     const int T = I.T, n = I.nnodes;
     const bool internal = I.internal != 0;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int S = B.S;
 
+    auto align16 = [](void *p) {
+        return (char *)(((uintptr_t)p + 15) & ~(uintptr_t)15);
+    };
     int4 *nd = dyn;
-    double *muts = (double *)(nd + n);
-    double *nomuts = muts + n;
-    int *order = (int *)(nomuts + n);
+    F *muts = (F *)align16(nd + n);
+    F *nomuts = muts + n;
+    F *pm = (F *)align16(nomuts + n);            // [S][6]: mut0..2, nomut0..2 per state
+    int *order = (int *)align16(pm + (size_t)6 * maxS);
     int *visit = order + n;
-    double *scratch = (double *)(visit + n);  // 8-byte aligned (offset 40n); per warp: inner, outer
-    int *stacks = (int *)(scratch + (size_t)nwarps * n * 8);
+    int *snode = visit + n;                      // [maxS]
+    F *scratch = (F *)align16(snode + maxS);     // per warp: inner[n][4], outer[n][4]
+    int *stacks = (int *)align16(scratch + (size_t)nwarps * n * 8);
     __shared__ double times[MAXT];
 
     const double *model = d.model + I.model0;
@@ -788,19 +842,40 @@ __global__ void k_varemit(BatchDev d, int want32, int nwarps) {
     for (int i = tid; i < n; i += blockDim.x) nd[i] = d.nodes[B.nodes0 + i];
     __syncthreads();
     const int root = B.root;
-    if (tid == 0) {
-        // prob_tree_mutation (emit.cpp:97-116)
-        for (int i = 0; i < n; i++) {
-            muts[i] = 0.0;
-            nomuts[i] = 0.0;
-            if (i == root) continue;
+    for (int i = tid; i < n; i += blockDim.x) {  // prob_tree_mutation (emit.cpp:97-116)
+        double m1 = 0.0, m0 = 0.0;
+        if (i != root) {
             const int pa = nd[nd[i].x].w;
-            if (pa == T + 1) continue;
-            const double t = fmax(times[pa] - times[nd[i].w], mintime);
-            muts[i] = prob_branch(t, mu, true);
-            nomuts[i] = prob_branch(t, mu, false);
+            if (pa != T + 1) {
+                const double t = fmax(times[pa] - times[nd[i].w], mintime);
+                m1 = prob_branch(t, mu, true);
+                m0 = prob_branch(t, mu, false);
+            }
         }
-        // postorder (local_tree.h:274-304)
+        muts[i] = (F)m1;
+        nomuts[i] = (F)m0;
+    }
+    const int mainr = internal ? nd[root].z : root;
+    const int node1 = internal ? nd[root].y : 0;
+    const double time1 = internal ? times[nd[node1].w] : 0.0;
+    const StateInfo *sinfo = d.sinfo + B.state0;
+    for (int k = tid; k < S; k += blockDim.x) {  // per-state split branches (emit.cpp:782-805)
+        const int node2 = sinfo[k].node;
+        snode[k] = node2;
+        const int parent = nd[node2].x;
+        const double time2 = times[nd[node2].w];
+        const double parent_time = (parent != -1) ? times[min(nd[parent].w, T - 1)] : 0.0;
+        const double coal_time = times[sinfo[k].time];
+        double dist[3];
+        dist[0] = fmax(coal_time - time1, mintime);
+        dist[1] = fmax(coal_time - time2, mintime);
+        dist[2] = fmax(parent_time - coal_time, mintime);
+        for (int x = 0; x < 3; x++) {
+            pm[6 * k + x] = (F)prob_branch(dist[x], mu, true);
+            pm[6 * k + 3 + x] = (F)prob_branch(dist[x], mu, false);
+        }
+    }
+    if (tid == 0) {  // postorder (local_tree.h:274-304)
         int i;
         for (i = 0; i < n; i++) visit[i] = 0;
         for (i = 0; i < n; i++) {
@@ -818,47 +893,41 @@ __global__ void k_varemit(BatchDev d, int want32, int nwarps) {
     }
     __syncthreads();
 
-    const int S = B.S;
-    const int mainr = internal ? nd[root].z : root;
-    const int node1 = internal ? nd[root].y : 0;
-    const double time1 = internal ? times[nd[node1].w] : 0.0;
-    const StateInfo *sinfo = d.sinfo + B.state0;
-    double (*in)[4] = (double (*)[4])(scratch + (size_t)warp * n * 8);
-    double (*out)[4] = in + n;
+    F (*in)[4] = (F (*)[4])(scratch + (size_t)warp * n * 8);
+    F (*out)[4] = in + n;
     int *stack = stacks + warp * n;
     const uint8_t *cls = d.colclass + I.col0 + B.start;
     const int ns = I.nseqs;
+    F *vout = (sizeof(F) == 4) ? (F *)d.var32 : (F *)d.varemit;
 
-    // walk the block's variant columns in order; warp w takes every nwarps-th
+    // the block's variant columns in order; warp w takes every nwarps-th
     int seen = 0;
     for (int base = 0; base < B.len; base += 32) {
         const int i = base + lane;
         const bool isvar = i < B.len && cls[i] == COL_VARIANT;
-        const unsigned mask = __ballot_sync(0xffffffffu, isvar);
-        unsigned mm = mask;
+        unsigned mm = __ballot_sync(0xffffffffu, isvar);
         while (mm) {
             const int bit = __ffs(mm) - 1;
             mm &= mm - 1;
             const int vslot = seen++;
             if (vslot % nwarps != warp) continue;
-            const int col = base + bit;
-            const uint8_t *chars = d.seqT + I.seq0 + (size_t)(B.start + col) * ns;
+            const uint8_t *chars = d.seqT + I.seq0 + (size_t)(B.start + base + bit) * ns;
             if (lane == 0) {
                 for (int oi = 0; oi < n; oi++) {  // likelihood_site_node_inner (emit.cpp:151-196)
                     const int j = order[oi];
                     if (nd[j].y == -1) {
                         const uint8_t ch = chars[j];
-                        if (ch == 'N') { in[j][0] = in[j][1] = in[j][2] = in[j][3] = 1.0; }
+                        if (ch == 'N') { in[j][0] = in[j][1] = in[j][2] = in[j][3] = F(1); }
                         else {
-                            in[j][0] = in[j][1] = in[j][2] = in[j][3] = 0.0;
+                            in[j][0] = in[j][1] = in[j][2] = in[j][3] = F(0);
                             const int x = (ch == 'A' || ch == 'a') ? 0 : (ch == 'C' || ch == 'c') ? 1
                                         : (ch == 'G' || ch == 'g') ? 2 : 3;
-                            in[j][x] = 1.0;
+                            in[j][x] = F(1);
                         }
                     } else {
                         const int c1 = nd[j].y, c2 = nd[j].z;
                         for (int a = 0; a < 4; a++) {
-                            double p1 = 0.0, p2 = 0.0;
+                            F p1 = 0, p2 = 0;
                             for (int b = 0; b < 4; b++) {
                                 if (a == b) { p1 += in[c1][b] * nomuts[c1]; p2 += in[c2][b] * nomuts[c2]; }
                                 else { p1 += in[c1][b] * muts[c1]; p2 += in[c2][b] * muts[c2]; }
@@ -872,13 +941,13 @@ __global__ void k_varemit(BatchDev d, int want32, int nwarps) {
                 while (sp > 0) {
                     const int j = stack[--sp];
                     if (j == mainr) {
-                        out[j][0] = out[j][1] = out[j][2] = out[j][3] = 1.0;
+                        out[j][0] = out[j][1] = out[j][2] = out[j][3] = F(1);
                     } else {
                         const int p = nd[j].x;
                         const int sib = nd[p].y == j ? nd[p].z : nd[p].y;
                         if (p != mainr) {
                             for (int a = 0; a < 4; a++) {
-                                double p1 = 0.0, p2 = 0.0;
+                                F p1 = 0, p2 = 0;
                                 for (int b = 0; b < 4; b++) {
                                     if (a == b) { p1 += in[sib][b] * nomuts[sib]; p2 += out[p][b] * nomuts[p]; }
                                     else { p1 += in[sib][b] * muts[sib]; p2 += out[p][b] * muts[p]; }
@@ -887,7 +956,7 @@ __global__ void k_varemit(BatchDev d, int want32, int nwarps) {
                             }
                         } else {
                             for (int a = 0; a < 4; a++) {
-                                double p1 = 0.0;
+                                F p1 = 0;
                                 for (int b = 0; b < 4; b++) {
                                     if (a == b) p1 += in[sib][b] * nomuts[sib];
                                     else p1 += in[sib][b] * muts[sib];
@@ -900,50 +969,38 @@ __global__ void k_varemit(BatchDev d, int want32, int nwarps) {
                 }
             }
             __syncwarp();
-            // leaf partial of the threaded sequence (external) or of the subtree root
-            double in2[4];
+            // leaf partial of the threaded sequence (external) or the subtree root (internal)
+            F in2[4];
             if (internal) {
                 for (int a = 0; a < 4; a++) in2[a] = in[node1][a];
             } else {
                 const uint8_t ch = chars[I.nleaves];
-                if (ch == 'N') { in2[0] = in2[1] = in2[2] = in2[3] = 1.0; }
+                if (ch == 'N') { in2[0] = in2[1] = in2[2] = in2[3] = F(1); }
                 else {
-                    in2[0] = in2[1] = in2[2] = in2[3] = 0.0;
+                    in2[0] = in2[1] = in2[2] = in2[3] = F(0);
                     const int x = (ch == 'A' || ch == 'a') ? 0 : (ch == 'C' || ch == 'c') ? 1
                                 : (ch == 'G' || ch == 'g') ? 2 : 3;
-                    in2[x] = 1.0;
+                    in2[x] = F(1);
                 }
             }
-            double *row = d.varemit + B.var0 + (size_t)d.colvar[I.col0 + B.start + col] * S;
+            F *row = vout + B.var0 + (size_t)d.colvar[I.col0 + B.start + base + bit] * S;
             for (int k = lane; k < S; k += 32) {
-                const int node2 = sinfo[k].node;
-                const int parent = nd[node2].x;
-                const double time2 = times[nd[node2].w];
-                const double parent_time = (parent != -1) ? times[min(nd[parent].w, T - 1)] : 0.0;
-                const double coal_time = times[sinfo[k].time];
-                double dist[3], mut[3], nomut[3];
-                dist[0] = fmax(coal_time - time1, mintime);
-                dist[1] = fmax(coal_time - time2, mintime);
-                dist[2] = fmax(parent_time - coal_time, mintime);
-                for (int x = 0; x < 3; x++) mut[x] = prob_branch(dist[x], mu, true);
-                for (int x = 0; x < 3; x++) nomut[x] = prob_branch(dist[x], mu, false);
-                double e = 0.0;  // calc_emit (emit.cpp:620-645)
+                const int node2 = snode[k];
+                const F *q = pm + 6 * k;
+                F e = 0;  // calc_emit (emit.cpp:620-645)
                 for (int a = 0; a < 4; a++) {
-                    double p1 = 0.0, p2 = 0.0, p3 = 0.0;
+                    F p1 = 0, p2 = 0, p3 = 0;
                     for (int b = 0; b < 4; b++) {
                         if (a == b) {
-                            p1 += in2[b] * nomut[0]; p2 += in[node2][b] * nomut[1];
-                            p3 += out[node2][b] * nomut[2];
+                            p1 += in2[b] * q[3]; p2 += in[node2][b] * q[4]; p3 += out[node2][b] * q[5];
                         } else {
-                            p1 += in2[b] * mut[0]; p2 += in[node2][b] * mut[1];
-                            p3 += out[node2][b] * mut[2];
+                            p1 += in2[b] * q[0]; p2 += in[node2][b] * q[1]; p3 += out[node2][b] * q[2];
                         }
                     }
-                    if (node2 != mainr) e += p1 * p2 * p3 * .25;
-                    else e += p1 * p2 * .25;
+                    if (node2 != mainr) e += p1 * p2 * p3 * F(.25);
+                    else e += p1 * p2 * F(.25);
                 }
                 row[k] = e;
-                if (want32) d.var32[(row - d.varemit) + k] = (float)e;
             }
             __syncwarp();
         }
@@ -963,31 +1020,37 @@ size_t tables_smem(int n, int S, int S1) {
 void launch_tables(const BatchDev &d, bool want32, cudaStream_t s) {
     size_t smem = tables_smem(d.maxnodes, d.maxS, d.maxS);
     static size_t configured = 0;
-    if (smem > 48 * 1024 && smem > configured) {
-        cudaFuncSetAttribute(k_tables, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (smem > configured) {  // opt in; static shared memory counts against 48 KB too
+        if (cudaFuncSetAttribute(k_tables, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return;
         configured = smem;
     }
     k_tables<<<d.nblocks, TAB_THREADS, smem, s>>>(d, want32 ? 1 : 0);
     note_launch();
 }
 
-void launch_varemit(const BatchDev &d, bool want32, cudaStream_t s) {
-    const int n = d.maxnodes;
+template <typename F>
+void launch_varemit_t(const BatchDev &d, cudaStream_t s) {
+    const int n = d.maxnodes, maxS = imax(d.maxS, 1);
     int nwarps = 4;
     auto need = [&](int w) {
-        return (size_t)n * sizeof(int4) + 2 * (size_t)n * sizeof(double) +
-               (2 * (size_t)n + 2) * sizeof(int) + (size_t)w * n * 8 * sizeof(double) +
-               (size_t)w * n * sizeof(int) + 16;
+        return (size_t)n * sizeof(int4) + (2 * (size_t)n + 6 * (size_t)maxS) * sizeof(F) +
+               (2 * (size_t)n + maxS + 4) * sizeof(int) + (size_t)w * n * 8 * sizeof(F) +
+               (size_t)w * n * sizeof(int) + 6 * 16;
     };
     while (nwarps > 1 && need(nwarps) > 200 * 1024) nwarps--;
-    size_t smem = need(nwarps);
+    const size_t smem = need(nwarps);
     static size_t configured = 0;
-    if (smem > 48 * 1024 && smem > configured) {
-        cudaFuncSetAttribute(k_varemit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (smem > configured) {  // opt in; static shared memory counts against 48 KB too
+        if (cudaFuncSetAttribute(k_varemit<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return;
         configured = smem;
     }
-    k_varemit<<<d.nblocks, nwarps * 32, smem, s>>>(d, want32 ? 1 : 0, nwarps);
+    k_varemit<F><<<d.nblocks, nwarps * 32, smem, s>>>(d, nwarps, maxS);
     note_launch();
+}
+
+void launch_varemit(const BatchDev &d, bool fp32, cudaStream_t s) {
+    if (fp32) launch_varemit_t<float>(d, s);
+    else launch_varemit_t<double>(d, s);
 }
 
 }  // namespace awg

@@ -47,10 +47,12 @@ def parse():
     ap.add_argument("--instances", type=int, default=256)
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--cpu-sample-seconds", type=float, default=15.0)
+    ap.add_argument("--max-columns", type=int, default=0,
+                    help="cap each problem's length (small cases for profiling)")
     return ap.parse_args()
 
 
-def make_workload(n: int, seed: int, rank: int = 0):
+def make_workload(n: int, seed: int, rank: int = 0, max_columns: int = 0):
     from argweaver_gb300.sim import simulate
 
     rng = np.random.default_rng(seed + 7919 * rank)
@@ -58,6 +60,8 @@ def make_workload(n: int, seed: int, rank: int = 0):
     bps = rng.uniform(1e5, 1e6, size=n)
     seeds = rng.integers(1, 2**62, size=n)
     specs = [(int(k) - 1, int(bp // 10), int(s)) for k, bp, s in zip(ks, bps, seeds)]
+    if max_columns:
+        specs = [(k, min(L, max_columns), s) for k, L, s in specs]
 
     def one(spec):
         nl, L, s = spec
@@ -157,7 +161,7 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        problems = make_workload(args.instances, args.seed)
+        problems = make_workload(args.instances, args.seed, 0, args.max_columns)
         for _ in range(args.warmup):
             cpu_reference(problems, min(2.0, args.cpu_sample_seconds), threads)
         vals = []
@@ -191,7 +195,7 @@ def main():
         dist.init_process_group("nccl")
     from argweaver_gb300 import api
 
-    problems = make_workload(args.instances, args.seed, rank)
+    problems = make_workload(args.instances, args.seed, rank, args.max_columns)
     cells = sum(p.cells() for p in problems)
     h2d = sum(p.ptrees.nbytes + p.ages.nbytes + p.sprs.nbytes + p.blocklens.nbytes +
               p.seqs.nbytes for p in problems)
@@ -212,12 +216,13 @@ def main():
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    dev_ms, fwd_ms, tb_ms, wall = [], [], [], []
+    dev_ms, fwd_ms, tb_ms, wall, phases = [], [], [], [], []
     for _ in range(args.steps):
         t0 = time.perf_counter()
         step()
         wall.append(time.perf_counter() - t0)
         t = api.last_timings()
+        phases.append(t)
         dev_ms.append(t["tables"] + t["emit"] + t["forward"] + t["traceback"])
         fwd_ms.append(t["forward"])
         tb_ms.append(t["traceback"])
@@ -243,6 +248,7 @@ def main():
         a = api.run_batch([p], precision="fp32", want_forward=False, want_posterior=True)[0]
         b = api.run_batch([p], precision="fp64", want_forward=False, want_posterior=True)[0]
         errs.append(float(np.max(np.abs(a.posterior - b.posterior))))
+    errs = errs or [float("nan")]
 
     if rank != 0:
         return
@@ -274,7 +280,8 @@ def main():
         "fp32_vs_fp64_posterior_max_abs_err": max(errs),
         "gpu_launches": launches,
         "clocks": clocks,
-        "phase_ms": api.last_timings(),
+        "phase_ms": {k: float(np.mean([t[k] for t in phases])) for k in phases[0]},
+        "longest_instance_columns": max(p.seqlen for p in problems),
     }
     print(json.dumps(line))
 

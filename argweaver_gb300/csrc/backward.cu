@@ -27,9 +27,7 @@ template <> struct BTab<double> {
     __device__ explicit BTab(const BatchDev &d)
         : tm(d.tm), inv(d.inv_lk), var(d.varemit), dprob(d.determprob), rrow(d.recombrow),
           crow(d.recoalrow), gts(d.gts), fw(d.fw64) {}
-    __device__ double t2(long long t2_0, int off, int y, double tmab) const {
-        return gts[t2_0 + off + y] - tmab;
-    }
+    __device__ double t2(long long idx, double tmab) const { return gts[idx] - tmab; }
 };
 template <> struct BTab<float> {
     // complements of the stay probability and of the invariant emissions, as in the forward
@@ -39,7 +37,7 @@ template <> struct BTab<float> {
     __device__ explicit BTab(const BatchDev &d)
         : rstay(d.rstay32), tm(d.tm32), inv(d.inv32), var(d.var32), dprob(d.determprob32),
           rrow(d.recombrow32), crow(d.recoalrow32), t2d(d.t2d32), fw(d.fw32) {}
-    __device__ float t2(long long t2_0, int off, int y, float) const { return t2d[t2_0 + off + y]; }
+    __device__ float t2(long long idx, float) const { return t2d[idx]; }
 };
 
 template <typename F>
@@ -53,17 +51,23 @@ struct Meta {
     int time, j1, m, off;
 };
 
-// Block-wide sum in a fixed order; every thread gets the result.
-template <typename F>
-__device__ F block_sum(F part, F *red) {
+// Block-wide sum of fn(k), k < n, in an order fixed by n alone (groups of 32 consecutive
+// k, then the group sums), so results do not depend on the block size. Every thread gets
+// the result; gs holds ceil(n / 32) group sums.
+template <typename F, typename Fn>
+__device__ F fixed_sum(int n, Fn fn, F *gs) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    part = warp_sum(part);
-    __syncthreads();
-    if (lane == 0) red[warp] = part;
+    const int ng = (n + 31) >> 5;
+    __syncthreads();  // gs free, inputs complete
+    for (int g = warp; g < ng; g += nw) {
+        const int k = g * 32 + lane;
+        const F x = warp_sum(k < n ? fn(k) : F(0));
+        if (lane == 0) gs[g] = x;
+    }
     __syncthreads();
     F s = 0;
-    for (int w = 0; w < nw; w++) s += red[w];
-    return s;
+    for (int g = lane; g < ng; g += 32) s += gs[g];
+    return warp_sum(s);
 }
 
 template <typename F>
@@ -80,8 +84,10 @@ __global__ void k_backward(BatchDev d, int maxS, double *bw_out) {
     F *g = bwB + maxS;
     Meta *meta = (Meta *)(g + maxS + (maxS & 1));
     int *perm = (int *)(meta + maxS);
+    F *gs = (F *)(perm + maxS + 1) + 1;     // [maxS / 32 + 1] group sums, 8-byte aligned
+    gs = (F *)(((uintptr_t)gs + 7) & ~(uintptr_t)7);
     __shared__ F tm[MAXT * MAXT];
-    __shared__ F G[MAXT], H[MAXT], red[32], rS[MAXT];
+    __shared__ F G[MAXT], H[MAXT], rS[MAXT];
     __shared__ int bptr[MAXT + 1];
 
     F *cur = bwA, *nxt = bwB;  // cur: bw of column i+1, nxt: bw of column i
@@ -124,9 +130,7 @@ __global__ void k_backward(BatchDev d, int maxS, double *bw_out) {
         // posterior of one column from its bw (in `bw`) and fw
         auto posterior = [&](int i, const F *bw) {
             const F *f = fw + (size_t)i * Sm;
-            F part = 0;
-            for (int k = tid; k < Sm; k += blockDim.x) part += f[k] * bw[k];
-            const F z = block_sum(part, red);
+            const F z = fixed_sum<F>(Sm, [&](int k) { return f[k] * bw[k]; }, gs);
             const long long c0 = B.cell0 + (long long)i * Sm;
             for (int k = tid; k < Sm; k += blockDim.x) {
                 if (d.post) d.post[c0 + k] = (double)(f[k] * bw[k] / z);
@@ -162,15 +166,13 @@ __global__ void k_backward(BatchDev d, int maxS, double *bw_out) {
                     F s = H[a];
                     for (int x = 0; x < mj.m; x++) {
                         const int k = mj.j1 + x;  // target on the same node, time a0 + x
-                        s += tab.t2(B.t2_0, meta[k].off, y, tm[a * MAXT + a0 + x]) * g[k];
+                        s += tab.t2(B.t2_0 + meta[k].off + y * mj.m, tm[a * MAXT + a0 + x]) * g[k];
                     }
                     if (BTab<F>::split) s = g[j] + (s - rS[a] * g[j]);  // stay term apart
                     nxt[j] = s;
                 }
             }
-            F part = 0;
-            for (int k = tid; k < Sm; k += blockDim.x) part += nxt[k];
-            const F z = block_sum(part, red);
+            const F z = fixed_sum<F>(Sm, [&](int k) { return nxt[k]; }, gs);
             for (int k = tid; k < Sm; k += blockDim.x) nxt[k] /= z;
             __syncthreads();
             posterior(i, nxt);
@@ -198,9 +200,7 @@ __global__ void k_backward(BatchDev d, int maxS, double *bw_out) {
                 }
                 nxt[j] = s;
             }
-            F part = 0;
-            for (int k = tid; k < n1; k += blockDim.x) part += nxt[k];
-            const F z = block_sum(part, red);
+            const F z = fixed_sum<F>(n1, [&](int k) { return nxt[k]; }, gs);
             for (int k = tid; k < n1; k += blockDim.x) nxt[k] /= z;
             __syncthreads();
             (void)P;
@@ -218,7 +218,8 @@ int backward_threads(int maxS) {
 template <typename F>
 void launch(const BatchDev &d, double *bw_out, cudaStream_t s) {
     const int maxS = imax(d.maxS, 1);
-    const size_t smem = 3 * (size_t)maxS * sizeof(F) + 8 + (size_t)maxS * (sizeof(Meta) + sizeof(int));
+    const size_t smem = 3 * (size_t)maxS * sizeof(F) + 8 + (size_t)maxS * (sizeof(Meta) + sizeof(int)) +
+                        sizeof(int) + 16 + ((size_t)maxS / 32 + 1) * sizeof(F);
     static size_t configured = 0;
     if (smem > configured) {  // opt in; static shared memory counts against 48 KB too
         if (cudaFuncSetAttribute(k_backward<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return;

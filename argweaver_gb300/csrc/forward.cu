@@ -8,12 +8,14 @@
 // At a local-tree boundary the first column comes from the switch matrix
 // (arghmm_forward_switch, sample_thread.cpp:345-389), gathered per target state.
 //
-// Schedule: one CTA barrier per column. Column values stay unnormalised in shared memory;
-// after the barrier every warp sums the time bins of the previous column (a fixed order per
-// bin), which also gives that column's norm, forms tf with shuffles, and then each thread
-//   - writes its entries of the previous column, now divided by that norm, to HBM, and
-//   - computes its entries of the new column, scaled by 1/norm (the reference's
-//     normalise-then-step, reordered; the normalised values are the same).
+// Schedule per column, two CTA barriers:
+//   A  the previous column is complete, in state order (for same-branch neighbours) and in
+//      time-sorted order (each time bin a contiguous range);
+//      warps split the bins; a warp sums a bin with coalesced, conflict-free loads
+//   B  every thread reads the bins: the previous column's norm and tf (lane b); then each
+//      thread writes its entries of the previous column, divided by that norm, to HBM and
+//      computes its entries of the new column scaled by 1/norm (the reference's
+//      normalise-then-step, reordered; the normalised values are the same).
 // Reductions have a fixed order, so results do not depend on the run or the batch.
 // log(norm) goes into an FP64 mantissa product plus an integer exponent (one FP64 log
 // every 64 columns instead of one per column).
@@ -104,27 +106,28 @@ __global__ void __launch_bounds__(512) k_forward(BatchDev d, int maxS, int maxM,
     extern __shared__ double dyn_d[];
     const Tab<F> tab(d);
     const InstDev I = d.inst[blockIdx.x];
-    const int T = I.T;
-    const int tid = threadIdx.x, lane = tid & 31;
-    const int NT = blockDim.x;
+    const int T = I.T, NB = T - 1;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int NT = blockDim.x, NW = NT >> 5;
 
-    F *col = (F *)dyn_d;                       // [2][maxS]
-    F *t2s = col + 2 * maxS;                   // [maxM] tmatrix2 rows of the block
-    Meta *meta = (Meta *)(t2s + maxM + ((2 * maxS + maxM) & 1));
-    int *perm = (int *)(meta + maxS);          // states grouped by time
-    F *invS = (F *)(perm + maxS + (maxS & 1)); // invariant-site emission per state
+    F *col = (F *)dyn_d;                       // [2][maxS] columns in state order
+    F *colT = col + 2 * maxS;                  // [maxS] newest column, time-sorted
+    F *t2s = colT + maxS;                      // [maxM] tmatrix2 entries of the block
+    F *invS = t2s + maxM;                      // [maxS] invariant-site emissions
+    Meta *meta = (Meta *)(((uintptr_t)(invS + maxS) + 15) & ~(uintptr_t)15);
+    int *rank = (int *)(meta + maxS);          // time-sorted position of each state
     __shared__ F tmS[MAXT * MAXT];
     __shared__ F rS[MAXT];
+    __shared__ F tfrow[MAXT - 1][32];          // per bin b: tm[b][lane] * sum_b, sum_b (lane 31)
     __shared__ int bptr[MAXT + 1];
 
-    F tmcol[MAXT - 1];                         // lane b: tmatrix[a][b] for every a
     LogAcc acc;
     int c = 0;                                 // buffer holding the current column
 
     for (int bi = 0; bi < I.ntrees; bi++) {
         const int blk = I.block0 + bi;
-        const BlockDev &B = d.blocks[blk];
-        const int S = B.S, Sm = imax(S, 1);
+        const BlockDev B = d.blocks[blk];
+        const int S = B.S;
         F *fw = tab.fw + B.cell0;
 
         if (S == 0) {
@@ -164,30 +167,28 @@ __global__ void __launch_bounds__(512) k_forward(BatchDev d, int maxS, int maxM,
         for (int k = tid; k < S; k += NT) {
             const StateInfo si = d.sinfo[B.state0 + k];
             meta[k] = Meta{si.time, si.j1, si.m, d.t2off[B.state0 + k]};
-            perm[k] = d.bt_perm[B.state0 + k];
+            rank[d.bt_perm[B.state0 + k]] = k;  // k as sorted position: rank[state] = position
             invS[k] = tab.inv[B.state0 + k];
         }
         const F *tmg = tab.tm + (size_t)blk * MAXT * MAXT;
-        for (int e = tid; e < (T - 1) * MAXT; e += NT) tmS[e] = tmg[e];
+        for (int e = tid; e < NB * MAXT; e += NT) tmS[e] = tmg[e];
         for (int a = tid; a <= MAXT; a += NT) bptr[a] = d.bt_ptr[(size_t)blk * (MAXT + 1) + a];
         if (Tab<F>::split)
             for (int a = tid; a < MAXT; a += NT) rS[a] = tab.rstay[(size_t)blk * MAXT + a];
         __syncthreads();
         if (t2_in_smem)
-            for (int k = tid; k < S; k += NT) {  // same-branch rows, one per state
+            for (int k = tid; k < S; k += NT) {  // same-branch entries, node blocks source-major
                 const Meta mk = meta[k];
                 const int a0 = mk.time - (k - mk.j1);
                 for (int y = 0; y < mk.m; y++)
-                    t2s[mk.off + y] = tab.t2(B.t2_0 + mk.off + y, tmS[(a0 + y) * MAXT + mk.time]);
+                    t2s[mk.off + y * mk.m] =
+                        tab.t2(B.t2_0 + mk.off + y * mk.m, tmS[(a0 + y) * MAXT + mk.time]);
             }
-        const double lner = Tab<F>::split ? tab.lneref[blk] : 0.0;
-#pragma unroll
-        for (int a = 0; a < MAXT - 1; a++)
-            tmcol[a] = (a < T - 1 && lane < T - 1) ? tmS[a * MAXT + lane] : F(0);
         const uint8_t *cls = d.colclass + I.col0 + B.start;
         const int *cvar = d.colvar + I.col0 + B.start;
         const F *inv = invS;
         const F *var = tab.var + B.var0;
+        const double lner = Tab<F>::split ? tab.lneref[blk] : 0.0;
         // column classes and variant rows, 32 columns per load, read back by shuffles
         int ccache = 0, vcache = 0, cbase = -32;
         auto colinfo = [&](int i, uint8_t &ci, int &vi) {
@@ -200,10 +201,15 @@ __global__ void __launch_bounds__(512) k_forward(BatchDev d, int maxS, int maxM,
             ci = (uint8_t)__shfl_sync(0xffffffffu, ccache, i - cbase);
             vi = __shfl_sync(0xffffffffu, vcache, i - cbase);
         };
+        __syncthreads();  // rank[] complete
 
         // ---- first column of the block
         if (bi == 0) {
-            for (int k = tid; k < S; k += NT) col[c * maxS + k] = fw[k];  // priors (K1)
+            for (int k = tid; k < S; k += NT) {
+                const F v = fw[k];  // priors (K1)
+                col[c * maxS + k] = v;
+                colT[rank[k]] = v;
+            }
         } else {
             // previous column is normalised in col[c] (S1 entries)
             const int2 src = d.srcs[blk];
@@ -229,6 +235,7 @@ __global__ void __launch_bounds__(512) k_forward(BatchDev d, int maxS, int maxM,
                 else if (c0 == COL_INVARIANT) v = Tab<F>::split ? s - s * inv[k] : s * inv[k];
                 else v = s * var[(size_t)v0 * S + k];
                 col[(c ^ 1) * maxS + k] = v;
+                colT[rank[k]] = v;
             }
             if (Tab<F>::split && tid == 0 && c0 == COL_INVARIANT) acc.extra += lner;
             c ^= 1;
@@ -236,29 +243,23 @@ __global__ void __launch_bounds__(512) k_forward(BatchDev d, int maxS, int maxM,
 
         // ---- remaining columns; iteration i also finalises column i-1
         for (int i = 1; i <= B.len; i++) {
-            __syncthreads();
-            const F *cur = col + c * maxS;
-            // time bins of column i-1 (lane a), its norm, tf (lane b)
-            F fg = 0;
-            if (lane < T - 1) {
-                F s0 = 0, s1 = 0, s2 = 0, s3 = 0;
-                int p = bptr[lane];
-                const int pe = bptr[lane + 1];
-                for (; p + 3 < pe; p += 4) {
-                    s0 += cur[perm[p]]; s1 += cur[perm[p + 1]];
-                    s2 += cur[perm[p + 2]]; s3 += cur[perm[p + 3]];
-                }
-                for (; p < pe; p++) s0 += cur[perm[p]];
-                fg = (s0 + s1) + (s2 + s3);
+            __syncthreads();  // A: column i-1 complete
+            // each bin's sum, and its terms of tf[a] = sum_b tm[b][a] sum_b (lane a); the
+            // terms are added in bin order below, so the result does not depend on NT
+            for (int b = warp; b < NB; b += NW) {
+                F s = 0;
+                for (int p = bptr[b] + lane; p < bptr[b + 1]; p += 32) s += colT[p];
+                s = warp_sum(s);
+                tfrow[b][lane] = lane == 31 ? s : (lane < NB ? tmS[b * MAXT + lane] : F(0)) * s;
             }
-            const F norm = warp_sum(fg);
+            __syncthreads();  // B: bin rows of column i-1
+            F norm = 0, tf = 0;
+            for (int b = 0; b < NB; b++) {
+                tf += tfrow[b][lane];
+                norm += tfrow[b][31];
+            }
             const F inv_norm = F(1) / norm;
-            F tf = 0;
-#pragma unroll
-            for (int a = 0; a < MAXT - 1; a++) {
-                const F f = __shfl_sync(0xffffffffu, fg, a);
-                tf += tmcol[a] * f;
-            }
+            const F *cur = col + c * maxS;
             if (tid == 0) {
                 acc.add((double)norm);
                 if (!(norm > F(0))) report_error(d.err, ERR_ZERO_NORM, blockIdx.x, bi, B.start + i - 1);
@@ -292,11 +293,20 @@ __global__ void __launch_bounds__(512) k_forward(BatchDev d, int maxS, int maxM,
                     F s = tfb;
                     if (t2_in_smem) {
                         const F *row = t2s + mk.off;
-                        for (int y = 0; y < mk.m; y++) s += row[y] * nb[y];
+                        const int m = mk.m;
+                        int y = 0;
+                        F s1 = 0;
+                        for (; y + 1 < m; y += 2) {
+                            s += row[0] * nb[y];
+                            s1 += row[m] * nb[y + 1];
+                            row += 2 * m;
+                        }
+                        if (y < m) s += row[0] * nb[y];
+                        s += s1;
                     } else {
                         const int a0 = mk.time - (k - mk.j1);
                         for (int y = 0; y < mk.m; y++)
-                            s += tab.t2(B.t2_0 + mk.off + y, tmS[(a0 + y) * MAXT + mk.time]) * nb[y];
+                            s += tab.t2(B.t2_0 + mk.off + y * mk.m, tmS[(a0 + y) * MAXT + mk.time]) * nb[y];
                     }
                     F v;
                     if (Tab<F>::split) {
@@ -309,7 +319,9 @@ __global__ void __launch_bounds__(512) k_forward(BatchDev d, int maxS, int maxM,
                                   : ci == COL_INVARIANT ? inv[k] : var[(size_t)vrow * S + k];
                         v = s * e;
                     }
-                    nxt[k] = v * inv_norm;
+                    v *= inv_norm;
+                    nxt[k] = v;
+                    colT[rank[k]] = v;
                 }
             }
             c ^= 1;
@@ -323,14 +335,15 @@ __global__ void __launch_bounds__(512) k_forward(BatchDev d, int maxS, int maxM,
 }
 
 int forward_threads(int maxS) {
-    if (maxS > 1024) return 512;
-    if (maxS > 256) return 256;
+    if (maxS > 256) return 512;
+    if (maxS > 128) return 256;
     return 128;
 }
 
+
 template <typename F>
 size_t forward_smem(int maxS, int maxM) {
-    return (size_t)(3 * maxS + maxM + 2) * sizeof(F) + (size_t)maxS * (sizeof(Meta) + sizeof(int)) + 16;
+    return (size_t)(4 * maxS + maxM) * sizeof(F) + 16 + (size_t)maxS * (sizeof(Meta) + sizeof(int));
 }
 
 template <typename F>

@@ -358,7 +358,7 @@ __global__ void __launch_bounds__(TAB_THREADS) k_tables(BatchDev d, int want32) 
         for (int y = 0; y < m; y++) {
             const int k = first[v] + y;
             sinfo[k] = StateInfo{v, t0[v] + y, first[v], m};
-            t2off[k] = t2base[v] + y * m;
+            t2off[k] = t2base[v] + y;  // entry (k, source y') at t2off[k] + y' * m
         }
     }
     if (S == 0 && tid == 0) {
@@ -445,7 +445,9 @@ __global__ void __launch_bounds__(TAB_THREADS) k_tables(BatchDev d, int want32) 
     }
     __syncthreads();
 
-    // same-branch rows: row k holds get_time(a, b_k, c_k, minage, true) for the node's times a
+    // same-branch rows: get_time(a, b_k, c_k, minage, true) for the node's times a; a node's
+    // m x m block is stored source-major (entry (k, y) at t2off[k] + y * m) so lanes holding
+    // consecutive states of one node read consecutive words
     double *gts = d.gts + B.t2_0;
     for (int k = tid; k < S; k += blockDim.x) {
         const StateInfo si = sinfo[k];
@@ -454,9 +456,9 @@ __global__ void __launch_bounds__(TAB_THREADS) k_tables(BatchDev d, int want32) 
         for (int y = 0; y < si.m; y++) {
             const int a = t0[si.node] + y;
             const double g = get_time(tr, a, b, c, minage, true);
-            gts[base + y] = g;
+            gts[base + y * si.m] = g;
             if (want32)  // the moving part: the diagonal's no-recombination term is apart
-                d.t2d32[B.t2_0 + base + y] =
+                d.t2d32[B.t2_0 + base + y * si.m] =
                     (float)(g - tm[a * MAXT + b] - (a == b ? tr.norecombs[a] : 0.0));
         }
     }

@@ -60,9 +60,14 @@ __device__ int warp_sample(int n, double u, W w) {
     const int lane = threadIdx.x & 31;
     const int chunk = (n + 31) >> 5;
     const int lo = imin(lane * chunk, n), hi = imin(lo + chunk, n);
-    F ls = 0;
-    for (int j = lo; j < hi; j++) ls += w(j);
-    F incl = ls;
+    F l0 = 0, l1 = 0;
+    int j = lo;
+    for (; j + 1 < hi; j += 2) {
+        l0 += w(j);
+        l1 += w(j + 1);
+    }
+    if (j < hi) l0 += w(j);
+    F incl = l0 + l1;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
         const F v = __shfl_up_sync(0xffffffffu, incl, o);
@@ -73,19 +78,28 @@ __device__ int warp_sample(int n, double u, W w) {
     const F total = __shfl_sync(0xffffffffu, incl, 31);
     const F pick = (F)u * total;
     const unsigned hit = __ballot_sync(0xffffffffu, incl >= pick && hi > lo);
-    int result = n - 1;
-    if (hit) {
-        const int src = __ffs(hit) - 1;
-        int found = -1;
-        if (lane == src) {
-            F x = excl;
-            for (int j = lo; j < hi; j++) {
-                x += w(j);
-                if (x >= pick) { found = j; break; }
-            }
-            if (found < 0) found = hi - 1;
+    if (!hit) return n - 1;
+    // rescan the chunk that holds the pick, all lanes at once: lane t takes element
+    // lo_src + t, a lane scan gives the running sums in state order
+    const int src = __ffs(hit) - 1;
+    const int slo = __shfl_sync(0xffffffffu, lo, src), shi = __shfl_sync(0xffffffffu, hi, src);
+    F carry = __shfl_sync(0xffffffffu, excl, src);
+    int result = shi - 1;
+    for (int b0 = slo; b0 < shi; b0 += 32) {
+        const int jj = b0 + lane;
+        F x = jj < shi ? w(jj) : F(0);
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const F v = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += v;
         }
-        result = __shfl_sync(0xffffffffu, found, src);
+        const F run = carry + x;
+        const unsigned got = __ballot_sync(0xffffffffu, jj < shi && run >= pick);
+        if (got) {
+            result = b0 + __ffs(got) - 1;
+            break;
+        }
+        carry += __shfl_sync(0xffffffffu, x, 31);
     }
     return result;
 }
@@ -105,17 +119,22 @@ __global__ void k_traceback(BatchDev d, int maxS) {
     const double *u = d.uniforms + I.col0;
     const int L = I.seqlen;
 
-    // prefetch cursor: next column to copy (descending) and its block
+    // prefetch cursor: next column to copy (descending), its tree's fields in registers
     int pcol = L - 1, pblk = I.ntrees - 1;
+    int pS = imax(d.blocks[I.block0 + pblk].S, 1), pstart = d.blocks[I.block0 + pblk].start;
+    long long pcell = d.blocks[I.block0 + pblk].cell0;
     auto issue = [&]() {
         if (pcol >= 0) {
-            const BlockDev &B = d.blocks[I.block0 + pblk];
-            const int Sm = imax(B.S, 1);
-            const F *src = tab.fw + B.cell0 + (size_t)(pcol - B.start) * Sm;
+            const F *src = tab.fw + pcell + (size_t)(pcol - pstart) * pS;
             F *dst = ring + (size_t)(pcol % DEPTH) * maxS;
-            for (int j = lane; j < Sm; j += 32) cp_async(dst + j, src + j, sizeof(F));
+            for (int j = lane; j < pS; j += 32) cp_async(dst + j, src + j, sizeof(F));
             pcol--;
-            if (pblk > 0 && pcol < B.start) pblk--;
+            if (pblk > 0 && pcol < pstart) {
+                pblk--;
+                pS = imax(d.blocks[I.block0 + pblk].S, 1);
+                pstart = d.blocks[I.block0 + pblk].start;
+                pcell = d.blocks[I.block0 + pblk].cell0;
+            }
         }
         cp_commit();  // one group per column, empty ones included
     };
@@ -138,9 +157,9 @@ __global__ void k_traceback(BatchDev d, int maxS) {
     {
         cp_wait<DEPTH - 1>();
         __syncwarp();
-        const BlockDev &B = d.blocks[I.block0 + I.ntrees - 1];
+        const int Slast = d.blocks[I.block0 + I.ntrees - 1].S;
         const F *c = ring + (size_t)(col % DEPTH) * maxS;
-        const int x = warp_sample<F>(imax(B.S, 1), uni(col), [&](int j) { return c[j]; });
+        const int x = warp_sample<F>(imax(Slast, 1), uni(col), [&](int j) { return c[j]; });
         if (lane == 0) path[col] = x;
         state = x;
         __syncwarp();
@@ -148,7 +167,7 @@ __global__ void k_traceback(BatchDev d, int maxS) {
     }
     for (int bi = I.ntrees - 1; bi >= 0; bi--) {
         const int blk = I.block0 + bi;
-        const BlockDev &B = d.blocks[blk];
+        const BlockDev B = d.blocks[blk];
         const int S = B.S, Sm = imax(S, 1);
         // stage the tree's state times/nodes and tmatrix
         for (int j = lane; j < S; j += 32) {
@@ -176,7 +195,7 @@ __global__ void k_traceback(BatchDev d, int maxS) {
                         const F tmab = tmS[stime[j] * MAXT + sk.time];
                         F t = tmab;
                         if (snode[j] == sk.node) {
-                            t = tab.same(row + (j - sk.j1), tmab);
+                            t = tab.same(row + (long long)(j - sk.j1) * sk.m, tmab);
                             if (j == k) t += stay;
                         }
                         trans[j] = t;

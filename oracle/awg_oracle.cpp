@@ -1446,8 +1446,8 @@ int oracle_debug_tables(const oracle_problem *p, double *tm_out, double *gts_out
             int m = 0;
             while (k + m < S && blk.states.node[k + m] == v) m++;
             const int t0 = blk.states.time[k];
-            for (int x = 0; x < m; x++)
-                for (int y = 0; y < m; y++)
+            for (int y = 0; y < m; y++)      // source-major: entry (x, y) at y * m + x
+                for (int x = 0; x < m; x++)
                     gts_out[goff++] = blk.tm.get_time(t0 + y, t0 + x, t.age[v], blk.tm.minage, true);
             k += m;
         }

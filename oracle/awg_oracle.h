@@ -58,8 +58,9 @@ int oracle_block_terms(const oracle_problem *p, double *out_terms, int *out_mina
 int oracle_emissions(const oracle_problem *p, double *emit);
 
 /* The tables of the GPU table kernel, same layouts (for kernel-level checks): tmatrix
- * [ntrees][T-1][T-1]; same-branch rows get_time(a, b_k, c_k, minage, true) for a over the
- * times of k's node, nodes in index order, [sum over trees of sum over nodes of m^2];
+ * [ntrees][T-1][T-1]; same-branch entries get_time(a_y, b_x, c, minage, true) of each node
+ * (states x, y of the node, nodes in index order), entry (x, y) at y * m + x,
+ * [sum over trees of sum over nodes of m^2];
  * invariant-site emissions [sum over trees of max(S,1)]; column-0 prior [max(S0,1)]. */
 int oracle_debug_tables(const oracle_problem *p, double *tm, double *gts, double *inv,
                         double *prior);

@@ -73,6 +73,8 @@ PROTOTYPES = [
     ("awg_problem_cells", C.c_longlong, [C.POINTER(AwgProblem)]),
     ("awg_run_batch", C.c_int, [C.POINTER(AwgProblem), C.POINTER(AwgOutputs), C.c_int,
                                 C.c_int]),
+    ("awg_forward_static", C.c_int, [C.POINTER(AwgProblem), C.POINTER(AwgOutputs), C.c_int,
+                                     C.c_void_p]),
     ("awg_last_error", C.c_char_p, []),
     ("awg_device_name", C.c_int, [C.c_char_p, C.c_int]),
     ("awg_kernel_launches", C.c_longlong, []),

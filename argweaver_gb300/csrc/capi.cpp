@@ -157,6 +157,15 @@ int awg_run_batch(const awg_problem *problems, awg_outputs *outputs, int n, int 
     return rc;
 }
 
+int awg_forward_static(const awg_problem *problem, awg_outputs *output, int precision,
+                       void *stream) {
+    g_err.clear();
+    std::string err;
+    const int rc = awg::run_static(problem, output, precision, (cudaStream_t)stream, err);
+    if (rc != 0) set_error(err);
+    return rc;
+}
+
 awg_local_trees *arghmm_new_trees(int **ptrees, int **ages, int **sprs, int *blocklens,
                                   int ntrees, int nnodes, int start_coord) {
     if (!ptrees || !ages || !sprs || !blocklens || ntrees < 1 || nnodes < 1) {

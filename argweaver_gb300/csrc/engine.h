@@ -2,6 +2,8 @@
 // kernels -> downloads. One engine per process and device; calls are serialised.
 #pragma once
 
+#include <cuda_runtime.h>
+
 #include <string>
 
 #include "argweaver_gb300.h"
@@ -23,5 +25,10 @@ struct RunOptions {
 // Runs a batch; returns 0 or a negative code with err set.
 int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptions &opt,
               std::string &err);
+
+// Forward table and log-likelihood of one problem with every device buffer in a static
+// device array (no allocation); returns 0 or a negative code with err set.
+int run_static(const awg_problem *p, awg_outputs *out, int precision, cudaStream_t s,
+               std::string &err);
 
 }  // namespace awg

@@ -138,6 +138,40 @@ long long awg_problem_cells(const awg_problem *p);
  * Returns 0 on success, a negative code on error (awg_last_error() has the message). */
 int awg_run_batch(const awg_problem *problems, awg_outputs *outputs, int n, int precision);
 
+/* Bytes of device memory awg_forward_static draws all of its buffers from. */
+#define AWG_STATIC_SCRATCH_BYTES (64ull << 20)
+
+/* Forward table and log-likelihood of ONE problem, allocating nothing: no cudaMalloc or
+ * cudaFree, no page-locked host memory, no memory pool. No counterpart in the reference
+ * (its forward pass, arghmm_forward_alg in sample_thread.cpp:887-925, allocates the table
+ * per call); the results equal awg_run_batch's for the same problem and precision.
+ *
+ * For callers that cannot allocate device memory: a process whose device memory belongs
+ * to another allocator (a framework's caching allocator, a per-process memory cap), or a
+ * loop on its own stream that cannot afford cudaFree's implicit device-wide
+ * synchronisation, which awg_run_batch incurs when its arena grows.
+ *
+ * Every device buffer (inputs, tables, forward table, error record) is carved out of one
+ * file-scope device array of AWG_STATIC_SCRATCH_BYTES (64 MiB). A problem whose buffers
+ * exceed it is rejected before any device work: return -5, awg_last_error() gives both
+ * sizes. (FP64, a problem of S states per column and L columns needs a little over 8*S*L
+ * bytes: S = 300 fits about 25,000 columns.)
+ *
+ * Set-up: the first call on each device, with that device current, resolves the array's
+ * device address (cudaGetSymbolAddress, which may load the module that holds it). Make
+ * that first call before any stream capture starts.
+ * Zeroing: only the 16-byte error record has to start at zero, and each call clears it
+ * itself (cudaMemsetAsync). Every other byte of the array is written before it is read.
+ * Concurrency: the array is shared by every call on a device. Calls that overlap in time
+ * (from several host threads, or streams of several threads) race on it and corrupt each
+ * other's results: serialise them. A call returns after its stream has finished its work.
+ *
+ * output: forward (AWG_FP64) or forward32 (AWG_FP32) and loglik may be set, as in
+ * awg_outputs; path and posterior must be NULL. stream: a cudaStream_t, NULL for the
+ * default stream. Returns 0, or a negative code with awg_last_error() set. */
+int awg_forward_static(const awg_problem *problem, awg_outputs *output, int precision,
+                       void *stream);
+
 /* Message of the last error on this thread ("" when none). */
 const char *awg_last_error(void);
 

@@ -19,6 +19,7 @@ def declared_functions():
     text = open(HEADER).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
     text = re.sub(r"//[^\n]*", "", text)
+    text = re.sub(r"^\s*#[^\n]*", "", text, flags=re.M)  # preprocessor lines
     names = []
     for decl in text.split(";"):
         decl = " ".join(decl.split())

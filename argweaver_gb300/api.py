@@ -77,11 +77,12 @@ def run_batch(problems: Sequence[Problem], *, precision: str = "fp64",
     probs = (capi.AwgProblem * n)(*[b.c for b in bound])
     outs = (capi.AwgOutputs * n)()
     results, keep = [], []
+    ncells = np.zeros(n, dtype=np.int64)
+    if lib.awg_problems_cells(probs, n, ncells.ctypes.data) != 0:
+        raise ValueError(capi.last_error())
     for q, b in enumerate(bound):
         r = Result()
-        ncell = lib.awg_problem_cells(C.byref(b.c))
-        if ncell < 0:
-            raise ValueError(capi.last_error())
+        ncell = int(ncells[q])
         o = outs[q]
         if want_forward:
             r.forward = np.empty(ncell, dtype=np.float32 if fp32 else np.float64)

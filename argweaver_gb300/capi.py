@@ -71,6 +71,7 @@ PROTOTYPES = [
     ("delete_double_matrix", None, [c_double_pp, C.c_int]),
     ("delete_forward_matrix", None, [c_double_pp, C.c_int]),
     ("awg_problem_cells", C.c_longlong, [C.POINTER(AwgProblem)]),
+    ("awg_problems_cells", C.c_int, [C.POINTER(AwgProblem), C.c_int, C.c_void_p]),
     ("awg_run_batch", C.c_int, [C.POINTER(AwgProblem), C.POINTER(AwgOutputs), C.c_int,
                                 C.c_int]),
     ("awg_forward_static", C.c_int, [C.POINTER(AwgProblem), C.POINTER(AwgOutputs), C.c_int,

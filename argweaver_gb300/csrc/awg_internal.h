@@ -72,6 +72,8 @@ struct StateInfo {
 struct BatchDev {
     int ninst, nblocks, maxS, maxT, maxnodes, maxM;
     const InstDev *inst;
+    const int *order;            // [ninst] or NULL: CTA x of a per-instance kernel runs
+                                 // instance order[x] (largest work first)
     BlockDev *blocks;
     const double *model;         // [ninst * MODEL_STRIDE]
     const int4 *nodes;           // {parent, child0, child1, age} per tree node
@@ -117,6 +119,11 @@ struct BatchDev {
 
 // Records the first failure (code, instance, block, column); later ones are dropped.
 #if defined(__CUDACC__)
+// Instance run by this CTA of a per-instance kernel.
+__device__ __forceinline__ int cta_instance(const BatchDev &d) {
+    return d.order ? d.order[blockIdx.x] : (int)blockIdx.x;
+}
+
 __device__ inline void report_error(int *err, int code, int inst, int blk, int col) {
     if (atomicCAS(err, 0, code) == 0) {
         err[1] = inst;

@@ -74,7 +74,8 @@ template <typename F>
 __global__ void k_backward(BatchDev d, int maxS, double *bw_out) {
     extern __shared__ double dyn_d[];
     const BTab<F> tab(d);
-    const InstDev I = d.inst[blockIdx.x];
+    const int qi = cta_instance(d);
+    const InstDev I = d.inst[qi];
     const int T = I.T;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int nwarps = blockDim.x >> 5;

@@ -92,7 +92,7 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
     if (!fp32 && opt.precision != AWG_FP64) { err = "precision must be AWG_FP64 or AWG_FP32"; return -1; }
 
     HostPlan plan;
-    if (!build_plan(probs, n, plan, err)) return -1;
+    if (!plan_layout(probs, n, plan, err, true)) return -1;
 
     bool want_path = false, want_post = false, want_bw = false;
     for (int q = 0; q < n; q++) {
@@ -123,13 +123,33 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
     const size_t o_inst = in.add(sizeof(InstDev) * plan.ninst);
     const size_t o_blocks = in.add(sizeof(BlockDev) * plan.nblocks);
     const size_t o_model = in.add(sizeof(double) * plan.model.size());
-    const size_t o_nodes = in.add(sizeof(int) * plan.nodes.size());
-    const size_t o_map = in.add(sizeof(int) * plan.mapping.size());
-    const size_t o_seq = in.add(plan.seqT.size());
-    const size_t o_cls = in.add(plan.colclass.size());
-    const size_t o_cvar = in.add(sizeof(int) * plan.colvar.size());
+    const size_t o_nodes = in.add(sizeof(int) * 4 * (size_t)plan.total_nodes);
+    const size_t o_map = in.add(sizeof(int) * (size_t)std::max(plan.total_map, 1LL));
+    const size_t o_seq = in.add((size_t)std::max(plan.total_seq, 1LL));
+    const size_t o_cls = in.add((size_t)plan.total_cols);
+    const size_t o_cvar = in.add(sizeof(int) * (size_t)plan.total_cols);
+    const size_t o_order = in.add(sizeof(int) * plan.ninst);
     const size_t o_u = in.add(want_path ? sizeof(double) * COLS : 0);
     const size_t in_bytes = in.total;
+
+    if (in_bytes > E.host_cap) {
+        if (E.host) cudaFreeHost(E.host);
+        E.host = nullptr;
+        E.host_cap = 0;
+        const size_t cap = in_bytes + in_bytes / 8;
+        CK(cudaMallocHost(&E.host, cap));
+        E.host_cap = cap;
+    }
+
+    // ---------------- stage inputs
+    char *h = E.host;
+    // per-node, per-column and sequence arrays straight into the staging buffer
+    plan_fill(probs, n, plan, PlanDst{(int *)(h + o_nodes), (int *)(h + o_map),
+                                      (uint8_t *)(h + o_seq), (uint8_t *)(h + o_cls),
+                                      (int *)(h + o_cvar)});
+    memcpy(h + o_inst, plan.inst.data(), sizeof(InstDev) * plan.ninst);
+    memcpy(h + o_blocks, plan.blocks.data(), sizeof(BlockDev) * plan.nblocks);
+    memcpy(h + o_model, plan.model.data(), sizeof(double) * plan.model.size());
 
     Layout w;  // work region follows the inputs
     w.total = in_bytes;
@@ -177,25 +197,20 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
         CK(cudaMalloc(&E.dev, cap));
         E.dev_cap = cap;
     }
-    if (in_bytes > E.host_cap) {
-        if (E.host) cudaFreeHost(E.host);
-        E.host = nullptr;
-        E.host_cap = 0;
-        const size_t cap = in_bytes + in_bytes / 8;
-        CK(cudaMallocHost(&E.host, cap));
-        E.host_cap = cap;
-    }
 
-    // ---------------- stage inputs
-    char *h = E.host;
-    memcpy(h + o_inst, plan.inst.data(), sizeof(InstDev) * plan.ninst);
-    memcpy(h + o_blocks, plan.blocks.data(), sizeof(BlockDev) * plan.nblocks);
-    memcpy(h + o_model, plan.model.data(), sizeof(double) * plan.model.size());
-    memcpy(h + o_nodes, plan.nodes.data(), sizeof(int) * plan.nodes.size());
-    memcpy(h + o_map, plan.mapping.data(), sizeof(int) * plan.mapping.size());
-    memcpy(h + o_seq, plan.seqT.data(), plan.seqT.size());
-    memcpy(h + o_cls, plan.colclass.data(), plan.colclass.size());
-    memcpy(h + o_cvar, plan.colvar.data(), sizeof(int) * plan.colvar.size());
+    {
+        // per-instance kernels take the largest instances first: their time is a chain of
+        // columns, so the batch ends when its longest chain does
+        int *ord = (int *)(h + o_order);
+        std::vector<long long> cost(plan.ninst);
+        for (int q = 0; q < plan.ninst; q++) {
+            const long long cells =
+                (q + 1 < plan.ninst ? plan.inst[q + 1].cell0 : plan.total_cells) - plan.inst[q].cell0;
+            cost[q] = 256LL * plan.inst[q].seqlen + cells;
+            ord[q] = q;
+        }
+        std::stable_sort(ord, ord + plan.ninst, [&](int a, int b) { return cost[a] > cost[b]; });
+    }
     if (want_path) {
         double *u = (double *)(h + o_u);
         for (int q = 0; q < n; q++) {
@@ -216,6 +231,7 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
     d.maxnodes = plan.maxnodes;
     d.maxM = plan.maxM;
     d.inst = (const InstDev *)(D + o_inst);
+    d.order = (const int *)(D + o_order);
     d.blocks = (BlockDev *)(D + o_blocks);
     d.model = (const double *)(D + o_model);
     d.nodes = (const int4 *)(D + o_nodes);

@@ -139,11 +139,24 @@ long long awg_problem_cells(const awg_problem *p) {
     g_err.clear();
     awg::HostPlan plan;
     std::string err;
-    if (!p || !awg::build_plan(p, 1, plan, err)) {
+    if (!p || !awg::plan_layout(p, 1, plan, err, true)) {
         set_error(err.empty() ? "NULL problem" : err);
         return -1;
     }
     return plan.total_cells;
+}
+
+int awg_problems_cells(const awg_problem *problems, int n, long long *cells) {
+    g_err.clear();
+    awg::HostPlan plan;
+    std::string err;
+    if (!problems || !cells || !awg::plan_layout(problems, n, plan, err, false)) {
+        set_error(err.empty() ? "NULL argument" : err);
+        return -1;
+    }
+    for (int q = 0; q < n; q++)
+        cells[q] = (q + 1 < n ? plan.inst[q + 1].cell0 : plan.total_cells) - plan.inst[q].cell0;
+    return 0;
 }
 
 int awg_run_batch(const awg_problem *problems, awg_outputs *outputs, int n, int precision) {

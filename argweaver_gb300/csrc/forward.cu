@@ -32,6 +32,8 @@
 
 #include <cuda_runtime.h>
 
+#include <cstdlib>
+
 #include "kernels.h"
 
 namespace awg {
@@ -105,7 +107,8 @@ template <typename F>
 __global__ void __launch_bounds__(512) k_forward(BatchDev d, int maxS, int maxM, int t2_in_smem) {
     extern __shared__ double dyn_d[];
     const Tab<F> tab(d);
-    const InstDev I = d.inst[blockIdx.x];
+    const int qi = cta_instance(d);
+    const InstDev I = d.inst[qi];
     const int T = I.T, NB = T - 1;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int NT = blockDim.x, NW = NT >> 5;
@@ -262,7 +265,7 @@ __global__ void __launch_bounds__(512) k_forward(BatchDev d, int maxS, int maxM,
             const F *cur = col + c * maxS;
             if (tid == 0) {
                 acc.add((double)norm);
-                if (!(norm > F(0))) report_error(d.err, ERR_ZERO_NORM, blockIdx.x, bi, B.start + i - 1);
+                if (!(norm > F(0))) report_error(d.err, ERR_ZERO_NORM, qi, bi, B.start + i - 1);
             }
             // finalise column i-1: normalised into the table (the instance's column 0
             // keeps the unnormalised prior, as the reference's table does)
@@ -330,7 +333,288 @@ __global__ void __launch_bounds__(512) k_forward(BatchDev d, int maxS, int maxM,
     }
     if (tid == 0 && d.lnl) {
         acc.flush();
-        d.lnl[blockIdx.x] = acc.lnl;
+        d.lnl[qi] = acc.lnl;
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// Register-resident variant for trees of up to KPT * blockDim.x states.
+//
+// Thread t owns states k = t + q * NT (q < KPT) of every tree, in state order, so lanes
+// holding one node's states read the same neighbours and consecutive same-branch entries
+// (no bank conflicts). The state's time, node span, row offset, time-sorted rank and
+// invariant emission stay in registers for the tree's columns, and the next variant
+// column's emissions are loaded a column ahead. Per column, two CTA barriers:
+//   A  column i-1 complete in state order and time-sorted; warps sum the time bins
+//      (bin b a contiguous range of the sorted copy: lane-strided loads, butterfly sum)
+//   B  every warp forms tf[a] = sum_b tm[b][a] * bin[b] in lane a, lane 31 (ones) the norm;
+//      column i-1 / norm goes to HBM and column i of the owned states is computed
+// Every sum has an order fixed by the tree alone, so results do not depend on the block
+// size or on the other problems of the batch.
+template <typename F, int KPT>
+__global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int maxM, int t2_in_smem) {
+    extern __shared__ double dyn_d[];
+    const Tab<F> tab(d);
+    const int qi = cta_instance(d);
+    const InstDev I = d.inst[qi];
+    const int T = I.T, NB = T - 1;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int NT = blockDim.x, NW = NT >> 5;
+
+    F *col = (F *)dyn_d;                       // [2][maxS] columns in state order
+    F *colT = col + 2 * maxS;                  // [maxS] newest column, time-sorted
+    F *t2s = colT + maxS;                      // [maxM] same-branch entries of the block
+    __shared__ F tmS[MAXT * MAXT];             // [b][a] tmatrix; column 31 holds ones
+    __shared__ F bins[MAXT];
+    __shared__ int bptr[MAXT + 1];
+
+    LogAcc acc;
+    int c = 0;                                 // buffer holding the current column
+
+    for (int bi = 0; bi < I.ntrees; bi++) {
+        const int blk = I.block0 + bi;
+        const BlockDev &B = d.blocks[blk];
+        const int S = B.S, len = B.len;
+        F *fw = tab.fw + B.cell0;
+
+        if (S == 0) {
+            // fully specified tree: one state that carries over (sample_thread.cpp:201-206)
+            F v;
+            if (bi == 0) {
+                v = fw[0];
+                if (tid == 0) col[c * maxS] = v;
+            } else {
+                const int2 src = d.srcs[blk];
+                const int *gp = d.gptr + B.gptr0;
+                const int *gi = d.gidx + B.prev_state0;
+                const F *dp = tab.dprob + B.prev_state0;
+                const F *rr = tab.rrow + B.state0;
+                const F *cr = tab.crow + B.state0;
+                F part = 0;
+                if (tid < 32) {
+                    for (int p = gp[0] + lane; p < gp[1]; p += 32) part += col[c * maxS + gi[p]] * dp[gi[p]];
+                    part = warp_sum(part);
+                }
+                if (tid == 0) {
+                    if (src.x != -1 && rr[0] > F(0)) part += col[c * maxS + src.x] * rr[0];
+                    if (src.y != -1 && cr[0] > F(0)) part += col[c * maxS + src.y] * cr[0];
+                    acc.add((double)part);
+                    col[c * maxS] = F(1);
+                    fw[0] = F(1);
+                }
+                v = F(1);
+            }
+            for (int i = 1 + tid; i < len; i += NT) fw[i] = v;
+            __syncthreads();
+            continue;
+        }
+
+        // ---- stage the tree: tmatrix, bins, owned states
+        const long long s0 = B.state0;
+        const F *tmg = tab.tm + (size_t)blk * MAXT * MAXT;
+        for (int e = tid; e < NB * MAXT; e += NT) {
+            const int a = e & (MAXT - 1);
+            tmS[e] = a == MAXT - 1 ? F(1) : tmg[e];
+        }
+        for (int a = tid; a <= MAXT; a += NT) bptr[a] = d.bt_ptr[(size_t)blk * (MAXT + 1) + a];
+        int st_time[KPT], st_j1[KPT], st_m[KPT], st_off[KPT], st_rank[KPT];
+        F st_inv[KPT], st_rs[KPT], x_own[KPT], e_next[KPT];
+#pragma unroll
+        for (int q = 0; q < KPT; q++) {
+            const int k = tid + q * NT;
+            const bool valid = k < S;
+            const StateInfo si = d.sinfo[s0 + (valid ? k : 0)];
+            st_time[q] = si.time;
+            st_j1[q] = si.j1;
+            st_m[q] = valid ? si.m : 0;
+            st_off[q] = d.t2off[s0 + (valid ? k : 0)];
+            st_inv[q] = tab.inv[s0 + (valid ? k : 0)];
+            st_rs[q] = Tab<F>::split ? (F)tab.rstay[(size_t)blk * MAXT + si.time] : F(0);
+            x_own[q] = F(0);
+            e_next[q] = F(0);
+        }
+        // time-sorted rank of each state: bt_perm lists the states of each time in order
+        for (int p = tid; p < S; p += NT) col[(c ^ 1) * maxS + d.bt_perm[s0 + p]] = (F)p;
+        __syncthreads();  // tmS, bptr, ranks (parked in the free column buffer)
+#pragma unroll
+        for (int q = 0; q < KPT; q++) {
+            const int k = tid + q * NT;
+            st_rank[q] = k < S ? (int)col[(c ^ 1) * maxS + k] : 0;
+        }
+        if (t2_in_smem) {
+#pragma unroll
+            for (int q = 0; q < KPT; q++) {
+                const int k = tid + q * NT;
+                if (k >= S) continue;
+                const int m = st_m[q], off = st_off[q];
+                const int a0 = st_time[q] - (k - st_j1[q]);
+                for (int y = 0; y < m; y++)
+                    t2s[off + y * m] = tab.t2(B.t2_0 + off + y * m, tmS[(a0 + y) * MAXT + st_time[q]]);
+            }
+        }
+        const uint8_t *cls = d.colclass + I.col0 + B.start;
+        const int *cvar = d.colvar + I.col0 + B.start;
+        const F *var = tab.var + B.var0;
+        const double lner = Tab<F>::split ? tab.lneref[blk] : 0.0;
+        int ccache = 0, vcache = 0, cbase = -32;
+        auto colinfo = [&](int i, uint8_t &ci, int &vi) {
+            if (i - cbase >= 32) {
+                cbase = i;
+                const int q = i + lane;
+                ccache = q < len ? cls[q] : 0;
+                vcache = q < len ? cvar[q] : 0;
+            }
+            ci = (uint8_t)__shfl_sync(0xffffffffu, ccache, i - cbase);
+            vi = __shfl_sync(0xffffffffu, vcache, i - cbase);
+        };
+        auto emit = [&](F s, uint8_t ci, int vrow, int q, bool prefetched) -> F {
+            if (ci == COL_MASKED) return s;
+            if (ci == COL_INVARIANT) return Tab<F>::split ? s - s * st_inv[q] : s * st_inv[q];
+            return s * (prefetched ? e_next[q] : var[(size_t)vrow * S + tid + q * NT]);
+        };
+        auto prefetch = [&](int i) {  // emissions of column i, if variant
+            uint8_t c1;
+            int v1;
+            colinfo(i, c1, v1);
+            if (c1 == COL_VARIANT)
+#pragma unroll
+                for (int q = 0; q < KPT; q++)
+                    if (tid + q * NT < S) e_next[q] = var[(size_t)v1 * S + tid + q * NT];
+        };
+        __syncthreads();  // t2s; the rank scratch is read
+
+        // ---- first column of the block
+        if (bi == 0) {
+#pragma unroll
+            for (int q = 0; q < KPT; q++) {
+                const int k = tid + q * NT;
+                if (k >= S) continue;
+                const F v = fw[k];  // priors (K1)
+                col[c * maxS + k] = v;
+                colT[st_rank[q]] = v;
+                x_own[q] = v;
+            }
+        } else {
+            const int2 src = d.srcs[blk];
+            const int *gp = d.gptr + B.gptr0;
+            const int *gi = d.gidx + B.prev_state0;
+            const F *dp = tab.dprob + B.prev_state0;
+            const F *rr = tab.rrow + s0;
+            const F *cr = tab.crow + s0;
+            uint8_t c0;
+            int v0;
+            colinfo(0, c0, v0);
+            const F *prev = col + c * maxS;
+#pragma unroll
+            for (int q = 0; q < KPT; q++) {
+                const int k = tid + q * NT;
+                if (k >= S) continue;
+                F s = 0;
+                for (int p = gp[k]; p < gp[k + 1]; p++) {
+                    const int j = gi[p];
+                    s += prev[j] * dp[j];
+                }
+                if (src.x != -1 && rr[k] > F(0)) s += prev[src.x] * rr[k];
+                if (src.y != -1 && cr[k] > F(0)) s += prev[src.y] * cr[k];
+                const F v = emit(s, c0, v0, q, false);
+                col[(c ^ 1) * maxS + k] = v;
+                colT[st_rank[q]] = v;
+                x_own[q] = v;
+            }
+            if (Tab<F>::split && tid == 0 && c0 == COL_INVARIANT) acc.extra += lner;
+            c ^= 1;
+        }
+        if (len > 1) prefetch(1);
+
+        // ---- remaining columns; iteration i also finalises column i-1
+        for (int i = 1; i <= len; i++) {
+            __syncthreads();  // A: column i-1 complete
+            for (int b = warp; b < NB; b += NW) {
+                F s = 0;
+                for (int p = bptr[b] + lane; p < bptr[b + 1]; p += 32) s += colT[p];
+                s = warp_sum(s);
+                if (lane == 0) bins[b] = s;
+            }
+            __syncthreads();  // B: bins of column i-1
+            F tf = 0;
+            for (int b = 0; b < NB; b++) tf += tmS[b * MAXT + lane] * bins[b];
+            const F norm = __shfl_sync(0xffffffffu, tf, MAXT - 1);
+            const F inv_norm = F(1) / norm;
+            const F *cur = col + c * maxS;
+            if (tid == 0) {
+                acc.add((double)norm);
+                if (!(norm > F(0))) report_error(d.err, ERR_ZERO_NORM, qi, bi, B.start + i - 1);
+            }
+            // finalise column i-1: normalised into the table (the instance's column 0
+            // keeps the unnormalised prior, as the reference's table does)
+            const bool write_prev = !(bi == 0 && i == 1);
+            F *outp = fw + (size_t)(i - 1) * S;
+            if (i == len) {
+#pragma unroll
+                for (int q = 0; q < KPT; q++) {
+                    const int k = tid + q * NT;
+                    if (k >= S) continue;
+                    const F v = x_own[q] * inv_norm;
+                    if (write_prev) outp[k] = v;
+                    col[c * maxS + k] = v;  // normalised, for the next switch
+                }
+                break;
+            }
+            uint8_t ci;
+            int vrow;
+            colinfo(i, ci, vrow);
+            F *nxt = col + (c ^ 1) * maxS;
+            if (Tab<F>::split && tid == 0 && ci == COL_INVARIANT) acc.extra += lner;
+#pragma unroll
+            for (int q = 0; q < KPT; q++) {
+                const F tfb = __shfl_sync(0xffffffffu, tf, st_time[q]);
+                const int k = tid + q * NT;
+                if (k >= S) continue;
+                const F xk = x_own[q];
+                if (write_prev) outp[k] = xk * inv_norm;
+                const F *nb = cur + st_j1[q];
+                const int m = st_m[q];
+                F s = tfb;
+                if (t2_in_smem) {
+                    // even terms into s, odd into s1, four loads ahead
+                    const F *row = t2s + st_off[q];
+                    int y = 0;
+                    F s1 = 0;
+                    for (; y + 3 < m; y += 4) {
+                        const F r0 = row[0], r1 = row[m], r2 = row[2 * m], r3 = row[3 * m];
+                        const F n0 = nb[y], n1 = nb[y + 1], n2 = nb[y + 2], n3 = nb[y + 3];
+                        s += r0 * n0;
+                        s1 += r1 * n1;
+                        s += r2 * n2;
+                        s1 += r3 * n3;
+                        row += 4 * m;
+                    }
+                    for (; y + 1 < m; y += 2) {
+                        s += row[0] * nb[y];
+                        s1 += row[m] * nb[y + 1];
+                        row += 2 * m;
+                    }
+                    if (y < m) s += row[0] * nb[y];
+                    s += s1;
+                } else {
+                    const int a0 = st_time[q] - (k - st_j1[q]);
+                    for (int y = 0; y < m; y++)
+                        s += tab.t2(B.t2_0 + st_off[q] + y * m, tmS[(a0 + y) * MAXT + st_time[q]]) * nb[y];
+                }
+                if (Tab<F>::split) s = xk + (s - st_rs[q] * xk);  // stay term apart
+                const F v = emit(s, ci, vrow, q, true) * inv_norm;
+                nxt[k] = v;
+                colT[st_rank[q]] = v;
+                x_own[q] = v;
+            }
+            if (i + 1 < len) prefetch(i + 1);
+            c ^= 1;
+        }
+        __syncthreads();
+    }
+    if (tid == 0 && d.lnl) {
+        acc.flush();
+        d.lnl[qi] = acc.lnl;
     }
 }
 
@@ -347,7 +631,7 @@ size_t forward_smem(int maxS, int maxM) {
 }
 
 template <typename F>
-void launch(const BatchDev &d, int maxM, cudaStream_t s) {
+void launch_old(const BatchDev &d, int maxM, cudaStream_t s) {
     const int maxS = imax(d.maxS, 1);
     maxM = imax(maxM, 1);
     // stage the same-branch rows in shared memory when they fit, else read them from L1/L2
@@ -363,11 +647,55 @@ void launch(const BatchDev &d, int maxM, cudaStream_t s) {
     note_launch();
 }
 
+template <typename F, int KPT>
+void launch_reg(const BatchDev &d, int nt, cudaStream_t s) {
+    const int maxS = imax(d.maxS, 1);
+    int maxM = imax(d.maxM, 1);
+    auto bytes = [&](int m) { return (size_t)(3 * maxS + m) * sizeof(F) + 16; };
+    const int t2_in_smem = bytes(maxM) <= 200 * 1024;
+    if (!t2_in_smem) maxM = 1;
+    const size_t smem = bytes(maxM);
+    static size_t configured = 0;
+    if (smem > configured) {
+        if (cudaFuncSetAttribute(k_forward_reg<F, KPT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem) != cudaSuccess)
+            return;
+        configured = smem;
+    }
+    k_forward_reg<F, KPT><<<d.ninst, nt, smem, s>>>(d, maxS, maxM, t2_in_smem);
+    note_launch();
+}
+
+// States per thread of the register variant (1, 2, 4 or 8; AWG_FORWARD_KPT overrides it
+// for tuning); the CTA then has ceil(maxS / KPT) threads rounded up to whole warps.
+int reg_kpt(int maxS) {
+    static const int env = [] {
+        const char *e = getenv("AWG_FORWARD_KPT");
+        return e ? atoi(e) : 0;
+    }();
+    int k = (env == 1 || env == 2 || env == 4 || env == 8) ? env
+          : maxS <= 64 ? 1 : maxS <= 1024 ? 2 : maxS <= 2048 ? 4 : 8;
+    while (k < 8 && (maxS + k - 1) / k > 512) k *= 2;
+    return k;
+}
+
+template <typename F>
+void launch(const BatchDev &d, cudaStream_t s) {
+    const int maxS = imax(d.maxS, 1);
+    const int kpt = reg_kpt(maxS);
+    const int nt = imax(32, ((maxS + kpt - 1) / kpt + 31) / 32 * 32);
+    if (nt > 512) launch_old<F>(d, d.maxM, s);
+    else if (kpt == 1) launch_reg<F, 1>(d, nt, s);
+    else if (kpt == 2) launch_reg<F, 2>(d, nt, s);
+    else if (kpt == 4) launch_reg<F, 4>(d, nt, s);
+    else launch_reg<F, 8>(d, nt, s);
+}
+
 }  // namespace
 
 void launch_forward(const BatchDev &d, bool fp32, cudaStream_t s) {
-    if (fp32) launch<float>(d, d.maxM, s);
-    else launch<double>(d, d.maxM, s);
+    if (fp32) launch<float>(d, s);
+    else launch<double>(d, s);
 }
 
 }  // namespace awg

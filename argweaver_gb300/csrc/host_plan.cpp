@@ -28,14 +28,12 @@ bool valid_base(char c) {
 }
 
 struct TreeScratch {
-    std::vector<int> c0, c1;
-    std::vector<char> ignore;
+    int c0[MAXNODES], c1[MAXNODES];
 };
 
 // Children in index order (set_ptree), root, optional child[0] override of the root.
 bool make_children(const int *parent, int n, int rc0, TreeScratch &ts, int &root) {
-    ts.c0.assign(n, -1);
-    ts.c1.assign(n, -1);
+    for (int i = 0; i < n; i++) ts.c0[i] = ts.c1[i] = -1;
     root = -1;
     for (int i = 0; i < n; i++) {
         int p = parent[i];
@@ -98,22 +96,32 @@ int count_states(const int *parent, const int *age, int n, int T, bool internal,
     return (int)S;
 }
 
-bool build_plan(const awg_problem *probs, int n, HostPlan &plan, std::string &err) {
-    plan = HostPlan();
-    if (n <= 0) { err = "empty batch"; return false; }
-    plan.ninst = n;
-    plan.inst.resize(n);
+namespace {
 
-    // pass 1: validation and sizes
-    std::vector<std::vector<int>> S_of(n), M_of(n);
-    long long nblocks = 0;
-    for (int q = 0; q < n; q++) {
-        const awg_problem &p = probs[q];
+// Runs f(q) for q < n on up to hardware_concurrency threads, problems interleaved.
+template <typename Fn>
+void parallel_for(int n, Fn f) {
+    const int nthreads = std::max(1, std::min<int>(n, (int)std::thread::hardware_concurrency()));
+    if (nthreads <= 1 || n < 4) {
+        for (int q = 0; q < n; q++) f(q);
+        return;
+    }
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nthreads; t++)
+        pool.emplace_back([&, t]() {
+            for (int q = t; q < n; q += nthreads) f(q);
+        });
+    for (auto &th : pool) th.join();
+}
+
+// Validation and per-tree state counts of one problem; "" or the failure.
+std::string check_problem(const awg_problem &p, int q, bool check_seqs, std::vector<int> &S_of,
+                          std::vector<int> &M_of) {
+    {
         char buf[256];
         auto fail = [&](const char *what) {
             snprintf(buf, sizeof(buf), "problem %d: %s", q, what);
-            err = buf;
-            return false;
+            return std::string(buf);
         };
         if (p.ntrees < 1) return fail("ntrees < 1");
         if (p.nnodes < 1 || p.nnodes > MAXNODES) return fail("nnodes out of range [1, 1024]");
@@ -135,8 +143,8 @@ bool build_plan(const awg_problem *probs, int n, HostPlan &plan, std::string &er
             if (!(p.times[i] >= 0) || !(p.popsizes[i] > 0)) return fail("bad times or popsizes");
         for (int i = 1; i < p.ntimes; i++)
             if (!(p.times[i] > p.times[i - 1])) return fail("times not increasing");
-        S_of[q].resize(p.ntrees);
-        M_of[q].resize(p.ntrees);
+        S_of.resize(p.ntrees);
+        M_of.resize(p.ntrees);
         for (int b = 0; b < p.ntrees; b++) {
             const int *par = p.ptrees + (size_t)b * p.nnodes;
             const int *age = p.ages + (size_t)b * p.nnodes;
@@ -149,10 +157,8 @@ bool build_plan(const awg_problem *probs, int n, HostPlan &plan, std::string &er
             int S = count_states(par, age, p.nnodes, p.ntimes, p.internal != 0, p.minage, rc0, &M);
             if (S < 0) return fail("malformed tree (parents/children)");
             if (!p.internal && S == 0) return fail("external tree with no states");
-            S_of[q][b] = S;
-            M_of[q][b] = M;
-            plan.maxS = std::max(plan.maxS, S);
-            plan.maxM = std::max(plan.maxM, M);
+            S_of[b] = S;
+            M_of[b] = M;
             if (b > 0) {
                 const int *s = p.sprs + (size_t)b * 4;
                 if (s[0] < 0 || s[0] >= p.nnodes || s[2] < 0 || s[2] >= p.nnodes)
@@ -163,8 +169,34 @@ bool build_plan(const awg_problem *probs, int n, HostPlan &plan, std::string &er
                 if (prev[s[0]] < 0) return fail("SPR recombines the root");
             }
         }
-        for (long long c = 0; c < (long long)nemit * p.seqlen; c++)
-            if (!valid_base(p.seqs[c])) return fail("sequence byte outside A,C,G,T,N");
+        if (check_seqs)
+            for (long long c = 0; c < (long long)nemit * p.seqlen; c++)
+                if (!valid_base(p.seqs[c])) return fail("sequence byte outside A,C,G,T,N");
+    }
+    return std::string();
+}
+
+}  // namespace
+
+bool plan_layout(const awg_problem *probs, int n, HostPlan &plan, std::string &err,
+                 bool check_seqs) {
+    plan = HostPlan();
+    if (n <= 0) { err = "empty batch"; return false; }
+    plan.ninst = n;
+    plan.inst.resize(n);
+
+    // pass 1: validation and sizes, problems in parallel
+    std::vector<std::vector<int>> S_of(n), M_of(n);
+    std::vector<std::string> errs(n);
+    parallel_for(n, [&](int q) { errs[q] = check_problem(probs[q], q, check_seqs, S_of[q], M_of[q]); });
+    long long nblocks = 0;
+    for (int q = 0; q < n; q++) {
+        if (!errs[q].empty()) { err = errs[q]; return false; }
+        const awg_problem &p = probs[q];
+        for (int b = 0; b < p.ntrees; b++) {
+            plan.maxS = std::max(plan.maxS, S_of[q][b]);
+            plan.maxM = std::max(plan.maxM, M_of[q][b]);
+        }
         nblocks += p.ntrees;
         plan.maxnodes = std::max(plan.maxnodes, p.nnodes);
         plan.maxT = std::max(plan.maxT, p.ntimes);
@@ -240,15 +272,11 @@ bool build_plan(const awg_problem *probs, int n, HostPlan &plan, std::string &er
     }
     plan.total_cells = cell; plan.total_cols = col; plan.total_states = st;
     plan.total_M = t2; plan.total_nodes = nodes; plan.total_map = map; plan.total_seq = seq;
+    return true;
+}
 
-    // pass 3: arrays (instances in parallel)
-    plan.nodes.assign((size_t)nodes * 4, -1);
-    plan.mapping.assign((size_t)std::max(map, 1LL), -1);
-    plan.seqT.assign((size_t)std::max(seq, 1LL), 'N');
-    plan.colclass.assign((size_t)col, COL_INVARIANT);
-    plan.colvar.assign((size_t)col, -1);
-    std::vector<std::string> errs(n);
-
+void plan_fill(const awg_problem *probs, int n, HostPlan &plan, const PlanDst &out) {
+    // pass 3: arrays (instances in parallel), straight into the caller's buffers
     auto fill = [&](int q) {
         const awg_problem &p = probs[q];
         const InstDev &I = plan.inst[q];
@@ -261,7 +289,7 @@ bool build_plan(const awg_problem *probs, int n, HostPlan &plan, std::string &er
             int rc0 = p.root_child0 ? p.root_child0[b] : -1;
             make_children(par, p.nnodes, rc0, ts, root);
             B.root = root;
-            int *nd = &plan.nodes[(size_t)B.nodes0 * 4];
+            int *nd = out.nodes + (size_t)B.nodes0 * 4;
             for (int i = 0; i < p.nnodes; i++) {
                 nd[4 * i + 0] = par[i];
                 nd[4 * i + 1] = ts.c0[i];
@@ -270,7 +298,7 @@ bool build_plan(const awg_problem *probs, int n, HostPlan &plan, std::string &er
             }
             if (b > 0) {
                 B.prev_root = plan.blocks[I.block0 + b - 1].root;
-                int *mp = &plan.mapping[B.map0];
+                int *mp = out.mapping + B.map0;
                 if (p.mapping) {
                     memcpy(mp, p.mapping + (size_t)b * p.nnodes, sizeof(int) * p.nnodes);
                 } else {
@@ -284,13 +312,17 @@ bool build_plan(const awg_problem *probs, int n, HostPlan &plan, std::string &er
         }
         // column-major sequences and column classes
         const int ns = I.nseqs, L = p.seqlen;
-        uint8_t *dst = &plan.seqT[I.seq0];
-        for (int r = 0; r < ns; r++) {
-            const char *row = p.seqs + (size_t)r * L;
-            for (int i = 0; i < L; i++) dst[(size_t)i * ns + r] = (uint8_t)row[i];
+        uint8_t *dst = out.seqT + I.seq0;
+        constexpr int TILE = 256;  // columns per tile: the tile's rows stay in cache
+        for (int i0 = 0; i0 < L; i0 += TILE) {
+            const int i1 = std::min(L, i0 + TILE);
+            for (int r = 0; r < ns; r++) {
+                const char *row = p.seqs + (size_t)r * L;
+                for (int i = i0; i < i1; i++) dst[(size_t)i * ns + r] = (uint8_t)row[i];
+            }
         }
-        uint8_t *cls = &plan.colclass[I.col0];
-        int *cv = &plan.colvar[I.col0];
+        uint8_t *cls = out.colclass + I.col0;
+        int *cv = out.colvar + I.col0;
         for (int b = 0; b < p.ntrees; b++) {
             BlockDev &B = plan.blocks[I.block0 + b];
             int nv = 0;
@@ -301,6 +333,7 @@ bool build_plan(const awg_problem *probs, int n, HostPlan &plan, std::string &er
                     if (c[r] != c[0]) { inv = false; break; }
                 if (inv) {
                     cls[i] = (c[0] == 'N') ? COL_MASKED : COL_INVARIANT;
+                    cv[i] = -1;
                 } else {
                     cls[i] = COL_VARIANT;
                     cv[i] = nv++;
@@ -309,23 +342,24 @@ bool build_plan(const awg_problem *probs, int n, HostPlan &plan, std::string &er
             B.nvar = nv;
         }
     };
-    const int nthreads = std::max(1, std::min<int>(n, (int)std::thread::hardware_concurrency()));
-    if (nthreads <= 1 || n < 4) {
-        for (int q = 0; q < n; q++) fill(q);
-    } else {
-        std::vector<std::thread> pool;
-        for (int t = 0; t < nthreads; t++)
-            pool.emplace_back([&, t]() {
-                for (int q = t; q < n; q += nthreads) fill(q);
-            });
-        for (auto &th : pool) th.join();
-    }
+    parallel_for(n, fill);
     long long var = 0;
     for (auto &B : plan.blocks) {
         B.var0 = var;
         var += (long long)B.nvar * std::max(B.S, 1);
     }
     plan.total_var = var;
+}
+
+bool build_plan(const awg_problem *probs, int n, HostPlan &plan, std::string &err) {
+    if (!plan_layout(probs, n, plan, err, true)) return false;
+    plan.nodes.assign((size_t)plan.total_nodes * 4, -1);
+    plan.mapping.assign((size_t)std::max(plan.total_map, 1LL), -1);
+    plan.seqT.assign((size_t)std::max(plan.total_seq, 1LL), 'N');
+    plan.colclass.assign((size_t)plan.total_cols, COL_INVARIANT);
+    plan.colvar.assign((size_t)plan.total_cols, -1);
+    plan_fill(probs, n, plan, PlanDst{plan.nodes.data(), plan.mapping.data(), plan.seqT.data(),
+                                      plan.colclass.data(), plan.colvar.data()});
     return true;
 }
 

@@ -29,7 +29,22 @@ struct HostPlan {
     std::vector<int> colvar;
 };
 
-// Validates the problems and fills the plan; returns false with a message on bad input.
+// Where plan_fill writes the per-node, per-column and sequence arrays.
+struct PlanDst {
+    int *nodes;          // [total_nodes * 4]
+    int *mapping;        // [max(total_map, 1)]
+    uint8_t *seqT;       // [total_seq]
+    uint8_t *colclass;   // [total_cols]
+    int *colvar;         // [total_cols]
+};
+
+// Passes 1-2: validates the problems (sequence bytes too when check_seqs) and sizes the
+// plan: instances, blocks and every offset except the variant-emission ones.
+bool plan_layout(const awg_problem *probs, int n, HostPlan &plan, std::string &err,
+                 bool check_seqs);
+// Pass 3: fills the arrays into dst, the trees' roots and the variant-emission offsets.
+void plan_fill(const awg_problem *probs, int n, HostPlan &plan, const PlanDst &dst);
+// Both, into the plan's own vectors; returns false with a message on bad input.
 bool build_plan(const awg_problem *probs, int n, HostPlan &plan, std::string &err);
 
 // Number of states of a local tree given by parent/age arrays (states.cpp:53-199).

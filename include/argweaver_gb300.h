@@ -133,6 +133,11 @@ typedef struct {
  * or -1 when the problem is invalid. */
 long long awg_problem_cells(const awg_problem *p);
 
+/* awg_problem_cells of n problems at once into cells[n], the problems checked in parallel
+ * (all but their sequence bytes, which awg_run_batch checks). Returns 0, or -1 with
+ * awg_last_error() naming the first invalid problem. */
+int awg_problems_cells(const awg_problem *problems, int n, long long *cells);
+
 /* Run forward (+ traceback when path is wanted, + backward when posterior is wanted) for
  * n problems in one batch on the current device. precision: AWG_FP64 or AWG_FP32.
  * Returns 0 on success, a negative code on error (awg_last_error() has the message). */

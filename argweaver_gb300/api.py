@@ -137,12 +137,14 @@ def kernel_launches() -> int:
     return int(capi.load().awg_kernel_launches())
 
 
-def set_timing(on: bool) -> None:
-    capi.load().awg_set_timing(1 if on else 0)
+def set_timing(mode) -> None:
+    """0/False: off; 1/True: device times of the overlapped schedule (compute total);
+    2: kernels one phase after another, each phase timed."""
+    capi.load().awg_set_timing(int(mode))
 
 
 def last_timings() -> dict:
-    out = np.zeros(7, dtype=np.float64)
+    out = np.zeros(8, dtype=np.float64)
     capi.load().awg_last_timings(out.ctypes.data_as(capi.c_double_p))
-    keys = ["h2d", "tables", "emit", "forward", "traceback", "backward", "d2h"]
+    keys = ["h2d", "tables", "emit", "forward", "traceback", "backward", "d2h", "compute"]
     return {k: float(v) for k, v in zip(keys, out)}

@@ -74,6 +74,8 @@ struct BatchDev {
     const InstDev *inst;
     const int *order;            // [ninst] or NULL: CTA x of a per-instance kernel runs
                                  // instance order[x] (largest work first)
+    const int *blkmap;           // [nblocks] or NULL: CTA x of a per-tree kernel builds
+                                 // tree blkmap[x]
     BlockDev *blocks;
     const double *model;         // [ninst * MODEL_STRIDE]
     const int4 *nodes;           // {parent, child0, child1, age} per tree node
@@ -122,6 +124,11 @@ struct BatchDev {
 // Instance run by this CTA of a per-instance kernel.
 __device__ __forceinline__ int cta_instance(const BatchDev &d) {
     return d.order ? d.order[blockIdx.x] : (int)blockIdx.x;
+}
+
+// Local tree built by this CTA of a per-tree kernel.
+__device__ __forceinline__ int cta_block(const BatchDev &d) {
+    return d.blkmap ? d.blkmap[blockIdx.x] : (int)blockIdx.x;
 }
 
 __device__ inline void report_error(int *err, int code, int inst, int blk, int col) {

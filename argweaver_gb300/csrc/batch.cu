@@ -27,21 +27,26 @@ std::atomic<long long> g_launches{0};
 
 struct Timings {
     float plan_ms = 0, h2d_ms = 0, tables_ms = 0, emit_ms = 0, forward_ms = 0,
-          traceback_ms = 0, backward_ms = 0, d2h_ms = 0;
+          traceback_ms = 0, backward_ms = 0, d2h_ms = 0, compute_ms = 0;
 };
+
+constexpr int MAXG = 12;  // instance groups of the pipelined schedule
 
 struct Engine {
     std::mutex mu;
     bool init = false;
     int device = -1;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;       // uploads, per-tree kernels, downloads
+    cudaStream_t gstream[MAXG] = {};     // per group: forward, traceback, backward (high
+                                         // priority, so their CTAs are placed first)
     char *dev = nullptr;
     size_t dev_cap = 0;
     char *host = nullptr;
     size_t host_cap = 0;
     cudaEvent_t ev[8];
+    cudaEvent_t gev[2 * MAXG + 2];
     Timings last;
-    bool timing = false;
+    int timing = 0;  // 0 off; 1 on (overlapped schedule: one compute time); 2 serial phases
 };
 
 Engine &engine() {
@@ -110,7 +115,13 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
         }
         CK(cudaGetDevice(&E.device));
         CK(cudaStreamCreateWithFlags(&E.stream, cudaStreamNonBlocking));
+        int lo = 0, hi = 0;
+        CK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+        for (int g = 0; g < MAXG; g++)
+            CK(cudaStreamCreateWithPriority(&E.gstream[g], cudaStreamNonBlocking, hi));
         for (int i = 0; i < 8; i++) CK(cudaEventCreate(&E.ev[i]));
+        for (int i = 0; i < 2 * MAXG + 2; i++)
+            CK(cudaEventCreateWithFlags(&E.gev[i], cudaEventDisableTiming));
         E.init = true;
     }
     cudaStream_t s = E.stream;
@@ -129,6 +140,7 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
     const size_t o_cls = in.add((size_t)plan.total_cols);
     const size_t o_cvar = in.add(sizeof(int) * (size_t)plan.total_cols);
     const size_t o_order = in.add(sizeof(int) * plan.ninst);
+    const size_t o_blkmap = in.add(sizeof(int) * plan.nblocks);
     const size_t o_u = in.add(want_path ? sizeof(double) * COLS : 0);
     const size_t in_bytes = in.total;
 
@@ -210,6 +222,13 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
             ord[q] = q;
         }
         std::stable_sort(ord, ord + plan.ninst, [&](int a, int b) { return cost[a] > cost[b]; });
+        // trees of the instances in that order, so a group of instances is a range
+        int *bm = (int *)(h + o_blkmap);
+        int k = 0;
+        for (int j = 0; j < plan.ninst; j++) {
+            const InstDev &I = plan.inst[ord[j]];
+            for (int b = 0; b < I.ntrees; b++) bm[k++] = I.block0 + b;
+        }
     }
     if (want_path) {
         double *u = (double *)(h + o_u);
@@ -274,78 +293,129 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
     d.path = want_path ? (int *)(D + o_path) : nullptr;
     d.err = (int *)(D + o_err);
 
-    const bool T = E.timing;
+    // Schedule. Serial: per-tree kernels over the batch, then per-instance kernels. Pipelined
+    // (larger batches): instances in groups, largest first; a group's per-tree kernels run
+    // on the main stream and its forward (then traceback/backward) on high-priority streams
+    // as soon as they are done, so the long per-instance chains start early and the
+    // per-tree work of later groups fills the SMs they leave idle.
+    const bool pipelined = n >= 16 && !opt.tables_only && !opt.priors && E.timing != 2;
+    const bool T = E.timing != 0;
     if (T) CK(cudaEventRecord(E.ev[0], s));
     CK(cudaMemcpyAsync(D, h, in_bytes, cudaMemcpyHostToDevice, s));
     CK(cudaMemsetAsync(d.err, 0, 4 * sizeof(int), s));
     if (T) CK(cudaEventRecord(E.ev[1], s));
-    launch_tables(d, fp32, s);
-    CKL("table kernel");
-    if (opt.priors) {
-        for (int q = 0; q < n; q++) {
-            if (!opt.priors[q]) continue;
-            const InstDev &I = plan.inst[q];
-            const int S0 = std::max(plan.blocks[I.block0].S, 1);
-            if (fp32) {
-                std::vector<float> tmp(opt.priors[q], opt.priors[q] + S0);
-                CK(cudaMemcpyAsync(d.fw32 + I.cell0, tmp.data(), sizeof(float) * S0,
-                                   cudaMemcpyHostToDevice, s));
-                CK(cudaStreamSynchronize(s));
-            } else {
-                CK(cudaMemcpyAsync(d.fw64 + I.cell0, opt.priors[q], sizeof(double) * S0,
-                                   cudaMemcpyHostToDevice, s));
+    if (pipelined) {
+        // group sizes n/32, doubling; the last takes the rest
+        int bounds[MAXG + 1];
+        int ng = 0, q0 = 0, sz = std::max(1, n / 32);
+        bounds[0] = 0;
+        while (q0 < n) {
+            const int q1 = (ng == MAXG - 1) ? n : std::min(n, q0 + sz);
+            bounds[++ng] = q1;
+            q0 = q1;
+            sz *= 2;
+        }
+        const int *ord = (const int *)(h + o_order);
+        int boff = 0;
+        for (int g = 0; g < ng; g++) {
+            BatchDev dg = d;
+            int nb = 0;
+            for (int j = bounds[g]; j < bounds[g + 1]; j++) nb += plan.inst[ord[j]].ntrees;
+            dg.order = d.order + bounds[g];
+            dg.ninst = bounds[g + 1] - bounds[g];
+            dg.blkmap = (const int *)(D + o_blkmap) + boff;
+            dg.nblocks = nb;
+            boff += nb;
+            launch_tables(dg, fp32, s);
+            CKL("table kernel");
+            launch_varemit(dg, fp32, s);
+            CKL("emission kernel");
+            cudaStream_t gs = E.gstream[g];
+            CK(cudaEventRecord(E.gev[2 * g], s));
+            CK(cudaStreamWaitEvent(gs, E.gev[2 * g], 0));
+            launch_forward(dg, fp32, gs);
+            CKL("forward kernel");
+            if (want_path) {
+                launch_traceback(dg, fp32, gs);
+                CKL("traceback kernel");
+            }
+            if (want_post) {
+                launch_backward(dg, fp32, want_bw ? (double *)(D + o_bw) : nullptr, gs);
+                CKL("backward kernel");
+            }
+            CK(cudaEventRecord(E.gev[2 * g + 1], gs));
+        }
+        for (int g = 0; g < ng; g++) CK(cudaStreamWaitEvent(s, E.gev[2 * g + 1], 0));
+        if (T) CK(cudaEventRecord(E.ev[6], s));
+    } else {
+        launch_tables(d, fp32, s);
+        CKL("table kernel");
+        if (opt.priors) {
+            for (int q = 0; q < n; q++) {
+                if (!opt.priors[q]) continue;
+                const InstDev &I = plan.inst[q];
+                const int S0 = std::max(plan.blocks[I.block0].S, 1);
+                if (fp32) {
+                    std::vector<float> tmp(opt.priors[q], opt.priors[q] + S0);
+                    CK(cudaMemcpyAsync(d.fw32 + I.cell0, tmp.data(), sizeof(float) * S0,
+                                       cudaMemcpyHostToDevice, s));
+                    CK(cudaStreamSynchronize(s));
+                } else {
+                    CK(cudaMemcpyAsync(d.fw64 + I.cell0, opt.priors[q], sizeof(double) * S0,
+                                       cudaMemcpyHostToDevice, s));
+                }
             }
         }
-    }
-    if (opt.tables_only) {
-        const InstDev &I = plan.inst[0];
-        std::vector<double> tmall((size_t)plan.nblocks * MAXT * MAXT);
-        CK(cudaMemcpyAsync(tmall.data(), d.tm, sizeof(double) * tmall.size(),
-                           cudaMemcpyDeviceToHost, s));
-        if (opt.dbg_gts)
-            CK(cudaMemcpyAsync(opt.dbg_gts, d.gts, sizeof(double) * plan.total_M,
+        if (opt.tables_only) {
+            const InstDev &I = plan.inst[0];
+            std::vector<double> tmall((size_t)plan.nblocks * MAXT * MAXT);
+            CK(cudaMemcpyAsync(tmall.data(), d.tm, sizeof(double) * tmall.size(),
                                cudaMemcpyDeviceToHost, s));
-        if (opt.dbg_inv)
-            CK(cudaMemcpyAsync(opt.dbg_inv, d.inv_lk, sizeof(double) * plan.total_states,
-                               cudaMemcpyDeviceToHost, s));
-        if (opt.dbg_btptr)
-            CK(cudaMemcpyAsync(opt.dbg_btptr, d.bt_ptr, sizeof(int) * plan.nblocks * (MAXT + 1),
-                               cudaMemcpyDeviceToHost, s));
-        if (opt.dbg_btperm)
-            CK(cudaMemcpyAsync(opt.dbg_btperm, d.bt_perm, sizeof(int) * plan.total_states,
-                               cudaMemcpyDeviceToHost, s));
-        if (opt.dbg_prior)
-            CK(cudaMemcpyAsync(opt.dbg_prior, d.fw64 + I.cell0,
-                               sizeof(double) * std::max(plan.blocks[0].S, 1),
-                               cudaMemcpyDeviceToHost, s));
-        CK(cudaStreamSynchronize(s));
-        if (opt.dbg_tm) {
-            const int T = I.T;
-            for (int b = 0; b < plan.nblocks; b++)
-                for (int a = 0; a < T - 1; a++)
-                    for (int c = 0; c < T - 1; c++)
-                        opt.dbg_tm[((size_t)b * (T - 1) + a) * (T - 1) + c] =
-                            tmall[((size_t)b * MAXT + a) * MAXT + c];
+            if (opt.dbg_gts)
+                CK(cudaMemcpyAsync(opt.dbg_gts, d.gts, sizeof(double) * plan.total_M,
+                                   cudaMemcpyDeviceToHost, s));
+            if (opt.dbg_inv)
+                CK(cudaMemcpyAsync(opt.dbg_inv, d.inv_lk, sizeof(double) * plan.total_states,
+                                   cudaMemcpyDeviceToHost, s));
+            if (opt.dbg_btptr)
+                CK(cudaMemcpyAsync(opt.dbg_btptr, d.bt_ptr, sizeof(int) * plan.nblocks * (MAXT + 1),
+                                   cudaMemcpyDeviceToHost, s));
+            if (opt.dbg_btperm)
+                CK(cudaMemcpyAsync(opt.dbg_btperm, d.bt_perm, sizeof(int) * plan.total_states,
+                                   cudaMemcpyDeviceToHost, s));
+            if (opt.dbg_prior)
+                CK(cudaMemcpyAsync(opt.dbg_prior, d.fw64 + I.cell0,
+                                   sizeof(double) * std::max(plan.blocks[0].S, 1),
+                                   cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            if (opt.dbg_tm) {
+                const int T = I.T;
+                for (int b = 0; b < plan.nblocks; b++)
+                    for (int a = 0; a < T - 1; a++)
+                        for (int c = 0; c < T - 1; c++)
+                            opt.dbg_tm[((size_t)b * (T - 1) + a) * (T - 1) + c] =
+                                tmall[((size_t)b * MAXT + a) * MAXT + c];
+            }
+            return 0;
         }
-        return 0;
+        if (T) CK(cudaEventRecord(E.ev[2], s));
+        launch_varemit(d, fp32, s);
+        CKL("emission kernel");
+        if (T) CK(cudaEventRecord(E.ev[3], s));
+        launch_forward(d, fp32, s);
+        CKL("forward kernel");
+        if (T) CK(cudaEventRecord(E.ev[4], s));
+        if (want_path) {
+            launch_traceback(d, fp32, s);
+            CKL("traceback kernel");
+        }
+        if (T) CK(cudaEventRecord(E.ev[5], s));
+        if (want_post) {
+            launch_backward(d, fp32, want_bw ? (double *)(D + o_bw) : nullptr, s);
+            CKL("backward kernel");
+        }
+        if (T) CK(cudaEventRecord(E.ev[6], s));
     }
-    if (T) CK(cudaEventRecord(E.ev[2], s));
-    launch_varemit(d, fp32, s);
-    CKL("emission kernel");
-    if (T) CK(cudaEventRecord(E.ev[3], s));
-    launch_forward(d, fp32, s);
-    CKL("forward kernel");
-    if (T) CK(cudaEventRecord(E.ev[4], s));
-    if (want_path) {
-        launch_traceback(d, fp32, s);
-        CKL("traceback kernel");
-    }
-    if (T) CK(cudaEventRecord(E.ev[5], s));
-    if (want_post) {
-        launch_backward(d, fp32, want_bw ? (double *)(D + o_bw) : nullptr, s);
-        CKL("backward kernel");
-    }
-    if (T) CK(cudaEventRecord(E.ev[6], s));
 
     // ---------------- downloads
     for (int q = 0; q < n; q++) {
@@ -375,11 +445,17 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
     if (T) CK(cudaEventRecord(E.ev[7], s));
     CK(cudaStreamSynchronize(s));
     if (T) {
-        float ms[7];
-        for (int i = 0; i < 7; i++) cudaEventElapsedTime(&ms[i], E.ev[i], E.ev[i + 1]);
-        E.last.h2d_ms = ms[0]; E.last.tables_ms = ms[1]; E.last.emit_ms = ms[2];
-        E.last.forward_ms = ms[3]; E.last.traceback_ms = ms[4]; E.last.backward_ms = ms[5];
-        E.last.d2h_ms = ms[6];
+        Timings t;
+        cudaEventElapsedTime(&t.h2d_ms, E.ev[0], E.ev[1]);
+        cudaEventElapsedTime(&t.compute_ms, E.ev[1], E.ev[6]);
+        cudaEventElapsedTime(&t.d2h_ms, E.ev[6], E.ev[7]);
+        if (!pipelined) {
+            float ms[5];
+            for (int i = 0; i < 5; i++) cudaEventElapsedTime(&ms[i], E.ev[i + 1], E.ev[i + 2]);
+            t.tables_ms = ms[0]; t.emit_ms = ms[1]; t.forward_ms = ms[2];
+            t.traceback_ms = ms[3]; t.backward_ms = ms[4];
+        }
+        E.last = t;
     }
     if (dev_err[0] != 0) {
         static const char *what[] = {"", "switch from a fully specified tree found no state",
@@ -399,14 +475,16 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
 
 extern "C" {
 
-// Per-phase device times (ms) of the last batch when timing is on: h2d, tables, emissions,
-// forward, traceback, backward, d2h.
-void awg_set_timing(int on) { awg::engine().timing = on != 0; }
-void awg_last_timings(double *out7) {
+// Device times (ms) of the last batch when timing is on: h2d, tables, emissions, forward,
+// traceback, backward, d2h, compute (the kernels from the end of the upload to the start of
+// the downloads). mode 1 keeps the overlapped schedule (phases read 0 when it ran); mode 2
+// runs the kernels one phase after another to time each.
+void awg_set_timing(int mode) { awg::engine().timing = mode; }
+void awg_last_timings(double *out8) {
     const auto &t = awg::engine().last;
-    const float v[7] = {t.h2d_ms, t.tables_ms, t.emit_ms, t.forward_ms, t.traceback_ms,
-                        t.backward_ms, t.d2h_ms};
-    for (int i = 0; i < 7; i++) out7[i] = v[i];
+    const float v[8] = {t.h2d_ms, t.tables_ms, t.emit_ms, t.forward_ms, t.traceback_ms,
+                        t.backward_ms, t.d2h_ms, t.compute_ms};
+    for (int i = 0; i < 8; i++) out8[i] = v[i];
 }
 
 }  // extern "C"

@@ -38,13 +38,18 @@ struct Terms {
     double CT[MAXT][MAXT];        // [b][c] exp(lnG4[b] + lnB[c-1]), c > 0
 };
 
-// Fill the exponential tables (the same arguments get_time exponentiates).
+// Fill the exponential tables (the same arguments get_time exponentiates), only the
+// entries get_time reads: E2B/E2N[a][b] for a < b (the a < b branch), CT[b][c] for
+// 1 <= c <= b (c_term and minage_term: a state's time is at least its node's age and minage).
 __device__ void exp_tables(Terms &t, int T) {
     for (int e = threadIdx.x; e < (T - 1) * (T - 1); e += blockDim.x) {
         const int a = e / (T - 1), b = e % (T - 1);
-        t.E2B[a][b] = exp(t.lnE2[b] + t.lnB[a]);
-        t.E2N[a][b] = exp(t.lnE2[b] + t.lnNegG1[a]);
-        t.CT[a][b + 1] = exp(t.lnG4[a] + t.lnB[b]);  // [b=a][c=b+1]
+        if (a < b) {
+            t.E2B[a][b] = exp(t.lnE2[b] + t.lnB[a]);
+            t.E2N[a][b] = exp(t.lnE2[b] + t.lnNegG1[a]);
+        } else if (b < a) {
+            t.CT[a][b + 1] = exp(t.lnG4[a] + t.lnB[b]);  // [b=a][c=b+1]
+        }
     }
     for (int b = threadIdx.x; b < T - 1; b += blockDim.x)
         t.EB[b] = b > 0 ? exp(t.lnE2[b] + t.lnB[b - 1]) : 0.0;
@@ -284,7 +289,7 @@ __device__ __forceinline__ double prob_branch(double t, double mu, bool mut) {  
 
 __global__ void __launch_bounds__(TAB_THREADS) k_tables(BatchDev d, int want32) {
     extern __shared__ int4 dyn[];
-    const int blk = blockIdx.x;
+    const int blk = cta_block(d);
     BlockDev &Bg = d.blocks[blk];
     const BlockDev B = Bg;
     const InstDev I = d.inst[B.inst];
@@ -314,6 +319,7 @@ __global__ void __launch_bounds__(TAB_THREADS) k_tables(BatchDev d, int want32) 
     __shared__ double sums2[2 * MAXT + 1], recoals[MAXT];
     __shared__ double sh_treelen, sh_sums, sh_maintreelen, sh_subtreelen, sh_tlmin;
     __shared__ double wmin[TAB_THREADS / 32];
+    __shared__ double tl_tab[2 * MAXT], inv_tab[2 * MAXT], dp_tab[3 * MAXT];
     __shared__ int sh_S, sh_S1, sh_minage, sh_rootage, sh_src[2];
 
     const double *model = d.model + I.model0;
@@ -448,18 +454,42 @@ __global__ void __launch_bounds__(TAB_THREADS) k_tables(BatchDev d, int want32) 
     // same-branch rows: get_time(a, b_k, c_k, minage, true) for the node's times a; a node's
     // m x m block is stored source-major (entry (k, y) at t2off[k] + y * m) so lanes holding
     // consecutive states of one node read consecutive words
-    double *gts = d.gts + B.t2_0;
-    for (int k = tid; k < S; k += blockDim.x) {
-        const StateInfo si = sinfo[k];
-        const int b = si.time, c = cur[si.node].w;
-        const int base = t2off[k];
-        for (int y = 0; y < si.m; y++) {
-            const int a = t0[si.node] + y;
-            const double g = get_time(tr, a, b, c, minage, true);
-            gts[base + y * si.m] = g;
-            if (want32)  // the moving part: the diagonal's no-recombination term is apart
-                d.t2d32[B.t2_0 + base + y * si.m] =
-                    (float)(g - tm[a * MAXT + b] - (a == b ? tr.norecombs[a] : 0.0));
+    if (!want32) {
+        double *gts = d.gts + B.t2_0;
+        for (int k = tid; k < S; k += blockDim.x) {
+            const StateInfo si = sinfo[k];
+            const int b = si.time, c = cur[si.node].w;
+            const int base = t2off[k];
+            for (int y = 0; y < si.m; y++) {
+                const int a = t0[si.node] + y;
+                gts[base + y * si.m] = get_time(tr, a, b, c, minage, true);
+            }
+        }
+    } else {
+        // FP32 path: only the moving part, get_time(a, b, c, true) - get_time(a, b, 0, false)
+        // - [a == b] norecombs[a], which in exact arithmetic is D[a] E[b] (X[a][b] - c_term)
+        // (X the different-node bracket without its minage term); formed from that product
+        // it keeps its relative accuracy where the two get_time values nearly cancel.
+        // X and D[a] E[b] overwrite E2B and E2N, which nothing reads after this point.
+        for (int e = tid; e < (T - 1) * (T - 1); e += blockDim.x) {
+            const int a = e / (T - 1), b = e % (T - 1);
+            const double x = a < b ? tr.E2B[a][b] - tr.E2N[a][b]
+                                   : tr.EB[b] + (a == b ? tr.G3[b] : tr.G2[b]);
+            tr.E2N[a][b] = __dmul_rn(tr.D[a], tr.E[b]);
+            tr.E2B[a][b] = x;
+        }
+        __syncthreads();
+        float *t2d = d.t2d32 + B.t2_0;
+        for (int k = tid; k < S; k += blockDim.x) {
+            const StateInfo si = sinfo[k];
+            const int b = si.time, c = cur[si.node].w;
+            const int base = t2off[k];
+            const double ct = c > 0 ? tr.CT[b][c] : 0.0;
+            for (int y = 0; y < si.m; y++) {
+                const int a = t0[si.node] + y;
+                t2d[base + y * si.m] =
+                    (a < minage || b < minage) ? 0.0f : (float)(tr.E2N[a][b] * (tr.E2B[a][b] - ct));
+            }
         }
     }
 
@@ -528,22 +558,30 @@ __global__ void __launch_bounds__(TAB_THREADS) k_tables(BatchDev d, int want32) 
         const int node1 = internal ? cur[root].y : 0;
         const double time1 = internal ? times[cur[node1].w] : 0.0;
         // tree length seen by each state (emit.cpp:807-816), floored at mintime
-        auto tlen = [&](int k) {
-            const StateInfo si = sinfo[k];
-            const double coal_time = times[si.time];
+        // the tree length depends on the state only through (node == main root, time):
+        // one value per pair, then a lookup per state
+        for (int e = tid; e < 2 * T; e += blockDim.x) {
+            const int t = e % T;
+            const double coal_time = times[t];
             double treelen;
-            if (si.node == mainr)
+            if (e >= T)
                 treelen = sh_maintreelen + sh_subtreelen + fmax(coal_time - time1, mintime) +
                           fmax(coal_time - times[cur[mainr].w], mintime);
             else
                 treelen = sh_maintreelen + sh_subtreelen + fmax(coal_time - time1, mintime);
-            return fmax(treelen, mintime);
+            tl_tab[e] = fmax(treelen, mintime);
+            inv_tab[e] = .25 * exp(-mu * tl_tab[e]);
+        }
+        __syncthreads();
+        auto pair = [&](int k) {
+            const StateInfo si = sinfo[k];
+            return (si.node == mainr ? T : 0) + si.time;
         };
         double lmin = INFINITY;
         for (int k = tid; k < S; k += blockDim.x) {
-            const double tl = tlen(k);
-            inv[k] = .25 * exp(-mu * tl);
-            lmin = fmin(lmin, tl);
+            const int e = pair(k);
+            inv[k] = inv_tab[e];
+            lmin = fmin(lmin, tl_tab[e]);
         }
         if (want32) {
             for (int o = 16; o > 0; o >>= 1) lmin = fmin(lmin, __shfl_xor_sync(0xffffffffu, lmin, o));
@@ -556,8 +594,10 @@ __global__ void __launch_bounds__(TAB_THREADS) k_tables(BatchDev d, int want32) 
                 d.lneref[blk] = S == 0 ? 0.0 : log(.25) - mu * m;
             }
             __syncthreads();
-            for (int k = tid; k < S; k += blockDim.x)
-                d.inv32[B.state0 + k] = (float)(-expm1(-mu * (tlen(k) - sh_tlmin)));
+            for (int e = tid; e < 2 * T; e += blockDim.x)
+                inv_tab[e] = -expm1(-mu * (tl_tab[e] - sh_tlmin));
+            __syncthreads();
+            for (int k = tid; k < S; k += blockDim.x) d.inv32[B.state0 + k] = (float)inv_tab[pair(k)];
         }
         if (S == 0 && tid == 0) {
             inv[0] = 1.0;
@@ -718,25 +758,44 @@ __global__ void __launch_bounds__(TAB_THREADS) k_tables(BatchDev d, int want32) 
         }
         for (int a = tid; a < T; a += blockDim.x) recoals[a] = calc_recoal(c, spr, a, rpa0, false);
         __syncthreads();
-        for (int i = tid; i < S1; i += blockDim.x) {
-            if (determ[i] < 0) continue;
-            if (s1node[i] == spr[0] && s1time[i] > spr[1]) {
-                determprob[i] = calc_recomb_recoal(c, spr, s1node[i], s1time[i], s1time[i]);
-            } else {
-                const int idx = max(min(2 * spr[3] - 1, 2 * s1time[i]), 2 * spr[1]);
-                determprob[i] = calc_recomb(c, spr, s1node[i], s1time[i], c.last_treelen) *
-                                exp(-sh_sums - sums2[idx]) * recoals[s1time[i]];
+        auto dprob = [&](int node, int a) {
+            if (node == spr[0] && a > spr[1]) return calc_recomb_recoal(c, spr, node, a, a);
+            const int idx = max(min(2 * spr[3] - 1, 2 * a), 2 * spr[1]);
+            return calc_recomb(c, spr, node, a, c.last_treelen) * exp(-sh_sums - sums2[idx]) *
+                   recoals[a];
+        };
+        if (!internal) {
+            // external trees: the value depends on the source state only through its time
+            // and whether its node is the root (calc_recomb) or the recombining node above
+            // the recombination (calc_recomb_recoal); one evaluation per case. Node -1
+            // stands for any other node (the external calc_recomb only compares it with the
+            // root; the recombining node is never the root).
+            for (int e = tid; e < 3 * (T - 1); e += blockDim.x) {
+                const int f = e / (T - 1), a = e % (T - 1);
+                const int node = f == 0 ? -1 : f == 1 ? B.prev_root : spr[0];
+                dp_tab[f * MAXT + a] = dprob(node, a);
+            }
+            __syncthreads();
+            for (int i = tid; i < S1; i += blockDim.x) {
+                if (determ[i] < 0) continue;
+                const int node = s1node[i], a = s1time[i];
+                const int f = (node == spr[0] && a > spr[1]) ? 2 : node == B.prev_root ? 1 : 0;
+                determprob[i] = dp_tab[f * MAXT + a];
+            }
+        } else {
+            for (int i = tid; i < S1; i += blockDim.x) {
+                if (determ[i] < 0) continue;
+                determprob[i] = dprob(s1node[i], s1time[i]);
             }
         }
-        // probabilistic sources
+        // probabilistic sources (each state at most once: states are distinct)
+        for (int i = tid; i < S1; i += blockDim.x) {
+            if (s1node[i] == spr[0] && s1time[i] == spr[1]) sh_src[0] = i;
+            else if (s1node[i] == spr[2] && s1time[i] == spr[3]) sh_src[1] = i;
+        }
+        __syncthreads();
         if (tid == 0) {
-            int recombsrc = -1, recoalsrc = -1;
-            for (int i = 0; i < S1; i++) {
-                if (s1node[i] == spr[0] && s1time[i] == spr[1]) recombsrc = i;
-                else if (s1node[i] == spr[2] && s1time[i] == spr[3]) recoalsrc = i;
-            }
-            sh_src[0] = recombsrc;
-            sh_src[1] = recoalsrc;
+            const int recombsrc = sh_src[0];
             if (recombsrc != -1) {  // get_recomb_transition_switch (trans.cpp:278-313)
                 const int parent = prv[spr[0]].x;
                 const int time2 = prv[parent].w;
@@ -775,21 +834,49 @@ __global__ void __launch_bounds__(TAB_THREADS) k_tables(BatchDev d, int want32) 
     }
     __syncthreads();
 
-    // gather lists: sources of every target, ascending (sample_thread.cpp:357-362)
-    if (tid == 0) {
+    // gather lists: sources of every target, ascending (sample_thread.cpp:357-362), by a
+    // counting sort: counts (integer atomics), a scan, then warp 0 places 32 sources at a
+    // time, each after the earlier sources of its target in the same batch of 32
+    {
         const int n1 = imax(S1, 1);
         const int rs = sh_src[0], cs = sh_src[1];
-        d.srcs[blk] = make_int2(rs, cs);
-        for (int k = 0; k <= Sm; k++) gcnt[k] = 0;
-        for (int j = 0; j < n1; j++) {
+        if (tid == 0) d.srcs[blk] = make_int2(rs, cs);
+        for (int k = tid; k <= Sm; k += blockDim.x) gcnt[k] = 0;
+        __syncthreads();
+        for (int j = tid; j < n1; j += blockDim.x) {
             const int k = determ[j];
-            if (j != rs && j != cs && k >= 0) gcnt[k + 1]++;
+            if (j != rs && j != cs && k >= 0) atomicAdd(&gcnt[k + 1], 1);
         }
-        for (int k = 0; k < Sm; k++) gcnt[k + 1] += gcnt[k];
-        for (int k = 0; k <= Sm; k++) gptr[k] = gcnt[k];
-        for (int j = 0; j < n1; j++) {
-            const int k = determ[j];
-            if (j != rs && j != cs && k >= 0) gidx[gcnt[k]++] = j;
+        __syncthreads();
+        if (tid < 32) {
+            const int lane = tid;
+            const int per = (Sm + 1 + 31) / 32;
+            const int lo = imin(lane * per, Sm + 1), hi = imin(lo + per, Sm + 1);
+            int run = 0;
+            for (int i = lo; i < hi; i++) {
+                run += gcnt[i];
+                gcnt[i] = run;
+            }
+            int incl = run;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += v;
+            }
+            for (int i = lo; i < hi; i++) {
+                gcnt[i] += incl - run;  // gcnt[k]: first slot of target k
+                gptr[i] = gcnt[i];
+            }
+            __syncwarp();
+            for (int jb = 0; jb < n1; jb += 32) {
+                const int j = jb + lane;
+                const int k = j < n1 ? determ[j] : -1;
+                const bool ok = j < n1 && j != rs && j != cs && k >= 0;
+                const unsigned peers = __match_any_sync(0xffffffffu, ok ? k : -1 - lane);
+                if (ok) gidx[gcnt[k] + __popc(peers & ((1u << lane) - 1))] = j;
+                __syncwarp();
+                if (ok && lane == 31 - __clz(peers)) gcnt[k] += __popc(peers);
+                __syncwarp();
+            }
         }
     }
     if (want32) {
@@ -815,7 +902,7 @@ __global__ void __launch_bounds__(TAB_THREADS) k_tables(BatchDev d, int want32) 
 template <typename F>
 __global__ void k_varemit(BatchDev d, int nwarps, int maxS) {
     extern __shared__ int4 dyn[];
-    const int blk = blockIdx.x;
+    const int blk = cta_block(d);
     const BlockDev B = d.blocks[blk];
     if (B.nvar == 0 || B.S == 0) return;
     const InstDev I = d.inst[B.inst];

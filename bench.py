@@ -6,11 +6,13 @@ DSMC ARG with k ~ U{8..64} haplotypes (k-1 in the ARG, one re-threaded), L ~ U[1
 1 Mb] at 10 bp per column, ntimes=20, N=1e4, r=1.6e-8, mu=1.8e-8, 0.5% missing calls.
 One step = forward + traceback of the whole batch in FP32 (log scales in FP64).
 
-  value     cells / device time of the step's kernels, inputs resident in HBM
+  value     cells / device time of the step's kernels (upload done, downloads not begun)
   e2e       cells / wall time of the public call awg_run_batch with host buffers: host
-            plan, host->device copy of the inputs, kernels, device->host copy of the paths
-  roofline  forward+traceback kernels: 8 B per cell (FP32 write + read) over their time,
-            against the measured HBM copy bandwidth
+            plan, host->device copy of the inputs, kernels, device->host copy of the paths;
+            p50/p99 of the per-step latency
+  roofline  the forward kernel: 4 B of FP32 table written per cell over its time (phases
+            timed one after another), against the measured HBM copy bandwidth
+  fp64_plain  the drop-in FP64 path, one problem per reference C-ABI call
   cpu_baseline  the CPU port of the reference's algorithm (oracle/) on the host cores,
             one problem per thread, on a bounded sample of the same problems
 
@@ -207,7 +209,7 @@ def main():
         return api.run_batch(problems, precision="fp32", want_forward=False, want_path=True,
                              uniforms=uniforms)
 
-    api.set_timing(True)
+    api.set_timing(1)
     for _ in range(max(args.warmup, 3)):
         step()
     launches0 = api.kernel_launches()
@@ -216,16 +218,12 @@ def main():
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    dev_ms, fwd_ms, tb_ms, wall, phases = [], [], [], [], []
+    dev_ms, wall = [], []
     for _ in range(args.steps):
         t0 = time.perf_counter()
         step()
         wall.append(time.perf_counter() - t0)
-        t = api.last_timings()
-        phases.append(t)
-        dev_ms.append(t["tables"] + t["emit"] + t["forward"] + t["traceback"])
-        fwd_ms.append(t["forward"])
-        tb_ms.append(t["traceback"])
+        dev_ms.append(api.last_timings()["compute"])
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
@@ -241,6 +239,29 @@ def main():
     value = world * cells * args.steps / dev_s
     e2e = world * cells * args.steps / wall_s
 
+    # per-kernel times: the same step with its kernels run one phase after another
+    api.set_timing(2)
+    phases = []
+    for _ in range(2):
+        step()
+        phases.append(api.last_timings())
+    api.set_timing(0)
+    phase_ms = {k: float(np.mean([t[k] for t in phases])) for k in phases[0]}
+
+    # the plain FP64 path: one problem per call through the reference's C ABI
+    # (arghmm_sample_posterior: forward + traceback), smallest problems first, ~3 s
+    from argweaver_gb300 import refapi
+    plain_cells, plain_t, plain_n = 0, 0.0, 0
+    for p in sorted(problems, key=lambda p: p.cells()):
+        t0 = time.perf_counter()
+        refapi.arghmm_sample_posterior(p)
+        plain_t += time.perf_counter() - t0
+        plain_cells += p.cells()
+        plain_n += 1
+        if plain_t > 3.0:
+            break
+    plain = plain_cells / plain_t
+
     # error report outside the timed region: FP32 vs FP64 posteriors on a few problems
     sample = sorted(problems, key=lambda p: p.cells())[:4]
     errs = []
@@ -253,9 +274,11 @@ def main():
     if rank != 0:
         return
     hbm, src = peaks()
-    achieved = cells * 8 / ((sum(fwd_ms) + sum(tb_ms)) / args.steps / 1e3) / 1e9
+    # dominant kernel: the forward pass, 4 B of FP32 table written per cell
+    achieved = cells * 4 / (phase_ms["forward"] / 1e3) / 1e9
     cpu_v, cpu_cells, cpu_dt = cpu_reference(problems, args.cpu_sample_seconds, os.cpu_count() or 1)
     per_inst = sorted(p.cells() for p in problems)
+    lat = np.array(wall) * 1e3
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps,
@@ -269,18 +292,22 @@ def main():
                    "l2": "inputs and tables larger than L2 (129 MB)",
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * wall_s / args.steps},
+                "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * wall_s / args.steps,
+                "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99))},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": None,
-                     "peak_source": src,
-                     "kernels": "forward+traceback, 8 B per cell (FP32 write + read)"},
+                     "frac": achieved / hbm, "traffic": None, "peak_source": src,
+                     "kernel": "forward (k_forward_reg), 4 B of FP32 table written per cell, "
+                               "timed alone (phases run one after another)"},
         "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                          "sample": f"{cpu_cells} cells in {cpu_dt:.1f} s: the same problems, "
                                    "smallest first, one per thread"},
+        "fp64_plain": {"value": plain, "unit": UNIT, "speedup_of_value": value / plain,
+                       "sample": f"{plain_n} smallest problems, one arghmm_sample_posterior "
+                                 "call each (FP64, forward + traceback)"},
         "fp32_vs_fp64_posterior_max_abs_err": max(errs),
         "gpu_launches": launches,
         "clocks": clocks,
-        "phase_ms": {k: float(np.mean([t[k] for t in phases])) for k in phases[0]},
+        "phase_ms": phase_ms,
         "longest_instance_columns": max(p.seqlen for p in problems),
     }
     print(json.dumps(line))

@@ -61,6 +61,7 @@ struct BlockDev {
     long long gptr0;          // offset of the switch gather pointers [max(S,1)+1]
     long long t2_0;           // offset of the same-branch rows
     long long var0;           // offset of the block's variant emission rows
+    long long vrow0;          // index of the block's first variant column among the batch's
 };
 
 // Per-state metadata: node, time, first state of the node (block-relative), node states.
@@ -106,8 +107,12 @@ struct BatchDev {
     //   rstay32  [nblocks * MAXT] 1 - norecombs[b]
     //   inv32    1 - e_k / e_ref for invariant sites, e_ref the block's largest emission
     //   lneref   [nblocks] log(e_ref), added to the log-likelihood per invariant column
+    //   var32    1 - e_k / e_ref for variant columns too, e_ref the column's largest
+    //            emission (formed in FP64: a column that varies only through missing calls
+    //            has emissions equal to a few digits, which FP32 values would lose)
+    //   lnvref   [variant columns] log(e_ref) of each variant column
     float *tm32, *t2d32, *inv32, *var32, *determprob32, *recombrow32, *recoalrow32, *rstay32;
-    double *lneref;
+    double *lneref, *lnvref;
 
     // outputs
     double *fw64;                // forward table (FP64 path)
@@ -150,6 +155,7 @@ enum : int {
     ERR_SMEM_LIMIT = 2,         // a block exceeded the kernel's shared-memory plan
     ERR_ZERO_NORM = 3,          // a forward column summed to zero (reference asserts top > 0)
     ERR_PLAN_MISMATCH = 4,      // device state count disagrees with the host plan
+    ERR_BOUNDS = 5,             // an index derived from the inputs fell outside its array
 };
 
 }  // namespace awg

@@ -40,6 +40,32 @@ template <> struct BTab<float> {
     __device__ float t2(long long idx, float) const { return t2d[idx]; }
 };
 
+// FP32 pair arithmetic for the dominant path of the FP32 backward step (the same reason
+// and transforms as the forward's: the column's fixed point within a tree would otherwise
+// move by the step's rounding over one minus the chain's contraction).
+struct F2 {
+    float hi, lo;
+};
+__device__ __forceinline__ F2 f2_renorm(float a, float b) {  // |a| >= |b|
+    const float s = a + b;
+    return F2{s, b - (s - a)};
+}
+__device__ __forceinline__ F2 f2_keep(F2 x, float r) {  // x * (1 - r), 0 <= r < 1
+    const float t = x.hi * r;
+    const float h = x.hi - t;
+    return f2_renorm(h, ((x.hi - h) - t) + x.lo);
+}
+__device__ __forceinline__ F2 f2_mul(F2 x, float e) {
+    const float p = x.hi * e;
+    return f2_renorm(p, fmaf(x.hi, e, -p) + x.lo * e);
+}
+__device__ __forceinline__ F2 f2_add(F2 x, float s) {
+    const float h = x.hi + s;
+    const float bb = h - x.hi;
+    const float err = (x.hi - (h - bb)) + (s - bb);
+    return f2_renorm(h, err + x.lo);
+}
+
 template <typename F>
 __device__ __forceinline__ F warp_sum(F v) {
 #pragma unroll
@@ -83,7 +109,9 @@ __global__ void k_backward(BatchDev d, int maxS, double *bw_out) {
     F *bwA = (F *)dyn_d;
     F *bwB = bwA + maxS;
     F *g = bwB + maxS;
-    Meta *meta = (Meta *)(g + maxS + (maxS & 1));
+    float *loA = (float *)(g + maxS);           // FP32 path: low parts of bwA / bwB
+    float *loB = loA + maxS;
+    Meta *meta = (Meta *)(((uintptr_t)(loB + maxS) + 15) & ~(uintptr_t)15);
     int *perm = (int *)(meta + maxS);
     F *gs = (F *)(perm + maxS + 1) + 1;     // [maxS / 32 + 1] group sums, 8-byte aligned
     gs = (F *)(((uintptr_t)gs + 7) & ~(uintptr_t)7);
@@ -92,10 +120,14 @@ __global__ void k_backward(BatchDev d, int maxS, double *bw_out) {
     __shared__ int bptr[MAXT + 1];
 
     F *cur = bwA, *nxt = bwB;  // cur: bw of column i+1, nxt: bw of column i
+    float *curlo = loA, *nxtlo = loB;
     {
         const BlockDev &B = d.blocks[I.block0 + I.ntrees - 1];
         const int Sm = imax(B.S, 1);
-        for (int k = tid; k < Sm; k += blockDim.x) cur[k] = F(1) / F(Sm);
+        for (int k = tid; k < Sm; k += blockDim.x) {
+            cur[k] = F(1) / F(Sm);
+            curlo[k] = 0.0f;
+        }
     }
     __syncthreads();
 
@@ -126,7 +158,9 @@ __global__ void k_backward(BatchDev d, int maxS, double *bw_out) {
             const uint8_t c = cls[i];
             if (c == COL_MASKED || S == 0) return x;
             if (c == COL_INVARIANT) return BTab<F>::split ? x - x * inv[k] : x * inv[k];
-            return x * var[(size_t)cvar[i] * S + k];
+            const F e = var[(size_t)cvar[i] * S + k];
+            if (!BTab<F>::split) return x * e;
+            return e >= F(0) ? x - x * e : x * -e;  // FP32: 1 - e_k / e_ref, or -e_k / e_ref
         };
         // posterior of one column from its bw (in `bw`) and fw
         auto posterior = [&](int i, const F *bw) {
@@ -169,15 +203,38 @@ __global__ void k_backward(BatchDev d, int maxS, double *bw_out) {
                         const int k = mj.j1 + x;  // target on the same node, time a0 + x
                         s += tab.t2(B.t2_0 + meta[k].off + y * mj.m, tm[a * MAXT + a0 + x]) * g[k];
                     }
-                    if (BTab<F>::split) s = g[j] + (s - rS[a] * g[j]);  // stay term apart
-                    nxt[j] = s;
+                    if constexpr (BTab<F>::split) {
+                        // pairs: (e * bw) of state j kept with (1 - rs), plus the inflow
+                        F2 gj = F2{cur[j], curlo[j]};
+                        const uint8_t c = cls[i + 1];
+                        if (c == COL_INVARIANT) gj = f2_keep(gj, inv[j]);
+                        else if (c != COL_MASKED) {
+                            const float e = var[(size_t)cvar[i + 1] * S + j];
+                            gj = e >= 0.0f ? f2_keep(gj, e) : f2_mul(gj, -e);
+                        }
+                        const F2 x = f2_add(f2_keep(gj, rS[a]), s);
+                        nxt[j] = x.hi;
+                        nxtlo[j] = x.lo;
+                    } else {
+                        nxt[j] = s;
+                    }
                 }
             }
             const F z = fixed_sum<F>(Sm, [&](int k) { return nxt[k]; }, gs);
-            for (int k = tid; k < Sm; k += blockDim.x) nxt[k] /= z;
+            if constexpr (BTab<F>::split) {
+                const float iz = 1.0f / z;
+                for (int k = tid; k < Sm; k += blockDim.x) {
+                    const F2 x = f2_mul(F2{nxt[k], S == 0 ? 0.0f : nxtlo[k]}, iz);
+                    nxt[k] = x.hi;
+                    nxtlo[k] = x.lo;
+                }
+            } else {
+                for (int k = tid; k < Sm; k += blockDim.x) nxt[k] /= z;
+            }
             __syncthreads();
             posterior(i, nxt);
             F *t = cur; cur = nxt; nxt = t;
+            float *tl = curlo; curlo = nxtlo; nxtlo = tl;
         }
         if (bi > 0) {
             // into the previous tree's last column through the switch matrix
@@ -202,10 +259,14 @@ __global__ void k_backward(BatchDev d, int maxS, double *bw_out) {
                 nxt[j] = s;
             }
             const F z = fixed_sum<F>(n1, [&](int k) { return nxt[k]; }, gs);
-            for (int k = tid; k < n1; k += blockDim.x) nxt[k] /= z;
+            for (int k = tid; k < n1; k += blockDim.x) {
+                nxt[k] /= z;
+                nxtlo[k] = 0.0f;  // the switch starts the previous tree's pairs afresh
+            }
             __syncthreads();
             (void)P;
             F *t = cur; cur = nxt; nxt = t;
+            float *tl = curlo; curlo = nxtlo; nxtlo = tl;
         }
     }
 }
@@ -219,8 +280,9 @@ int backward_threads(int maxS) {
 template <typename F>
 void launch(const BatchDev &d, double *bw_out, cudaStream_t s) {
     const int maxS = imax(d.maxS, 1);
-    const size_t smem = 3 * (size_t)maxS * sizeof(F) + 8 + (size_t)maxS * (sizeof(Meta) + sizeof(int)) +
-                        sizeof(int) + 16 + ((size_t)maxS / 32 + 1) * sizeof(F);
+    const size_t smem = 3 * (size_t)maxS * sizeof(F) + 2 * (size_t)maxS * sizeof(float) + 16 +
+                        (size_t)maxS * (sizeof(Meta) + sizeof(int)) + sizeof(int) + 16 +
+                        ((size_t)maxS / 32 + 1) * sizeof(F);
     static size_t configured = 0;
     if (smem > configured) {  // opt in; static shared memory counts against 48 KB too
         if (cudaFuncSetAttribute(k_backward<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return;

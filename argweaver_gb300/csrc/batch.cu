@@ -181,7 +181,7 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
     const size_t o_gidx = w.add(sizeof(int) * ST);
     const size_t o_var = w.add(sizeof(double) * std::max(plan.total_var, 1LL));
     size_t o_tm32 = 0, o_t2d32 = 0, o_inv32 = 0, o_var32 = 0, o_detp32 = 0, o_rrow32 = 0,
-           o_crow32 = 0, o_rstay32 = 0, o_lneref = 0;
+           o_crow32 = 0, o_rstay32 = 0, o_lneref = 0, o_lnvref = 0;
     if (fp32) {
         o_tm32 = w.add(sizeof(float) * (size_t)plan.nblocks * MAXT * MAXT);
         o_t2d32 = w.add(sizeof(float) * std::max(plan.total_M, 1LL));
@@ -192,6 +192,7 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
         o_crow32 = w.add(sizeof(float) * ST);
         o_rstay32 = w.add(sizeof(float) * (size_t)plan.nblocks * MAXT);
         o_lneref = w.add(sizeof(double) * plan.nblocks);
+        o_lnvref = w.add(sizeof(double) * std::max(plan.total_vcols, 1LL));
     }
     const size_t o_fw = w.add((fp32 ? sizeof(float) : sizeof(double)) * CELLS);
     const size_t o_lnl = w.add(sizeof(double) * plan.ninst);
@@ -283,6 +284,7 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
         d.recoalrow32 = (float *)(D + o_crow32);
         d.rstay32 = (float *)(D + o_rstay32);
         d.lneref = (double *)(D + o_lneref);
+        d.lnvref = (double *)(D + o_lnvref);
         d.fw32 = (float *)(D + o_fw);
     } else {
         d.fw64 = (double *)(D + o_fw);
@@ -460,10 +462,11 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
     if (dev_err[0] != 0) {
         static const char *what[] = {"", "switch from a fully specified tree found no state",
                                      "shared-memory plan exceeded", "a forward column summed to "
-                                     "zero or NaN", "device state count differs from the plan"};
+                                     "zero or NaN", "device state count differs from the plan",
+                                     "an index derived from the inputs is out of range"};
         char buf[256];
         snprintf(buf, sizeof(buf), "device error %d (%s) at problem %d, tree %d, column %d",
-                 dev_err[0], dev_err[0] < 5 ? what[dev_err[0]] : "?", dev_err[1], dev_err[2],
+                 dev_err[0], dev_err[0] < 6 ? what[dev_err[0]] : "?", dev_err[1], dev_err[2],
                  dev_err[3]);
         err = buf;
         return -4;

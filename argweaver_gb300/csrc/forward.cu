@@ -46,7 +46,7 @@ template <> struct Tab<double> {
     static constexpr bool split = false;
     const double *tm, *inv, *var, *dprob, *rrow, *crow, *gts;
     const float *rstay = nullptr;
-    const double *lneref = nullptr;
+    const double *lneref = nullptr, *lnvref = nullptr;
     double *fw;
     __device__ explicit Tab(const BatchDev &d)
         : tm(d.tm), inv(d.inv_lk), var(d.varemit), dprob(d.determprob), rrow(d.recombrow),
@@ -59,11 +59,12 @@ template <> struct Tab<float> {
     static constexpr bool split = true;
     const float *tm, *inv, *var, *dprob, *rrow, *crow, *t2d;
     const float *rstay;
-    const double *lneref;
+    const double *lneref, *lnvref;
     float *fw;
     __device__ explicit Tab(const BatchDev &d)
         : tm(d.tm32), inv(d.inv32), var(d.var32), dprob(d.determprob32), rrow(d.recombrow32),
-          crow(d.recoalrow32), t2d(d.t2d32), rstay(d.rstay32), lneref(d.lneref), fw(d.fw32) {}
+          crow(d.recoalrow32), t2d(d.t2d32), rstay(d.rstay32), lneref(d.lneref), lnvref(d.lnvref),
+          fw(d.fw32) {}
     __device__ float t2(long long idx, float) const { return t2d[idx]; }
 };
 
@@ -236,11 +237,15 @@ __global__ void __launch_bounds__(512) k_forward(BatchDev d, int maxS, int maxM,
                 F v;
                 if (c0 == COL_MASKED) v = s;
                 else if (c0 == COL_INVARIANT) v = Tab<F>::split ? s - s * inv[k] : s * inv[k];
-                else v = s * var[(size_t)v0 * S + k];
+                else {
+                    const F e = var[(size_t)v0 * S + k];
+                    v = !Tab<F>::split ? s * e : e >= F(0) ? s - s * e : s * -e;
+                }
                 col[(c ^ 1) * maxS + k] = v;
                 colT[rank[k]] = v;
             }
             if (Tab<F>::split && tid == 0 && c0 == COL_INVARIANT) acc.extra += lner;
+            if (Tab<F>::split && tid == 0 && c0 == COL_VARIANT) acc.extra += tab.lnvref[B.vrow0 + v0];
             c ^= 1;
         }
 
@@ -284,6 +289,7 @@ __global__ void __launch_bounds__(512) k_forward(BatchDev d, int maxS, int maxM,
             colinfo(i, ci, vrow);
             F *nxt = col + (c ^ 1) * maxS;
             if (Tab<F>::split && tid == 0 && ci == COL_INVARIANT) acc.extra += lner;
+            if (Tab<F>::split && tid == 0 && ci == COL_VARIANT) acc.extra += tab.lnvref[B.vrow0 + vrow];
             for (int k0 = 0; k0 < S; k0 += NT) {
                 const int k = k0 + tid;
                 const bool valid = k < S;
@@ -316,7 +322,10 @@ __global__ void __launch_bounds__(512) k_forward(BatchDev d, int maxS, int maxM,
                         s = xk + (s - rS[mk.time] * xk);  // stay term apart
                         if (ci == COL_MASKED) v = s;
                         else if (ci == COL_INVARIANT) v = s - s * inv[k];
-                        else v = s * var[(size_t)vrow * S + k];
+                        else {
+                            const F e = var[(size_t)vrow * S + k];
+                            v = e >= F(0) ? s - s * e : s * -e;
+                        }
                     } else {
                         const F e = ci == COL_MASKED ? F(1)
                                   : ci == COL_INVARIANT ? inv[k] : var[(size_t)vrow * S + k];
@@ -351,6 +360,40 @@ __global__ void __launch_bounds__(512) k_forward(BatchDev d, int maxS, int maxM,
 //      column i-1 / norm goes to HBM and column i of the owned states is computed
 // Every sum has an order fixed by the tree alone, so results do not depend on the block
 // size or on the other problems of the batch.
+// FP32 pair arithmetic (value = hi + lo, |lo| <= ulp(hi) / 2) for the dominant path of
+// the FP32 forward step. Within a tree the normalised column converges to the fixed point
+// of the step; a rounding error of the step shifts that fixed point by about the error
+// divided by (1 - the chain's contraction), and with stay probabilities near 1 the
+// contraction is slow. The stay, emission and rescaling factors, which carry almost all of
+// a state's mass from column to column, therefore run on pairs built from error-free
+// transforms (Fast2Sum, and products split by FMA); the mass moving in from other states
+// (a few percent) stays plain FP32.
+struct F2 {
+    float hi, lo;
+};
+__device__ __forceinline__ F2 f2_renorm(float a, float b) {  // |a| >= |b|
+    const float s = a + b;
+    return F2{s, b - (s - a)};
+}
+// (x.hi + x.lo) * (1 - r), 0 <= r < 1 (x.lo * r dropped: below the pair's precision)
+__device__ __forceinline__ F2 f2_keep(F2 x, float r) {
+    const float t = x.hi * r;
+    const float h = x.hi - t;
+    return f2_renorm(h, ((x.hi - h) - t) + x.lo);
+}
+// x * e
+__device__ __forceinline__ F2 f2_mul(F2 x, float e) {
+    const float p = x.hi * e;
+    return f2_renorm(p, fmaf(x.hi, e, -p) + x.lo * e);
+}
+// x + s (any magnitudes: two-sum)
+__device__ __forceinline__ F2 f2_add(F2 x, float s) {
+    const float h = x.hi + s;
+    const float bb = h - x.hi;
+    const float err = (x.hi - (h - bb)) + (s - bb);
+    return f2_renorm(h, err + x.lo);
+}
+
 template <typename F, int KPT>
 __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int maxM, int t2_in_smem) {
     extern __shared__ double dyn_d[];
@@ -419,6 +462,7 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
         for (int a = tid; a <= MAXT; a += NT) bptr[a] = d.bt_ptr[(size_t)blk * (MAXT + 1) + a];
         int st_time[KPT], st_j1[KPT], st_m[KPT], st_off[KPT], st_rank[KPT];
         F st_inv[KPT], st_rs[KPT], x_own[KPT], e_next[KPT];
+        float x_lo[KPT];  // FP32 path: low parts of the owned states (pairs x_own + x_lo)
 #pragma unroll
         for (int q = 0; q < KPT; q++) {
             const int k = tid + q * NT;
@@ -431,6 +475,7 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
             st_inv[q] = tab.inv[s0 + (valid ? k : 0)];
             st_rs[q] = Tab<F>::split ? (F)tab.rstay[(size_t)blk * MAXT + si.time] : F(0);
             x_own[q] = F(0);
+            x_lo[q] = 0.0f;
             e_next[q] = F(0);
         }
         // time-sorted rank of each state: bt_perm lists the states of each time in order
@@ -470,7 +515,9 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
         auto emit = [&](F s, uint8_t ci, int vrow, int q, bool prefetched) -> F {
             if (ci == COL_MASKED) return s;
             if (ci == COL_INVARIANT) return Tab<F>::split ? s - s * st_inv[q] : s * st_inv[q];
-            return s * (prefetched ? e_next[q] : var[(size_t)vrow * S + tid + q * NT]);
+            const F e = prefetched ? e_next[q] : var[(size_t)vrow * S + tid + q * NT];
+            if (!Tab<F>::split) return s * e;
+            return e >= F(0) ? s - s * e : s * -e;  // FP32: 1 - e_k / e_ref, or -e_k / e_ref
         };
         auto prefetch = [&](int i) {  // emissions of column i, if variant
             uint8_t c1;
@@ -520,8 +567,10 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
                 col[(c ^ 1) * maxS + k] = v;
                 colT[st_rank[q]] = v;
                 x_own[q] = v;
+                x_lo[q] = 0.0f;
             }
             if (Tab<F>::split && tid == 0 && c0 == COL_INVARIANT) acc.extra += lner;
+            if (Tab<F>::split && tid == 0 && c0 == COL_VARIANT) acc.extra += tab.lnvref[B.vrow0 + v0];
             c ^= 1;
         }
         if (len > 1) prefetch(1);
@@ -565,6 +614,7 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
             colinfo(i, ci, vrow);
             F *nxt = col + (c ^ 1) * maxS;
             if (Tab<F>::split && tid == 0 && ci == COL_INVARIANT) acc.extra += lner;
+            if (Tab<F>::split && tid == 0 && ci == COL_VARIANT) acc.extra += tab.lnvref[B.vrow0 + vrow];
 #pragma unroll
             for (int q = 0; q < KPT; q++) {
                 const F tfb = __shfl_sync(0xffffffffu, tf, st_time[q]);
@@ -601,8 +651,20 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
                     for (int y = 0; y < m; y++)
                         s += tab.t2(B.t2_0 + st_off[q] + y * m, tmS[(a0 + y) * MAXT + st_time[q]]) * nb[y];
                 }
-                if (Tab<F>::split) s = xk + (s - st_rs[q] * xk);  // stay term apart
-                const F v = emit(s, ci, vrow, q, true) * inv_norm;
+                F v;
+                if constexpr (Tab<F>::split) {
+                    // pairs: stay (1 - rs), plus the inflow s, times the emission, rescaled
+                    F2 x = f2_keep(F2{xk, x_lo[q]}, st_rs[q]);
+                    x = f2_add(x, s);
+                    if (ci == COL_INVARIANT) x = f2_keep(x, st_inv[q]);
+                    else if (ci != COL_MASKED)
+                        x = e_next[q] >= 0.0f ? f2_keep(x, e_next[q]) : f2_mul(x, -e_next[q]);
+                    x = f2_mul(x, inv_norm);
+                    v = x.hi;
+                    x_lo[q] = x.lo;
+                } else {
+                    v = emit(s, ci, vrow, q, true) * inv_norm;
+                }
                 nxt[k] = v;
                 colT[st_rank[q]] = v;
                 x_own[q] = v;

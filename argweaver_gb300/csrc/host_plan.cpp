@@ -343,12 +343,15 @@ void plan_fill(const awg_problem *probs, int n, HostPlan &plan, const PlanDst &o
         }
     };
     parallel_for(n, fill);
-    long long var = 0;
+    long long var = 0, vcols = 0;
     for (auto &B : plan.blocks) {
         B.var0 = var;
+        B.vrow0 = vcols;
         var += (long long)B.nvar * std::max(B.S, 1);
+        vcols += B.nvar;
     }
     plan.total_var = var;
+    plan.total_vcols = vcols;
 }
 
 bool build_plan(const awg_problem *probs, int n, HostPlan &plan, std::string &err) {

@@ -16,6 +16,7 @@ struct HostPlan {
     long long total_cols = 0;    // columns of the batch
     long long total_M = 0;       // same-branch row entries
     long long total_var = 0;     // variant emission cells
+    long long total_vcols = 0;   // variant columns
     long long total_nodes = 0;   // tree nodes (int4 each)
     long long total_map = 0;     // mapping ints
     long long total_seq = 0;     // sequence bytes

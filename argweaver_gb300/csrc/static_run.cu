@@ -87,7 +87,7 @@ int run_static(const awg_problem *p, awg_outputs *out, int precision, cudaStream
     const size_t o_gidx = c.add(sizeof(int) * ST);
     const size_t o_var = c.add(sizeof(double) * std::max(plan.total_var, 1LL));
     size_t o_tm32 = 0, o_t2d32 = 0, o_inv32 = 0, o_var32 = 0, o_detp32 = 0, o_rrow32 = 0,
-           o_crow32 = 0, o_rstay32 = 0, o_lneref = 0;
+           o_crow32 = 0, o_rstay32 = 0, o_lneref = 0, o_lnvref = 0;
     if (fp32) {
         o_tm32 = c.add(sizeof(float) * (size_t)plan.nblocks * MAXT * MAXT);
         o_t2d32 = c.add(sizeof(float) * std::max(plan.total_M, 1LL));
@@ -98,6 +98,7 @@ int run_static(const awg_problem *p, awg_outputs *out, int precision, cudaStream
         o_crow32 = c.add(sizeof(float) * ST);
         o_rstay32 = c.add(sizeof(float) * (size_t)plan.nblocks * MAXT);
         o_lneref = c.add(sizeof(double) * plan.nblocks);
+        o_lnvref = c.add(sizeof(double) * std::max(plan.total_vcols, 1LL));
     }
     const size_t o_fw = c.add((fp32 ? sizeof(float) : sizeof(double)) * CELLS);
     const size_t o_lnl = c.add(sizeof(double));
@@ -176,6 +177,7 @@ int run_static(const awg_problem *p, awg_outputs *out, int precision, cudaStream
         d.recoalrow32 = (float *)(D + o_crow32);
         d.rstay32 = (float *)(D + o_rstay32);
         d.lneref = (double *)(D + o_lneref);
+        d.lnvref = (double *)(D + o_lnvref);
         d.fw32 = (float *)(D + o_fw);
     } else {
         d.fw64 = (double *)(D + o_fw);

@@ -17,6 +17,8 @@
 
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include <cmath>
 #include <cstdio>
 
@@ -893,14 +895,292 @@ __global__ void __launch_bounds__(TAB_THREADS) k_tables(BatchDev d, int want32) 
 // ---------------------------------------------------------------------------------------
 // K2: emissions of variant columns (calc_emissions' non-invariant branch, emit.cpp:822-844)
 //
-// One CTA per local tree. The per-state branch factors (prob_branch of the three split
-// branches, emit.cpp:787-805) are computed once per tree in FP64; each warp then takes
-// every nwarps-th variant column of the tree: lane 0 runs the inner (postorder) and outer
-// (preorder) partial likelihoods, the warp evaluates calc_emit for all states. F is the
-// arithmetic type of the partials and emissions (FP64 plain path / FP32 chosen path).
+// One CTA per local tree. Once per tree: the branch mutation probabilities, the per-state
+// factors of the three split branches (prob_branch, emit.cpp:787-805, FP64), and two level
+// schedules of the tree: nodes by height (children before parents) for the inner partials
+// and nodes below the main root by depth for the outer ones. Each warp then takes every
+// nwarps-th variant column of the tree: its lanes compute one level of inner partials
+// (likelihood_site_node_inner, emit.cpp:151-196), then one level of outer partials
+// (likelihood_site_outer, emit.cpp:273-296) at a time, and calc_emit (emit.cpp:620-645) for
+// the states.
+//
+// Plain path (FP64): the reference's order of operations, emissions written as they are.
+// FP32 path: a column whose observed calls agree except for missing ones has emissions that
+// agree to a few digits, which FP32 values would lose. The partials are therefore carried
+// relative to the column's first observed base X: component 0 holds 1 - P(.. | X), the
+// others P(.. | Y) for the bases after X, and the JC69 step P x = mut * sum(x) +
+// (nomut - mut) * x is written for that form (1 - nomut = 3 mut). Each state's emission
+// comes out as D_k = 1 - 4 e_k, exact to FP32 relative precision even when tiny. Per column
+// the kernel writes log(e_ref) of the largest emission and, per state, either the
+// complement 1 - e_k / e_ref when it is at most 1/2, or -e_k / e_ref: the forward and
+// backward steps apply x - x * c or x * r, both without cancellation.
 
 template <typename F>
-__global__ void k_varemit(BatchDev d, int nwarps, int maxS) {
+__device__ __forceinline__ void leaf_partial(uint8_t ch, F *v) {
+    if (ch == 'N') { v[0] = v[1] = v[2] = v[3] = F(1); return; }
+    v[0] = v[1] = v[2] = v[3] = F(0);
+    const int x = (ch == 'A' || ch == 'a') ? 0 : (ch == 'C' || ch == 'c') ? 1
+                : (ch == 'G' || ch == 'g') ? 2 : 3;
+    v[x] = F(1);
+}
+
+// (P x)[a] for the JC69 matrix with off-diagonal m and diagonal nm: the reference's order
+// (FAST false) or the structured form
+template <bool FAST>
+__device__ __forceinline__ void jc_apply(const double *x, double m, double nm, double *y) {
+    if constexpr (FAST) {
+        const double sum = (x[0] + x[1]) + (x[2] + x[3]);
+        const double dlt = nm - m;
+#pragma unroll
+        for (int a = 0; a < 4; a++) y[a] = fma(dlt, x[a], m * sum);
+    } else {
+#pragma unroll
+        for (int a = 0; a < 4; a++) {
+            double p = 0;
+#pragma unroll
+            for (int b = 0; b < 4; b++) p += x[b] * (a == b ? nm : m);
+            y[a] = p;
+        }
+    }
+}
+
+// FP32 path: leaf partial relative to base X (component 0: 1 - P(X), then X+1, X+2, X+3)
+template <typename R>
+__device__ __forceinline__ void leaf_partial_x(uint8_t ch, int X, R *v) {
+    if (ch == 'N') { v[0] = R(0); v[1] = v[2] = v[3] = R(1); return; }
+    const int b = (ch == 'A' || ch == 'a') ? 0 : (ch == 'C' || ch == 'c') ? 1
+                : (ch == 'G' || ch == 'g') ? 2 : 3;
+    v[0] = v[1] = v[2] = v[3] = R(0);
+    if (b != X) {
+        v[0] = R(1);
+        v[(b - X) & 3] = R(1);
+    }
+}
+// JC69 step in that form: off-diagonal m, diagonal 1 - 3m
+template <typename R>
+__device__ __forceinline__ void jc_apply_x(const R *x, R m, R nm, R *y) {
+    const R s3 = (x[1] + x[2]) + x[3];
+    const R u = R(1) - x[0];
+    y[0] = fma(nm, x[0], fma(-m, s3, R(3) * m));
+#pragma unroll
+    for (int a = 1; a < 4; a++) y[a] = fma(m, (u + s3) - x[a], nm * x[a]);
+}
+// complement of a product: 1 - (1 - a)(1 - b)
+template <typename R>
+__device__ __forceinline__ R cprod(R a, R b) { return (a + b) - a * b; }
+
+// Per-tree context of K2 shared by the column passes.
+struct EmitCtx {
+    const int4 *nd;
+    const double *muts, *nomuts, *pm;  // branch and per-state split-branch probabilities
+    const float *muts32, *nomuts32;    // FP32 copies (converted once per tree)
+    const float *pm32;                 // [S][8]: mut0..2, nomut0..2, 1 - 4 mut0, unused
+    const int *snode, *inl, *inp, *outl, *outp;
+    const uint8_t *sfloor;  // per state: a split branch of it was raised to mintime
+    int nlev_in, nlev_out, mainr, node1, S, ns, nleaves;
+    bool internal;
+};
+
+// Column forms of the partials and emissions:
+//   REF  FP64, the reference's order of operations (plain path)
+//   F64  FP64, JC69 structure (FP32 path: internal-branch columns with two or more
+//        observed bases)
+//   REL  FP32 relative to base X (FP32 path, columns whose observed calls agree)
+//   SNP  FP32 (FP32 path: external columns with two or more observed bases). With u, v the
+//        partials either side of the attachment point and b the threaded base,
+//        4 e_k = sum_a p1_a u_a v_a = W_k (m1 + (1 - 4 m1) P_k(b)), P_k(b) = u_b v_b / W_k,
+//        W_k = sum_a u_a v_a. W_k is the likelihood of the tree's own calls: the same W for
+//        every state, except where the reference raises a split branch to mintime (the
+//        lowest and highest state of a branch), which lengthens that branch. The column
+//        keeps one W (sum of the main root's inner partial); such states their own W_k / W;
+//        and every state its bracket, written as 1 - bracket = 3 m1 + (1 - 4 m1)(1 - P_k(b))
+//        when P_k(b) >= 1/2, else the bracket itself: sums of positive terms, so FP32 keeps
+//        the small differences between states that decide the posterior.
+enum { EM_REF = 0, EM_F64 = 1, EM_REL = 2, EM_SNP = 3 };
+
+// One variant column by one warp: inner partials by height level, outer partials by
+// depth, then the states' emissions (4 e_k, or D_k = 1 - 4 e_k in the relative form) into
+// eb[S]. Returns, over the warp, the reference value: the largest 4 e_k, or the smallest D_k.
+template <typename R, int MODE>
+__device__ R emit_column(const EmitCtx &c, const uint8_t *chars, int X, R (*in)[4], R (*out)[4],
+                         R *eb) {
+    const int lane = threadIdx.x & 31;
+    const int4 *nd = c.nd;
+    auto leaf = [&](uint8_t ch, R *v) {
+        if constexpr (MODE == EM_REL) leaf_partial_x<R>(ch, X, v);
+        else leaf_partial<R>(ch, v);
+    };
+    constexpr bool F32 = std::is_same<R, float>::value;
+    auto bm = [&](int j) -> R { if constexpr (F32) return c.muts32[j]; else return (R)c.muts[j]; };
+    auto bn = [&](int j) -> R { if constexpr (F32) return c.nomuts32[j]; else return (R)c.nomuts[j]; };
+    auto step = [&](const R *x, R m, R nm, R *y) {
+        const double m64 = (double)m, nm64 = (double)nm;
+        if constexpr (MODE == EM_REL) {
+            jc_apply_x<R>(x, m, nm, y);
+        } else if constexpr (MODE == EM_F64 || MODE == EM_SNP) {
+            const R sum = (x[0] + x[1]) + (x[2] + x[3]);
+#pragma unroll
+            for (int a = 0; a < 4; a++) y[a] = fma(nm - m, x[a], m * sum);
+        } else {
+            jc_apply<false>((const double *)x, m64, nm64, (double *)y);
+        }
+    };
+    auto mul = [&](const R *a, const R *b, R *z) {
+        z[0] = MODE == EM_REL ? cprod<R>(a[0], b[0]) : a[0] * b[0];
+#pragma unroll
+        for (int t = 1; t < 4; t++) z[t] = a[t] * b[t];
+    };
+    // inner partials, one height level at a time (level 0: the leaves)
+    for (int x = lane; x < c.inp[1]; x += 32) leaf(chars[c.inl[x]], in[c.inl[x]]);
+    __syncwarp();
+    for (int h = 1; h < c.nlev_in; h++) {
+        for (int x = c.inp[h] + lane; x < c.inp[h + 1]; x += 32) {
+            const int j = c.inl[x];
+            const int c1 = nd[j].y, c2 = nd[j].z;
+            R p1[4], p2[4];
+            step(in[c1], bm(c1), bn(c1), p1);
+            step(in[c2], bm(c2), bn(c2), p2);
+            mul(p1, p2, in[j]);
+        }
+        __syncwarp();
+    }
+    // outer partials from the main root down, one depth level at a time
+    for (int h = 0; h < c.nlev_out; h++) {
+        for (int x = c.outp[h] + lane; x < c.outp[h + 1]; x += 32) {
+            const int j = c.outl[x];
+            if (j == c.mainr) {
+                out[j][0] = MODE == EM_REL ? R(0) : R(1);
+                out[j][1] = out[j][2] = out[j][3] = R(1);
+                continue;
+            }
+            const int p = nd[j].x;
+            const int sib = nd[p].y == j ? nd[p].z : nd[p].y;
+            R p1[4];
+            step(in[sib], bm(sib), bn(sib), p1);
+            if (p != c.mainr) {
+                R p2[4];
+                step(out[p], bm(p), bn(p), p2);
+                mul(p1, p2, out[j]);
+            } else {
+#pragma unroll
+                for (int a = 0; a < 4; a++) out[j][a] = p1[a];
+            }
+        }
+        __syncwarp();
+    }
+    // leaf partial of the threaded sequence (external) or the subtree root (internal)
+    R in2[4];
+    if (c.internal) {
+        for (int a = 0; a < 4; a++) in2[a] = in[c.node1][a];
+    } else {
+        leaf(chars[c.nleaves], in2);
+    }
+    R ref = MODE == EM_REL || MODE == EM_SNP ? R(4) : R(0);
+    R vmax = R(0);  // SNP: the largest bracket among states in the plain form
+    R wcol = R(1);  // SNP: the column's W, sum over the main root's inner partial
+    if constexpr (MODE == EM_SNP) {
+        const R *im = in[c.mainr];
+        wcol = (im[0] + im[1]) + (im[2] + im[3]);
+    }
+    // SNP: the threaded base (external trees), 4 for a missing call
+    const uint8_t chb = MODE == EM_SNP ? chars[c.nleaves] : 'N';
+    const int bnew = chb == 'N' ? 4 : (chb == 'A' || chb == 'a') ? 0 : (chb == 'C' || chb == 'c') ? 1
+                   : (chb == 'G' || chb == 'g') ? 2 : 3;
+    for (int k = lane; k < c.S; k += 32) {
+        const int node2 = c.snode[k];
+        R q[7];
+        if constexpr (F32) {
+            const float4 qa = *(const float4 *)(c.pm32 + 8 * k);
+            const float4 qb = *(const float4 *)(c.pm32 + 8 * k + 4);
+            q[0] = qa.x; q[1] = qa.y; q[2] = qa.z; q[3] = qa.w; q[4] = qb.x; q[5] = qb.y; q[6] = qb.z;
+        } else {
+            for (int t = 0; t < 6; t++) q[t] = (R)c.pm[6 * k + t];
+            q[6] = R(1) - R(4) * q[0];
+        }
+        R p1[4], p2[4], p3[4];
+        if constexpr (MODE != EM_SNP) step(in2, q[0], q[3], p1);
+        step(in[node2], q[1], q[4], p2);
+        if (node2 != c.mainr) step(out[node2], q[2], q[5], p3);
+        else p3[0] = p3[1] = p3[2] = p3[3] = R(1);
+        R v;  // calc_emit (emit.cpp:620-645)
+        if constexpr (MODE == EM_SNP) {
+            // 4 e_k / (4 e of a state with W and bracket 1), as D = 1 - value (>= 0) or,
+            // stored negated, the value itself
+            R w = 0, rest = 0;
+#pragma unroll
+            for (int a = 0; a < 4; a++) {
+                const R t = p2[a] * p3[a];
+                w += t;
+                if (a != bnew) rest += t;
+            }
+            // omega = W_k / W - 1: 0 unless a split branch was raised to mintime (states on
+            // the main root's branch always have W_k = W: the JC69 rows sum to one)
+            const R omega = (c.sfloor[k] && node2 != c.mainr) ? (w - wcol) / wcol : R(0);
+            if (bnew == 4) {
+                v = -(R(1) + omega);  // missing threaded call: bracket 1
+                vmax = fmax(vmax, -v);
+            } else {
+                const R m1 = q[0], a41 = q[6];
+                const R pb = (p2[bnew] * p3[bnew]) / w;
+                if (pb >= R(0.5)) {
+                    const R dd = fma(a41, rest / w, R(3) * m1);  // 1 - bracket
+                    v = dd - omega * (R(1) - dd);                // 1 - (1 + omega) bracket
+                    if (v >= R(0)) ref = fmin(ref, v);
+                    else { v = -(R(1) - v); vmax = fmax(vmax, -v); }
+                } else {
+                    v = -((R(1) + omega) * fma(a41, pb, m1));
+                    vmax = fmax(vmax, -v);
+                }
+            }
+        } else if constexpr (MODE == EM_REL) {
+            if (node2 != c.mainr) {
+                v = cprod<R>(p1[0], cprod<R>(p2[0], p3[0]));
+#pragma unroll
+                for (int a = 1; a < 4; a++) v -= p1[a] * p2[a] * p3[a];
+            } else {
+                v = cprod<R>(p1[0], p2[0]);
+#pragma unroll
+                for (int a = 1; a < 4; a++) v -= p1[a] * p2[a];
+            }
+            ref = fmin(ref, v);
+        } else if constexpr (MODE == EM_F64) {
+            v = 0;
+#pragma unroll
+            for (int a = 0; a < 4; a++) v += node2 != c.mainr ? p1[a] * p2[a] * p3[a] : p1[a] * p2[a];
+            ref = fmax(ref, v);
+        } else {
+            v = 0;
+#pragma unroll
+            for (int a = 0; a < 4; a++) {
+                if (node2 != c.mainr) v += p1[a] * p2[a] * p3[a] * R(.25);
+                else v += p1[a] * p2[a] * R(.25);
+            }
+        }
+        eb[k] = v;
+    }
+    if constexpr (MODE == EM_SNP) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            ref = fmin(ref, __shfl_xor_sync(0xffffffffu, ref, o));
+            vmax = fmax(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+        }
+        // the largest bracket: 1 - min D, or the largest plain one (returned negated)
+        if (ref != R(4) && R(1) - ref >= vmax) return ref;
+        return -vmax;
+    }
+    if constexpr (MODE == EM_REL) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) ref = fmin(ref, __shfl_xor_sync(0xffffffffu, ref, o));
+    } else if constexpr (MODE == EM_F64) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) ref = fmax(ref, __shfl_xor_sync(0xffffffffu, ref, o));
+    }
+    __syncwarp();
+    return ref;
+}
+
+template <bool FP32OUT>
+__global__ void k_varemit(BatchDev d, int nwarps, int maxS, int smem_bytes) {
     extern __shared__ int4 dyn[];
     const int blk = cta_block(d);
     const BlockDev B = d.blocks[blk];
@@ -910,20 +1190,56 @@ __global__ void k_varemit(BatchDev d, int nwarps, int maxS) {
     const bool internal = I.internal != 0;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int S = B.S;
+    if (S > maxS || n > d.maxnodes || n < 1) {
+        if (tid == 0) report_error(d.err, ERR_PLAN_MISMATCH, B.inst, B.b, B.start);
+        return;
+    }
 
     auto align16 = [](void *p) {
         return (char *)(((uintptr_t)p + 15) & ~(uintptr_t)15);
     };
     int4 *nd = dyn;
-    F *muts = (F *)align16(nd + n);
-    F *nomuts = muts + n;
-    F *pm = (F *)align16(nomuts + n);            // [S][6]: mut0..2, nomut0..2 per state
+    double *muts = (double *)align16(nd + n);
+    double *nomuts = muts + n;
+    double *pm = (double *)align16(nomuts + n);  // [S][6]: mut0..2, nomut0..2 per state
     int *order = (int *)align16(pm + (size_t)6 * maxS);
-    int *visit = order + n;
-    int *snode = visit + n;                      // [maxS]
-    F *scratch = (F *)align16(snode + maxS);     // per warp: inner[n][4], outer[n][4]
-    int *stacks = (int *)align16(scratch + (size_t)nwarps * n * 8);
+    int *hgt = order + n;                        // height, then depth scratch
+    int *snode = hgt + n;                        // [maxS]
+    int *inl = snode + maxS;                     // nodes by height
+    int *inp = inl + n;                          // [n + 2] level starts
+    int *outl = inp + n + 2;                     // nodes below the main root by depth
+    int *outp = outl + n;                        // [n + 2]
+    uint8_t *sfloor = (uint8_t *)(outp + n + 2);  // [maxS]
+    float *muts32 = (float *)align16(sfloor + maxS);     // FP32 path copies
+    float *nomuts32 = muts32 + n;
+    float *pm32 = (float *)align16(nomuts32 + n);        // [maxS][8]
+    double *scratch = (double *)align16(pm32 + (size_t)8 * maxS);  // per warp: inner[n][4], outer[n][4]
+    double *ebuf = scratch + (size_t)nwarps * n * 8;    // per warp: the column's emissions
     __shared__ double times[MAXT];
+    __shared__ int nlev_in, nlev_out;
+    if ((char *)(ebuf + (size_t)nwarps * maxS) - (char *)dyn > smem_bytes) {
+        if (tid == 0) report_error(d.err, ERR_SMEM_LIMIT, B.inst, B.b, B.start);
+        return;
+    }
+    // tree and state indices the passes use as addresses
+    {
+        bool bad = false;
+        for (int i = tid; i < n; i += blockDim.x) {
+            const int4 v = d.nodes[B.nodes0 + i];
+            if (v.x < -1 || v.x >= n || v.y < -1 || v.y >= n || v.z < -1 || v.z >= n ||
+                v.w < 0 || v.w > T + 1)
+                bad = true;
+        }
+        for (int k = tid; k < S; k += blockDim.x) {
+            const StateInfo si = d.sinfo[B.state0 + k];
+            if (si.node < 0 || si.node >= n || si.time < 0 || si.time >= T) bad = true;
+        }
+        if (B.root < 0 || B.root >= n) bad = true;
+        if (__syncthreads_or(bad)) {
+            if (tid == 0) report_error(d.err, ERR_BOUNDS, B.inst, B.b, B.start);
+            return;
+        }
+    }
 
     const double *model = d.model + I.model0;
     for (int i = tid; i < T; i += blockDim.x) times[i] = model[M_TIMES + i];
@@ -941,8 +1257,12 @@ __global__ void k_varemit(BatchDev d, int nwarps, int maxS) {
                 m0 = prob_branch(t, mu, false);
             }
         }
-        muts[i] = (F)m1;
-        nomuts[i] = (F)m0;
+        muts[i] = m1;
+        nomuts[i] = m0;
+        if (FP32OUT) {
+            muts32[i] = (float)m1;
+            nomuts32[i] = (float)m0;
+        }
     }
     const int mainr = internal ? nd[root].z : root;
     const int node1 = internal ? nd[root].y : 0;
@@ -959,14 +1279,21 @@ __global__ void k_varemit(BatchDev d, int nwarps, int maxS) {
         dist[0] = fmax(coal_time - time1, mintime);
         dist[1] = fmax(coal_time - time2, mintime);
         dist[2] = fmax(parent_time - coal_time, mintime);
+        sfloor[k] = (coal_time - time2 < mintime) || (parent_time - coal_time < mintime);
         for (int x = 0; x < 3; x++) {
-            pm[6 * k + x] = (F)prob_branch(dist[x], mu, true);
-            pm[6 * k + 3 + x] = (F)prob_branch(dist[x], mu, false);
+            pm[6 * k + x] = prob_branch(dist[x], mu, true);
+            pm[6 * k + 3 + x] = prob_branch(dist[x], mu, false);
+        }
+        if (FP32OUT) {
+            for (int x = 0; x < 6; x++) pm32[8 * k + x] = (float)pm[6 * k + x];
+            pm32[8 * k + 6] = (float)(1.0 - 4.0 * pm[6 * k]);
+            pm32[8 * k + 7] = 0.f;
         }
     }
-    if (tid == 0) {  // postorder (local_tree.h:274-304)
+    if (tid == 0) {
+        // postorder (local_tree.h:274-304)
         int i;
-        for (i = 0; i < n; i++) visit[i] = 0;
+        for (i = 0; i < n; i++) hgt[i] = 0;
         for (i = 0; i < n; i++) {
             if (nd[i].y != -1) break;
             order[i] = i;
@@ -975,19 +1302,51 @@ __global__ void k_varemit(BatchDev d, int nwarps, int maxS) {
         for (i = 0; i < n; i++) {
             const int p = nd[order[i]].x;
             if (p != -1) {
-                visit[p]++;
-                if (visit[p] == 2) order[end++] = p;
+                hgt[p]++;
+                if (hgt[p] == 2) order[end++] = p;
             }
         }
+        // heights (children first), then nodes bucketed by height
+        int H = 0;
+        for (i = 0; i < n; i++) {
+            const int j = order[i];
+            const int h = nd[j].y == -1 ? 0 : max(hgt[nd[j].y], hgt[nd[j].z]) + 1;
+            hgt[j] = h;
+            H = max(H, h);
+        }
+        for (int h = 0; h <= H + 1; h++) inp[h] = 0;
+        for (i = 0; i < n; i++) inp[hgt[i] + 1]++;
+        for (int h = 0; h <= H; h++) inp[h + 1] += inp[h];
+        for (i = 0; i < n; i++) inl[inp[hgt[i]]++] = i;  // inp[h] now holds level h's end
+        for (int h = H; h > 0; h--) inp[h] = inp[h - 1];
+        inp[0] = 0;
+        nlev_in = H + 1;
+        // depth below the main root (parents first: reverse postorder); -1 elsewhere
+        int D = 0;
+        for (i = n - 1; i >= 0; i--) {
+            const int j = order[i];
+            const int p = nd[j].x;
+            hgt[j] = j == mainr ? 0 : (p != -1 && hgt[p] >= 0) ? hgt[p] + 1 : -1;
+            D = max(D, hgt[j]);
+        }
+        for (int h = 0; h <= D + 1; h++) outp[h] = 0;
+        for (i = 0; i < n; i++)
+            if (hgt[i] >= 0) outp[hgt[i] + 1]++;
+        for (int h = 0; h <= D; h++) outp[h + 1] += outp[h];
+        for (i = 0; i < n; i++)
+            if (hgt[i] >= 0) outl[outp[hgt[i]]++] = i;
+        for (int h = D; h > 0; h--) outp[h] = outp[h - 1];
+        outp[0] = 0;
+        nlev_out = D + 1;
     }
     __syncthreads();
 
-    F (*in)[4] = (F (*)[4])(scratch + (size_t)warp * n * 8);
-    F (*out)[4] = in + n;
-    int *stack = stacks + warp * n;
+    const EmitCtx ctx{nd, muts, nomuts, pm, muts32, nomuts32, pm32, snode, inl, inp, outl, outp,
+                      sfloor, nlev_in, nlev_out, mainr, node1, S, I.nseqs, I.nleaves, internal};
+    double *wscr = scratch + (size_t)warp * n * 8;
+    double *eb = ebuf + (size_t)warp * maxS;
     const uint8_t *cls = d.colclass + I.col0 + B.start;
     const int ns = I.nseqs;
-    F *vout = (sizeof(F) == 4) ? (F *)d.var32 : (F *)d.varemit;
 
     // the block's variant columns in order; warp w takes every nwarps-th
     int seen = 0;
@@ -1001,95 +1360,81 @@ __global__ void k_varemit(BatchDev d, int nwarps, int maxS) {
             const int vslot = seen++;
             if (vslot % nwarps != warp) continue;
             const uint8_t *chars = d.seqT + I.seq0 + (size_t)(B.start + base + bit) * ns;
-            if (lane == 0) {
-                for (int oi = 0; oi < n; oi++) {  // likelihood_site_node_inner (emit.cpp:151-196)
-                    const int j = order[oi];
-                    if (nd[j].y == -1) {
-                        const uint8_t ch = chars[j];
-                        if (ch == 'N') { in[j][0] = in[j][1] = in[j][2] = in[j][3] = F(1); }
-                        else {
-                            in[j][0] = in[j][1] = in[j][2] = in[j][3] = F(0);
-                            const int x = (ch == 'A' || ch == 'a') ? 0 : (ch == 'C' || ch == 'c') ? 1
-                                        : (ch == 'G' || ch == 'g') ? 2 : 3;
-                            in[j][x] = F(1);
-                        }
-                    } else {
-                        const int c1 = nd[j].y, c2 = nd[j].z;
-                        for (int a = 0; a < 4; a++) {
-                            F p1 = 0, p2 = 0;
-                            for (int b = 0; b < 4; b++) {
-                                if (a == b) { p1 += in[c1][b] * nomuts[c1]; p2 += in[c2][b] * nomuts[c2]; }
-                                else { p1 += in[c1][b] * muts[c1]; p2 += in[c2][b] * muts[c2]; }
-                            }
-                            in[j][a] = p1 * p2;
-                        }
-                    }
-                }
-                int sp = 0;  // likelihood_site_outer (emit.cpp:273-296), preorder
-                stack[sp++] = mainr;
-                while (sp > 0) {
-                    const int j = stack[--sp];
-                    if (j == mainr) {
-                        out[j][0] = out[j][1] = out[j][2] = out[j][3] = F(1);
-                    } else {
-                        const int p = nd[j].x;
-                        const int sib = nd[p].y == j ? nd[p].z : nd[p].y;
-                        if (p != mainr) {
-                            for (int a = 0; a < 4; a++) {
-                                F p1 = 0, p2 = 0;
-                                for (int b = 0; b < 4; b++) {
-                                    if (a == b) { p1 += in[sib][b] * nomuts[sib]; p2 += out[p][b] * nomuts[p]; }
-                                    else { p1 += in[sib][b] * muts[sib]; p2 += out[p][b] * muts[p]; }
-                                }
-                                out[j][a] = p1 * p2;
-                            }
-                        } else {
-                            for (int a = 0; a < 4; a++) {
-                                F p1 = 0;
-                                for (int b = 0; b < 4; b++) {
-                                    if (a == b) p1 += in[sib][b] * nomuts[sib];
-                                    else p1 += in[sib][b] * muts[sib];
-                                }
-                                out[j][a] = p1;
-                            }
-                        }
-                    }
-                    if (nd[j].y != -1) { stack[sp++] = nd[j].y; stack[sp++] = nd[j].z; }
-                }
+            const int vrow = d.colvar[I.col0 + B.start + base + bit];
+            if (vrow < 0 || vrow >= B.nvar) {
+                if (lane == 0) report_error(d.err, ERR_BOUNDS, B.inst, B.b, B.start + base + bit);
+                continue;
             }
-            __syncwarp();
-            // leaf partial of the threaded sequence (external) or the subtree root (internal)
-            F in2[4];
-            if (internal) {
-                for (int a = 0; a < 4; a++) in2[a] = in[node1][a];
+            if constexpr (!FP32OUT) {
+                emit_column<double, EM_REF>(ctx, chars, 0, (double (*)[4])wscr,
+                                            (double (*)[4])wscr + n, eb);
+                double *row = d.varemit + B.var0 + (size_t)vrow * S;
+                for (int k = lane; k < S; k += 32) row[k] = eb[k];
             } else {
-                const uint8_t ch = chars[I.nleaves];
-                if (ch == 'N') { in2[0] = in2[1] = in2[2] = in2[3] = F(1); }
-                else {
-                    in2[0] = in2[1] = in2[2] = in2[3] = F(0);
-                    const int x = (ch == 'A' || ch == 'a') ? 0 : (ch == 'C' || ch == 'c') ? 1
-                                : (ch == 'G' || ch == 'g') ? 2 : 3;
-                    in2[x] = F(1);
+                // X = the column's first observed base; near = every observed call (the
+                // threaded sequence's too) is X
+                int jfirst = ns;
+                for (int j = lane; j < ns; j += 32)
+                    if (chars[j] != 'N') { jfirst = j; break; }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) jfirst = min(jfirst, __shfl_xor_sync(0xffffffffu, jfirst, o));
+                int X = 0;
+                bool near = false;
+                if (jfirst < ns) {
+                    const uint8_t ch = chars[jfirst];
+                    X = (ch == 'A' || ch == 'a') ? 0 : (ch == 'C' || ch == 'c') ? 1
+                      : (ch == 'G' || ch == 'g') ? 2 : 3;
+                    bool other = false;
+                    for (int j = lane; j < ns; j += 32) {
+                        const uint8_t c = chars[j];
+                        if (c != 'N' && (c & 0xDF) != (ch & 0xDF)) other = true;
+                    }
+                    near = !__any_sync(0xffffffffu, other);
                 }
-            }
-            F *row = vout + B.var0 + (size_t)d.colvar[I.col0 + B.start + base + bit] * S;
-            for (int k = lane; k < S; k += 32) {
-                const int node2 = snode[k];
-                const F *q = pm + 6 * k;
-                F e = 0;  // calc_emit (emit.cpp:620-645)
-                for (int a = 0; a < 4; a++) {
-                    F p1 = 0, p2 = 0, p3 = 0;
-                    for (int b = 0; b < 4; b++) {
-                        if (a == b) {
-                            p1 += in2[b] * q[3]; p2 += in[node2][b] * q[4]; p3 += out[node2][b] * q[5];
+                float *row = d.var32 + B.var0 + (size_t)vrow * S;
+                if (near) {
+                    float *fs = (float *)wscr, *fe = (float *)eb;
+                    const float dref = emit_column<float, EM_REL>(ctx, chars, X, (float (*)[4])fs,
+                                                                  (float (*)[4])fs + n, fe);
+                    const float inv1 = 1.f / (1.f - dref);  // 1 / (4 e_ref)
+                    for (int k = lane; k < S; k += 32) {
+                        const float c = (fe[k] - dref) * inv1;  // 1 - e_k / e_ref
+                        row[k] = c <= 0.5f ? c : -((1.f - fe[k]) * inv1);
+                    }
+                    if (lane == 0) d.lnvref[B.vrow0 + vrow] = log(.25) + log1p(-(double)dref);
+                } else if (!internal) {
+                    // brackets against the column's largest: D form x / plain form y
+                    float *fs = (float *)wscr, *fe = (float *)eb;
+                    const float ref = emit_column<float, EM_SNP>(ctx, chars, X, (float (*)[4])fs,
+                                                                 (float (*)[4])fs + n, fe);
+                    const float bref = ref >= 0.f ? 1.f - ref : -ref;  // the largest bracket
+                    const float inv1 = 1.f / bref;
+                    for (int k = lane; k < S; k += 32) {
+                        const float v = fe[k];
+                        if (v >= 0.f && ref >= 0.f) {
+                            const float cc = (v - ref) * inv1;  // 1 - e_k / e_ref
+                            row[k] = cc <= 0.5f ? cc : -((1.f - v) * inv1);
                         } else {
-                            p1 += in2[b] * q[0]; p2 += in[node2][b] * q[1]; p3 += out[node2][b] * q[2];
+                            const float r = (v >= 0.f ? 1.f - v : -v) * inv1;  // e_k / e_ref
+                            row[k] = r >= 0.5f ? 1.f - r : -r;
                         }
                     }
-                    if (node2 != mainr) e += p1 * p2 * p3 * F(.25);
-                    else e += p1 * p2 * F(.25);
+                    if (lane == 0) {
+                        // W: the tree's own likelihood, sum over the main root's inner partial
+                        const float *im = fs + 4 * mainr;
+                        const double w = (double)((im[0] + im[1]) + (im[2] + im[3]));
+                        d.lnvref[B.vrow0 + vrow] = log(.25 * w * (double)bref);
+                    }
+                } else {
+                    const double eref = emit_column<double, EM_F64>(ctx, chars, X, (double (*)[4])wscr,
+                                                                    (double (*)[4])wscr + n, eb);
+                    const double inv1 = 1.0 / eref;  // 1 / (4 e_ref)
+                    for (int k = lane; k < S; k += 32) {
+                        const double r = eb[k] * inv1;  // e_k / e_ref
+                        row[k] = (float)(r >= 0.5 ? 1.0 - r : -r);
+                    }
+                    if (lane == 0) d.lnvref[B.vrow0 + vrow] = log(.25 * eref);
                 }
-                row[k] = e;
             }
             __syncwarp();
         }
@@ -1117,29 +1462,38 @@ void launch_tables(const BatchDev &d, bool want32, cudaStream_t s) {
     note_launch();
 }
 
-template <typename F>
+template <bool FP32OUT>
 void launch_varemit_t(const BatchDev &d, cudaStream_t s) {
     const int n = d.maxnodes, maxS = imax(d.maxS, 1);
     int nwarps = 4;
+    // the kernel's carve, offset by offset (16-byte alignment where it aligns)
     auto need = [&](int w) {
-        return (size_t)n * sizeof(int4) + (2 * (size_t)n + 6 * (size_t)maxS) * sizeof(F) +
-               (2 * (size_t)n + maxS + 4) * sizeof(int) + (size_t)w * n * 8 * sizeof(F) +
-               (size_t)w * n * sizeof(int) + 6 * 16;
+        auto a16 = [](size_t o) { return (o + 15) & ~(size_t)15; };
+        size_t o = (size_t)n * sizeof(int4);                              // nd
+        o = a16(o) + 2 * (size_t)n * sizeof(double);                      // muts, nomuts
+        o = a16(o) + 6 * (size_t)maxS * sizeof(double);                   // pm
+        o = a16(o) + (6 * (size_t)n + 4 + maxS) * sizeof(int);            // order .. outp
+        o += (size_t)maxS;                                                // sfloor
+        o = a16(o) + 2 * (size_t)n * sizeof(float);                       // muts32, nomuts32
+        o = a16(o) + 8 * (size_t)maxS * sizeof(float);                    // pm32
+        o = a16(o) + (size_t)w * n * 8 * sizeof(double);                  // scratch
+        o += (size_t)w * maxS * sizeof(double);                           // ebuf
+        return o + 16;
     };
     while (nwarps > 1 && need(nwarps) > 200 * 1024) nwarps--;
     const size_t smem = need(nwarps);
     static size_t configured = 0;
     if (smem > configured) {  // opt in; static shared memory counts against 48 KB too
-        if (cudaFuncSetAttribute(k_varemit<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return;
+        if (cudaFuncSetAttribute(k_varemit<FP32OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return;
         configured = smem;
     }
-    k_varemit<F><<<d.nblocks, nwarps * 32, smem, s>>>(d, nwarps, maxS);
+    k_varemit<FP32OUT><<<d.nblocks, nwarps * 32, smem, s>>>(d, nwarps, maxS, (int)smem);
     note_launch();
 }
 
 void launch_varemit(const BatchDev &d, bool fp32, cudaStream_t s) {
-    if (fp32) launch_varemit_t<float>(d, s);
-    else launch_varemit_t<double>(d, s);
+    if (fp32) launch_varemit_t<true>(d, s);
+    else launch_varemit_t<false>(d, s);
 }
 
 }  // namespace awg

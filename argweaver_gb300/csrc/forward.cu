@@ -347,17 +347,21 @@ __global__ void __launch_bounds__(512) k_forward(BatchDev d, int maxS, int maxM,
 }
 
 // ---------------------------------------------------------------------------------------
-// Register-resident variant for trees of up to KPT * blockDim.x states.
+// Register-resident variant for trees of up to KPT * (blockDim.x - 32) states.
 //
-// Thread t owns states k = t + q * NT (q < KPT) of every tree, in state order, so lanes
-// holding one node's states read the same neighbours and consecutive same-branch entries
-// (no bank conflicts). The state's time, node span, row offset, time-sorted rank and
-// invariant emission stay in registers for the tree's columns, and the next variant
-// column's emissions are loaded a column ahead. Per column, two CTA barriers:
-//   A  column i-1 complete in state order and time-sorted; warps sum the time bins
-//      (bin b a contiguous range of the sorted copy: lane-strided loads, butterfly sum)
-//   B  every warp forms tf[a] = sum_b tm[b][a] * bin[b] in lane a, lane 31 (ones) the norm;
-//      column i-1 / norm goes to HBM and column i of the owned states is computed
+// Warp 0 is the reduction warp; the other threads own states k = (t - 32) + q * NTS
+// (q < KPT), in state order, so lanes holding one node's states read the same neighbours
+// and consecutive same-branch entries. A state's time, node span, row offset, time-sorted
+// rank and invariant emission stay in registers for the tree's columns, and the next
+// variant column's emissions are loaded a column ahead. Per column, two CTA barriers:
+//   A  column i-1 complete in state order and time-sorted (each time bin a contiguous
+//      range of the sorted copy). In parallel:
+//        warp 0: lane l sums its contiguous chunk of ceil(S/32) sorted positions bin by
+//                bin; lane b adds bin b's chunk sums in lane order; lane a forms
+//                tf[a] = sum_b tm[b][a] bin[b] by shuffles, lane 31 (ones) the norm
+//        owners: the same-branch dot sum_y tmatrix2[a_y][k] col[j1 + y] of their states
+//   B  tf and the norm published: owners finish column i (tf of their time + dot, stay,
+//      emission, rescaling) and write column i-1 / norm to HBM.
 // Every sum has an order fixed by the tree alone, so results do not depend on the block
 // size or on the other problems of the batch.
 // FP32 pair arithmetic (value = hi + lo, |lo| <= ulp(hi) / 2) for the dominant path of
@@ -401,15 +405,19 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
     const int qi = cta_instance(d);
     const InstDev I = d.inst[qi];
     const int T = I.T, NB = T - 1;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int NT = blockDim.x, NW = NT >> 5;
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int NT = blockDim.x, NTS = NT - 32;   // state owners: threads 32 ..
+    const int st = tid - 32;                    // owner index (negative in warp 0)
+    const bool reducer = tid < 32;
 
     F *col = (F *)dyn_d;                       // [2][maxS] columns in state order
     F *colT = col + 2 * maxS;                  // [maxS] newest column, time-sorted
     F *t2s = colT + maxS;                      // [maxM] same-branch entries of the block
     __shared__ F tmS[MAXT * MAXT];             // [b][a] tmatrix; column 31 holds ones
-    __shared__ F bins[MAXT];
+    __shared__ F part[32][MAXT];               // reducer: per lane, its chunk's bin sums
+    __shared__ F tfs[32];                      // tf by time; [31]: the column's norm
     __shared__ int bptr[MAXT + 1];
+    __shared__ int fbin[32];                   // reducer: first bin of each lane's chunk
 
     LogAcc acc;
     int c = 0;                                 // buffer holding the current column
@@ -433,15 +441,15 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
                 const F *dp = tab.dprob + B.prev_state0;
                 const F *rr = tab.rrow + B.state0;
                 const F *cr = tab.crow + B.state0;
-                F part = 0;
+                F sum = 0;
                 if (tid < 32) {
-                    for (int p = gp[0] + lane; p < gp[1]; p += 32) part += col[c * maxS + gi[p]] * dp[gi[p]];
-                    part = warp_sum(part);
+                    for (int p = gp[0] + lane; p < gp[1]; p += 32) sum += col[c * maxS + gi[p]] * dp[gi[p]];
+                    sum = warp_sum(sum);
                 }
                 if (tid == 0) {
-                    if (src.x != -1 && rr[0] > F(0)) part += col[c * maxS + src.x] * rr[0];
-                    if (src.y != -1 && cr[0] > F(0)) part += col[c * maxS + src.y] * cr[0];
-                    acc.add((double)part);
+                    if (src.x != -1 && rr[0] > F(0)) sum += col[c * maxS + src.x] * rr[0];
+                    if (src.y != -1 && cr[0] > F(0)) sum += col[c * maxS + src.y] * cr[0];
+                    acc.add((double)sum);
                     col[c * maxS] = F(1);
                     fw[0] = F(1);
                 }
@@ -452,7 +460,7 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
             continue;
         }
 
-        // ---- stage the tree: tmatrix, bins, owned states
+        // ---- stage the tree: tmatrix, bins, owned states, reducer chunks
         const long long s0 = B.state0;
         const F *tmg = tab.tm + (size_t)blk * MAXT * MAXT;
         for (int e = tid; e < NB * MAXT; e += NT) {
@@ -461,36 +469,67 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
         }
         for (int a = tid; a <= MAXT; a += NT) bptr[a] = d.bt_ptr[(size_t)blk * (MAXT + 1) + a];
         int st_time[KPT], st_j1[KPT], st_m[KPT], st_off[KPT], st_rank[KPT];
-        F st_inv[KPT], st_rs[KPT], x_own[KPT], e_next[KPT];
+        F st_inv[KPT], st_rs[KPT], x_own[KPT], e_next[KPT], dq[KPT];
         float x_lo[KPT];  // FP32 path: low parts of the owned states (pairs x_own + x_lo)
+        auto owned = [&](int q) { return reducer ? -1 : st + q * NTS; };  // the reducer owns none
+        auto valid = [&](int k) { return k >= 0 && k < S; };
 #pragma unroll
         for (int q = 0; q < KPT; q++) {
-            const int k = tid + q * NT;
-            const bool valid = k < S;
-            const StateInfo si = d.sinfo[s0 + (valid ? k : 0)];
+            const int k = owned(q);
+            const int kk = valid(k) ? k : 0;
+            const StateInfo si = d.sinfo[s0 + kk];
             st_time[q] = si.time;
             st_j1[q] = si.j1;
-            st_m[q] = valid ? si.m : 0;
-            st_off[q] = d.t2off[s0 + (valid ? k : 0)];
-            st_inv[q] = tab.inv[s0 + (valid ? k : 0)];
+            st_m[q] = valid(k) ? si.m : 0;
+            st_off[q] = d.t2off[s0 + kk];
+            st_inv[q] = tab.inv[s0 + kk];
             st_rs[q] = Tab<F>::split ? (F)tab.rstay[(size_t)blk * MAXT + si.time] : F(0);
             x_own[q] = F(0);
             x_lo[q] = 0.0f;
             e_next[q] = F(0);
+            dq[q] = F(0);
         }
         // time-sorted rank of each state: bt_perm lists the states of each time in order
         for (int p = tid; p < S; p += NT) col[(c ^ 1) * maxS + d.bt_perm[s0 + p]] = (F)p;
         __syncthreads();  // tmS, bptr, ranks (parked in the free column buffer)
 #pragma unroll
         for (int q = 0; q < KPT; q++) {
-            const int k = tid + q * NT;
-            st_rank[q] = k < S ? (int)col[(c ^ 1) * maxS + k] : 0;
+            const int k = owned(q);
+            st_rank[q] = valid(k) ? (int)col[(c ^ 1) * maxS + k] : 0;
         }
+        // reducer: lane l sums sorted positions [l C, (l + 1) C); lane b adds the chunk
+        // sums of lanes l0_b .. l1_b
+        const int chunk = (S + 31) >> 5;
+        const int clo = imin(lane * chunk, S), chi = imin(clo + chunk, S);
+        int l0 = 0, l1 = -1;
+        int o1 = 0, o2 = 0, nbc = 0;  // bin boundaries inside the chunk, bins it spans
+        if (reducer) {
+            int fb = 0;
+            while (fb < NB - 1 && bptr[fb + 1] <= clo) fb++;
+            fbin[lane] = fb;
+            if (lane < NB && bptr[lane + 1] > bptr[lane]) {
+                l0 = bptr[lane] / chunk;
+                l1 = (bptr[lane + 1] - 1) / chunk;
+            }
+            if (chi > clo) {
+                int b = fb;
+                nbc = 1;
+                o1 = o2 = chi - clo;
+                while (b < NB - 1 && bptr[b + 1] < chi) {
+                    if (nbc == 1) o1 = bptr[b + 1] - clo;
+                    else if (nbc == 2) o2 = bptr[b + 1] - clo;
+                    nbc++;
+                    b++;
+                }
+            }
+        }
+        // the fast chunk sum handles chunks of up to 32 positions spanning up to 3 bins
+        const bool fast_chunk = __all_sync(0xffffffffu, !reducer || (chunk <= 32 && nbc <= 3));
         if (t2_in_smem) {
 #pragma unroll
             for (int q = 0; q < KPT; q++) {
-                const int k = tid + q * NT;
-                if (k >= S) continue;
+                const int k = owned(q);
+                if (!valid(k)) continue;
                 const int m = st_m[q], off = st_off[q];
                 const int a0 = st_time[q] - (k - st_j1[q]);
                 for (int y = 0; y < m; y++)
@@ -512,12 +551,12 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
             ci = (uint8_t)__shfl_sync(0xffffffffu, ccache, i - cbase);
             vi = __shfl_sync(0xffffffffu, vcache, i - cbase);
         };
-        auto emit = [&](F s, uint8_t ci, int vrow, int q, bool prefetched) -> F {
-            if (ci == COL_MASKED) return s;
-            if (ci == COL_INVARIANT) return Tab<F>::split ? s - s * st_inv[q] : s * st_inv[q];
-            const F e = prefetched ? e_next[q] : var[(size_t)vrow * S + tid + q * NT];
-            if (!Tab<F>::split) return s * e;
-            return e >= F(0) ? s - s * e : s * -e;  // FP32: 1 - e_k / e_ref, or -e_k / e_ref
+        auto emit = [&](F sv, uint8_t ci, int vrow, int q, bool prefetched) -> F {
+            if (ci == COL_MASKED) return sv;
+            if (ci == COL_INVARIANT) return Tab<F>::split ? sv - sv * st_inv[q] : sv * st_inv[q];
+            const F e = prefetched ? e_next[q] : var[(size_t)vrow * S + owned(q)];
+            if (!Tab<F>::split) return sv * e;
+            return e >= F(0) ? sv - sv * e : sv * -e;  // FP32: 1 - e_k / e_ref, or -e_k / e_ref
         };
         auto prefetch = [&](int i) {  // emissions of column i, if variant
             uint8_t c1;
@@ -526,16 +565,16 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
             if (c1 == COL_VARIANT)
 #pragma unroll
                 for (int q = 0; q < KPT; q++)
-                    if (tid + q * NT < S) e_next[q] = var[(size_t)v1 * S + tid + q * NT];
+                    if (valid(owned(q))) e_next[q] = var[(size_t)v1 * S + owned(q)];
         };
-        __syncthreads();  // t2s; the rank scratch is read
+        __syncthreads();  // t2s, fbin; the rank scratch is read
 
         // ---- first column of the block
         if (bi == 0) {
 #pragma unroll
             for (int q = 0; q < KPT; q++) {
-                const int k = tid + q * NT;
-                if (k >= S) continue;
+                const int k = owned(q);
+                if (!valid(k)) continue;
                 const F v = fw[k];  // priors (K1)
                 col[c * maxS + k] = v;
                 colT[st_rank[q]] = v;
@@ -554,16 +593,16 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
             const F *prev = col + c * maxS;
 #pragma unroll
             for (int q = 0; q < KPT; q++) {
-                const int k = tid + q * NT;
-                if (k >= S) continue;
-                F s = 0;
+                const int k = owned(q);
+                if (!valid(k)) continue;
+                F sv = 0;
                 for (int p = gp[k]; p < gp[k + 1]; p++) {
                     const int j = gi[p];
-                    s += prev[j] * dp[j];
+                    sv += prev[j] * dp[j];
                 }
-                if (src.x != -1 && rr[k] > F(0)) s += prev[src.x] * rr[k];
-                if (src.y != -1 && cr[k] > F(0)) s += prev[src.y] * cr[k];
-                const F v = emit(s, c0, v0, q, false);
+                if (src.x != -1 && rr[k] > F(0)) sv += prev[src.x] * rr[k];
+                if (src.y != -1 && cr[k] > F(0)) sv += prev[src.y] * cr[k];
+                const F v = emit(sv, c0, v0, q, false);
                 col[(c ^ 1) * maxS + k] = v;
                 colT[st_rank[q]] = v;
                 x_own[q] = v;
@@ -573,23 +612,106 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
             if (Tab<F>::split && tid == 0 && c0 == COL_VARIANT) acc.extra += tab.lnvref[B.vrow0 + v0];
             c ^= 1;
         }
-        if (len > 1) prefetch(1);
+        if (len > 1 && !reducer) prefetch(1);
 
         // ---- remaining columns; iteration i also finalises column i-1
         for (int i = 1; i <= len; i++) {
             __syncthreads();  // A: column i-1 complete
-            for (int b = warp; b < NB; b += NW) {
-                F s = 0;
-                for (int p = bptr[b] + lane; p < bptr[b + 1]; p += 32) s += colT[p];
-                s = warp_sum(s);
-                if (lane == 0) bins[b] = s;
-            }
-            __syncthreads();  // B: bins of column i-1
-            F tf = 0;
-            for (int b = 0; b < NB; b++) tf += tmS[b * MAXT + lane] * bins[b];
-            const F norm = __shfl_sync(0xffffffffu, tf, MAXT - 1);
-            const F inv_norm = F(1) / norm;
             const F *cur = col + c * maxS;
+            if (reducer) {
+                // chunk sums by bin (positions sorted by time)
+                if (fast_chunk) {
+                    // eight loads at a time; three independent sums over the chunk's bin ranges
+                    F a0 = 0, a1 = 0, a2 = 0;
+                    const int len_c = chi - clo;
+                    for (int j0 = 0; j0 < len_c; j0 += 8) {
+                        F v[8];
+#pragma unroll
+                        for (int j = 0; j < 8; j++) v[j] = j0 + j < len_c ? colT[clo + j0 + j] : F(0);
+#pragma unroll
+                        for (int j = 0; j < 8; j++) {
+                            const int jj = j0 + j;
+                            a0 += jj < o1 ? v[j] : F(0);
+                            a1 += (jj >= o1 && jj < o2) ? v[j] : F(0);
+                            a2 += jj >= o2 ? v[j] : F(0);
+                        }
+                    }
+                    if (nbc >= 1) part[lane][0] = a0;
+                    if (nbc >= 2) part[lane][1] = a1;
+                    if (nbc >= 3) part[lane][2] = a2;
+                } else {
+                    int bcur = fbin[lane], j = 0, nextb = bptr[bcur + 1];
+                    F a = 0;
+                    for (int p = clo; p < chi; p++) {
+                        while (p >= nextb) {
+                            part[lane][j++] = a;
+                            a = F(0);
+                            bcur++;
+                            nextb = bptr[bcur + 1];
+                        }
+                        a += colT[p];
+                    }
+                    if (chi > clo) part[lane][j] = a;
+                }
+                __syncwarp();
+                F bin = 0;
+                for (int l = l0; l <= l1; l++) bin += part[l][lane - fbin[l]];
+                // tf[a] = sum_b tm[b][a] bin[b]: four partial sums (b mod 4), then combined
+                F t0 = 0, t1 = 0, t2 = 0, t3 = 0;
+#pragma unroll
+                for (int b = 0; b < MAXT - 1; b += 4) {
+                    const F g0 = __shfl_sync(0xffffffffu, bin, b);
+                    const F g1 = __shfl_sync(0xffffffffu, bin, b + 1);
+                    const F g2 = __shfl_sync(0xffffffffu, bin, b + 2);
+                    const F g3 = __shfl_sync(0xffffffffu, bin, b + 3);
+                    if (b < NB) t0 += tmS[b * MAXT + lane] * g0;
+                    if (b + 1 < NB) t1 += tmS[(b + 1) * MAXT + lane] * g1;
+                    if (b + 2 < NB) t2 += tmS[(b + 2) * MAXT + lane] * g2;
+                    if (b + 3 < NB) t3 += tmS[(b + 3) * MAXT + lane] * g3;
+                }
+                tfs[lane] = (t0 + t1) + (t2 + t3);
+            } else {
+                // same-branch dot of the owned states: sum_y tmatrix2[a_y][k] col[j1 + y]
+#pragma unroll
+                for (int q = 0; q < KPT; q++) {
+                    const int k = owned(q);
+                    F sv = 0;
+                    if (valid(k)) {
+                        const F *nb = cur + st_j1[q];
+                        const int m = st_m[q];
+                        if (t2_in_smem) {
+                            // even terms into sv, odd into s1, four loads ahead
+                            const F *row = t2s + st_off[q];
+                            int y = 0;
+                            F s1 = 0;
+                            for (; y + 3 < m; y += 4) {
+                                const F r0 = row[0], r1 = row[m], r2 = row[2 * m], r3 = row[3 * m];
+                                const F n0 = nb[y], n1 = nb[y + 1], n2 = nb[y + 2], n3 = nb[y + 3];
+                                sv += r0 * n0;
+                                s1 += r1 * n1;
+                                sv += r2 * n2;
+                                s1 += r3 * n3;
+                                row += 4 * m;
+                            }
+                            for (; y + 1 < m; y += 2) {
+                                sv += row[0] * nb[y];
+                                s1 += row[m] * nb[y + 1];
+                                row += 2 * m;
+                            }
+                            if (y < m) sv += row[0] * nb[y];
+                            sv += s1;
+                        } else {
+                            const int a0 = st_time[q] - (k - st_j1[q]);
+                            for (int y = 0; y < m; y++)
+                                sv += tab.t2(B.t2_0 + st_off[q] + y * m, tmS[(a0 + y) * MAXT + st_time[q]]) * nb[y];
+                        }
+                    }
+                    dq[q] = sv;
+                }
+            }
+            __syncthreads();  // B: tf and the norm of column i-1
+            const F norm = tfs[MAXT - 1];
+            const F inv_norm = F(1) / norm;
             if (tid == 0) {
                 acc.add((double)norm);
                 if (!(norm > F(0))) report_error(d.err, ERR_ZERO_NORM, qi, bi, B.start + i - 1);
@@ -601,8 +723,8 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
             if (i == len) {
 #pragma unroll
                 for (int q = 0; q < KPT; q++) {
-                    const int k = tid + q * NT;
-                    if (k >= S) continue;
+                    const int k = owned(q);
+                    if (!valid(k)) continue;
                     const F v = x_own[q] * inv_norm;
                     if (write_prev) outp[k] = v;
                     col[c * maxS + k] = v;  // normalised, for the next switch
@@ -615,61 +737,34 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
             F *nxt = col + (c ^ 1) * maxS;
             if (Tab<F>::split && tid == 0 && ci == COL_INVARIANT) acc.extra += lner;
             if (Tab<F>::split && tid == 0 && ci == COL_VARIANT) acc.extra += tab.lnvref[B.vrow0 + vrow];
+            if (!reducer) {
 #pragma unroll
-            for (int q = 0; q < KPT; q++) {
-                const F tfb = __shfl_sync(0xffffffffu, tf, st_time[q]);
-                const int k = tid + q * NT;
-                if (k >= S) continue;
-                const F xk = x_own[q];
-                if (write_prev) outp[k] = xk * inv_norm;
-                const F *nb = cur + st_j1[q];
-                const int m = st_m[q];
-                F s = tfb;
-                if (t2_in_smem) {
-                    // even terms into s, odd into s1, four loads ahead
-                    const F *row = t2s + st_off[q];
-                    int y = 0;
-                    F s1 = 0;
-                    for (; y + 3 < m; y += 4) {
-                        const F r0 = row[0], r1 = row[m], r2 = row[2 * m], r3 = row[3 * m];
-                        const F n0 = nb[y], n1 = nb[y + 1], n2 = nb[y + 2], n3 = nb[y + 3];
-                        s += r0 * n0;
-                        s1 += r1 * n1;
-                        s += r2 * n2;
-                        s1 += r3 * n3;
-                        row += 4 * m;
+                for (int q = 0; q < KPT; q++) {
+                    const int k = owned(q);
+                    if (!valid(k)) continue;
+                    const F xk = x_own[q];
+                    if (write_prev) outp[k] = xk * inv_norm;
+                    const F sv = tfs[st_time[q]] + dq[q];
+                    F v;
+                    if constexpr (Tab<F>::split) {
+                        // pairs: stay (1 - rs), plus the inflow, times the emission, rescaled
+                        F2 x = f2_keep(F2{xk, x_lo[q]}, st_rs[q]);
+                        x = f2_add(x, sv);
+                        if (ci == COL_INVARIANT) x = f2_keep(x, st_inv[q]);
+                        else if (ci != COL_MASKED)
+                            x = e_next[q] >= 0.0f ? f2_keep(x, e_next[q]) : f2_mul(x, -e_next[q]);
+                        x = f2_mul(x, inv_norm);
+                        v = x.hi;
+                        x_lo[q] = x.lo;
+                    } else {
+                        v = emit(sv, ci, vrow, q, true) * inv_norm;
                     }
-                    for (; y + 1 < m; y += 2) {
-                        s += row[0] * nb[y];
-                        s1 += row[m] * nb[y + 1];
-                        row += 2 * m;
-                    }
-                    if (y < m) s += row[0] * nb[y];
-                    s += s1;
-                } else {
-                    const int a0 = st_time[q] - (k - st_j1[q]);
-                    for (int y = 0; y < m; y++)
-                        s += tab.t2(B.t2_0 + st_off[q] + y * m, tmS[(a0 + y) * MAXT + st_time[q]]) * nb[y];
+                    nxt[k] = v;
+                    colT[st_rank[q]] = v;
+                    x_own[q] = v;
                 }
-                F v;
-                if constexpr (Tab<F>::split) {
-                    // pairs: stay (1 - rs), plus the inflow s, times the emission, rescaled
-                    F2 x = f2_keep(F2{xk, x_lo[q]}, st_rs[q]);
-                    x = f2_add(x, s);
-                    if (ci == COL_INVARIANT) x = f2_keep(x, st_inv[q]);
-                    else if (ci != COL_MASKED)
-                        x = e_next[q] >= 0.0f ? f2_keep(x, e_next[q]) : f2_mul(x, -e_next[q]);
-                    x = f2_mul(x, inv_norm);
-                    v = x.hi;
-                    x_lo[q] = x.lo;
-                } else {
-                    v = emit(s, ci, vrow, q, true) * inv_norm;
-                }
-                nxt[k] = v;
-                colT[st_rank[q]] = v;
-                x_own[q] = v;
+                if (i + 1 < len) prefetch(i + 1);
             }
-            if (i + 1 < len) prefetch(i + 1);
             c ^= 1;
         }
         __syncthreads();
@@ -728,16 +823,17 @@ void launch_reg(const BatchDev &d, int nt, cudaStream_t s) {
     note_launch();
 }
 
-// States per thread of the register variant (1, 2, 4 or 8; AWG_FORWARD_KPT overrides it
-// for tuning); the CTA then has ceil(maxS / KPT) threads rounded up to whole warps.
+// States per owner thread of the register variant (1, 2, 4 or 8; AWG_FORWARD_KPT overrides
+// it for tuning); the CTA then has the reduction warp plus ceil(maxS / KPT) owners rounded
+// up to whole warps.
 int reg_kpt(int maxS) {
     static const int env = [] {
         const char *e = getenv("AWG_FORWARD_KPT");
         return e ? atoi(e) : 0;
     }();
     int k = (env == 1 || env == 2 || env == 4 || env == 8) ? env
-          : maxS <= 64 ? 1 : maxS <= 1024 ? 2 : maxS <= 2048 ? 4 : 8;
-    while (k < 8 && (maxS + k - 1) / k > 512) k *= 2;
+          : maxS <= 64 ? 1 : maxS <= 960 ? 2 : maxS <= 1920 ? 4 : 8;
+    while (k < 8 && (maxS + k - 1) / k > 480) k *= 2;
     return k;
 }
 
@@ -745,7 +841,8 @@ template <typename F>
 void launch(const BatchDev &d, cudaStream_t s) {
     const int maxS = imax(d.maxS, 1);
     const int kpt = reg_kpt(maxS);
-    const int nt = imax(32, ((maxS + kpt - 1) / kpt + 31) / 32 * 32);
+    // the reduction warp plus ceil(maxS / KPT) owners in whole warps
+    const int nt = 32 + imax(32, ((maxS + kpt - 1) / kpt + 31) / 32 * 32);
     if (nt > 512) launch_old<F>(d, d.maxM, s);
     else if (kpt == 1) launch_reg<F, 1>(d, nt, s);
     else if (kpt == 2) launch_reg<F, 2>(d, nt, s);

@@ -398,6 +398,9 @@ __device__ __forceinline__ F2 f2_add(F2 x, float s) {
     return f2_renorm(h, err + x.lo);
 }
 
+constexpr int NRW = 4;                      // reduction warps of the register variant
+constexpr int RBINS = (MAXT - 1 + NRW - 1) / NRW;  // time bins per reduction warp (<= 8)
+
 template <typename F, int KPT>
 __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int maxM, int t2_in_smem) {
     extern __shared__ double dyn_d[];
@@ -406,18 +409,19 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
     const InstDev I = d.inst[qi];
     const int T = I.T, NB = T - 1;
     const int tid = threadIdx.x, lane = tid & 31;
-    const int NT = blockDim.x, NTS = NT - 32;   // state owners: threads 32 ..
-    const int st = tid - 32;                    // owner index (negative in warp 0)
-    const bool reducer = tid < 32;
+    const int NT = blockDim.x, NTS = NT - 32 * NRW;  // state owners: threads 32 NRW ..
+    const int st = tid - 32 * NRW;                   // owner index (negative in reducers)
+    const bool reducer = tid < 32 * NRW;
+    const int rw = tid >> 5;                         // reducer warp: bins [blo, bhi)
 
     F *col = (F *)dyn_d;                       // [2][maxS] columns in state order
     F *colT = col + 2 * maxS;                  // [maxS] newest column, time-sorted
     F *t2s = colT + maxS;                      // [maxM] same-branch entries of the block
     __shared__ F tmS[MAXT * MAXT];             // [b][a] tmatrix; column 31 holds ones
-    __shared__ F part[32][MAXT];               // reducer: per lane, its chunk's bin sums
-    __shared__ F tfs[32];                      // tf by time; [31]: the column's norm
+    __shared__ F part[NRW][32][RBINS];         // reducers: per lane, its chunk's bin sums
+    __shared__ F tfp[NRW][32];                 // each reducer's share of tf; [31]: of the norm
     __shared__ int bptr[MAXT + 1];
-    __shared__ int fbin[32];                   // reducer: first bin of each lane's chunk
+    __shared__ int fbin[NRW][32];              // reducers: first bin of each lane's chunk
 
     LogAcc acc;
     int c = 0;                                 // buffer holding the current column
@@ -497,29 +501,32 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
             const int k = owned(q);
             st_rank[q] = valid(k) ? (int)col[(c ^ 1) * maxS + k] : 0;
         }
-        // reducer: lane l sums sorted positions [l C, (l + 1) C); lane b adds the chunk
-        // sums of lanes l0_b .. l1_b
-        const int chunk = (S + 31) >> 5;
-        const int clo = imin(lane * chunk, S), chi = imin(clo + chunk, S);
+        // reducer warp rw: bins [blo, bhi), sorted positions [plo, phi); lane l sums its
+        // chunk of ceil((phi - plo) / 32) positions, lane b - blo adds bin b's chunk sums
+        const int blo = reducer ? rw * NB / NRW : 0, bhi = reducer ? (rw + 1) * NB / NRW : 0;
+        const int plo = reducer ? bptr[blo] : 0, phi = reducer ? bptr[bhi] : 0;
+        const int chunk = imax((phi - plo + 31) >> 5, 1);
+        const int clo = imin(plo + lane * chunk, phi), chi = imin(clo + chunk, phi);
         int l0 = 0, l1 = -1;
         int o1 = 0, o2 = 0, nbc = 0;  // bin boundaries inside the chunk, bins it spans
         if (reducer) {
-            int fb = 0;
-            while (fb < NB - 1 && bptr[fb + 1] <= clo) fb++;
-            fbin[lane] = fb;
-            if (lane < NB && bptr[lane + 1] > bptr[lane]) {
-                l0 = bptr[lane] / chunk;
-                l1 = (bptr[lane + 1] - 1) / chunk;
+            int fb = blo;
+            while (fb < bhi - 1 && bptr[fb + 1] <= clo) fb++;
+            fbin[rw][lane] = fb;
+            const int b = blo + lane;
+            if (b < bhi && bptr[b + 1] > bptr[b]) {
+                l0 = (bptr[b] - plo) / chunk;
+                l1 = (bptr[b + 1] - 1 - plo) / chunk;
             }
             if (chi > clo) {
-                int b = fb;
+                int bb = fb;
                 nbc = 1;
                 o1 = o2 = chi - clo;
-                while (b < NB - 1 && bptr[b + 1] < chi) {
-                    if (nbc == 1) o1 = bptr[b + 1] - clo;
-                    else if (nbc == 2) o2 = bptr[b + 1] - clo;
+                while (bb < bhi - 1 && bptr[bb + 1] < chi) {
+                    if (nbc == 1) o1 = bptr[bb + 1] - clo;
+                    else if (nbc == 2) o2 = bptr[bb + 1] - clo;
                     nbc++;
-                    b++;
+                    bb++;
                 }
             }
         }
@@ -636,40 +643,34 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
                             a2 += jj >= o2 ? v[j] : F(0);
                         }
                     }
-                    if (nbc >= 1) part[lane][0] = a0;
-                    if (nbc >= 2) part[lane][1] = a1;
-                    if (nbc >= 3) part[lane][2] = a2;
+                    if (nbc >= 1) part[rw][lane][0] = a0;
+                    if (nbc >= 2) part[rw][lane][1] = a1;
+                    if (nbc >= 3) part[rw][lane][2] = a2;
                 } else {
-                    int bcur = fbin[lane], j = 0, nextb = bptr[bcur + 1];
+                    int bcur = fbin[rw][lane], j = 0, nextb = bptr[bcur + 1];
                     F a = 0;
                     for (int p = clo; p < chi; p++) {
                         while (p >= nextb) {
-                            part[lane][j++] = a;
+                            part[rw][lane][j++] = a;
                             a = F(0);
                             bcur++;
                             nextb = bptr[bcur + 1];
                         }
                         a += colT[p];
                     }
-                    if (chi > clo) part[lane][j] = a;
+                    if (chi > clo) part[rw][lane][j] = a;
                 }
                 __syncwarp();
-                F bin = 0;
-                for (int l = l0; l <= l1; l++) bin += part[l][lane - fbin[l]];
-                // tf[a] = sum_b tm[b][a] bin[b]: four partial sums (b mod 4), then combined
-                F t0 = 0, t1 = 0, t2 = 0, t3 = 0;
+                F bin = 0;  // lane b - blo: bin b
+                for (int l = l0; l <= l1; l++) bin += part[rw][l][blo + lane - fbin[rw][l]];
+                // this warp's share of tf[a] = sum_b tm[b][a] bin[b], its bins in order
+                F tf = 0;
 #pragma unroll
-                for (int b = 0; b < MAXT - 1; b += 4) {
-                    const F g0 = __shfl_sync(0xffffffffu, bin, b);
-                    const F g1 = __shfl_sync(0xffffffffu, bin, b + 1);
-                    const F g2 = __shfl_sync(0xffffffffu, bin, b + 2);
-                    const F g3 = __shfl_sync(0xffffffffu, bin, b + 3);
-                    if (b < NB) t0 += tmS[b * MAXT + lane] * g0;
-                    if (b + 1 < NB) t1 += tmS[(b + 1) * MAXT + lane] * g1;
-                    if (b + 2 < NB) t2 += tmS[(b + 2) * MAXT + lane] * g2;
-                    if (b + 3 < NB) t3 += tmS[(b + 3) * MAXT + lane] * g3;
+                for (int j = 0; j < RBINS; j++) {
+                    const F g = __shfl_sync(0xffffffffu, bin, j);
+                    if (blo + j < bhi) tf += tmS[(blo + j) * MAXT + lane] * g;
                 }
-                tfs[lane] = (t0 + t1) + (t2 + t3);
+                tfp[rw][lane] = tf;
             } else {
                 // same-branch dot of the owned states: sum_y tmatrix2[a_y][k] col[j1 + y]
 #pragma unroll
@@ -710,7 +711,9 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
                 }
             }
             __syncthreads();  // B: tf and the norm of column i-1
-            const F norm = tfs[MAXT - 1];
+            F norm = 0;
+#pragma unroll
+            for (int r = 0; r < NRW; r++) norm += tfp[r][MAXT - 1];
             const F inv_norm = F(1) / norm;
             if (tid == 0) {
                 acc.add((double)norm);
@@ -744,7 +747,10 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
                     if (!valid(k)) continue;
                     const F xk = x_own[q];
                     if (write_prev) outp[k] = xk * inv_norm;
-                    const F sv = tfs[st_time[q]] + dq[q];
+                    F tfk = 0;
+#pragma unroll
+                    for (int r = 0; r < NRW; r++) tfk += tfp[r][st_time[q]];
+                    const F sv = tfk + dq[q];
                     F v;
                     if constexpr (Tab<F>::split) {
                         // pairs: stay (1 - rs), plus the inflow, times the emission, rescaled
@@ -832,8 +838,8 @@ int reg_kpt(int maxS) {
         return e ? atoi(e) : 0;
     }();
     int k = (env == 1 || env == 2 || env == 4 || env == 8) ? env
-          : maxS <= 64 ? 1 : maxS <= 960 ? 2 : maxS <= 1920 ? 4 : 8;
-    while (k < 8 && (maxS + k - 1) / k > 480) k *= 2;
+          : maxS <= 64 ? 1 : maxS <= 768 ? 2 : maxS <= 1536 ? 4 : 8;
+    while (k < 8 && (maxS + k - 1) / k > 384) k *= 2;
     return k;
 }
 
@@ -841,8 +847,8 @@ template <typename F>
 void launch(const BatchDev &d, cudaStream_t s) {
     const int maxS = imax(d.maxS, 1);
     const int kpt = reg_kpt(maxS);
-    // the reduction warp plus ceil(maxS / KPT) owners in whole warps
-    const int nt = 32 + imax(32, ((maxS + kpt - 1) / kpt + 31) / 32 * 32);
+    // the reduction warps plus ceil(maxS / KPT) owners in whole warps
+    const int nt = 32 * NRW + imax(32, ((maxS + kpt - 1) / kpt + 31) / 32 * 32);
     if (nt > 512) launch_old<F>(d, d.maxM, s);
     else if (kpt == 1) launch_reg<F, 1>(d, nt, s);
     else if (kpt == 2) launch_reg<F, 2>(d, nt, s);

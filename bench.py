@@ -37,6 +37,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "HMM state-cells/s fwd+traceback, batched FP32 vs plain FP64 @<=1e-5 err; p50/p99"
+FWD_DRAM_BYTES_PER_CELL = 3.93  # forward kernel, ncu capture summarised in profiles/
 UNIT = "state-cells/s"
 
 
@@ -262,8 +263,10 @@ def main():
             break
     plain = plain_cells / plain_t
 
-    # error report outside the timed region: FP32 vs FP64 posteriors on a few problems
-    sample = sorted(problems, key=lambda p: p.cells())[:4]
+    # error report outside the timed region: FP32 vs FP64 posteriors on the two largest
+    # problems and two from the middle of the size range
+    by_size = sorted(problems, key=lambda p: p.cells())
+    sample = by_size[-2:] + by_size[len(by_size) // 2:len(by_size) // 2 + 2]
     errs = []
     for p in sample:
         a = api.run_batch([p], precision="fp32", want_forward=False, want_posterior=True)[0]
@@ -295,7 +298,11 @@ def main():
                 "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * wall_s / args.steps,
                 "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99))},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": None, "peak_source": src,
+                     "frac": achieved / hbm,
+                     # DRAM bytes of one forward launch: ncu dram__bytes_read.sum +
+                     # dram__bytes_write.sum on the 16 x 10,000-column capture, 3.93 B per
+                     # state-cell, scaled to this launch's cells (profiles/)
+                     "traffic": FWD_DRAM_BYTES_PER_CELL * cells, "peak_source": src,
                      "kernel": "forward (k_forward_reg), 4 B of FP32 table written per cell, "
                                "timed alone (phases run one after another)"},
         "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
@@ -305,6 +312,7 @@ def main():
                        "sample": f"{plain_n} smallest problems, one arghmm_sample_posterior "
                                  "call each (FP64, forward + traceback)"},
         "fp32_vs_fp64_posterior_max_abs_err": max(errs),
+        "error_sample": "the 2 largest and 2 median problems of the batch, full length",
         "gpu_launches": launches,
         "clocks": clocks,
         "phase_ms": phase_ms,

@@ -91,6 +91,18 @@ def test_fp32_close_to_fp64(name):
     assert abs(r32.loglik - r64.loglik) <= 1e-5 * abs(r64.loglik)
 
 
+@pytest.mark.parametrize("k,seed", [(59, 11), (31, 12), (63, 13)])
+def test_fp32_close_to_fp64_long(k, seed):
+    """The FP32 bar on long problems (20,000 columns, 0.5% missing calls): the FP32
+    column step converges to its own fixed point within each tree, so errors that are
+    invisible on short fixtures show here first."""
+    prob = simulate(k, 20000, seed=seed, missing=0.005)
+    r32, r64 = (api.run_batch([prob], precision=p, want_forward=False, want_posterior=True)[0]
+                for p in ("fp32", "fp64"))
+    assert np.max(np.abs(r32.posterior - r64.posterior)) <= 1e-5
+    assert abs(r32.loglik - r64.loglik) <= 1e-5 * abs(r64.loglik)
+
+
 @pytest.mark.parametrize("name", EXTERNAL_DEFAULT_MAP)
 def test_c_abi_forward_alg(name):
     prob, gold = load(name)

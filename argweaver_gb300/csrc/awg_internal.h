@@ -113,6 +113,10 @@ struct BatchDev {
     //   lnvref   [variant columns] log(e_ref) of each variant column
     float *tm32, *t2d32, *inv32, *var32, *determprob32, *recombrow32, *recoalrow32, *rstay32;
     double *lneref, *lnvref;
+    // [total columns * MAXT] or NULL: per stored FP32 forward column, its time-bin sums
+    // (the fgroups of arghmm_forward_block, sample_thread.cpp:258-263), written by the
+    // forward kernel for the traceback's decomposed draw
+    float *bins32;
 
     // outputs
     double *fw64;                // forward table (FP64 path)
@@ -156,6 +160,7 @@ enum : int {
     ERR_ZERO_NORM = 3,          // a forward column summed to zero (reference asserts top > 0)
     ERR_PLAN_MISMATCH = 4,      // device state count disagrees with the host plan
     ERR_BOUNDS = 5,             // an index derived from the inputs fell outside its array
+    ERR_WAIT_LIMIT = 6,         // a bounded wait for an asynchronous copy ran out
 };
 
 }  // namespace awg

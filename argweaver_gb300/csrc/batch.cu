@@ -199,6 +199,9 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
     const size_t o_post = w.add(want_post ? sizeof(double) * CELLS : 0);
     const size_t o_bw = w.add(want_bw ? sizeof(double) * CELLS : 0);
     const size_t o_path = w.add(want_path ? sizeof(int) * COLS : 0);
+    // FP32 traceback: the forward columns' time-bin sums
+    const bool want_bins = fp32 && want_path && forward_writes_bins(plan.maxS);
+    const size_t o_bins = w.add(want_bins ? sizeof(float) * MAXT * COLS : 0);
     const size_t o_err = w.add(4 * sizeof(int));
     const size_t total = w.total;
 
@@ -293,6 +296,7 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
     d.post = want_post ? (double *)(D + o_post) : nullptr;
     d.uniforms = want_path ? (const double *)(D + o_u) : nullptr;
     d.path = want_path ? (int *)(D + o_path) : nullptr;
+    d.bins32 = want_bins ? (float *)(D + o_bins) : nullptr;
     d.err = (int *)(D + o_err);
 
     // Schedule. Serial: per-tree kernels over the batch, then per-instance kernels. Pipelined
@@ -463,10 +467,11 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
         static const char *what[] = {"", "switch from a fully specified tree found no state",
                                      "shared-memory plan exceeded", "a forward column summed to "
                                      "zero or NaN", "device state count differs from the plan",
-                                     "an index derived from the inputs is out of range"};
+                                     "an index derived from the inputs is out of range",
+                                     "a bounded wait for an asynchronous copy ran out"};
         char buf[256];
         snprintf(buf, sizeof(buf), "device error %d (%s) at problem %d, tree %d, column %d",
-                 dev_err[0], dev_err[0] < 6 ? what[dev_err[0]] : "?", dev_err[1], dev_err[2],
+                 dev_err[0], dev_err[0] < 7 ? what[dev_err[0]] : "?", dev_err[1], dev_err[2],
                  dev_err[3]);
         err = buf;
         return -4;

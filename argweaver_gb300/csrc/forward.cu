@@ -625,6 +625,7 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
         for (int i = 1; i <= len; i++) {
             __syncthreads();  // A: column i-1 complete
             const F *cur = col + c * maxS;
+            F binv = F(0);  // reducers, lane b - blo: bin b of column i-1
             if (reducer) {
                 // chunk sums by bin (positions sorted by time)
                 if (fast_chunk) {
@@ -663,6 +664,7 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
                 __syncwarp();
                 F bin = 0;  // lane b - blo: bin b
                 for (int l = l0; l <= l1; l++) bin += part[rw][l][blo + lane - fbin[rw][l]];
+                binv = bin;
                 // this warp's share of tf[a] = sum_b tm[b][a] bin[b], its bins in order
                 F tf = 0;
 #pragma unroll
@@ -722,6 +724,12 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
             // finalise column i-1: normalised into the table (the instance's column 0
             // keeps the unnormalised prior, as the reference's table does)
             const bool write_prev = !(bi == 0 && i == 1);
+            if constexpr (Tab<F>::split) {
+                // the stored column's time-bin sums, on the stored column's scale
+                if (reducer && d.bins32 && blo + lane < bhi)
+                    d.bins32[(size_t)(I.col0 + B.start + i - 1) * MAXT + blo + lane] =
+                        write_prev ? binv * inv_norm : binv;
+            }
             F *outp = fw + (size_t)(i - 1) * S;
             if (i == len) {
 #pragma unroll
@@ -857,6 +865,11 @@ void launch(const BatchDev &d, cudaStream_t s) {
 }
 
 }  // namespace
+
+bool forward_writes_bins(int maxS) {
+    const int kpt = reg_kpt(imax(maxS, 1));
+    return 32 * NRW + imax(32, ((imax(maxS, 1) + kpt - 1) / kpt + 31) / 32 * 32) <= 512;
+}
 
 void launch_forward(const BatchDev &d, bool fp32, cudaStream_t s) {
     if (fp32) launch<float>(d, s);

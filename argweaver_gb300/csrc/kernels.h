@@ -14,7 +14,10 @@ void launch_tables(const BatchDev &d, bool want32, cudaStream_t s);
 void launch_varemit(const BatchDev &d, bool want32, cudaStream_t s);
 // K3: forward pass, one CTA per instance.
 void launch_forward(const BatchDev &d, bool fp32, cudaStream_t s);
-// K4: stochastic traceback, one warp per instance.
+// Whether K3 writes the FP32 columns' time-bin sums (BatchDev::bins32) at this state count
+// (the register-resident variant does; the fallback for the largest trees does not).
+bool forward_writes_bins(int maxS);
+// K4: stochastic traceback, one warp per instance; FP32 with bins32 set: the decomposed draw.
 void launch_traceback(const BatchDev &d, bool fp32, cudaStream_t s);
 // K5: backward pass fused with the posterior marginals, one CTA per instance.
 void launch_backward(const BatchDev &d, bool fp32, double *bw_out, cudaStream_t s);

@@ -360,6 +360,445 @@ __global__ void k_traceback(BatchDev d, int maxS, int slot_elems) {
     cp_wait<0>();
 }
 
+// ---------------------------------------------------------------------------------------
+// FP32 path: the draw decomposed by the structure of the transition.
+//
+// Inside a tree P(j -> k) = tm[a_j][b_k] + [node_j = node_k] tm2[a_j][k] (the structured
+// step of arghmm_forward_block, sample_thread.cpp:255-290; tm2 >= 0 is the same-branch
+// excess, the no-recombination stay included on the diagonal). Column i's weights
+// fw[i][j] P(j -> k) thus split into the same-branch part V_y = fw[i][j1 + y] tm2[a_y][k]
+// over the m states of k's node, and a background part whose total over the states of
+// time bin a is W_a = bins[i][a] tm[a][b_k], bins[i] being the stored column's time-bin
+// sums that the forward kernel writes. With t = u (V + W): if t <= V the draw is the first
+// y whose running V sum reaches t; else the first bin whose running W sum reaches t - V,
+// then the first state of that bin (states of a bin in time-sorted order) whose running
+// fw sum reaches the remainder over tm[a][b_k]. This draws from exactly the distribution
+// of the reference's scan over all states (sample(), common.h:272-290), mapping the
+// uniform to states in another order, with O(T + m) work per column instead of O(S).
+//
+// Speculation: the warp tests 8 columns at once for the common case, the draw staying at
+// the current state k: lanes 4g .. 4g+3 take column g, each a quarter of the node's states
+// and of the bins, and combine V before k, V at k, V and W by two butterfly steps. The
+// first column whose draw leaves k (if any) is drawn exactly by the whole warp; the
+// columns after it are tested again under the new state.
+//
+// Data movement is TMA bulk copies (cp.async.bulk) completing on mbarriers, issued by one
+// lane: each forward column (with its bins and uniform) streams into a ring DEPTH columns
+// ahead of the sampler, and each tree's tables (tmatrix, stay complements, time-bin CSR,
+// state info, row offsets, switch targets and probabilities) into one of two buffers one
+// tree ahead, so the warp's time goes into sampling rather than load latency. Every wait
+// is bounded; one that runs out records ERR_WAIT_LIMIT and the kernel returns.
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) {
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+// Global -> shared bulk copy: both addresses 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+__device__ __forceinline__ bool mbar_test(uint64_t *bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+constexpr int WAIT_TRIES = 1 << 22;  // try_wait rounds before a wait gives up
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
+    for (int it = 0; it < WAIT_TRIES; it++)
+        if (mbar_test(bar, parity)) return true;
+    return false;
+}
+
+// An array of 4-byte elements copied from its 16-byte-aligned start: bytes to copy and the
+// element offset of the array inside the copy.
+struct Rounded {
+    const char *a16;
+    unsigned bytes;
+    int off;
+};
+__device__ __forceinline__ Rounded rounded(const void *p, int count) {
+    Rounded r;
+    r.a16 = (const char *)((uintptr_t)p & ~(uintptr_t)15);
+    r.off = (int)(((uintptr_t)p & 15) >> 2);
+    r.bytes = count > 0 ? (unsigned)(((const char *)p + 4 * (size_t)count - r.a16 + 15) & ~(size_t)15) : 0u;
+    return r;
+}
+
+// Fields of a tree the traceback needs, in registers.
+struct TreeRef {
+    int blk, start, len, S, S1;
+    long long cell0, state0, prev_state0, t2_0;
+};
+__device__ __forceinline__ TreeRef tree_ref(const BatchDev &d, int blk) {
+    const BlockDev &B = d.blocks[blk];
+    return TreeRef{blk, B.start, B.len, B.S, B.S1, B.cell0, B.state0, B.prev_state0, B.t2_0};
+}
+
+// Layout of one tree buffer (bytes from its start; every part 16-byte aligned).
+struct TreeBufLayout {
+    int tm, rstay, bptr, sinfo, t2off, perm, determ, dp, total;
+    __host__ __device__ explicit TreeBufLayout(int maxS) {
+        const int arr = (4 * maxS + 16 + 15) & ~15;  // a 4-byte array copied from 16-B start
+        tm = 0;
+        rstay = tm + 4 * MAXT * MAXT;
+        bptr = rstay + 4 * MAXT;
+        sinfo = bptr + 160;
+        t2off = sinfo + 16 * maxS;
+        perm = t2off + arr;
+        determ = perm + arr;
+        dp = determ + arr;
+        total = dp + arr;
+    }
+};
+
+template <int DEPTH>
+__global__ void __launch_bounds__(32) k_traceback_split(BatchDev d, int maxS, int slot_elems) {
+    constexpr int G = 8;
+    constexpr unsigned FULL = 0xffffffffu;
+    extern __shared__ __align__(16) unsigned char dyn_b[];
+    float *ring = (float *)dyn_b;                                   // [DEPTH][slot_elems]
+    float *bring = ring + (size_t)DEPTH * slot_elems;               // [DEPTH][MAXT] bins
+    double *uring = (double *)(bring + DEPTH * MAXT);               // [DEPTH][2] uniform pairs
+    unsigned char *tbuf = (unsigned char *)(uring + 2 * DEPTH);     // [2] tree buffers
+    __shared__ uint64_t cbar[DEPTH];                                // column ring barriers
+    __shared__ uint64_t tbar[2];                                    // tree buffer barriers
+    __shared__ float t2row[32], tmcol[32];                          // the state's V, W factors
+    const TreeBufLayout TL(maxS);
+    const TTab<float> tab(d);
+    const int qi = cta_instance(d);
+    const InstDev I = d.inst[qi];
+    const int lane = threadIdx.x;
+    const int NB = I.T - 1;
+    int *path = d.path + I.col0;
+    const double *u = d.uniforms + I.col0;
+    const float *bins = d.bins32 + (size_t)I.col0 * MAXT;
+    const int L = I.seqlen;
+    bool failed = false;
+
+    if (lane == 0) {
+        for (int q = 0; q < DEPTH; q++) mbar_init(&cbar[q], 1);
+        mbar_init(&tbar[0], 1);
+        mbar_init(&tbar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncwarp();
+
+    // ---- column ring: column c is the n-th issued (n = L - 1 - c), slot n % DEPTH, phase n / DEPTH
+    int pcol = L - 1, pblk = I.ntrees - 1;
+    TreeRef pc = tree_ref(d, I.block0 + pblk);
+    TreeRef pn = pblk > 0 ? tree_ref(d, I.block0 + pblk - 1) : pc;  // the cursor's next tree
+    auto issue = [&]() {
+        if (pcol < 0) return;
+        if (lane == 0) {
+            const int n = L - 1 - pcol, slot = n % DEPTH;
+            const int Sm = imax(pc.S, 1);
+            const Rounded r = rounded(tab.fw + pc.cell0 + (size_t)(pcol - pc.start) * Sm, Sm);
+            const double *up = (const double *)((uintptr_t)(u + pcol) & ~(uintptr_t)15);
+            mbar_expect_tx(&cbar[slot], r.bytes + 4 * MAXT + 16);
+            bulk_g2s(ring + (size_t)slot * slot_elems, r.a16, r.bytes, &cbar[slot]);
+            bulk_g2s(bring + slot * MAXT, bins + (size_t)pcol * MAXT, 4 * MAXT, &cbar[slot]);
+            bulk_g2s(uring + 2 * slot, up, 16, &cbar[slot]);
+        }
+        pcol--;
+        if (pblk > 0 && pcol < pc.start) {
+            pblk--;
+            pc = pn;
+            if (pblk > 0) pn = tree_ref(d, I.block0 + pblk - 1);
+        }
+    };
+    auto wait_col = [&](int c) -> bool {
+        const int n = L - 1 - c;
+        return mbar_wait(&cbar[n % DEPTH], (unsigned)((n / DEPTH) & 1));
+    };
+    auto slot_of = [&](int c) { return (L - 1 - c) % DEPTH; };
+    auto column = [&](const TreeRef &B, int c) -> const float * {
+        const int Sm = imax(B.S, 1);
+        const float *g = tab.fw + B.cell0 + (size_t)(c - B.start) * Sm;
+        return ring + (size_t)slot_of(c) * slot_elems + col_offset(g);
+    };
+    auto uniform = [&](int c) -> double {
+        return uring[2 * slot_of(c) + (int)(((uintptr_t)(u + c) >> 3) & 1)];
+    };
+
+    // ---- tree buffers: tree x in buffer x & 1
+    unsigned tphase[2] = {0u, 0u};
+    bool tpend[2] = {false, false};  // staged, not yet waited for
+    int o_t2off[2], o_perm[2], o_determ[2], o_dp[2], o_bptr[2];
+    auto stage = [&](const TreeRef &X) {
+        const int b = X.blk & 1;
+        unsigned char *base = tbuf + (size_t)b * TL.total;
+        const int S = X.S, S1 = imax(X.S1, 1);
+        const Rounded rb = rounded(d.bt_ptr + (size_t)X.blk * (MAXT + 1), MAXT + 1);
+        const Rounded rt = rounded(d.t2off + X.state0, S);
+        const Rounded rp = rounded(d.bt_perm + X.state0, S);
+        const Rounded rd = rounded(d.determ + X.prev_state0, S1);
+        const Rounded rq = rounded(tab.dprob + X.prev_state0, S1);
+        const bool sw = X.start > 0;  // a switch into this tree exists
+        tpend[b] = true;
+        o_bptr[b] = rb.off;
+        o_t2off[b] = rt.off;
+        o_perm[b] = rp.off;
+        o_determ[b] = rd.off;
+        o_dp[b] = rq.off;
+        if (lane == 0) {
+            const unsigned tmb = 4u * MAXT * (unsigned)NB;
+            const unsigned tx = (S > 0 ? tmb + 4 * MAXT + rb.bytes + 16u * S + rt.bytes + rp.bytes : 0u) +
+                                (sw ? rd.bytes + rq.bytes : 0u);
+            mbar_expect_tx(&tbar[b], tx);
+            if (S > 0) {
+                bulk_g2s(base + TL.tm, tab.tm + (size_t)X.blk * MAXT * MAXT, tmb, &tbar[b]);
+                bulk_g2s(base + TL.rstay, tab.rstay + (size_t)X.blk * MAXT, 4 * MAXT, &tbar[b]);
+                bulk_g2s(base + TL.bptr, rb.a16, rb.bytes, &tbar[b]);
+                bulk_g2s(base + TL.sinfo, d.sinfo + X.state0, 16u * S, &tbar[b]);
+                bulk_g2s(base + TL.t2off, rt.a16, rt.bytes, &tbar[b]);
+                bulk_g2s(base + TL.perm, rp.a16, rp.bytes, &tbar[b]);
+            }
+            if (sw) {
+                bulk_g2s(base + TL.determ, rd.a16, rd.bytes, &tbar[b]);
+                bulk_g2s(base + TL.dp, rq.a16, rq.bytes, &tbar[b]);
+            }
+        }
+    };
+    auto wait_tree = [&](int blk) -> bool {
+        const int b = blk & 1;
+        const bool ok = mbar_wait(&tbar[b], tphase[b]);
+        tphase[b] ^= 1u;
+        tpend[b] = false;
+        return ok;
+    };
+
+    for (int q = 0; q < DEPTH; q++) issue();
+    TreeRef cur = tree_ref(d, I.block0 + I.ntrees - 1);
+    TreeRef nx1 = I.ntrees > 1 ? tree_ref(d, I.block0 + I.ntrees - 2) : cur;
+    stage(cur);
+
+    int col = L - 1;
+    int state;
+    {
+        failed |= !wait_col(col);
+        __syncwarp();
+        const float *c = column(cur, col);
+        const int x = warp_sample<float>(imax(cur.S, 1), uniform(col), [&](int j) { return c[j]; });
+        if (lane == 0) path[col] = x;
+        state = x;
+        __syncwarp();
+        issue();
+    }
+    const int g = lane >> 2, sub = lane & 3;  // fast path: column g of a group, quarter sub
+    for (int bi = I.ntrees - 1; bi >= 0 && !failed; bi--) {
+        const TreeRef B = cur;
+        const int b = B.blk & 1;
+        const unsigned char *base = tbuf + (size_t)b * TL.total;
+        failed |= !wait_tree(B.blk);
+        __syncwarp();
+        // tables of the next tree, while this one is sampled
+        TreeRef nx2 = nx1;
+        if (bi > 0) {
+            stage(nx1);
+            if (bi > 1) nx2 = tree_ref(d, I.block0 + bi - 2);
+        }
+        const float *tmS = (const float *)(base + TL.tm);
+        const float *rst = (const float *)(base + TL.rstay);
+        const int *bptr = (const int *)(base + TL.bptr) + o_bptr[b];
+        const StateInfo *sinfo = (const StateInfo *)(base + TL.sinfo);
+        const int *t2off = (const int *)(base + TL.t2off) + o_t2off[b];
+        const int *perm = (const int *)(base + TL.perm) + o_perm[b];
+        const int S = B.S;
+        int c0 = B.start + B.len - 2;
+        if (S == 0) {
+            // fully specified tree: its single state carries over (each column is still
+            // waited for, so its ring slot is free before the slot is issued again)
+            for (; c0 >= B.start && !failed; c0--) {
+                failed |= !wait_col(c0);
+                __syncwarp();
+                if (lane == 0) path[c0] = 0;
+                issue();
+            }
+        } else {
+            int kj1 = 0, km = 0, ys = 0;
+            float t2r[8], tmr[8];
+            auto set_state = [&](int k) {
+                const StateInfo sk = sinfo[k];
+                kj1 = sk.j1;
+                km = sk.m;
+                ys = k - sk.j1;
+                const long long row = B.t2_0 + t2off[k];
+                const float stay = 1.0f - rst[sk.time];
+                __syncwarp();
+                t2row[lane] = lane < km ? tab.t2d[row + (long long)lane * km] + (lane == ys ? stay : 0.0f) : 0.0f;
+                tmcol[lane] = lane < NB ? tmS[lane * MAXT + sk.time] : 0.0f;
+                __syncwarp();
+#pragma unroll
+                for (int q = 0; q < 8; q++) {
+                    t2r[q] = t2row[8 * sub + q];
+                    tmr[q] = tmcol[8 * sub + q];
+                }
+            };
+            set_state(state);
+            while (c0 >= B.start && !failed) {
+                const int ng = imin(G, c0 - B.start + 1);
+                const int cg = c0 - imin(g, ng - 1);
+                failed |= !__all_sync(FULL, wait_col(cg));
+                if (failed) break;
+                // fast path: does column g's draw stay at the current state?
+                const float *cp = column(B, cg);
+                const float *bp = bring + slot_of(cg) * MAXT;
+                float sb = 0.0f, ss = 0.0f, sa = 0.0f, sw = 0.0f;
+#pragma unroll
+                for (int q = 0; q < 8; q++) {
+                    const int y = 8 * sub + q;
+                    const float v = y < km ? cp[kj1 + y] * t2r[q] : 0.0f;
+                    sa += v;
+                    sb += y < ys ? v : 0.0f;
+                    ss += y == ys ? v : 0.0f;
+                    sw += y < NB ? bp[y] * tmr[q] : 0.0f;
+                }
+#pragma unroll
+                for (int o = 1; o < 4; o <<= 1) {
+                    sb += __shfl_xor_sync(FULL, sb, o);
+                    ss += __shfl_xor_sync(FULL, ss, o);
+                    sa += __shfl_xor_sync(FULL, sa, o);
+                    sw += __shfl_xor_sync(FULL, sw, o);
+                }
+                const float t = (float)uniform(cg) * (sa + sw);
+                const bool stay = (ys == 0 || sb < t) && t <= sb + ss;
+                const unsigned leave = __ballot_sync(FULL, sub == 0 && g < ng && !stay);
+                const int nstay = leave ? (__ffs(leave) - 1) >> 2 : ng;
+                if (sub == 0 && g < nstay) path[c0 - g] = state;
+                int x = state;
+                if (leave) {
+                    // exact draw of the first column that leaves, by the whole warp
+                    const int cs = c0 - nstay;
+                    const float *cq = column(B, cs);
+                    const float *bq = bring + slot_of(cs) * MAXT;
+                    const float v = lane < km ? cq[kj1 + lane] * t2row[lane] : 0.0f;
+                    const float w = lane < NB ? bq[lane] * tmcol[lane] : 0.0f;
+                    const float vin = lane_scan(v, lane), win = lane_scan(w, lane);
+                    const float vt = __shfl_sync(FULL, vin, 31), wt = __shfl_sync(FULL, win, 31);
+                    const float tt = (float)uniform(cs) * (vt + wt);
+                    if (tt <= vt) {
+                        const unsigned hit = __ballot_sync(FULL, lane < km && vin >= tt);
+                        x = kj1 + (hit ? __ffs(hit) - 1 : km - 1);
+                    } else {
+                        const float t2 = tt - vt;
+                        const unsigned hit = __ballot_sync(FULL, lane < NB && win >= t2);
+                        const unsigned pos = __ballot_sync(FULL, w > 0.0f);
+                        const int a = hit ? __ffs(hit) - 1 : (pos ? 31 - __clz(pos) : 0);
+                        const float excl = __shfl_sync(FULL, win - w, a);
+                        const float r = (t2 - excl) / tmcol[a];  // threshold on the fw scale
+                        const int p0 = bptr[a], p1 = bptr[a + 1];
+                        float carry = 0.0f;
+                        int res = -1, last = p0;
+                        for (int pb = p0; pb < p1; pb += 32) {
+                            const int pp = pb + lane;
+                            const float f = pp < p1 ? cq[perm[pp]] : 0.0f;
+                            const float fin = lane_scan(f, lane);
+                            const unsigned got = __ballot_sync(FULL, pp < p1 && carry + fin >= r);
+                            const unsigned nz = __ballot_sync(FULL, pp < p1 && f > 0.0f);
+                            if (nz) last = pb + 31 - __clz(nz);
+                            if (got) {
+                                res = pb + __ffs(got) - 1;
+                                break;
+                            }
+                            carry += __shfl_sync(FULL, fin, 31);
+                        }
+                        // past the bin's sum by rounding: its last state of positive weight
+                        x = res >= 0 ? perm[res] : (p1 > p0 ? perm[last] : state);
+                    }
+                    if (lane == 0) path[cs] = x;
+                }
+                __syncwarp();
+                const int r = leave ? nstay + 1 : nstay;
+                for (int q = 0; q < r; q++) issue();
+                c0 -= r;
+                if (x != state) {
+                    state = x;
+                    set_state(state);
+                }
+            }
+        }
+        if (bi > 0 && !failed) {
+            // switch into this tree (sample_hmm_posterior_step)
+            col = B.start - 1;
+            const int k = state;
+            const int n1 = imax(B.S1, 1);
+            const int2 src = d.srcs[B.blk];
+            const int *determ = (const int *)(base + TL.determ) + o_determ[b];
+            const float *dp = (const float *)(base + TL.dp) + o_dp[b];
+            const float rr = tab.rrow[B.state0 + k], cr = tab.crow[B.state0 + k];
+            failed |= !wait_col(col);
+            __syncwarp();
+            const TreeRef P = nx1;
+            const float *c = column(P, col);
+            auto w = [&](int j) -> float {
+                float gg;
+                if (j == src.y) gg = cr;
+                else if (j == src.x) gg = rr;
+                else gg = (determ[j] == k) ? dp[j] : 0.0f;
+                return c[j] * gg;
+            };
+            const int x = warp_sample<float>(n1, uniform(col), w);
+            if (lane == 0) path[col] = x;
+            state = x;
+            __syncwarp();
+            issue();
+        }
+        cur = nx1;
+        nx1 = nx2;
+    }
+    if (failed) {
+        if (lane == 0) report_error(d.err, ERR_WAIT_LIMIT, qi, -1, -1);
+    }
+    // every copy issued has completed before the CTA's shared memory is released
+    if (lane == 0) {
+        for (int q = 0; q < DEPTH; q++) {
+            // issued columns n in [0, L - 1 - pcol): the last use of each slot
+            const int issued = L - 1 - pcol;
+            if (q < issued) {
+                const int nlast = q + ((issued - 1 - q) / DEPTH) * DEPTH;
+                mbar_wait(&cbar[q], (unsigned)((nlast / DEPTH) & 1));
+            }
+        }
+        for (int b = 0; b < 2; b++)
+            if (tpend[b]) mbar_wait(&tbar[b], tphase[b]);
+    }
+    __syncwarp();
+}
+
+template <int DEPTH>
+bool launch_split(const BatchDev &d, cudaStream_t s, size_t budget) {
+    const int maxS = imax(d.maxS, 1);
+    const int slot_elems = (int)(((size_t)maxS * sizeof(float) + 32 + 15) / 16 * 16 / sizeof(float));
+    const size_t smem = (size_t)DEPTH * slot_elems * sizeof(float) + (size_t)DEPTH * MAXT * sizeof(float) +
+                        2 * DEPTH * sizeof(double) + 2 * (size_t)TreeBufLayout(maxS).total;
+    if (smem > budget) return false;
+    static size_t configured = 0;
+    if (smem > configured) {
+        if (cudaFuncSetAttribute(k_traceback_split<DEPTH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem) != cudaSuccess)
+            return true;  // the launch reports the error
+        configured = smem;
+    }
+    k_traceback_split<DEPTH><<<d.ninst, 32, smem, s>>>(d, maxS, slot_elems);
+    note_launch();
+    return true;
+}
+
 template <typename F, int G, int DEPTH>
 bool launch_cfg(const BatchDev &d, cudaStream_t s, size_t budget) {
     const int maxS = imax(d.maxS, 1);
@@ -383,6 +822,15 @@ template <typename F>
 void launch(const BatchDev &d, cudaStream_t s) {
     // the deepest speculation whose ring leaves room for two CTAs per SM, else one
     constexpr size_t two = 100 * 1024, one = 200 * 1024;
+    if constexpr (sizeof(F) == 4) {
+        if (d.bins32) {
+            if (launch_split<32>(d, s, two)) return;
+            if (launch_split<24>(d, s, two)) return;
+            if (launch_split<16>(d, s, two)) return;
+            if (launch_split<32>(d, s, one)) return;
+            if (launch_split<16>(d, s, one)) return;
+        }
+    }
     if (launch_cfg<F, 8, 24>(d, s, two)) return;
     if (launch_cfg<F, 4, 12>(d, s, two)) return;
     if (launch_cfg<F, 4, 12>(d, s, one)) return;

@@ -1306,6 +1306,107 @@ int oracle_traceback(const oracle_problem *p, const double *fw, const double *u,
     return 0;
 }
 
+// The FP32 path's decomposed draw, restated in FP64 (no counterpart in the reference; it
+// draws from the same distribution as sample_hmm_posterior, sample_thread.cpp:470-503, with
+// the uniform mapped to states in another order). Inside a tree the weights
+// fw[i][j] P(j -> k) split into the same-branch part over the states of k's node
+// (tmatrix2 of arghmm_forward_block, sample_thread.cpp:215-226) and a background part
+// that depends on j only through its time (tmatrix, :211-213). With t = u (V + W): t <= V
+// picks the first same-branch state (times ascending) whose running sum reaches t; else
+// the first time bin whose running background sum reaches t - V, then the first state of
+// that bin (state order) whose running fw sum reaches the remainder over tmatrix[a][b_k].
+// Tree switches and the last column draw as the reference does. With `given` non-NULL each
+// column draws conditioned on given[i + 1] instead of the path drawn so far (a per-column
+// check of another sampler's draws).
+int oracle_traceback_split(const oracle_problem *p, const double *fw, const double *u,
+                           const int *given, int *path) {
+    Hmm h;
+    if (!setup(p, h)) return -1;
+    vector<int> nst;
+    vector<long long> off = column_offsets(h, nst);
+    const int L = p->seqlen;
+    const int B = (int)h.arg.trees.size();
+    const int T = h.m.T;
+    path[L - 1] = sample(fw + off[L - 1], std::max(nst[L - 1], 1), u[L - 1]);
+    vector<double> A, V, W, bins(T);
+    for (int b = B - 1; b >= 0; b--) {
+        Block blk;
+        if (!make_block(h, b, blk, true)) return -2;
+        const Tree &t = h.arg.trees[b];
+        const int nstates = blk.states.size();
+        const int ma = blk.tm.minage;
+        for (int i = blk.len - 2; i >= 0; i--) {
+            const int col = blk.start + i;
+            if (nstates == 0) { path[col] = 0; continue; }
+            const double *f = fw + off[col];
+            const int k = given ? given[col + 1] : path[col + 1];
+            const int bk = blk.states.time[k], nk = blk.states.node[k];
+            const int ck = t.age[nk];
+            int j1 = k;
+            while (j1 > 0 && blk.states.node[j1 - 1] == nk) j1--;
+            int j2 = k;
+            while (j2 + 1 < nstates && blk.states.node[j2 + 1] == nk) j2++;
+            V.assign(j2 - j1 + 1, 0.0);
+            double vt = 0.0;
+            for (int j = j1; j <= j2; j++) {
+                const int a = blk.states.time[j];
+                V[j - j1] = f[j] * (blk.tm.get_time(a, bk, ck, ma, true) -
+                                    blk.tm.get_time(a, bk, 0, ma, false));
+                vt += V[j - j1];
+            }
+            std::fill(bins.begin(), bins.end(), 0.0);
+            for (int j = 0; j < nstates; j++) bins[blk.states.time[j]] += f[j];
+            W.assign(T - 1, 0.0);
+            double wt = 0.0;
+            for (int a = 0; a < T - 1; a++) {
+                W[a] = bins[a] * blk.tm.get_time(a, bk, 0, ma, false);
+                wt += W[a];
+            }
+            const double pick = u[col] * (vt + wt);
+            int x = -1;
+            if (pick <= vt) {
+                double run = 0.0;
+                for (int y = 0; y <= j2 - j1 && x < 0; y++) {
+                    run += V[y];
+                    if (run >= pick) x = j1 + y;
+                }
+                if (x < 0) x = j2;
+            } else {
+                const double p2 = pick - vt;
+                double run = 0.0;
+                int a = -1;
+                for (int q = 0; q < T - 1 && a < 0; q++) {
+                    if (run + W[q] >= p2) a = q;
+                    else run += W[q];
+                }
+                if (a < 0)
+                    for (int q = T - 2; q >= 0 && a < 0; q--)
+                        if (W[q] > 0.0) a = q;
+                const double r = (p2 - run) / blk.tm.get_time(a, bk, 0, ma, false);
+                double fr = 0.0;
+                int last = -1;
+                for (int j = 0; j < nstates && x < 0; j++) {
+                    if (blk.states.time[j] != a) continue;
+                    fr += f[j];
+                    if (f[j] > 0.0) last = j;
+                    if (fr >= r) x = j;
+                }
+                if (x < 0) x = last;
+            }
+            path[col] = x;
+        }
+        if (blk.start > 0) {  // sample_hmm_posterior_step (sample_thread.cpp:506-519)
+            const int col = blk.start - 1;
+            const int n1 = std::max(blk.sw.nstates1, 1);
+            A.assign(n1, 0.0);
+            const int k = given ? given[col + 1] : path[col + 1];
+            for (int j = 0; j < n1; j++) A[j] = fw[off[col] + j] * blk.sw.get(j, k);
+            path[col] = sample(A.data(), n1, u[col]);
+        }
+    }
+    return 0;
+}
+
 int oracle_backward(const oracle_problem *p, double *bw) {
     Hmm h;
     if (!setup(p, h)) return -1;

@@ -43,6 +43,8 @@ def load():
         for name, args in [("oracle_nstates", [P, C.c_void_p]),
                            ("oracle_forward", [P, C.c_void_p, C.c_void_p]),
                            ("oracle_traceback", [P, C.c_void_p, C.c_void_p, C.c_void_p]),
+                           ("oracle_traceback_split", [P, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                       C.c_void_p]),
                            ("oracle_backward", [P, C.c_void_p]),
                            ("oracle_posterior", [P, C.c_void_p, C.c_void_p, C.c_void_p]),
                            ("oracle_block_terms", [P, C.c_void_p, C.c_void_p]),
@@ -114,6 +116,20 @@ def traceback(prob, fw: np.ndarray, u: np.ndarray) -> np.ndarray:
     path = np.zeros(prob.seqlen, dtype=np.int32)
     _check(load().oracle_traceback(b.ref, fw.ctypes.data, u.ctypes.data, path.ctypes.data),
            "traceback")
+    return path
+
+
+def traceback_split(prob, fw: np.ndarray, u: np.ndarray, given=None) -> np.ndarray:
+    """The FP32 path's decomposed draw (same distribution, another uniform-to-state map).
+    With ``given``, column i draws conditioned on given[i + 1]."""
+    b = Bound(prob)
+    fw = np.ascontiguousarray(fw, dtype=np.float64)
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    g = None if given is None else np.ascontiguousarray(given, dtype=np.int32)
+    path = np.zeros(prob.seqlen, dtype=np.int32)
+    _check(load().oracle_traceback_split(b.ref, fw.ctypes.data, u.ctypes.data,
+                                         None if g is None else g.ctypes.data,
+                                         path.ctypes.data), "split traceback")
     return path
 
 

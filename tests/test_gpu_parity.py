@@ -103,6 +103,47 @@ def test_fp32_close_to_fp64_long(k, seed):
     assert abs(r32.loglik - r64.loglik) <= 1e-5 * abs(r64.loglik)
 
 
+def _split_mismatches(prob, u):
+    r = api.run_batch([prob], precision="fp32", want_path=True, uniforms=[u])[0]
+    ref = pyoracle.traceback_split(prob, r.forward.astype(np.float64), u, given=r.path)
+    return int(np.count_nonzero(ref != r.path))
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_fp32_path_matches_decomposed_oracle(name):
+    """FP32 traceback: every column's draw equals the oracle's decomposed draw given the
+    GPU's own next state and FP32 forward table; the oracle computes in FP64, so a draw may
+    differ only where the uniform falls within rounding of a boundary."""
+    prob, gold = load(name)
+    assert _split_mismatches(prob, gold["uniforms"]) <= 1
+
+
+@pytest.mark.parametrize("k,L,seed", [(40, 5000, 21), (63, 3000, 22)])
+def test_fp32_path_matches_decomposed_oracle_larger(k, L, seed):
+    prob = simulate(k, L, seed=seed, missing=0.005)
+    u = np.random.default_rng(seed).random(prob.seqlen)
+    assert _split_mismatches(prob, u) <= 2
+
+
+def test_fp32_paths_sample_the_posterior():
+    """Empirical state marginals of 2000 FP32 paths (one batch, independent uniforms)
+    against the FP64 posterior marginals: within 5 sigma + 2e-3 at every cell."""
+    prob = simulate(6, 120, seed=8, missing=0.005)
+    n = 2000
+    rng = np.random.default_rng(3)
+    us = [rng.random(prob.seqlen) for _ in range(n)]
+    rs = api.run_batch([prob] * n, precision="fp32", want_forward=False, want_path=True,
+                       uniforms=us)
+    post = api.posterior(prob)
+    off = pyoracle.offsets(pyoracle.nstates(prob))
+    counts = np.zeros_like(post)
+    for r in rs:
+        counts[off[:-1] + r.path] += 1
+    emp = counts / n
+    sig = np.sqrt(post * (1.0 - post) / n)
+    assert np.all(np.abs(emp - post) <= 5.0 * sig + 2e-3)
+
+
 @pytest.mark.parametrize("name", EXTERNAL_DEFAULT_MAP)
 def test_c_abi_forward_alg(name):
     prob, gold = load(name)

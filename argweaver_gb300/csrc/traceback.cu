@@ -375,6 +375,9 @@ __global__ void k_traceback(BatchDev d, int maxS, int slot_elems) {
 // fw sum reaches the remainder over tm[a][b_k]. This draws from exactly the distribution
 // of the reference's scan over all states (sample(), common.h:272-290), mapping the
 // uniform to states in another order, with O(T + m) work per column instead of O(S).
+// At a tree switch only the sources with a nonzero switch probability into the drawn
+// state carry weight (its gather list plus the recombination and recoalescence sources),
+// so the switch draw runs over those, in state order.
 //
 // Speculation: the warp tests 8 columns at once for the common case, the draw staying at
 // the current state k: lanes 4g .. 4g+3 take column g, each a quarter of the node's states
@@ -383,11 +386,12 @@ __global__ void k_traceback(BatchDev d, int maxS, int slot_elems) {
 // columns after it are tested again under the new state.
 //
 // Data movement is TMA bulk copies (cp.async.bulk) completing on mbarriers, issued by one
-// lane: each forward column (with its bins and uniform) streams into a ring DEPTH columns
-// ahead of the sampler, and each tree's tables (tmatrix, stay complements, time-bin CSR,
-// state info, row offsets, switch targets and probabilities) into one of two buffers one
-// tree ahead, so the warp's time goes into sampling rather than load latency. Every wait
-// is bounded; one that runs out records ERR_WAIT_LIMIT and the kernel returns.
+// lane: the forward table streams into a ring of NCH chunks of up to 8 consecutive columns
+// of one tree (one copy for the chunk's columns, one for their bins, one for their
+// uniforms), and each tree's tables (tmatrix, stay complements, time-bin CSR, state info,
+// row offsets, switch gather lists and probabilities) into one of two buffers one tree
+// ahead. Every wait is bounded; one that runs out records ERR_WAIT_LIMIT and the kernel
+// returns after its copies have landed.
 
 __device__ __forceinline__ unsigned smem_u32(const void *p) {
     return (unsigned)__cvta_generic_to_shared(p);
@@ -424,60 +428,67 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
     return false;
 }
 
-// An array of 4-byte elements copied from its 16-byte-aligned start: bytes to copy and the
-// element offset of the array inside the copy.
+// count elements of ESZ bytes at p, copied from the 16-byte boundary below p: the bytes to
+// copy (a multiple of 16) and the element offset of p inside the copy.
+template <int ESZ>
 struct Rounded {
     const char *a16;
     unsigned bytes;
     int off;
+    __device__ __forceinline__ Rounded(const void *p, long long count) {
+        a16 = (const char *)((uintptr_t)p & ~(uintptr_t)15);
+        off = (int)(((uintptr_t)p & 15) / ESZ);
+        bytes = count > 0 ? (unsigned)(((const char *)p + ESZ * count - a16 + 15) & ~(long long)15) : 0u;
+    }
 };
-__device__ __forceinline__ Rounded rounded(const void *p, int count) {
-    Rounded r;
-    r.a16 = (const char *)((uintptr_t)p & ~(uintptr_t)15);
-    r.off = (int)(((uintptr_t)p & 15) >> 2);
-    r.bytes = count > 0 ? (unsigned)(((const char *)p + 4 * (size_t)count - r.a16 + 15) & ~(size_t)15) : 0u;
-    return r;
-}
 
 // Fields of a tree the traceback needs, in registers.
 struct TreeRef {
     int blk, start, len, S, S1;
-    long long cell0, state0, prev_state0, t2_0;
+    long long cell0, state0, prev_state0, t2_0, gptr0;
 };
 __device__ __forceinline__ TreeRef tree_ref(const BatchDev &d, int blk) {
     const BlockDev &B = d.blocks[blk];
-    return TreeRef{blk, B.start, B.len, B.S, B.S1, B.cell0, B.state0, B.prev_state0, B.t2_0};
+    return TreeRef{blk, B.start, B.len, B.S, B.S1, B.cell0, B.state0, B.prev_state0, B.t2_0, B.gptr0};
 }
 
 // Layout of one tree buffer (bytes from its start; every part 16-byte aligned).
 struct TreeBufLayout {
-    int tm, rstay, bptr, sinfo, t2off, perm, determ, dp, total;
+    int tm, rstay, bptr, sinfo, t2off, perm, gptr, gidx, dp, total;
     __host__ __device__ explicit TreeBufLayout(int maxS) {
-        const int arr = (4 * maxS + 16 + 15) & ~15;  // a 4-byte array copied from 16-B start
+        const int arr = (4 * maxS + 32 + 15) & ~15;  // a 4-byte array copied from its 16-B start
         tm = 0;
         rstay = tm + 4 * MAXT * MAXT;
         bptr = rstay + 4 * MAXT;
         sinfo = bptr + 160;
         t2off = sinfo + 16 * maxS;
         perm = t2off + arr;
-        determ = perm + arr;
-        dp = determ + arr;
+        gptr = perm + arr;
+        gidx = gptr + arr;
+        dp = gidx + arr;
         total = dp + arr;
     }
 };
 
-template <int DEPTH>
-__global__ void __launch_bounds__(32) k_traceback_split(BatchDev d, int maxS, int slot_elems) {
-    constexpr int G = 8;
+constexpr int CW = 8;  // columns per ring chunk (= the speculation group)
+
+// Bytes of one ring chunk's table part.
+__host__ __device__ inline int chunk_tab_bytes(int maxS) { return (4 * CW * maxS + 32 + 15) & ~15; }
+
+template <int NCH>
+__global__ void __launch_bounds__(32) k_traceback_split(BatchDev d, int maxS) {
+    constexpr int G = CW;
     constexpr unsigned FULL = 0xffffffffu;
     extern __shared__ __align__(16) unsigned char dyn_b[];
-    float *ring = (float *)dyn_b;                                   // [DEPTH][slot_elems]
-    float *bring = ring + (size_t)DEPTH * slot_elems;               // [DEPTH][MAXT] bins
-    double *uring = (double *)(bring + DEPTH * MAXT);               // [DEPTH][2] uniform pairs
-    unsigned char *tbuf = (unsigned char *)(uring + 2 * DEPTH);     // [2] tree buffers
-    __shared__ uint64_t cbar[DEPTH];                                // column ring barriers
-    __shared__ uint64_t tbar[2];                                    // tree buffer barriers
-    __shared__ float t2row[32], tmcol[32];                          // the state's V, W factors
+    const int tab_bytes = chunk_tab_bytes(maxS);
+    unsigned char *rtab = dyn_b;                                     // [NCH] table chunks
+    float *rbins = (float *)(rtab + (size_t)NCH * tab_bytes);        // [NCH][CW][MAXT]
+    double *ru = (double *)(rbins + NCH * CW * MAXT);                // [NCH][CW + 2]
+    unsigned char *tbuf = (unsigned char *)(ru + NCH * (CW + 2));    // [2] tree buffers
+    __shared__ uint64_t cbar[NCH];                                   // chunk barriers
+    __shared__ uint64_t tbar[2];                                     // tree buffer barriers
+    __shared__ int ch_lo[NCH], ch_cnt[NCH], ch_off[NCH], ch_uoff[NCH], ch_S[NCH];
+    __shared__ float t2row[32], tmcol[32];                           // the state's V, W factors
     const TreeBufLayout TL(maxS);
     const TTab<float> tab(d);
     const int qi = cta_instance(d);
@@ -491,74 +502,106 @@ __global__ void __launch_bounds__(32) k_traceback_split(BatchDev d, int maxS, in
     bool failed = false;
 
     if (lane == 0) {
-        for (int q = 0; q < DEPTH; q++) mbar_init(&cbar[q], 1);
+        for (int q = 0; q < NCH; q++) mbar_init(&cbar[q], 1);
         mbar_init(&tbar[0], 1);
         mbar_init(&tbar[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
     __syncwarp();
 
-    // ---- column ring: column c is the n-th issued (n = L - 1 - c), slot n % DEPTH, phase n / DEPTH
+    // ---- chunk ring: chunk m in slot m % NCH, phase (m / NCH) & 1; chunks hold columns in
+    // descending order of their highest column, never across a tree start
     int pcol = L - 1, pblk = I.ntrees - 1;
     TreeRef pc = tree_ref(d, I.block0 + pblk);
     TreeRef pn = pblk > 0 ? tree_ref(d, I.block0 + pblk - 1) : pc;  // the cursor's next tree
+    int issued = 0, waited = 0, mc = 0;  // chunks issued, complete, oldest in use
     auto issue = [&]() {
         if (pcol < 0) return;
+        const int cnt = imin(CW, pcol - pc.start + 1), lo = pcol - cnt + 1;
+        const int slot = issued % NCH;
+        const int Sm = imax(pc.S, 1);
+        __syncwarp();  // the slot's previous chunk is no longer read
         if (lane == 0) {
-            const int n = L - 1 - pcol, slot = n % DEPTH;
-            const int Sm = imax(pc.S, 1);
-            const Rounded r = rounded(tab.fw + pc.cell0 + (size_t)(pcol - pc.start) * Sm, Sm);
-            const double *up = (const double *)((uintptr_t)(u + pcol) & ~(uintptr_t)15);
-            mbar_expect_tx(&cbar[slot], r.bytes + 4 * MAXT + 16);
-            bulk_g2s(ring + (size_t)slot * slot_elems, r.a16, r.bytes, &cbar[slot]);
-            bulk_g2s(bring + slot * MAXT, bins + (size_t)pcol * MAXT, 4 * MAXT, &cbar[slot]);
-            bulk_g2s(uring + 2 * slot, up, 16, &cbar[slot]);
+            const Rounded<4> rt(tab.fw + pc.cell0 + (size_t)(lo - pc.start) * Sm, (long long)cnt * Sm);
+            const Rounded<8> ru8(u + lo, cnt);
+            ch_lo[slot] = lo;
+            ch_cnt[slot] = cnt;
+            ch_off[slot] = rt.off;
+            ch_uoff[slot] = ru8.off;
+            ch_S[slot] = Sm;
+            mbar_expect_tx(&cbar[slot], rt.bytes + 4u * MAXT * cnt + ru8.bytes);
+            bulk_g2s(rtab + (size_t)slot * tab_bytes, rt.a16, rt.bytes, &cbar[slot]);
+            bulk_g2s(rbins + slot * CW * MAXT, bins + (size_t)lo * MAXT, 4u * MAXT * cnt, &cbar[slot]);
+            bulk_g2s(ru + slot * (CW + 2), ru8.a16, ru8.bytes, &cbar[slot]);
         }
-        pcol--;
+        __syncwarp();
+        issued++;
+        pcol = lo - 1;
         if (pblk > 0 && pcol < pc.start) {
             pblk--;
             pc = pn;
             if (pblk > 0) pn = tree_ref(d, I.block0 + pblk - 1);
         }
     };
-    auto wait_col = [&](int c) -> bool {
-        const int n = L - 1 - c;
-        return mbar_wait(&cbar[n % DEPTH], (unsigned)((n / DEPTH) & 1));
+    // chunk index of column c: mc, or mc + 1 when c lies below chunk mc
+    auto chunk_of = [&](int c) { return c >= ch_lo[mc % NCH] ? mc : mc + 1; };
+    auto ensure = [&](int m) -> bool {  // chunks up to m have landed
+        bool ok = true;
+        while (waited <= m && ok) {
+            ok = mbar_wait(&cbar[waited % NCH], (unsigned)((waited / NCH) & 1));
+            waited++;
+        }
+        return ok;
     };
-    auto slot_of = [&](int c) { return (L - 1 - c) % DEPTH; };
-    auto column = [&](const TreeRef &B, int c) -> const float * {
-        const int Sm = imax(B.S, 1);
-        const float *g = tab.fw + B.cell0 + (size_t)(c - B.start) * Sm;
-        return ring + (size_t)slot_of(c) * slot_elems + col_offset(g);
+    auto column = [&](int c) -> const float * {
+        const int s = chunk_of(c) % NCH;
+        return (const float *)(rtab + (size_t)s * tab_bytes) + ch_off[s] + (size_t)(c - ch_lo[s]) * ch_S[s];
+    };
+    auto colbins = [&](int c) -> const float * {
+        const int s = chunk_of(c) % NCH;
+        return rbins + (s * CW + (c - ch_lo[s])) * MAXT;
     };
     auto uniform = [&](int c) -> double {
-        return uring[2 * slot_of(c) + (int)(((uintptr_t)(u + c) >> 3) & 1)];
+        const int s = chunk_of(c) % NCH;
+        return ru[s * (CW + 2) + ch_uoff[s] + (c - ch_lo[s])];
+    };
+    // columns >= c consumed: release the chunks wholly above c (each landed first, so its
+    // barrier phase is complete before the slot is issued again) and issue new ones
+    auto consumed_to = [&](int c) {
+        while (mc < issued && ch_lo[mc % NCH] >= c) {
+            failed |= !ensure(mc);
+            mc++;
+            issue();
+        }
     };
 
     // ---- tree buffers: tree x in buffer x & 1
     unsigned tphase[2] = {0u, 0u};
     bool tpend[2] = {false, false};  // staged, not yet waited for
-    int o_t2off[2], o_perm[2], o_determ[2], o_dp[2], o_bptr[2];
+    __shared__ int o_t2off[2], o_perm[2], o_gptr[2], o_gidx[2], o_dp[2], o_bptr[2];
     auto stage = [&](const TreeRef &X) {
         const int b = X.blk & 1;
         unsigned char *base = tbuf + (size_t)b * TL.total;
         const int S = X.S, S1 = imax(X.S1, 1);
-        const Rounded rb = rounded(d.bt_ptr + (size_t)X.blk * (MAXT + 1), MAXT + 1);
-        const Rounded rt = rounded(d.t2off + X.state0, S);
-        const Rounded rp = rounded(d.bt_perm + X.state0, S);
-        const Rounded rd = rounded(d.determ + X.prev_state0, S1);
-        const Rounded rq = rounded(tab.dprob + X.prev_state0, S1);
         const bool sw = X.start > 0;  // a switch into this tree exists
+        const Rounded<4> rb(d.bt_ptr + (size_t)X.blk * (MAXT + 1), MAXT + 1);
+        const Rounded<4> rt(d.t2off + X.state0, S);
+        const Rounded<4> rp(d.bt_perm + X.state0, S);
+        const Rounded<4> rg(d.gptr + X.gptr0, imax(S, 1) + 1);
+        const Rounded<4> ri(d.gidx + X.prev_state0, S1);
+        const Rounded<4> rq(tab.dprob + X.prev_state0, S1);
         tpend[b] = true;
-        o_bptr[b] = rb.off;
-        o_t2off[b] = rt.off;
-        o_perm[b] = rp.off;
-        o_determ[b] = rd.off;
-        o_dp[b] = rq.off;
+        __syncwarp();
         if (lane == 0) {
+            o_bptr[b] = rb.off;
+            o_t2off[b] = rt.off;
+            o_perm[b] = rp.off;
+            o_gptr[b] = rg.off;
+            o_gidx[b] = ri.off;
+            o_dp[b] = rq.off;
             const unsigned tmb = 4u * MAXT * (unsigned)NB;
             const unsigned tx = (S > 0 ? tmb + 4 * MAXT + rb.bytes + 16u * S + rt.bytes + rp.bytes : 0u) +
-                                (sw ? rd.bytes + rq.bytes : 0u);
+                                (sw ? rg.bytes + ri.bytes + rq.bytes : 0u);
             mbar_expect_tx(&tbar[b], tx);
             if (S > 0) {
                 bulk_g2s(base + TL.tm, tab.tm + (size_t)X.blk * MAXT * MAXT, tmb, &tbar[b]);
@@ -569,10 +612,12 @@ __global__ void __launch_bounds__(32) k_traceback_split(BatchDev d, int maxS, in
                 bulk_g2s(base + TL.perm, rp.a16, rp.bytes, &tbar[b]);
             }
             if (sw) {
-                bulk_g2s(base + TL.determ, rd.a16, rd.bytes, &tbar[b]);
+                bulk_g2s(base + TL.gptr, rg.a16, rg.bytes, &tbar[b]);
+                bulk_g2s(base + TL.gidx, ri.a16, ri.bytes, &tbar[b]);
                 bulk_g2s(base + TL.dp, rq.a16, rq.bytes, &tbar[b]);
             }
         }
+        __syncwarp();
     };
     auto wait_tree = [&](int blk) -> bool {
         const int b = blk & 1;
@@ -582,22 +627,22 @@ __global__ void __launch_bounds__(32) k_traceback_split(BatchDev d, int maxS, in
         return ok;
     };
 
-    for (int q = 0; q < DEPTH; q++) issue();
+    for (int q = 0; q < NCH; q++) issue();
     TreeRef cur = tree_ref(d, I.block0 + I.ntrees - 1);
     TreeRef nx1 = I.ntrees > 1 ? tree_ref(d, I.block0 + I.ntrees - 2) : cur;
     stage(cur);
 
-    int col = L - 1;
     int state;
     {
-        failed |= !wait_col(col);
+        const int col = L - 1;
+        failed |= !ensure(chunk_of(col));
         __syncwarp();
-        const float *c = column(cur, col);
+        const float *c = column(col);
         const int x = warp_sample<float>(imax(cur.S, 1), uniform(col), [&](int j) { return c[j]; });
         if (lane == 0) path[col] = x;
         state = x;
         __syncwarp();
-        issue();
+        consumed_to(col);
     }
     const int g = lane >> 2, sub = lane & 3;  // fast path: column g of a group, quarter sub
     for (int bi = I.ntrees - 1; bi >= 0 && !failed; bi--) {
@@ -621,14 +666,10 @@ __global__ void __launch_bounds__(32) k_traceback_split(BatchDev d, int maxS, in
         const int S = B.S;
         int c0 = B.start + B.len - 2;
         if (S == 0) {
-            // fully specified tree: its single state carries over (each column is still
-            // waited for, so its ring slot is free before the slot is issued again)
-            for (; c0 >= B.start && !failed; c0--) {
-                failed |= !wait_col(c0);
-                __syncwarp();
+            // fully specified tree: its single state carries over
+            for (; c0 >= B.start; c0--)
                 if (lane == 0) path[c0] = 0;
-                issue();
-            }
+            if (B.len > 1) consumed_to(B.start);
         } else {
             int kj1 = 0, km = 0, ys = 0;
             float t2r[8], tmr[8];
@@ -653,11 +694,12 @@ __global__ void __launch_bounds__(32) k_traceback_split(BatchDev d, int maxS, in
             while (c0 >= B.start && !failed) {
                 const int ng = imin(G, c0 - B.start + 1);
                 const int cg = c0 - imin(g, ng - 1);
-                failed |= !__all_sync(FULL, wait_col(cg));
+                failed |= !ensure(chunk_of(c0 - ng + 1));
+                __syncwarp();
                 if (failed) break;
                 // fast path: does column g's draw stay at the current state?
-                const float *cp = column(B, cg);
-                const float *bp = bring + slot_of(cg) * MAXT;
+                const float *cp = column(cg);
+                const float *bp = colbins(cg);
                 float sb = 0.0f, ss = 0.0f, sa = 0.0f, sw = 0.0f;
 #pragma unroll
                 for (int q = 0; q < 8; q++) {
@@ -684,8 +726,8 @@ __global__ void __launch_bounds__(32) k_traceback_split(BatchDev d, int maxS, in
                 if (leave) {
                     // exact draw of the first column that leaves, by the whole warp
                     const int cs = c0 - nstay;
-                    const float *cq = column(B, cs);
-                    const float *bq = bring + slot_of(cs) * MAXT;
+                    const float *cq = column(cs);
+                    const float *bq = colbins(cs);
                     const float v = lane < km ? cq[kj1 + lane] * t2row[lane] : 0.0f;
                     const float w = lane < NB ? bq[lane] * tmcol[lane] : 0.0f;
                     const float vin = lane_scan(v, lane), win = lane_scan(w, lane);
@@ -724,8 +766,8 @@ __global__ void __launch_bounds__(32) k_traceback_split(BatchDev d, int maxS, in
                 }
                 __syncwarp();
                 const int r = leave ? nstay + 1 : nstay;
-                for (int q = 0; q < r; q++) issue();
                 c0 -= r;
+                consumed_to(c0 + 1);
                 if (x != state) {
                     state = x;
                     set_state(state);
@@ -733,68 +775,98 @@ __global__ void __launch_bounds__(32) k_traceback_split(BatchDev d, int maxS, in
             }
         }
         if (bi > 0 && !failed) {
-            // switch into this tree (sample_hmm_posterior_step)
-            col = B.start - 1;
+            // switch into this tree (sample_hmm_posterior_step): sources in state order,
+            // the gather list of the drawn state merged with the recombination and
+            // recoalescence sources
+            const int col = B.start - 1;
             const int k = state;
-            const int n1 = imax(B.S1, 1);
             const int2 src = d.srcs[B.blk];
-            const int *determ = (const int *)(base + TL.determ) + o_determ[b];
+            const int *gp = (const int *)(base + TL.gptr) + o_gptr[b];
+            const int *gi = (const int *)(base + TL.gidx) + o_gidx[b];
             const float *dp = (const float *)(base + TL.dp) + o_dp[b];
             const float rr = tab.rrow[B.state0 + k], cr = tab.crow[B.state0 + k];
-            failed |= !wait_col(col);
+            failed |= !ensure(chunk_of(col));
             __syncwarp();
-            const TreeRef P = nx1;
-            const float *c = column(P, col);
-            auto w = [&](int j) -> float {
-                float gg;
-                if (j == src.y) gg = cr;
-                else if (j == src.x) gg = rr;
-                else gg = (determ[j] == k) ? dp[j] : 0.0f;
-                return c[j] * gg;
-            };
-            const int x = warp_sample<float>(n1, uniform(col), w);
-            if (lane == 0) path[col] = x;
-            state = x;
-            __syncwarp();
-            issue();
+            if (!failed) {
+                const float *c = column(col);
+                const int p0 = gp[k], ng2 = gp[k + 1] - p0;
+                int x = 0;
+                if (lane == 0) {
+                    // the two extra sources in state order (get(): recoalescence wins a tie)
+                    int e0 = -1, e1 = -1;
+                    float w0 = 0.0f, w1 = 0.0f;
+                    if (src.x >= 0 && src.x != src.y) { e0 = src.x; w0 = rr; }
+                    if (src.y >= 0) {
+                        if (e0 < 0) { e0 = src.y; w0 = cr; }
+                        else if (src.y < e0) { e1 = e0; w1 = w0; e0 = src.y; w0 = cr; }
+                        else { e1 = src.y; w1 = cr; }
+                    }
+                    // merged walk of the gather list and the extras: pass 0 sums, pass 1 draws
+                    float tot = 0.0f, run = 0.0f, pick = 0.0f;
+                    int last = -1;
+                    x = -1;
+                    for (int pass = 0; pass < 2 && x < 0; pass++) {
+                        int p = 0, q = 0;
+                        while ((p < ng2 || q < 2) && x < 0) {
+                            const int eq = q == 0 ? e0 : (q == 1 ? e1 : -1);
+                            if (eq < 0 && q < 2) { q++; continue; }
+                            int j;
+                            float wv;
+                            if (q < 2 && (p >= ng2 || eq < gi[p0 + p])) {
+                                j = eq;
+                                wv = c[j] * (q == 0 ? w0 : w1);
+                                q++;
+                            } else {
+                                j = gi[p0 + p];
+                                wv = c[j] * dp[j];
+                                p++;
+                            }
+                            if (pass == 0) {
+                                tot += wv;
+                            } else {
+                                run += wv;
+                                if (wv > 0.0f) last = j;
+                                if (run >= pick) x = j;
+                            }
+                        }
+                        if (pass == 0) pick = (float)uniform(col) * tot;
+                    }
+                    if (x < 0) x = last >= 0 ? last : 0;
+                }
+                x = __shfl_sync(FULL, x, 0);
+                if (lane == 0) path[col] = x;
+                state = x;
+                __syncwarp();
+                consumed_to(col);
+            }
         }
         cur = nx1;
         nx1 = nx2;
     }
-    if (failed) {
-        if (lane == 0) report_error(d.err, ERR_WAIT_LIMIT, qi, -1, -1);
-    }
-    // every copy issued has completed before the CTA's shared memory is released
+    if (failed && lane == 0) report_error(d.err, ERR_WAIT_LIMIT, qi, -1, -1);
+    // every copy issued has landed before the CTA's shared memory is released
     if (lane == 0) {
-        for (int q = 0; q < DEPTH; q++) {
-            // issued columns n in [0, L - 1 - pcol): the last use of each slot
-            const int issued = L - 1 - pcol;
-            if (q < issued) {
-                const int nlast = q + ((issued - 1 - q) / DEPTH) * DEPTH;
-                mbar_wait(&cbar[q], (unsigned)((nlast / DEPTH) & 1));
-            }
-        }
-        for (int b = 0; b < 2; b++)
-            if (tpend[b]) mbar_wait(&tbar[b], tphase[b]);
+        for (int m = waited; m < issued; m++) mbar_wait(&cbar[m % NCH], (unsigned)((m / NCH) & 1));
+        for (int q = 0; q < 2; q++)
+            if (tpend[q]) mbar_wait(&tbar[q], tphase[q]);
     }
     __syncwarp();
 }
 
-template <int DEPTH>
+template <int NCH>
 bool launch_split(const BatchDev &d, cudaStream_t s, size_t budget) {
     const int maxS = imax(d.maxS, 1);
-    const int slot_elems = (int)(((size_t)maxS * sizeof(float) + 32 + 15) / 16 * 16 / sizeof(float));
-    const size_t smem = (size_t)DEPTH * slot_elems * sizeof(float) + (size_t)DEPTH * MAXT * sizeof(float) +
-                        2 * DEPTH * sizeof(double) + 2 * (size_t)TreeBufLayout(maxS).total;
+    const size_t smem = (size_t)NCH * chunk_tab_bytes(maxS) + (size_t)NCH * CW * MAXT * sizeof(float) +
+                        (size_t)NCH * (CW + 2) * sizeof(double) + 2 * (size_t)TreeBufLayout(maxS).total;
     if (smem > budget) return false;
     static size_t configured = 0;
     if (smem > configured) {
-        if (cudaFuncSetAttribute(k_traceback_split<DEPTH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        if (cudaFuncSetAttribute(k_traceback_split<NCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)smem) != cudaSuccess)
             return true;  // the launch reports the error
         configured = smem;
     }
-    k_traceback_split<DEPTH><<<d.ninst, 32, smem, s>>>(d, maxS, slot_elems);
+    k_traceback_split<NCH><<<d.ninst, 32, smem, s>>>(d, maxS);
     note_launch();
     return true;
 }
@@ -824,11 +896,10 @@ void launch(const BatchDev &d, cudaStream_t s) {
     constexpr size_t two = 100 * 1024, one = 200 * 1024;
     if constexpr (sizeof(F) == 4) {
         if (d.bins32) {
-            if (launch_split<32>(d, s, two)) return;
-            if (launch_split<24>(d, s, two)) return;
-            if (launch_split<16>(d, s, two)) return;
-            if (launch_split<32>(d, s, one)) return;
-            if (launch_split<16>(d, s, one)) return;
+            if (launch_split<4>(d, s, 112 * 1024)) return;
+            if (launch_split<3>(d, s, 112 * 1024)) return;
+            if (launch_split<4>(d, s, 224 * 1024)) return;
+            if (launch_split<3>(d, s, 224 * 1024)) return;
         }
     }
     if (launch_cfg<F, 8, 24>(d, s, two)) return;

@@ -111,8 +111,11 @@ struct BatchDev {
     //            emission (formed in FP64: a column that varies only through missing calls
     //            has emissions equal to a few digits, which FP32 values would lose)
     //   lnvref   [variant columns] log(e_ref) of each variant column
+    //   blkext   [nblocks] a tree's sum of those references over its columns (lneref per
+    //            invariant column, lnvref per variant column; not the instance's column 0),
+    //            added to the log-likelihood once per tree
     float *tm32, *t2d32, *inv32, *var32, *determprob32, *recombrow32, *recoalrow32, *rstay32;
-    double *lneref, *lnvref;
+    double *lneref, *lnvref, *blkext;
     // [total columns * MAXT] or NULL: per stored FP32 forward column, its time-bin sums
     // (the fgroups of arghmm_forward_block, sample_thread.cpp:258-263), written by the
     // forward kernel for the traceback's decomposed draw

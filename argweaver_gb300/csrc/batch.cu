@@ -47,6 +47,10 @@ struct Engine {
     cudaEvent_t gev[2 * MAXG + 2];
     Timings last;
     int timing = 0;  // 0 off; 1 on (overlapped schedule: one compute time); 2 serial phases
+    int group_div = [] {  // the largest instance group holds n / group_div instances
+        const char *e = getenv("AWG_GROUP_DIV");
+        return e && atoi(e) > 0 ? atoi(e) : 8;
+    }();
 };
 
 Engine &engine() {
@@ -181,7 +185,8 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
     const size_t o_gidx = w.add(sizeof(int) * ST);
     const size_t o_var = w.add(sizeof(double) * std::max(plan.total_var, 1LL));
     size_t o_tm32 = 0, o_t2d32 = 0, o_inv32 = 0, o_var32 = 0, o_detp32 = 0, o_rrow32 = 0,
-           o_crow32 = 0, o_rstay32 = 0, o_lneref = 0, o_lnvref = 0;
+           o_crow32 = 0, o_rstay32 = 0, o_lneref = 0, o_lnvref = 0,
+           o_blkext = 0;
     if (fp32) {
         o_tm32 = w.add(sizeof(float) * (size_t)plan.nblocks * MAXT * MAXT);
         o_t2d32 = w.add(sizeof(float) * std::max(plan.total_M, 1LL));
@@ -193,6 +198,7 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
         o_rstay32 = w.add(sizeof(float) * (size_t)plan.nblocks * MAXT);
         o_lneref = w.add(sizeof(double) * plan.nblocks);
         o_lnvref = w.add(sizeof(double) * std::max(plan.total_vcols, 1LL));
+        o_blkext = w.add(sizeof(double) * plan.nblocks);
     }
     const size_t o_fw = w.add((fp32 ? sizeof(float) : sizeof(double)) * CELLS);
     const size_t o_lnl = w.add(sizeof(double) * plan.ninst);
@@ -288,6 +294,7 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
         d.rstay32 = (float *)(D + o_rstay32);
         d.lneref = (double *)(D + o_lneref);
         d.lnvref = (double *)(D + o_lnvref);
+        d.blkext = (double *)(D + o_blkext);
         d.fw32 = (float *)(D + o_fw);
     } else {
         d.fw64 = (double *)(D + o_fw);
@@ -311,15 +318,16 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
     CK(cudaMemsetAsync(d.err, 0, 4 * sizeof(int), s));
     if (T) CK(cudaEventRecord(E.ev[1], s));
     if (pipelined) {
-        // group sizes n/32, doubling; the last takes the rest
+        // group sizes n/32, doubling up to n/div; the last takes the rest
         int bounds[MAXG + 1];
         int ng = 0, q0 = 0, sz = std::max(1, n / 32);
+        const int cap = std::max(1, n / std::max(1, E.group_div));
         bounds[0] = 0;
         while (q0 < n) {
             const int q1 = (ng == MAXG - 1) ? n : std::min(n, q0 + sz);
             bounds[++ng] = q1;
             q0 = q1;
-            sz *= 2;
+            sz = std::min(2 * sz, std::max(cap, sz));
         }
         const int *ord = (const int *)(h + o_order);
         int boff = 0;

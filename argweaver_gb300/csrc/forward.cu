@@ -192,7 +192,8 @@ __global__ void __launch_bounds__(512) k_forward(BatchDev d, int maxS, int maxM,
         const int *cvar = d.colvar + I.col0 + B.start;
         const F *inv = invS;
         const F *var = tab.var + B.var0;
-        const double lner = Tab<F>::split ? tab.lneref[blk] : 0.0;
+        // FP32: the tree's emission references, added once the tree is done
+        const double blkx = Tab<F>::split && tid == 0 ? d.blkext[blk] : 0.0;
         // column classes and variant rows, 32 columns per load, read back by shuffles
         int ccache = 0, vcache = 0, cbase = -32;
         auto colinfo = [&](int i, uint8_t &ci, int &vi) {
@@ -244,8 +245,6 @@ __global__ void __launch_bounds__(512) k_forward(BatchDev d, int maxS, int maxM,
                 col[(c ^ 1) * maxS + k] = v;
                 colT[rank[k]] = v;
             }
-            if (Tab<F>::split && tid == 0 && c0 == COL_INVARIANT) acc.extra += lner;
-            if (Tab<F>::split && tid == 0 && c0 == COL_VARIANT) acc.extra += tab.lnvref[B.vrow0 + v0];
             c ^= 1;
         }
 
@@ -288,8 +287,6 @@ __global__ void __launch_bounds__(512) k_forward(BatchDev d, int maxS, int maxM,
             int vrow;
             colinfo(i, ci, vrow);
             F *nxt = col + (c ^ 1) * maxS;
-            if (Tab<F>::split && tid == 0 && ci == COL_INVARIANT) acc.extra += lner;
-            if (Tab<F>::split && tid == 0 && ci == COL_VARIANT) acc.extra += tab.lnvref[B.vrow0 + vrow];
             for (int k0 = 0; k0 < S; k0 += NT) {
                 const int k = k0 + tid;
                 const bool valid = k < S;
@@ -338,6 +335,7 @@ __global__ void __launch_bounds__(512) k_forward(BatchDev d, int maxS, int maxM,
             }
             c ^= 1;
         }
+        if (Tab<F>::split && tid == 0) acc.extra += blkx;
         __syncthreads();
     }
     if (tid == 0 && d.lnl) {
@@ -546,14 +544,26 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
         const uint8_t *cls = d.colclass + I.col0 + B.start;
         const int *cvar = d.colvar + I.col0 + B.start;
         const F *var = tab.var + B.var0;
-        const double lner = Tab<F>::split ? tab.lneref[blk] : 0.0;
-        int ccache = 0, vcache = 0, cbase = -32;
-        auto colinfo = [&](int i, uint8_t &ci, int &vi) {
+        // FP32: the tree's emission references, added once the tree is done
+        const double blkx = Tab<F>::split && tid == 0 ? d.blkext[blk] : 0.0;
+        // column classes and variant rows, 32 columns per lane-window; the next window is
+        // loaded when the current one is entered, so its loads overlap 32 columns of work
+        int ccache, vcache, ncc, nvc, cbase = 0;
+        {
+            const int q = lane, q2 = 32 + lane;
+            ccache = q < len ? cls[q] : 0;
+            vcache = q < len ? cvar[q] : 0;
+            ncc = q2 < len ? cls[q2] : 0;
+            nvc = q2 < len ? cvar[q2] : 0;
+        }
+        auto colinfo = [&](int i, uint8_t &ci, int &vi) {  // i never decreases, steps <= 1
             if (i - cbase >= 32) {
-                cbase = i;
-                const int q = i + lane;
-                ccache = q < len ? cls[q] : 0;
-                vcache = q < len ? cvar[q] : 0;
+                cbase += 32;
+                ccache = ncc;
+                vcache = nvc;
+                const int q2 = cbase + 32 + lane;
+                ncc = q2 < len ? cls[q2] : 0;
+                nvc = q2 < len ? cvar[q2] : 0;
             }
             ci = (uint8_t)__shfl_sync(0xffffffffu, ccache, i - cbase);
             vi = __shfl_sync(0xffffffffu, vcache, i - cbase);
@@ -615,8 +625,6 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
                 x_own[q] = v;
                 x_lo[q] = 0.0f;
             }
-            if (Tab<F>::split && tid == 0 && c0 == COL_INVARIANT) acc.extra += lner;
-            if (Tab<F>::split && tid == 0 && c0 == COL_VARIANT) acc.extra += tab.lnvref[B.vrow0 + v0];
             c ^= 1;
         }
         if (len > 1 && !reducer) prefetch(1);
@@ -746,8 +754,6 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
             int vrow;
             colinfo(i, ci, vrow);
             F *nxt = col + (c ^ 1) * maxS;
-            if (Tab<F>::split && tid == 0 && ci == COL_INVARIANT) acc.extra += lner;
-            if (Tab<F>::split && tid == 0 && ci == COL_VARIANT) acc.extra += tab.lnvref[B.vrow0 + vrow];
             if (!reducer) {
 #pragma unroll
                 for (int q = 0; q < KPT; q++) {
@@ -781,6 +787,7 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
             }
             c ^= 1;
         }
+        if (Tab<F>::split && tid == 0) acc.extra += blkx;
         __syncthreads();
     }
     if (tid == 0 && d.lnl) {

@@ -1179,12 +1179,37 @@ __device__ R emit_column(const EmitCtx &c, const uint8_t *chars, int X, R (*in)[
     return ref;
 }
 
+// FP32 path: a tree's share of the log-likelihood's emission references, lneref per
+// invariant column and lnvref per variant column (the instance's column 0, the prior, has
+// none), summed by one warp in a fixed order.
+__device__ void block_log_offset(const BatchDev &d, const BlockDev &B, const InstDev &I, int blk,
+                                 int lane) {
+    const uint8_t *cls = d.colclass + I.col0 + B.start;
+    const int *cvar = d.colvar + I.col0 + B.start;
+    const double lner = d.lneref[blk];
+    double s = 0.0;
+    if (B.S > 0) {
+        for (int i = lane; i < B.len; i += 32) {
+            if (B.b == 0 && i == 0) continue;
+            const uint8_t c = cls[i];
+            if (c == COL_INVARIANT) s += lner;
+            else if (c == COL_VARIANT) s += d.lnvref[B.vrow0 + cvar[i]];
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) d.blkext[blk] = s;
+}
+
 template <bool FP32OUT>
 __global__ void k_varemit(BatchDev d, int nwarps, int maxS, int smem_bytes) {
     extern __shared__ int4 dyn[];
     const int blk = cta_block(d);
     const BlockDev B = d.blocks[blk];
-    if (B.nvar == 0 || B.S == 0) return;
+    if (B.nvar == 0 || B.S == 0) {
+        if (FP32OUT && threadIdx.x < 32) block_log_offset(d, B, d.inst[B.inst], blk, threadIdx.x);
+        return;
+    }
     const InstDev I = d.inst[B.inst];
     const int T = I.T, n = I.nnodes;
     const bool internal = I.internal != 0;
@@ -1438,6 +1463,10 @@ __global__ void k_varemit(BatchDev d, int nwarps, int maxS, int smem_bytes) {
             }
             __syncwarp();
         }
+    }
+    if constexpr (FP32OUT) {
+        __syncthreads();  // every variant column's lnvref written
+        if (warp == 0) block_log_offset(d, B, I, blk, lane);
     }
 }
 

@@ -116,6 +116,79 @@ def run_batch(problems: Sequence[Problem], *, precision: str = "fp64",
     return out
 
 
+def _bind_batch(problems, precision, want_forward, want_path, want_posterior, uniforms):
+    """ctypes views of a batch and its output arrays (kept alive by the returned lists)."""
+    fp32 = precision == "fp32"
+    if precision not in ("fp32", "fp64"):
+        raise ValueError("precision must be 'fp64' or 'fp32'")
+    lib = capi.load()
+    n = len(problems)
+    bound = [_Bound(p) for p in problems]
+    probs = (capi.AwgProblem * n)(*[b.c for b in bound])
+    outs = (capi.AwgOutputs * n)()
+    ncells = np.zeros(n, dtype=np.int64)
+    if lib.awg_problems_cells(probs, n, ncells.ctypes.data) != 0:
+        raise ValueError(capi.last_error())
+    results, keep = [], [bound]
+    for q, b in enumerate(bound):
+        r = Result()
+        o = outs[q]
+        if want_forward:
+            r.forward = np.empty(int(ncells[q]), dtype=np.float32 if fp32 else np.float64)
+            if fp32:
+                o.forward32 = r.forward.ctypes.data
+            else:
+                o.forward = r.forward.ctypes.data
+        if want_posterior:
+            r.posterior = np.empty(int(ncells[q]), dtype=np.float64)
+            o.posterior = r.posterior.ctypes.data
+        if want_path:
+            r.path = np.empty(b.p.seqlen, dtype=np.int32)
+            o.path = r.path.ctypes.data
+            if uniforms is not None and uniforms[q] is not None:
+                u = np.ascontiguousarray(uniforms[q], dtype=np.float64)
+                keep.append(u)
+                o.uniforms = u.ctypes.data
+        ll = np.zeros(1, dtype=np.float64)
+        keep.append(ll)
+        o.loglik = ll.ctypes.data
+        results.append((r, ll))
+    return probs, outs, results, keep
+
+
+def autotune(problems: Sequence[Problem], *, precision: str = "fp32", want_path: bool = True,
+             trials: int = 2) -> dict:
+    """Time the candidate schedules on this batch and keep the fastest for its shape class
+    (awg_autotune); returns the chosen knobs and the best compute time (ms)."""
+    lib = capi.load()
+    probs, outs, _, keep = _bind_batch(problems, precision, False, want_path, False, None)
+    buf = C.create_string_buffer(256)
+    rc = lib.awg_autotune(probs, outs, len(problems),
+                          capi.AWG_FP32 if precision == "fp32" else capi.AWG_FP64, trials, buf, 256)
+    del keep
+    if rc != 0:
+        raise GpuError(f"awg_autotune failed ({rc}): {capi.last_error()}")
+    out = {}
+    for kv in buf.value.decode().split():
+        k, v = kv.split("=")
+        out[k] = float(v) if k == "ms" else int(v)
+    return out
+
+
+def set_graphs(on: bool) -> None:
+    capi.load().awg_set_graphs(int(bool(on)))
+
+
+def set_schedule(kpt: int = 0, group_div: int = 8, chunk: int = 1, persistent: bool = True) -> None:
+    """Default schedule knobs (awg_set_schedule); forgets the autotuner's choices."""
+    capi.load().awg_set_schedule(int(kpt), int(group_div), int(chunk), int(bool(persistent)))
+
+
+def graph_counts() -> dict:
+    lib = capi.load()
+    return {"replays": int(lib.awg_graph_replays()), "captures": int(lib.awg_graph_captures())}
+
+
 def forward(prob: Problem, precision: str = "fp64"):
     r = run_batch([prob], precision=precision)[0]
     return r.forward, r.loglik

@@ -88,6 +88,15 @@ EXTRA = [
     ("awg_set_timing", None, [C.c_int]),
     ("awg_last_timings", None, [c_double_p]),
 ]
+# exports of the batch API beyond the reference's (declared in include/argweaver_gb300.h)
+PROTOTYPES += [
+    ("awg_autotune", C.c_int, [C.POINTER(AwgProblem), C.POINTER(AwgOutputs), C.c_int, C.c_int,
+                               C.c_int, C.c_char_p, C.c_int]),
+    ("awg_set_graphs", None, [C.c_int]),
+    ("awg_set_schedule", None, [C.c_int, C.c_int, C.c_int, C.c_int]),
+    ("awg_graph_replays", C.c_longlong, []),
+    ("awg_graph_captures", C.c_longlong, []),
+]
 
 
 def library_path() -> str:

@@ -12,6 +12,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <vector>
 
@@ -47,11 +48,39 @@ struct Engine {
     cudaEvent_t gev[2 * MAXG + 2];
     Timings last;
     int timing = 0;  // 0 off; 1 on (overlapped schedule: one compute time); 2 serial phases
-    int group_div = [] {  // the largest instance group holds n / group_div instances
-        const char *e = getenv("AWG_GROUP_DIV");
-        return e && atoi(e) > 0 ? atoi(e) : 8;
+    // schedule defaults (environment overrides for experiments) and the tuned ones by class
+    TuneCfg defaults = [] {
+        TuneCfg c;
+        if (const char *e = getenv("AWG_GROUP_DIV")) c.group_div = std::max(1, atoi(e));
+        if (const char *e = getenv("AWG_FORWARD_KPT")) c.kpt = atoi(e);
+        if (const char *e = getenv("AWG_PERSISTENT")) c.persistent = atoi(e) != 0;
+        return c;
     }();
+    std::map<long long, TuneCfg> tuned;
+    // the captured step of the last batch (kernels, memsets, cross-stream events) and the
+    // launch parameters it was captured with; replayed while they match
+    bool graphs = [] {
+        const char *e = getenv("AWG_GRAPHS");
+        return !(e && atoi(e) == 0);
+    }();
+    cudaGraphExec_t gexec = nullptr;
+    std::vector<long long> gsig;
+    long long gkernels = 0;
+    long long graph_replays = 0, graph_captures = 0;
+    long long last_key = -1;  // shape class of the last batch
 };
+
+// Shape class of a batch for the tuned schedules: precision, path or not, ntimes, and the
+// binary orders of magnitude of the largest state count and of the instance count.
+long long shape_key(const HostPlan &plan, bool fp32, bool path) {
+    auto lg = [](long long v) {
+        int k = 0;
+        while ((1LL << (k + 1)) <= v && k < 30) k++;
+        return (long long)k;
+    };
+    return (long long)fp32 | (long long)path << 1 | (long long)plan.maxT << 2 |
+           lg(std::max(plan.maxS, 1)) << 8 | lg(std::max(plan.ninst, 1)) << 14;
+}
 
 Engine &engine() {
     static Engine e;
@@ -110,6 +139,14 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
         if (opt.backward && opt.backward[q]) want_bw = true;
     }
     want_post |= want_bw;
+    TuneCfg cfg = E.defaults;
+    E.last_key = shape_key(plan, fp32, want_path);
+    if (opt.cfg) {
+        cfg = *opt.cfg;
+    } else {
+        auto it = E.tuned.find(shape_key(plan, fp32, want_path));
+        if (it != E.tuned.end()) cfg = it->second;
+    }
 
     if (!E.init) {
         int dc = 0;
@@ -206,9 +243,10 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
     const size_t o_bw = w.add(want_bw ? sizeof(double) * CELLS : 0);
     const size_t o_path = w.add(want_path ? sizeof(int) * COLS : 0);
     // FP32 traceback: the forward columns' time-bin sums
-    const bool want_bins = fp32 && want_path && forward_writes_bins(plan.maxS);
+    const bool want_bins = fp32 && want_path && forward_writes_bins(plan.maxS, cfg.kpt);
     const size_t o_bins = w.add(want_bins ? sizeof(float) * MAXT * COLS : 0);
     const size_t o_err = w.add(4 * sizeof(int));
+    const size_t o_queue = w.add(sizeof(int) * 2 * MAXG);  // work counters of the groups
     const size_t total = w.total;
 
     if (total > E.dev_cap) {
@@ -310,56 +348,155 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
     // (larger batches): instances in groups, largest first; a group's per-tree kernels run
     // on the main stream and its forward (then traceback/backward) on high-priority streams
     // as soon as they are done, so the long per-instance chains start early and the
-    // per-tree work of later groups fills the SMs they leave idle.
-    const bool pipelined = n >= 16 && !opt.tables_only && !opt.priors && E.timing != 2;
+    // per-tree work of later groups fills the SMs they leave idle. The per-tree kernels are
+    // persistent, work-stealing over units of trees; the device part of a step is captured
+    // once as a CUDA graph and replayed while its launch parameters repeat.
+    const bool special = opt.tables_only || opt.priors;
+    const bool serial_timing = E.timing == 2;
+    const bool pipelined = n >= 16 && !special && !serial_timing;
     const bool T = E.timing != 0;
+    int *queues = (int *)(D + o_queue);
     if (T) CK(cudaEventRecord(E.ev[0], s));
     CK(cudaMemcpyAsync(D, h, in_bytes, cudaMemcpyHostToDevice, s));
     CK(cudaMemsetAsync(d.err, 0, 4 * sizeof(int), s));
     if (T) CK(cudaEventRecord(E.ev[1], s));
+
+    // groups of the pipelined schedule: sizes n/32, doubling up to n/group_div, the last
+    // takes the rest
+    int bounds[MAXG + 1];
+    int ng = 1;
+    bounds[0] = 0;
+    bounds[1] = n;
     if (pipelined) {
-        // group sizes n/32, doubling up to n/div; the last takes the rest
-        int bounds[MAXG + 1];
-        int ng = 0, q0 = 0, sz = std::max(1, n / 32);
-        const int cap = std::max(1, n / std::max(1, E.group_div));
-        bounds[0] = 0;
+        int q0 = 0, sz = std::max(1, n / 32);
+        const int cap = std::max(1, n / std::max(1, cfg.group_div));
+        ng = 0;
         while (q0 < n) {
             const int q1 = (ng == MAXG - 1) ? n : std::min(n, q0 + sz);
             bounds[++ng] = q1;
             q0 = q1;
             sz = std::min(2 * sz, std::max(cap, sz));
         }
-        const int *ord = (const int *)(h + o_order);
-        int boff = 0;
-        for (int g = 0; g < ng; g++) {
-            BatchDev dg = d;
-            int nb = 0;
-            for (int j = bounds[g]; j < bounds[g + 1]; j++) nb += plan.inst[ord[j]].ntrees;
-            dg.order = d.order + bounds[g];
-            dg.ninst = bounds[g + 1] - bounds[g];
-            dg.blkmap = (const int *)(D + o_blkmap) + boff;
-            dg.nblocks = nb;
-            boff += nb;
-            launch_tables(dg, fp32, s);
-            CKL("table kernel");
-            launch_varemit(dg, fp32, s);
-            CKL("emission kernel");
-            cudaStream_t gs = E.gstream[g];
-            CK(cudaEventRecord(E.gev[2 * g], s));
-            CK(cudaStreamWaitEvent(gs, E.gev[2 * g], 0));
-            launch_forward(dg, fp32, gs);
-            CKL("forward kernel");
+    }
+    int *qk = cfg.persistent ? queues : nullptr;
+    auto qp = [&](int i) { return qk ? qk + i : nullptr; };
+    // the device part of the step (no host synchronisation: it is also what is captured)
+    auto enqueue = [&]() -> cudaError_t {
+        cudaError_t rc;
+#define EQ(x)                                                                         \
+    do {                                                                              \
+        if ((rc = (x)) != cudaSuccess) return rc;                                     \
+    } while (0)
+        if (qk) EQ(cudaMemsetAsync(queues, 0, sizeof(int) * 2 * MAXG, s));
+        if (pipelined) {
+            const int *ord = (const int *)(h + o_order);
+            int boff = 0;
+            for (int g = 0; g < ng; g++) {
+                BatchDev dg = d;
+                int nb = 0;
+                for (int j = bounds[g]; j < bounds[g + 1]; j++) nb += plan.inst[ord[j]].ntrees;
+                dg.order = d.order + bounds[g];
+                dg.ninst = bounds[g + 1] - bounds[g];
+                dg.blkmap = (const int *)(D + o_blkmap) + boff;
+                dg.nblocks = nb;
+                boff += nb;
+                launch_tables(dg, fp32, s, qp(2 * g), cfg.chunk);
+                EQ(cudaGetLastError());
+                launch_varemit(dg, fp32, s, qp(2 * g + 1), cfg.chunk);
+                EQ(cudaGetLastError());
+                cudaStream_t gs = E.gstream[g];
+                EQ(cudaEventRecord(E.gev[2 * g], s));
+                EQ(cudaStreamWaitEvent(gs, E.gev[2 * g], 0));
+                launch_forward(dg, fp32, gs, cfg.kpt);
+                EQ(cudaGetLastError());
+                if (want_path) {
+                    launch_traceback(dg, fp32, gs);
+                    EQ(cudaGetLastError());
+                }
+                if (want_post) {
+                    launch_backward(dg, fp32, want_bw ? (double *)(D + o_bw) : nullptr, gs);
+                    EQ(cudaGetLastError());
+                }
+                EQ(cudaEventRecord(E.gev[2 * g + 1], gs));
+            }
+            for (int g = 0; g < ng; g++) EQ(cudaStreamWaitEvent(s, E.gev[2 * g + 1], 0));
+        } else {
+            launch_tables(d, fp32, s, qp(0), cfg.chunk);
+            EQ(cudaGetLastError());
+            launch_varemit(d, fp32, s, qp(1), cfg.chunk);
+            EQ(cudaGetLastError());
+            launch_forward(d, fp32, s, cfg.kpt);
+            EQ(cudaGetLastError());
             if (want_path) {
-                launch_traceback(dg, fp32, gs);
-                CKL("traceback kernel");
+                launch_traceback(d, fp32, s);
+                EQ(cudaGetLastError());
             }
             if (want_post) {
-                launch_backward(dg, fp32, want_bw ? (double *)(D + o_bw) : nullptr, gs);
-                CKL("backward kernel");
+                launch_backward(d, fp32, want_bw ? (double *)(D + o_bw) : nullptr, s);
+                EQ(cudaGetLastError());
             }
-            CK(cudaEventRecord(E.gev[2 * g + 1], gs));
         }
-        for (int g = 0; g < ng; g++) CK(cudaStreamWaitEvent(s, E.gev[2 * g + 1], 0));
+#undef EQ
+        return cudaSuccess;
+    };
+    auto cuda_fail = [&](cudaError_t rc, const char *what) {
+        char b[320];
+        snprintf(b, sizeof(b), "%s (maxS %d, maxM %d, nodes %d): %s", what, plan.maxS, plan.maxM,
+                 plan.maxnodes, cudaGetErrorString(rc));
+        err = b;
+        return -3;
+    };
+
+    if (!special && !serial_timing) {
+        if (E.graphs) {
+            // everything a launch depends on: buffers, counts, groups and schedule knobs
+            std::vector<long long> sig = {(long long)(uintptr_t)D, (long long)fp32, want_path,
+                                          want_post, want_bw, want_bins, plan.ninst, plan.nblocks,
+                                          plan.maxS, plan.maxT, plan.maxnodes, plan.maxM,
+                                          cfg.kpt, cfg.chunk, cfg.group_div, cfg.persistent, ng,
+                                          (long long)total};
+            for (size_t o : {o_inst, o_blocks, o_model, o_nodes, o_map, o_seq, o_cls, o_cvar,
+                             o_order, o_blkmap, o_u, o_sinfo, o_t2off, o_btptr, o_btperm, o_tm,
+                             o_gts, o_inv, o_det, o_detp, o_srcs, o_rrow, o_crow, o_gptr, o_gidx,
+                             o_var, o_tm32, o_t2d32, o_inv32, o_var32, o_detp32, o_rrow32,
+                             o_crow32, o_rstay32, o_lneref, o_lnvref, o_blkext, o_fw, o_lnl,
+                             o_post, o_bw, o_path, o_bins, o_err, o_queue})
+                sig.push_back((long long)o);
+            for (int g = 0; g <= ng; g++) sig.push_back(bounds[g]);
+            const int *ord = (const int *)(h + o_order);
+            for (int j = 0; j < n && pipelined; j++) sig.push_back(plan.inst[ord[j]].ntrees);
+            if (!(E.gexec && sig == E.gsig)) {
+                if (E.gexec) cudaGraphExecDestroy(E.gexec);
+                E.gexec = nullptr;
+                E.gsig.clear();
+                const long long before = kernel_launch_count();
+                CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+                const cudaError_t rc = enqueue();
+                cudaGraph_t graph = nullptr;
+                const cudaError_t rc2 = cudaStreamEndCapture(s, &graph);
+                if (rc != cudaSuccess || rc2 != cudaSuccess) {
+                    if (graph) cudaGraphDestroy(graph);
+                    return cuda_fail(rc != cudaSuccess ? rc : rc2, "capturing the step");
+                }
+                const cudaError_t rc3 =
+                    cudaGraphInstantiateWithFlags(&E.gexec, graph, cudaGraphInstantiateFlagUseNodePriority);
+                cudaGraphDestroy(graph);
+                if (rc3 != cudaSuccess) {
+                    E.gexec = nullptr;
+                    return cuda_fail(rc3, "instantiating the step's graph");
+                }
+                E.gsig = std::move(sig);
+                E.gkernels = kernel_launch_count() - before;
+                E.graph_captures++;
+            } else {
+                for (long long q = 0; q < E.gkernels; q++) note_launch();
+                E.graph_replays++;
+            }
+            CK(cudaGraphLaunch(E.gexec, s));
+        } else {
+            const cudaError_t rc = enqueue();
+            if (rc != cudaSuccess) return cuda_fail(rc, "kernel launch");
+        }
         if (T) CK(cudaEventRecord(E.ev[6], s));
     } else {
         launch_tables(d, fp32, s);
@@ -416,7 +553,7 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
         launch_varemit(d, fp32, s);
         CKL("emission kernel");
         if (T) CK(cudaEventRecord(E.ev[3], s));
-        launch_forward(d, fp32, s);
+        launch_forward(d, fp32, s, cfg.kpt);
         CKL("forward kernel");
         if (T) CK(cudaEventRecord(E.ev[4], s));
         if (want_path) {
@@ -463,7 +600,7 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
         cudaEventElapsedTime(&t.h2d_ms, E.ev[0], E.ev[1]);
         cudaEventElapsedTime(&t.compute_ms, E.ev[1], E.ev[6]);
         cudaEventElapsedTime(&t.d2h_ms, E.ev[6], E.ev[7]);
-        if (!pipelined) {
+        if (serial_timing || special) {
             float ms[5];
             for (int i = 0; i < 5; i++) cudaEventElapsedTime(&ms[i], E.ev[i + 1], E.ev[i + 2]);
             t.tables_ms = ms[0]; t.emit_ms = ms[1]; t.forward_ms = ms[2];
@@ -487,9 +624,82 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
     return 0;
 }
 
+int autotune(const awg_problem *probs, awg_outputs *outs, int n, int precision, int trials,
+             TuneCfg &best, double &best_ms, std::string &err) {
+    Engine &E = engine();
+    const int saved_timing = E.timing;
+    E.timing = 1;
+    trials = std::max(trials, 1);
+    auto measure = [&](const TuneCfg &c, double &ms) -> int {
+        RunOptions o;
+        o.cfg = &c;
+        o.precision = precision;
+        ms = 1e300;
+        for (int t = 0; t < trials; t++) {
+            const int rc = run_batch(probs, outs, n, o, err);
+            if (rc != 0) return rc;
+            ms = std::min(ms, (double)E.last.compute_ms);
+        }
+        return 0;
+    };
+    // coordinate descent from the defaults: forward CTA size (states per owner thread),
+    // group cap of the pipelined schedule, unit length of the per-tree work queue, and
+    // persistent versus one-CTA-per-tree per-tree kernels
+    best = E.defaults;
+    int rc = measure(best, best_ms);
+    const long long key = E.last_key;
+    const std::vector<std::pair<int TuneCfg::*, std::vector<int>>> knobs = {
+        {&TuneCfg::kpt, {0, 2, 4}},
+        {&TuneCfg::group_div, {4, 8, 16}},
+        {&TuneCfg::chunk, {1, 4}},
+        {&TuneCfg::persistent, {1, 0}},
+    };
+    for (const auto &k : knobs) {
+        if (rc != 0) break;
+        const TuneCfg base = best;
+        for (int v : k.second) {
+            if (base.*(k.first) == v) continue;
+            TuneCfg c = base;
+            c.*(k.first) = v;
+            double ms;
+            rc = measure(c, ms);
+            if (rc != 0) break;
+            if (ms < best_ms) {
+                best_ms = ms;
+                best = c;
+            }
+        }
+    }
+    E.timing = saved_timing;
+    if (rc != 0) return rc;
+    {
+        std::lock_guard<std::mutex> lock(E.mu);
+        E.tuned[key] = best;
+    }
+    return 0;
+}
+
 }  // namespace awg
 
 extern "C" {
+
+// Whether steps are captured as CUDA graphs and replayed (1, the default) or launched
+// kernel by kernel (0); and how many steps were replayed / captured so far.
+void awg_set_graphs(int on) { awg::engine().graphs = on != 0; }
+
+// Default schedule (kpt 0 = by state count; group_div, chunk >= 1; persistent 0/1); clears
+// the autotuner's choices so the defaults apply to every shape class.
+void awg_set_schedule(int kpt, int group_div, int chunk, int persistent) {
+    awg::Engine &E = awg::engine();
+    std::lock_guard<std::mutex> lock(E.mu);
+    E.defaults.kpt = (kpt == 1 || kpt == 2 || kpt == 4 || kpt == 8) ? kpt : 0;
+    E.defaults.group_div = std::max(1, group_div);
+    E.defaults.chunk = std::max(1, chunk);
+    E.defaults.persistent = persistent != 0;
+    E.tuned.clear();
+}
+long long awg_graph_replays(void) { return awg::engine().graph_replays; }
+long long awg_graph_captures(void) { return awg::engine().graph_captures; }
 
 // Device times (ms) of the last batch when timing is on: h2d, tables, emissions, forward,
 // traceback, backward, d2h, compute (the kernels from the end of the upload to the start of

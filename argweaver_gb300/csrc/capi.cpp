@@ -170,6 +170,24 @@ int awg_run_batch(const awg_problem *problems, awg_outputs *outputs, int n, int 
     return rc;
 }
 
+int awg_autotune(const awg_problem *problems, awg_outputs *outputs, int n, int precision,
+                 int trials, char *report, int report_len) {
+    g_err.clear();
+    if (!problems || !outputs || n <= 0) { set_error("empty batch"); return -1; }
+    awg::TuneCfg best;
+    double ms = 0.0;
+    std::string err;
+    const int rc = awg::autotune(problems, outputs, n, precision, trials, best, ms, err);
+    if (rc != 0) {
+        set_error(err);
+        return rc;
+    }
+    if (report && report_len > 0)
+        snprintf(report, report_len, "kpt=%d group_div=%d chunk=%d persistent=%d ms=%.3f", best.kpt,
+                 best.group_div, best.chunk, best.persistent, ms);
+    return 0;
+}
+
 int awg_forward_static(const awg_problem *problem, awg_outputs *output, int precision,
                        void *stream) {
     g_err.clear();

@@ -10,7 +10,16 @@
 
 namespace awg {
 
+// Schedule knobs of a batch, chosen by the autotuner (awg_autotune) per shape class.
+struct TuneCfg {
+    int kpt = 0;         // forward: states per owner thread (0: chosen by the state count)
+    int chunk = 1;       // trees per work unit of the persistent per-tree kernels
+    int group_div = 8;   // pipelined schedule: the largest instance group holds n / group_div
+    int persistent = 1;  // per-tree kernels as persistent work-stealing kernels
+};
+
 struct RunOptions {
+    const TuneCfg *cfg = nullptr;  // explicit schedule (the autotuner's trials), else tuned
     int precision = AWG_FP64;
     const double *const *priors = nullptr;  // per problem: given column-0 prior, or NULL
     double *const *backward = nullptr;      // per problem: backward table output, or NULL
@@ -25,6 +34,11 @@ struct RunOptions {
 // Runs a batch; returns 0 or a negative code with err set.
 int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptions &opt,
               std::string &err);
+
+// Times the candidate schedules on this batch (each run `trials` times, the fastest kept)
+// and records the best for the batch's shape class; later batches of the class use it.
+int autotune(const awg_problem *probs, awg_outputs *outs, int n, int precision, int trials,
+             TuneCfg &best, double &best_ms, std::string &err);
 
 // Forward table and log-likelihood of one problem with every device buffer in a static
 // device array (no allocation); returns 0 or a negative code with err set.

@@ -847,21 +847,22 @@ void launch_reg(const BatchDev &d, int nt, cudaStream_t s) {
 // States per owner thread of the register variant (1, 2, 4 or 8; AWG_FORWARD_KPT overrides
 // it for tuning); the CTA then has the reduction warp plus ceil(maxS / KPT) owners rounded
 // up to whole warps.
-int reg_kpt(int maxS) {
+int reg_kpt(int maxS, int want) {
     static const int env = [] {
         const char *e = getenv("AWG_FORWARD_KPT");
         return e ? atoi(e) : 0;
     }();
-    int k = (env == 1 || env == 2 || env == 4 || env == 8) ? env
+    if (!(want == 1 || want == 2 || want == 4 || want == 8)) want = env;
+    int k = (want == 1 || want == 2 || want == 4 || want == 8) ? want
           : maxS <= 64 ? 1 : maxS <= 768 ? 2 : maxS <= 1536 ? 4 : 8;
     while (k < 8 && (maxS + k - 1) / k > 384) k *= 2;
     return k;
 }
 
 template <typename F>
-void launch(const BatchDev &d, cudaStream_t s) {
+void launch(const BatchDev &d, cudaStream_t s, int want_kpt) {
     const int maxS = imax(d.maxS, 1);
-    const int kpt = reg_kpt(maxS);
+    const int kpt = reg_kpt(maxS, want_kpt);
     // the reduction warps plus ceil(maxS / KPT) owners in whole warps
     const int nt = 32 * NRW + imax(32, ((maxS + kpt - 1) / kpt + 31) / 32 * 32);
     if (nt > 512) launch_old<F>(d, d.maxM, s);
@@ -873,14 +874,14 @@ void launch(const BatchDev &d, cudaStream_t s) {
 
 }  // namespace
 
-bool forward_writes_bins(int maxS) {
-    const int kpt = reg_kpt(imax(maxS, 1));
-    return 32 * NRW + imax(32, ((imax(maxS, 1) + kpt - 1) / kpt + 31) / 32 * 32) <= 512;
+bool forward_writes_bins(int maxS, int kpt) {
+    const int k = reg_kpt(imax(maxS, 1), kpt);
+    return 32 * NRW + imax(32, ((imax(maxS, 1) + k - 1) / k + 31) / 32 * 32) <= 512;
 }
 
-void launch_forward(const BatchDev &d, bool fp32, cudaStream_t s) {
-    if (fp32) launch<float>(d, s);
-    else launch<double>(d, s);
+void launch_forward(const BatchDev &d, bool fp32, cudaStream_t s, int kpt) {
+    if (fp32) launch<float>(d, s, kpt);
+    else launch<double>(d, s, kpt);
 }
 
 }  // namespace awg

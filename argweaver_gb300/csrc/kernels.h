@@ -8,15 +8,19 @@
 namespace awg {
 
 // K1: per-block tables (states, transition matrix, same-branch rows, switch matrix,
-// priors into forward column 0, invariant emissions); one CTA per local tree.
-void launch_tables(const BatchDev &d, bool want32, cudaStream_t s);
-// K2: emissions of variant columns (Felsenstein pruning); one CTA per local tree.
-void launch_varemit(const BatchDev &d, bool want32, cudaStream_t s);
-// K3: forward pass, one CTA per instance.
-void launch_forward(const BatchDev &d, bool fp32, cudaStream_t s);
+// priors into forward column 0, invariant emissions); one CTA per local tree, or with a
+// work counter (zeroed) a persistent kernel whose CTAs take units of `chunk` trees.
+void launch_tables(const BatchDev &d, bool want32, cudaStream_t s, int *queue = nullptr,
+                   int chunk = 1);
+// K2: emissions of variant columns (Felsenstein pruning); as K1.
+void launch_varemit(const BatchDev &d, bool want32, cudaStream_t s, int *queue = nullptr,
+                    int chunk = 1);
+// K3: forward pass, one CTA per instance; kpt: states per owner thread of the
+// register-resident variant (0: chosen by the state count).
+void launch_forward(const BatchDev &d, bool fp32, cudaStream_t s, int kpt = 0);
 // Whether K3 writes the FP32 columns' time-bin sums (BatchDev::bins32) at this state count
 // (the register-resident variant does; the fallback for the largest trees does not).
-bool forward_writes_bins(int maxS);
+bool forward_writes_bins(int maxS, int kpt = 0);
 // K4: stochastic traceback, one warp per instance; FP32 with bins32 set: the decomposed draw.
 void launch_traceback(const BatchDev &d, bool fp32, cudaStream_t s);
 // K5: backward pass fused with the posterior marginals, one CTA per instance.

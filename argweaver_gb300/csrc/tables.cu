@@ -289,9 +289,9 @@ __device__ __forceinline__ double prob_branch(double t, double mu, bool mut) {  
 // ---------------------------------------------------------------------------------------
 // K1
 
-__global__ void __launch_bounds__(TAB_THREADS) k_tables(BatchDev d, int want32) {
+// The tables of one local tree, by the whole CTA (TAB_THREADS threads).
+__device__ __forceinline__ void tables_tree(const BatchDev &d, int blk, int want32) {
     extern __shared__ int4 dyn[];
-    const int blk = cta_block(d);
     BlockDev &Bg = d.blocks[blk];
     const BlockDev B = Bg;
     const InstDev I = d.inst[B.inst];
@@ -892,6 +892,39 @@ __global__ void __launch_bounds__(TAB_THREADS) k_tables(BatchDev d, int want32) 
     }
 }
 
+__global__ void __launch_bounds__(TAB_THREADS) k_tables(BatchDev d, int want32) {
+    tables_tree(d, cta_block(d), want32);
+}
+
+// Work queue of a persistent per-tree kernel: units of `chunk` consecutive trees in the
+// batch's tree order (largest instances first), taken by CTAs with an atomic counter.
+struct WorkQueue {
+    int *counter;
+    int nunits, chunk;
+};
+
+// Takes the next unit for the whole CTA; -1 when the queue is empty.
+__device__ __forceinline__ int next_unit(const WorkQueue &q) {
+    __shared__ int unit;
+    __syncthreads();  // the previous unit's reads of `unit` are done
+    if (threadIdx.x == 0) unit = atomicAdd(q.counter, 1);
+    __syncthreads();
+    const int u = unit;
+    return u < q.nunits ? u : -1;
+}
+
+// K1 as a persistent kernel: as many CTAs as fit on the GPU at once, each taking units of
+// trees until the queue is empty (work-stealing over (instance, tree-chunk) units).
+__global__ void __launch_bounds__(TAB_THREADS) k_tables_ws(BatchDev d, int want32, WorkQueue q) {
+    for (int u = next_unit(q); u >= 0; u = next_unit(q)) {
+        const int t1 = imin((u + 1) * q.chunk, d.nblocks);
+        for (int t = u * q.chunk; t < t1; t++) {
+            tables_tree(d, d.blkmap ? d.blkmap[t] : t, want32);
+            __syncthreads();
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------------------
 // K2: emissions of variant columns (calc_emissions' non-invariant branch, emit.cpp:822-844)
 //
@@ -1201,10 +1234,11 @@ __device__ void block_log_offset(const BatchDev &d, const BlockDev &B, const Ins
     if (lane == 0) d.blkext[blk] = s;
 }
 
+// Variant-column emissions of one local tree, by the whole CTA (nwarps warps).
 template <bool FP32OUT>
-__global__ void k_varemit(BatchDev d, int nwarps, int maxS, int smem_bytes) {
+__device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwarps, int maxS,
+                                             int smem_bytes) {
     extern __shared__ int4 dyn[];
-    const int blk = cta_block(d);
     const BlockDev B = d.blocks[blk];
     if (B.nvar == 0 || B.S == 0) {
         if (FP32OUT && threadIdx.x < 32) block_log_offset(d, B, d.inst[B.inst], blk, threadIdx.x);
@@ -1470,6 +1504,23 @@ __global__ void k_varemit(BatchDev d, int nwarps, int maxS, int smem_bytes) {
     }
 }
 
+template <bool FP32OUT>
+__global__ void k_varemit(BatchDev d, int nwarps, int maxS, int smem_bytes) {
+    varemit_tree<FP32OUT>(d, cta_block(d), nwarps, maxS, smem_bytes);
+}
+
+// K2 as a persistent kernel over the same units as k_tables_ws.
+template <bool FP32OUT>
+__global__ void k_varemit_ws(BatchDev d, int nwarps, int maxS, int smem_bytes, WorkQueue q) {
+    for (int u = next_unit(q); u >= 0; u = next_unit(q)) {
+        const int t1 = imin((u + 1) * q.chunk, d.nblocks);
+        for (int t = u * q.chunk; t < t1; t++) {
+            varemit_tree<FP32OUT>(d, d.blkmap ? d.blkmap[t] : t, nwarps, maxS, smem_bytes);
+            __syncthreads();
+        }
+    }
+}
+
 size_t tables_smem(int n, int S, int S1) {
     size_t b = 2 * (size_t)n * sizeof(int4) + 8 * (size_t)n * sizeof(int);
     b += ((n + 15) & ~15);
@@ -1480,19 +1531,47 @@ size_t tables_smem(int n, int S, int S1) {
 
 }  // namespace
 
-void launch_tables(const BatchDev &d, bool want32, cudaStream_t s) {
-    size_t smem = tables_smem(d.maxnodes, d.maxS, d.maxS);
-    static size_t configured = 0;
-    if (smem > configured) {  // opt in; static shared memory counts against 48 KB too
-        if (cudaFuncSetAttribute(k_tables, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return;
-        configured = smem;
+// CTAs of a persistent kernel: as many as are resident on the GPU at once, at most one per
+// unit of work.
+template <typename K>
+int persistent_grid(K kernel, int threads, size_t smem, int nunits) {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
     }
-    k_tables<<<d.nblocks, TAB_THREADS, smem, s>>>(d, want32 ? 1 : 0);
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    return imax(1, imin(nunits, per_sm * sms));
+}
+
+void launch_tables(const BatchDev &d, bool want32, cudaStream_t s, int *queue, int chunk) {
+    size_t smem = tables_smem(d.maxnodes, d.maxS, d.maxS);
+    static size_t configured = 0, configured_ws = 0;
+    if (!queue) {
+        if (smem > configured) {  // opt in; static shared memory counts against 48 KB too
+            if (cudaFuncSetAttribute(k_tables, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return;
+            configured = smem;
+        }
+        k_tables<<<d.nblocks, TAB_THREADS, smem, s>>>(d, want32 ? 1 : 0);
+    } else {
+        if (smem > configured_ws) {
+            if (cudaFuncSetAttribute(k_tables_ws, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return;
+            configured_ws = smem;
+        }
+        chunk = imax(chunk, 1);
+        const WorkQueue q{queue, (d.nblocks + chunk - 1) / chunk, chunk};
+        const int grid = persistent_grid(k_tables_ws, TAB_THREADS, smem, q.nunits);
+        k_tables_ws<<<grid, TAB_THREADS, smem, s>>>(d, want32 ? 1 : 0, q);
+    }
     note_launch();
 }
 
 template <bool FP32OUT>
-void launch_varemit_t(const BatchDev &d, cudaStream_t s) {
+void launch_varemit_t(const BatchDev &d, cudaStream_t s, int *queue, int chunk) {
     const int n = d.maxnodes, maxS = imax(d.maxS, 1);
     int nwarps = 4;
     // the kernel's carve, offset by offset (16-byte alignment where it aligns)
@@ -1511,18 +1590,29 @@ void launch_varemit_t(const BatchDev &d, cudaStream_t s) {
     };
     while (nwarps > 1 && need(nwarps) > 200 * 1024) nwarps--;
     const size_t smem = need(nwarps);
-    static size_t configured = 0;
-    if (smem > configured) {  // opt in; static shared memory counts against 48 KB too
-        if (cudaFuncSetAttribute(k_varemit<FP32OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return;
-        configured = smem;
+    static size_t configured = 0, configured_ws = 0;
+    if (!queue) {
+        if (smem > configured) {  // opt in; static shared memory counts against 48 KB too
+            if (cudaFuncSetAttribute(k_varemit<FP32OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return;
+            configured = smem;
+        }
+        k_varemit<FP32OUT><<<d.nblocks, nwarps * 32, smem, s>>>(d, nwarps, maxS, (int)smem);
+    } else {
+        if (smem > configured_ws) {
+            if (cudaFuncSetAttribute(k_varemit_ws<FP32OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return;
+            configured_ws = smem;
+        }
+        chunk = imax(chunk, 1);
+        const WorkQueue q{queue, (d.nblocks + chunk - 1) / chunk, chunk};
+        const int grid = persistent_grid(k_varemit_ws<FP32OUT>, nwarps * 32, smem, q.nunits);
+        k_varemit_ws<FP32OUT><<<grid, nwarps * 32, smem, s>>>(d, nwarps, maxS, (int)smem, q);
     }
-    k_varemit<FP32OUT><<<d.nblocks, nwarps * 32, smem, s>>>(d, nwarps, maxS, (int)smem);
     note_launch();
 }
 
-void launch_varemit(const BatchDev &d, bool fp32, cudaStream_t s) {
-    if (fp32) launch_varemit_t<true>(d, s);
-    else launch_varemit_t<false>(d, s);
+void launch_varemit(const BatchDev &d, bool fp32, cudaStream_t s, int *queue, int chunk) {
+    if (fp32) launch_varemit_t<true>(d, s, queue, chunk);
+    else launch_varemit_t<false>(d, s, queue, chunk);
 }
 
 }  // namespace awg

@@ -210,9 +210,13 @@ def main():
         return api.run_batch(problems, precision="fp32", want_forward=False, want_path=True,
                              uniforms=uniforms)
 
+    # the autotuner's schedule for this batch (outside the timed region): forward CTA size,
+    # instance groups, work-queue unit length, persistent per-tree kernels
+    schedule = api.autotune(problems, precision="fp32", want_path=True, trials=1)
     api.set_timing(1)
     for _ in range(max(args.warmup, 3)):
         step()
+    graphs0 = api.graph_counts()
     launches0 = api.kernel_launches()
     sampler = ClockSampler()
     sampler.start()
@@ -230,6 +234,7 @@ def main():
         torch.distributed.barrier()
     clocks = sampler.stop()
     launches = api.kernel_launches() - launches0
+    graphs1 = api.graph_counts()
 
     dev_s = sum(dev_ms) / 1e3
     wall_s = sum(wall)
@@ -314,6 +319,9 @@ def main():
         "fp32_vs_fp64_posterior_max_abs_err": max(errs),
         "error_sample": "the 2 largest and 2 median problems of the batch, full length",
         "gpu_launches": launches,
+        "schedule": dict(schedule, graph_replays_in_timed_steps=graphs1["replays"] - graphs0["replays"],
+                         note="autotuned once before the timed steps; each step replays the "
+                              "captured CUDA graph of its kernels"),
         "clocks": clocks,
         "phase_ms": phase_ms,
         "longest_instance_columns": max(p.seqlen for p in problems),

@@ -143,6 +143,30 @@ int awg_problems_cells(const awg_problem *problems, int n, long long *cells);
  * Returns 0 on success, a negative code on error (awg_last_error() has the message). */
 int awg_run_batch(const awg_problem *problems, awg_outputs *outputs, int n, int precision);
 
+/* Autotuner (no counterpart in the reference): runs the batch under each candidate
+ * schedule (states per owner thread of the forward kernel, i.e. its CTA size; instance
+ * group cap of the pipelined schedule; trees per work unit of the persistent per-tree
+ * kernels; persistent or one CTA per tree), each `trials` times, coordinate by coordinate
+ * from the defaults, and keeps the fastest for the batch's shape class (precision, path
+ * wanted, ntimes, binary magnitudes of the largest state count and of the batch size);
+ * later awg_run_batch calls of that class use it. outputs receive the last run's results.
+ * report (optional) receives "kpt=.. group_div=.. chunk=.. persistent=.. ms=..".
+ * Returns 0 or a negative code as awg_run_batch. */
+int awg_autotune(const awg_problem *problems, awg_outputs *outputs, int n, int precision,
+                 int trials, char *report, int report_len);
+
+/* CUDA graphs (no counterpart in the reference): awg_run_batch captures the device part of
+ * a step (kernels, memsets, cross-stream dependencies) once and replays it while a batch
+ * has the same launch parameters (sizes, buffers, schedule); on by default. */
+void awg_set_graphs(int on);
+/* The default schedule (what the autotuner chooses among): kpt = states per owner thread
+ * of the forward kernel (1, 2, 4, 8; 0 = by the largest state count), group_div, chunk as
+ * awg_autotune; persistent 0 launches one CTA per tree. Forgets the autotuner's choices.
+ * Results do not depend on the schedule (every sum has an order fixed by the tree). */
+void awg_set_schedule(int kpt, int group_div, int chunk, int persistent);
+long long awg_graph_replays(void);
+long long awg_graph_captures(void);
+
 /* Bytes of device memory awg_forward_static draws all of its buffers from. */
 #define AWG_STATIC_SCRATCH_BYTES (64ull << 20)
 

@@ -88,10 +88,34 @@ EXTRA = [
     ("awg_set_timing", None, [C.c_int]),
     ("awg_last_timings", None, [c_double_p]),
 ]
+class AwgServerOptions(C.Structure):
+    _fields_ = [("device_bytes", C.c_size_t), ("max_inflight", C.c_int), ("max_batch", C.c_int)]
+
+
+class AwgServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_longlong), ("completed", C.c_longlong), ("failed", C.c_longlong),
+                ("cells", C.c_longlong), ("p50_ms", C.c_double), ("p99_ms", C.c_double),
+                ("mean_ms", C.c_double), ("max_ms", C.c_double), ("span_s", C.c_double),
+                ("busy_s", C.c_double), ("inflight_max", C.c_int)]
+
+
 # exports of the batch API beyond the reference's (declared in include/argweaver_gb300.h)
 PROTOTYPES += [
+    ("awg_server_create", C.c_void_p, [C.POINTER(AwgServerOptions)]),
+    ("awg_server_destroy", None, [C.c_void_p]),
+    ("awg_server_submit", C.c_longlong, [C.c_void_p, C.POINTER(AwgProblem),
+                                         C.POINTER(AwgOutputs), C.c_int, C.c_int]),
+    ("awg_server_wait", C.c_int, [C.c_void_p, C.c_longlong, C.c_int]),
+    ("awg_server_request_times", C.c_int, [C.c_void_p, C.c_longlong, c_double_p]),
+    ("awg_server_forget", C.c_int, [C.c_void_p, C.c_longlong]),
+    ("awg_server_stats_get", C.c_int, [C.c_void_p, C.POINTER(AwgServerStats)]),
+    ("awg_server_resample", C.c_int, [C.c_void_p, C.c_longlong, C.c_void_p, C.c_void_p]),
+    ("awg_server_release", C.c_int, [C.c_void_p, C.c_longlong]),
+    ("awg_server_last_error", C.c_char_p, []),
     ("awg_autotune", C.c_int, [C.POINTER(AwgProblem), C.POINTER(AwgOutputs), C.c_int, C.c_int,
                                C.c_int, C.c_char_p, C.c_int]),
+    ("awg_batch_device_bytes", C.c_longlong, [C.POINTER(AwgProblem), C.c_int, C.c_int, C.c_int,
+                                              C.c_int]),
     ("awg_set_graphs", None, [C.c_int]),
     ("awg_set_schedule", None, [C.c_int, C.c_int, C.c_int, C.c_int]),
     ("awg_graph_replays", C.c_longlong, []),

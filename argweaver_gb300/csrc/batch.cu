@@ -22,10 +22,6 @@
 
 namespace awg {
 
-namespace {
-
-std::atomic<long long> g_launches{0};
-
 struct Timings {
     float plan_ms = 0, h2d_ms = 0, tables_ms = 0, emit_ms = 0, forward_ms = 0,
           traceback_ms = 0, backward_ms = 0, d2h_ms = 0, compute_ms = 0;
@@ -33,8 +29,9 @@ struct Timings {
 
 constexpr int MAXG = 12;  // instance groups of the pipelined schedule
 
-struct Engine {
-    std::mutex mu;
+// One execution context: streams, device arena, page-locked staging and the captured graph
+// of its last step. The engine owns one; a server owns one per in-flight batch.
+struct Ctx {
     bool init = false;
     int device = -1;
     cudaStream_t stream = nullptr;       // uploads, per-tree kernels, downloads
@@ -42,11 +39,43 @@ struct Engine {
                                          // priority, so their CTAs are placed first)
     char *dev = nullptr;
     size_t dev_cap = 0;
-    char *host = nullptr;
+    char *host = nullptr;                // inputs staging (page-locked)
     size_t host_cap = 0;
+    char *ext = nullptr;                 // device region given by the owner (a server's
+    size_t ext_cap = 0;                  // pool), used instead of the grow-only arena
+    char *hout = nullptr;                // outputs staging of an asynchronous batch
+    size_t hout_cap = 0;
     cudaEvent_t ev[8];
     cudaEvent_t gev[2 * MAXG + 2];
+    cudaEvent_t done = nullptr;          // end of the last batch's downloads
     Timings last;
+    // the captured step of the last batch (kernels, memsets, cross-stream events) and the
+    // launch parameters it was captured with; replayed while they match
+    cudaGraphExec_t gexec = nullptr;
+    std::vector<long long> gsig;
+    long long gkernels = 0;
+    // an asynchronous batch's outputs: (caller buffer, staging offset, bytes)
+    struct Copy {
+        void *dst;
+        size_t off, bytes;
+    };
+    std::vector<Copy> copies;
+    size_t err_off = 0;
+    bool timed = false, serial_phases = false;
+    HostPlan plan;
+    // the last batch's device view, for draws from its resident forward tables
+    BatchDev d{};
+    bool have_d = false, d_fp32 = false;
+    size_t o_u = 0;
+};
+
+namespace {
+
+std::atomic<long long> g_launches{0};
+
+struct Engine {
+    std::mutex mu;
+    Ctx ctx;
     int timing = 0;  // 0 off; 1 on (overlapped schedule: one compute time); 2 serial phases
     // schedule defaults (environment overrides for experiments) and the tuned ones by class
     TuneCfg defaults = [] {
@@ -56,18 +85,14 @@ struct Engine {
         if (const char *e = getenv("AWG_PERSISTENT")) c.persistent = atoi(e) != 0;
         return c;
     }();
+    std::mutex tune_mu;  // the tuned table, read by every context
     std::map<long long, TuneCfg> tuned;
-    // the captured step of the last batch (kernels, memsets, cross-stream events) and the
-    // launch parameters it was captured with; replayed while they match
     bool graphs = [] {
         const char *e = getenv("AWG_GRAPHS");
         return !(e && atoi(e) == 0);
     }();
-    cudaGraphExec_t gexec = nullptr;
-    std::vector<long long> gsig;
-    long long gkernels = 0;
-    long long graph_replays = 0, graph_captures = 0;
-    long long last_key = -1;  // shape class of the last batch
+    std::atomic<long long> graph_replays{0}, graph_captures{0};
+    long long last_key = -1;  // shape class of the engine's last batch
 };
 
 // Shape class of a batch for the tuned schedules: precision, path or not, ntimes, and the
@@ -122,14 +147,21 @@ struct Layout {
 long long kernel_launch_count() { return g_launches.load(); }
 void note_launch() { g_launches.fetch_add(1); }
 
-int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptions &opt,
-              std::string &err) {
+// Plans, uploads and enqueues one batch on context C. Synchronous (async false): outputs go
+// straight to the caller's buffers and the call returns when they are there. Asynchronous:
+// outputs go to C's page-locked staging, C.done marks their arrival, and ctx_complete (on
+// the same thread, before C's next batch) checks the device error record and hands them
+// over. timing: 0 off, 1 one compute time, 2 kernels one phase after another.
+int ctx_launch(Ctx &C, const awg_problem *probs, awg_outputs *outs, int n, const RunOptions &opt,
+               bool async, int timing, long long *key_out, std::string &err,
+               size_t *dry_bytes) {
+    const bool dry = dry_bytes != nullptr;  // only the device bytes the batch needs
     Engine &E = engine();
-    std::lock_guard<std::mutex> lock(E.mu);
     const bool fp32 = opt.precision == AWG_FP32;
     if (!fp32 && opt.precision != AWG_FP64) { err = "precision must be AWG_FP64 or AWG_FP32"; return -1; }
 
-    HostPlan plan;
+    HostPlan &plan = C.plan;
+    plan = HostPlan();
     if (!plan_layout(probs, n, plan, err, true)) return -1;
 
     bool want_path = false, want_post = false, want_bw = false;
@@ -140,32 +172,35 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
     }
     want_post |= want_bw;
     TuneCfg cfg = E.defaults;
-    E.last_key = shape_key(plan, fp32, want_path);
+    const long long key = shape_key(plan, fp32, want_path);
+    if (key_out) *key_out = key;
     if (opt.cfg) {
         cfg = *opt.cfg;
     } else {
-        auto it = E.tuned.find(shape_key(plan, fp32, want_path));
+        std::lock_guard<std::mutex> lock(E.tune_mu);
+        auto it = E.tuned.find(key);
         if (it != E.tuned.end()) cfg = it->second;
     }
 
-    if (!E.init) {
+    if (!dry && !C.init) {
         int dc = 0;
         if (cudaGetDeviceCount(&dc) != cudaSuccess || dc == 0) {
             err = "no CUDA device: the threading HMM runs on the GPU only";
             return -2;
         }
-        CK(cudaGetDevice(&E.device));
-        CK(cudaStreamCreateWithFlags(&E.stream, cudaStreamNonBlocking));
+        CK(cudaGetDevice(&C.device));
+        CK(cudaStreamCreateWithFlags(&C.stream, cudaStreamNonBlocking));
         int lo = 0, hi = 0;
         CK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
         for (int g = 0; g < MAXG; g++)
-            CK(cudaStreamCreateWithPriority(&E.gstream[g], cudaStreamNonBlocking, hi));
-        for (int i = 0; i < 8; i++) CK(cudaEventCreate(&E.ev[i]));
+            CK(cudaStreamCreateWithPriority(&C.gstream[g], cudaStreamNonBlocking, hi));
+        for (int i = 0; i < 8; i++) CK(cudaEventCreate(&C.ev[i]));
         for (int i = 0; i < 2 * MAXG + 2; i++)
-            CK(cudaEventCreateWithFlags(&E.gev[i], cudaEventDisableTiming));
-        E.init = true;
+            CK(cudaEventCreateWithFlags(&C.gev[i], cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&C.done, cudaEventDisableTiming));
+        C.init = true;
     }
-    cudaStream_t s = E.stream;
+    cudaStream_t s = C.stream;
 
     // ---------------- layout
     const long long ST = std::max(plan.total_states, 1LL);
@@ -185,24 +220,34 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
     const size_t o_u = in.add(want_path ? sizeof(double) * COLS : 0);
     const size_t in_bytes = in.total;
 
-    if (in_bytes > E.host_cap) {
-        if (E.host) cudaFreeHost(E.host);
-        E.host = nullptr;
-        E.host_cap = 0;
-        const size_t cap = in_bytes + in_bytes / 8;
-        CK(cudaMallocHost(&E.host, cap));
-        E.host_cap = cap;
-    }
+    char *h = C.host;
+    std::vector<char> dry_stage;  // a dry run still fills the plan (variant counts) on the host
+    if (dry) {
+        dry_stage.resize(in_bytes);
+        h = dry_stage.data();
+        plan_fill(probs, n, plan, PlanDst{(int *)(h + o_nodes), (int *)(h + o_map),
+                                          (uint8_t *)(h + o_seq), (uint8_t *)(h + o_cls),
+                                          (int *)(h + o_cvar)});
+    } else {
+        if (in_bytes > C.host_cap) {
+            if (C.host) cudaFreeHost(C.host);
+            C.host = nullptr;
+            C.host_cap = 0;
+            const size_t cap = in_bytes + in_bytes / 8;
+            CK(cudaMallocHost(&C.host, cap));
+            C.host_cap = cap;
+        }
 
-    // ---------------- stage inputs
-    char *h = E.host;
-    // per-node, per-column and sequence arrays straight into the staging buffer
-    plan_fill(probs, n, plan, PlanDst{(int *)(h + o_nodes), (int *)(h + o_map),
-                                      (uint8_t *)(h + o_seq), (uint8_t *)(h + o_cls),
-                                      (int *)(h + o_cvar)});
-    memcpy(h + o_inst, plan.inst.data(), sizeof(InstDev) * plan.ninst);
-    memcpy(h + o_blocks, plan.blocks.data(), sizeof(BlockDev) * plan.nblocks);
-    memcpy(h + o_model, plan.model.data(), sizeof(double) * plan.model.size());
+        // ---------------- stage inputs
+        h = C.host;
+        // per-node, per-column and sequence arrays straight into the staging buffer
+        plan_fill(probs, n, plan, PlanDst{(int *)(h + o_nodes), (int *)(h + o_map),
+                                          (uint8_t *)(h + o_seq), (uint8_t *)(h + o_cls),
+                                          (int *)(h + o_cvar)});
+        memcpy(h + o_inst, plan.inst.data(), sizeof(InstDev) * plan.ninst);
+        memcpy(h + o_blocks, plan.blocks.data(), sizeof(BlockDev) * plan.nblocks);
+        memcpy(h + o_model, plan.model.data(), sizeof(double) * plan.model.size());
+    }
 
     Layout w;  // work region follows the inputs
     w.total = in_bytes;
@@ -248,14 +293,26 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
     const size_t o_err = w.add(4 * sizeof(int));
     const size_t o_queue = w.add(sizeof(int) * 2 * MAXG);  // work counters of the groups
     const size_t total = w.total;
+    if (dry) {
+        *dry_bytes = total;
+        return 0;
+    }
 
-    if (total > E.dev_cap) {
-        if (E.dev) cudaFree(E.dev);
-        E.dev = nullptr;
-        E.dev_cap = 0;
+    if (C.ext) {
+        if (total > C.ext_cap) {
+            char b[200];
+            snprintf(b, sizeof(b), "the batch needs %zu bytes of device memory; its region holds %zu",
+                     total, C.ext_cap);
+            err = b;
+            return -5;
+        }
+    } else if (total > C.dev_cap) {
+        if (C.dev) cudaFree(C.dev);
+        C.dev = nullptr;
+        C.dev_cap = 0;
         const size_t cap = total + total / 8;
-        CK(cudaMalloc(&E.dev, cap));
-        E.dev_cap = cap;
+        CK(cudaMalloc(&C.dev, cap));
+        C.dev_cap = cap;
     }
 
     {
@@ -293,7 +350,7 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
 
     BatchDev d;
     memset(&d, 0, sizeof(d));
-    char *D = E.dev;
+    char *D = C.ext ? C.ext : C.dev;
     d.ninst = plan.ninst; d.nblocks = plan.nblocks; d.maxS = plan.maxS; d.maxT = plan.maxT;
     d.maxnodes = plan.maxnodes;
     d.maxM = plan.maxM;
@@ -343,6 +400,10 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
     d.path = want_path ? (int *)(D + o_path) : nullptr;
     d.bins32 = want_bins ? (float *)(D + o_bins) : nullptr;
     d.err = (int *)(D + o_err);
+    C.d = d;
+    C.have_d = true;
+    C.d_fp32 = fp32;
+    C.o_u = o_u;
 
     // Schedule. Serial: per-tree kernels over the batch, then per-instance kernels. Pipelined
     // (larger batches): instances in groups, largest first; a group's per-tree kernels run
@@ -352,14 +413,14 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
     // persistent, work-stealing over units of trees; the device part of a step is captured
     // once as a CUDA graph and replayed while its launch parameters repeat.
     const bool special = opt.tables_only || opt.priors;
-    const bool serial_timing = E.timing == 2;
+    const bool serial_timing = timing == 2;
     const bool pipelined = n >= 16 && !special && !serial_timing;
-    const bool T = E.timing != 0;
+    const bool T = timing != 0;
     int *queues = (int *)(D + o_queue);
-    if (T) CK(cudaEventRecord(E.ev[0], s));
+    if (T) CK(cudaEventRecord(C.ev[0], s));
     CK(cudaMemcpyAsync(D, h, in_bytes, cudaMemcpyHostToDevice, s));
     CK(cudaMemsetAsync(d.err, 0, 4 * sizeof(int), s));
-    if (T) CK(cudaEventRecord(E.ev[1], s));
+    if (T) CK(cudaEventRecord(C.ev[1], s));
 
     // groups of the pipelined schedule: sizes n/32, doubling up to n/group_div, the last
     // takes the rest
@@ -404,9 +465,9 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
                 EQ(cudaGetLastError());
                 launch_varemit(dg, fp32, s, qp(2 * g + 1), cfg.chunk);
                 EQ(cudaGetLastError());
-                cudaStream_t gs = E.gstream[g];
-                EQ(cudaEventRecord(E.gev[2 * g], s));
-                EQ(cudaStreamWaitEvent(gs, E.gev[2 * g], 0));
+                cudaStream_t gs = C.gstream[g];
+                EQ(cudaEventRecord(C.gev[2 * g], s));
+                EQ(cudaStreamWaitEvent(gs, C.gev[2 * g], 0));
                 launch_forward(dg, fp32, gs, cfg.kpt);
                 EQ(cudaGetLastError());
                 if (want_path) {
@@ -417,9 +478,9 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
                     launch_backward(dg, fp32, want_bw ? (double *)(D + o_bw) : nullptr, gs);
                     EQ(cudaGetLastError());
                 }
-                EQ(cudaEventRecord(E.gev[2 * g + 1], gs));
+                EQ(cudaEventRecord(C.gev[2 * g + 1], gs));
             }
-            for (int g = 0; g < ng; g++) EQ(cudaStreamWaitEvent(s, E.gev[2 * g + 1], 0));
+            for (int g = 0; g < ng; g++) EQ(cudaStreamWaitEvent(s, C.gev[2 * g + 1], 0));
         } else {
             launch_tables(d, fp32, s, qp(0), cfg.chunk);
             EQ(cudaGetLastError());
@@ -465,10 +526,10 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
             for (int g = 0; g <= ng; g++) sig.push_back(bounds[g]);
             const int *ord = (const int *)(h + o_order);
             for (int j = 0; j < n && pipelined; j++) sig.push_back(plan.inst[ord[j]].ntrees);
-            if (!(E.gexec && sig == E.gsig)) {
-                if (E.gexec) cudaGraphExecDestroy(E.gexec);
-                E.gexec = nullptr;
-                E.gsig.clear();
+            if (!(C.gexec && sig == C.gsig)) {
+                if (C.gexec) cudaGraphExecDestroy(C.gexec);
+                C.gexec = nullptr;
+                C.gsig.clear();
                 const long long before = kernel_launch_count();
                 CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
                 const cudaError_t rc = enqueue();
@@ -479,25 +540,25 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
                     return cuda_fail(rc != cudaSuccess ? rc : rc2, "capturing the step");
                 }
                 const cudaError_t rc3 =
-                    cudaGraphInstantiateWithFlags(&E.gexec, graph, cudaGraphInstantiateFlagUseNodePriority);
+                    cudaGraphInstantiateWithFlags(&C.gexec, graph, cudaGraphInstantiateFlagUseNodePriority);
                 cudaGraphDestroy(graph);
                 if (rc3 != cudaSuccess) {
-                    E.gexec = nullptr;
+                    C.gexec = nullptr;
                     return cuda_fail(rc3, "instantiating the step's graph");
                 }
-                E.gsig = std::move(sig);
-                E.gkernels = kernel_launch_count() - before;
+                C.gsig = std::move(sig);
+                C.gkernels = kernel_launch_count() - before;
                 E.graph_captures++;
             } else {
-                for (long long q = 0; q < E.gkernels; q++) note_launch();
+                for (long long q = 0; q < C.gkernels; q++) note_launch();
                 E.graph_replays++;
             }
-            CK(cudaGraphLaunch(E.gexec, s));
+            CK(cudaGraphLaunch(C.gexec, s));
         } else {
             const cudaError_t rc = enqueue();
             if (rc != cudaSuccess) return cuda_fail(rc, "kernel launch");
         }
-        if (T) CK(cudaEventRecord(E.ev[6], s));
+        if (T) CK(cudaEventRecord(C.ev[6], s));
     } else {
         launch_tables(d, fp32, s);
         CKL("table kernel");
@@ -549,65 +610,93 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
             }
             return 0;
         }
-        if (T) CK(cudaEventRecord(E.ev[2], s));
+        if (T) CK(cudaEventRecord(C.ev[2], s));
         launch_varemit(d, fp32, s);
         CKL("emission kernel");
-        if (T) CK(cudaEventRecord(E.ev[3], s));
+        if (T) CK(cudaEventRecord(C.ev[3], s));
         launch_forward(d, fp32, s, cfg.kpt);
         CKL("forward kernel");
-        if (T) CK(cudaEventRecord(E.ev[4], s));
+        if (T) CK(cudaEventRecord(C.ev[4], s));
         if (want_path) {
             launch_traceback(d, fp32, s);
             CKL("traceback kernel");
         }
-        if (T) CK(cudaEventRecord(E.ev[5], s));
+        if (T) CK(cudaEventRecord(C.ev[5], s));
         if (want_post) {
             launch_backward(d, fp32, want_bw ? (double *)(D + o_bw) : nullptr, s);
             CKL("backward kernel");
         }
-        if (T) CK(cudaEventRecord(E.ev[6], s));
+        if (T) CK(cudaEventRecord(C.ev[6], s));
     }
 
-    // ---------------- downloads
+    // ---------------- downloads (asynchronous: into the page-locked output staging)
+    C.copies.clear();
+    size_t hout_bytes = 0;
+    auto out_slot = [&](size_t bytes) {
+        const size_t off = hout_bytes;
+        hout_bytes += (bytes + 15) & ~(size_t)15;
+        return off;
+    };
+    struct Pending {
+        void *dst;
+        const void *src;
+        size_t bytes;
+    };
+    std::vector<Pending> pend;
     for (int q = 0; q < n; q++) {
         const InstDev &I = plan.inst[q];
         const long long cells = (q + 1 < n ? plan.inst[q + 1].cell0 : plan.total_cells) - I.cell0;
         const awg_outputs &o = outs[q];
-        if (o.forward && !fp32)
-            CK(cudaMemcpyAsync(o.forward, d.fw64 + I.cell0, sizeof(double) * cells,
-                               cudaMemcpyDeviceToHost, s));
-        if (o.forward32 && fp32)
-            CK(cudaMemcpyAsync(o.forward32, d.fw32 + I.cell0, sizeof(float) * cells,
-                               cudaMemcpyDeviceToHost, s));
-        if (o.posterior)
-            CK(cudaMemcpyAsync(o.posterior, d.post + I.cell0, sizeof(double) * cells,
-                               cudaMemcpyDeviceToHost, s));
+        if (o.forward && !fp32) pend.push_back({o.forward, d.fw64 + I.cell0, sizeof(double) * cells});
+        if (o.forward32 && fp32) pend.push_back({o.forward32, d.fw32 + I.cell0, sizeof(float) * cells});
+        if (o.posterior) pend.push_back({o.posterior, d.post + I.cell0, sizeof(double) * cells});
         if (opt.backward && opt.backward[q])
-            CK(cudaMemcpyAsync(opt.backward[q], (double *)(D + o_bw) + I.cell0,
-                               sizeof(double) * cells, cudaMemcpyDeviceToHost, s));
-        if (o.path)
-            CK(cudaMemcpyAsync(o.path, d.path + I.col0, sizeof(int) * I.seqlen,
-                               cudaMemcpyDeviceToHost, s));
-        if (o.loglik)
-            CK(cudaMemcpyAsync(o.loglik, d.lnl + q, sizeof(double), cudaMemcpyDeviceToHost, s));
+            pend.push_back({opt.backward[q], (double *)(D + o_bw) + I.cell0, sizeof(double) * cells});
+        if (o.path) pend.push_back({o.path, d.path + I.col0, sizeof(int) * I.seqlen});
+        if (o.loglik) pend.push_back({o.loglik, d.lnl + q, sizeof(double)});
     }
-    int dev_err[4] = {0, 0, 0, 0};
-    CK(cudaMemcpyAsync(dev_err, d.err, 4 * sizeof(int), cudaMemcpyDeviceToHost, s));
-    if (T) CK(cudaEventRecord(E.ev[7], s));
-    CK(cudaStreamSynchronize(s));
-    if (T) {
+    if (async) {
+        for (const Pending &pd : pend) C.copies.push_back({pd.dst, out_slot(pd.bytes), pd.bytes});
+    }
+    C.err_off = out_slot(4 * sizeof(int));
+    if (hout_bytes > C.hout_cap) {
+        if (C.hout) cudaFreeHost(C.hout);
+        C.hout = nullptr;
+        C.hout_cap = 0;
+        const size_t cap = std::max(hout_bytes + hout_bytes / 8, (size_t)256);
+        CK(cudaMallocHost(&C.hout, cap));
+        C.hout_cap = cap;
+    }
+    for (size_t i = 0; i < pend.size(); i++)
+        CK(cudaMemcpyAsync(async ? (void *)(C.hout + C.copies[i].off) : pend[i].dst, pend[i].src,
+                           pend[i].bytes, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(C.hout + C.err_off, d.err, 4 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (T) CK(cudaEventRecord(C.ev[7], s));
+    CK(cudaEventRecord(C.done, s));
+    C.timed = T;
+    C.serial_phases = serial_timing || special;
+    return 0;
+}
+
+// Waits for context C's last batch, records its timings, checks its device error record
+// and (asynchronous batches) hands the outputs to the caller's buffers.
+int ctx_complete(Ctx &C, std::string &err) {
+    CK(cudaEventSynchronize(C.done));
+    if (C.timed) {
         Timings t;
-        cudaEventElapsedTime(&t.h2d_ms, E.ev[0], E.ev[1]);
-        cudaEventElapsedTime(&t.compute_ms, E.ev[1], E.ev[6]);
-        cudaEventElapsedTime(&t.d2h_ms, E.ev[6], E.ev[7]);
-        if (serial_timing || special) {
+        cudaEventElapsedTime(&t.h2d_ms, C.ev[0], C.ev[1]);
+        cudaEventElapsedTime(&t.compute_ms, C.ev[1], C.ev[6]);
+        cudaEventElapsedTime(&t.d2h_ms, C.ev[6], C.ev[7]);
+        if (C.serial_phases) {
             float ms[5];
-            for (int i = 0; i < 5; i++) cudaEventElapsedTime(&ms[i], E.ev[i + 1], E.ev[i + 2]);
+            for (int i = 0; i < 5; i++) cudaEventElapsedTime(&ms[i], C.ev[i + 1], C.ev[i + 2]);
             t.tables_ms = ms[0]; t.emit_ms = ms[1]; t.forward_ms = ms[2];
             t.traceback_ms = ms[3]; t.backward_ms = ms[4];
         }
-        E.last = t;
+        C.last = t;
     }
+    int dev_err[4];
+    memcpy(dev_err, C.hout + C.err_off, sizeof(dev_err));
     if (dev_err[0] != 0) {
         static const char *what[] = {"", "switch from a fully specified tree found no state",
                                      "shared-memory plan exceeded", "a forward column summed to "
@@ -619,9 +708,139 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
                  dev_err[0], dev_err[0] < 7 ? what[dev_err[0]] : "?", dev_err[1], dev_err[2],
                  dev_err[3]);
         err = buf;
+        C.copies.clear();
         return -4;
     }
+    for (const Ctx::Copy &c : C.copies) memcpy(c.dst, C.hout + c.off, c.bytes);
+    C.copies.clear();
     return 0;
+}
+
+Ctx *ctx_create() { return new Ctx(); }
+
+void ctx_destroy(Ctx *C) {
+    if (!C) return;
+    if (C->init) {
+        cudaStreamSynchronize(C->stream);
+        for (int g = 0; g < MAXG; g++) cudaStreamSynchronize(C->gstream[g]);
+        if (C->gexec) cudaGraphExecDestroy(C->gexec);
+        for (int g = 0; g < MAXG; g++) cudaStreamDestroy(C->gstream[g]);
+        cudaStreamDestroy(C->stream);
+        for (int i = 0; i < 8; i++) cudaEventDestroy(C->ev[i]);
+        for (int i = 0; i < 2 * MAXG + 2; i++) cudaEventDestroy(C->gev[i]);
+        cudaEventDestroy(C->done);
+    }
+    if (C->dev) cudaFree(C->dev);
+    if (C->host) cudaFreeHost(C->host);
+    if (C->hout) cudaFreeHost(C->hout);
+    delete C;
+}
+
+void ctx_set_region(Ctx *C, char *dev, size_t bytes) {
+    C->ext = dev;
+    C->ext_cap = bytes;
+}
+
+bool ctx_ready(Ctx *C) { return cudaEventQuery(C->done) == cudaSuccess; }
+
+void ctx_sync(Ctx *C) {
+    if (!C->init) return;
+    cudaStreamSynchronize(C->stream);
+    for (int g = 0; g < MAXG; g++) cudaStreamSynchronize(C->gstream[g]);
+}
+
+int ctx_launch_async(Ctx *C, const awg_problem *probs, awg_outputs *outs, int n, int precision,
+                     std::string &err) {
+    RunOptions opt;
+    opt.precision = precision;
+    return ctx_launch(*C, probs, outs, n, opt, true, 0, nullptr, err, nullptr);
+}
+
+int ctx_finish(Ctx *C, std::string &err) { return ctx_complete(*C, err); }
+
+long long batch_device_bytes(const awg_problem *probs, int n, int precision, bool path,
+                             bool posterior, std::string &err) {
+    Ctx tmp;
+    std::vector<awg_outputs> outs(n);
+    static double sink;
+    for (auto &o : outs) {
+        memset(&o, 0, sizeof(o));
+        if (path) o.path = (int *)&sink;  // never written: only the wanted outputs count
+        if (posterior) o.posterior = &sink;
+    }
+    RunOptions opt;
+    opt.precision = precision;
+    size_t bytes = 0;
+    const int rc = ctx_launch(tmp, probs, outs.data(), n, opt, false, 0, nullptr, err, &bytes);
+    return rc != 0 ? rc : (long long)bytes;
+}
+
+// Draws new paths from context C's last batch: its forward tables (and FP32 bin sums) are
+// still on the device, so only the uniforms go up and only the traceback runs.
+int ctx_resample(Ctx *C, const double *const *uniforms, int *const *paths, std::string &err) {
+    if (!C->have_d || !C->d.path || !C->d.uniforms) {
+        err = "the context's last batch drew no paths";
+        return -1;
+    }
+    const HostPlan &plan = C->plan;
+    cudaStream_t s = C->stream;
+    CK(cudaEventSynchronize(C->done));  // the staging buffers are free
+    double *u = (double *)(C->host + C->o_u);
+    for (int q = 0; q < plan.ninst; q++) {
+        const InstDev &I = plan.inst[q];
+        if (uniforms && uniforms[q]) {
+            memcpy(u + I.col0, uniforms[q], sizeof(double) * I.seqlen);
+        } else {
+            for (int c = I.seqlen - 1; c >= 0; c--) u[I.col0 + c] = rand() / double(RAND_MAX);
+        }
+    }
+    CK(cudaMemcpyAsync((void *)C->d.uniforms, u, sizeof(double) * std::max(plan.total_cols, 1LL),
+                       cudaMemcpyHostToDevice, s));
+    CK(cudaMemsetAsync(C->d.err, 0, 4 * sizeof(int), s));
+    launch_traceback(C->d, C->d_fp32, s);
+    CK(cudaGetLastError());
+    C->copies.clear();
+    size_t off = 16;  // the error record first
+    for (int q = 0; q < plan.ninst; q++) {
+        const InstDev &I = plan.inst[q];
+        if (!paths || !paths[q]) continue;
+        const size_t bytes = sizeof(int) * I.seqlen;
+        C->copies.push_back({paths[q], off, bytes});
+        off += (bytes + 15) & ~(size_t)15;
+    }
+    if (off > C->hout_cap) {
+        if (C->hout) cudaFreeHost(C->hout);
+        C->hout = nullptr;
+        C->hout_cap = 0;
+        CK(cudaMallocHost(&C->hout, off + off / 8));
+        C->hout_cap = off + off / 8;
+    }
+    C->err_off = 0;
+    CK(cudaMemcpyAsync(C->hout, C->d.err, 4 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    int k = 0;
+    for (int q = 0; q < plan.ninst; q++) {
+        if (!paths || !paths[q]) continue;
+        CK(cudaMemcpyAsync(C->hout + C->copies[k].off, C->d.path + plan.inst[q].col0,
+                           C->copies[k].bytes, cudaMemcpyDeviceToHost, s));
+        k++;
+    }
+    CK(cudaEventRecord(C->done, s));
+    C->timed = false;
+    return ctx_complete(*C, err);
+}
+
+int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptions &opt,
+              std::string &err) {
+    Engine &E = engine();
+    std::lock_guard<std::mutex> lock(E.mu);
+    long long key = -1;
+    const int rc = ctx_launch(E.ctx, probs, outs, n, opt, false, E.timing, &key, err, nullptr);
+    E.last_key = key;
+    if (rc != 0) {
+        if (E.ctx.init) cudaStreamSynchronize(E.ctx.stream);  // nothing left in flight
+        return rc;
+    }
+    return ctx_complete(E.ctx, err);
 }
 
 int autotune(const awg_problem *probs, awg_outputs *outs, int n, int precision, int trials,
@@ -638,7 +857,7 @@ int autotune(const awg_problem *probs, awg_outputs *outs, int n, int precision, 
         for (int t = 0; t < trials; t++) {
             const int rc = run_batch(probs, outs, n, o, err);
             if (rc != 0) return rc;
-            ms = std::min(ms, (double)E.last.compute_ms);
+            ms = std::min(ms, (double)E.ctx.last.compute_ms);
         }
         return 0;
     };
@@ -673,7 +892,7 @@ int autotune(const awg_problem *probs, awg_outputs *outs, int n, int precision, 
     E.timing = saved_timing;
     if (rc != 0) return rc;
     {
-        std::lock_guard<std::mutex> lock(E.mu);
+        std::lock_guard<std::mutex> lock(E.tune_mu);
         E.tuned[key] = best;
     }
     return 0;
@@ -696,6 +915,7 @@ void awg_set_schedule(int kpt, int group_div, int chunk, int persistent) {
     E.defaults.group_div = std::max(1, group_div);
     E.defaults.chunk = std::max(1, chunk);
     E.defaults.persistent = persistent != 0;
+    std::lock_guard<std::mutex> tl(E.tune_mu);
     E.tuned.clear();
 }
 long long awg_graph_replays(void) { return awg::engine().graph_replays; }
@@ -707,7 +927,7 @@ long long awg_graph_captures(void) { return awg::engine().graph_captures; }
 // runs the kernels one phase after another to time each.
 void awg_set_timing(int mode) { awg::engine().timing = mode; }
 void awg_last_timings(double *out8) {
-    const auto &t = awg::engine().last;
+    const auto &t = awg::engine().ctx.last;
     const float v[8] = {t.h2d_ms, t.tables_ms, t.emit_ms, t.forward_ms, t.traceback_ms,
                         t.backward_ms, t.d2h_ms, t.compute_ms};
     for (int i = 0; i < 8; i++) out8[i] = v[i];

@@ -170,6 +170,17 @@ int awg_run_batch(const awg_problem *problems, awg_outputs *outputs, int n, int 
     return rc;
 }
 
+long long awg_batch_device_bytes(const awg_problem *problems, int n, int precision, int want_path,
+                                 int want_posterior) {
+    g_err.clear();
+    if (!problems || n <= 0) { set_error("empty batch"); return -1; }
+    std::string err;
+    const long long b = awg::batch_device_bytes(problems, n, precision, want_path != 0,
+                                                want_posterior != 0, err);
+    if (b < 0) set_error(err);
+    return b;
+}
+
 int awg_autotune(const awg_problem *problems, awg_outputs *outputs, int n, int precision,
                  int trials, char *report, int report_len) {
     g_err.clear();

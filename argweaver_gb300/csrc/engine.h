@@ -40,6 +40,25 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
 int autotune(const awg_problem *probs, awg_outputs *outs, int n, int precision, int trials,
              TuneCfg &best, double &best_ms, std::string &err);
 
+// Execution contexts for callers that keep several batches in flight (the server): each
+// has its own streams, page-locked staging and either a grow-only device arena or a region
+// the owner hands it. A context runs one batch at a time: launch, then finish (which waits).
+struct Ctx;
+Ctx *ctx_create();
+void ctx_destroy(Ctx *C);
+void ctx_set_region(Ctx *C, char *dev, size_t bytes);
+int ctx_launch_async(Ctx *C, const awg_problem *probs, awg_outputs *outs, int n, int precision,
+                     std::string &err);
+bool ctx_ready(Ctx *C);  // the launched batch's outputs have arrived
+void ctx_sync(Ctx *C);   // everything enqueued on the context has finished
+int ctx_finish(Ctx *C, std::string &err);
+// New paths from the context's last batch (paths wanted), its forward tables still resident:
+// uniforms[q] per problem (NULL: libc rand()), paths[q] per problem (NULL: not wanted).
+int ctx_resample(Ctx *C, const double *const *uniforms, int *const *paths, std::string &err);
+// Device bytes a batch needs (the engine's layout), or a negative code with err set.
+long long batch_device_bytes(const awg_problem *probs, int n, int precision, bool path,
+                             bool posterior, std::string &err);
+
 // Forward table and log-likelihood of one problem with every device buffer in a static
 // device array (no allocation); returns 0 or a negative code with err set.
 int run_static(const awg_problem *p, awg_outputs *out, int precision, cudaStream_t s,

@@ -143,6 +143,11 @@ int awg_problems_cells(const awg_problem *problems, int n, long long *cells);
  * Returns 0 on success, a negative code on error (awg_last_error() has the message). */
 int awg_run_batch(const awg_problem *problems, awg_outputs *outputs, int n, int precision);
 
+/* Device bytes awg_run_batch needs for this batch with these outputs wanted (the size of a
+ * server pool or of a region to set aside), or a negative code (awg_last_error). */
+long long awg_batch_device_bytes(const awg_problem *problems, int n, int precision, int want_path,
+                                 int want_posterior);
+
 /* Autotuner (no counterpart in the reference): runs the batch under each candidate
  * schedule (states per owner thread of the forward kernel, i.e. its CTA size; instance
  * group cap of the pipelined schedule; trees per work unit of the persistent per-tree
@@ -166,6 +171,52 @@ void awg_set_graphs(int on);
 void awg_set_schedule(int kpt, int group_div, int chunk, int persistent);
 long long awg_graph_replays(void);
 long long awg_graph_captures(void);
+
+/* ---------------------------------------------------------------------------------
+ * Serving loop (no counterpart in the reference): continuous batching of threading
+ * requests. Requests from any thread queue FIFO; a worker forms batches from the queue head
+ * (one precision and one set of wanted outputs, as many as fit the free device memory and
+ * max_batch) and keeps up to max_inflight of them on the GPU at once, each on its own
+ * streams and region of one device pool allocated at creation (no allocation while
+ * serving). Requests arriving while others run are admitted as a batch slot and memory
+ * free up; their kernels overlap the running ones. A request's results equal those of the
+ * same problem run alone.
+ * --------------------------------------------------------------------------------- */
+typedef struct awg_server awg_server;
+typedef struct {
+    size_t device_bytes;  /* device pool for batches in flight (and resident requests) */
+    int max_inflight;     /* batches on the GPU at once */
+    int max_batch;        /* problems per batch */
+} awg_server_options;
+typedef struct {
+    long long submitted, completed, failed, cells;  /* cells: forward cells of completed */
+    double p50_ms, p99_ms, mean_ms, max_ms;  /* latency, submission to results in place */
+    double span_s;        /* first submission to last completion */
+    double busy_s;        /* time with at least one batch on the GPU */
+    int inflight_max;     /* most batches on the GPU at once */
+} awg_server_stats;
+
+awg_server *awg_server_create(const awg_server_options *opt);  /* NULL: awg_server_last_error */
+void awg_server_destroy(awg_server *s);  /* finishes queued and running requests first */
+/* Queues one problem; its arrays (and out->uniforms) are copied, out's result buffers must
+ * stay valid until the request completes. resident: keep the request's device data after
+ * it completes for awg_server_resample, until awg_server_release (a path must be wanted).
+ * Returns the request id (> 0) or -1 (awg_server_last_error). */
+long long awg_server_submit(awg_server *s, const awg_problem *p, const awg_outputs *out,
+                            int precision, int resident);
+/* Waits up to timeout_ms (< 0: no limit): 1 done (results in place), 0 still pending,
+ * < 0 failed (awg_server_last_error). */
+int awg_server_wait(awg_server *s, long long id, int timeout_ms);
+/* submission, start (admitted to a batch) and completion times (seconds, steady clock) */
+int awg_server_request_times(awg_server *s, long long id, double *times3);
+/* forgets a finished, non-resident request (its id becomes unknown) */
+int awg_server_forget(awg_server *s, long long id);
+int awg_server_stats_get(awg_server *s, awg_server_stats *out);
+/* A new path from a completed resident request: the traceback alone over its resident
+ * forward table with these uniforms (NULL: libc rand(), the reference's order). */
+int awg_server_resample(awg_server *s, long long id, const double *uniforms, int *path);
+int awg_server_release(awg_server *s, long long id);
+const char *awg_server_last_error(void);
 
 /* Bytes of device memory awg_forward_static draws all of its buffers from. */
 #define AWG_STATIC_SCRATCH_BYTES (64ull << 20)

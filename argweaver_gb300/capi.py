@@ -96,7 +96,7 @@ class AwgServerStats(C.Structure):
     _fields_ = [("submitted", C.c_longlong), ("completed", C.c_longlong), ("failed", C.c_longlong),
                 ("cells", C.c_longlong), ("p50_ms", C.c_double), ("p99_ms", C.c_double),
                 ("mean_ms", C.c_double), ("max_ms", C.c_double), ("span_s", C.c_double),
-                ("busy_s", C.c_double), ("inflight_max", C.c_int)]
+                ("busy_s", C.c_double), ("launch_s", C.c_double), ("inflight_max", C.c_int)]
 
 
 # exports of the batch API beyond the reference's (declared in include/argweaver_gb300.h)

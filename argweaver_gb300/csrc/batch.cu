@@ -62,6 +62,11 @@ struct Ctx {
     std::vector<Copy> copies;
     size_t err_off = 0;
     bool timed = false, serial_phases = false;
+    bool graphs = true;  // capture and replay steps (off for one-shot batches: a server's)
+    // Page-locked buffers outgrown while other batches run are kept until the context is
+    // destroyed: cudaFreeHost would wait for the whole device, stalling every batch in flight.
+    bool defer_free = false;
+    std::vector<char *> stale;
     HostPlan plan;
     // the last batch's device view, for draws from its resident forward tables
     BatchDev d{};
@@ -72,6 +77,11 @@ struct Ctx {
 namespace {
 
 std::atomic<long long> g_launches{0};
+
+void drop_host(Ctx &C, char *p) {
+    if (C.defer_free) C.stale.push_back(p);
+    else cudaFreeHost(p);
+}
 
 struct Engine {
     std::mutex mu;
@@ -230,7 +240,7 @@ int ctx_launch(Ctx &C, const awg_problem *probs, awg_outputs *outs, int n, const
                                           (int *)(h + o_cvar)});
     } else {
         if (in_bytes > C.host_cap) {
-            if (C.host) cudaFreeHost(C.host);
+            if (C.host) drop_host(C, C.host);
             C.host = nullptr;
             C.host_cap = 0;
             const size_t cap = in_bytes + in_bytes / 8;
@@ -509,7 +519,7 @@ int ctx_launch(Ctx &C, const awg_problem *probs, awg_outputs *outs, int n, const
     };
 
     if (!special && !serial_timing) {
-        if (E.graphs) {
+        if (E.graphs && C.graphs) {
             // everything a launch depends on: buffers, counts, groups and schedule knobs
             std::vector<long long> sig = {(long long)(uintptr_t)D, (long long)fp32, want_path,
                                           want_post, want_bw, want_bins, plan.ninst, plan.nblocks,
@@ -660,7 +670,7 @@ int ctx_launch(Ctx &C, const awg_problem *probs, awg_outputs *outs, int n, const
     }
     C.err_off = out_slot(4 * sizeof(int));
     if (hout_bytes > C.hout_cap) {
-        if (C.hout) cudaFreeHost(C.hout);
+        if (C.hout) drop_host(C, C.hout);
         C.hout = nullptr;
         C.hout_cap = 0;
         const size_t cap = std::max(hout_bytes + hout_bytes / 8, (size_t)256);
@@ -716,7 +726,30 @@ int ctx_complete(Ctx &C, std::string &err) {
     return 0;
 }
 
-Ctx *ctx_create() { return new Ctx(); }
+Ctx *ctx_create() {
+    Ctx *C = new Ctx();
+    C->graphs = false;      // a server's batches rarely repeat a shape
+    C->defer_free = true;   // and other batches are in flight when its staging grows
+    return C;
+}
+
+int ctx_reserve_host(Ctx *C, size_t in_bytes, size_t out_bytes) {
+    if (in_bytes > C->host_cap) {
+        if (C->host) drop_host(*C, C->host);
+        C->host = nullptr;
+        C->host_cap = 0;
+        if (cudaMallocHost(&C->host, in_bytes) != cudaSuccess) return -3;
+        C->host_cap = in_bytes;
+    }
+    if (out_bytes > C->hout_cap) {
+        if (C->hout) drop_host(*C, C->hout);
+        C->hout = nullptr;
+        C->hout_cap = 0;
+        if (cudaMallocHost(&C->hout, out_bytes) != cudaSuccess) return -3;
+        C->hout_cap = out_bytes;
+    }
+    return 0;
+}
 
 void ctx_destroy(Ctx *C) {
     if (!C) return;
@@ -733,6 +766,7 @@ void ctx_destroy(Ctx *C) {
     if (C->dev) cudaFree(C->dev);
     if (C->host) cudaFreeHost(C->host);
     if (C->hout) cudaFreeHost(C->hout);
+    for (char *p : C->stale) cudaFreeHost(p);
     delete C;
 }
 
@@ -809,7 +843,7 @@ int ctx_resample(Ctx *C, const double *const *uniforms, int *const *paths, std::
         off += (bytes + 15) & ~(size_t)15;
     }
     if (off > C->hout_cap) {
-        if (C->hout) cudaFreeHost(C->hout);
+        if (C->hout) drop_host(*C, C->hout);
         C->hout = nullptr;
         C->hout_cap = 0;
         CK(cudaMallocHost(&C->hout, off + off / 8));

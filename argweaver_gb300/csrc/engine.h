@@ -47,6 +47,8 @@ struct Ctx;
 Ctx *ctx_create();
 void ctx_destroy(Ctx *C);
 void ctx_set_region(Ctx *C, char *dev, size_t bytes);
+// Page-locked input and output staging of at least these sizes, allocated now.
+int ctx_reserve_host(Ctx *C, size_t in_bytes, size_t out_bytes);
 int ctx_launch_async(Ctx *C, const awg_problem *probs, awg_outputs *outs, int n, int precision,
                      std::string &err);
 bool ctx_ready(Ctx *C);  // the launched batch's outputs have arrived

@@ -96,12 +96,17 @@ int count_states(const int *parent, const int *age, int n, int T, bool internal,
     return (int)S;
 }
 
+thread_local int g_plan_threads = 0;
+void set_plan_threads(int n) { g_plan_threads = std::max(0, n); }
+
 namespace {
 
-// Runs f(q) for q < n on up to hardware_concurrency threads, problems interleaved.
+// Runs f(q) for q < n on up to hardware_concurrency threads (or the calling thread's cap),
+// problems interleaved.
 template <typename Fn>
 void parallel_for(int n, Fn f) {
-    const int nthreads = std::max(1, std::min<int>(n, (int)std::thread::hardware_concurrency()));
+    const int hw = g_plan_threads > 0 ? g_plan_threads : (int)std::thread::hardware_concurrency();
+    const int nthreads = std::max(1, std::min<int>(n, hw));
     if (nthreads <= 1 || n < 4) {
         for (int q = 0; q < n; q++) f(q);
         return;

@@ -48,6 +48,10 @@ void plan_fill(const awg_problem *probs, int n, HostPlan &plan, const PlanDst &d
 // Both, into the plan's own vectors; returns false with a message on bad input.
 bool build_plan(const awg_problem *probs, int n, HostPlan &plan, std::string &err);
 
+// Threads the calling thread's planning may use (0: all hardware threads); callers that
+// plan several batches at once share the cores this way.
+void set_plan_threads(int n);
+
 // Number of states of a local tree given by parent/age arrays (states.cpp:53-199).
 int count_states(const int *parent, const int *age, int n, int T, bool internal, int minage,
                  int root_child0, int *M_out);

@@ -2,10 +2,12 @@
 // reference, whose arg-sample threads one sequence at a time on the CPU).
 //
 // Requests arrive through awg_server_submit from any thread and wait in a FIFO queue. A
-// worker thread forms batches ("waves") from the queue head — requests of one precision and
-// one set of wanted outputs, as many as fit the free device memory and max_batch — and
+// worker thread forms batches ("waves") led by the oldest request — with it, queued requests
+// of one precision, one set of wanted outputs and a like number of columns (a batch lasts as
+// long as its longest chain), as many as fit the free device memory and max_batch — and
 // launches each on an execution context of its own (streams, staging, a region of the
-// server's device pool). Up to max_inflight waves are on the GPU at once, so requests that
+// server's device pool) and a thread of its own that plans, launches and completes it. Up
+// to max_inflight waves are on the GPU at once, so requests that
 // arrive while others run are admitted as soon as a context and memory free up and their
 // kernels overlap on the device with the running ones. Device memory is one pool allocated
 // at creation and handed out first-fit, so serving never calls cudaMalloc or cudaFree.
@@ -34,6 +36,7 @@
 
 #include "argweaver_gb300.h"
 #include "engine.h"
+#include "plan.h"
 
 namespace {
 
@@ -59,12 +62,17 @@ struct Req {
     int slot = -1;  // resident and done: the slot holding its data
 };
 
+// A batch slot: an execution context and the thread that plans, launches and completes the
+// batches assigned to it, so host-side planning of different batches runs in parallel.
 struct Slot {
+    enum State { IDLE, ASSIGNED, HELD };
     awg::Ctx *ctx = nullptr;
     std::vector<Req *> reqs;
     size_t off = 0, bytes = 0;  // pool region
-    bool busy = false;          // a wave in flight
-    bool held = false;          // keeps a resident request's data
+    State state = IDLE;         // ASSIGNED: a batch being launched or on the GPU; HELD: keeps
+                                // a resident request's data
+    std::thread th;
+    std::condition_variable cv;
 };
 
 // First-fit allocator over the device pool, in 256-byte units.
@@ -118,7 +126,8 @@ struct awg_server {
     awg_server_options opt{};
     char *pool_dev = nullptr;
     Pool pool;
-    std::vector<Slot> slots;
+    std::vector<std::unique_ptr<Slot>> slots;
+    bool stop_slots = false;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
     std::deque<Req *> queue;
@@ -132,6 +141,7 @@ struct awg_server {
     double t_first = -1.0, t_last = 0.0;
     int inflight = 0, inflight_max = 0;
     double busy_since = -1.0, busy_s = 0.0;  // time with at least one wave on the GPU
+    double launch_s = 0.0;                   // worker time spent planning and launching
     std::string create_err;
 };
 
@@ -146,53 +156,72 @@ void note_busy(awg_server *S, int delta, double t) {
     if (S->inflight == 0 && delta < 0 && S->busy_since >= 0) S->busy_s += t - S->busy_since;
 }
 
-// The worker: completes finished waves, admits new ones, sleeps when there is nothing to do.
-void serve(awg_server *S) {
-    int dev = 0;
-    cudaGetDevice(&dev);
+// A slot's thread: launches each batch assigned to it, waits for it on its own streams,
+// hands the results over and frees the slot (or holds it for a resident request).
+void slot_main(awg_server *S, int si) {
+    Slot &sl = *S->slots[si];
+    // the host's cores shared among the slots planning batches at once
+    const int hw = (int)std::thread::hardware_concurrency();
+    awg::set_plan_threads(std::max(2, hw / std::max(1, (int)S->slots.size() / 2)));
     std::unique_lock<std::mutex> lk(S->mu);
     for (;;) {
-        bool progressed = false;
-        // ---- finished waves
-        for (size_t si = 0; si < S->slots.size(); si++) {
-            Slot &sl = S->slots[si];
-            if (!sl.busy || !awg::ctx_ready(sl.ctx)) continue;
-            std::string err;
-            lk.unlock();
-            const int rc = awg::ctx_finish(sl.ctx, err);
-            lk.lock();
-            const double t = now_s();
-            for (Req *r : sl.reqs) {
-                r->t_done = t;
-                if (rc == 0) {
-                    r->status = 1;
-                    S->completed++;
-                    S->cells_done += r->cells;
-                    S->lat_ms.push_back(1e3 * (r->t_done - r->t_submit));
-                } else {
-                    r->status = rc;
-                    r->err = err;
-                    S->failed++;
-                }
-            }
-            S->t_last = t;
-            sl.busy = false;
-            note_busy(S, -1, t);
-            if (rc == 0 && sl.reqs.size() == 1 && sl.reqs[0]->resident) {
-                sl.held = true;
-                sl.reqs[0]->slot = (int)si;
-            } else {
-                S->pool.release(sl.off, sl.bytes);
-                sl.reqs.clear();
-            }
-            progressed = true;
-            S->cv_done.notify_all();
+        sl.cv.wait(lk, [&] { return sl.state == Slot::ASSIGNED || S->stop_slots; });
+        if (sl.state != Slot::ASSIGNED) break;
+        const std::vector<Req *> wave = sl.reqs;
+        std::vector<awg_problem> probs(wave.size());
+        std::vector<awg_outputs> outs(wave.size());
+        for (size_t q = 0; q < wave.size(); q++) {
+            probs[q] = wave[q]->p;
+            outs[q] = wave[q]->out;
         }
-        // ---- admission: waves from the queue head while a context and memory are free
+        const int precision = wave[0]->precision;
+        lk.unlock();
+        std::string err;
+        const double t0 = now_s();
+        int rc = awg::ctx_launch_async(sl.ctx, probs.data(), outs.data(), (int)wave.size(),
+                                       precision, err);
+        const double t1 = now_s();
+        if (rc == 0) rc = awg::ctx_finish(sl.ctx, err);
+        else awg::ctx_sync(sl.ctx);  // whatever of the batch was enqueued has finished
+        lk.lock();
+        const double t = now_s();
+        S->launch_s += t1 - t0;
+        for (Req *r : wave) {
+            r->t_done = t;
+            if (rc == 0) {
+                r->status = 1;
+                S->completed++;
+                S->cells_done += r->cells;
+                S->lat_ms.push_back(1e3 * (r->t_done - r->t_submit));
+            } else {
+                r->status = rc;
+                r->err = err;
+                S->failed++;
+            }
+        }
+        S->t_last = t;
+        note_busy(S, -1, t);
+        if (rc == 0 && wave.size() == 1 && wave[0]->resident) {
+            sl.state = Slot::HELD;
+            wave[0]->slot = si;
+        } else {
+            S->pool.release(sl.off, sl.bytes);
+            sl.reqs.clear();
+            sl.state = Slot::IDLE;
+        }
+        S->cv_done.notify_all();
+        S->cv_work.notify_one();
+    }
+}
+
+// The admitter: forms batches from the queue and assigns them to idle slots.
+void serve(awg_server *S) {
+    std::unique_lock<std::mutex> lk(S->mu);
+    for (;;) {
         while (!S->queue.empty()) {
             int free_slot = -1;
             for (size_t si = 0; si < S->slots.size(); si++)
-                if (!S->slots[si].busy && !S->slots[si].held) {
+                if (S->slots[si]->state == Slot::IDLE) {
                     free_slot = (int)si;
                     break;
                 }
@@ -206,68 +235,51 @@ void serve(awg_server *S) {
                              std::to_string(S->pool.cap);
                 S->failed++;
                 S->cv_done.notify_all();
-                progressed = true;
                 continue;
             }
+            // the oldest request, then queued requests of like length: a batch lasts as long
+            // as its longest chain of columns, so short requests ride with short ones and
+            // are not held back by long ones (length within a factor of two of the head's)
             const size_t avail = S->pool.largest();
             std::vector<Req *> wave;
+            std::vector<size_t> taken;
             size_t bytes = 0;
-            for (Req *r : S->queue) {
+            const long long L0 = first->p.seqlen;
+            for (size_t qi = 0; qi < S->queue.size(); qi++) {
+                Req *r = S->queue[qi];
                 if ((int)wave.size() >= S->opt.max_batch) break;
-                if (!wave.empty() &&
-                    (r->resident || first->resident || r->precision != first->precision ||
-                     r->want_path != first->want_path || r->want_post != first->want_post))
-                    break;
-                if (bytes + (size_t)r->bytes > avail) break;
+                if (!wave.empty()) {
+                    if (first->resident) break;
+                    if (r->resident || r->precision != first->precision ||
+                        r->want_path != first->want_path || r->want_post != first->want_post)
+                        continue;
+                    if (2LL * r->p.seqlen < L0 || r->p.seqlen > 2LL * L0) continue;
+                }
+                if (bytes + (size_t)r->bytes > avail) {
+                    if (wave.empty()) break;
+                    continue;
+                }
                 wave.push_back(r);
+                taken.push_back(qi);
                 bytes += (size_t)r->bytes;
             }
             if (wave.empty()) break;  // the head waits for memory to free up
-            Slot &sl = S->slots[free_slot];
+            Slot &sl = *S->slots[free_slot];
             if (!S->pool.alloc(bytes, sl.off)) break;
-            for (size_t q = 0; q < wave.size(); q++) S->queue.pop_front();
+            for (size_t q = taken.size(); q-- > 0;) S->queue.erase(S->queue.begin() + taken[q]);
             sl.bytes = bytes;
             sl.reqs = wave;
-            sl.busy = true;
+            sl.state = Slot::ASSIGNED;
             const double t = now_s();
             for (Req *r : wave) r->t_start = t;
             note_busy(S, +1, t);
             awg::ctx_set_region(sl.ctx, S->pool_dev + sl.off, bytes);
-            std::vector<awg_problem> probs(wave.size());
-            std::vector<awg_outputs> outs(wave.size());
-            for (size_t q = 0; q < wave.size(); q++) {
-                probs[q] = wave[q]->p;
-                outs[q] = wave[q]->out;
-            }
-            std::string err;
-            lk.unlock();
-            const int rc = awg::ctx_launch_async(sl.ctx, probs.data(), outs.data(), (int)wave.size(),
-                                                 first->precision, err);
-            lk.lock();
-            if (rc != 0) {
-                awg::ctx_sync(sl.ctx);  // whatever of the wave was enqueued has finished
-                for (Req *r : wave) {
-                    r->status = rc;
-                    r->err = err;
-                    S->failed++;
-                }
-                sl.busy = false;
-                note_busy(S, -1, now_s());
-                S->pool.release(sl.off, sl.bytes);
-                sl.reqs.clear();
-                S->cv_done.notify_all();
-            }
-            progressed = true;
+            sl.cv.notify_one();
         }
         bool any_busy = false;
-        for (const Slot &sl : S->slots) any_busy |= sl.busy;
+        for (const auto &sl : S->slots) any_busy |= sl->state == Slot::ASSIGNED;
         if (S->stop && S->queue.empty() && !any_busy) break;
-        if (!progressed) {
-            if (any_busy)
-                S->cv_work.wait_for(lk, std::chrono::microseconds(50));
-            else
-                S->cv_work.wait(lk);
-        }
+        S->cv_work.wait(lk);
     }
 }
 
@@ -300,9 +312,22 @@ awg_server *awg_server_create(const awg_server_options *opt) {
         return nullptr;
     }
     S->pool.init(opt->device_bytes);
-    S->slots.resize(opt->max_inflight);
-    for (Slot &sl : S->slots) sl.ctx = awg::ctx_create();
     awg_server *raw = S.get();
+    // each slot's page-locked staging, sized up front from its share of the pool (inputs
+    // and downloaded outputs are a small part of a batch's device footprint)
+    const size_t stage = std::min<size_t>(
+        256 << 20, std::max<size_t>(64 << 20, opt->device_bytes / opt->max_inflight / 32));
+    for (int i = 0; i < opt->max_inflight; i++) {
+        S->slots.emplace_back(new Slot());
+        S->slots.back()->ctx = awg::ctx_create();
+        if (awg::ctx_reserve_host(S->slots.back()->ctx, stage, stage / 2) != 0) {
+            g_srv_err = "awg_server_create: page-locked staging";
+            for (auto &sl : S->slots) awg::ctx_destroy(sl->ctx);
+            cudaFree(S->pool_dev);
+            return nullptr;
+        }
+    }
+    for (int i = 0; i < opt->max_inflight; i++) S->slots[i]->th = std::thread(slot_main, raw, i);
     S->worker = std::thread(serve, raw);
     return S.release();
 }
@@ -315,7 +340,15 @@ void awg_server_destroy(awg_server *S) {
     }
     S->cv_work.notify_all();
     if (S->worker.joinable()) S->worker.join();
-    for (Slot &sl : S->slots) awg::ctx_destroy(sl.ctx);
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        S->stop_slots = true;
+        for (auto &sl : S->slots) sl->cv.notify_all();
+    }
+    for (auto &sl : S->slots) {
+        if (sl->th.joinable()) sl->th.join();
+        awg::ctx_destroy(sl->ctx);
+    }
     if (S->pool_dev) cudaFree(S->pool_dev);
     delete S;
 }
@@ -332,6 +365,7 @@ long long awg_server_submit(awg_server *S, const awg_problem *p, const awg_outpu
         return -1;
     }
     std::unique_ptr<Req> r(new Req());
+    r->t_submit = now_s();  // latency counts this call's copying and sizing too
     const size_t tn = (size_t)p->ntrees * p->nnodes;
     copy_arr(r->ptrees, p->ptrees, tn);
     copy_arr(r->ages, p->ages, tn);
@@ -383,8 +417,7 @@ long long awg_server_submit(awg_server *S, const awg_problem *p, const awg_outpu
     }
     std::lock_guard<std::mutex> lk(S->mu);
     r->id = S->next_id++;
-    r->t_submit = now_s();
-    if (S->t_first < 0) S->t_first = r->t_submit;
+    if (S->t_first < 0 || r->t_submit < S->t_first) S->t_first = r->t_submit;
     S->submitted++;
     const long long id = r->id;
     S->queue.push_back(r.get());
@@ -442,6 +475,7 @@ int awg_server_stats_get(awg_server *S, awg_server_stats *out) {
     out->inflight_max = S->inflight_max;
     out->busy_s = S->busy_s + (S->inflight > 0 && S->busy_since >= 0 ? now_s() - S->busy_since : 0.0);
     out->span_s = S->t_first >= 0 ? S->t_last - S->t_first : 0.0;
+    out->launch_s = S->launch_s;
     if (!S->lat_ms.empty()) {
         std::vector<double> v = S->lat_ms;
         std::sort(v.begin(), v.end());
@@ -471,7 +505,7 @@ int awg_server_resample(awg_server *S, long long id, const double *uniforms, int
             g_srv_err = "awg_server_resample: not a completed resident request";
             return -1;
         }
-        sl = &S->slots[it->second->slot];
+        sl = S->slots[it->second->slot].get();
     }
     // the slot is held: the worker does not touch its context until it is released
     std::string err;
@@ -486,10 +520,10 @@ int awg_server_release(awg_server *S, long long id) {
     std::lock_guard<std::mutex> lk(S->mu);
     auto it = S->reqs.find(id);
     if (it == S->reqs.end() || it->second->slot < 0) return -1;
-    Slot &sl = S->slots[it->second->slot];
+    Slot &sl = *S->slots[it->second->slot];
     S->pool.release(sl.off, sl.bytes);
     sl.reqs.clear();
-    sl.held = false;
+    sl.state = Slot::IDLE;
     it->second->slot = -1;
     S->cv_work.notify_one();
     return 0;

@@ -90,3 +90,46 @@ def simulate(nleaves: int, seqlen: int, seed: int, *, compress: int = 10, ntimes
     finally:
         lib.awg_sim_free(r)
     return prob
+
+
+def leaf_cut(p: Problem) -> Problem:
+    """The internal-branch form of an external threading problem: the threaded haplotype
+    becomes leaf k of a (k+1)-leaf tree whose root is the virtual root of a cut
+    (age ntimes+1), with child[0] the cut subtree (the single leaf k) and child[1] the main
+    tree, the layout remove_arg_thread_path leaves for a removed leaf (thread.cpp:1481,
+    states.cpp:109-167). Nodes are renumbered leaves first (main leaves 0..k-1, leaf k, the
+    main tree's internal nodes, the virtual root last); SPRs and node maps follow."""
+    k = (p.nnodes + 1) // 2            # leaves of the main trees
+    n2 = p.nnodes + 2
+    T = p.ntimes
+    remap = np.arange(p.nnodes + 1, dtype=np.int64)
+    remap[k:p.nnodes] = np.arange(k, p.nnodes) + 1
+    vroot, leaf = n2 - 1, k
+
+    def rm(v):
+        return np.where(v >= 0, remap[np.maximum(v, 0)], -1)
+
+    B = p.ntrees
+    ptrees = np.empty((B, n2), dtype=np.int32)
+    ages = np.empty((B, n2), dtype=np.int32)
+    for b in range(B):
+        par = p.ptrees[b]
+        newp = rm(par)
+        newp[par == -1] = vroot
+        ptrees[b, remap[:p.nnodes]] = newp
+        ages[b, remap[:p.nnodes]] = p.ages[b]
+        ptrees[b, leaf], ages[b, leaf] = vroot, 0
+        ptrees[b, vroot], ages[b, vroot] = -1, T + 1
+    sprs = p.sprs.copy()
+    sprs[:, 0] = rm(sprs[:, 0])
+    sprs[:, 2] = rm(sprs[:, 2])
+    mapping = None
+    if p.mapping is not None:
+        mapping = np.empty((B, n2), dtype=np.int32)
+        for b in range(B):
+            mapping[b, remap[:p.nnodes]] = rm(p.mapping[b])
+            mapping[b, leaf], mapping[b, vroot] = leaf, vroot
+    return Problem(times=p.times, popsizes=p.popsizes, rho=p.rho, mu=p.mu, ptrees=ptrees,
+                   ages=ages, sprs=sprs, blocklens=p.blocklens.copy(), seqs=p.seqs.copy(),
+                   internal=True, mapping=mapping,
+                   root_child0=np.full(B, leaf, dtype=np.int32))

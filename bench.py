@@ -50,6 +50,9 @@ def parse():
     ap.add_argument("--instances", type=int, default=256)
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--cpu-sample-seconds", type=float, default=15.0)
+    ap.add_argument("--configs", type=int, default=1,
+                    help="also measure the single-instance, large-instance, internal-batch "
+                         "and serving configurations (0: skip)")
     ap.add_argument("--max-columns", type=int, default=0,
                     help="cap each problem's length (small cases for profiling)")
     return ap.parse_args()
@@ -144,6 +147,185 @@ def cpu_reference(problems, seconds: float, threads: int):
         list(ex.map(work, order))
     dt = time.perf_counter() - t0
     return done_cells[0] / dt, done_cells[0], dt
+
+
+def _sim_pool(specs):
+    """Problems simulated in parallel from (nleaves, columns, seed, ntimes, missing) specs."""
+    from argweaver_gb300.sim import simulate
+
+    def one(spec):
+        nl, L, sd, T, miss = spec
+        return simulate(nl, L, sd, compress=10, ntimes=T, maxtime=200e3, popsize=1e4,
+                        rho=1.6e-8, mu=1.8e-8, missing=miss)
+
+    with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        return list(ex.map(one, specs))
+
+
+def _prefix(p, columns):
+    """The problem cut to its first `columns` columns (whole trees, the last one shortened)."""
+    from argweaver_gb300.problem import Problem
+
+    ends = np.cumsum(p.blocklens)
+    B = int(np.searchsorted(ends, columns) + 1)
+    bl = p.blocklens[:B].copy()
+    bl[-1] -= int(ends[B - 1] - columns) if ends[B - 1] > columns else 0
+    L = int(bl.sum())
+    return Problem(times=p.times, popsizes=p.popsizes, rho=p.rho, mu=p.mu,
+                   ptrees=p.ptrees[:B].copy(), ages=p.ages[:B].copy(), sprs=p.sprs[:B].copy(),
+                   blocklens=bl, seqs=p.seqs[:, :L].copy(), internal=p.internal,
+                   mapping=None if p.mapping is None else p.mapping[:B].copy(),
+                   root_child0=None if p.root_child0 is None else p.root_child0[:B].copy())
+
+
+def config_runs(seed: int):
+    """The other configurations of the benchmark spec, each measured once with a bounded workload:
+    c0 the plain FP64 single instance, c2 one large instance in FP32 and FP64, c3 the
+    internal-branch batch under the autotuned schedule and graph replay, c4 the serving
+    loop under Poisson arrivals."""
+    from argweaver_gb300 import api, refapi
+    from argweaver_gb300.server import Server
+    from argweaver_gb300.sim import leaf_cut
+
+    out = {}
+    rng = np.random.default_rng(seed + 17)
+
+    # ---- c0: k = 8 (7 leaves + the threaded haplotype), 100 kb = 10,000 columns, FP64
+    p0 = _sim_pool([(7, 10000, int(rng.integers(1, 2**62)), 20, 0.0)])[0]
+    refapi.arghmm_sample_posterior(p0)
+    lat = []
+    for _ in range(20):
+        t0 = time.perf_counter()
+        refapi.arghmm_sample_posterior(p0)
+        lat.append(1e3 * (time.perf_counter() - t0))
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    t0 = time.perf_counter()
+    fw, _ = pyoracle.forward(p0)
+    pyoracle.traceback(p0, fw, np.random.default_rng(1).random(p0.seqlen))
+    cpu_ms = 1e3 * (time.perf_counter() - t0)
+    out["c0_plain_fp64_single"] = {
+        "workload": "k=8 (7 + 1 threaded), 10,000 columns, ntimes=20, FP64, one "
+                    "arghmm_sample_posterior call (reference C ABI)",
+        "cells": int(p0.cells()), "p50_ms": float(np.percentile(lat, 50)),
+        "p99_ms": float(np.percentile(lat, 99)),
+        "cells_per_s": p0.cells() / (np.median(lat) / 1e3),
+        "cpu_port_1core_ms": cpu_ms}
+
+    # ---- c2: k = 100, 10 Mb = 1e6 columns, FP32 and FP64 forward + traceback
+    p2 = _sim_pool([(99, 1000000, int(rng.integers(1, 2**62)), 20, 0.0)])[0]
+    c2 = {"workload": "k=100 (99 + 1 threaded), 1e6 columns (10 Mb at 10 bp), ntimes=20",
+          "cells": int(p2.cells()), "trees": int(p2.ntrees),
+          "max_states": int(p2.nstates_per_tree().max())}
+    u2 = np.random.default_rng(2).random(p2.seqlen)
+    for prec in ("fp32", "fp64"):
+        api.set_timing(1)
+        api.run_batch([p2], precision=prec, want_forward=False, want_path=True, uniforms=[u2])
+        t0 = time.perf_counter()
+        api.run_batch([p2], precision=prec, want_forward=False, want_path=True, uniforms=[u2])
+        wall = time.perf_counter() - t0
+        dev = api.last_timings()["compute"] / 1e3
+        api.set_timing(0)
+        c2[prec] = {"value": p2.cells() / dev, "e2e": p2.cells() / wall,
+                    "ms": 1e3 * dev, "e2e_ms": 1e3 * wall}
+    c2["fp32_speedup_over_fp64"] = c2["fp32"]["value"] / c2["fp64"]["value"]
+    q2 = _prefix(p2, 50000)
+    a = api.run_batch([q2], precision="fp32", want_forward=False, want_posterior=True)[0]
+    b = api.run_batch([q2], precision="fp64", want_forward=False, want_posterior=True)[0]
+    c2["fp32_vs_fp64_posterior_max_abs_err"] = float(np.max(np.abs(a.posterior - b.posterior)))
+    c2["error_sample"] = "the instance's first 50,000 columns"
+    out["c2_large_single"] = c2
+    del p2, a, b
+
+    # ---- c3: 128 internal-branch instances, k = 50, 2 Mb = 2e5 columns, missing ~U[0,2%]
+    specs = [(49, 200000, int(rng.integers(1, 2**62)), 20, float(rng.uniform(0, 0.02)))
+             for _ in range(128)]
+    p3 = [leaf_cut(p) for p in _sim_pool(specs)]
+    cells3 = sum(p.cells() for p in p3)
+    u3 = [np.random.default_rng(300 + i).random(p.seqlen) for i, p in enumerate(p3)]
+    sched3 = api.autotune(p3, precision="fp32", want_path=True, trials=1)
+    api.set_timing(1)
+    for _ in range(2):
+        api.run_batch(p3, precision="fp32", want_forward=False, want_path=True, uniforms=u3)
+    g0 = api.graph_counts()
+    dev3, wall3 = [], []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        api.run_batch(p3, precision="fp32", want_forward=False, want_path=True, uniforms=u3)
+        wall3.append(time.perf_counter() - t0)
+        dev3.append(api.last_timings()["compute"] / 1e3)
+    api.set_timing(0)
+    out["c3_internal_batch"] = {
+        "workload": "128 internal-branch threading problems, k=50, 2e5 columns (2 Mb), "
+                    "ntimes=20, missing ~U[0,2%], FP32 forward + traceback; the cut subtree is "
+                    "a single leaf (the threaded haplotype) of each seeded ARG",
+        "cells_per_step": int(cells3), "value": cells3 / float(np.mean(dev3)),
+        "e2e": cells3 / float(np.mean(wall3)), "ms_per_step": 1e3 * float(np.mean(dev3)),
+        "schedule": sched3,
+        "graph_replays": api.graph_counts()["replays"] - g0["replays"]}
+    del p3
+
+    # ---- c4: serving. Requests drawn from config 4's distribution (k log-U[8,200],
+    # 50 kb - 5 Mb log-uniform, ntimes in {16, 20, 32}), pre-simulated (off the clock), a
+    # pool of distinct ARGs reused with fresh uniforms; Poisson arrivals
+    npool = 160
+    specs = []
+    for _ in range(npool):
+        k = int(np.exp(rng.uniform(np.log(8), np.log(200))))
+        L = int(np.exp(rng.uniform(np.log(5e3), np.log(5e5))))
+        T = int(rng.choice([16, 20, 32]))
+        specs.append((k - 1, L, int(rng.integers(1, 2**62)), T, 0.005))
+    pool = _sim_pool(specs)
+    rate, duration = 40.0, 10.0
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=int(rate * duration * 1.5)))
+    arrivals = arrivals[arrivals < duration]
+    picks = rng.integers(0, npool, size=arrivals.size)
+    unis = {}
+    for q, j in enumerate(picks):
+        unis[q] = np.random.default_rng(1000 + q).random(pool[j].seqlen)
+    with Server(device_bytes=128 << 30, max_inflight=24, max_batch=32) as srv, \
+            cf.ThreadPoolExecutor(max_workers=8) as clients:
+        # clients submit at the arrival times (each call copies and sizes its request)
+        t_start = time.perf_counter()
+        futs = []
+        for q, (t_arr, j) in enumerate(zip(arrivals, picks)):
+            delay = t_start + t_arr - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            futs.append(clients.submit(srv.submit, pool[j], precision="fp32", uniforms=unis[q]))
+        for f in futs:
+            srv.wait(f.result())
+        st = srv.stats()
+    served_cells = sum(pool[j].cells() for j in picks)
+    # the plain FP64 per-request path: one arghmm_sample_posterior call per request, no
+    # batching, on requests drawn from the same pool (bounded to ~10 s)
+    lat64, c64, t64 = [], 0, 0.0
+    for j in rng.permutation(npool):
+        t0 = time.perf_counter()
+        refapi.arghmm_sample_posterior(pool[j])
+        dt = time.perf_counter() - t0
+        lat64.append(1e3 * dt)
+        c64 += pool[j].cells()
+        t64 += dt
+        if t64 > 6.0:
+            break
+    out["c4_serving"] = {
+        "workload": f"Poisson arrivals at {rate:g} requests/s for {duration:g} s "
+                    f"({arrivals.size} requests) drawn from {npool} pre-simulated ARGs: "
+                    "k log-U[8,200], 5e3-5e5 columns log-uniform, ntimes in {16,20,32}, FP32 "
+                    "forward + traceback per request",
+        "requests": int(st["completed"]), "failed": int(st["failed"]),
+        "throughput": st["cells"] / st["span_s"] if st["span_s"] > 0 else None,
+        "unit": UNIT, "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "max_ms": st["max_ms"],
+        "mean_cells_per_request": served_cells / max(1, arrivals.size),
+        "batches_in_flight_max": int(st["inflight_max"]),
+        "fp64_plain_per_request": {"requests": len(lat64),
+                                   "p50_ms": float(np.percentile(lat64, 50)),
+                                   "p99_ms": float(np.percentile(lat64, 99)),
+                                   "throughput": c64 / t64,
+                                   "sample": "requests of the same pool, one "
+                                             "arghmm_sample_posterior call each, ~6 s"}}
+    return out
 
 
 def peaks():
@@ -281,6 +463,12 @@ def main():
 
     if rank != 0:
         return
+    configs = None
+    if args.configs:
+        try:
+            configs = config_runs(args.seed)
+        except Exception as e:  # the headline line is printed regardless
+            configs = {"error": f"{type(e).__name__}: {e}"}
     hbm, src = peaks()
     # dominant kernel: the forward pass, 4 B of FP32 table written per cell
     achieved = cells * 4 / (phase_ms["forward"] / 1e3) / 1e9
@@ -326,6 +514,8 @@ def main():
         "phase_ms": phase_ms,
         "longest_instance_columns": max(p.seqlen for p in problems),
     }
+    if configs is not None:
+        line["other_configs"] = configs
     print(json.dumps(line))
 
 

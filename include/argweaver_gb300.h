@@ -193,6 +193,7 @@ typedef struct {
     double p50_ms, p99_ms, mean_ms, max_ms;  /* latency, submission to results in place */
     double span_s;        /* first submission to last completion */
     double busy_s;        /* time with at least one batch on the GPU */
+    double launch_s;      /* server thread time spent planning and launching batches */
     int inflight_max;     /* most batches on the GPU at once */
 } awg_server_stats;
 

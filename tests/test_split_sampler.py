@@ -51,3 +51,18 @@ def test_decomposed_draw_path_is_a_valid_path_on_real_tables():
     u = np.random.default_rng(2).random(p.seqlen)
     path = pyoracle.traceback_split(p, fw, u)
     assert all(post[off[i] + path[i]] > 0 for i in range(p.seqlen))
+
+
+def test_leaf_cut_is_the_external_problem_in_internal_form():
+    # a single-leaf subtree cut: the internal-branch HMM over the main tree equals the
+    # external threading HMM of that leaf (same states, same likelihood)
+    from argweaver_gb300.sim import leaf_cut
+
+    p = simulate(12, 800, seed=9, missing=0.01)
+    q = leaf_cut(p)
+    assert q.internal and q.nnodes == p.nnodes + 2
+    fe, le = pyoracle.forward(p)
+    fi, li = pyoracle.forward(q)
+    assert fi.shape == fe.shape
+    assert abs(li - le) <= 1e-12 * abs(le)
+    np.testing.assert_allclose(fi, fe, rtol=1e-12, atol=0)

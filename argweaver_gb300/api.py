@@ -175,6 +175,11 @@ def autotune(problems: Sequence[Problem], *, precision: str = "fp32", want_path:
     return out
 
 
+def release_memory() -> None:
+    """Free the engine's device arena and staging (awg_release_memory)."""
+    capi.load().awg_release_memory()
+
+
 def set_graphs(on: bool) -> None:
     capi.load().awg_set_graphs(int(bool(on)))
 

@@ -116,6 +116,7 @@ PROTOTYPES += [
                                C.c_int, C.c_char_p, C.c_int]),
     ("awg_batch_device_bytes", C.c_longlong, [C.POINTER(AwgProblem), C.c_int, C.c_int, C.c_int,
                                               C.c_int]),
+    ("awg_release_memory", C.c_int, []),
     ("awg_set_graphs", None, [C.c_int]),
     ("awg_set_schedule", None, [C.c_int, C.c_int, C.c_int, C.c_int]),
     ("awg_graph_replays", C.c_longlong, []),

@@ -936,6 +936,29 @@ int autotune(const awg_problem *probs, awg_outputs *outs, int n, int precision, 
 
 extern "C" {
 
+// Frees the engine's device arena, page-locked staging and captured graph (the next batch
+// allocates again); returns 0.
+int awg_release_memory(void) {
+    awg::Engine &E = awg::engine();
+    std::lock_guard<std::mutex> lock(E.mu);
+    awg::Ctx &C = E.ctx;
+    if (C.init) cudaStreamSynchronize(C.stream);
+    if (C.gexec) cudaGraphExecDestroy(C.gexec);
+    C.gexec = nullptr;
+    C.gsig.clear();
+    if (C.dev) cudaFree(C.dev);
+    C.dev = nullptr;
+    C.dev_cap = 0;
+    if (C.host) cudaFreeHost(C.host);
+    C.host = nullptr;
+    C.host_cap = 0;
+    if (C.hout) cudaFreeHost(C.hout);
+    C.hout = nullptr;
+    C.hout_cap = 0;
+    C.have_d = false;
+    return 0;
+}
+
 // Whether steps are captured as CUDA graphs and replayed (1, the default) or launched
 // kernel by kernel (0); and how many steps were replayed / captured so far.
 void awg_set_graphs(int on) { awg::engine().graphs = on != 0; }

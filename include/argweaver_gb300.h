@@ -160,6 +160,10 @@ long long awg_batch_device_bytes(const awg_problem *problems, int n, int precisi
 int awg_autotune(const awg_problem *problems, awg_outputs *outputs, int n, int precision,
                  int trials, char *report, int report_len);
 
+/* Frees the batch engine's grow-only device arena, its page-locked staging and captured
+ * graph (the next awg_run_batch allocates again). Returns 0. */
+int awg_release_memory(void);
+
 /* CUDA graphs (no counterpart in the reference): awg_run_batch captures the device part of
  * a step (kernels, memsets, cross-stream dependencies) once and replays it while a batch
  * has the same launch parameters (sizes, buffers, schedule); on by default. */

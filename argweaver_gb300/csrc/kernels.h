@@ -26,6 +26,18 @@ void launch_traceback(const BatchDev &d, bool fp32, cudaStream_t s);
 // K5: backward pass fused with the posterior marginals, one CTA per instance.
 void launch_backward(const BatchDev &d, bool fp32, double *bw_out, cudaStream_t s);
 
+// Asks for the largest shared-memory carveout for a kernel (once per kernel): the default
+// carveout can leave room for fewer CTAs per SM than the registers and threads allow.
+template <typename K>
+inline void prefer_shared(K kernel) {
+    static bool done = false;
+    if (!done) {
+        cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared);
+        done = true;
+    }
+}
+
 // Count of kernels launched by this library (process-wide).
 long long kernel_launch_count();
 void note_launch();

@@ -38,6 +38,10 @@ struct Terms {
     double E2B[MAXT][MAXT];       // [a][b] exp(lnE2[b] + lnB[a])
     double E2N[MAXT][MAXT];       // [a][b] exp(lnE2[b] + lnNegG1[a])
     double CT[MAXT][MAXT];        // [b][c] exp(lnG4[b] + lnB[c-1]), c > 0
+    // FP32 path: the exponentials factor, exp(lnE2[b] + lnB[a]) = exp(lnE2[b]) exp(lnB[a])
+    // and so on, so T of each are enough; dBN[a] = exp(lnB[a]) - exp(lnNegG1[a]) formed
+    // without cancellation as exp(lnB[a]) (-expm1(lnNegG1[a] - lnB[a]))
+    double eE2[MAXT], eB[MAXT], eG4[MAXT], dBN[MAXT];
 };
 
 // Fill the exponential tables (the same arguments get_time exponentiates), only the
@@ -83,48 +87,7 @@ __device__ __forceinline__ double logadd(double lna, double lnb) {  // common.h:
 }
 
 // State ranges of every node of one tree (states.cpp:53-167): first state, first time,
-// count, and (optionally) the offset of the node's same-branch rows. Thread 0 only.
-__device__ int node_ranges(const int4 *nd, int n, int root, int T, bool internal,
-                           int minage_param, int *first, int *t0, int *cnt, int *t2base,
-                           int *stack, char *ignore) {
-    int S = 0, M = 0;
-    for (int v = 0; v < n; v++) ignore[v] = 0;
-    int minage = 0;
-    bool none = false;
-    if (internal) {
-        if (nd[root].w < T) {
-            none = true;
-        } else {
-            const int sub = nd[root].y;
-            minage = max(minage_param, nd[sub].w);
-            ignore[root] = 1;
-            int sp = 0;
-            stack[sp++] = sub;
-            while (sp > 0) {
-                int v = stack[--sp];
-                ignore[v] = 1;
-                if (nd[v].y != -1) { stack[sp++] = nd[v].y; stack[sp++] = nd[v].z; }
-            }
-        }
-    }
-    for (int v = 0; v < n; v++) {
-        int m = 0, start = nd[v].w;
-        if (!none && !ignore[v]) {
-            const int p = nd[v].x;
-            start = internal ? max(nd[v].w, minage) : nd[v].w;
-            const bool top_branch = internal ? (p == root) : (p == -1);
-            const int top = top_branch ? T - 2 : nd[p].w;
-            m = max(0, top - start + 1);
-        }
-        first[v] = S;
-        t0[v] = start;
-        cnt[v] = m;
-        if (t2base) t2base[v] = M;
-        S += m;
-        M += m * m;
-    }
-    return S;
-}
+// count, and the offset of the node's same-branch rows (node_ranges_par below).
 
 __device__ __forceinline__ int lookup(const int *first, const int *t0, const int *cnt, int v,
                                       int t) {
@@ -132,6 +95,94 @@ __device__ __forceinline__ int lookup(const int *first, const int *t0, const int
     int d = t - t0[v];
     if (d < 0 || d >= cnt[v]) return -1;
     return first[v] + d;
+}
+
+// Whether v lies strictly below `top` (walks up the parents, at most n steps).
+__device__ __forceinline__ bool below(const int4 *nd, int v, int top, int n) {
+    int u = nd[v].x;
+    for (int s = 0; u != -1 && s < n; s++, u = nd[u].x)
+        if (u == top) return true;
+    return false;
+}
+
+// node_ranges by the whole CTA (the same outputs): per node its state count and first time
+// in parallel, then exclusive prefix sums over node order for the first state and the
+// same-branch row offset (integers: exact in any order). Returns S.
+__device__ int node_ranges_par(const int4 *nd, int n, int root, int T, bool internal,
+                               int minage_param, int *first, int *t0, int *cnt, int *t2base) {
+    __shared__ int part[TAB_THREADS], part2[TAB_THREADS];
+    __shared__ int sh_tot;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    bool none = false;
+    int minage = 0, sub = -1;
+    if (internal) {
+        if (nd[root].w < T) {
+            none = true;
+        } else {
+            sub = nd[root].y;
+            minage = max(minage_param, nd[sub].w);
+        }
+    }
+    for (int v = tid; v < n; v += nt) {
+        int m = 0, start = nd[v].w;
+        const bool ign = internal && !none && (v == root || v == sub || below(nd, v, sub, n));
+        if (!none && !ign) {
+            const int p = nd[v].x;
+            start = internal ? max(nd[v].w, minage) : nd[v].w;
+            const bool top_branch = internal ? (p == root) : (p == -1);
+            const int top = top_branch ? T - 2 : nd[p].w;
+            m = max(0, top - start + 1);
+        }
+        t0[v] = start;
+        cnt[v] = m;
+    }
+    __syncthreads();
+    const int c = (n + nt - 1) / nt;
+    const int lo = min(tid * c, n), hi = min(lo + c, n);
+    int s1 = 0, s2 = 0;
+    for (int v = lo; v < hi; v++) {
+        s1 += cnt[v];
+        s2 += cnt[v] * cnt[v];
+    }
+    part[tid] = s1;
+    part2[tid] = s2;
+    __syncthreads();
+    if (tid == 0) {
+        int a = 0, b = 0;
+        for (int t = 0; t < nt; t++) {
+            const int x = part[t], y = part2[t];
+            part[t] = a;
+            part2[t] = b;
+            a += x;
+            b += y;
+        }
+        sh_tot = a;
+    }
+    __syncthreads();
+    int a = part[tid], b = part2[tid];
+    for (int v = lo; v < hi; v++) {
+        first[v] = a;
+        if (t2base) t2base[v] = b;
+        a += cnt[v];
+        b += cnt[v] * cnt[v];
+    }
+    const int S = sh_tot;
+    __syncthreads();
+    return S;
+}
+
+// Sum of one double per thread in a fixed order (warp trees, then the warps in order);
+// every thread gets the total.
+__device__ double block_sum(double v) {
+    __shared__ double red[TAB_THREADS / 32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double s = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += red[w];
+    __syncthreads();
+    return s;
 }
 
 // Lineage counts of one tree (count_lineages[_internal], local_tree.cpp:34-131); thread t
@@ -339,14 +390,17 @@ __device__ __forceinline__ void tables_tree(const BatchDev &d, int blk, int want
     __syncthreads();
 
     const int root = B.root;
-    if (tid == 0) {
-        sh_S = node_ranges(cur, n, root, T, internal, I.minage, first, t0, cnt, t2base, stack,
-                           ignore);
-        if (B.b > 0)
-            sh_S1 = node_ranges(prv, n, B.prev_root, T, internal, I.minage, pfirst, pt0, pcnt,
-                                nullptr, stack, ignore);
-        // TransMatrix::minage: max(StatesModel::minage, subtree age) when internal
-        sh_minage = internal ? max(I.minage, cur[cur[root].y].w) : 0;
+    {
+        const int S0 = node_ranges_par(cur, n, root, T, internal, I.minage, first, t0, cnt, t2base);
+        const int S10 = B.b > 0 ? node_ranges_par(prv, n, B.prev_root, T, internal, I.minage,
+                                                  pfirst, pt0, pcnt, nullptr)
+                                : 0;
+        if (tid == 0) {
+            sh_S = S0;
+            sh_S1 = S10;
+            // TransMatrix::minage: max(StatesModel::minage, subtree age) when internal
+            sh_minage = internal ? max(I.minage, cur[cur[root].y].w) : 0;
+        }
     }
     __syncthreads();
     const int S = sh_S;
@@ -380,10 +434,23 @@ __device__ __forceinline__ void tables_tree(const BatchDev &d, int blk, int want
     __syncthreads();
 
     // transition terms (calc_transition_probs, trans.cpp:26-115)
+    for (int i = tid; i < 2 * T; i += blockDim.x)
+        coal_rates_alloc[1 + i] = csteps[i] * nb[i / 2] / (2.0 * pops[i / 2]);
+    double tl_par = 0.0;
+    if (want32) {
+        // FP32 path: the tree length summed by the CTA (the FP64 path keeps node order)
+        double part = 0.0;
+        for (int i = tid; i < n; i += blockDim.x) {
+            const int p = cur[i].x;
+            if (p == -1 || (internal && p == root)) continue;
+            part += times[cur[p].w] - times[cur[i].w];
+        }
+        tl_par = block_sum(part);
+    }
+    __syncthreads();
     if (tid == 0) {
         double *coal_rates = &coal_rates_alloc[1];
         coal_rates[-1] = 0.0;
-        for (int i = 0; i < 2 * T; i++) coal_rates[i] = csteps[i] * nb[i / 2] / (2.0 * pops[i / 2]);
         double *C = &C_alloc[2];
         C[-2] = 0.0;
         C[-1] = 0.0;
@@ -393,10 +460,10 @@ __device__ __forceinline__ void tables_tree(const BatchDev &d, int blk, int want
         if (internal) {
             const int sub = cur[root].y, mainr = cur[root].z;
             root_age_index = cur[mainr].w;
-            treelen = treelen_of(cur, n, root, times, true) - times[cur[sub].w];
+            treelen = (want32 ? tl_par : treelen_of(cur, n, root, times, true)) - times[cur[sub].w];
         } else {
             root_age_index = cur[root].w;
-            treelen = treelen_of(cur, n, root, times, false);
+            treelen = want32 ? tl_par : treelen_of(cur, n, root, times, false);
         }
         sh_treelen = treelen;
         sh_rootage = root_age_index;
@@ -434,22 +501,64 @@ __device__ __forceinline__ void tables_tree(const BatchDev &d, int blk, int want
         }
     }
     __syncthreads();
-    if (tid == 0) {
-        tr.lnB[0] = lnBterm[0];
-        for (int b = 1; b < T - 1; b++) tr.lnB[b] = logadd(tr.lnB[b - 1], lnBterm[b]);
-        tr.E[T - 2] = 1.0 / nc[T - 2];
+    if (!want32) {
+        if (tid == 0) {
+            tr.lnB[0] = lnBterm[0];
+            for (int b = 1; b < T - 1; b++) tr.lnB[b] = logadd(tr.lnB[b - 1], lnBterm[b]);
+            tr.E[T - 2] = 1.0 / nc[T - 2];
+        }
+    } else {
+        // FP32 path: the log-sum-exp prefix lnB[b] = log(sum_{i <= b} exp(lnBterm[i])) as T
+        // exponentials shifted by the largest term, one prefix sum and T logarithms (the
+        // reference adds one term at a time with logadd)
+        __shared__ double wexp[MAXT];
+        double mx = -INFINITY;
+        for (int i = 0; i < T - 1; i++) mx = fmax(mx, lnBterm[i]);
+        for (int b = tid; b < T - 1; b += blockDim.x) wexp[b] = exp(lnBterm[b] - mx);
+        __syncthreads();
+        if (tid == 0) {
+            double acc = 0.0;
+            for (int b = 0; b < T - 1; b++) {
+                acc += wexp[b];
+                wexp[b] = acc;
+            }
+            tr.E[T - 2] = 1.0 / nc[T - 2];
+        }
+        __syncthreads();
+        for (int b = tid; b < T - 1; b += blockDim.x) tr.lnB[b] = mx + log(wexp[b]);
     }
     __syncthreads();
-    exp_tables(tr, T);
-    __syncthreads();
-
-    // tmatrix[a][b] = get_time(a, b, 0, minage, false) (sample_thread.cpp:212-216)
-    double *tm = d.tm + (size_t)blk * MAXT * MAXT;
-    for (int e = tid; e < (T - 1) * (T - 1); e += blockDim.x) {
-        const int a = e / (T - 1), b = e % (T - 1);
-        const double v = get_time(tr, a, b, 0, minage, false);
-        tm[a * MAXT + b] = v;
-        if (want32) d.tm32[(size_t)blk * MAXT * MAXT + a * MAXT + b] = (float)v;
+    if (!want32) {
+        exp_tables(tr, T);
+        __syncthreads();
+        // tmatrix[a][b] = get_time(a, b, 0, minage, false) (sample_thread.cpp:212-216)
+        double *tm = d.tm + (size_t)blk * MAXT * MAXT;
+        for (int e = tid; e < (T - 1) * (T - 1); e += blockDim.x) {
+            const int a = e / (T - 1), b = e % (T - 1);
+            tm[a * MAXT + b] = get_time(tr, a, b, 0, minage, false);
+        }
+    } else {
+        // FP32 path: 4 (T-1) exponentials instead of 1.5 (T-1)^2; tmatrix = D[a] E[b] (X[a][b]
+        // - minage_term[b]), X the different-node bracket (get_time, trans.h:101-109), kept
+        // with D[a] E[b] for the same-branch rows below
+        for (int i = tid; i < T - 1; i += blockDim.x) {
+            tr.eE2[i] = exp(tr.lnE2[i]);
+            tr.eB[i] = exp(tr.lnB[i]);
+            tr.eG4[i] = exp(tr.lnG4[i]);
+            tr.dBN[i] = tr.eB[i] * -expm1(tr.lnNegG1[i] - tr.lnB[i]);
+        }
+        __syncthreads();
+        float *tm32 = d.tm32 + (size_t)blk * MAXT * MAXT;
+        for (int e = tid; e < (T - 1) * (T - 1); e += blockDim.x) {
+            const int a = e / (T - 1), b = e % (T - 1);
+            const double eb = b > 0 ? tr.eE2[b] * tr.eB[b - 1] : 0.0;
+            const double x = a < b ? tr.eE2[b] * tr.dBN[a] : eb + (a == b ? tr.G3[b] : tr.G2[b]);
+            const double de = __dmul_rn(tr.D[a], tr.E[b]);
+            const double mt = minage > 0 ? tr.eG4[b] * tr.eB[minage - 1] : 0.0;
+            tr.E2B[a][b] = x;
+            tr.E2N[a][b] = de;
+            tm32[a * MAXT + b] = (a < minage || b < minage) ? 0.0f : (float)(de * (x - mt));
+        }
     }
     __syncthreads();
 
@@ -470,23 +579,15 @@ __device__ __forceinline__ void tables_tree(const BatchDev &d, int blk, int want
     } else {
         // FP32 path: only the moving part, get_time(a, b, c, true) - get_time(a, b, 0, false)
         // - [a == b] norecombs[a], which in exact arithmetic is D[a] E[b] (X[a][b] - c_term)
-        // (X the different-node bracket without its minage term); formed from that product
-        // it keeps its relative accuracy where the two get_time values nearly cancel.
-        // X and D[a] E[b] overwrite E2B and E2N, which nothing reads after this point.
-        for (int e = tid; e < (T - 1) * (T - 1); e += blockDim.x) {
-            const int a = e / (T - 1), b = e % (T - 1);
-            const double x = a < b ? tr.E2B[a][b] - tr.E2N[a][b]
-                                   : tr.EB[b] + (a == b ? tr.G3[b] : tr.G2[b]);
-            tr.E2N[a][b] = __dmul_rn(tr.D[a], tr.E[b]);
-            tr.E2B[a][b] = x;
-        }
-        __syncthreads();
+        // (X the different-node bracket without its minage term; both in E2B / E2N above);
+        // formed from that product it keeps its relative accuracy where the two get_time
+        // values nearly cancel.
         float *t2d = d.t2d32 + B.t2_0;
         for (int k = tid; k < S; k += blockDim.x) {
             const StateInfo si = sinfo[k];
             const int b = si.time, c = cur[si.node].w;
             const int base = t2off[k];
-            const double ct = c > 0 ? tr.CT[b][c] : 0.0;
+            const double ct = c > 0 ? tr.eG4[b] * tr.eB[c - 1] : 0.0;
             for (int y = 0; y < si.m; y++) {
                 const int a = t0[si.node] + y;
                 t2d[base + y * si.m] =
@@ -523,7 +624,25 @@ __device__ __forceinline__ void tables_tree(const BatchDev &d, int blk, int want
     }
 
     // invariant-site emission per state (emit.cpp:744-819)
-    if (tid == 0) {
+    if (want32) {
+        // FP32 path: the main tree's and the subtree's lengths (branches floored at mintime)
+        // summed by the CTA; the FP64 path keeps the reference's walk order
+        const int mainr = internal ? cur[root].z : root;
+        const int sub = internal ? cur[root].y : root;
+        double pm = 0.0, ps = 0.0;
+        for (int v = tid; v < n; v += blockDim.x) {
+            const int p = cur[v].x;
+            const double w = fmax(p != -1 ? times[cur[p].w] - times[cur[v].w] : 0.0, mintime);
+            if (v != mainr && below(cur, v, mainr, n)) pm += w;
+            if (internal && v != sub && below(cur, v, sub, n)) ps += w;
+        }
+        const double mt = block_sum(pm);
+        const double st = internal ? block_sum(ps) : 0.0;
+        if (tid == 0) {
+            sh_maintreelen = mt;
+            sh_subtreelen = st;
+        }
+    } else if (tid == 0) {
         const int mainr = internal ? cur[root].z : root;
         const int sub = internal ? cur[root].y : root;
         double mt = 0.0, st = 0.0;
@@ -1552,12 +1671,14 @@ void launch_tables(const BatchDev &d, bool want32, cudaStream_t s, int *queue, i
     size_t smem = tables_smem(d.maxnodes, d.maxS, d.maxS);
     static size_t configured = 0, configured_ws = 0;
     if (!queue) {
+        prefer_shared(k_tables);
         if (smem > configured) {  // opt in; static shared memory counts against 48 KB too
             if (cudaFuncSetAttribute(k_tables, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return;
             configured = smem;
         }
         k_tables<<<d.nblocks, TAB_THREADS, smem, s>>>(d, want32 ? 1 : 0);
     } else {
+        prefer_shared(k_tables_ws);
         if (smem > configured_ws) {
             if (cudaFuncSetAttribute(k_tables_ws, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return;
             configured_ws = smem;
@@ -1592,12 +1713,14 @@ void launch_varemit_t(const BatchDev &d, cudaStream_t s, int *queue, int chunk) 
     const size_t smem = need(nwarps);
     static size_t configured = 0, configured_ws = 0;
     if (!queue) {
+        prefer_shared(k_varemit<FP32OUT>);
         if (smem > configured) {  // opt in; static shared memory counts against 48 KB too
             if (cudaFuncSetAttribute(k_varemit<FP32OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return;
             configured = smem;
         }
         k_varemit<FP32OUT><<<d.nblocks, nwarps * 32, smem, s>>>(d, nwarps, maxS, (int)smem);
     } else {
+        prefer_shared(k_varemit_ws<FP32OUT>);
         if (smem > configured_ws) {
             if (cudaFuncSetAttribute(k_varemit_ws<FP32OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return;
             configured_ws = smem;

@@ -860,6 +860,7 @@ bool launch_split(const BatchDev &d, cudaStream_t s, size_t budget) {
                         (size_t)NCH * (CW + 2) * sizeof(double) + 2 * (size_t)TreeBufLayout(maxS).total;
     if (smem > budget) return false;
     static size_t configured = 0;
+    prefer_shared(k_traceback_split<NCH>);
     if (smem > configured) {
         if (cudaFuncSetAttribute(k_traceback_split<NCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)smem) != cudaSuccess)

@@ -185,25 +185,37 @@ __device__ double block_sum(double v) {
     return s;
 }
 
-// Lineage counts of one tree (count_lineages[_internal], local_tree.cpp:34-131); thread t
-// fills time slice t.
-__device__ void lineage_counts(const int4 *nd, int n, int root, int T, bool internal, int *nb,
-                               int *nr, int *nc) {
-    for (int t = threadIdx.x; t < T; t += blockDim.x) {
-        int b = 0, r = 0, c = 0;
-        const int sub = internal ? nd[root].y : -1;
-        for (int i = 0; i < n; i++) {
-            if (internal && (i == sub || i == root)) continue;
-            const int p = nd[i].x;
-            const bool top_branch = internal ? (p == root) : (p == -1);
-            const int pa = top_branch ? T - 2 : nd[p].w;
-            if (nd[i].w <= t && t < pa) { b++; r++; c++; }
-            if (t == pa) { r++; c++; if (top_branch) b++; }
+// Lineage counts of one tree (count_lineages[_internal], local_tree.cpp:34-131) by the
+// whole CTA: each node adds its branch to the time slices it spans (integer shared-memory
+// atomics: exact in any order), then the per-slice corrections. Ends with a barrier.
+__device__ void lineage_counts_par(const int4 *nd, int n, int root, int T, bool internal,
+                                   int *nb, int *nr, int *nc) {
+    const int tid = threadIdx.x;
+    for (int t = tid; t < T; t += blockDim.x) nb[t] = nr[t] = nc[t] = 0;
+    __syncthreads();
+    const int sub = internal ? nd[root].y : -1;
+    for (int i = tid; i < n; i += blockDim.x) {
+        if (internal && (i == sub || i == root)) continue;
+        const int p = nd[i].x;
+        const bool top_branch = internal ? (p == root) : (p == -1);
+        const int pa = top_branch ? T - 2 : nd[p].w;
+        for (int t = max(nd[i].w, 0); t < pa && t < T; t++) {
+            atomicAdd(&nb[t], 1);
+            atomicAdd(&nr[t], 1);
+            atomicAdd(&nc[t], 1);
         }
-        if (internal && t < nd[sub].w) { b--; c--; r--; }
-        if (t == T - 1) b = 1;
-        nb[t] = b; nr[t] = r; nc[t] = c;
+        if (pa >= 0 && pa < T) {
+            atomicAdd(&nr[pa], 1);
+            atomicAdd(&nc[pa], 1);
+            if (top_branch) atomicAdd(&nb[pa], 1);
+        }
     }
+    __syncthreads();
+    for (int t = tid; t < T; t += blockDim.x) {
+        if (internal && t < nd[sub].w) { nb[t]--; nc[t]--; nr[t]--; }
+        if (t == T - 1) nb[t] = 1;
+    }
+    __syncthreads();
 }
 
 // get_treelen (use_basal=false) / get_treelen_internal; node order as the reference.
@@ -429,9 +441,8 @@ __device__ __forceinline__ void tables_tree(const BatchDev &d, int blk, int want
     }
 
     // lineage counts of this tree, and of the previous tree for the switch
-    lineage_counts(cur, n, root, T, internal, nb, nr, nc);
-    if (B.b > 0) lineage_counts(prv, n, B.prev_root, T, internal, pnb, pnr, pnc);
-    __syncthreads();
+    lineage_counts_par(cur, n, root, T, internal, nb, nr, nc);
+    if (B.b > 0) lineage_counts_par(prv, n, B.prev_root, T, internal, pnb, pnr, pnc);
 
     // transition terms (calc_transition_probs, trans.cpp:26-115)
     for (int i = tid; i < 2 * T; i += blockDim.x)
@@ -474,30 +485,38 @@ __device__ __forceinline__ void tables_tree(const BatchDev &d, int blk, int want
         const double *C = &C_alloc[2];
         const int root_age_index = sh_rootage;
         const double root_age = times[root_age_index];
-        for (int b = tid; b < T - 1; b += blockDim.x) {
-            double treelen2 = sh_treelen + times[b];
-            double treelen2_b;
-            if (b > root_age_index) {
-                treelen2 += times[b] - root_age;
-                treelen2_b = treelen2 + tsteps[b];
+        // one (term, time) pair per thread, each term's expression as the reference writes
+        // it (lnE2 and lnG4 are the same expression, trans.cpp:80-86)
+        for (int e = tid; e < 5 * (T - 1); e += blockDim.x) {
+            const int f = e / (T - 1), b = e % (T - 1);
+            if (f == 0) {
+                lnBterm[b] = C[2 * b - 1] + log(tsteps[b] * (nb[b] + 1.0) / (nr[b] + 1.0));
+                tr.E[b] = 1.0 / nc[b];
+            } else if (f == 1) {
+                const double v = -C[2 * b - 2] +
+                    (b < T - 2 ? log(1 - exp(-coal_rates[2 * b] - coal_rates[2 * b - 1])) : 0.0);
+                tr.lnE2[b] = v;
+                tr.lnG4[b] = v;
+            } else if (f == 2) {
+                tr.lnNegG1[b] = C[2 * b - 1] + log(-tsteps[b] *
+                    ((nb[b] / (nr[b] + 1.0 + int(b < root_age_index))) - (nb[b] + 1.0) / (nr[b] + 1.0)));
+            } else if (f == 3) {
+                const double g = b < T - 2 ? 1.0 - exp(-coal_rates[2 * b]) : 1.0;
+                tr.G2[b] = g * tsteps[b] * (nb[b] + 1.0) / (nr[b] + 1.0);
+                tr.G3[b] = g * tsteps[b] * (nb[b] / (nr[b] + 1.0 + int(b < root_age_index)));
             } else {
-                treelen2_b = treelen2 + tsteps[root_age_index];
+                double treelen2 = sh_treelen + times[b];
+                double treelen2_b;
+                if (b > root_age_index) {
+                    treelen2 += times[b] - root_age;
+                    treelen2_b = treelen2 + tsteps[b];
+                } else {
+                    treelen2_b = treelen2 + tsteps[root_age_index];
+                }
+                tr.D[b] = (1.0 - exp(-rho * treelen2)) / treelen2_b;
+                tr.norecombs[b] = exp(-fmax(rho * treelen2, rho));
+                if (want32) d.rstay32[(size_t)blk * MAXT + b] = (float)(-expm1(-fmax(rho * treelen2, rho)));
             }
-            lnBterm[b] = C[2 * b - 1] + log(tsteps[b] * (nb[b] + 1.0) / (nr[b] + 1.0));
-            tr.lnE2[b] = -C[2 * b - 2] +
-                (b < T - 2 ? log(1 - exp(-coal_rates[2 * b] - coal_rates[2 * b - 1])) : 0.0);
-            tr.lnNegG1[b] = C[2 * b - 1] + log(-tsteps[b] *
-                ((nb[b] / (nr[b] + 1.0 + int(b < root_age_index))) - (nb[b] + 1.0) / (nr[b] + 1.0)));
-            tr.G2[b] = (b < T - 2 ? 1.0 - exp(-coal_rates[2 * b]) : 1.0) * tsteps[b] *
-                       (nb[b] + 1.0) / (nr[b] + 1.0);
-            tr.G3[b] = (b < T - 2 ? 1.0 - exp(-coal_rates[2 * b]) : 1.0) * tsteps[b] *
-                       (nb[b] / (nr[b] + 1.0 + int(b < root_age_index)));
-            tr.lnG4[b] = -C[2 * b - 2] +
-                (b < T - 2 ? log(1.0 - exp(-coal_rates[2 * b] - coal_rates[2 * b - 1])) : 0.0);
-            tr.D[b] = (1.0 - exp(-rho * treelen2)) / treelen2_b;
-            tr.E[b] = 1.0 / nc[b];
-            tr.norecombs[b] = exp(-fmax(rho * treelen2, rho));
-            if (want32) d.rstay32[(size_t)blk * MAXT + b] = (float)(-expm1(-fmax(rho * treelen2, rho)));
         }
     }
     __syncthreads();
@@ -915,7 +934,7 @@ __device__ __forceinline__ void tables_tree(const BatchDev &d, int blk, int want
             else if (s1node[i] == spr[2] && s1time[i] == spr[3]) sh_src[1] = i;
         }
         __syncthreads();
-        if (tid == 0) {
+        if (tid == 0 || tid == 32) {  // the two entries on two warps
             const int recombsrc = sh_src[0];
             if (recombsrc != -1) {  // get_recomb_transition_switch (trans.cpp:278-313)
                 const int parent = prv[spr[0]].x;
@@ -924,10 +943,26 @@ __device__ __forceinline__ void tables_tree(const BatchDev &d, int blk, int want
                 const int node2 = (other == spr[2] ? cur[mapping[other]].x : mapping[other]);
                 const int next0 = lookup(first, t0, cnt, mapping[spr[0]], spr[1]);
                 const int next1 = lookup(first, t0, cnt, node2, time2);
-                if (next0 != -1)
+                if (tid == 0 && next0 != -1)
                     recombrow[next0] = calc_recomb_recoal(c, spr, s1node[recombsrc],
                                                           s1time[recombsrc], rpa0);
-                if (next1 != -1)
+                // where both entries are one state the second write wins (the block below)
+                if (tid == 32 && next1 != -1 && next1 != next0)
+                    recombrow[next1] = calc_recomb_recoal(c, spr, s1node[recombsrc],
+                                                          s1time[recombsrc], s1time[recombsrc]);
+            }
+        }
+        __syncthreads();
+        if (tid == 32) {  // next0 == next1: the second evaluation overwrites the first
+            const int recombsrc = sh_src[0];
+            if (recombsrc != -1) {
+                const int parent = prv[spr[0]].x;
+                const int time2 = prv[parent].w;
+                const int other = sibling(prv, spr[0]);
+                const int node2 = (other == spr[2] ? cur[mapping[other]].x : mapping[other]);
+                const int next0 = lookup(first, t0, cnt, mapping[spr[0]], spr[1]);
+                const int next1 = lookup(first, t0, cnt, node2, time2);
+                if (next1 != -1 && next1 == next0)
                     recombrow[next1] = calc_recomb_recoal(c, spr, s1node[recombsrc],
                                                           s1time[recombsrc], s1time[recombsrc]);
             }

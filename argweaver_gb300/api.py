@@ -37,7 +37,7 @@ class _Bound:
                                  int(p.internal), p.start_coord, 0, ptr(p.ptrees),
                                  ptr(p.ages), ptr(p.sprs), ptr(p.blocklens), ptr(p.mapping),
                                  ptr(p.root_child0), ptr(p.times), ptr(p.popsizes), p.rho,
-                                 p.mu, ptr(p.seqs))
+                                 p.mu, ptr(p.seqs), float(p.infsites_penalty))
 
 
 def cells(prob: Problem) -> int:

@@ -32,7 +32,7 @@ class AwgProblem(C.Structure):
                 ("blocklens", C.c_void_p), ("mapping", C.c_void_p),
                 ("root_child0", C.c_void_p), ("times", C.c_void_p),
                 ("popsizes", C.c_void_p), ("rho", C.c_double), ("mu", C.c_double),
-                ("seqs", C.c_void_p)]
+                ("seqs", C.c_void_p), ("infsites_penalty", C.c_double)]
 
 
 class AwgOutputs(C.Structure):

@@ -30,7 +30,7 @@ constexpr int M_TIMES = 0;              // times[T]
 constexpr int M_POPSIZES = MAXT;        // popsizes[T]
 constexpr int M_TIMESTEPS = 2 * MAXT;   // time_steps[T] (model.h:322-329)
 constexpr int M_COALSTEPS = 3 * MAXT;   // coal_time_steps[2T] (model.cpp:9-23)
-constexpr int M_CONST = 5 * MAXT;       // rho, mu, mintime
+constexpr int M_CONST = 5 * MAXT;       // rho, mu, mintime, infinite-sites penalty (1: off)
 
 // Column classes (find_invariant_sites / find_masked_sites, emit.cpp:30-58).
 enum : uint8_t { COL_INVARIANT = 0, COL_MASKED = 1, COL_VARIANT = 2 };

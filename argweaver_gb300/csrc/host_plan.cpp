@@ -245,6 +245,7 @@ bool plan_layout(const awg_problem *probs, int n, HostPlan &plan, std::string &e
         m[M_CONST + 0] = p.rho;
         m[M_CONST + 1] = p.mu;
         m[M_CONST + 2] = p.times[1] * .1;
+        m[M_CONST + 3] = (p.infsites_penalty > 0.0 && p.infsites_penalty < 1.0) ? p.infsites_penalty : 1.0;
 
         int pos = 0;
         for (int b = 0; b < p.ntrees; b++, blk++) {

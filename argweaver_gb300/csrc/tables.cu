@@ -1164,9 +1164,85 @@ struct EmitCtx {
     const float *pm32;                 // [S][8]: mut0..2, nomut0..2, 1 - 4 mut0, unused
     const int *snode, *inl, *inp, *outl, *outp;
     const uint8_t *sfloor;  // per state: a split branch of it was raised to mintime
-    int nlev_in, nlev_out, mainr, node1, S, ns, nleaves;
+    int nlev_in, nlev_out, mainr, node1, S, ns, nleaves, n;
     bool internal;
 };
+
+__device__ __forceinline__ int base_bit(uint8_t ch) {
+    if (ch == 'N') return 0;
+    return 1 << ((ch == 'A' || ch == 'a') ? 0 : (ch == 'C' || ch == 'c') ? 1
+                 : (ch == 'G' || ch == 'g') ? 2 : 3);
+}
+
+// Infinite-sites validity of one variant column's nodes (get_infinite_sites_states,
+// emit.cpp:454-589, with parsimony_ancestral_set :898-953) by one warp over the level
+// schedules: Fitch sets by height, then refined from the main root down (any order with
+// children first, then parents first, gives the reference's sets). A state on node j keeps
+// the model when the threaded base (the cut subtree's set) meets the set of j or of its
+// parent. Node j's flag is bit j / 32 of lane j % 32's word; all flags are 1 when the
+// column cannot break the model. sets, anc: n bytes each of the warp's scratch.
+__device__ unsigned infsites_nodes(const EmitCtx &c, const uint8_t *chars, uint8_t *sets,
+                                   uint8_t *anc) {
+    constexpr unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int4 *nd = c.nd;
+    int all = 0, subset = 0, mainset = 0;
+    for (int x = lane; x < c.inp[1]; x += 32) {
+        const int j = c.inl[x];
+        const int b = base_bit(chars[j]);
+        sets[j] = (uint8_t)b;
+        if (!c.internal) {
+            all |= b;
+        } else {
+            int u = j;
+            for (int s = 0; u != -1 && u != c.node1 && s < c.n; s++) u = nd[u].x;
+            if (u == c.node1) subset |= b;
+            else mainset |= b;
+        }
+    }
+    all = __reduce_or_sync(FULL, all);
+    subset = __reduce_or_sync(FULL, subset);
+    mainset = __reduce_or_sync(FULL, mainset);
+    __syncwarp();
+    for (int h = 1; h < c.nlev_in; h++) {
+        for (int x = c.inp[h] + lane; x < c.inp[h + 1]; x += 32) {
+            const int j = c.inl[x];
+            const int l = sets[nd[j].y], r = sets[nd[j].z];
+            sets[j] = (uint8_t)((l & r) ? (l & r) : (l | r));
+        }
+        __syncwarp();
+    }
+    const int cset = c.internal ? sets[c.node1] : base_bit(chars[c.nleaves]);
+    if (c.internal ? !(subset & mainset) : !(cset & all)) return FULL;
+    for (int h = 0; h < c.nlev_out; h++) {
+        for (int x = c.outp[h] + lane; x < c.outp[h + 1]; x += 32) {
+            const int j = c.outl[x];
+            if (j == c.mainr) {
+                anc[j] = sets[j];
+            } else {
+                const int ps = anc[nd[j].x] & sets[j];
+                anc[j] = (uint8_t)(ps ? ps : sets[j]);
+            }
+        }
+        __syncwarp();
+    }
+    unsigned word = FULL;
+    for (int w = 0; w * 32 + lane < c.n && w < 32; w++) {
+        const int j = w * 32 + lane;
+        int u = j;  // in the main tree (the only nodes with states)
+        for (int s = 0; u != -1 && u != c.mainr && s < c.n; s++) u = nd[u].x;
+        if (u != c.mainr) continue;
+        const bool ok = (cset & anc[j]) || (j != c.mainr && (cset & anc[nd[j].x]));
+        if (!ok) word &= ~(1u << w);
+    }
+    __syncwarp();
+    return word;
+}
+
+// Whether state k's node keeps the infinite-sites model (all lanes call it).
+__device__ __forceinline__ bool state_ok(unsigned word, int node) {
+    return (__shfl_sync(0xffffffffu, word, node & 31) >> (node >> 5)) & 1;
+}
 
 // Column forms of the partials and emissions:
 //   REF  FP64, the reference's order of operations (plain path)
@@ -1457,6 +1533,7 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
     const double *model = d.model + I.model0;
     for (int i = tid; i < T; i += blockDim.x) times[i] = model[M_TIMES + i];
     const double mu = model[M_CONST + 1], mintime = model[M_CONST + 2];
+    const double penalty = model[M_CONST + 3];  // infinite-sites penalty, 1: off
     for (int i = tid; i < n; i += blockDim.x) nd[i] = d.nodes[B.nodes0 + i];
     __syncthreads();
     const int root = B.root;
@@ -1555,7 +1632,7 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
     __syncthreads();
 
     const EmitCtx ctx{nd, muts, nomuts, pm, muts32, nomuts32, pm32, snode, inl, inp, outl, outp,
-                      sfloor, nlev_in, nlev_out, mainr, node1, S, I.nseqs, I.nleaves, internal};
+                      sfloor, nlev_in, nlev_out, mainr, node1, S, I.nseqs, I.nleaves, n, internal};
     double *wscr = scratch + (size_t)warp * n * 8;
     double *eb = ebuf + (size_t)warp * maxS;
     const uint8_t *cls = d.colclass + I.col0 + B.start;
@@ -1578,11 +1655,55 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
                 if (lane == 0) report_error(d.err, ERR_BOUNDS, B.inst, B.b, B.start + base + bit);
                 continue;
             }
+            // infinite-sites model (calc_emissions, emit.cpp:847-862): states whose node
+            // breaks it have their emission multiplied by the penalty
+            unsigned vword = 0xffffffffu;
+            bool penalised = false;
+            if (penalty < 1.0) {
+                vword = infsites_nodes(ctx, chars, (uint8_t *)wscr, (uint8_t *)wscr + n);
+                bool bad = false;
+                for (int kb = 0; kb < S; kb += 32) {
+                    const int k = kb + lane;
+                    bad |= !state_ok(vword, k < S ? snode[k] : 0) && k < S;
+                }
+                penalised = __any_sync(0xffffffffu, bad);
+                __syncwarp();
+            }
+            auto penalise = [&](double *e) {  // e[k] *= penalty where state k breaks it
+                for (int kb = 0; kb < S; kb += 32) {
+                    const int k = kb + lane;
+                    const bool ok = state_ok(vword, k < S ? snode[k] : 0);
+                    if (k < S && !ok) e[k] *= penalty;
+                }
+                __syncwarp();
+            };
             if constexpr (!FP32OUT) {
                 emit_column<double, EM_REF>(ctx, chars, 0, (double (*)[4])wscr,
                                             (double (*)[4])wscr + n, eb);
+                if (penalised) penalise(eb);
                 double *row = d.varemit + B.var0 + (size_t)vrow * S;
                 for (int k = lane; k < S; k += 32) row[k] = eb[k];
+            } else if (penalised) {
+                // FP64 emissions, penalised, then relative to the column's largest
+                const int X0 = 0;
+                emit_column<double, EM_F64>(ctx, chars, X0, (double (*)[4])wscr,
+                                            (double (*)[4])wscr + n, eb);
+                penalise(eb);
+                double eref = 0.0;
+                for (int k = lane; k < S; k += 32) eref = fmax(eref, eb[k]);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) eref = fmax(eref, __shfl_xor_sync(0xffffffffu, eref, o));
+                float *row = d.var32 + B.var0 + (size_t)vrow * S;
+                const double inv1 = 1.0 / eref;  // 1 / (4 e_ref)
+                for (int k = lane; k < S; k += 32) {
+                    const double r = eb[k] * inv1;  // e_k / e_ref
+                    float v = (float)(r >= 0.5 ? 1.0 - r : -r);
+                    // a ratio below FP32's range (a penalised state) stays a ratio: -0
+                    // would read as the complement 0, i.e. the largest emission
+                    if (r < 0.5 && v == 0.0f) v = -__int_as_float(1);
+                    row[k] = v;
+                }
+                if (lane == 0) d.lnvref[B.vrow0 + vrow] = log(.25 * eref);
             } else {
                 // X = the column's first observed base; near = every observed call (the
                 // threaded sequence's too) is X

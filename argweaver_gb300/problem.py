@@ -45,6 +45,9 @@ class Problem:
     root_child0: Optional[np.ndarray] = None  # i32 [ntrees]
     path_node: Optional[np.ndarray] = None  # true thread (simulated inputs only)
     path_time: Optional[np.ndarray] = None
+    # ArgModel::infsites_penalty (model.h:53): emissions of states that break the
+    # infinite-sites model are multiplied by it (emit.cpp:847-862); 1 (or 0): off
+    infsites_penalty: float = 1.0
 
     @property
     def ntimes(self) -> int:

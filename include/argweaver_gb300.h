@@ -113,6 +113,10 @@ typedef struct {
     double rho, mu;         /* per column */
     const char *seqs;       /* [nseqs*seqlen] rows: leaves in leaf order, then (external)
                                the sequence being threaded; bytes A,C,G,T (either case), N */
+    double infsites_penalty; /* ArgModel::infsites_penalty (model.h:53, arg-sample
+                               --infsites: 1e-100): the emissions of states that break the
+                               infinite-sites model are multiplied by it (emit.cpp:847-862);
+                               outside (0, 1), e.g. 0 from a zeroed struct: off */
 } awg_problem;
 
 enum { AWG_FP64 = 0, AWG_FP32 = 1 };

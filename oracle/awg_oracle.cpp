@@ -52,6 +52,7 @@ struct Model {
     int T = 0;
     vector<double> times, time_steps, coal_time_steps, popsizes;
     double rho = 0, mu = 0;
+    double infsites_penalty = 1.0;  // model.h:53 (1: off)
     double mintime() const { return times[1] * .1; }
     int removed_root_time() const { return T + 1; }
 };
@@ -178,6 +179,8 @@ bool build_model(const oracle_problem *p, Model &m) {
     m.popsizes.assign(p->popsizes, p->popsizes + T);
     m.rho = p->rho;
     m.mu = p->mu;
+    m.infsites_penalty =
+        (p->infsites_penalty > 0.0 && p->infsites_penalty < 1.0) ? p->infsites_penalty : 1.0;
     m.time_steps.assign(T, 0.0);
     for (int i = 0; i < T - 1; i++) m.time_steps[i] = m.times[i + 1] - m.times[i];
     m.time_steps[T - 1] = INFINITY;
@@ -830,6 +833,93 @@ inline double prob_branch(double t, double mu, bool mut) {  // emit.cpp:86-93
 typedef double lk_row[4];
 
 // calc_emissions (emit.cpp:650-869) for one block: emit[i*S + j], S = max(nstates,1)
+// parsimony_ancestral_set (emit.cpp:898-953): Fitch sets over `order` (children before
+// parents, the root last), then refined from the root down.
+void parsimony_sets(const Tree &t, const char *const *seqs, int pos, const vector<int> &order,
+                    vector<char> &anc) {
+    vector<char> sets(t.n, 0);
+    for (int node : order) {
+        if (t.leaf(node)) {
+            const char c = seqs[node][pos];
+            sets[node] = c == 'N' ? 0 : (char)(1 << dna2int(c));
+        } else {
+            const char l = sets[t.c0[node]], r = sets[t.c1[node]];
+            const char x = l & r;
+            sets[node] = x ? x : (char)(l | r);
+        }
+    }
+    const int root = order.back();
+    anc[root] = sets[root];
+    for (int i = (int)order.size() - 2; i >= 0; i--) {
+        const int node = order[i];
+        const char pset = anc[t.parent[node]] & sets[node];
+        anc[node] = pset ? pset : sets[node];
+    }
+}
+
+// get_infinite_sites_states (emit.cpp:454-589): whether each state of a non-invariant
+// column keeps the infinite-sites model (the threaded base needs no second mutation).
+void infsites_valid(const States &states, const Tree &t, const char *const *seqs, int pos,
+                    bool internal, vector<char> &valid) {
+    const int nstates = states.size();
+    const int n = t.n;
+    valid.assign(nstates, 1);
+    auto preorder = [&](int top) {  // LocalTree::get_preorder (local_tree.h:305-322)
+        vector<int> out, stack{top};
+        while (!stack.empty()) {
+            const int v = stack.back();
+            stack.pop_back();
+            out.push_back(v);
+            if (!t.leaf(v)) { stack.push_back(t.c0[v]); stack.push_back(t.c1[v]); }
+        }
+        return out;
+    };
+    vector<char> anc(n, 0), vnode(n, 0);
+    if (internal) {
+        const int mainr = t.c1[t.root], subr = t.c0[t.root];
+        vector<int> sub = preorder(subr), main = preorder(mainr);
+        std::reverse(sub.begin(), sub.end());
+        std::reverse(main.begin(), main.end());
+        char subset = 0, mainset = 0;
+        for (int j : sub)
+            if (t.leaf(j) && seqs[j][pos] != 'N') subset |= (char)(1 << dna2int(seqs[j][pos]));
+        for (int j : main)
+            if (t.leaf(j) && seqs[j][pos] != 'N') mainset |= (char)(1 << dna2int(seqs[j][pos]));
+        if (!(subset & mainset)) return;
+        parsimony_sets(t, seqs, pos, sub, anc);
+        const char cset = anc[subr];
+        parsimony_sets(t, seqs, pos, main, anc);
+        for (int j : main)
+            vnode[j] = (cset & anc[j]) || (j != mainr && (cset & anc[t.parent[j]]));
+    } else {
+        const int newleaf = t.nleaves();
+        char set = 0;
+        for (int j = 0; j < newleaf; j++)
+            if (seqs[j][pos] != 'N') set |= (char)(1 << dna2int(seqs[j][pos]));
+        const char c = seqs[newleaf][pos];
+        const char cset = c != 'N' ? (char)(1 << dna2int(c)) : 0;
+        if (!(cset & set)) return;
+        vector<int> order(n);  // LocalTree::get_postorder (local_tree.h:274-304)
+        {
+            vector<char> visit(n, 0);
+            int i;
+            for (i = 0; i < n; i++) {
+                if (!t.leaf(i)) break;
+                order[i] = i;
+            }
+            int end = i;
+            for (i = 0; i < n; i++) {
+                const int parent = t.parent[order[i]];
+                if (parent != -1 && ++visit[parent] == 2) order[end++] = parent;
+            }
+        }
+        parsimony_sets(t, seqs, pos, order, anc);
+        for (int j = 0; j < n; j++)
+            vnode[j] = (cset & anc[j]) || (t.parent[j] != -1 && (cset & anc[t.parent[j]]));
+    }
+    for (int k = 0; k < nstates; k++) valid[k] = vnode[states.node[k]];
+}
+
 void calc_emissions(const States &states, const Tree &t, const char *const *seqs, int nseqs,
                     int seqlen, const Model &m, bool internal, double *emit) {
     const int nstates = states.size();
@@ -1023,6 +1113,17 @@ void calc_emissions(const States &states, const Tree &t, const char *const *seqs
                 }
             }
             emit[(size_t)i * S + j] = e;
+        }
+    }
+
+    // optionally the infinite-sites model (calc_emissions, emit.cpp:847-862)
+    if (m.infsites_penalty < 1.0) {
+        vector<char> valid;
+        for (int i = 0; i < seqlen; i++) {
+            if (invariant[i]) continue;
+            infsites_valid(states, t, seqs, i, internal, valid);
+            for (int j = 0; j < nstates; j++)
+                if (!valid[j]) emit[(size_t)i * S + j] *= m.infsites_penalty;
         }
     }
 }

@@ -27,6 +27,7 @@ typedef struct {
     const double *popsizes; /* [ntimes] */
     double rho, mu;         /* per column */
     const char *seqs;       /* [nseqs*seqlen] */
+    double infsites_penalty; /* ArgModel::infsites_penalty (model.h:53); outside (0, 1): off */
 } oracle_problem;
 
 /* Number of states of every column (arghmm_get_nstates, states.cpp:209). */

@@ -25,7 +25,7 @@ class OracleProblem(C.Structure):
                 ("blocklens", C.c_void_p), ("mapping", C.c_void_p),
                 ("root_child0", C.c_void_p), ("times", C.c_void_p),
                 ("popsizes", C.c_void_p), ("rho", C.c_double), ("mu", C.c_double),
-                ("seqs", C.c_void_p)]
+                ("seqs", C.c_void_p), ("infsites_penalty", C.c_double)]
 
 
 def build() -> str:
@@ -71,7 +71,8 @@ class Bound:
                                int(p.internal), p.start_coord, 0,
                                ptr(p.ptrees), ptr(p.ages), ptr(p.sprs), ptr(p.blocklens),
                                ptr(p.mapping), ptr(p.root_child0), ptr(p.times),
-                               ptr(p.popsizes), p.rho, p.mu, ptr(p.seqs))
+                               ptr(p.popsizes), p.rho, p.mu, ptr(p.seqs),
+                               float(p.infsites_penalty))
 
     @property
     def ref(self):

@@ -4,9 +4,11 @@
 // problem file (format below, written by argweaver_gb300/problem.py), runs the
 // reference's own C++ threading HMM on it and writes the results as golden data:
 //
-//   forward <problem> <out> <seed>   forward table (arghmm_forward_alg, sample_thread.cpp:394)
+//   forward <problem> <out> <seed> [penalty]
+//                                    forward table (arghmm_forward_alg, sample_thread.cpp:394)
 //                                    + stochastic_traceback (sample_thread.cpp:522) after
-//                                    srand(seed); per-column nstates (states.cpp:209)
+//                                    srand(seed); per-column nstates (states.cpp:209); with
+//                                    penalty, the model's infsites_penalty (emit.cpp:847-862)
 //   tables  <problem> <out>          per-block TransMatrix terms (trans.cpp:26),
 //                                    TransMatrixSwitch (trans.cpp:538), emissions (emit.cpp:650)
 //   dense   <problem> <out>          single-block problems: the reference's dense log-space
@@ -202,10 +204,11 @@ static vector<char *> seq_ptrs(Problem &p) {
     return s;
 }
 
-static int cmd_forward(const char *in, const char *out, int seed) {
+static int cmd_forward(const char *in, const char *out, int seed, double penalty) {
     Problem p = read_problem(in);
     LocalTrees *trees = make_trees(p);
     ArgModel model(p.ntimes, p.times.data(), p.popsizes.data(), p.rho, p.mu);
+    model.infsites_penalty = penalty;  // 1: off (the model's default, model.h:53)
     vector<char *> sp = seq_ptrs(p);
     Sequences sequences(sp.data(), p.nseqs, p.seqlen);
     const bool internal = p.internal != 0;
@@ -397,7 +400,9 @@ static int cmd_cut(const char *in, int seed, const char *out) {
 int main(int argc, char **argv) {
     if (argc < 2) die("usage: ref_harness forward|tables|dense|sim1|cut ...");
     std::string cmd = argv[1];
-    if (cmd == "forward" && argc == 5) return cmd_forward(argv[2], argv[3], atoi(argv[4]));
+    if (cmd == "forward" && argc == 5) return cmd_forward(argv[2], argv[3], atoi(argv[4]), 1.0);
+    if (cmd == "forward" && argc == 6)
+        return cmd_forward(argv[2], argv[3], atoi(argv[4]), atof(argv[5]));
     if (cmd == "tables" && argc == 4) return cmd_tables(argv[2], argv[3]);
     if (cmd == "dense" && argc == 4) return cmd_dense(argv[2], argv[3]);
     if (cmd == "sim1" && argc == 6) return cmd_sim1(argv[2], argv[3], atoi(argv[4]), argv[5]);

@@ -18,3 +18,16 @@ def pytest_configure(config):
 
 def golden_names():
     return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+
+
+def load_golden(name):
+    """A fixture's problem (with the model's infinite-sites penalty it ran with) and data."""
+    import numpy as np
+
+    from argweaver_gb300.problem import Problem
+
+    prob = Problem.load(os.path.join(GOLDEN, name + ".prob"))
+    gold = np.load(os.path.join(GOLDEN, name + ".npz"))
+    if "infsites_penalty" in gold.files:
+        prob.infsites_penalty = float(gold["infsites_penalty"])
+    return prob, gold

@@ -2,7 +2,8 @@
 
 Run where the reference checkout exists (default /root/reference, or $AWG_REFERENCE):
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py            # all fixtures
+    python tests/golden/make_golden.py infsites   # only the infinite-sites ones
 
 It builds the reference from its own sources (oracle/Makefile target ``ref``), writes
 each problem as an AWGPROB1 file and runs the reference's threading HMM on it through
@@ -16,6 +17,7 @@ oracle/ref_harness.cpp. Each ``<name>.npz`` then holds, from the reference:
   seed         int          srand seed of the traceback
   uniforms     f64   [L]    rand()/RAND_MAX the traceback drew, indexed by column
   path         int32 [L]    sampled state path (stochastic_traceback, sample_thread.cpp:522)
+  infsites_penalty  f64     (infsites_* fixtures) the model's infsites_penalty they ran with
 and for single-tree problems the reference's dense log-space backward (hmm.cpp:48) with
 the log transition matrix (calc_transition_probs, trans.cpp:136) and log emissions it ran on:
   dense_bw     f64   [L, S]
@@ -96,10 +98,14 @@ def run(*args):
     subprocess.run([HARNESS] + [str(a) for a in args], check=True)
 
 
-def make(name: str, prob_path: str, seed: int, tmp: str, dense: bool = False):
+def make(name: str, prob_path: str, seed: int, tmp: str, dense: bool = False,
+         penalty: float = 1.0):
     prob = Problem.load(prob_path)
     out = os.path.join(tmp, name + ".ref")
-    run("forward", prob_path, out, seed)
+    if penalty < 1.0:
+        run("forward", prob_path, out, seed, repr(penalty))
+    else:
+        run("forward", prob_path, out, seed)
     ns, fw, path = read_ref(out)
     colsum, colwsum, rows, rowvals = summarize(ns, fw)
     extra = {}
@@ -107,6 +113,8 @@ def make(name: str, prob_path: str, seed: int, tmp: str, dense: bool = False):
         dout = os.path.join(tmp, name + ".dense")
         run("dense", prob_path, dout)
         extra["dense_bw"], extra["dense_trans"], extra["dense_emit"] = read_dense(dout)
+    if penalty < 1.0:
+        extra["infsites_penalty"] = penalty
     u = pyoracle.rand_uniforms(seed, prob.seqlen)
     np.savez_compressed(os.path.join(HERE, name + ".npz"), nstates=ns, colsum=colsum,
                         colwsum=colwsum, rows=rows, rowvals=rowvals, seed=seed,
@@ -127,11 +135,32 @@ def first_tree(prob: Problem) -> Problem:
                    seqs=prob.seqs[:, :L].copy(), internal=prob.internal)
 
 
+def infsites(tmp):
+    """The infinite-sites penalty (ArgModel::infsites_penalty, emit.cpp:847-862; arg-sample
+    --infsites uses 1e-100): external, with missing calls, and an internal-branch cut."""
+    prob = simulate(7, 3000, 13)
+    p = os.path.join(tmp, "p.prob"); prob.save(p)
+    make("infsites_k8_s13", p, 113, tmp, penalty=1e-3)
+    prob = simulate(16, 1500, 22, missing=0.02)
+    p = os.path.join(tmp, "p.prob"); prob.save(p)
+    make("infsites_k17_missing", p, 122, tmp, penalty=1e-100)
+    full = simulate(10, 1500, 205, add_thread=False)
+    pf = os.path.join(tmp, "full.prob"); full.save(pf)
+    pc = os.path.join(tmp, "cut.prob")
+    run("cut", pf, 5, pc)
+    make("infsites_cut_k10_s5", pc, 505, tmp, penalty=1e-3)
+
+
 def main():
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={REF}"],
                    check=True)
     pyoracle.build()
+    if sys.argv[1:] == ["infsites"]:
+        with tempfile.TemporaryDirectory() as tmp:
+            infsites(tmp)
+        return
     with tempfile.TemporaryDirectory() as tmp:
+        infsites(tmp)
         # the reference's bundled example, re-threading its last sequence (k=8, 100 kb)
         p = os.path.join(HERE, "sim1_c20.prob")
         run("sim1", os.path.join(REF, "examples/sim1/sim1.sites"),

@@ -20,7 +20,7 @@ import pyoracle
 from argweaver_gb300 import api, refapi
 from argweaver_gb300.problem import Problem
 from argweaver_gb300.sim import simulate
-from conftest import GOLDEN, golden_names
+from conftest import GOLDEN, golden_names, load_golden
 
 pytestmark = pytest.mark.gpu
 
@@ -29,8 +29,7 @@ EXTERNAL_DEFAULT_MAP = [n for n in NAMES if n.startswith(("dsmc_", "single_"))]
 
 
 def load(name):
-    return (Problem.load(os.path.join(GOLDEN, name + ".prob")),
-            np.load(os.path.join(GOLDEN, name + ".npz")))
+    return load_golden(name)
 
 
 def weights(n):

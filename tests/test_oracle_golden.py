@@ -19,15 +19,13 @@ import pytest
 
 import pyoracle
 from argweaver_gb300.problem import Problem
-from conftest import GOLDEN, golden_names
+from conftest import GOLDEN, golden_names, load_golden
 
 NAMES = golden_names()
 
 
 def load(name):
-    prob = Problem.load(os.path.join(GOLDEN, name + ".prob"))
-    gold = np.load(os.path.join(GOLDEN, name + ".npz"))
-    return prob, gold
+    return load_golden(name)
 
 
 def weights(n):

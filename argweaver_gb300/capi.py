@@ -70,6 +70,9 @@ PROTOTYPES = [
     ("delete_path", None, [c_int_p]),
     ("delete_double_matrix", None, [c_double_pp, C.c_int]),
     ("delete_forward_matrix", None, [c_double_pp, C.c_int]),
+    ("forward_alg", None, [C.c_int, C.c_int, c_double_pp, c_double_pp, c_double_pp]),
+    ("backward_alg", None, [C.c_int, C.c_int, c_double_pp, c_double_pp, c_double_pp]),
+    ("sample_hmm_posterior", None, [C.c_int, C.c_int, c_double_pp, c_double_pp, c_int_p]),
     ("awg_problem_cells", C.c_longlong, [C.POINTER(AwgProblem)]),
     ("awg_problems_cells", C.c_int, [C.POINTER(AwgProblem), C.c_int, C.c_void_p]),
     ("awg_run_batch", C.c_int, [C.POINTER(AwgProblem), C.POINTER(AwgOutputs), C.c_int,

@@ -366,4 +366,24 @@ void delete_forward_matrix(double **mat, int nrows) {
     delete[] base;
 }
 
+// The dense HMM (hmm.cpp:27-85, bound by argweaver/argweaverc.py:42-56): the first column of
+// fw (last of bw, last entry of path) is the caller's, as in the reference.
+void forward_alg(int n, int nstates, double **trans, double **emit, double **fw) {
+    g_err.clear();
+    std::string err;
+    if (!awg::dense_hmm(0, n, nstates, trans, emit, fw, nullptr, err)) set_error(err);
+}
+
+void backward_alg(int n, int nstates, double **trans, double **emit, double **bw) {
+    g_err.clear();
+    std::string err;
+    if (!awg::dense_hmm(1, n, nstates, trans, emit, bw, nullptr, err)) set_error(err);
+}
+
+void sample_hmm_posterior(int n, int nstates, double **trans, double **fw, int *path) {
+    g_err.clear();
+    std::string err;
+    if (!awg::dense_hmm(2, n, nstates, trans, nullptr, fw, path, err)) set_error(err);
+}
+
 }  // extern "C"

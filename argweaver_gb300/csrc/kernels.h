@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include <string>
+
 #include "awg_internal.h"
 
 namespace awg {
@@ -41,5 +43,11 @@ inline void prefer_shared(K kernel) {
 // Count of kernels launched by this library (process-wide).
 long long kernel_launch_count();
 void note_launch();
+
+// The dense HMM of hmm.cpp:27-85 on the device: which 0 = forward_alg, 1 = backward_alg,
+// 2 = sample_hmm_posterior (uniforms from libc rand(), last column first). Tables are the
+// reference's row pointers; false with err set on failure.
+bool dense_hmm(int which, int n, int nstates, double **trans, double **emit, double **tab,
+               int *path, std::string &err);
 
 }  // namespace awg

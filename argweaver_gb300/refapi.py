@@ -160,3 +160,60 @@ def arghmm_sample_arg_thread_internal(prob: Problem) -> np.ndarray:
     if err:
         raise RuntimeError(err)
     return out
+
+
+# ----------------------------------------------------------------------------- dense HMM
+# forward_alg / backward_alg / sample_hmm_posterior (argweaverc.py:42-56, hmm.cpp:27-85):
+# the tables are filled in place, as the reference's c_out matrices are.
+
+def _double_rows(a: np.ndarray, name: str):
+    if a.dtype != np.float64 or a.ndim != 2 or not a.flags.c_contiguous:
+        raise ValueError(f"{name} must be a C-contiguous 2-D float64 array")
+    return (capi.c_double_p * a.shape[0])(*[a[i].ctypes.data_as(capi.c_double_p)
+                                           for i in range(a.shape[0])])
+
+
+def _dense_check(trans: np.ndarray, tab: np.ndarray):
+    S = tab.shape[1]
+    if trans.shape != (S, S):
+        raise ValueError("trans must be nstates x nstates")
+    return tab.shape[0], S
+
+
+def forward_alg(trans: np.ndarray, emit: np.ndarray, fw: np.ndarray) -> np.ndarray:
+    """Fill fw[1:] from fw[0] (the caller's) in place; log-space tables, n x nstates."""
+    n, S = _dense_check(trans, fw)
+    if emit.shape != fw.shape:
+        raise ValueError("emit must have the shape of fw")
+    capi.load().forward_alg(n, S, _double_rows(trans, "trans"), _double_rows(emit, "emit"),
+                            _double_rows(fw, "fw"))
+    err = capi.last_error()
+    if err:
+        raise RuntimeError(err)
+    return fw
+
+
+def backward_alg(trans: np.ndarray, emit: np.ndarray, bw: np.ndarray) -> np.ndarray:
+    """Fill bw[:-1] from bw[-1] (the caller's) in place."""
+    n, S = _dense_check(trans, bw)
+    if emit.shape != bw.shape:
+        raise ValueError("emit must have the shape of bw")
+    capi.load().backward_alg(n, S, _double_rows(trans, "trans"), _double_rows(emit, "emit"),
+                             _double_rows(bw, "bw"))
+    err = capi.last_error()
+    if err:
+        raise RuntimeError(err)
+    return bw
+
+
+def sample_hmm_posterior(trans: np.ndarray, fw: np.ndarray, path: np.ndarray) -> np.ndarray:
+    """Fill path[:-1] from path[-1] (the caller's) in place, one rand() per column."""
+    n, S = _dense_check(trans, fw)
+    if path.dtype != np.int32 or path.shape != (n,) or not path.flags.c_contiguous:
+        raise ValueError("path must be a contiguous int32 array of n entries")
+    capi.load().sample_hmm_posterior(n, S, _double_rows(trans, "trans"), _double_rows(fw, "fw"),
+                                     path.ctypes.data_as(capi.c_int_p))
+    err = capi.last_error()
+    if err:
+        raise RuntimeError(err)
+    return path

@@ -94,6 +94,15 @@ void delete_path(int *path);
 void delete_double_matrix(double **mat, int nrows);
 void delete_forward_matrix(double **mat, int nrows);
 
+/* The dense HMM over a full nstates x nstates log transition matrix (hmm.h:14-19,
+ * hmm.cpp:27-85; bound by argweaver/argweaverc.py:42-56). Tables are n row pointers of
+ * nstates doubles, in natural log. As in the reference the caller fills the boundary:
+ * fw[0] before forward_alg, bw[n-1] before backward_alg, path[n-1] before
+ * sample_hmm_posterior, which draws one rand() per column from n-2 down to 0. */
+void forward_alg(int n, int nstates, double **trans, double **emit, double **fw);
+void backward_alg(int n, int nstates, double **trans, double **emit, double **bw);
+void sample_hmm_posterior(int n, int nstates, double **trans, double **fw, int *path);
+
 /* ---------------------------------------------------------------------------------
  * Flat batch API
  * --------------------------------------------------------------------------------- */

@@ -1684,4 +1684,69 @@ int oracle_emissions(const oracle_problem *p, double *emit_out) {
     return 0;
 }
 
+// ----------------------------------------------------------------------------- dense HMM
+// The reference's generic HMM over a full log transition matrix (hmm.cpp:27-85), tables
+// row-major n x S. Each entry is a logsum over one row or column, as common.h:182-202:
+// the maximum, then the terms within e^-15 of it summed in index order.
+
+static double dense_logsum(const double *v, int n) {
+    double mx = v[0];
+    for (int i = 1; i < n; i++) mx = v[i] > mx ? v[i] : mx;
+    double s = 0.0;
+    for (int i = 0; i < n; i++)
+        if (v[i] - mx > -15.0) s += std::exp(v[i] - mx);
+    return mx + std::log(s);
+}
+
+int oracle_dense_forward(int n, int S, const double *trans, const double *emit, double *fw) {
+    if (n < 1 || S < 1) return -1;
+    vector<double> v(S);
+    for (int i = 1; i < n; i++)
+        for (int k = 0; k < S; k++) {
+            for (int j = 0; j < S; j++) v[j] = fw[(size_t)(i - 1) * S + j] + trans[(size_t)j * S + k];
+            fw[(size_t)i * S + k] = dense_logsum(v.data(), S) + emit[(size_t)i * S + k];
+        }
+    return 0;
+}
+
+int oracle_dense_backward(int n, int S, const double *trans, const double *emit, double *bw) {
+    if (n < 1 || S < 1) return -1;
+    vector<double> v(S);
+    for (int i = n - 2; i >= 0; i--)
+        for (int j = 0; j < S; j++) {
+            for (int k = 0; k < S; k++)
+                v[k] = trans[(size_t)j * S + k] + bw[(size_t)(i + 1) * S + k] +
+                       emit[(size_t)(i + 1) * S + k];
+            bw[(size_t)i * S + j] = dense_logsum(v.data(), S);
+        }
+    return 0;
+}
+
+// path[n-1] is given; u[i] is the uniform of column i (the reference draws them from n-2
+// down to 0). The pick is the first index whose running weight reaches u[i] times the
+// weights' sum (common.h:272-290).
+int oracle_dense_sample(int n, int S, const double *trans, const double *fw, const double *u,
+                        int *path) {
+    if (n < 1 || S < 1) return -1;
+    vector<double> a(S);
+    for (int i = n - 2; i >= 0; i--) {
+        const int k = path[i + 1];
+        if (k < 0 || k >= S) return -2;
+        for (int j = 0; j < S; j++) a[j] = fw[(size_t)i * S + j] + trans[(size_t)j * S + k];
+        const double total = dense_logsum(a.data(), S);
+        double sum = 0.0;
+        for (int j = 0; j < S; j++) sum += (a[j] = std::exp(a[j] - total));
+        const double pick = u[i] * sum;
+        double run = 0.0;
+        int pickj = S - 1;
+        for (int j = 0; j < S; j++) {
+            run += a[j];
+            if (run >= pick) { pickj = j; break; }
+        }
+        path[i] = pickj;
+    }
+    return 0;
+}
+
 }  // extern "C"
+

@@ -66,6 +66,14 @@ int oracle_emissions(const oracle_problem *p, double *emit);
 int oracle_debug_tables(const oracle_problem *p, double *tm, double *gts, double *inv,
                         double *prior);
 
+/* The dense HMM over a full log transition matrix trans[S][S] (hmm.cpp:27-85), tables
+ * row-major n x S: fill fw[1..n-1] from fw[0]; bw[0..n-2] from bw[n-1]; path[0..n-2] from
+ * path[n-1] with u[i] the uniform of column i. */
+int oracle_dense_forward(int n, int S, const double *trans, const double *emit, double *fw);
+int oracle_dense_backward(int n, int S, const double *trans, const double *emit, double *bw);
+int oracle_dense_sample(int n, int S, const double *trans, const double *fw, const double *u,
+                        int *path);
+
 /* Total cells: sum over columns of max(nstates,1). */
 long long oracle_cells(const oracle_problem *p);
 

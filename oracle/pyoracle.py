@@ -50,7 +50,10 @@ def load():
                            ("oracle_block_terms", [P, C.c_void_p, C.c_void_p]),
                            ("oracle_emissions", [P, C.c_void_p]),
                            ("oracle_debug_tables", [P, C.c_void_p, C.c_void_p, C.c_void_p,
-                                                    C.c_void_p])]:
+                                                    C.c_void_p]),
+                           ("oracle_dense_forward", [C.c_int, C.c_int] + [C.c_void_p] * 3),
+                           ("oracle_dense_backward", [C.c_int, C.c_int] + [C.c_void_p] * 3),
+                           ("oracle_dense_sample", [C.c_int, C.c_int] + [C.c_void_p] * 4)]:
             fn = getattr(lib, name)
             fn.restype = C.c_int
             fn.argtypes = args
@@ -213,3 +216,39 @@ def rand_uniforms(seed: int, n: int) -> np.ndarray:
     rmax = 2147483647.0  # glibc RAND_MAX
     draws = np.array([libc.rand() / rmax for _ in range(n)], dtype=np.float64)
     return draws[::-1].copy()
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def dense_forward(trans, emit, fw0) -> np.ndarray:
+    """The dense forward table (hmm.cpp:27-43) from its first column fw0."""
+    trans, emit = _f64(trans), _f64(emit)
+    fw = np.zeros_like(emit)
+    fw[0] = fw0
+    _check(load().oracle_dense_forward(emit.shape[0], emit.shape[1], trans.ctypes.data,
+                                       emit.ctypes.data, fw.ctypes.data), "dense forward")
+    return fw
+
+
+def dense_backward(trans, emit, bwlast) -> np.ndarray:
+    """The dense backward table (hmm.cpp:48-64) from its last column bwlast."""
+    trans, emit = _f64(trans), _f64(emit)
+    bw = np.zeros_like(emit)
+    bw[-1] = bwlast
+    _check(load().oracle_dense_backward(emit.shape[0], emit.shape[1], trans.ctypes.data,
+                                        emit.ctypes.data, bw.ctypes.data), "dense backward")
+    return bw
+
+
+def dense_sample(trans, fw, u, last: int) -> np.ndarray:
+    """A path drawn by sample_hmm_posterior (hmm.cpp:67-85) with uniforms u by column."""
+    trans, fw, u = _f64(trans), _f64(fw), _f64(u)
+    path = np.zeros(fw.shape[0], dtype=np.int32)
+    path[-1] = last
+    _check(load().oracle_dense_sample(fw.shape[0], fw.shape[1], trans.ctypes.data,
+                                      fw.ctypes.data, u.ctypes.data, path.ctypes.data),
+           "dense sample")
+    return path
+

@@ -11,9 +11,15 @@
 //                                    penalty, the model's infsites_penalty (emit.cpp:847-862)
 //   tables  <problem> <out>          per-block TransMatrix terms (trans.cpp:26),
 //                                    TransMatrixSwitch (trans.cpp:538), emissions (emit.cpp:650)
-//   dense   <problem> <out>          single-block problems: the reference's dense log-space
+//   dense   <problem> <out> <seed>   single-block problems: the reference's dense log-space
 //                                    backward_alg (hmm.cpp:48) on calc_transition_probs
-//                                    (trans.cpp:136) + calc_emissions, for the backward oracle
+//                                    (trans.cpp:136) + calc_emissions, for the backward oracle;
+//                                    its forward_alg (hmm.cpp:26) and sample_hmm_posterior
+//                                    (hmm.cpp:76) after srand(seed)
+//   densernd <S> <n> <seed> <out>    the dense HMM (hmm.cpp:27-85) on a random S-state
+//                                    matrix (about a tenth of the entries zero) and random
+//                                    emissions, inputs from a fixed integer hash: forward_alg,
+//                                    backward_alg, then a path after srand(seed)
 //   sim1    <sites> <smc> <c> <out>  reads a sites file + SMC ARG the way arg-sample does
 //                                    (arg-sample.cpp:996-1155), removes the last sequence's
 //                                    thread (thread.cpp:425) and writes the external problem
@@ -296,7 +302,7 @@ static int cmd_tables(const char *in, const char *out) {
 }
 
 // Dense log-space backward of the reference's generic HMM on one block.
-static int cmd_dense(const char *in, const char *out) {
+static int cmd_dense(const char *in, const char *out, int seed) {
     Problem p = read_problem(in);
     if (p.ntrees != 1 || p.internal) die("dense: single external tree only");
     LocalTrees *trees = make_trees(p);
@@ -317,17 +323,92 @@ static int cmd_dense(const char *in, const char *out) {
     double **bw = new_matrix<double>(p.seqlen, S);
     for (int k = 0; k < S; k++) bw[p.seqlen - 1][k] = 0.0;
     backward_alg(p.seqlen, S, trans, emit, bw);
+    // the dense forward (first column: the log emissions) and a path drawn from it after
+    // srand(seed): the last column from its normalised weights, the rest by
+    // sample_hmm_posterior (hmm.cpp:76-95), one rand() per column, last column first
+    double **fw = new_matrix<double>(p.seqlen, S);
+    for (int k = 0; k < S; k++) fw[0][k] = emit[0][k];
+    forward_alg(p.seqlen, S, trans, emit, fw);
+    srand(seed);
+    vector<int> path(p.seqlen);
+    {
+        vector<double> A(S);
+        const double total = logsum(fw[p.seqlen - 1], S);
+        for (int k = 0; k < S; k++) A[k] = exp(fw[p.seqlen - 1][k] - total);
+        path[p.seqlen - 1] = sample(A.data(), S);
+    }
+    sample_hmm_posterior(p.seqlen, S, trans, fw, path.data());
     FILE *f = fopen(out, "wb");
     if (!f) die("cannot write output");
-    wr(f, "AWGDNS02", 8);
+    wr(f, "AWGDNS03", 8);
     int hdr[2] = {p.seqlen, S};
     wr(f, hdr, 2);
     for (int i = 0; i < p.seqlen; i++) wr(f, bw[i], S);
     for (int i = 0; i < S; i++) wr(f, trans[i], S);      // log transition matrix
     for (int i = 0; i < p.seqlen; i++) wr(f, emit[i], S); // log emissions
+    for (int i = 0; i < p.seqlen; i++) wr(f, fw[i], S);   // dense forward
+    wr(f, path.data(), p.seqlen);
     fclose(f);
     delete_matrix(trans, S); delete_matrix(emit, p.seqlen); delete_matrix(bw, p.seqlen);
+    delete_matrix(fw, p.seqlen);
     delete trees;
+    return 0;
+}
+
+// uniform in [0, 1) from an integer hash of (a, b, c): the random fixture's inputs
+static double hash01(unsigned a, unsigned b, unsigned c) {
+    unsigned long long x = 0x9E3779B97F4A7C15ull * (a + 1) ^ 0xC2B2AE3D27D4EB4Full * (b + 7) ^
+                           0x165667B19E3779F9ull * (c + 13);
+    x ^= x >> 31; x *= 0xBF58476D1CE4E5B9ull; x ^= x >> 27; x *= 0x94D049BB133111EBull;
+    x ^= x >> 33;
+    return (double)(x >> 11) / 9007199254740992.0;
+}
+
+static int cmd_densernd(int S, int n, int seed, const char *out) {
+    if (S < 1 || n < 2) die("densernd: S >= 1 and n >= 2");
+    double **trans = new_matrix<double>(S, S);
+    for (int j = 0; j < S; j++) {
+        double tot = 0.0;
+        vector<double> w(S);
+        for (int k = 0; k < S; k++) {
+            const double h = hash01(seed, j, k);
+            w[k] = (k != j && h < 0.1) ? 0.0 : 0.05 + h;
+            tot += w[k];
+        }
+        for (int k = 0; k < S; k++) trans[j][k] = log(w[k] / tot);
+    }
+    double **emit = new_matrix<double>(n, S);
+    for (int i = 0; i < n; i++)
+        for (int k = 0; k < S; k++) emit[i][k] = log(0.01 + hash01(seed + 1000, i, k));
+    double **fw = new_matrix<double>(n, S), **bw = new_matrix<double>(n, S);
+    for (int k = 0; k < S; k++) {
+        fw[0][k] = emit[0][k] - log((double)S);
+        bw[n - 1][k] = 0.0;
+    }
+    forward_alg(n, S, trans, emit, fw);
+    backward_alg(n, S, trans, emit, bw);
+    srand(seed);
+    vector<int> path(n);
+    {
+        vector<double> A(S);
+        const double total = logsum(fw[n - 1], S);
+        for (int k = 0; k < S; k++) A[k] = exp(fw[n - 1][k] - total);
+        path[n - 1] = sample(A.data(), S);
+    }
+    sample_hmm_posterior(n, S, trans, fw, path.data());
+    FILE *f = fopen(out, "wb");
+    if (!f) die("cannot write output");
+    wr(f, "AWGDNS03", 8);
+    int hdr[2] = {n, S};
+    wr(f, hdr, 2);
+    for (int i = 0; i < n; i++) wr(f, bw[i], S);
+    for (int i = 0; i < S; i++) wr(f, trans[i], S);
+    for (int i = 0; i < n; i++) wr(f, emit[i], S);
+    for (int i = 0; i < n; i++) wr(f, fw[i], S);
+    wr(f, path.data(), n);
+    fclose(f);
+    delete_matrix(trans, S); delete_matrix(emit, n); delete_matrix(bw, n);
+    delete_matrix(fw, n);
     return 0;
 }
 
@@ -404,7 +485,9 @@ int main(int argc, char **argv) {
     if (cmd == "forward" && argc == 6)
         return cmd_forward(argv[2], argv[3], atoi(argv[4]), atof(argv[5]));
     if (cmd == "tables" && argc == 4) return cmd_tables(argv[2], argv[3]);
-    if (cmd == "dense" && argc == 4) return cmd_dense(argv[2], argv[3]);
+    if (cmd == "dense" && argc == 5) return cmd_dense(argv[2], argv[3], atoi(argv[4]));
+    if (cmd == "densernd" && argc == 6)
+        return cmd_densernd(atoi(argv[2]), atoi(argv[3]), atoi(argv[4]), argv[5]);
     if (cmd == "sim1" && argc == 6) return cmd_sim1(argv[2], argv[3], atoi(argv[4]), argv[5]);
     if (cmd == "cut" && argc == 5) return cmd_cut(argv[2], atoi(argv[3]), argv[4]);
     die("bad arguments");

@@ -4,6 +4,7 @@ Run where the reference checkout exists (default /root/reference, or $AWG_REFERE
 
     python tests/golden/make_golden.py            # all fixtures
     python tests/golden/make_golden.py infsites   # only the infinite-sites ones
+    python tests/golden/make_golden.py dense      # only the dense-HMM ones
 
 It builds the reference from its own sources (oracle/Makefile target ``ref``), writes
 each problem as an AWGPROB1 file and runs the reference's threading HMM on it through
@@ -23,6 +24,12 @@ the log transition matrix (calc_transition_probs, trans.cpp:136) and log emissio
   dense_bw     f64   [L, S]
   dense_trans  f64   [S, S]
   dense_emit   f64   [L, S]
+  dense_fw     f64   [L, S]   the reference's dense forward_alg (first column: dense_emit[0])
+  dense_path   int32 [L]      a path drawn from it after srand(seed) (sample_hmm_posterior)
+
+``densehmm/s<S>_n<n>.npz`` hold the same dense_* arrays (and seed) for the generic HMM of
+hmm.cpp run on random S-state matrices with zero entries (harness command densernd); their
+first forward column is dense_emit[0] - log(S), the last backward column zero.
 
 Sources of the problems: examples/sim1 (the reference's bundled data, converted by
 the harness the way arg-sample reads it), the seeded DSMC generator of this project
@@ -71,13 +78,15 @@ def read_ref(path: str):
 
 def read_dense(path: str):
     d = open(path, "rb").read()
-    assert d[:8] == b"AWGDNS02"
+    assert d[:8] == b"AWGDNS03"
     L, S = (int(x) for x in np.frombuffer(d, np.int32, 2, 8))
     off = 16
     bw = np.frombuffer(d, np.float64, L * S, off).reshape(L, S).copy(); off += 8 * L * S
     trans = np.frombuffer(d, np.float64, S * S, off).reshape(S, S).copy(); off += 8 * S * S
-    emit = np.frombuffer(d, np.float64, L * S, off).reshape(L, S).copy()
-    return bw, trans, emit
+    emit = np.frombuffer(d, np.float64, L * S, off).reshape(L, S).copy(); off += 8 * L * S
+    fw = np.frombuffer(d, np.float64, L * S, off).reshape(L, S).copy(); off += 8 * L * S
+    path = np.frombuffer(d, np.int32, L, off).copy()
+    return bw, trans, emit, fw, path
 
 
 def summarize(ns, fw):
@@ -111,8 +120,9 @@ def make(name: str, prob_path: str, seed: int, tmp: str, dense: bool = False,
     extra = {}
     if dense:
         dout = os.path.join(tmp, name + ".dense")
-        run("dense", prob_path, dout)
-        extra["dense_bw"], extra["dense_trans"], extra["dense_emit"] = read_dense(dout)
+        run("dense", prob_path, dout, seed)
+        (extra["dense_bw"], extra["dense_trans"], extra["dense_emit"], extra["dense_fw"],
+         extra["dense_path"]) = read_dense(dout)
     if penalty < 1.0:
         extra["infsites_penalty"] = penalty
     u = pyoracle.rand_uniforms(seed, prob.seqlen)
@@ -133,6 +143,28 @@ def first_tree(prob: Problem) -> Problem:
                    ptrees=prob.ptrees[:1].copy(), ages=prob.ages[:1].copy(),
                    sprs=prob.sprs[:1].copy(), blocklens=prob.blocklens[:1].copy(),
                    seqs=prob.seqs[:, :L].copy(), internal=prob.internal)
+
+
+def dense(tmp):
+    """Single-tree problems with the reference's dense HMM (hmm.cpp): backward, forward and
+    a sampled path."""
+    for seed in (41, 43):
+        prob = first_tree(simulate(6, 400, seed))
+        p = os.path.join(tmp, "p.prob"); prob.save(p)
+        make(f"single_k7_s{seed}", p, seed, tmp, dense=True)
+
+
+def densernd(tmp):
+    """The dense HMM (hmm.cpp) on random matrices with zero entries: S = 37 (a warp and a
+    few states) and S = 5 (fewer states than a warp)."""
+    for S, n, seed in ((37, 160, 7), (5, 64, 9)):
+        out = os.path.join(tmp, "d.bin")
+        run("densernd", S, n, seed, out)
+        bw, trans, emit, fw, path = read_dense(out)
+        os.makedirs(os.path.join(HERE, "densehmm"), exist_ok=True)
+        np.savez_compressed(os.path.join(HERE, "densehmm", f"s{S}_n{n}.npz"), seed=seed,
+                            dense_bw=bw, dense_trans=trans, dense_emit=emit, dense_fw=fw,
+                            dense_path=path)
 
 
 def infsites(tmp):
@@ -158,6 +190,11 @@ def main():
     if sys.argv[1:] == ["infsites"]:
         with tempfile.TemporaryDirectory() as tmp:
             infsites(tmp)
+        return
+    if sys.argv[1:] == ["dense"]:
+        with tempfile.TemporaryDirectory() as tmp:
+            dense(tmp)
+            densernd(tmp)
         return
     with tempfile.TemporaryDirectory() as tmp:
         infsites(tmp)
@@ -192,11 +229,8 @@ def main():
             run("cut", pf, seed, pc)
             make(f"cut_k10_s{seed}", pc, 500 + seed, tmp)
 
-        # single-tree problems with the reference's dense backward
-        for seed in (41, 43):
-            prob = first_tree(simulate(6, 400, seed))
-            p = os.path.join(tmp, "p.prob"); prob.save(p)
-            make(f"single_k7_s{seed}", p, seed, tmp, dense=True)
+        dense(tmp)
+        densernd(tmp)
 
 
 if __name__ == "__main__":

@@ -95,6 +95,38 @@ def test_backward_matches_dense_reference(name):
         np.testing.assert_allclose(bw[off[i]:off[i + 1]], d, rtol=2e-3, atol=0)
 
 
+@pytest.mark.parametrize("name", [n for n in NAMES if n.startswith("single_")])
+def test_dense_hmm_matches_reference(name):
+    # the generic HMM of hmm.cpp over the reference's own dense matrix and emissions: the
+    # restatement follows its operation order, so the tables and the drawn path agree
+    _, gold = load(name)
+    trans, emit = gold["dense_trans"], gold["dense_emit"]
+    fw = pyoracle.dense_forward(trans, emit, emit[0])
+    np.testing.assert_allclose(fw, gold["dense_fw"], rtol=1e-13, atol=0)
+    bw = pyoracle.dense_backward(trans, emit, np.zeros(trans.shape[0]))
+    np.testing.assert_allclose(bw, gold["dense_bw"], rtol=1e-13, atol=1e-300)
+    L = emit.shape[0]
+    u = pyoracle.rand_uniforms(int(gold["seed"]), L)  # u[L-1] drew the last column
+    path = pyoracle.dense_sample(trans, gold["dense_fw"], u, int(gold["dense_path"][-1]))
+    np.testing.assert_array_equal(path, gold["dense_path"])
+
+
+@pytest.mark.parametrize("name", ["s37_n160", "s5_n64"])
+def test_dense_hmm_random_matrices_match_reference(name):
+    gold = np.load(os.path.join(GOLDEN, "densehmm", name + ".npz"))
+    trans, emit = gold["dense_trans"], gold["dense_emit"]
+    S = trans.shape[0]
+    assert np.isinf(trans).any() or S < 10  # zero transitions reach the logsum as -inf
+    fw = pyoracle.dense_forward(trans, emit, emit[0] - np.log(S))
+    np.testing.assert_allclose(fw, gold["dense_fw"], rtol=1e-13, atol=0)
+    bw = pyoracle.dense_backward(trans, emit, np.zeros(S))
+    np.testing.assert_allclose(bw, gold["dense_bw"], rtol=1e-13, atol=1e-300)
+    u = pyoracle.rand_uniforms(int(gold["seed"]), emit.shape[0])
+    path = pyoracle.dense_sample(trans, gold["dense_fw"], u, int(gold["dense_path"][-1]))
+    np.testing.assert_array_equal(path, gold["dense_path"])
+    assert len(set(path.tolist())) > S // 2
+
+
 @pytest.mark.parametrize("name", NAMES)
 def test_posterior_properties(name):
     prob, gold = load(name)

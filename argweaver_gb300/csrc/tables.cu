@@ -342,11 +342,6 @@ __device__ double calc_recomb_recoal(const SwitchCtx &c, const int *spr, int sta
     return p;
 }
 
-__device__ __forceinline__ double prob_branch(double t, double mu, bool mut) {  // emit.cpp:86
-    const double f = 4. / 3.;
-    if (!mut) return .25 * (1.0 + 3. * exp(-f * mu * t));
-    return .25 * (1.0 - exp(-f * mu * t));
-}
 
 
 // ---------------------------------------------------------------------------------------
@@ -1465,9 +1460,74 @@ __device__ void block_log_offset(const BatchDev &d, const BlockDev &B, const Ins
 }
 
 // Variant-column emissions of one local tree, by the whole CTA (nwarps warps).
+// exp(-4/3 mu t), the exponential of prob_branch (emit.cpp:86-93), and the branch
+// probabilities formed from it exactly as prob_branch forms them
+__device__ __forceinline__ double branch_exp(double t, double mu) { return exp(-(4. / 3.) * mu * t); }
+__device__ __forceinline__ double branch_mut(double e) { return .25 * (1.0 - e); }
+__device__ __forceinline__ double branch_nomut(double e) { return .25 * (1.0 + 3. * e); }
+
+// The branch exponentials of one instance: every branch length K2 forms is a difference
+// of two time points (or of a time point and 0) floored at mintime, so the exponentials
+// are tabulated once per instance, not once per state: e[i][j] for max(times[j] -
+// times[i], mintime), e0[j] for max(times[j] - 0, mintime), ez[j] for max(0 - times[j],
+// mintime). A persistent CTA keeps the table of the instance it last served.
+struct BranchCache {
+    int inst;
+    double e[MAXT][MAXT], e0[MAXT], ez[MAXT];
+};
+
+// Nodes bucketed by key (key < 0: left out), by one warp: list holds the nodes level by
+// level, ascending node index within a level; ptr[l] is the start of level l and
+// ptr[nlev] the end (nlev = largest key + 1, returned). cursor: n ints of scratch.
+__device__ int warp_levels(const int *key, int n, int *list, int *ptr, int *cursor, int lane) {
+    int kmax = -1;
+    for (int i = lane; i < n; i += 32) kmax = max(kmax, key[i]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) kmax = max(kmax, __shfl_xor_sync(0xffffffffu, kmax, o));
+    const int nlev = kmax + 1;
+    for (int l = lane; l <= nlev; l += 32) ptr[l] = 0;
+    __syncwarp();
+    const unsigned lt = (1u << lane) - 1u;
+    for (int base = 0; base < n; base += 32) {  // counts of level l into ptr[l + 1]
+        const int k = base + lane < n ? key[base + lane] : -1;
+        const unsigned m = __match_any_sync(0xffffffffu, k);
+        if (k >= 0 && (m & lt) == 0) ptr[k + 1] += __popc(m);
+        __syncwarp();
+    }
+    int carry = 0;  // prefix sums: ptr[l] = nodes on levels below l
+    for (int b = 0; b <= nlev; b += 32) {
+        const int l = b + lane;
+        int v = l <= nlev ? ptr[l] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, v, o);
+            if (lane >= o) v += y;
+        }
+        if (l <= nlev) ptr[l] = v + carry;
+        if (l < nlev) cursor[l] = v + carry;
+        carry += __shfl_sync(0xffffffffu, v, 31);
+    }
+    __syncwarp();
+    for (int base = 0; base < n; base += 32) {
+        const int i = base + lane;
+        const int k = i < n ? key[i] : -1;
+        const unsigned m = __match_any_sync(0xffffffffu, k);
+        const int leader = __ffs(m) - 1;
+        int pos = 0;
+        if (k >= 0 && lane == leader) {
+            pos = cursor[k];
+            cursor[k] = pos + __popc(m);
+        }
+        pos = __shfl_sync(0xffffffffu, pos, leader);
+        if (k >= 0) list[pos + __popc(m & lt)] = i;
+        __syncwarp();
+    }
+    return nlev;
+}
+
 template <bool FP32OUT>
 __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwarps, int maxS,
-                                             int smem_bytes) {
+                                             int smem_bytes, BranchCache *bc) {
     extern __shared__ int4 dyn[];
     const BlockDev B = d.blocks[blk];
     if (B.nvar == 0 || B.S == 0) {
@@ -1491,7 +1551,7 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
     double *muts = (double *)align16(nd + n);
     double *nomuts = muts + n;
     double *pm = (double *)align16(nomuts + n);  // [S][6]: mut0..2, nomut0..2 per state
-    int *order = (int *)align16(pm + (size_t)6 * maxS);
+    int *order = (int *)align16(pm + (size_t)6 * maxS);  // level cursors
     int *hgt = order + n;                        // height, then depth scratch
     int *snode = hgt + n;                        // [maxS]
     int *inl = snode + maxS;                     // nodes by height
@@ -1535,16 +1595,31 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
     const double mu = model[M_CONST + 1], mintime = model[M_CONST + 2];
     const double penalty = model[M_CONST + 3];  // infinite-sites penalty, 1: off
     for (int i = tid; i < n; i += blockDim.x) nd[i] = d.nodes[B.nodes0 + i];
+    const bool refill = bc->inst != B.inst;  // read by all before anyone rewrites it
     __syncthreads();
+    if (refill) {
+        for (int e = tid; e < T * T; e += blockDim.x) {
+            const int i = e / T, j = e % T;
+            bc->e[i][j] = branch_exp(fmax(times[j] - times[i], mintime), mu);
+        }
+        for (int j = tid; j < T; j += blockDim.x) {
+            bc->e0[j] = branch_exp(fmax(times[j] - 0.0, mintime), mu);
+            bc->ez[j] = branch_exp(fmax(0.0 - times[j], mintime), mu);
+        }
+        if (tid == 0) bc->inst = B.inst;
+        __syncthreads();
+    }
     const int root = B.root;
     for (int i = tid; i < n; i += blockDim.x) {  // prob_tree_mutation (emit.cpp:97-116)
         double m1 = 0.0, m0 = 0.0;
         if (i != root) {
-            const int pa = nd[nd[i].x].w;
+            const int pa = nd[nd[i].x].w, ag = nd[i].w;
             if (pa != T + 1) {
-                const double t = fmax(times[pa] - times[nd[i].w], mintime);
-                m1 = prob_branch(t, mu, true);
-                m0 = prob_branch(t, mu, false);
+                const double e = (pa < T && ag < T)
+                                     ? bc->e[ag][pa]
+                                     : branch_exp(fmax(times[pa] - times[ag], mintime), mu);
+                m1 = branch_mut(e);
+                m0 = branch_nomut(e);
             }
         }
         muts[i] = m1;
@@ -1556,23 +1631,28 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
     }
     const int mainr = internal ? nd[root].z : root;
     const int node1 = internal ? nd[root].y : 0;
-    const double time1 = internal ? times[nd[node1].w] : 0.0;
+    const int age1 = nd[node1].w;
+    const double time1 = internal ? times[age1] : 0.0;
     const StateInfo *sinfo = d.sinfo + B.state0;
     for (int k = tid; k < S; k += blockDim.x) {  // per-state split branches (emit.cpp:782-805)
-        const int node2 = sinfo[k].node;
+        const int node2 = sinfo[k].node, a = sinfo[k].time;
         snode[k] = node2;
-        const int parent = nd[node2].x;
-        const double time2 = times[nd[node2].w];
-        const double parent_time = (parent != -1) ? times[min(nd[parent].w, T - 1)] : 0.0;
-        const double coal_time = times[sinfo[k].time];
-        double dist[3];
-        dist[0] = fmax(coal_time - time1, mintime);
-        dist[1] = fmax(coal_time - time2, mintime);
-        dist[2] = fmax(parent_time - coal_time, mintime);
+        const int parent = nd[node2].x, age2 = nd[node2].w;
+        const int pidx = parent != -1 ? min(nd[parent].w, T - 1) : -1;
+        const double time2 = times[age2];
+        const double parent_time = (parent != -1) ? times[pidx] : 0.0;
+        const double coal_time = times[a];
         sfloor[k] = (coal_time - time2 < mintime) || (parent_time - coal_time < mintime);
+        // the three branch exponentials, each the table entry of the same difference
+        double e[3];
+        e[0] = !internal ? bc->e0[a]
+             : age1 < T  ? bc->e[age1][a]
+                         : branch_exp(fmax(coal_time - time1, mintime), mu);
+        e[1] = age2 < T ? bc->e[age2][a] : branch_exp(fmax(coal_time - time2, mintime), mu);
+        e[2] = parent != -1 ? bc->e[a][pidx] : bc->ez[a];
         for (int x = 0; x < 3; x++) {
-            pm[6 * k + x] = prob_branch(dist[x], mu, true);
-            pm[6 * k + 3 + x] = prob_branch(dist[x], mu, false);
+            pm[6 * k + x] = branch_mut(e[x]);
+            pm[6 * k + 3 + x] = branch_nomut(e[x]);
         }
         if (FP32OUT) {
             for (int x = 0; x < 6; x++) pm32[8 * k + x] = (float)pm[6 * k + x];
@@ -1580,54 +1660,37 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
             pm32[8 * k + 7] = 0.f;
         }
     }
-    if (tid == 0) {
-        // postorder (local_tree.h:274-304)
-        int i;
-        for (i = 0; i < n; i++) hgt[i] = 0;
-        for (i = 0; i < n; i++) {
-            if (nd[i].y != -1) break;
-            order[i] = i;
+    // level schedules: heights (longest path down to a leaf; leaves 0), then the depth below
+    // the main root (-1 outside its subtree), each bucketed by one warp. Walks are bounded
+    // by n steps.
+    for (int i = tid; i < n; i += blockDim.x) hgt[i] = 0;
+    __syncthreads();
+    for (int i = tid; i < n; i += blockDim.x) {
+        if (nd[i].y != -1) continue;
+        int v = i;
+        for (int dd = 1; dd <= n && nd[v].x != -1; dd++) {
+            v = nd[v].x;
+            atomicMax(&hgt[v], dd);
         }
-        int end = i;
-        for (i = 0; i < n; i++) {
-            const int p = nd[order[i]].x;
-            if (p != -1) {
-                hgt[p]++;
-                if (hgt[p] == 2) order[end++] = p;
-            }
+    }
+    __syncthreads();
+    if (warp == 0) {
+        const int nl = warp_levels(hgt, n, inl, inp, order, lane);
+        if (lane == 0) nlev_in = nl;
+    }
+    __syncthreads();
+    for (int i = tid; i < n; i += blockDim.x) {
+        int v = i, dd = 0;
+        while (v != mainr && v != -1 && dd <= n) {
+            v = nd[v].x;
+            dd++;
         }
-        // heights (children first), then nodes bucketed by height
-        int H = 0;
-        for (i = 0; i < n; i++) {
-            const int j = order[i];
-            const int h = nd[j].y == -1 ? 0 : max(hgt[nd[j].y], hgt[nd[j].z]) + 1;
-            hgt[j] = h;
-            H = max(H, h);
-        }
-        for (int h = 0; h <= H + 1; h++) inp[h] = 0;
-        for (i = 0; i < n; i++) inp[hgt[i] + 1]++;
-        for (int h = 0; h <= H; h++) inp[h + 1] += inp[h];
-        for (i = 0; i < n; i++) inl[inp[hgt[i]]++] = i;  // inp[h] now holds level h's end
-        for (int h = H; h > 0; h--) inp[h] = inp[h - 1];
-        inp[0] = 0;
-        nlev_in = H + 1;
-        // depth below the main root (parents first: reverse postorder); -1 elsewhere
-        int D = 0;
-        for (i = n - 1; i >= 0; i--) {
-            const int j = order[i];
-            const int p = nd[j].x;
-            hgt[j] = j == mainr ? 0 : (p != -1 && hgt[p] >= 0) ? hgt[p] + 1 : -1;
-            D = max(D, hgt[j]);
-        }
-        for (int h = 0; h <= D + 1; h++) outp[h] = 0;
-        for (i = 0; i < n; i++)
-            if (hgt[i] >= 0) outp[hgt[i] + 1]++;
-        for (int h = 0; h <= D; h++) outp[h + 1] += outp[h];
-        for (i = 0; i < n; i++)
-            if (hgt[i] >= 0) outl[outp[hgt[i]]++] = i;
-        for (int h = D; h > 0; h--) outp[h] = outp[h - 1];
-        outp[0] = 0;
-        nlev_out = D + 1;
+        hgt[i] = v == mainr ? dd : -1;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        const int nl = warp_levels(hgt, n, outl, outp, order, lane);
+        if (lane == 0) nlev_out = nl;
     }
     __syncthreads();
 
@@ -1781,16 +1844,22 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
 
 template <bool FP32OUT>
 __global__ void k_varemit(BatchDev d, int nwarps, int maxS, int smem_bytes) {
-    varemit_tree<FP32OUT>(d, cta_block(d), nwarps, maxS, smem_bytes);
+    __shared__ BranchCache bc;
+    if (threadIdx.x == 0) bc.inst = -1;
+    __syncthreads();
+    varemit_tree<FP32OUT>(d, cta_block(d), nwarps, maxS, smem_bytes, &bc);
 }
 
 // K2 as a persistent kernel over the same units as k_tables_ws.
 template <bool FP32OUT>
 __global__ void k_varemit_ws(BatchDev d, int nwarps, int maxS, int smem_bytes, WorkQueue q) {
+    __shared__ BranchCache bc;
+    if (threadIdx.x == 0) bc.inst = -1;
+    __syncthreads();
     for (int u = next_unit(q); u >= 0; u = next_unit(q)) {
         const int t1 = imin((u + 1) * q.chunk, d.nblocks);
         for (int t = u * q.chunk; t < t1; t++) {
-            varemit_tree<FP32OUT>(d, d.blkmap ? d.blkmap[t] : t, nwarps, maxS, smem_bytes);
+            varemit_tree<FP32OUT>(d, d.blkmap ? d.blkmap[t] : t, nwarps, maxS, smem_bytes, &bc);
             __syncthreads();
         }
     }

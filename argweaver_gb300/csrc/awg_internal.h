@@ -72,6 +72,8 @@ struct StateInfo {
 // Device views of a batch (all pointers are device memory).
 struct BatchDev {
     int ninst, nblocks, maxS, maxT, maxnodes, maxM;
+    int emit64;                  // some instance forms FP64 emission partials even on the
+                                 // FP32 path (internal-branch or infinite-sites problems)
     const InstDev *inst;
     const int *order;            // [ninst] or NULL: CTA x of a per-instance kernel runs
                                  // instance order[x] (largest work first)

@@ -364,6 +364,10 @@ int ctx_launch(Ctx &C, const awg_problem *probs, awg_outputs *outs, int n, const
     d.ninst = plan.ninst; d.nblocks = plan.nblocks; d.maxS = plan.maxS; d.maxT = plan.maxT;
     d.maxnodes = plan.maxnodes;
     d.maxM = plan.maxM;
+    d.emit64 = 0;
+    for (int i = 0; i < plan.ninst; i++)
+        if (plan.inst[i].internal || plan.model[(size_t)i * MODEL_STRIDE + M_CONST + 3] < 1.0)
+            d.emit64 = 1;
     d.inst = (const InstDev *)(D + o_inst);
     d.order = (const int *)(D + o_order);
     d.blocks = (BlockDev *)(D + o_blocks);
@@ -525,7 +529,7 @@ int ctx_launch(Ctx &C, const awg_problem *probs, awg_outputs *outs, int n, const
                                           want_post, want_bw, want_bins, plan.ninst, plan.nblocks,
                                           plan.maxS, plan.maxT, plan.maxnodes, plan.maxM,
                                           cfg.kpt, cfg.chunk, cfg.group_div, cfg.persistent, ng,
-                                          (long long)total};
+                                          (long long)total, d.emit64};
             for (size_t o : {o_inst, o_blocks, o_model, o_nodes, o_map, o_seq, o_cls, o_cvar,
                              o_order, o_blkmap, o_u, o_sinfo, o_t2off, o_btptr, o_btperm, o_tm,
                              o_gts, o_inv, o_det, o_detp, o_srcs, o_rrow, o_crow, o_gptr, o_gidx,

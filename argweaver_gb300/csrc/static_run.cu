@@ -146,6 +146,10 @@ int run_static(const awg_problem *p, awg_outputs *out, int precision, cudaStream
     d.ninst = plan.ninst; d.nblocks = plan.nblocks; d.maxS = plan.maxS; d.maxT = plan.maxT;
     d.maxnodes = plan.maxnodes;
     d.maxM = plan.maxM;
+    d.emit64 = 0;
+    for (int i = 0; i < plan.ninst; i++)
+        if (plan.inst[i].internal || plan.model[(size_t)i * MODEL_STRIDE + M_CONST + 3] < 1.0)
+            d.emit64 = 1;
     d.inst = (const InstDev *)(D + o_inst);
     d.blocks = (BlockDev *)(D + o_blocks);
     d.model = (const double *)(D + o_model);

@@ -35,14 +35,22 @@ struct Terms {
         lnG4[MAXT], norecombs[MAXT];
     // the exponentials get_time needs, each evaluated once per tree:
     double EB[MAXT];              // exp(lnE2[b] + lnB[b-1]), b > 0
-    double E2B[MAXT][MAXT];       // [a][b] exp(lnE2[b] + lnB[a])
-    double E2N[MAXT][MAXT];       // [a][b] exp(lnE2[b] + lnNegG1[a])
-    double CT[MAXT][MAXT];        // [b][c] exp(lnG4[b] + lnB[c-1]), c > 0
+    // T x T tables in dynamic shared memory (row length ld = T), sized by the instance's T:
+    double *E2B;                  // [a][b] exp(lnE2[b] + lnB[a])
+    double *E2N;                  // [a][b] exp(lnE2[b] + lnNegG1[a])
+    double *CT;                   // [b][c] exp(lnG4[b] + lnB[c-1]), c > 0 (FP64 path only)
+    int ld;
     // FP32 path: the exponentials factor, exp(lnE2[b] + lnB[a]) = exp(lnE2[b]) exp(lnB[a])
     // and so on, so T of each are enough; dBN[a] = exp(lnB[a]) - exp(lnNegG1[a]) formed
     // without cancellation as exp(lnB[a]) (-expm1(lnNegG1[a] - lnB[a]))
     double eE2[MAXT], eB[MAXT], eG4[MAXT], dBN[MAXT];
 };
+
+// Doubles of K1's exponential tables in dynamic shared memory (kept a multiple of two, so
+// the int4 arrays after them stay 16-byte aligned).
+__host__ __device__ inline int exp_table_doubles(int T, bool want32) {
+    return ((want32 ? 2 : 3) * T * T + 1) & ~1;
+}
 
 // Fill the exponential tables (the same arguments get_time exponentiates), only the
 // entries get_time reads: E2B/E2N[a][b] for a < b (the a < b branch), CT[b][c] for
@@ -51,10 +59,10 @@ __device__ void exp_tables(Terms &t, int T) {
     for (int e = threadIdx.x; e < (T - 1) * (T - 1); e += blockDim.x) {
         const int a = e / (T - 1), b = e % (T - 1);
         if (a < b) {
-            t.E2B[a][b] = exp(t.lnE2[b] + t.lnB[a]);
-            t.E2N[a][b] = exp(t.lnE2[b] + t.lnNegG1[a]);
+            t.E2B[a * t.ld + b] = exp(t.lnE2[b] + t.lnB[a]);
+            t.E2N[a * t.ld + b] = exp(t.lnE2[b] + t.lnNegG1[a]);
         } else if (b < a) {
-            t.CT[a][b + 1] = exp(t.lnG4[a] + t.lnB[b]);  // [b=a][c=b+1]
+            t.CT[a * t.ld + b + 1] = exp(t.lnG4[a] + t.lnB[b]);  // [b=a][c=b+1]
         }
     }
     for (int b = threadIdx.x; b < T - 1; b += blockDim.x)
@@ -67,15 +75,16 @@ __device__ double get_time(const Terms &t, int a, int b, int c, int minage, bool
     if (a < minage || b < minage) return 0.0;
     double term1 = __dmul_rn(t.D[a], t.E[b]);
     double minage_term = 0.0;
-    if (minage > 0) minage_term = t.CT[b][minage];
+    if (minage > 0) minage_term = t.CT[b * t.ld + minage];
     const double eb = t.EB[b];
     if (!same_node) {
-        if (a < b) return term1 * (t.E2B[a][b] - t.E2N[a][b] - minage_term);
+        if (a < b) return term1 * (t.E2B[a * t.ld + b] - t.E2N[a * t.ld + b] - minage_term);
         if (a == b) return term1 * (eb + t.G3[b] - minage_term);
         return term1 * (eb + t.G2[b] - minage_term);
     }
-    double c_term = (c > 0 ? t.CT[b][c] : 0.0);
-    if (a < b) return term1 * (2 * (t.E2B[a][b] - t.E2N[a][b]) - c_term - minage_term);
+    double c_term = (c > 0 ? t.CT[b * t.ld + c] : 0.0);
+    if (a < b)
+        return term1 * (2 * (t.E2B[a * t.ld + b] - t.E2N[a * t.ld + b]) - c_term - minage_term);
     if (a == b) return term1 * ((2 * (eb + t.G3[b])) - c_term - minage_term) + t.norecombs[a];
     return term1 * ((2 * (eb + t.G2[b])) - c_term - minage_term);
 }
@@ -357,7 +366,8 @@ __device__ __forceinline__ void tables_tree(const BatchDev &d, int blk, int want
     const bool internal = I.internal != 0;
     const int tid = threadIdx.x;
 
-    int4 *cur = dyn;
+    double *dtab = (double *)dyn;  // the T x T exponential tables, then the tree arrays
+    int4 *cur = (int4 *)(dtab + exp_table_doubles(T, want32 != 0));
     int4 *prv = cur + n;
     int *first = (int *)(prv + n);
     int *t0 = first + n;
@@ -382,6 +392,12 @@ __device__ __forceinline__ void tables_tree(const BatchDev &d, int blk, int want
     __shared__ double tl_tab[2 * MAXT], inv_tab[2 * MAXT], dp_tab[3 * MAXT];
     __shared__ int sh_S, sh_S1, sh_minage, sh_rootage, sh_src[2];
 
+    if (tid == 0) {
+        tr.ld = T;
+        tr.E2B = dtab;
+        tr.E2N = dtab + T * T;
+        tr.CT = want32 ? nullptr : dtab + 2 * T * T;
+    }
     const double *model = d.model + I.model0;
     for (int i = tid; i < T; i += blockDim.x) {
         times[i] = model[M_TIMES + i];
@@ -569,8 +585,8 @@ __device__ __forceinline__ void tables_tree(const BatchDev &d, int blk, int want
             const double x = a < b ? tr.eE2[b] * tr.dBN[a] : eb + (a == b ? tr.G3[b] : tr.G2[b]);
             const double de = __dmul_rn(tr.D[a], tr.E[b]);
             const double mt = minage > 0 ? tr.eG4[b] * tr.eB[minage - 1] : 0.0;
-            tr.E2B[a][b] = x;
-            tr.E2N[a][b] = de;
+            tr.E2B[a * T + b] = x;
+            tr.E2N[a * T + b] = de;
             tm32[a * MAXT + b] = (a < minage || b < minage) ? 0.0f : (float)(de * (x - mt));
         }
     }
@@ -605,7 +621,8 @@ __device__ __forceinline__ void tables_tree(const BatchDev &d, int blk, int want
             for (int y = 0; y < si.m; y++) {
                 const int a = t0[si.node] + y;
                 t2d[base + y * si.m] =
-                    (a < minage || b < minage) ? 0.0f : (float)(tr.E2N[a][b] * (tr.E2B[a][b] - ct));
+                    (a < minage || b < minage) ? 0.0f
+                                               : (float)(tr.E2N[a * T + b] * (tr.E2B[a * T + b] - ct));
             }
         }
     }
@@ -1547,11 +1564,14 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
     auto align16 = [](void *p) {
         return (char *)(((uintptr_t)p + 15) & ~(uintptr_t)15);
     };
+    // lean: an FP32 batch with no internal-branch or infinite-sites problem needs no FP64
+    // emission partials, so neither the FP64 per-state factors nor FP64-sized scratch
+    const bool lean = FP32OUT && !d.emit64;
     int4 *nd = dyn;
     double *muts = (double *)align16(nd + n);
     double *nomuts = muts + n;
-    double *pm = (double *)align16(nomuts + n);  // [S][6]: mut0..2, nomut0..2 per state
-    int *order = (int *)align16(pm + (size_t)6 * maxS);  // level cursors
+    double *pm = lean ? nullptr : (double *)align16(nomuts + n);  // [S][6]: mut0..2, nomut0..2
+    int *order = (int *)align16(lean ? (void *)(nomuts + n) : (void *)(pm + (size_t)6 * maxS));
     int *hgt = order + n;                        // height, then depth scratch
     int *snode = hgt + n;                        // [maxS]
     int *inl = snode + maxS;                     // nodes by height
@@ -1562,11 +1582,14 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
     float *muts32 = (float *)align16(sfloor + maxS);     // FP32 path copies
     float *nomuts32 = muts32 + n;
     float *pm32 = (float *)align16(nomuts32 + n);        // [maxS][8]
-    double *scratch = (double *)align16(pm32 + (size_t)8 * maxS);  // per warp: inner[n][4], outer[n][4]
-    double *ebuf = scratch + (size_t)nwarps * n * 8;    // per warp: the column's emissions
+    // per warp: inner[n][4], outer[n][4] partials, then the column's emissions (float-sized
+    // when lean)
+    const int esz = lean ? 4 : 8;
+    double *scratch = (double *)align16(pm32 + (size_t)8 * maxS);
+    char *ebuf = (char *)scratch + (size_t)nwarps * n * 8 * esz;
     __shared__ double times[MAXT];
     __shared__ int nlev_in, nlev_out;
-    if ((char *)(ebuf + (size_t)nwarps * maxS) - (char *)dyn > smem_bytes) {
+    if (ebuf + (size_t)nwarps * maxS * esz - (char *)dyn > smem_bytes) {
         if (tid == 0) report_error(d.err, ERR_SMEM_LIMIT, B.inst, B.b, B.start);
         return;
     }
@@ -1594,6 +1617,10 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
     for (int i = tid; i < T; i += blockDim.x) times[i] = model[M_TIMES + i];
     const double mu = model[M_CONST + 1], mintime = model[M_CONST + 2];
     const double penalty = model[M_CONST + 3];  // infinite-sites penalty, 1: off
+    if (lean && (internal || penalty < 1.0)) {  // the batch flag says otherwise
+        if (tid == 0) report_error(d.err, ERR_PLAN_MISMATCH, B.inst, B.b, B.start);
+        return;
+    }
     for (int i = tid; i < n; i += blockDim.x) nd[i] = d.nodes[B.nodes0 + i];
     const bool refill = bc->inst != B.inst;  // read by all before anyone rewrites it
     __syncthreads();
@@ -1650,13 +1677,17 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
                          : branch_exp(fmax(coal_time - time1, mintime), mu);
         e[1] = age2 < T ? bc->e[age2][a] : branch_exp(fmax(coal_time - time2, mintime), mu);
         e[2] = parent != -1 ? bc->e[a][pidx] : bc->ez[a];
-        for (int x = 0; x < 3; x++) {
-            pm[6 * k + x] = branch_mut(e[x]);
-            pm[6 * k + 3 + x] = branch_nomut(e[x]);
-        }
+        if (!lean)
+            for (int x = 0; x < 3; x++) {
+                pm[6 * k + x] = branch_mut(e[x]);
+                pm[6 * k + 3 + x] = branch_nomut(e[x]);
+            }
         if (FP32OUT) {
-            for (int x = 0; x < 6; x++) pm32[8 * k + x] = (float)pm[6 * k + x];
-            pm32[8 * k + 6] = (float)(1.0 - 4.0 * pm[6 * k]);
+            for (int x = 0; x < 3; x++) {
+                pm32[8 * k + x] = (float)branch_mut(e[x]);
+                pm32[8 * k + 3 + x] = (float)branch_nomut(e[x]);
+            }
+            pm32[8 * k + 6] = (float)(1.0 - 4.0 * branch_mut(e[0]));
             pm32[8 * k + 7] = 0.f;
         }
     }
@@ -1696,8 +1727,8 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
 
     const EmitCtx ctx{nd, muts, nomuts, pm, muts32, nomuts32, pm32, snode, inl, inp, outl, outp,
                       sfloor, nlev_in, nlev_out, mainr, node1, S, I.nseqs, I.nleaves, n, internal};
-    double *wscr = scratch + (size_t)warp * n * 8;
-    double *eb = ebuf + (size_t)warp * maxS;
+    double *wscr = (double *)((char *)scratch + (size_t)warp * n * 8 * esz);
+    double *eb = (double *)(ebuf + (size_t)warp * maxS * esz);  // read as float when lean
     const uint8_t *cls = d.colclass + I.col0 + B.start;
     const int ns = I.nseqs;
 
@@ -1865,8 +1896,9 @@ __global__ void k_varemit_ws(BatchDev d, int nwarps, int maxS, int smem_bytes, W
     }
 }
 
-size_t tables_smem(int n, int S, int S1) {
-    size_t b = 2 * (size_t)n * sizeof(int4) + 8 * (size_t)n * sizeof(int);
+size_t tables_smem(int n, int S, int S1, int T, bool want32) {
+    size_t b = sizeof(double) * (size_t)exp_table_doubles(T, want32);
+    b += 2 * (size_t)n * sizeof(int4) + 8 * (size_t)n * sizeof(int);
     b += ((n + 15) & ~15);
     b += 2 * (size_t)imax(S1, 1) * sizeof(int);
     b += (size_t)(imax(imax(S, 1), MAXT) + 2) * sizeof(int);
@@ -1893,7 +1925,7 @@ int persistent_grid(K kernel, int threads, size_t smem, int nunits) {
 }
 
 void launch_tables(const BatchDev &d, bool want32, cudaStream_t s, int *queue, int chunk) {
-    size_t smem = tables_smem(d.maxnodes, d.maxS, d.maxS);
+    size_t smem = tables_smem(d.maxnodes, d.maxS, d.maxS, d.maxT, want32);
     static size_t configured = 0, configured_ws = 0;
     if (!queue) {
         prefer_shared(k_tables);
@@ -1919,19 +1951,21 @@ void launch_tables(const BatchDev &d, bool want32, cudaStream_t s, int *queue, i
 template <bool FP32OUT>
 void launch_varemit_t(const BatchDev &d, cudaStream_t s, int *queue, int chunk) {
     const int n = d.maxnodes, maxS = imax(d.maxS, 1);
+    const bool lean = FP32OUT && !d.emit64;
+    const size_t esz = lean ? sizeof(float) : sizeof(double);
     int nwarps = 4;
     // the kernel's carve, offset by offset (16-byte alignment where it aligns)
     auto need = [&](int w) {
         auto a16 = [](size_t o) { return (o + 15) & ~(size_t)15; };
         size_t o = (size_t)n * sizeof(int4);                              // nd
         o = a16(o) + 2 * (size_t)n * sizeof(double);                      // muts, nomuts
-        o = a16(o) + 6 * (size_t)maxS * sizeof(double);                   // pm
+        if (!lean) o = a16(o) + 6 * (size_t)maxS * sizeof(double);        // pm
         o = a16(o) + (6 * (size_t)n + 4 + maxS) * sizeof(int);            // order .. outp
         o += (size_t)maxS;                                                // sfloor
         o = a16(o) + 2 * (size_t)n * sizeof(float);                       // muts32, nomuts32
         o = a16(o) + 8 * (size_t)maxS * sizeof(float);                    // pm32
-        o = a16(o) + (size_t)w * n * 8 * sizeof(double);                  // scratch
-        o += (size_t)w * maxS * sizeof(double);                           // ebuf
+        o = a16(o) + (size_t)w * n * 8 * esz;                             // scratch
+        o += (size_t)w * maxS * esz;                                      // ebuf
         return o + 16;
     };
     while (nwarps > 1 && need(nwarps) > 200 * 1024) nwarps--;

@@ -246,6 +246,10 @@ struct SwitchCtx {
     const int *mapping;
     const double *times, *tsteps, *csteps, *pops;
     const int *nb, *nr, *nc;  // lineages of the previous tree
+    // q[m][1 + d] = csteps[m] * (nb[m / 2] + d) / (2.0 * pops[m / 2]) for d in {-1, 0, 1}:
+    // every coalescence-rate term of the switch formulas, the reference's expression with
+    // the lineage count it uses, evaluated once per tree
+    const double (*q)[3];
     double rho, last_treelen;
     bool internal;
 };
@@ -327,11 +331,13 @@ __device__ double calc_recoal(const SwitchCtx &c, const int *spr, int state1_tim
     if (j < c.T - 2) {
         double Z = 0.0;
         if (j > k) {
-            int b1 = c.nb[j - 1] - int(j - 1 < recomb_parent_age) + int(j - 1 < a);
-            if (over) b1 = 1;
-            Z = c.csteps[2 * j - 1] * b1 / (2.0 * c.pops[j - 1]);
+            if (over) Z = c.csteps[2 * j - 1] * 1 / (2.0 * c.pops[j - 1]);
+            else Z = c.q[2 * j - 1][1 - int(j - 1 < recomb_parent_age) + int(j - 1 < a)];
         }
-        p *= 1.0 - exp(-c.csteps[2 * j] * nbranches_j / (2.0 * c.pops[j]) - Z);
+        // -(x * n) / y is -(x * n / y) exactly
+        const double r = over ? c.csteps[2 * j] * nbranches_j / (2.0 * c.pops[j])
+                              : c.q[2 * j][1 - int(j < recomb_parent_age) + int(j < a)];
+        p *= 1.0 - exp(-r - Z);
     }
     return p;
 }
@@ -342,10 +348,8 @@ __device__ double calc_recomb_recoal(const SwitchCtx &c, const int *spr, int sta
     const int a = state_time, k = spr[1], j = spr[3];
     double p = calc_recomb(c, spr, state_node, state_time, c.last_treelen);
     double sum = 0.0;
-    for (int m = 2 * k; m < 2 * j - 1; m++) {
-        int nbm = c.nb[m / 2] - int(m / 2 < recomb_parent_age) + int(m / 2 < a);
-        sum += c.csteps[m] * nbm / (2.0 * c.pops[m / 2]);
-    }
+    for (int m = 2 * k; m < 2 * j - 1; m++)  // nb[m / 2] - [m / 2 < rpa] + [m / 2 < a]
+        sum += c.q[m][1 - int(m / 2 < recomb_parent_age) + int(m / 2 < a)];
     p *= exp(-sum);
     p *= calc_recoal(c, spr, state_time, recomb_parent_age, c.internal);
     return p;
@@ -497,8 +501,9 @@ __device__ __forceinline__ void tables_tree(const BatchDev &d, int blk, int want
         const int root_age_index = sh_rootage;
         const double root_age = times[root_age_index];
         // one (term, time) pair per thread, each term's expression as the reference writes
-        // it (lnE2 and lnG4 are the same expression, trans.cpp:80-86)
-        for (int e = tid; e < 5 * (T - 1); e += blockDim.x) {
+        // it (lnE2 and lnG4 are the same expression, trans.cpp:80-86); D and norecombs on
+        // separate threads
+        for (int e = tid; e < 6 * (T - 1); e += blockDim.x) {
             const int f = e / (T - 1), b = e % (T - 1);
             if (f == 0) {
                 lnBterm[b] = C[2 * b - 1] + log(tsteps[b] * (nb[b] + 1.0) / (nr[b] + 1.0));
@@ -524,9 +529,13 @@ __device__ __forceinline__ void tables_tree(const BatchDev &d, int blk, int want
                 } else {
                     treelen2_b = treelen2 + tsteps[root_age_index];
                 }
-                tr.D[b] = (1.0 - exp(-rho * treelen2)) / treelen2_b;
-                tr.norecombs[b] = exp(-fmax(rho * treelen2, rho));
-                if (want32) d.rstay32[(size_t)blk * MAXT + b] = (float)(-expm1(-fmax(rho * treelen2, rho)));
+                if (f == 4) {
+                    tr.D[b] = (1.0 - exp(-rho * treelen2)) / treelen2_b;
+                } else {
+                    tr.norecombs[b] = exp(-fmax(rho * treelen2, rho));
+                    if (want32)
+                        d.rstay32[(size_t)blk * MAXT + b] = (float)(-expm1(-fmax(rho * treelen2, rho)));
+                }
             }
         }
     }
@@ -804,12 +813,28 @@ __device__ __forceinline__ void tables_tree(const BatchDev &d, int blk, int want
         recombrow[k] = 0.0;
         recoalrow[k] = 0.0;
     }
+    // the switch's coalescence-rate terms, each once per tree (SwitchCtx::q), and the same
+    // without the lineage count
+    __shared__ double qrate[2 * MAXT][3], rrate[2 * MAXT];
+    for (int e = tid; e < 6 * T; e += blockDim.x) {
+        const int m = e / 3, dl = e % 3 - 1;
+        qrate[m][dl + 1] = csteps[m] * (pnb[m / 2] + dl) / (2.0 * pops[m / 2]);
+    }
+    for (int m = tid; m < 2 * T; m += blockDim.x) rrate[m] = csteps[m] / (2.0 * pops[m / 2]);
+    // the previous tree's length: FP64 path in node order (local_tree.cpp:136-176), FP32
+    // path summed by the CTA
+    double lt_part = 0.0;
+    if (want32)
+        for (int i = tid; i < n; i += blockDim.x) {
+            const int p = prv[i].x;
+            if (p == -1 || (internal && p == B.prev_root)) continue;
+            lt_part += times[prv[p].w] - times[prv[i].w];
+        }
+    const double lt32 = want32 ? block_sum(lt_part) : 0.0;
     if (tid == 0) {
         sh_src[0] = -1;
         sh_src[1] = -1;
-        const double lt = internal ? treelen_of(prv, n, B.prev_root, times, true)
-                                   : treelen_of(prv, n, B.prev_root, times, false);
-        sh_treelen = lt;
+        sh_treelen = want32 ? lt32 : treelen_of(prv, n, B.prev_root, times, internal);
     }
     __syncthreads();
 
@@ -817,7 +842,7 @@ __device__ __forceinline__ void tables_tree(const BatchDev &d, int blk, int want
     c.last = prv; c.cur = cur; c.last_root = B.prev_root; c.cur_root = root; c.T = T;
     c.mapping = d.mapping + B.map0;
     c.times = times; c.tsteps = tsteps; c.csteps = csteps; c.pops = pops;
-    c.nb = pnb; c.nr = pnr; c.nc = pnc; c.rho = rho; c.last_treelen = sh_treelen;
+    c.nb = pnb; c.nr = pnr; c.nc = pnc; c.q = qrate; c.rho = rho; c.last_treelen = sh_treelen;
     c.internal = internal;
     const int *spr = B.spr;
     const int *mapping = c.mapping;
@@ -896,15 +921,12 @@ __device__ __forceinline__ void tables_tree(const BatchDev &d, int blk, int want
         if (tid == 0) {
             const int k = spr[1], j = spr[3];
             double sum = 0.0;
-            for (int m = 2 * k; m < 2 * j - 1; m++) {
-                int nbm = pnb[m / 2] - int(m / 2 < rpa0);
-                sum += csteps[m] * nbm / (2.0 * pops[m / 2]);
-            }
+            for (int m = 2 * k; m < 2 * j - 1; m++) sum += qrate[m][1 - int(m / 2 < rpa0)];
             sh_sums = sum;
             sum = 0.0;
             sums2[2 * k] = sum;
             for (int m = 2 * k; m < 2 * j - 1; m++) {
-                sum += csteps[m] / (2.0 * pops[m / 2]);
+                sum += rrate[m];
                 sums2[m + 1] = sum;
             }
         }

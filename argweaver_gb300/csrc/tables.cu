@@ -548,23 +548,23 @@ __device__ __forceinline__ void tables_tree(const BatchDev &d, int blk, int want
         }
     } else {
         // FP32 path: the log-sum-exp prefix lnB[b] = log(sum_{i <= b} exp(lnBterm[i])) as T
-        // exponentials shifted by the largest term, one prefix sum and T logarithms (the
-        // reference adds one term at a time with logadd)
-        __shared__ double wexp[MAXT];
-        double mx = -INFINITY;
-        for (int i = 0; i < T - 1; i++) mx = fmax(mx, lnBterm[i]);
-        for (int b = tid; b < T - 1; b += blockDim.x) wexp[b] = exp(lnBterm[b] - mx);
-        __syncthreads();
-        if (tid == 0) {
-            double acc = 0.0;
-            for (int b = 0; b < T - 1; b++) {
-                acc += wexp[b];
-                wexp[b] = acc;
+        // exponentials shifted by the largest term, one prefix sum and T logarithms, by one
+        // warp (the reference adds one term at a time with logadd)
+        if (tid < 32) {
+            const int b = tid;
+            const double x = b < T - 1 ? lnBterm[b] : -INFINITY;
+            double mx = x;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+            double w = b < T - 1 ? exp(x - mx) : 0.0;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const double y = __shfl_up_sync(0xffffffffu, w, o);
+                if (b >= o) w += y;
             }
-            tr.E[T - 2] = 1.0 / nc[T - 2];
+            if (b < T - 1) tr.lnB[b] = mx + log(w);
+            if (b == 0) tr.E[T - 2] = 1.0 / nc[T - 2];
         }
-        __syncthreads();
-        for (int b = tid; b < T - 1; b += blockDim.x) tr.lnB[b] = mx + log(wexp[b]);
     }
     __syncthreads();
     if (!want32) {
@@ -580,11 +580,12 @@ __device__ __forceinline__ void tables_tree(const BatchDev &d, int blk, int want
         // FP32 path: 4 (T-1) exponentials instead of 1.5 (T-1)^2; tmatrix = D[a] E[b] (X[a][b]
         // - minage_term[b]), X the different-node bracket (get_time, trans.h:101-109), kept
         // with D[a] E[b] for the same-branch rows below
-        for (int i = tid; i < T - 1; i += blockDim.x) {
-            tr.eE2[i] = exp(tr.lnE2[i]);
-            tr.eB[i] = exp(tr.lnB[i]);
-            tr.eG4[i] = exp(tr.lnG4[i]);
-            tr.dBN[i] = tr.eB[i] * -expm1(tr.lnNegG1[i] - tr.lnB[i]);
+        for (int e = tid; e < 4 * (T - 1); e += blockDim.x) {  // one exponential per thread
+            const int f = e / (T - 1), i = e % (T - 1);
+            if (f == 0) tr.eE2[i] = exp(tr.lnE2[i]);
+            else if (f == 1) tr.eB[i] = exp(tr.lnB[i]);
+            else if (f == 2) tr.eG4[i] = exp(tr.lnG4[i]);
+            else tr.dBN[i] = exp(tr.lnB[i]) * -expm1(tr.lnNegG1[i] - tr.lnB[i]);
         }
         __syncthreads();
         float *tm32 = d.tm32 + (size_t)blk * MAXT * MAXT;
@@ -673,7 +674,8 @@ __device__ __forceinline__ void tables_tree(const BatchDev &d, int blk, int want
         for (int v = tid; v < n; v += blockDim.x) {
             const int p = cur[v].x;
             const double w = fmax(p != -1 ? times[cur[p].w] - times[cur[v].w] : 0.0, mintime);
-            if (v != mainr && below(cur, v, mainr, n)) pm += w;
+            // every node of an external tree is below its root
+            if (v != mainr && (!internal || below(cur, v, mainr, n))) pm += w;
             if (internal && v != sub && below(cur, v, sub, n)) ps += w;
         }
         const double mt = block_sum(pm);
@@ -977,26 +979,11 @@ __device__ __forceinline__ void tables_tree(const BatchDev &d, int blk, int want
                 const int node2 = (other == spr[2] ? cur[mapping[other]].x : mapping[other]);
                 const int next0 = lookup(first, t0, cnt, mapping[spr[0]], spr[1]);
                 const int next1 = lookup(first, t0, cnt, node2, time2);
-                if (tid == 0 && next0 != -1)
+                // where both entries are one state the reference's second write wins
+                if (tid == 0 && next0 != -1 && next0 != next1)
                     recombrow[next0] = calc_recomb_recoal(c, spr, s1node[recombsrc],
                                                           s1time[recombsrc], rpa0);
-                // where both entries are one state the second write wins (the block below)
-                if (tid == 32 && next1 != -1 && next1 != next0)
-                    recombrow[next1] = calc_recomb_recoal(c, spr, s1node[recombsrc],
-                                                          s1time[recombsrc], s1time[recombsrc]);
-            }
-        }
-        __syncthreads();
-        if (tid == 32) {  // next0 == next1: the second evaluation overwrites the first
-            const int recombsrc = sh_src[0];
-            if (recombsrc != -1) {
-                const int parent = prv[spr[0]].x;
-                const int time2 = prv[parent].w;
-                const int other = sibling(prv, spr[0]);
-                const int node2 = (other == spr[2] ? cur[mapping[other]].x : mapping[other]);
-                const int next0 = lookup(first, t0, cnt, mapping[spr[0]], spr[1]);
-                const int next1 = lookup(first, t0, cnt, node2, time2);
-                if (next1 != -1 && next1 == next0)
+                if (tid == 32 && next1 != -1)
                     recombrow[next1] = calc_recomb_recoal(c, spr, s1node[recombsrc],
                                                           s1time[recombsrc], s1time[recombsrc]);
             }

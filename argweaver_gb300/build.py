@@ -33,8 +33,8 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-
               "-Xcompiler", "-ffp-contract=off", "-I" + INCLUDE, "-I" + CSRC] + ARCH
 
 CUDA_SOURCES = ["host_plan.cpp", "tables.cu", "forward.cu", "traceback.cu",
-                "backward.cu", "batch.cu", "static_run.cu", "dense_hmm.cu", "capi.cpp",
-                "server.cpp"]
+                "backward.cu", "batch.cu", "static_run.cu", "dense_hmm.cu", "arg_prob.cu",
+                "capi.cpp", "server.cpp"]
 
 
 def _nvcc() -> str:

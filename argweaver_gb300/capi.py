@@ -70,6 +70,13 @@ PROTOTYPES = [
     ("delete_path", None, [c_int_p]),
     ("delete_double_matrix", None, [c_double_pp, C.c_int]),
     ("delete_forward_matrix", None, [c_double_pp, C.c_int]),
+    ("arghmm_likelihood", C.c_double, [C.c_void_p, c_double_p, C.c_int, C.c_double,
+                                        c_char_pp, C.c_int, C.c_int]),
+    ("arghmm_prior_prob", C.c_double, [C.c_void_p, c_double_p, C.c_int, c_double_p,
+                                        C.c_double]),
+    ("arghmm_tree_prior_prob", C.c_double, [C.c_void_p, c_double_p, C.c_int, c_double_p]),
+    ("arghmm_joint_prob", C.c_double, [C.c_void_p, c_double_p, C.c_int, c_double_p,
+                                        C.c_double, C.c_double, c_char_pp, C.c_int, C.c_int]),
     ("forward_alg", None, [C.c_int, C.c_int, c_double_pp, c_double_pp, c_double_pp]),
     ("backward_alg", None, [C.c_int, C.c_int, c_double_pp, c_double_pp, c_double_pp]),
     ("sample_hmm_posterior", None, [C.c_int, C.c_int, c_double_pp, c_double_pp, c_int_p]),

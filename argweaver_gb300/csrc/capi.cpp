@@ -5,6 +5,7 @@
 
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -386,4 +387,51 @@ void sample_hmm_posterior(int n, int nstates, double **trans, double **fw, int *
     if (!awg::dense_hmm(2, n, nstates, trans, nullptr, fw, path, err)) set_error(err);
 }
 
+// ARG probabilities (total_prob.cpp:315-382): computed on the device; NaN and
+// awg_last_error() on failure (the reference asserts).
+static double arg_prob_call(const awg_local_trees *t, const double *times, int ntimes,
+                            const double *popsizes, double rho, double mu, char **seqs,
+                            int nseqs, int seqlen, int what, int which) {
+    g_err.clear();
+    if (!t) {
+        set_error("ARG probability: NULL trees");
+        return NAN;
+    }
+    double out[3] = {0, 0, 0};
+    std::string err;
+    if (awg::arg_probabilities(t->ptrees.data(), t->ages.data(), t->sprs.data(),
+                               t->blocklens.data(), t->ntrees, t->nnodes, t->start_coord, times,
+                               ntimes, popsizes, rho, mu, seqs, nseqs, seqlen, what, out,
+                               err) != 0) {
+        set_error(err);
+        return NAN;
+    }
+    return which < 0 ? out[0] + out[1] : out[which];
+}
+
+double arghmm_likelihood(awg_local_trees *trees, double *times, int ntimes, double mu,
+                         char **seqs, int nseqs, int seqlen) {
+    if (trees && trees->nnodes < 3) return log(.25) * seqlen;  // total_prob.cpp:27-28
+    return arg_prob_call(trees, times, ntimes, nullptr, 0.0, mu, seqs, nseqs, seqlen, 1, 0);
+}
+
+double arghmm_prior_prob(awg_local_trees *trees, double *times, int ntimes, double *popsizes,
+                         double rho) {
+    return arg_prob_call(trees, times, ntimes, popsizes, rho, 0.0, nullptr, 0, 0, 2, 1);
+}
+
+double arghmm_tree_prior_prob(awg_local_trees *trees, double *times, int ntimes,
+                              double *popsizes) {
+    return arg_prob_call(trees, times, ntimes, popsizes, 0.0, 0.0, nullptr, 0, 0, 4, 2);
+}
+
+double arghmm_joint_prob(awg_local_trees *trees, double *times, int ntimes, double *popsizes,
+                         double mu, double rho, char **seqs, int nseqs, int seqlen) {
+    if (trees && trees->nnodes < 3)
+        return log(.25) * seqlen +
+               arg_prob_call(trees, times, ntimes, popsizes, rho, mu, nullptr, 0, 0, 2, 1);
+    return arg_prob_call(trees, times, ntimes, popsizes, rho, mu, seqs, nseqs, seqlen, 3, -1);
+}
+
 }  // extern "C"
+

@@ -15,6 +15,34 @@
 
 namespace awg {
 
+// An instance's model block (model.h:322-333, model.cpp:9-23): times, popsizes (zeros when
+// NULL), time_steps, coal_time_steps, rho, mu, mintime and the infinite-sites penalty.
+void model_arrays(const double *times, const double *popsizes, int T, double rho, double mu,
+                  double penalty, double *m) {
+    for (int i = 0; i < MODEL_STRIDE; i++) m[i] = 0.0;
+    for (int i = 0; i < T; i++) {
+        m[M_TIMES + i] = times[i];
+        m[M_POPSIZES + i] = popsizes ? popsizes[i] : 0.0;
+    }
+    for (int i = 0; i < T - 1; i++) m[M_TIMESTEPS + i] = times[i + 1] - times[i];
+    m[M_TIMESTEPS + T - 1] = INFINITY;
+    std::vector<double> times2(2 * T + 1, 0.0);
+    for (int i = 0; i < T - 1; i++) {
+        times2[2 * i] = times[i];
+        times2[2 * i + 1] = std::sqrt((times[i + 1] + 1.0) * (times[i] + 1.0));
+    }
+    times2[2 * T - 2] = times2[2 * T - 1] = times2[2 * T] = times[T - 1];
+    for (int i = 0; i < 2 * T - 2; i++)
+        m[M_COALSTEPS + i] = times2[std::min(i + 1, 2 * T)] - times2[i];
+    m[M_COALSTEPS + 2 * T - 2] = INFINITY;
+    m[M_COALSTEPS + 2 * T - 1] = INFINITY;
+    m[M_CONST + 0] = rho;
+    m[M_CONST + 1] = mu;
+    m[M_CONST + 2] = times[1] * .1;
+    m[M_CONST + 3] = (penalty > 0.0 && penalty < 1.0) ? penalty : 1.0;
+}
+
+
 namespace {
 
 bool valid_base(char c) {
@@ -223,29 +251,8 @@ bool plan_layout(const awg_problem *probs, int n, HostPlan &plan, std::string &e
         I.ntrees = p.ntrees; I.block0 = blk; I.pad = 0;
         I.cell0 = cell; I.col0 = col; I.seq0 = seq; I.model0 = (long long)q * MODEL_STRIDE;
 
-        // model (model.h:322-333, model.cpp:9-23)
-        double *m = &plan.model[(size_t)q * MODEL_STRIDE];
-        const int T = p.ntimes;
-        for (int i = 0; i < T; i++) {
-            m[M_TIMES + i] = p.times[i];
-            m[M_POPSIZES + i] = p.popsizes[i];
-        }
-        for (int i = 0; i < T - 1; i++) m[M_TIMESTEPS + i] = p.times[i + 1] - p.times[i];
-        m[M_TIMESTEPS + T - 1] = INFINITY;
-        std::vector<double> times2(2 * T + 1, 0.0);
-        for (int i = 0; i < T - 1; i++) {
-            times2[2 * i] = p.times[i];
-            times2[2 * i + 1] = std::sqrt((p.times[i + 1] + 1.0) * (p.times[i] + 1.0));
-        }
-        times2[2 * T - 2] = times2[2 * T - 1] = times2[2 * T] = p.times[T - 1];
-        for (int i = 0; i < 2 * T - 2; i++)
-            m[M_COALSTEPS + i] = times2[std::min(i + 1, 2 * T)] - times2[i];
-        m[M_COALSTEPS + 2 * T - 2] = INFINITY;
-        m[M_COALSTEPS + 2 * T - 1] = INFINITY;
-        m[M_CONST + 0] = p.rho;
-        m[M_CONST + 1] = p.mu;
-        m[M_CONST + 2] = p.times[1] * .1;
-        m[M_CONST + 3] = (p.infsites_penalty > 0.0 && p.infsites_penalty < 1.0) ? p.infsites_penalty : 1.0;
+        model_arrays(p.times, p.popsizes, p.ntimes, p.rho, p.mu, p.infsites_penalty,
+                     &plan.model[(size_t)q * MODEL_STRIDE]);
 
         int pos = 0;
         for (int b = 0; b < p.ntrees; b++, blk++) {

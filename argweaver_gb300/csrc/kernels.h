@@ -50,4 +50,13 @@ void note_launch();
 bool dense_hmm(int which, int n, int nstates, double **trans, double **emit, double **tab,
                int *path, std::string &err);
 
+// Probabilities of a whole ARG (total_prob.cpp) on the device: what = 1 likelihood, 2 prior,
+// 4 first-tree prior (bits combine); out[0..2] in that order. Trees as the reference's
+// arrays (ntrees x nnodes parents and ages, ntrees x 4 SPRs, block lengths). 0, or < 0 with
+// err set.
+int arg_probabilities(const int *ptrees, const int *ages, const int *sprs, const int *blocklens,
+                      int ntrees, int nnodes, int start_coord, const double *times, int T,
+                      const double *popsizes, double rho, double mu, char *const *seqs,
+                      int nseqs, int seqlen, int what, double *out, std::string &err);
+
 }  // namespace awg

@@ -48,6 +48,10 @@ void plan_fill(const awg_problem *probs, int n, HostPlan &plan, const PlanDst &d
 // Both, into the plan's own vectors; returns false with a message on bad input.
 bool build_plan(const awg_problem *probs, int n, HostPlan &plan, std::string &err);
 
+// The MODEL_STRIDE doubles of one instance's model (model.h:322-333, model.cpp:9-23).
+void model_arrays(const double *times, const double *popsizes, int T, double rho, double mu,
+                  double penalty, double *m);
+
 // Threads the calling thread's planning may use (0: all hardware threads); callers that
 // plan several batches at once share the cores this way.
 void set_plan_threads(int n);

@@ -217,3 +217,64 @@ def sample_hmm_posterior(trans: np.ndarray, fw: np.ndarray, path: np.ndarray) ->
     if err:
         raise RuntimeError(err)
     return path
+
+
+# ----------------------------------------------------------------------------- ARG probabilities
+# arghmm_likelihood / arghmm_prior_prob / arghmm_tree_prior_prob / arghmm_joint_prob
+# (argweaverc.py:219-245, total_prob.cpp:315-382), computed on the GPU.
+
+def _site_rows(p: Problem):
+    """The problem's sequences as the reference indexes them: by absolute position, the
+    trees' first site at start_coord (earlier positions padded with 'N')."""
+    seqs = np.ascontiguousarray(p.seqs, dtype=np.uint8)
+    if p.start_coord:
+        pad = np.full((seqs.shape[0], p.start_coord), ord("N"), dtype=np.uint8)
+        seqs = np.concatenate([pad, seqs], axis=1)
+    return seqs
+
+
+def _arg_call(prob: Problem, name: str) -> float:
+    lib = capi.load()
+    p = prob.normalized()
+    trees = LocalTrees(p)
+    rows = _site_rows(p)
+    seqs, _keep = _char_pp(rows)
+    times = p.times.ctypes.data_as(capi.c_double_p)
+    pops = p.popsizes.ctypes.data_as(capi.c_double_p)
+    try:
+        if name == "likelihood":
+            v = lib.arghmm_likelihood(trees.handle, times, p.ntimes, p.mu, seqs, p.nseqs,
+                                      rows.shape[1])
+        elif name == "prior":
+            v = lib.arghmm_prior_prob(trees.handle, times, p.ntimes, pops, p.rho)
+        elif name == "tree_prior":
+            v = lib.arghmm_tree_prior_prob(trees.handle, times, p.ntimes, pops)
+        else:
+            v = lib.arghmm_joint_prob(trees.handle, times, p.ntimes, pops, p.mu, p.rho, seqs,
+                                      p.nseqs, rows.shape[1])
+        err = capi.last_error()
+    finally:
+        trees.close()
+    if err:
+        raise ValueError(err)
+    return float(v)
+
+
+def arghmm_likelihood(prob: Problem) -> float:
+    """log P(sequences | ARG) (calc_arg_likelihood, total_prob.cpp:19-45)."""
+    return _arg_call(prob, "likelihood")
+
+
+def arghmm_prior_prob(prob: Problem) -> float:
+    """log P(ARG): recombination spacing and SPRs (calc_arg_prior, total_prob.cpp:262-300)."""
+    return _arg_call(prob, "prior")
+
+
+def arghmm_tree_prior_prob(prob: Problem) -> float:
+    """The first tree's coalescent prior (calc_tree_prior, total_prob.cpp:132-165)."""
+    return _arg_call(prob, "tree_prior")
+
+
+def arghmm_joint_prob(prob: Problem) -> float:
+    """Likelihood + prior (calc_arg_joint_prob, total_prob.cpp:303-308)."""
+    return _arg_call(prob, "joint")

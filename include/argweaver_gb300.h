@@ -94,6 +94,21 @@ void delete_path(int *path);
 void delete_double_matrix(double **mat, int nrows);
 void delete_forward_matrix(double **mat, int nrows);
 
+/* Probabilities of a whole ARG (total_prob.cpp:315-382; bound by
+ * argweaver/argweaverc.py:219-245), computed on the device. arghmm_likelihood: log P(seqs |
+ * ARG), sequences one per leaf (leaf i = seqs[i]) covering start_coord .. end of the trees;
+ * arghmm_prior_prob: log P(ARG) of the recombination spacing and SPRs; arghmm_tree_prior_prob:
+ * the first tree's coalescent prior; arghmm_joint_prob: likelihood + prior. NaN and
+ * awg_last_error() on invalid input. */
+double arghmm_likelihood(awg_local_trees *trees, double *times, int ntimes, double mu,
+                         char **seqs, int nseqs, int seqlen);
+double arghmm_prior_prob(awg_local_trees *trees, double *times, int ntimes, double *popsizes,
+                         double rho);
+double arghmm_tree_prior_prob(awg_local_trees *trees, double *times, int ntimes,
+                              double *popsizes);
+double arghmm_joint_prob(awg_local_trees *trees, double *times, int ntimes, double *popsizes,
+                         double mu, double rho, char **seqs, int nseqs, int seqlen);
+
 /* The dense HMM over a full nstates x nstates log transition matrix (hmm.h:14-19,
  * hmm.cpp:27-85; bound by argweaver/argweaverc.py:42-56). Tables are n row pointers of
  * nstates doubles, in natural log. As in the reference the caller fills the boundary:

@@ -1748,5 +1748,190 @@ int oracle_dense_sample(int n, int S, const double *trans, const double *fw, con
     return 0;
 }
 
+// ----------------------------------------------------------------------------- ARG probabilities
+// calc_arg_likelihood (total_prob.cpp:19-45, likelihood_tree emit.cpp:399-446),
+// calc_arg_prior (total_prob.cpp:262-300, calc_spr_prob :210-259) and calc_tree_prior
+// (total_prob.cpp:132-165, prob_coal_counts :108-127), in the reference's order. The
+// problem's sequences are one per leaf (more are allowed: the invariance test reads all),
+// columns = the trees' sites. out: likelihood, prior, first-tree prior.
+
+static double oracle_prob_coal_counts(int a, int b, double t, double n) {
+    double C = 1.0;
+    for (int y = 0; y < b; y++) C *= (b + y) * (a - y) / double(a + y);
+    double s = exp(-b * (b - 1) * t / 2.0 / n) * C;
+    for (int k = b + 1; k < a + 1; k++) {
+        const double k1 = double(k - 1);
+        C *= double(b + k1) * (a - k1) / (a + k1) / (b - k);
+        s += exp(-k * k1 * t / 2.0 / n) * (2 * k - 1) / double(k1 + b) * C;
+    }
+    for (int i = 1; i <= b; i++) s /= i;
+    return s;
+}
+
+int oracle_arg_prob(const oracle_problem *p, double *out) {
+    Model m;
+    if (!build_model(p, m)) return -1;
+    const int n = p->nnodes, B = p->ntrees, T = p->ntimes;
+    vector<Tree> trees(B);
+    for (int b = 0; b < B; b++) {  // set_ptree (local_tree.h:216-229)
+        Tree &t = trees[b];
+        t.n = n;
+        t.parent.assign(p->ptrees + (size_t)b * n, p->ptrees + (size_t)(b + 1) * n);
+        t.age.assign(p->ages + (size_t)b * n, p->ages + (size_t)(b + 1) * n);
+        t.c0.assign(n, -1);
+        t.c1.assign(n, -1);
+        for (int i = 0; i < n; i++) {
+            const int par = t.parent[i];
+            if (par < -1 || par >= n) return -2;
+            if (par == -1) t.root = i;
+            else if (t.c0[par] == -1) t.c0[par] = i;
+            else if (t.c1[par] == -1) t.c1[par] = i;
+            else return -2;
+        }
+        if (t.root < 0) return -2;
+    }
+    const double *times = m.times.data();
+    const double mintime = m.mintime();
+    // likelihood
+    double lik = 0.0;
+    if (n < 3) {
+        lik = log(.25) * p->seqlen;
+    } else {
+        int end = 0;
+        for (int b = 0; b < B; b++) {
+            const Tree &t = trees[b];
+            const int start = end;
+            end = start + p->blocklens[b];
+            vector<double> muts(n), nomuts(n);
+            for (int i = 0; i < n; i++)
+                if (i != t.root) {
+                    const double tt = std::max(times[t.age[t.parent[i]]] - times[t.age[i]], mintime);
+                    muts[i] = prob_branch(tt, m.mu, true);
+                    nomuts[i] = prob_branch(tt, m.mu, false);
+                }
+            vector<int> order(n);  // LocalTree::get_postorder (local_tree.h:274-304)
+            {
+                vector<char> visit(n, 0);
+                int i;
+                for (i = 0; i < n; i++) {
+                    if (!t.leaf(i)) break;
+                    order[i] = i;
+                }
+                int e = i;
+                for (i = 0; i < n; i++) {
+                    const int parent = t.parent[order[i]];
+                    if (parent != -1 && ++visit[parent] == 2) order[e++] = parent;
+                }
+            }
+            double invariant_lk = -1, tree_lnl = 0.0;  // a tree's sum, then the total
+            vector<lk_row> in(n);
+            for (int i = start; i < end; i++) {
+                bool inv = true;
+                const char c0 = p->seqs[(size_t)0 * p->seqlen + i];
+                for (int j = 1; j < p->nseqs && inv; j++) inv = p->seqs[(size_t)j * p->seqlen + i] == c0;
+                double lk;
+                if (inv && invariant_lk > 0) {
+                    lk = invariant_lk;
+                } else {
+                    for (int oi = 0; oi < n; oi++) {  // likelihood_site_node_inner (emit.cpp:151-196)
+                        const int j = order[oi];
+                        if (t.leaf(j)) {
+                            const char c = p->seqs[(size_t)j * p->seqlen + i];
+                            if (c == 'N') { in[j][0] = in[j][1] = in[j][2] = in[j][3] = 1.0; }
+                            else {
+                                in[j][0] = in[j][1] = in[j][2] = in[j][3] = 0.0;
+                                in[j][dna2int(c)] = 1.0;
+                            }
+                        } else {
+                            const int c1 = t.c0[j], c2 = t.c1[j];
+                            for (int a = 0; a < 4; a++) {
+                                double p1 = 0.0, p2 = 0.0;
+                                for (int bb = 0; bb < 4; bb++) {
+                                    if (a == bb) { p1 += in[c1][bb] * nomuts[c1]; p2 += in[c2][bb] * nomuts[c2]; }
+                                    else { p1 += in[c1][bb] * muts[c1]; p2 += in[c2][bb] * muts[c2]; }
+                                }
+                                in[j][a] = p1 * p2;
+                            }
+                        }
+                    }
+                    lk = 0.0;
+                    for (int a = 0; a < 4; a++) lk += in[t.root][a] * .25;
+                    if (inv) invariant_lk = lk;
+                }
+                tree_lnl += log(lk);
+            }
+            lik += tree_lnl;
+        }
+    }
+    // prior
+    double prior = 0.0;
+    {
+        long long total = 0;
+        for (int b = 0; b < B; b++) total += p->blocklens[b];
+        long long end = 0;
+        for (int b = 0; b < B; b++) {
+            const Tree &t = trees[b];
+            end += p->blocklens[b];
+            const int blocklen = p->blocklens[b];
+            const double treelen = get_treelen(t, times, false);
+            const double recomb_rate = std::max(m.rho * treelen, m.rho);
+            if (end < total) {
+                prior += log(recomb_rate) - recomb_rate * blocklen;
+                const int *s = p->sprs + (size_t)(b + 1) * 4;
+                const Spr spr{s[0], s[1], s[2], s[3]};
+                // calc_spr_prob
+                const int root_age = t.age[t.root];
+                const double treelen_b = treelen + m.time_steps[t.age[t.root]];
+                Lineages l;
+                count_lineages(t, T, l);
+                l.nrecombs[root_age]--;
+                double lnl = 0.0;
+                const int k = spr.recomb_time;
+                lnl += log(l.nbranches[k] * m.time_steps[k] / (l.nrecombs[k] * treelen_b));
+                const int broken_age = t.age[t.parent[spr.recomb_node]];
+                vector<double> coal_rates(2 * T);
+                for (int i = 0; i < 2 * T; i++) {  // calc_coal_rates_full_tree
+                    const int nb = l.nbranches[i / 2] - int(i / 2 < broken_age);
+                    coal_rates[i] = m.coal_time_steps[i] * nb / (2.0 * m.popsizes[i / 2]);
+                }
+                const int j = spr.coal_time;
+                const int ncoals_j = l.ncoals[j] - int(j <= broken_age) - int(j == broken_age);
+                lnl -= log(ncoals_j);
+                if (j < T - 2)
+                    lnl += log(1.0 - exp(-coal_rates[2 * j] - (j > k ? coal_rates[2 * j - 1] : 0.0)));
+                for (int mm = 2 * k; mm < 2 * j - 1; mm++) lnl -= coal_rates[mm];
+                prior += lnl;
+            } else {
+                prior += -recomb_rate * blocklen;
+            }
+        }
+    }
+    // first tree's prior
+    double tprior = 0.0;
+    {
+        const Tree &t = trees[0];
+        Lineages l;
+        count_lineages(t, T, l);
+        vector<double> tm(T), pm(T);
+        tm[0] = m.coal_time_steps[0];
+        pm[0] = m.popsizes[0];
+        for (int i = 1; i < T - 1; i++) {
+            const double t1 = m.coal_time_steps[2 * i - 1], t2 = m.coal_time_steps[2 * i];
+            const double n1 = m.popsizes[i - 1], n2 = m.popsizes[i];
+            tm[i] = t1 + t2;
+            pm[i] = (t1 + t2) / (t1 / n1 + t2 / n2);
+        }
+        for (int i = 0; i < T - 1; i++) {
+            const int a = (i == 0 ? t.nleaves() : l.nbranches[i - 1]);
+            const int b = l.nbranches[i];
+            tprior += log(oracle_prob_coal_counts(a, b, tm[i], 2.0 * pm[i]));
+        }
+    }
+    out[0] = lik;
+    out[1] = prior;
+    out[2] = tprior;
+    return 0;
+}
+
 }  // extern "C"
 

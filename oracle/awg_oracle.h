@@ -74,6 +74,11 @@ int oracle_dense_backward(int n, int S, const double *trans, const double *emit,
 int oracle_dense_sample(int n, int S, const double *trans, const double *fw, const double *u,
                         int *path);
 
+/* Probabilities of the problem's ARG (total_prob.cpp): out[0] log-likelihood of the
+ * sequences (one per leaf, columns = the trees' sites), out[1] the ARG prior, out[2] the
+ * first tree's coalescent prior. */
+int oracle_arg_prob(const oracle_problem *p, double *out);
+
 /* Total cells: sum over columns of max(nstates,1). */
 long long oracle_cells(const oracle_problem *p);
 

@@ -53,7 +53,8 @@ def load():
                                                     C.c_void_p]),
                            ("oracle_dense_forward", [C.c_int, C.c_int] + [C.c_void_p] * 3),
                            ("oracle_dense_backward", [C.c_int, C.c_int] + [C.c_void_p] * 3),
-                           ("oracle_dense_sample", [C.c_int, C.c_int] + [C.c_void_p] * 4)]:
+                           ("oracle_dense_sample", [C.c_int, C.c_int] + [C.c_void_p] * 4),
+                           ("oracle_arg_prob", [P, C.c_void_p])]:
             fn = getattr(lib, name)
             fn.restype = C.c_int
             fn.argtypes = args
@@ -251,4 +252,12 @@ def dense_sample(trans, fw, u, last: int) -> np.ndarray:
                                       fw.ctypes.data, u.ctypes.data, path.ctypes.data),
            "dense sample")
     return path
+
+
+def arg_prob(prob) -> np.ndarray:
+    """(log-likelihood, ARG prior, first-tree prior) of the problem's ARG (total_prob.cpp)."""
+    b = Bound(prob)
+    out = np.zeros(3)
+    _check(load().oracle_arg_prob(b.ref, out.ctypes.data), "ARG probability")
+    return out
 

@@ -20,6 +20,9 @@
 //                                    matrix (about a tenth of the entries zero) and random
 //                                    emissions, inputs from a fixed integer hash: forward_alg,
 //                                    backward_alg, then a path after srand(seed)
+//   argprob <problem> <out>          the ARG's probabilities through the reference's C
+//                                    exports (total_prob.cpp:315-382): likelihood, prior,
+//                                    first-tree prior, joint (4 doubles)
 //   sim1    <sites> <smc> <c> <out>  reads a sites file + SMC ARG the way arg-sample does
 //                                    (arg-sample.cpp:996-1155), removes the last sequence's
 //                                    thread (thread.cpp:425) and writes the external problem
@@ -67,6 +70,15 @@ void get_local_trees_ptrees(LocalTrees *trees, int **ptrees, int **ages, int **s
                             int *blocklens);          // local_tree.cpp:1846
 void arghmm_get_nstates(LocalTrees *trees, int ntimes, bool internal,
                         int *nstates);                // states.cpp:209
+double arghmm_likelihood(LocalTrees *trees, double *times, int ntimes, double mu,
+                         char **seqs, int nseqs, int seqlen);          // total_prob.cpp:317
+double arghmm_prior_prob(LocalTrees *trees, double *times, int ntimes, double *popsizes,
+                         double rho);                                  // total_prob.cpp:345
+double arghmm_tree_prior_prob(LocalTrees *trees, double *times, int ntimes,
+                              double *popsizes);                       // total_prob.cpp:355
+double arghmm_joint_prob(LocalTrees *trees, double *times, int ntimes, double *popsizes,
+                         double mu, double rho, char **seqs, int nseqs,
+                         int seqlen);                                  // total_prob.cpp:369
 }
 }
 
@@ -355,6 +367,24 @@ static int cmd_dense(const char *in, const char *out, int seed) {
     return 0;
 }
 
+static int cmd_argprob(const char *in, const char *out) {
+    Problem p = read_problem(in);
+    LocalTrees *trees = make_trees(p);
+    vector<char *> sp = seq_ptrs(p);
+    double v[4];
+    v[0] = arghmm_likelihood(trees, p.times.data(), p.ntimes, p.mu, sp.data(), p.nseqs, p.seqlen);
+    v[1] = arghmm_prior_prob(trees, p.times.data(), p.ntimes, p.popsizes.data(), p.rho);
+    v[2] = arghmm_tree_prior_prob(trees, p.times.data(), p.ntimes, p.popsizes.data());
+    v[3] = arghmm_joint_prob(trees, p.times.data(), p.ntimes, p.popsizes.data(), p.mu, p.rho,
+                             sp.data(), p.nseqs, p.seqlen);
+    FILE *f = fopen(out, "wb");
+    if (!f) die("cannot write output");
+    wr(f, v, 4);
+    fclose(f);
+    delete trees;
+    return 0;
+}
+
 // uniform in [0, 1) from an integer hash of (a, b, c): the random fixture's inputs
 static double hash01(unsigned a, unsigned b, unsigned c) {
     unsigned long long x = 0x9E3779B97F4A7C15ull * (a + 1) ^ 0xC2B2AE3D27D4EB4Full * (b + 7) ^
@@ -488,6 +518,7 @@ int main(int argc, char **argv) {
     if (cmd == "dense" && argc == 5) return cmd_dense(argv[2], argv[3], atoi(argv[4]));
     if (cmd == "densernd" && argc == 6)
         return cmd_densernd(atoi(argv[2]), atoi(argv[3]), atoi(argv[4]), argv[5]);
+    if (cmd == "argprob" && argc == 4) return cmd_argprob(argv[2], argv[3]);
     if (cmd == "sim1" && argc == 6) return cmd_sim1(argv[2], argv[3], atoi(argv[4]), argv[5]);
     if (cmd == "cut" && argc == 5) return cmd_cut(argv[2], atoi(argv[3]), argv[4]);
     die("bad arguments");

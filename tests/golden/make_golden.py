@@ -5,6 +5,7 @@ Run where the reference checkout exists (default /root/reference, or $AWG_REFERE
     python tests/golden/make_golden.py            # all fixtures
     python tests/golden/make_golden.py infsites   # only the infinite-sites ones
     python tests/golden/make_golden.py dense      # only the dense-HMM ones
+    python tests/golden/make_golden.py argprob    # only the ARG-probability ones
 
 It builds the reference from its own sources (oracle/Makefile target ``ref``), writes
 each problem as an AWGPROB1 file and runs the reference's threading HMM on it through
@@ -167,6 +168,35 @@ def densernd(tmp):
                             dense_path=path)
 
 
+def argprob(tmp):
+    """The ARG's probabilities (total_prob.cpp) from the reference's C exports, on full ARGs
+    (one sequence per leaf), one with missing calls and whole columns masked at tree starts
+    (the reference reuses a tree's first invariant site's likelihood for every invariant
+    site, an all-'N' one included), and a threading problem (one sequence more than
+    leaves)."""
+    out_dir = os.path.join(HERE, "argprob")
+    os.makedirs(out_dir, exist_ok=True)
+    cases = []
+    cases.append(("full_k10", simulate(10, 1500, 205, add_thread=False)))
+    cases.append(("full_k24_T16", simulate(24, 4000, 31, add_thread=False, ntimes=16)))
+    p = simulate(12, 3000, 77, add_thread=False, missing=0.02)
+    starts = np.concatenate([[0], np.cumsum(p.blocklens)[:-1]])
+    seqs = p.seqs.copy()
+    seqs[:, starts[::2]] = ord("N")
+    p.seqs = seqs
+    cases.append(("full_k12_masked", p))
+    cases.append(("thread_k8", simulate(7, 2000, 12)))
+    for name, prob in cases:
+        pp = os.path.join(out_dir, name + ".prob")
+        prob.save(pp)
+        ob = os.path.join(tmp, "ap.bin")
+        run("argprob", pp, ob)
+        v = np.fromfile(ob, dtype=np.float64)
+        np.savez(os.path.join(out_dir, name + ".npz"), likelihood=v[0], prior=v[1],
+                 tree_prior=v[2], joint=v[3])
+        print(name, v)
+
+
 def infsites(tmp):
     """The infinite-sites penalty (ArgModel::infsites_penalty, emit.cpp:847-862; arg-sample
     --infsites uses 1e-100): external, with missing calls, and an internal-branch cut."""
@@ -190,6 +220,10 @@ def main():
     if sys.argv[1:] == ["infsites"]:
         with tempfile.TemporaryDirectory() as tmp:
             infsites(tmp)
+        return
+    if sys.argv[1:] == ["argprob"]:
+        with tempfile.TemporaryDirectory() as tmp:
+            argprob(tmp)
         return
     if sys.argv[1:] == ["dense"]:
         with tempfile.TemporaryDirectory() as tmp:
@@ -231,6 +265,7 @@ def main():
 
         dense(tmp)
         densernd(tmp)
+        argprob(tmp)
 
 
 if __name__ == "__main__":

@@ -141,3 +141,20 @@ def test_posterior_properties(name):
     # at the last column the backward is flat, so the posterior is the forward column
     L = prob.seqlen
     np.testing.assert_allclose(post[off[L - 1]:], fw[off[L - 1]:], rtol=1e-12, atol=1e-300)
+
+
+ARGPROB = ["full_k10", "full_k24_T16", "full_k12_masked", "thread_k8"]
+
+
+@pytest.mark.parametrize("name", ARGPROB)
+def test_arg_probabilities_match_reference(name):
+    # calc_arg_likelihood / calc_arg_prior / calc_tree_prior (total_prob.cpp), restated in
+    # the reference's order: equal to its outputs on the same host
+    prob = Problem.load(os.path.join(GOLDEN, "argprob", name + ".prob"))
+    gold = np.load(os.path.join(GOLDEN, "argprob", name + ".npz"))
+    lik, prior, tprior = pyoracle.arg_prob(prob)
+    np.testing.assert_allclose(lik, gold["likelihood"], rtol=1e-13)
+    np.testing.assert_allclose(prior, gold["prior"], rtol=1e-13)
+    np.testing.assert_allclose(tprior, gold["tree_prior"], rtol=1e-13)
+    np.testing.assert_allclose(lik + prior, gold["joint"], rtol=1e-13)
+

@@ -77,6 +77,18 @@ PROTOTYPES = [
     ("arghmm_tree_prior_prob", C.c_double, [C.c_void_p, c_double_p, C.c_int, c_double_p]),
     ("arghmm_joint_prob", C.c_double, [C.c_void_p, c_double_p, C.c_int, c_double_p,
                                         C.c_double, C.c_double, c_char_pp, C.c_int, C.c_int]),
+    ("awg_read_arg_input", C.c_void_p, [C.c_char_p, C.c_char_p, C.c_int, c_double_p, C.c_int]),
+    ("awg_arg_input_dims", C.c_int, [C.c_void_p, c_int_p, c_int_p, c_int_p, c_int_p, c_int_p]),
+    ("awg_arg_input_name", C.c_char_p, [C.c_void_p, C.c_int]),
+    ("awg_arg_input_copy", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                     C.c_void_p, C.c_void_p]),
+    ("awg_free_arg_input", None, [C.c_void_p]),
+    ("awg_write_sites", C.c_int, [C.c_char_p, c_char_pp, C.c_int, C.c_char_p, C.c_int, C.c_int,
+                                  C.c_void_p]),
+    ("awg_write_smc", C.c_int, [C.c_char_p, c_char_pp, C.c_char_p, C.c_int, C.c_void_p,
+                                C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
+                                c_double_p, C.c_int]),
+    ("awg_formats_last_error", C.c_char_p, []),
     ("forward_alg", None, [C.c_int, C.c_int, c_double_pp, c_double_pp, c_double_pp]),
     ("backward_alg", None, [C.c_int, C.c_int, c_double_pp, c_double_pp, c_double_pp]),
     ("sample_hmm_posterior", None, [C.c_int, C.c_int, c_double_pp, c_double_pp, c_int_p]),

@@ -109,6 +109,36 @@ double arghmm_tree_prior_prob(awg_local_trees *trees, double *times, int ntimes,
 double arghmm_joint_prob(awg_local_trees *trees, double *times, int ntimes, double *popsizes,
                          double mu, double rho, char **seqs, int nseqs, int seqlen);
 
+/* Input formats, on the host (arg-sample's ingest, arg-sample.cpp:996-1155): a sites file
+ * (sequences.cpp:172-297) compressed by `compress` bases per non-variant column
+ * (find_compress_cols, sequences.cpp:523-592; make_sequences_from_sites, :315-343, default
+ * base 'A'), and optionally an SMC file of local trees (read_local_trees,
+ * local_tree.cpp:1422-1540; ages snapped to `times`) compressed the same way
+ * (compress_local_trees, local_tree.cpp:818-850). Leaves come out permuted so leaf i is
+ * sequence i (get_local_trees_ptrees, local_tree.cpp:1846); the SMC's leaves must be the
+ * first sequences of the sites file. ".gz" files are read through gzip. NULL and
+ * awg_formats_last_error() on failure. */
+typedef struct awg_arg_input awg_arg_input;
+awg_arg_input *awg_read_arg_input(const char *sites_path, const char *smc_path, int compress,
+                                  const double *times, int ntimes);
+int awg_arg_input_dims(const awg_arg_input *in, int *nseqs, int *seqlen, int *ntrees,
+                       int *nnodes, int *start_coord);
+const char *awg_arg_input_name(const awg_arg_input *in, int i);
+/* seqs: nseqs x seqlen; ptrees, ages: ntrees x nnodes; sprs: ntrees x 4; any may be NULL */
+int awg_arg_input_copy(const awg_arg_input *in, char *seqs, int *ptrees, int *ages, int *sprs,
+                       int *blocklens);
+void awg_free_arg_input(awg_arg_input *in);
+/* write_sites (sequences.cpp:133-157): the columns whose bases differ, 1-based */
+int awg_write_sites(const char *path, const char *const *names, int nseqs, const char *chrom,
+                    int start_coord, int seqlen, const char *seqs);
+/* write_local_trees (local_tree.cpp:1286-1362) for trees numbered by the default node
+ * mapping (a tree keeps the previous tree's node numbers; the broken node recoalesces) */
+int awg_write_smc(const char *path, const char *const *names, const char *chrom,
+                  int start_coord, const int *ptrees, const int *ages, const int *sprs,
+                  const int *blocklens, int ntrees, int nnodes, const double *times,
+                  int ntimes);
+const char *awg_formats_last_error(void);
+
 /* The dense HMM over a full nstates x nstates log transition matrix (hmm.h:14-19,
  * hmm.cpp:27-85; bound by argweaver/argweaverc.py:42-56). Tables are n row pointers of
  * nstates doubles, in natural log. As in the reference the caller fills the boundary:

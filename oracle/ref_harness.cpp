@@ -23,6 +23,10 @@
 //   argprob <problem> <out>          the ARG's probabilities through the reference's C
 //                                    exports (total_prob.cpp:315-382): likelihood, prior,
 //                                    first-tree prior, joint (4 doubles)
+//   ingest  <sites> <smc> <c> <out>  reads a sites file + SMC ARG the way arg-sample does
+//                                    (read_sites, find_compress_cols, compress_sites,
+//                                    make_sequences_from_sites, read_local_trees, set_seqids,
+//                                    compress_local_trees) and writes the full ARG problem
 //   sim1    <sites> <smc> <c> <out>  reads a sites file + SMC ARG the way arg-sample does
 //                                    (arg-sample.cpp:996-1155), removes the last sequence's
 //                                    thread (thread.cpp:425) and writes the external problem
@@ -492,6 +496,45 @@ static int cmd_sim1(const char *sites_file, const char *smc_file, int compress,
     return 0;
 }
 
+static int cmd_ingest(const char *sites_file, const char *smc_file, int compress,
+                      const char *out) {
+    const int ntimes = 20;
+    const double maxtime = 200e3, popsize = 1e4, rho = 1.5e-8, mu = 2.5e-8;
+    Sites sites;
+    CompressStream stream(sites_file);
+    if (!stream.stream || !read_sites(stream.stream, &sites, -1, -1)) die("cannot read sites");
+    stream.close();
+    SitesMapping mapping;
+    if (!find_compress_cols(&sites, compress, &mapping)) die("cannot compress");
+    compress_sites(&sites, &mapping);
+    Sequences sequences;
+    make_sequences_from_sites(&sites, &sequences);
+    ArgModel model(ntimes, maxtime, popsize, rho, mu);
+    LocalTrees *trees = new LocalTrees();
+    vector<std::string> seqnames;
+    CompressStream smc(smc_file, "r");
+    if (!smc.stream || !read_local_trees(smc.stream, model.times, model.ntimes, trees, seqnames))
+        die("cannot read smc");
+    if (!trees->set_seqids(seqnames, sequences.names)) die("seqids");
+    compress_local_trees(trees, &mapping, true);
+    Problem p;
+    p.ntimes = ntimes;
+    p.rho = rho * compress;
+    p.mu = mu * compress;
+    p.times.assign(model.times, model.times + ntimes);
+    p.popsizes.assign(model.popsizes, model.popsizes + ntimes);
+    p.internal = 0;
+    trees_to_problem(trees, p);
+    p.nseqs = sequences.get_num_seqs();
+    p.seqlen = sequences.length();
+    p.seqs.resize((size_t)p.nseqs * p.seqlen);
+    for (int r = 0; r < p.nseqs; r++)
+        memcpy(&p.seqs[(size_t)r * p.seqlen], sequences.seqs[r], p.seqlen);
+    write_problem(out, p);
+    delete trees;
+    return 0;
+}
+
 static int cmd_cut(const char *in, int seed, const char *out) {
     Problem p = read_problem(in);
     if (p.internal) die("cut: input must be a full (external-format) ARG");
@@ -519,6 +562,8 @@ int main(int argc, char **argv) {
     if (cmd == "densernd" && argc == 6)
         return cmd_densernd(atoi(argv[2]), atoi(argv[3]), atoi(argv[4]), argv[5]);
     if (cmd == "argprob" && argc == 4) return cmd_argprob(argv[2], argv[3]);
+    if (cmd == "ingest" && argc == 6)
+        return cmd_ingest(argv[2], argv[3], atoi(argv[4]), argv[5]);
     if (cmd == "sim1" && argc == 6) return cmd_sim1(argv[2], argv[3], atoi(argv[4]), argv[5]);
     if (cmd == "cut" && argc == 5) return cmd_cut(argv[2], atoi(argv[3]), argv[4]);
     die("bad arguments");

@@ -6,6 +6,7 @@ Run where the reference checkout exists (default /root/reference, or $AWG_REFERE
     python tests/golden/make_golden.py infsites   # only the infinite-sites ones
     python tests/golden/make_golden.py dense      # only the dense-HMM ones
     python tests/golden/make_golden.py argprob    # only the ARG-probability ones
+    python tests/golden/make_golden.py formats    # only the sites / SMC ones
 
 It builds the reference from its own sources (oracle/Makefile target ``ref``), writes
 each problem as an AWGPROB1 file and runs the reference's threading HMM on it through
@@ -197,6 +198,35 @@ def argprob(tmp):
         print(name, v)
 
 
+def formats(tmp):
+    """Sites and SMC files written by this library from seeded full ARGs (1 bp per column),
+    read back by the reference the way arg-sample reads them (harness `ingest`), at
+    compression 1 and 10 (1 and 4 where missing calls make most columns variant: the
+    reference refuses 10 there); one pair gzip-compressed."""
+    from argweaver_gb300 import formats as fm
+    out_dir = os.path.join(HERE, "formats")
+    os.makedirs(out_dir, exist_ok=True)
+    for name, k, L, seed, missing, gz, comp in (("k8", 8, 30000, 61, 0.0, False, (1, 10)),
+                                                ("k16_missing", 16, 8000, 62, 0.01, True, (1, 4))):
+        prob = simulate(k, L, seed, compress=1, add_thread=False, missing=missing)
+        names = [f"n{i}" for i in range(prob.nseqs)]
+        ext = ".gz" if gz else ""
+        sites = os.path.join(out_dir, name + ".sites" + ext)
+        smc = os.path.join(out_dir, name + ".smc" + ext)
+        fm.write_sites(sites, names, prob.seqs)
+        fm.write_smc(smc, prob, names)
+        for c in comp:
+            pc = os.path.join(out_dir, f"{name}_c{c}.prob")
+            run("ingest", sites, smc, c, pc)
+            # the reference's probabilities of the ARG it read
+            ob = os.path.join(tmp, "ap.bin")
+            run("argprob", pc, ob)
+            v = np.fromfile(ob, dtype=np.float64)
+            np.savez(os.path.join(out_dir, f"{name}_c{c}.npz"), likelihood=v[0], prior=v[1],
+                     tree_prior=v[2], joint=v[3])
+            print(name, c, v)
+
+
 def infsites(tmp):
     """The infinite-sites penalty (ArgModel::infsites_penalty, emit.cpp:847-862; arg-sample
     --infsites uses 1e-100): external, with missing calls, and an internal-branch cut."""
@@ -220,6 +250,10 @@ def main():
     if sys.argv[1:] == ["infsites"]:
         with tempfile.TemporaryDirectory() as tmp:
             infsites(tmp)
+        return
+    if sys.argv[1:] == ["formats"]:
+        with tempfile.TemporaryDirectory() as tmp:
+            formats(tmp)
         return
     if sys.argv[1:] == ["argprob"]:
         with tempfile.TemporaryDirectory() as tmp:
@@ -266,6 +300,7 @@ def main():
         dense(tmp)
         densernd(tmp)
         argprob(tmp)
+        formats(tmp)
 
 
 if __name__ == "__main__":

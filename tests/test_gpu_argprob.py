@@ -63,3 +63,18 @@ def test_arg_probability_edges():
     bad.ptrees = pt
     with pytest.raises(ValueError):
         refapi.arghmm_likelihood(bad)
+
+
+@pytest.mark.parametrize("name,ext,c", [("k8", "", 10), ("k16_missing", ".gz", 4)])
+def test_probabilities_of_an_arg_read_from_files(name, ext, c):
+    # sites + SMC files through the host readers, then the device: the reference's values
+    # for the ARG its own readers built from the same files
+    from argweaver_gb300 import formats as fm
+    fix = os.path.join(GOLDEN, "formats")
+    ref = Problem.load(os.path.join(fix, f"{name}_c{c}.prob"))
+    gold = np.load(os.path.join(fix, f"{name}_c{c}.npz"))
+    prob, _ = fm.read_arg(os.path.join(fix, name + ".sites" + ext),
+                          os.path.join(fix, name + ".smc" + ext), c, times=ref.times)
+    np.testing.assert_allclose(refapi.arghmm_likelihood(prob), gold["likelihood"], rtol=1e-12)
+    np.testing.assert_allclose(refapi.arghmm_prior_prob(prob), gold["prior"], rtol=1e-12)
+    np.testing.assert_allclose(refapi.arghmm_joint_prob(prob), gold["joint"], rtol=1e-12)

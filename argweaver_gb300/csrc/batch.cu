@@ -172,7 +172,7 @@ int ctx_launch(Ctx &C, const awg_problem *probs, awg_outputs *outs, int n, const
 
     HostPlan &plan = C.plan;
     plan = HostPlan();
-    if (!plan_layout(probs, n, plan, err, true)) return -1;
+    if (!plan_layout(probs, n, plan, err, false)) return -1;  // bytes: checked by plan_fill
 
     bool want_path = false, want_post = false, want_bw = false;
     for (int q = 0; q < n; q++) {
@@ -235,9 +235,11 @@ int ctx_launch(Ctx &C, const awg_problem *probs, awg_outputs *outs, int n, const
     if (dry) {
         dry_stage.resize(in_bytes);
         h = dry_stage.data();
-        plan_fill(probs, n, plan, PlanDst{(int *)(h + o_nodes), (int *)(h + o_map),
-                                          (uint8_t *)(h + o_seq), (uint8_t *)(h + o_cls),
-                                          (int *)(h + o_cvar)});
+        if (!plan_fill(probs, n, plan, PlanDst{(int *)(h + o_nodes), (int *)(h + o_map),
+                                               (uint8_t *)(h + o_seq), (uint8_t *)(h + o_cls),
+                                               (int *)(h + o_cvar)},
+                       &err))
+            return -1;
     } else {
         if (in_bytes > C.host_cap) {
             if (C.host) drop_host(C, C.host);
@@ -251,9 +253,11 @@ int ctx_launch(Ctx &C, const awg_problem *probs, awg_outputs *outs, int n, const
         // ---------------- stage inputs
         h = C.host;
         // per-node, per-column and sequence arrays straight into the staging buffer
-        plan_fill(probs, n, plan, PlanDst{(int *)(h + o_nodes), (int *)(h + o_map),
-                                          (uint8_t *)(h + o_seq), (uint8_t *)(h + o_cls),
-                                          (int *)(h + o_cvar)});
+        if (!plan_fill(probs, n, plan, PlanDst{(int *)(h + o_nodes), (int *)(h + o_map),
+                                               (uint8_t *)(h + o_seq), (uint8_t *)(h + o_cls),
+                                               (int *)(h + o_cvar)},
+                       &err))
+            return -1;
         memcpy(h + o_inst, plan.inst.data(), sizeof(InstDev) * plan.ninst);
         memcpy(h + o_blocks, plan.blocks.data(), sizeof(BlockDev) * plan.nblocks);
         memcpy(h + o_model, plan.model.data(), sizeof(double) * plan.model.size());

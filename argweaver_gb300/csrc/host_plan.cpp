@@ -10,7 +10,9 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstring>
+#include <atomic>
 #include <thread>
 
 namespace awg {
@@ -129,22 +131,59 @@ void set_plan_threads(int n) { g_plan_threads = std::max(0, n); }
 
 namespace {
 
-// Runs f(q) for q < n on up to hardware_concurrency threads (or the calling thread's cap),
-// problems interleaved.
+// Runs f(q) for q < n on up to hardware_concurrency threads (or the calling thread's cap).
+// Threads take problems from a shared counter, the costliest first (cost(q): sequence
+// bytes plus tree nodes), so a few large problems do not leave the other threads idle.
 template <typename Fn>
-void parallel_for(int n, Fn f) {
+void parallel_for(const awg_problem *probs, int n, Fn f) {
     const int hw = g_plan_threads > 0 ? g_plan_threads : (int)std::thread::hardware_concurrency();
     const int nthreads = std::max(1, std::min<int>(n, hw));
     if (nthreads <= 1 || n < 4) {
         for (int q = 0; q < n; q++) f(q);
         return;
     }
+    std::vector<int> order(n);
+    std::vector<long long> cost(n);
+    for (int q = 0; q < n; q++) {
+        order[q] = q;
+        const awg_problem &p = probs[q];
+        cost[q] = (long long)std::max(p.seqlen, 0) * std::max(p.nseqs, 0) +
+                  (long long)std::max(p.ntrees, 0) * std::max(p.nnodes, 0) * 4;
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+    std::atomic<int> next(0);
     std::vector<std::thread> pool;
     for (int t = 0; t < nthreads; t++)
-        pool.emplace_back([&, t]() {
-            for (int q = t; q < n; q += nthreads) f(q);
+        pool.emplace_back([&]() {
+            for (int k = next.fetch_add(1); k < n; k = next.fetch_add(1)) f(order[k]);
         });
     for (auto &th : pool) th.join();
+}
+
+// 1 for a byte outside A, C, G, T, N (either case of ACGT)
+inline uint8_t bad_base(uint8_t c) {
+    const uint8_t u = c & 0xDF;  // ACGT upper-cased; 'n' stays apart from 'N'
+    return !((u == 'A') | (u == 'C') | (u == 'G') | (u == 'T') | (c == 'N'));
+}
+
+// An 8 x 8 byte block transposed in registers: x[k] holds row k, byte j (little endian)
+// column j; afterwards x[j] holds column j. Three rounds swap 4x4, 2x2 and 1x1 sub-blocks.
+inline void transpose8x8(uint64_t x[8]) {
+    for (int k = 0; k < 4; k++) {
+        const uint64_t t = ((x[k] >> 32) ^ x[k + 4]) & 0x00000000FFFFFFFFull;
+        x[k] ^= t << 32;
+        x[k + 4] ^= t;
+    }
+    for (int a : {0, 1, 4, 5}) {
+        const uint64_t t = ((x[a] >> 16) ^ x[a + 2]) & 0x0000FFFF0000FFFFull;
+        x[a] ^= t << 16;
+        x[a + 2] ^= t;
+    }
+    for (int a : {0, 2, 4, 6}) {
+        const uint64_t t = ((x[a] >> 8) ^ x[a + 1]) & 0x00FF00FF00FF00FFull;
+        x[a] ^= t << 8;
+        x[a + 1] ^= t;
+    }
 }
 
 // Validation and per-tree state counts of one problem; "" or the failure.
@@ -221,7 +260,7 @@ bool plan_layout(const awg_problem *probs, int n, HostPlan &plan, std::string &e
     // pass 1: validation and sizes, problems in parallel
     std::vector<std::vector<int>> S_of(n), M_of(n);
     std::vector<std::string> errs(n);
-    parallel_for(n, [&](int q) { errs[q] = check_problem(probs[q], q, check_seqs, S_of[q], M_of[q]); });
+    parallel_for(probs, n, [&](int q) { errs[q] = check_problem(probs[q], q, check_seqs, S_of[q], M_of[q]); });
     long long nblocks = 0;
     for (int q = 0; q < n; q++) {
         if (!errs[q].empty()) { err = errs[q]; return false; }
@@ -288,8 +327,10 @@ bool plan_layout(const awg_problem *probs, int n, HostPlan &plan, std::string &e
     return true;
 }
 
-void plan_fill(const awg_problem *probs, int n, HostPlan &plan, const PlanDst &out) {
+bool plan_fill(const awg_problem *probs, int n, HostPlan &plan, const PlanDst &out,
+               std::string *err) {
     // pass 3: arrays (instances in parallel), straight into the caller's buffers
+    std::vector<std::string> errs(n);
     auto fill = [&](int q) {
         const awg_problem &p = probs[q];
         const InstDev &I = plan.inst[q];
@@ -323,39 +364,71 @@ void plan_fill(const awg_problem *probs, int n, HostPlan &plan, const PlanDst &o
                 B.prev_root = -1;
             }
         }
-        // column-major sequences and column classes
+        // column-major sequences, column classes and byte checks, a tile of columns at a
+        // time: the tile's transposed columns are classified and checked while in cache
         const int ns = I.nseqs, L = p.seqlen;
         uint8_t *dst = out.seqT + I.seq0;
-        constexpr int TILE = 256;  // columns per tile: the tile's rows stay in cache
-        for (int i0 = 0; i0 < L; i0 += TILE) {
-            const int i1 = std::min(L, i0 + TILE);
-            for (int r = 0; r < ns; r++) {
-                const char *row = p.seqs + (size_t)r * L;
-                for (int i = i0; i < i1; i++) dst[(size_t)i * ns + r] = (uint8_t)row[i];
-            }
-        }
         uint8_t *cls = out.colclass + I.col0;
         int *cv = out.colvar + I.col0;
-        for (int b = 0; b < p.ntrees; b++) {
-            BlockDev &B = plan.blocks[I.block0 + b];
-            int nv = 0;
-            for (int i = B.start; i < B.start + B.len; i++) {
+        constexpr int TILE = 256;
+        unsigned bad = 0;
+        int b = 0, bend = p.blocklens[0], nv = 0;
+        const uint8_t *src = (const uint8_t *)p.seqs;
+        const int r8 = ns & ~7;
+        for (int i0 = 0; i0 < L; i0 += TILE) {
+            const int i1 = std::min(L, i0 + TILE);
+            const int i8 = i0 + ((i1 - i0) & ~7);
+            // groups of 8 rows: 8 x 8 blocks through registers, 8-byte stores per column
+            for (int r = 0; r < r8; r += 8) {
+                const uint8_t *rows = src + (size_t)r * L;
+                for (int i = i0; i < i8; i += 8) {
+                    uint64_t x[8];
+                    for (int k = 0; k < 8; k++) memcpy(&x[k], rows + (size_t)k * L + i, 8);
+                    transpose8x8(x);
+                    for (int j = 0; j < 8; j++) memcpy(dst + (size_t)(i + j) * ns + r, &x[j], 8);
+                }
+                for (int i = i8; i < i1; i++)
+                    for (int k = 0; k < 8; k++) dst[(size_t)i * ns + r + k] = rows[(size_t)k * L + i];
+            }
+            for (int r = r8; r < ns; r++) {
+                const uint8_t *row = src + (size_t)r * L;
+                for (int i = i0; i < i1; i++) dst[(size_t)i * ns + r] = row[i];
+            }
+            for (int i = i0; i < i1; i++) {
+                while (i >= bend) {  // the block ends: its variant count
+                    plan.blocks[I.block0 + b].nvar = nv;
+                    b++;
+                    bend += p.blocklens[b];
+                    nv = 0;
+                }
                 const uint8_t *c = dst + (size_t)i * ns;
-                bool inv = true;
-                for (int r = 1; r < ns; r++)
-                    if (c[r] != c[0]) { inv = false; break; }
-                if (inv) {
+                uint8_t diff = 0;
+                for (int r = 1; r < ns; r++) diff |= (uint8_t)(c[r] ^ c[0]);
+                // bytes checked here, in cache: an invariant column's bytes all equal c[0]
+                if (!diff) {
+                    bad |= bad_base(c[0]);
                     cls[i] = (c[0] == 'N') ? COL_MASKED : COL_INVARIANT;
                     cv[i] = -1;
                 } else {
+                    for (int r = 0; r < ns; r++) bad |= bad_base(c[r]);
                     cls[i] = COL_VARIANT;
                     cv[i] = nv++;
                 }
             }
-            B.nvar = nv;
+        }
+        plan.blocks[I.block0 + b].nvar = nv;
+        if (bad) {
+            char buf[96];
+            snprintf(buf, sizeof(buf), "problem %d: sequence byte outside A,C,G,T,N", q);
+            errs[q] = buf;
         }
     };
-    parallel_for(n, fill);
+    parallel_for(probs, n, fill);
+    for (int q = 0; q < n; q++)
+        if (!errs[q].empty()) {
+            if (err) *err = errs[q];
+            return false;
+        }
     long long var = 0, vcols = 0;
     for (auto &B : plan.blocks) {
         B.var0 = var;
@@ -365,18 +438,20 @@ void plan_fill(const awg_problem *probs, int n, HostPlan &plan, const PlanDst &o
     }
     plan.total_var = var;
     plan.total_vcols = vcols;
+    return true;
 }
 
 bool build_plan(const awg_problem *probs, int n, HostPlan &plan, std::string &err) {
-    if (!plan_layout(probs, n, plan, err, true)) return false;
+    if (!plan_layout(probs, n, plan, err, false)) return false;
     plan.nodes.assign((size_t)plan.total_nodes * 4, -1);
     plan.mapping.assign((size_t)std::max(plan.total_map, 1LL), -1);
     plan.seqT.assign((size_t)std::max(plan.total_seq, 1LL), 'N');
     plan.colclass.assign((size_t)plan.total_cols, COL_INVARIANT);
     plan.colvar.assign((size_t)plan.total_cols, -1);
-    plan_fill(probs, n, plan, PlanDst{plan.nodes.data(), plan.mapping.data(), plan.seqT.data(),
-                                      plan.colclass.data(), plan.colvar.data()});
-    return true;
+    return plan_fill(probs, n, plan,
+                     PlanDst{plan.nodes.data(), plan.mapping.data(), plan.seqT.data(),
+                             plan.colclass.data(), plan.colvar.data()},
+                     &err);
 }
 
 }  // namespace awg

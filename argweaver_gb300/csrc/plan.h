@@ -39,12 +39,15 @@ struct PlanDst {
     int *colvar;         // [total_cols]
 };
 
-// Passes 1-2: validates the problems (sequence bytes too when check_seqs) and sizes the
-// plan: instances, blocks and every offset except the variant-emission ones.
+// Passes 1-2: validates the problems (sequence bytes too when check_seqs; plan_fill checks
+// them anyway) and sizes the plan: instances, blocks and every offset except the
+// variant-emission ones.
 bool plan_layout(const awg_problem *probs, int n, HostPlan &plan, std::string &err,
                  bool check_seqs);
-// Pass 3: fills the arrays into dst, the trees' roots and the variant-emission offsets.
-void plan_fill(const awg_problem *probs, int n, HostPlan &plan, const PlanDst &dst);
+// Pass 3: fills the arrays into dst, the trees' roots and the variant-emission offsets,
+// and checks every sequence byte (A, C, G, T or N); false with *err set on a bad byte.
+bool plan_fill(const awg_problem *probs, int n, HostPlan &plan, const PlanDst &dst,
+               std::string *err);
 // Both, into the plan's own vectors; returns false with a message on bad input.
 bool build_plan(const awg_problem *probs, int n, HostPlan &plan, std::string &err);
 

@@ -77,3 +77,20 @@ def test_invalid_problems_are_rejected():
         with pytest.raises(ValueError):
             api.cells(b)
     assert api.cells(prob) > 0
+
+
+def test_batch_sizing_checks_sequence_bytes():
+    # the batch path checks sequence bytes while it packs them (plan_fill); a dry sizing
+    # run goes through the same packing and must refuse a bad byte, in any problem
+    from argweaver_gb300 import capi
+    prob = Problem.load(os.path.join(GOLDEN, "dsmc_k8_s11.prob"))
+    lib = capi.load()
+    probs, _, _, keep = api._bind_batch([prob, prob], "fp32", False, True, False, None)
+    assert lib.awg_batch_device_bytes(probs, 2, capi.AWG_FP32, 1, 0) > 0
+    for row, col in ((0, 0), (prob.nseqs - 1, prob.seqlen - 1)):
+        seqs = prob.seqs.copy()
+        seqs[row, col] = ord("x")
+        probs, _, _, keep2 = api._bind_batch([prob, _bad(prob, seqs=seqs)], "fp32", False, True,
+                                             False, None)
+        assert lib.awg_batch_device_bytes(probs, 2, capi.AWG_FP32, 1, 0) < 0
+        assert "problem 1: sequence byte" in capi.last_error()

@@ -211,6 +211,31 @@ def posterior(prob: Problem, precision: str = "fp64") -> np.ndarray:
                      want_posterior=True)[0].posterior
 
 
+def sample_recombinations(prob: Problem, path: np.ndarray, uniforms: np.ndarray,
+                          cap: Optional[int] = None):
+    """Recombinations along a sampled thread path (sample_recombinations,
+    recomb.cpp:151-235), on the GPU, external problems: (columns, nodes (-1: the thread's
+    branch), times, uniforms used). The uniforms are consumed in order, one per draw
+    (at most 2 per column)."""
+    lib = capi.load()
+    b = _Bound(prob)
+    path = np.ascontiguousarray(path, dtype=np.int32)
+    u = np.ascontiguousarray(uniforms, dtype=np.float64)
+    if path.shape != (b.p.seqlen,):
+        raise ValueError("path must hold one state per column")
+    cap = b.p.seqlen if cap is None else int(cap)
+    pos, node, time = (np.zeros(max(cap, 1), dtype=np.int32) for _ in range(3))
+    used = C.c_int(0)
+    n = lib.awg_sample_recombinations(C.byref(b.c), path.ctypes.data_as(capi.c_int_p),
+                                      u.ctypes.data_as(capi.c_double_p), len(u),
+                                      pos.ctypes.data_as(capi.c_int_p),
+                                      node.ctypes.data_as(capi.c_int_p),
+                                      time.ctypes.data_as(capi.c_int_p), cap, C.byref(used))
+    if n < 0:
+        raise GpuError(capi.last_error())
+    return pos[:n].copy(), node[:n].copy(), time[:n].copy(), used.value
+
+
 def kernel_launches() -> int:
     return int(capi.load().awg_kernel_launches())
 

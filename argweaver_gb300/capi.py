@@ -77,6 +77,9 @@ PROTOTYPES = [
     ("arghmm_tree_prior_prob", C.c_double, [C.c_void_p, c_double_p, C.c_int, c_double_p]),
     ("arghmm_joint_prob", C.c_double, [C.c_void_p, c_double_p, C.c_int, c_double_p,
                                         C.c_double, C.c_double, c_char_pp, C.c_int, C.c_int]),
+    ("awg_sample_recombinations", C.c_int, [C.POINTER(AwgProblem), c_int_p, c_double_p,
+                                            C.c_int, c_int_p, c_int_p, c_int_p, C.c_int,
+                                            c_int_p]),
     ("awg_read_arg_input", C.c_void_p, [C.c_char_p, C.c_char_p, C.c_int, c_double_p, C.c_int]),
     ("awg_arg_input_dims", C.c_int, [C.c_void_p, c_int_p, c_int_p, c_int_p, c_int_p, c_int_p]),
     ("awg_arg_input_name", C.c_char_p, [C.c_void_p, C.c_int]),

@@ -433,5 +433,16 @@ double arghmm_joint_prob(awg_local_trees *trees, double *times, int ntimes, doub
     return arg_prob_call(trees, times, ntimes, popsizes, rho, mu, seqs, nseqs, seqlen, 3, -1);
 }
 
+int awg_sample_recombinations(const awg_problem *problem, const int *path,
+                              const double *uniforms, int n_uniforms, int *pos, int *node,
+                              int *time, int cap, int *used) {
+    g_err.clear();
+    std::string err;
+    const int rc = awg::sample_recombinations(problem, path, uniforms, n_uniforms, pos, node,
+                                              time, cap, used, err);
+    if (rc < 0) set_error(err);
+    return rc;
+}
+
 }  // extern "C"
 

@@ -5,6 +5,7 @@
 
 #include <string>
 
+#include "argweaver_gb300.h"
 #include "awg_internal.h"
 
 namespace awg {
@@ -49,6 +50,12 @@ void note_launch();
 // reference's row pointers; false with err set on failure.
 bool dense_hmm(int which, int n, int nstates, double **trans, double **emit, double **tab,
                int *path, std::string &err);
+
+// sample_recombinations (recomb.cpp:151-235) along a state path, on the device, external
+// problems: the recombinations' columns, nodes (-1: the thread) and times in pos/node/time
+// (cap entries); the count, or < 0 with err set. *used: the uniforms consumed.
+int sample_recombinations(const awg_problem *p, const int *path, const double *u, int nu,
+                          int *pos, int *node, int *time, int cap, int *used, std::string &err);
 
 // Probabilities of a whole ARG (total_prob.cpp) on the device: what = 1 likelihood, 2 prior,
 // 4 first-tree prior (bits combine); out[0..2] in that order. Trees as the reference's

@@ -278,3 +278,16 @@ def arghmm_tree_prior_prob(prob: Problem) -> float:
 def arghmm_joint_prob(prob: Problem) -> float:
     """Likelihood + prior (calc_arg_joint_prob, total_prob.cpp:303-308)."""
     return _arg_call(prob, "joint")
+
+
+def sample_recombinations(prob: Problem, path: np.ndarray, seed: int):
+    """sample_recombinations (recomb.cpp:151-235) along `path` with the draws rand() gives
+    after srand(seed), as the reference draws them: (columns, nodes, times, draws used).
+    The generator is left as after those draws plus the unused ones (2 per column are
+    drawn up front)."""
+    from . import api
+    srand(seed)
+    n = 2 * prob.seqlen + 2
+    u = np.array([_libc.rand() / 2147483647.0 for _ in range(n)], dtype=np.float64)
+    return api.sample_recombinations(prob, path, u)
+

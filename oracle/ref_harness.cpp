@@ -23,6 +23,10 @@
 //   argprob <problem> <out>          the ARG's probabilities through the reference's C
 //                                    exports (total_prob.cpp:315-382): likelihood, prior,
 //                                    first-tree prior, joint (4 doubles)
+//   recomb  <problem> <path> <seed> <out>
+//                                    sample_recombinations (recomb.cpp:151-235) along the
+//                                    int32 state path after srand(seed): count, positions,
+//                                    nodes, times, then the next rand() value
 //   ingest  <sites> <smc> <c> <out>  reads a sites file + SMC ARG the way arg-sample does
 //                                    (read_sites, find_compress_cols, compress_sites,
 //                                    make_sequences_from_sites, read_local_trees, set_seqids,
@@ -58,6 +62,7 @@
 #include "argweaver/local_tree.h"
 #include "argweaver/matrices.h"
 #include "argweaver/model.h"
+#include "argweaver/recomb.h"
 #include "argweaver/sample_thread.h"
 #include "argweaver/sequences.h"
 #include "argweaver/states.h"
@@ -535,6 +540,41 @@ static int cmd_ingest(const char *sites_file, const char *smc_file, int compress
     return 0;
 }
 
+static int cmd_recomb(const char *in, const char *path_file, int seed, const char *out) {
+    Problem p = read_problem(in);
+    LocalTrees *trees = make_trees(p);
+    ArgModel model(p.ntimes, p.times.data(), p.popsizes.data(), p.rho, p.mu);
+    vector<char *> sp = seq_ptrs(p);
+    Sequences sequences(sp.data(), p.nseqs, p.seqlen);
+    const bool internal = p.internal != 0;
+    ArgHmmMatrixList matrix_list(&model, &sequences, trees);
+    matrix_list.set_internal(internal);
+    matrix_list.setup();
+    vector<int> path(p.seqlen);
+    FILE *pf = fopen(path_file, "rb");
+    if (!pf) die("cannot read path");
+    rd(pf, path.data(), p.seqlen);
+    fclose(pf);
+    srand(seed);
+    vector<int> pos;
+    vector<NodePoint> recombs;
+    sample_recombinations(trees, &model, &matrix_list, path.data() - trees->start_coord, pos,
+                          recombs, internal);
+    const int next = rand();
+    FILE *f = fopen(out, "wb");
+    if (!f) die("cannot write output");
+    wr(f, "AWGREC01", 8);
+    int hdr[2] = {(int)pos.size(), next};
+    wr(f, hdr, 2);
+    for (size_t k = 0; k < pos.size(); k++) {
+        int v[3] = {pos[k] - trees->start_coord, recombs[k].node, recombs[k].time};
+        wr(f, v, 3);
+    }
+    fclose(f);
+    delete trees;
+    return 0;
+}
+
 static int cmd_cut(const char *in, int seed, const char *out) {
     Problem p = read_problem(in);
     if (p.internal) die("cut: input must be a full (external-format) ARG");
@@ -562,6 +602,8 @@ int main(int argc, char **argv) {
     if (cmd == "densernd" && argc == 6)
         return cmd_densernd(atoi(argv[2]), atoi(argv[3]), atoi(argv[4]), argv[5]);
     if (cmd == "argprob" && argc == 4) return cmd_argprob(argv[2], argv[3]);
+    if (cmd == "recomb" && argc == 6)
+        return cmd_recomb(argv[2], argv[3], atoi(argv[4]), argv[5]);
     if (cmd == "ingest" && argc == 6)
         return cmd_ingest(argv[2], argv[3], atoi(argv[4]), argv[5]);
     if (cmd == "sim1" && argc == 6) return cmd_sim1(argv[2], argv[3], atoi(argv[4]), argv[5]);

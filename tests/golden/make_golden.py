@@ -7,6 +7,7 @@ Run where the reference checkout exists (default /root/reference, or $AWG_REFERE
     python tests/golden/make_golden.py dense      # only the dense-HMM ones
     python tests/golden/make_golden.py argprob    # only the ARG-probability ones
     python tests/golden/make_golden.py formats    # only the sites / SMC ones
+    python tests/golden/make_golden.py recomb     # only the recombination-sampling ones
 
 It builds the reference from its own sources (oracle/Makefile target ``ref``), writes
 each problem as an AWGPROB1 file and runs the reference's threading HMM on it through
@@ -227,6 +228,56 @@ def formats(tmp):
             print(name, c, v)
 
 
+def recomb(tmp):
+    """sample_recombinations (recomb.cpp:151-235) along each fixture's sampled path, after
+    srand(seed + 7000): the recombination positions, nodes and times, and the rand() value
+    that follows (which pins how many draws the sampler consumed)."""
+    out_dir = os.path.join(HERE, "recomb")
+    os.makedirs(out_dir, exist_ok=True)
+    for f in sorted(os.listdir(HERE)):
+        if not f.endswith(".npz"):
+            continue
+        name = f[:-4]
+        gold = np.load(os.path.join(HERE, f))
+        if "path" not in gold.files:
+            continue
+        pp = os.path.join(HERE, name + ".prob")
+        path_file = os.path.join(tmp, "path.bin")
+        np.ascontiguousarray(gold["path"], dtype=np.int32).tofile(path_file)
+        seed = int(gold["seed"]) + 7000
+        ob = os.path.join(tmp, "rec.bin")
+        run("recomb", pp, path_file, seed, ob)
+        d = open(ob, "rb").read()
+        assert d[:8] == b"AWGREC01"
+        n, nxt = (int(x) for x in np.frombuffer(d, np.int32, 2, 8))
+        rec = np.frombuffer(d, np.int32, 3 * n, 16).reshape(n, 3)
+        np.savez(os.path.join(out_dir, name + ".npz"), seed=seed, pos=rec[:, 0].copy(),
+                 node=rec[:, 1].copy(), time=rec[:, 2].copy(), next_rand=nxt)
+        print(name, n)
+    # larger external problems, paths drawn by the oracle's traceback (pinned to the
+    # reference's) after srand(seed): many more state changes
+    for k, L, seed, T, missing, rho in ((12, 10000, 73, 32, 0.01, 1.6e-7),
+                                        (8, 15000, 74, 20, 0.0, 5e-7)):
+        name = f"extra_k{k}_T{T}"
+        prob = simulate(k, L, seed, ntimes=T, missing=missing, rho=rho)
+        pp = os.path.join(out_dir, name + ".prob")
+        prob.save(pp)
+        fw, _ = pyoracle.forward(prob)
+        path = pyoracle.traceback(prob, fw, pyoracle.rand_uniforms(seed, prob.seqlen))
+        path_file = os.path.join(tmp, "path.bin")
+        np.ascontiguousarray(path, dtype=np.int32).tofile(path_file)
+        rseed = seed + 7000
+        ob = os.path.join(tmp, "rec.bin")
+        run("recomb", pp, path_file, rseed, ob)
+        d = open(ob, "rb").read()
+        n, nxt = (int(x) for x in np.frombuffer(d, np.int32, 2, 8))
+        rec = np.frombuffer(d, np.int32, 3 * n, 16).reshape(n, 3)
+        np.savez_compressed(os.path.join(out_dir, name + ".npz"), seed=rseed,
+                            path=path.astype(np.int32), pos=rec[:, 0].copy(),
+                            node=rec[:, 1].copy(), time=rec[:, 2].copy(), next_rand=nxt)
+        print(name, n)
+
+
 def infsites(tmp):
     """The infinite-sites penalty (ArgModel::infsites_penalty, emit.cpp:847-862; arg-sample
     --infsites uses 1e-100): external, with missing calls, and an internal-branch cut."""
@@ -250,6 +301,10 @@ def main():
     if sys.argv[1:] == ["infsites"]:
         with tempfile.TemporaryDirectory() as tmp:
             infsites(tmp)
+        return
+    if sys.argv[1:] == ["recomb"]:
+        with tempfile.TemporaryDirectory() as tmp:
+            recomb(tmp)
         return
     if sys.argv[1:] == ["formats"]:
         with tempfile.TemporaryDirectory() as tmp:
@@ -301,6 +356,7 @@ def main():
         densernd(tmp)
         argprob(tmp)
         formats(tmp)
+        recomb(tmp)
 
 
 if __name__ == "__main__":

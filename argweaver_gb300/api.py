@@ -214,8 +214,8 @@ def posterior(prob: Problem, precision: str = "fp64") -> np.ndarray:
 def sample_recombinations(prob: Problem, path: np.ndarray, uniforms: np.ndarray,
                           cap: Optional[int] = None):
     """Recombinations along a sampled thread path (sample_recombinations,
-    recomb.cpp:151-235), on the GPU, external problems: (columns, nodes (-1: the thread's
-    branch), times, uniforms used). The uniforms are consumed in order, one per draw
+    recomb.cpp:151-235), on the GPU: (columns, nodes (-1: the thread's branch of an external
+    problem), times, uniforms used). The uniforms are consumed in order, one per draw
     (at most 2 per column)."""
     lib = capi.load()
     b = _Bound(prob)

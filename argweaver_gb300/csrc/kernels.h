@@ -51,8 +51,8 @@ void note_launch();
 bool dense_hmm(int which, int n, int nstates, double **trans, double **emit, double **tab,
                int *path, std::string &err);
 
-// sample_recombinations (recomb.cpp:151-235) along a state path, on the device, external
-// problems: the recombinations' columns, nodes (-1: the thread) and times in pos/node/time
+// sample_recombinations (recomb.cpp:151-235) along a state path, on the device: the
+// recombinations' columns, nodes (-1: the thread) and times in pos/node/time
 // (cap entries); the count, or < 0 with err set. *used: the uniforms consumed.
 int sample_recombinations(const awg_problem *p, const int *path, const double *u, int nu,
                           int *pos, int *node, int *time, int cap, int *used, std::string &err);

@@ -33,10 +33,6 @@ int sample_recombinations(const awg_problem *p, const int *path, const double *u
         err = "sample_recombinations: bad arguments";
         return -1;
     }
-    if (p->internal) {
-        err = "sample_recombinations: external-branch problems only";
-        return -1;
-    }
     HostPlan plan;
     if (!build_plan(p, 1, plan, err)) return -1;
     const int L = p->seqlen;
@@ -65,6 +61,8 @@ int sample_recombinations(const awg_problem *p, const int *path, const double *u
     in.nnodes = p->nnodes;
     in.nu = nu;
     in.start_coord = p->start_coord;
+    in.internal = p->internal != 0;
+    in.minage = p->minage;
     int *dout = (int *)(D + o_out);
     in.pos = dout;
     in.node = dout + std::max(cap, 1);

@@ -206,13 +206,14 @@ int awg_run_batch(const awg_problem *problems, awg_outputs *outputs, int n, int 
 long long awg_batch_device_bytes(const awg_problem *problems, int n, int precision, int want_path,
                                  int want_posterior);
 
-/* sample_recombinations (recomb.cpp:151-235), on the device, for an external problem: the
- * recombinations along a sampled thread path (path: the state index of every column, as
+/* sample_recombinations (recomb.cpp:151-235), on the device, external or internal-branch:
+ * the recombinations along a sampled thread path (path: the state index of every column, as
  * awg_outputs.path and the reference's thread_path hold it). The draws are the caller's
  * uniforms, consumed in order, one per draw: rand()/RAND_MAX after srand(seed) reproduces
  * the reference's recombinations. Returns their count, their columns, nodes (-1: the new
- * thread's branch) and times in pos/node/time (cap entries), and the uniforms used; or a
- * negative code (awg_last_error). At most 2 * seqlen uniforms are used. */
+ * thread's branch of an external problem; internal ones name the cut subtree's root) and
+ * times in pos/node/time (cap entries), and the uniforms used; or a negative code
+ * (awg_last_error). At most 2 * seqlen uniforms are used. */
 int awg_sample_recombinations(const awg_problem *problem, const int *path,
                               const double *uniforms, int n_uniforms, int *pos, int *node,
                               int *time, int cap, int *used);

@@ -12,7 +12,8 @@ extern "C" int rs_host(const awg_problem *p, const int *path, const double *u, i
     std::string err;
     if (!awg::build_plan(p, 1, plan, err)) return -100;
     awg::RsInstance in{(const int4 *)plan.nodes.data(), p->blocklens, path, u, p->ntrees,
-                       p->nnodes, nu, p->start_coord, pos, node, time, cap};
+                       p->nnodes, nu, p->start_coord, p->internal != 0, p->minage,
+                       pos, node, time, cap};
     const double *m = plan.model.data();
     const awg::RsModel mm{p->ntimes, m + awg::M_TIMES, m + awg::M_TIMESTEPS,
                           m + awg::M_COALSTEPS, m + awg::M_POPSIZES, m[awg::M_CONST]};

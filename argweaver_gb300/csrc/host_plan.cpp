@@ -257,71 +257,102 @@ bool plan_layout(const awg_problem *probs, int n, HostPlan &plan, std::string &e
     plan.ninst = n;
     plan.inst.resize(n);
 
-    // pass 1: validation and sizes, problems in parallel
+    // pass 1: validation and sizes, problems in parallel, with each problem's totals
+    struct Tot {
+        long long cells = 0, states = 0, t2 = 0;
+        int maxS = 1, maxM = 1, maxlen = 1;
+    };
     std::vector<std::vector<int>> S_of(n), M_of(n);
+    std::vector<Tot> tot(n);
     std::vector<std::string> errs(n);
-    parallel_for(probs, n, [&](int q) { errs[q] = check_problem(probs[q], q, check_seqs, S_of[q], M_of[q]); });
+    parallel_for(probs, n, [&](int q) {
+        errs[q] = check_problem(probs[q], q, check_seqs, S_of[q], M_of[q]);
+        if (!errs[q].empty()) return;
+        Tot &t = tot[q];
+        for (int b = 0; b < probs[q].ntrees; b++) {
+            const int S = S_of[q][b], len = probs[q].blocklens[b];
+            t.cells += (long long)len * std::max(S, 1);
+            t.states += std::max(S, 1);  // a zero-state space still takes one slot
+            t.t2 += M_of[q][b];
+            t.maxS = std::max(t.maxS, S);
+            t.maxM = std::max(t.maxM, M_of[q][b]);
+            t.maxlen = std::max(t.maxlen, len);
+        }
+    });
+    // offsets of every problem: a prefix over the problems
+    struct Off {
+        long long cell, col, st, t2, nodes, map, seq;
+        int blk;
+    };
+    std::vector<Off> off(n);
+    long long cell = 0, col = 0, st = 0, t2 = 0, nodes = 0, map = 0, seq = 0;
     long long nblocks = 0;
     for (int q = 0; q < n; q++) {
         if (!errs[q].empty()) { err = errs[q]; return false; }
         const awg_problem &p = probs[q];
-        for (int b = 0; b < p.ntrees; b++) {
-            plan.maxS = std::max(plan.maxS, S_of[q][b]);
-            plan.maxM = std::max(plan.maxM, M_of[q][b]);
-        }
-        nblocks += p.ntrees;
+        const int nleaves = (p.nnodes + 1) / 2;
+        const int nemit = p.internal ? nleaves : nleaves + 1;
+        off[q] = Off{cell, col, st, t2, nodes, map, seq, (int)nblocks};
+        plan.maxS = std::max(plan.maxS, tot[q].maxS);
+        plan.maxM = std::max(plan.maxM, tot[q].maxM);
+        plan.maxlen = std::max(plan.maxlen, tot[q].maxlen);
         plan.maxnodes = std::max(plan.maxnodes, p.nnodes);
         plan.maxT = std::max(plan.maxT, p.ntimes);
+        cell += tot[q].cells;
+        st += tot[q].states;
+        t2 += tot[q].t2;
+        nodes += (long long)p.ntrees * p.nnodes;
+        map += (long long)(p.ntrees - 1) * p.nnodes;
+        col += p.seqlen;
+        seq += (long long)p.seqlen * nemit;
+        nblocks += p.ntrees;
     }
     plan.nblocks = (int)nblocks;
     plan.blocks.resize(nblocks);
     plan.model.assign((size_t)n * MODEL_STRIDE, 0.0);
 
-    // pass 2: offsets
-    long long cell = 0, col = 0, st = 0, t2 = 0, nodes = 0, map = 0, seq = 0;
-    int blk = 0;
-    for (int q = 0; q < n; q++) {
+    // pass 2: instance and block descriptors, problems in parallel
+    parallel_for(probs, n, [&](int q) {
         const awg_problem &p = probs[q];
+        const Off &o = off[q];
         const int nleaves = (p.nnodes + 1) / 2;
         const int nemit = p.internal ? nleaves : nleaves + 1;
         InstDev &I = plan.inst[q];
         I.T = p.ntimes; I.internal = p.internal ? 1 : 0; I.minage = p.minage;
         I.nleaves = nleaves; I.nnodes = p.nnodes; I.nseqs = nemit; I.seqlen = p.seqlen;
-        I.ntrees = p.ntrees; I.block0 = blk; I.pad = 0;
-        I.cell0 = cell; I.col0 = col; I.seq0 = seq; I.model0 = (long long)q * MODEL_STRIDE;
+        I.ntrees = p.ntrees; I.block0 = o.blk; I.pad = 0;
+        I.cell0 = o.cell; I.col0 = o.col; I.seq0 = o.seq; I.model0 = (long long)q * MODEL_STRIDE;
 
         model_arrays(p.times, p.popsizes, p.ntimes, p.rho, p.mu, p.infsites_penalty,
                      &plan.model[(size_t)q * MODEL_STRIDE]);
 
-        int pos = 0;
+        long long cellq = o.cell, stq = o.st, t2q = o.t2, nodesq = o.nodes, mapq = o.map;
+        int pos = 0, blk = o.blk;
         for (int b = 0; b < p.ntrees; b++, blk++) {
             BlockDev &B = plan.blocks[blk];
             memset(&B, 0, sizeof(B));
             B.inst = q; B.b = b; B.start = pos; B.len = p.blocklens[b];
             B.S = S_of[q][b];
             B.S1 = b > 0 ? S_of[q][b - 1] : 0;
-            B.nodes0 = (int)nodes;
-            B.prev_nodes0 = b > 0 ? (int)(nodes - p.nnodes) : -1;
+            B.nodes0 = (int)nodesq;
+            B.prev_nodes0 = b > 0 ? (int)(nodesq - p.nnodes) : -1;
             const int *s = p.sprs + (size_t)b * 4;
             for (int k = 0; k < 4; k++) B.spr[k] = b > 0 ? s[k] : -1;
-            B.map0 = b > 0 ? (int)map : -1;
+            B.map0 = b > 0 ? (int)mapq : -1;
             B.M = M_of[q][b];
-            B.cell0 = cell;
-            B.state0 = st;
+            B.cell0 = cellq;
+            B.state0 = stq;
             B.prev_state0 = b > 0 ? plan.blocks[blk - 1].state0 : -1;
-            B.gptr0 = st + blk;
-            B.t2_0 = t2;
-            plan.maxlen = std::max(plan.maxlen, B.len);
-            cell += (long long)B.len * std::max(B.S, 1);
-            st += std::max(B.S, 1);  // a zero-state space still takes one slot
-            t2 += B.M;
-            nodes += p.nnodes;
-            if (b > 0) map += p.nnodes;
+            B.gptr0 = stq + blk;
+            B.t2_0 = t2q;
+            cellq += (long long)B.len * std::max(B.S, 1);
+            stq += std::max(B.S, 1);
+            t2q += B.M;
+            nodesq += p.nnodes;
+            if (b > 0) mapq += p.nnodes;
             pos += B.len;
         }
-        col += p.seqlen;
-        seq += (long long)p.seqlen * nemit;
-    }
+    });
     plan.total_cells = cell; plan.total_cols = col; plan.total_states = st;
     plan.total_M = t2; plan.total_nodes = nodes; plan.total_map = map; plan.total_seq = seq;
     return true;

@@ -1933,5 +1933,122 @@ int oracle_arg_prob(const oracle_problem *p, double *out) {
     return 0;
 }
 
+// ----------------------------------------------------------------------------- recombinations
+// sample_recombinations (recomb.cpp:151-235) with recomb_prob_unnormalized (:14-125) and
+// get_possible_recomb (:128-148), over the oracle's blocks (states, lineage counts and
+// TransMatrix as the reference builds them). u: the draws in order (frand() values).
+
+static double oracle_recomb_prob(const Tree &t, const Model &m, const Lineages &l,
+                                 int last_node, int last_time, int state_time, int rnode,
+                                 int k, bool internal) {
+    const int j = state_time;
+    int root_time, recomb_parent_age;
+    if (internal) {
+        const int subtree_root = t.c0[t.root], maintree_root = t.c1[t.root];
+        root_time = std::max(t.age[maintree_root], last_time);
+        recomb_parent_age = (rnode == subtree_root || t.parent[rnode] == -1 ||
+                             rnode == last_node) ? last_time : t.age[t.parent[rnode]];
+    } else {
+        root_time = std::max(t.age[t.root], last_time);
+        recomb_parent_age = (rnode == -1 || t.parent[rnode] == -1 || rnode == last_node)
+                                ? last_time : t.age[t.parent[rnode]];
+    }
+    const int nbranches_k = l.nbranches[k] + int(k < last_time);
+    const int nrecombs_k = l.nrecombs[k] + int(k <= last_time) + int(k == last_time) -
+                           int(k == root_time);
+    const double precomb = nbranches_k * m.time_steps[k] / nrecombs_k;
+    double sum = 0.0;
+    for (int q = k; q < j - 1; q++) {
+        const int nb = l.nbranches[q] + int(q < last_time) - int(q < recomb_parent_age);
+        sum += (m.time_steps[q] * nb / (2.0 * m.popsizes[q]));
+    }
+    double pcoal = 1.0;
+    const int nbranches_j = l.nbranches[j] + int(j < last_time) - int(j < recomb_parent_age);
+    if (k == j) {
+        if (j < m.T - 2)
+            pcoal = 1.0 - exp(-m.coal_time_steps[2 * j] * nbranches_j / (2.0 * m.popsizes[j]));
+    } else {
+        const int q = j - 1;
+        const int nb = l.nbranches[q] + int(q < last_time) - int(q < recomb_parent_age);
+        sum += (m.coal_time_steps[2 * q] * nb / (2.0 * m.popsizes[q]));
+        if (j < m.T - 2)
+            pcoal = 1.0 - exp(-m.coal_time_steps[2 * j - 1] * nb / (2.0 * m.popsizes[q]) -
+                              m.coal_time_steps[2 * j] * nbranches_j / (2.0 * m.popsizes[j]));
+    }
+    const int ncoals_j = l.ncoals[j] - int(j <= recomb_parent_age) -
+                         int(j == recomb_parent_age) + int(j <= last_time) +
+                         int(j == last_time);
+    pcoal /= ncoals_j;
+    return precomb * exp(-sum) * pcoal;
+}
+
+int oracle_sample_recombinations(const oracle_problem *p, const int *path, const double *u,
+                                 int nu, int *pos, int *node, int *time, int cap, int *used) {
+    Hmm h;
+    if (!setup(p, h)) return -10;
+    int count = 0, cu = 0;
+    for (size_t b = 0; b < h.arg.trees.size(); b++) {
+        Block blk;
+        if (!make_block(h, (int)b, blk, false)) return -11;
+        const Tree &t = h.arg.trees[b];
+        if (h.internal && blk.states.size() == 0) continue;
+        const int S = blk.states.size();
+        const int start = blk.start + 1;  // every block: the region's start or a switch
+        const int end = blk.start + blk.len;
+        int next_recomb = -1;
+        for (int i = start; i < end; i++) {
+            const int ia = p->start_coord + i;
+            if (path[i] < 0 || path[i] >= S || path[i - 1] < 0 || path[i - 1] >= S) return -1;
+            if (path[i] == path[i - 1]) {
+                if (ia > next_recomb) {
+                    const int last = path[i - 1];
+                    const int a = blk.states.time[last];
+                    const double self_trans = blk.tm.get(t, blk.states, last, last);
+                    const double rate = 1.0 - (blk.tm.norecombs[a] / self_trans);
+                    if (cu >= nu) return -2;
+                    const double e = -log(u[cu++]) / rate;  // expovariate (common.h:124)
+                    next_recomb = int(std::min(double(p->start_coord + end), ia + e));
+                }
+                if (ia < next_recomb) continue;
+            }
+            next_recomb = -1;
+            const int sn = blk.states.node[path[i]], st = blk.states.time[path[i]];
+            const int ln = blk.states.node[path[i - 1]], lt = blk.states.time[path[i - 1]];
+            vector<int> cn, ct;
+            const int end_time = std::min(st, lt);
+            if (sn == ln)
+                for (int k = t.age[sn]; k <= end_time; k++) { cn.push_back(sn); ct.push_back(k); }
+            if (h.internal) {
+                const int sub = t.c0[t.root];
+                for (int k = t.age[sub]; k <= end_time; k++) { cn.push_back(sub); ct.push_back(k); }
+            } else {
+                for (int k = 0; k <= end_time; k++) { cn.push_back(-1); ct.push_back(k); }
+            }
+            vector<double> probs(cn.size());
+            for (size_t c = 0; c < cn.size(); c++)
+                probs[c] = oracle_recomb_prob(t, h.m, blk.lineages, ln, lt, st, cn[c], ct[c],
+                                              h.internal);
+            // sample (common.h:272-290)
+            double total = 0.0;
+            for (double w : probs) total += w;
+            if (cu >= nu) return -2;
+            const double pick = u[cu++] * total;
+            int pickc = (int)probs.size() - 1;
+            double x = 0.0;
+            for (size_t c = 0; c < probs.size(); c++) {
+                x += probs[c];
+                if (x >= pick) { pickc = (int)c; break; }
+            }
+            if (count >= cap) return -3;
+            pos[count] = i;
+            node[count] = cn[pickc];
+            time[count] = ct[pickc];
+            count++;
+        }
+    }
+    *used = cu;
+    return count;
+}
+
 }  // extern "C"
 

@@ -79,6 +79,12 @@ int oracle_dense_sample(int n, int S, const double *trans, const double *fw, con
  * first tree's coalescent prior. */
 int oracle_arg_prob(const oracle_problem *p, double *out);
 
+/* sample_recombinations (recomb.cpp:151-235) along a state path: u holds the draws in
+ * order; the count of recombinations (columns, nodes, times in pos/node/time, cap entries)
+ * and the draws used; negative on a bad path (-1), too few draws (-2), a full output (-3). */
+int oracle_sample_recombinations(const oracle_problem *p, const int *path, const double *u,
+                                 int nu, int *pos, int *node, int *time, int cap, int *used);
+
 /* Total cells: sum over columns of max(nstates,1). */
 long long oracle_cells(const oracle_problem *p);
 

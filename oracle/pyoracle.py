@@ -54,7 +54,10 @@ def load():
                            ("oracle_dense_forward", [C.c_int, C.c_int] + [C.c_void_p] * 3),
                            ("oracle_dense_backward", [C.c_int, C.c_int] + [C.c_void_p] * 3),
                            ("oracle_dense_sample", [C.c_int, C.c_int] + [C.c_void_p] * 4),
-                           ("oracle_arg_prob", [P, C.c_void_p])]:
+                           ("oracle_arg_prob", [P, C.c_void_p]),
+                           ("oracle_sample_recombinations", [P, C.c_void_p, C.c_void_p, C.c_int,
+                                                             C.c_void_p, C.c_void_p, C.c_void_p,
+                                                             C.c_int, C.c_void_p])]:
             fn = getattr(lib, name)
             fn.restype = C.c_int
             fn.argtypes = args
@@ -260,4 +263,21 @@ def arg_prob(prob) -> np.ndarray:
     out = np.zeros(3)
     _check(load().oracle_arg_prob(b.ref, out.ctypes.data), "ARG probability")
     return out
+
+
+def sample_recombinations(prob, path, u):
+    """(columns, nodes, times, draws used) of sample_recombinations (recomb.cpp:151-235)
+    along `path` with the draws `u` in order."""
+    b = Bound(prob)
+    path = np.ascontiguousarray(path, dtype=np.int32)
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    L = prob.seqlen
+    pos, node, time = (np.zeros(L, dtype=np.int32) for _ in range(3))
+    used = np.zeros(1, dtype=np.int32)
+    n = load().oracle_sample_recombinations(b.ref, path.ctypes.data, u.ctypes.data, len(u),
+                                            pos.ctypes.data, node.ctypes.data, time.ctypes.data,
+                                            L, used.ctypes.data)
+    if n < 0:
+        raise ValueError(f"oracle sample_recombinations failed ({n})")
+    return pos[:n].copy(), node[:n].copy(), time[:n].copy(), int(used[0])
 

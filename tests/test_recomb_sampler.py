@@ -91,3 +91,59 @@ def test_host_routine_edges(shim):
     bad = p32.copy()
     bad[rec["pos"][0]] = 10 ** 6
     assert run_host(shim, prob, bad, u)[0] == -1
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_oracle_matches_reference(name):
+    import pyoracle
+    prob, path, rec = case(name)
+    u = draws(int(rec["seed"]), 2 * prob.seqlen + 2)
+    pos, node, time, used = pyoracle.sample_recombinations(prob, path, u)
+    np.testing.assert_array_equal(pos, rec["pos"])
+    np.testing.assert_array_equal(node, rec["node"])
+    np.testing.assert_array_equal(time, rec["time"])
+    assert u[used] == int(rec["next_rand"]) / RMAX
+
+
+def stress_path(prob, path, seed):
+    """The path with extra state changes inside blocks (each a valid state of its tree):
+    every recombination branch of the sampler runs many times."""
+    import pyoracle
+    ns = pyoracle.nstates(prob)
+    rng = np.random.default_rng(seed)
+    out = np.array(path, dtype=np.int32)
+    flip = rng.random(prob.seqlen) < 0.05
+    for i in np.nonzero(flip)[0]:
+        if ns[i] > 0:
+            out[i] = rng.integers(0, ns[i])
+    # a state holds until the next change, so the new state stays valid within its block
+    starts = np.concatenate([[0], np.cumsum(prob.blocklens)[:-1]])
+    block = np.searchsorted(starts, np.arange(prob.seqlen), side="right") - 1
+    for i in range(1, prob.seqlen):
+        if not flip[i] and block[i] == block[i - 1]:
+            out[i] = out[i - 1]
+    return out
+
+
+@pytest.mark.parametrize("k,L,T,missing,internal,seed", [
+    (10, 4000, 20, 0.0, False, 1), (25, 3000, 16, 0.02, False, 2), (6, 6000, 32, 0.0, False, 3),
+    (15, 3000, 20, 0.01, True, 4), (30, 2000, 20, 0.0, True, 5)])
+def test_device_routine_matches_oracle(shim, k, L, T, missing, internal, seed):
+    # random problems, traceback paths with extra state changes: the routine the device
+    # runs equals the oracle's restatement on thousands of draws
+    import pyoracle
+    from argweaver_gb300.sim import leaf_cut, simulate
+    prob = simulate(k, L, seed, ntimes=T, missing=missing, rho=1.6e-7)
+    if internal:
+        prob = leaf_cut(prob)
+    fw, _ = pyoracle.forward(prob)
+    path = pyoracle.traceback(prob, fw, pyoracle.rand_uniforms(seed, prob.seqlen))
+    path = stress_path(prob, path, seed)
+    u = np.random.default_rng(seed).random(2 * prob.seqlen + 2)
+    o = pyoracle.sample_recombinations(prob, path, u)
+    n, pos, node, time, used = run_host(shim, prob, path, u)
+    assert n == len(o[0]) > 20
+    np.testing.assert_array_equal(pos, o[0])
+    np.testing.assert_array_equal(node, o[1])
+    np.testing.assert_array_equal(time, o[2])
+    assert used == o[3]

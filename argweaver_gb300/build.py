@@ -34,7 +34,8 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-
 
 CUDA_SOURCES = ["host_plan.cpp", "tables.cu", "forward.cu", "traceback.cu",
                 "backward.cu", "batch.cu", "static_run.cu", "dense_hmm.cu", "arg_prob.cu",
-                "recomb.cu", "capi.cpp", "server.cpp", "formats.cpp"]
+                "recomb.cu", "capi.cpp", "server.cpp", "formats.cpp",
+                "thread_add.cpp"]
 
 
 def _nvcc() -> str:

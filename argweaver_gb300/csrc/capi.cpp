@@ -16,10 +16,13 @@
 #include "engine.h"
 #include "kernels.h"
 #include "plan.h"
+#include "thread_add.h"
 
 struct awg_local_trees {
     int ntrees = 0, nnodes = 0, start_coord = 0;
-    std::vector<int> ptrees, ages, sprs, blocklens, mapping;
+    // mapping: from the previous tree (empty: the default); c0, c1: children in the order
+    // the trees keep them after surgery (empty: index order)
+    std::vector<int> ptrees, ages, sprs, blocklens, mapping, c0, c1;
 };
 
 namespace {
@@ -230,6 +233,124 @@ awg_local_trees *arghmm_new_trees(int **ptrees, int **ages, int **sprs, int *blo
 }
 
 void delete_local_trees(awg_local_trees *trees) { delete trees; }
+
+void get_local_trees_ptrees(awg_local_trees *trees, int **ptrees, int **ages, int **sprs,
+                            int *blocklens) {
+    if (!trees) return;
+    const int n = trees->nnodes;
+    for (int b = 0; b < trees->ntrees; b++) {
+        if (ptrees) memcpy(ptrees[b], &trees->ptrees[(size_t)b * n], sizeof(int) * n);
+        if (ages) memcpy(ages[b], &trees->ages[(size_t)b * n], sizeof(int) * n);
+        if (sprs) memcpy(sprs[b], &trees->sprs[(size_t)b * 4], sizeof(int) * 4);
+        if (blocklens) blocklens[b] = trees->blocklens[b];
+    }
+}
+
+int awg_local_trees_mapping(awg_local_trees *trees, int *mapping) {
+    g_err.clear();
+    if (!trees || !mapping) {
+        set_error("awg_local_trees_mapping: NULL argument");
+        return -1;
+    }
+    const int n = trees->nnodes;
+    for (int b = 0; b < trees->ntrees; b++) {
+        int *m = mapping + (size_t)b * n;
+        if (b == 0) {
+            for (int j = 0; j < n; j++) m[j] = -1;
+        } else if (!trees->mapping.empty()) {
+            memcpy(m, &trees->mapping[(size_t)b * n], sizeof(int) * n);
+        } else {  // make_node_mapping (local_tree.h:767-776)
+            for (int j = 0; j < n; j++) m[j] = j;
+            const int broken = trees->ptrees[(size_t)(b - 1) * n + trees->sprs[(size_t)b * 4]];
+            if (broken >= 0) m[broken] = -1;
+        }
+    }
+    return 0;
+}
+
+int awg_local_trees_set_structure(awg_local_trees *trees, const int *mapping,
+                                  const int *root_child0) {
+    g_err.clear();
+    if (!trees) {
+        set_error("awg_local_trees_set_structure: NULL trees");
+        return -1;
+    }
+    const int n = trees->nnodes, B = trees->ntrees;
+    if (mapping) {
+        for (size_t i = (size_t)n; i < (size_t)B * n; i++)
+            if (mapping[i] < -1 || mapping[i] >= n) {
+                set_error("awg_local_trees_set_structure: mapping out of range");
+                return -1;
+            }
+        trees->mapping.assign(mapping, mapping + (size_t)B * n);
+        for (int j = 0; j < n; j++) trees->mapping[j] = -1;
+    } else {
+        trees->mapping.clear();
+    }
+    trees->c0.clear();
+    trees->c1.clear();
+    if (root_child0) {  // children in index order, each root's child[0] named (set_ptree)
+        trees->c0.assign((size_t)B * n, -1);
+        trees->c1.assign((size_t)B * n, -1);
+        for (int b = 0; b < B; b++) {
+            int *c0 = &trees->c0[(size_t)b * n], *c1 = &trees->c1[(size_t)b * n];
+            const int *par = &trees->ptrees[(size_t)b * n];
+            int root = -1;
+            for (int i = 0; i < n; i++) {
+                const int p = par[i];
+                if (p == -1) root = i;
+                else if (p < 0 || p >= n || c1[p] != -1) {
+                    set_error("awg_local_trees_set_structure: malformed tree");
+                    trees->c0.clear();
+                    trees->c1.clear();
+                    return -1;
+                } else if (c0[p] == -1) c0[p] = i;
+                else c1[p] = i;
+            }
+            const int want = root_child0[b];
+            if (root >= 0 && want != -1 && c0[root] != want) {
+                if (c1[root] != want) {
+                    set_error("awg_local_trees_set_structure: root_child0 is no child of the root");
+                    trees->c0.clear();
+                    trees->c1.clear();
+                    return -1;
+                }
+                std::swap(c0[root], c1[root]);
+            }
+        }
+    }
+    return 0;
+}
+
+int awg_add_arg_thread(awg_local_trees *trees, int ntimes, const int *path, int seqlen,
+                       const int *rec_pos, const int *rec_node, const int *rec_time, int nrec) {
+    g_err.clear();
+    if (!trees || !path || nrec < 0 || (nrec > 0 && (!rec_pos || !rec_node || !rec_time)) ||
+        ntimes < 3 || ntimes > awg::MAXT) {
+        set_error("awg_add_arg_thread: bad arguments");
+        return -1;
+    }
+    if ((trees->nnodes + 2 + 1) / 2 > awg::MAXNODES / 2 || trees->nnodes + 2 > awg::MAXNODES) {
+        set_error("awg_add_arg_thread: the grown trees exceed the node limit");
+        return -1;
+    }
+    awg::ThreadTrees a;
+    a.ntrees = trees->ntrees; a.nnodes = trees->nnodes; a.start_coord = trees->start_coord;
+    a.ptrees = trees->ptrees; a.ages = trees->ages; a.sprs = trees->sprs;
+    a.blocklens = trees->blocklens; a.mapping = trees->mapping; a.c0 = trees->c0;
+    a.c1 = trees->c1;
+    std::string err;
+    if (!awg::add_arg_thread(a, ntimes, path, seqlen, rec_pos, rec_node, rec_time, nrec, err)) {
+        set_error(err);
+        return -1;
+    }
+    trees->ntrees = a.ntrees; trees->nnodes = a.nnodes;
+    trees->ptrees = std::move(a.ptrees); trees->ages = std::move(a.ages);
+    trees->sprs = std::move(a.sprs); trees->blocklens = std::move(a.blocklens);
+    trees->mapping = std::move(a.mapping); trees->c0 = std::move(a.c0);
+    trees->c1 = std::move(a.c1);
+    return 0;
+}
 int get_local_trees_ntrees(awg_local_trees *trees) { return trees ? trees->ntrees : 0; }
 int get_local_trees_nnodes(awg_local_trees *trees) { return trees ? trees->nnodes : 0; }
 

@@ -49,6 +49,28 @@ void delete_local_trees(awg_local_trees *trees);
 int get_local_trees_ntrees(awg_local_trees *trees);
 int get_local_trees_nnodes(awg_local_trees *trees);
 
+/* get_local_trees_ptrees (local_tree.cpp:1846-1890): parents, ages, SPRs and block lengths
+ * of every tree, into ntrees rows of the caller's arrays (leaf i is sequence i). */
+void get_local_trees_ptrees(awg_local_trees *trees, int **ptrees, int **ages, int **sprs,
+                            int *blocklens);
+
+/* The node mappings from each previous tree (ntrees x nnodes, row 0 all -1): after
+ * awg_add_arg_thread they are no longer the default. 0, or -1 (awg_last_error). */
+int awg_local_trees_mapping(awg_local_trees *trees, int *mapping);
+
+/* Node mappings (ntrees x nnodes, row 0 ignored; NULL: make_node_mapping) and each root's
+ * child[0] (NULL: children in index order) of trees whose structure the parent arrays do
+ * not carry (an ARG after surgery). 0, or -1 (awg_last_error). */
+int awg_local_trees_set_structure(awg_local_trees *trees, const int *mapping,
+                                  const int *root_child0);
+
+/* add_arg_thread (thread.cpp:272-422), on the host: the thread of a new last leaf (a state
+ * path over the trees' columns, external trees) and its recombinations (columns, nodes
+ * (-1: the new branch), times; e.g. from awg_sample_recombinations) added to the trees,
+ * which grow by two nodes and one tree per recombination. 0, or -1 (awg_last_error). */
+int awg_add_arg_thread(awg_local_trees *trees, int ntimes, const int *path, int seqlen,
+                       const int *rec_pos, const int *rec_node, const int *rec_time, int nrec);
+
 /* arghmm_get_nstates (states.cpp:209): states of every column. */
 void arghmm_get_nstates(awg_local_trees *trees, int ntimes, bool internal, int *nstates);
 

@@ -27,6 +27,11 @@
 //                                    sample_recombinations (recomb.cpp:151-235) along the
 //                                    int32 state path after srand(seed): count, positions,
 //                                    nodes, times, then the next rand() value
+//   addthread <problem> <path> <recombs> <out>
+//                                    add_arg_thread (thread.cpp:272-422): the new leaf's
+//                                    thread (int32 state path) and its recombinations (int32
+//                                    triples column, node, time) added to the problem's
+//                                    trees; writes the grown ARG as a problem
 //   ingest  <sites> <smc> <c> <out>  reads a sites file + SMC ARG the way arg-sample does
 //                                    (read_sites, find_compress_cols, compress_sites,
 //                                    make_sequences_from_sites, read_local_trees, set_seqids,
@@ -575,6 +580,36 @@ static int cmd_recomb(const char *in, const char *path_file, int seed, const cha
     return 0;
 }
 
+static int cmd_addthread(const char *in, const char *path_file, const char *rec_file,
+                         const char *out) {
+    Problem p = read_problem(in);
+    if (p.internal) die("addthread: external problems only");
+    LocalTrees *trees = make_trees(p);
+    vector<int> path(p.seqlen);
+    FILE *pf = fopen(path_file, "rb");
+    if (!pf) die("cannot read path");
+    rd(pf, path.data(), p.seqlen);
+    fclose(pf);
+    FILE *rf = fopen(rec_file, "rb");
+    if (!rf) die("cannot read recombinations");
+    vector<int> pos;
+    vector<NodePoint> recombs;
+    int v[3];
+    while (fread(v, sizeof(int), 3, rf) == 3) {
+        pos.push_back(v[0] + trees->start_coord);
+        recombs.push_back(NodePoint(v[1], v[2]));
+    }
+    fclose(rf);
+    StatesModel states_model(p.ntimes, false, 0);
+    add_arg_thread(trees, states_model, p.ntimes, path.data() - trees->start_coord,
+                   p.nseqs - 1, pos, recombs);
+    Problem q = p;
+    trees_to_problem(trees, q);
+    write_problem(out, q);
+    delete trees;
+    return 0;
+}
+
 static int cmd_cut(const char *in, int seed, const char *out) {
     Problem p = read_problem(in);
     if (p.internal) die("cut: input must be a full (external-format) ARG");
@@ -602,6 +637,8 @@ int main(int argc, char **argv) {
     if (cmd == "densernd" && argc == 6)
         return cmd_densernd(atoi(argv[2]), atoi(argv[3]), atoi(argv[4]), argv[5]);
     if (cmd == "argprob" && argc == 4) return cmd_argprob(argv[2], argv[3]);
+    if (cmd == "addthread" && argc == 6)
+        return cmd_addthread(argv[2], argv[3], argv[4], argv[5]);
     if (cmd == "recomb" && argc == 6)
         return cmd_recomb(argv[2], argv[3], atoi(argv[4]), argv[5]);
     if (cmd == "ingest" && argc == 6)

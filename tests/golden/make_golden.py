@@ -8,6 +8,7 @@ Run where the reference checkout exists (default /root/reference, or $AWG_REFERE
     python tests/golden/make_golden.py argprob    # only the ARG-probability ones
     python tests/golden/make_golden.py formats    # only the sites / SMC ones
     python tests/golden/make_golden.py recomb     # only the recombination-sampling ones
+    python tests/golden/make_golden.py addthread  # only the thread-addition ones
 
 It builds the reference from its own sources (oracle/Makefile target ``ref``), writes
 each problem as an AWGPROB1 file and runs the reference's threading HMM on it through
@@ -278,6 +279,36 @@ def recomb(tmp):
         print(name, n)
 
 
+def addthread(tmp):
+    """add_arg_thread (thread.cpp:272-422): the recombination fixtures' threads and
+    recombinations added to their problems' trees by the reference; the grown ARG."""
+    out_dir = os.path.join(HERE, "addthread")
+    os.makedirs(out_dir, exist_ok=True)
+    rdir = os.path.join(HERE, "recomb")
+    for f in sorted(os.listdir(rdir)):
+        if not f.endswith(".npz"):
+            continue
+        name = f[:-4]
+        rec = np.load(os.path.join(rdir, f))
+        if name.startswith("extra_"):
+            if name != "extra_k8_T20":
+                continue
+            pp = os.path.join(rdir, name + ".prob")
+            path = rec["path"]
+        else:
+            pp = os.path.join(HERE, name + ".prob")
+            path = np.load(os.path.join(HERE, name + ".npz"))["path"]
+        if Problem.load(pp).internal:
+            continue
+        path_file = os.path.join(tmp, "path.bin")
+        np.ascontiguousarray(path, dtype=np.int32).tofile(path_file)
+        rec_file = os.path.join(tmp, "rec.bin")
+        np.ascontiguousarray(np.stack([rec["pos"], rec["node"], rec["time"]], axis=1),
+                             dtype=np.int32).tofile(rec_file)
+        run("addthread", pp, path_file, rec_file, os.path.join(out_dir, name + ".prob"))
+        print(name, len(rec["pos"]))
+
+
 def infsites(tmp):
     """The infinite-sites penalty (ArgModel::infsites_penalty, emit.cpp:847-862; arg-sample
     --infsites uses 1e-100): external, with missing calls, and an internal-branch cut."""
@@ -301,6 +332,10 @@ def main():
     if sys.argv[1:] == ["infsites"]:
         with tempfile.TemporaryDirectory() as tmp:
             infsites(tmp)
+        return
+    if sys.argv[1:] == ["addthread"]:
+        with tempfile.TemporaryDirectory() as tmp:
+            addthread(tmp)
         return
     if sys.argv[1:] == ["recomb"]:
         with tempfile.TemporaryDirectory() as tmp:
@@ -357,6 +392,7 @@ def main():
         argprob(tmp)
         formats(tmp)
         recomb(tmp)
+        addthread(tmp)
 
 
 if __name__ == "__main__":

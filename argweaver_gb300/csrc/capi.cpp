@@ -454,6 +454,53 @@ void arghmm_sample_arg_thread_internal(awg_local_trees *trees, double *times, in
     if (awg::run_batch(&v.p, &o, 1, opt, err) != 0) set_error(err);
 }
 
+// arghmm_sample_thread (sample_thread.cpp:1010-1023, sample_arg_thread :575-625): the last
+// sequence threaded into the trees in place: forward and traceback on the device (draws
+// from rand(), last column first), recombinations along the thread on the device (draws
+// continuing rand(): 2 * seqlen + 2 are taken up front, of which the sampler uses the
+// reference's number), then the thread added on the host.
+awg_local_trees *arghmm_sample_thread(awg_local_trees *trees, double *times, int ntimes,
+                                      double *popsizes, double rho, double mu, char **seqs,
+                                      int nseqs, int seqlen) {
+    g_err.clear();
+    if (!trees) {
+        set_error("arghmm_sample_thread: NULL trees");
+        return trees;
+    }
+    if (nseqs != (trees->nnodes + 1) / 2 + 1) {
+        set_error("arghmm_sample_thread: the new sequence must follow the trees' leaves "
+                  "(nseqs = leaves + 1)");
+        return trees;
+    }
+    ProblemView v;
+    if (!make_view(trees, times, ntimes, popsizes, rho, mu, seqs, nseqs, seqlen, false, v))
+        return trees;
+    std::vector<int> path(seqlen);
+    awg_outputs o;
+    memset(&o, 0, sizeof(o));
+    o.path = path.data();
+    awg::RunOptions opt;
+    std::string err;
+    if (awg::run_batch(&v.p, &o, 1, opt, err) != 0) {
+        set_error(err);
+        return trees;
+    }
+    const int nu = 2 * seqlen + 2;
+    std::vector<double> u(nu);
+    for (double &x : u) x = rand() / double(RAND_MAX);  // frand (common.h:103-110)
+    std::vector<int> pos(seqlen), node(seqlen), time(seqlen);
+    int used = 0;
+    const int nrec = awg::sample_recombinations(&v.p, path.data(), u.data(), nu, pos.data(),
+                                                node.data(), time.data(), seqlen, &used, err);
+    if (nrec < 0) {
+        set_error(err);
+        return trees;
+    }
+    awg_add_arg_thread(trees, ntimes, path.data(), seqlen, pos.data(), node.data(),
+                       time.data(), nrec);
+    return trees;
+}
+
 void delete_path(int *path) { delete[] path; }
 
 // Debug export: the FP64 tables the table kernel builds for one problem (layouts in

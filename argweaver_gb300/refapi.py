@@ -291,3 +291,60 @@ def sample_recombinations(prob: Problem, path: np.ndarray, seed: int):
     u = np.array([_libc.rand() / 2147483647.0 for _ in range(n)], dtype=np.float64)
     return api.sample_recombinations(prob, path, u)
 
+
+
+# ----------------------------------------------------------------------------- threading step
+# arghmm_sample_thread (argweaverc.py:157-161, sample_thread.cpp:1010-1023): the last sequence
+# threaded into the ARG (forward, traceback and recombinations on the GPU, the surgery on
+# the host).
+
+def _trees_handle(p: Problem) -> "LocalTrees":
+    lib = capi.load()
+    trees = LocalTrees(p)
+    if p.mapping is not None or p.root_child0 is not None:
+        mp = None if p.mapping is None else np.ascontiguousarray(p.mapping, dtype=np.int32)
+        rc0 = None if p.root_child0 is None else np.ascontiguousarray(p.root_child0, dtype=np.int32)
+        rc = lib.awg_local_trees_set_structure(
+            trees.handle, None if mp is None else mp.ctypes.data_as(capi.c_int_p),
+            None if rc0 is None else rc0.ctypes.data_as(capi.c_int_p))
+        if rc != 0:
+            trees.close()
+            raise ValueError(capi.last_error())
+    return trees
+
+
+def _read_trees(trees: "LocalTrees"):
+    lib = capi.load()
+    nt = lib.get_local_trees_ntrees(trees.handle)
+    nn = lib.get_local_trees_nnodes(trees.handle)
+    pt, ag, sp = (np.zeros((nt, k), dtype=np.int32) for k in (nn, nn, 4))
+    bl = np.zeros(nt, dtype=np.int32)
+    rows = lambda a: (capi.c_int_p * nt)(*[a[i].ctypes.data_as(capi.c_int_p) for i in range(nt)])
+    lib.get_local_trees_ptrees(trees.handle, rows(pt), rows(ag), rows(sp),
+                               bl.ctypes.data_as(capi.c_int_p))
+    mp = np.zeros((nt, nn), dtype=np.int32)
+    lib.awg_local_trees_mapping(trees.handle, mp.ctypes.data_as(capi.c_int_p))
+    return pt, ag, sp, bl, mp
+
+
+def arghmm_sample_thread(prob: Problem) -> Problem:
+    """The problem's ARG with its last sequence threaded in (draws from libc rand(): seed it
+    with srand). The result is a full ARG over all the problem's sequences."""
+    lib = capi.load()
+    p = prob.normalized()
+    if p.internal:
+        raise ValueError("arghmm_sample_thread: external (threading) problems only")
+    trees = _trees_handle(p)
+    try:
+        seqs, _keep = _char_pp(p.seqs)
+        lib.arghmm_sample_thread(trees.handle, p.times.ctypes.data_as(capi.c_double_p),
+                                 p.ntimes, p.popsizes.ctypes.data_as(capi.c_double_p), p.rho,
+                                 p.mu, seqs, p.nseqs, p.seqlen)
+        err = capi.last_error()
+        if err:
+            raise RuntimeError(err)
+        pt, ag, sp, bl, mp = _read_trees(trees)
+    finally:
+        trees.close()
+    return Problem(times=p.times, popsizes=p.popsizes, rho=p.rho, mu=p.mu, ptrees=pt, ages=ag,
+                   sprs=sp, blocklens=bl, seqs=p.seqs, start_coord=p.start_coord, mapping=mp)

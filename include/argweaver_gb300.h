@@ -111,6 +111,16 @@ void arghmm_sample_arg_thread_internal(awg_local_trees *trees, double *times, in
                                        double *popsizes, double rho, double mu, char **seqs,
                                        int nseqs, int seqlen, int *thread_path);
 
+/* arghmm_sample_thread (sample_thread.cpp:1010-1023): threads the last sequence (nseqs =
+ * the trees' leaves + 1) into the trees, in place: forward and traceback on the device
+ * (rand() draws as arghmm_sample_posterior), recombinations along the thread on the device
+ * (draws continuing rand(); 2 * seqlen + 2 are taken, the reference's number used) and the
+ * thread added on the host (add_arg_thread). Returns trees; on failure they are unchanged
+ * and awg_last_error() says why. */
+awg_local_trees *arghmm_sample_thread(awg_local_trees *trees, double *times, int ntimes,
+                                      double *popsizes, double rho, double mu, char **seqs,
+                                      int nseqs, int seqlen);
+
 /* delete_path / delete_double_matrix / delete_forward_matrix (sample_thread.cpp:1026-1042) */
 void delete_path(int *path);
 void delete_double_matrix(double **mat, int nrows);

@@ -32,6 +32,10 @@
 //                                    thread (int32 state path) and its recombinations (int32
 //                                    triples column, node, time) added to the problem's
 //                                    trees; writes the grown ARG as a problem
+//   samplethread <problem> <seed> <out>
+//                                    arghmm_sample_thread (sample_thread.cpp:1010-1023)
+//                                    after srand(seed): the last sequence threaded into the
+//                                    trees; writes the grown ARG as a problem
 //   ingest  <sites> <smc> <c> <out>  reads a sites file + SMC ARG the way arg-sample does
 //                                    (read_sites, find_compress_cols, compress_sites,
 //                                    make_sequences_from_sites, read_local_trees, set_seqids,
@@ -84,6 +88,9 @@ void get_local_trees_ptrees(LocalTrees *trees, int **ptrees, int **ages, int **s
                             int *blocklens);          // local_tree.cpp:1846
 void arghmm_get_nstates(LocalTrees *trees, int ntimes, bool internal,
                         int *nstates);                // states.cpp:209
+LocalTrees *arghmm_sample_thread(LocalTrees *trees, double *times, int ntimes,
+                                 double *popsizes, double rho, double mu, char **seqs,
+                                 int nseqs, int seqlen);       // sample_thread.cpp:1010
 double arghmm_likelihood(LocalTrees *trees, double *times, int ntimes, double mu,
                          char **seqs, int nseqs, int seqlen);          // total_prob.cpp:317
 double arghmm_prior_prob(LocalTrees *trees, double *times, int ntimes, double *popsizes,
@@ -610,6 +617,21 @@ static int cmd_addthread(const char *in, const char *path_file, const char *rec_
     return 0;
 }
 
+static int cmd_samplethread(const char *in, int seed, const char *out) {
+    Problem p = read_problem(in);
+    if (p.internal) die("samplethread: external problems only");
+    LocalTrees *trees = make_trees(p);
+    vector<char *> sp = seq_ptrs(p);
+    srand(seed);
+    arghmm_sample_thread(trees, p.times.data(), p.ntimes, p.popsizes.data(), p.rho, p.mu,
+                         sp.data(), p.nseqs, p.seqlen);
+    Problem q = p;
+    trees_to_problem(trees, q);
+    write_problem(out, q);
+    delete trees;
+    return 0;
+}
+
 static int cmd_cut(const char *in, int seed, const char *out) {
     Problem p = read_problem(in);
     if (p.internal) die("cut: input must be a full (external-format) ARG");
@@ -637,6 +659,8 @@ int main(int argc, char **argv) {
     if (cmd == "densernd" && argc == 6)
         return cmd_densernd(atoi(argv[2]), atoi(argv[3]), atoi(argv[4]), argv[5]);
     if (cmd == "argprob" && argc == 4) return cmd_argprob(argv[2], argv[3]);
+    if (cmd == "samplethread" && argc == 5)
+        return cmd_samplethread(argv[2], atoi(argv[3]), argv[4]);
     if (cmd == "addthread" && argc == 6)
         return cmd_addthread(argv[2], argv[3], argv[4], argv[5]);
     if (cmd == "recomb" && argc == 6)

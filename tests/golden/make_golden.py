@@ -9,6 +9,7 @@ Run where the reference checkout exists (default /root/reference, or $AWG_REFERE
     python tests/golden/make_golden.py formats    # only the sites / SMC ones
     python tests/golden/make_golden.py recomb     # only the recombination-sampling ones
     python tests/golden/make_golden.py addthread  # only the thread-addition ones
+    python tests/golden/make_golden.py samplethread  # only the full threading step
 
 It builds the reference from its own sources (oracle/Makefile target ``ref``), writes
 each problem as an AWGPROB1 file and runs the reference's threading HMM on it through
@@ -309,6 +310,20 @@ def addthread(tmp):
         print(name, len(rec["pos"]))
 
 
+def samplethread(tmp):
+    """arghmm_sample_thread (sample_thread.cpp:1010-1023) after srand(seed + 9000) on the
+    external fixtures: the ARG with the last sequence threaded in, as the reference grows it."""
+    out_dir = os.path.join(HERE, "samplethread")
+    os.makedirs(out_dir, exist_ok=True)
+    for name in ("dsmc_k8_s11", "dsmc_k8_s12", "dsmc_k10_T16", "dsmc_k17_missing", "sim1_c20",
+                 "single_k7_s41"):
+        pp = os.path.join(HERE, name + ".prob")
+        seed = int(np.load(os.path.join(HERE, name + ".npz"))["seed"]) + 9000
+        run("samplethread", pp, seed, os.path.join(out_dir, name + ".prob"))
+        np.savez(os.path.join(out_dir, name + ".npz"), seed=seed)
+        print(name, Problem.load(os.path.join(out_dir, name + ".prob")).ntrees)
+
+
 def infsites(tmp):
     """The infinite-sites penalty (ArgModel::infsites_penalty, emit.cpp:847-862; arg-sample
     --infsites uses 1e-100): external, with missing calls, and an internal-branch cut."""
@@ -332,6 +347,10 @@ def main():
     if sys.argv[1:] == ["infsites"]:
         with tempfile.TemporaryDirectory() as tmp:
             infsites(tmp)
+        return
+    if sys.argv[1:] == ["samplethread"]:
+        with tempfile.TemporaryDirectory() as tmp:
+            samplethread(tmp)
         return
     if sys.argv[1:] == ["addthread"]:
         with tempfile.TemporaryDirectory() as tmp:
@@ -393,6 +412,7 @@ def main():
         formats(tmp)
         recomb(tmp)
         addthread(tmp)
+        samplethread(tmp)
 
 
 if __name__ == "__main__":

@@ -77,3 +77,31 @@ def test_add_thread_rejects_bad_input():
         grown(prob, bad, rec["pos"], rec["node"], rec["time"])
     with pytest.raises(ValueError, match="increase"):
         grown(prob, path, rec["pos"][::-1], rec["node"][::-1], rec["time"][::-1])
+
+
+ST_NAMES = sorted(os.path.basename(p)[:-5] for p in glob.glob(os.path.join(GOLDEN, "samplethread", "*.prob")))
+
+
+@pytest.mark.parametrize("name", ST_NAMES)
+def test_threading_step_on_the_host_matches_reference(name):
+    # arghmm_sample_thread's steps with the device ones replaced by the oracle (pinned to
+    # the reference): the traceback's rand() draws, then the recombination sampler's draws
+    # continuing rand(), then the thread added by this library; the grown ARG must be the
+    # reference's, so the composite export's draw order and glue are those of the reference
+    import pyoracle
+    prob, _ = load_golden(name)
+    ref = Problem.load(os.path.join(GOLDEN, "samplethread", name + ".prob"))
+    seed = int(np.load(os.path.join(GOLDEN, "samplethread", name + ".npz"))["seed"])
+    L = prob.seqlen
+    libc = C.CDLL(None)
+    libc.srand(C.c_uint(seed))
+    d = np.array([libc.rand() / 2147483647.0 for _ in range(L + 2 * L + 2)])
+    fw, _ = pyoracle.forward(prob)
+    path = pyoracle.traceback(prob, fw, d[:L][::-1].copy())
+    pos, node, time, used = pyoracle.sample_recombinations(prob, path, d[L:])
+    pt, ag, sp, bl, mp = grown(prob, path, pos, node, time)
+    np.testing.assert_array_equal(pt, ref.ptrees)
+    np.testing.assert_array_equal(ag, ref.ages)
+    np.testing.assert_array_equal(sp[1:], ref.sprs[1:])
+    np.testing.assert_array_equal(bl, ref.blocklens)
+    np.testing.assert_array_equal(mp[1:], ref.mapping[1:])

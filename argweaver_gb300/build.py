@@ -35,7 +35,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-
 CUDA_SOURCES = ["host_plan.cpp", "tables.cu", "forward.cu", "traceback.cu",
                 "backward.cu", "batch.cu", "static_run.cu", "dense_hmm.cu", "arg_prob.cu",
                 "recomb.cu", "capi.cpp", "server.cpp", "formats.cpp",
-                "thread_add.cpp"]
+                "arg_surgery.cpp"]
 
 
 def _nvcc() -> str:

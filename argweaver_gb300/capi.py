@@ -81,12 +81,15 @@ PROTOTYPES = [
                                             C.c_int, c_int_p, c_int_p, c_int_p, C.c_int,
                                             c_int_p]),
     ("get_local_trees_ptrees", None, [C.c_void_p, c_int_pp, c_int_pp, c_int_pp, c_int_p]),
+    ("awg_local_trees_seqids", C.c_int, [C.c_void_p, c_int_p]),
     ("awg_local_trees_mapping", C.c_int, [C.c_void_p, c_int_p]),
+    ("awg_local_trees_children", C.c_int, [C.c_void_p, c_int_p, c_int_p]),
     ("awg_local_trees_set_structure", C.c_int, [C.c_void_p, c_int_p, c_int_p]),
     ("arghmm_sample_thread", C.c_void_p, [C.c_void_p, c_double_p, C.c_int, c_double_p,
                                           C.c_double, C.c_double, c_char_pp, C.c_int, C.c_int]),
     ("awg_add_arg_thread", C.c_int, [C.c_void_p, C.c_int, c_int_p, C.c_int, c_int_p, c_int_p,
                                      c_int_p, C.c_int]),
+    ("awg_remove_arg_thread", C.c_int, [C.c_void_p, C.c_int]),
     ("awg_read_arg_input", C.c_void_p, [C.c_char_p, C.c_char_p, C.c_int, c_double_p, C.c_int]),
     ("awg_arg_input_dims", C.c_int, [C.c_void_p, c_int_p, c_int_p, c_int_p, c_int_p, c_int_p]),
     ("awg_arg_input_name", C.c_char_p, [C.c_void_p, C.c_int]),

@@ -1,9 +1,11 @@
-// Adding a sampled thread to the ARG (add_arg_thread, thread.cpp:272-422), on the host:
+// ARG surgery on the host. Adding a sampled thread (add_arg_thread, thread.cpp:272-422):
 // the new leaf joins every local tree at the state its thread takes at the tree's first
 // column, each sampled recombination splits its tree in two by an SPR, and the node
 // mappings and SPRs between neighbouring trees are renamed for the two new nodes
-// (add_spr_branch, thread.cpp:176-269). Pointer surgery on a few hundred nodes per tree:
-// host work between the device's threading passes.
+// (add_spr_branch, thread.cpp:176-269). Removing a leaf's thread (remove_arg_thread,
+// thread.cpp:425-556): the inverse, with trees whose SPR disappears merged into their
+// neighbour. Pointer surgery on a few hundred nodes per tree: host work between the
+// device's threading passes.
 //
 // Node names follow the reference: the new leaf takes the name nleaves, the node that had
 // it moves to nnodes (displaced), the new coalescence node is nnodes + 1. Child order is
@@ -14,7 +16,7 @@
 #include <string>
 #include <vector>
 
-#include "thread_add.h"
+#include "arg_surgery.h"
 
 namespace awg {
 
@@ -27,6 +29,10 @@ struct Node {
 struct Tree {
     std::vector<Node> nd;
     int root = -1;
+};
+
+struct Spr4 {
+    int v[4];
 };
 
 // rename_node (thread.cpp:9-36): node src moves to dest, its neighbours follow
@@ -315,6 +321,228 @@ bool add_arg_thread(ThreadTrees &a, int T, const int *path, int seqlen, const in
         err = "add_arg_thread: a recombination outside the trees";
         return false;
     }
+    a = std::move(out);
+    return true;
+}
+
+namespace {
+
+// remove_tree_branch (thread.cpp:102-163): the leaf and its coalescence node leave the
+// tree; the last leaf and the nodes nnodes-2, nnodes-1 move into the holes (displace[]:
+// every old name's new one, -1 for the two removed)
+void remove_tree_branch(Tree &t, int nnodes, int remove_leaf, std::vector<int> &displace) {
+    const int last_leaf = (nnodes + 1) / 2 - 1;
+    const int remove_coal = t.nd[remove_leaf].parent;
+    const int coal_child =
+        t.nd[remove_coal].c0 == remove_leaf ? t.nd[remove_coal].c1 : t.nd[remove_coal].c0;
+    const int coal_parent = t.nd[remove_coal].parent;
+    t.nd[coal_child].parent = coal_parent;
+    if (coal_parent != -1) {
+        if (t.nd[coal_parent].c0 == remove_coal) t.nd[coal_parent].c0 = coal_child;
+        else t.nd[coal_parent].c1 = coal_child;
+    }
+    displace.assign(nnodes, 0);
+    for (int i = 0; i < nnodes; i++) displace[i] = i;
+    displace[remove_leaf] = -1;
+    displace[remove_coal] = -1;
+    if (last_leaf != remove_leaf) {
+        displace[last_leaf] = remove_leaf;
+        rename_node(t, last_leaf, remove_leaf);
+    }
+    int hole = last_leaf;
+    if (remove_coal != nnodes - 2) {
+        displace[nnodes - 2] = hole;
+        rename_node(t, nnodes - 2, hole);
+        hole = remove_coal;
+    }
+    if (remove_coal != nnodes - 1) {
+        displace[nnodes - 1] = hole;
+        rename_node(t, nnodes - 1, hole);
+    }
+    int root = t.root;
+    if (root == remove_coal) root = coal_child;
+    if (root == nnodes - 2) root = last_leaf;
+    if (root == nnodes - 1) root = hole;
+    t.root = root;
+    t.nd.resize(nnodes - 2);
+}
+
+}  // namespace
+
+bool remove_arg_thread(ThreadTrees &a, int seqid, std::string &err) {
+    const int nnodes = a.nnodes, B = a.ntrees;
+    const int nleaves = (nnodes + 1) / 2, last_leaf = nleaves - 1;
+    std::vector<int> seqids = a.seqids;
+    if (seqids.empty())
+        for (int i = 0; i < nleaves; i++) seqids.push_back(i);
+    if ((int)seqids.size() != nleaves || nnodes != 2 * nleaves - 1) {
+        err = "remove_arg_thread: the sequence ids do not match the leaves";
+        return false;
+    }
+    int remove_leaf = -1;
+    for (int i = 0; i < (int)seqids.size(); i++)
+        if (seqids[i] == seqid) {
+            remove_leaf = i;
+            break;
+        }
+    if (remove_leaf < 0) {
+        err = "remove_arg_thread: no leaf holds that sequence";
+        return false;
+    }
+    long long total = 0;
+    for (int b = 0; b < B; b++) total += a.blocklens[b];
+    if (nnodes == 3) {  // the trunk genealogy is left (make_trunk, local_tree.h:576-590)
+        const int other = seqids[1 - remove_leaf];
+        ThreadTrees out;
+        out.ntrees = 1;
+        out.nnodes = 1;
+        out.start_coord = a.start_coord;
+        out.ptrees = {-1};
+        out.ages = {0};
+        out.sprs = {-1, -1, -1, -1};
+        out.blocklens = {(int)total};
+        out.c0 = {-1};
+        out.c1 = {-1};
+        out.seqids = {other};
+        a = std::move(out);
+        return true;
+    }
+    if (nnodes < 3) {
+        err = "remove_arg_thread: no thread to remove";
+        return false;
+    }
+    // the trees with their children (stored order, else index order) and mappings
+    std::vector<Tree> trees(B);
+    std::vector<std::vector<int>> maps(B);
+    std::vector<Spr4> sprs(B);
+    for (int b = 0; b < B; b++) {
+        Tree &t = trees[b];
+        t.nd.resize(nnodes);
+        for (int i = 0; i < nnodes; i++) {
+            t.nd[i].parent = a.ptrees[(size_t)b * nnodes + i];
+            t.nd[i].age = a.ages[(size_t)b * nnodes + i];
+            if (t.nd[i].parent == -1) t.root = i;
+        }
+        if (!a.c0.empty()) {
+            for (int i = 0; i < nnodes; i++) {
+                t.nd[i].c0 = a.c0[(size_t)b * nnodes + i];
+                t.nd[i].c1 = a.c1[(size_t)b * nnodes + i];
+            }
+        } else {
+            for (int i = 0; i < nnodes; i++) {
+                const int p = t.nd[i].parent;
+                if (p == -1) continue;
+                if (t.nd[p].c0 == -1) t.nd[p].c0 = i;
+                else t.nd[p].c1 = i;
+            }
+        }
+        for (int k = 0; k < 4; k++) sprs[b].v[k] = b > 0 ? a.sprs[(size_t)b * 4 + k] : -1;
+        if (b > 0) {
+            if (!a.mapping.empty()) {
+                maps[b].assign(a.mapping.begin() + (size_t)b * nnodes,
+                               a.mapping.begin() + (size_t)(b + 1) * nnodes);
+            } else {  // make_node_mapping (local_tree.h:767-776)
+                maps[b].resize(nnodes);
+                for (int i = 0; i < nnodes; i++) maps[b][i] = i;
+                const int r = sprs[b].v[0];
+                if (r < 0 || r >= nnodes) {
+                    err = "remove_arg_thread: an SPR node out of range";
+                    return false;
+                }
+                maps[b][trees[b - 1].nd[r].parent] = -1;
+            }
+        }
+    }
+    std::vector<int> displace;
+    for (int b = 0; b < B; b++) {
+        Tree &t = trees[b];
+        const int remove_coal = t.nd[remove_leaf].parent;
+        if (remove_coal < 0) {
+            err = "remove_arg_thread: the leaf has no parent";
+            return false;
+        }
+        const int coal_time = t.nd[remove_coal].age;
+        int coal_child =
+            t.nd[remove_coal].c0 == remove_leaf ? t.nd[remove_coal].c1 : t.nd[remove_coal].c0;
+        remove_tree_branch(t, nnodes, remove_leaf, displace);
+        if (b > 0) {  // this mapping's targets renamed
+            std::vector<int> &m = maps[b];
+            for (int i = 0; i < nnodes - 2; i++) m[i] = m[i] != -1 ? displace[m[i]] : -1;
+        }
+        if (b + 1 == B) continue;
+        // the next mapping's sources renamed (the moved nodes keep their targets)
+        std::vector<int> &m = maps[b + 1];
+        if (displace[last_leaf] != -1) m[displace[last_leaf]] = m[last_leaf];
+        if (displace[nnodes - 2] != -1) m[displace[nnodes - 2]] = m[nnodes - 2];
+        if (displace[nnodes - 1] != -1) m[displace[nnodes - 1]] = m[nnodes - 1];
+        int *spr = sprs[b + 1].v;
+        coal_child = displace[coal_child];
+        auto set_null = [&]() { spr[0] = spr[1] = spr[2] = spr[3] = -1; };
+        if (spr[0] < 0 || spr[0] >= nnodes || spr[2] < 0 || spr[2] >= nnodes) {
+            err = "remove_arg_thread: an SPR node out of range";
+            return false;
+        }
+        if (spr[0] == remove_leaf) { set_null(); continue; }  // recombination on the branch
+        spr[0] = spr[0] == remove_coal ? coal_child : displace[spr[0]];
+        if (spr[0] == coal_child && t.nd[coal_child].parent == -1) { set_null(); continue; }
+        if (spr[2] == remove_leaf) {  // mediated coalescence
+            spr[2] = coal_child;
+            spr[3] = coal_time;
+        } else if (spr[2] == remove_coal) {
+            spr[2] = coal_child;
+        } else {
+            spr[2] = displace[spr[2]];
+        }
+        if (spr[0] == spr[2]) { set_null(); continue; }  // a bubble
+    }
+    const int n2 = nnodes - 2;
+    seqids[remove_leaf] = seqids[last_leaf];
+    seqids.resize(nleaves - 1);
+    // remove_null_sprs (local_tree.cpp:409-469): a tree whose successor has no SPR is
+    // absorbed by it (block lengths add, the mappings compose, its SPR moves over)
+    ThreadTrees out;
+    out.nnodes = n2;
+    out.start_coord = a.start_coord;
+    out.seqids = seqids;
+    struct Pending {
+        int b, blocklen;
+        Spr4 spr;
+        std::vector<int> map;
+        bool has_map;
+    };
+    auto emit = [&](const Pending &p) {
+        const Tree &t = trees[p.b];
+        for (int i = 0; i < n2; i++) {
+            out.ptrees.push_back(t.nd[i].parent);
+            out.ages.push_back(t.nd[i].age);
+            out.c0.push_back(t.nd[i].c0);
+            out.c1.push_back(t.nd[i].c1);
+            out.mapping.push_back(p.has_map ? p.map[i] : -1);
+        }
+        for (int k = 0; k < 4; k++) out.sprs.push_back(p.spr.v[k]);
+        out.blocklens.push_back(p.blocklen);
+        out.ntrees++;
+    };
+    Pending cur{0, a.blocklens[0], sprs[0], {}, false};
+    for (int b = 1; b < B; b++) {
+        Pending nx{b, a.blocklens[b], sprs[b], maps[b], true};
+        nx.map.resize(n2);
+        if (nx.spr.v[0] == -1) {  // no SPR into tree b: tree cur merges into it
+            if (!cur.has_map) {
+                nx.has_map = false;
+            } else {
+                std::vector<int> comp(n2);
+                for (int i = 0; i < n2; i++) comp[i] = cur.map[i] != -1 ? nx.map[cur.map[i]] : -1;
+                nx.map = comp;
+                nx.spr = cur.spr;
+            }
+            nx.blocklen += cur.blocklen;
+        } else {
+            emit(cur);
+        }
+        cur = nx;
+    }
+    emit(cur);
     a = std::move(out);
     return true;
 }

@@ -1,5 +1,5 @@
 // Host-side ARG surgery: adding a sampled thread to local trees (add_arg_thread,
-// thread.cpp:272-422).
+// thread.cpp:272-422) and removing a leaf's thread (remove_arg_thread, thread.cpp:425-556).
 #pragma once
 
 #include <string>
@@ -14,6 +14,7 @@ namespace awg {
 struct ThreadTrees {
     int ntrees = 0, nnodes = 0, start_coord = 0;
     std::vector<int> ptrees, ages, sprs, blocklens, mapping, c0, c1;
+    std::vector<int> seqids;  // sequence of each leaf (empty: leaf i is sequence i)
 };
 
 // Adds the thread of a new leaf (state path over the trees' columns, external trees) and
@@ -21,5 +22,11 @@ struct ThreadTrees {
 // two nodes and one tree per recombination. False with err set on inconsistent input.
 bool add_arg_thread(ThreadTrees &a, int T, const int *path, int seqlen, const int *rec_pos,
                     const int *rec_node, const int *rec_time, int nrec, std::string &err);
+
+// Removes the thread of the leaf holding sequence `seqid` (remove_arg_thread,
+// thread.cpp:425-556): every tree loses that leaf and its coalescence node, the last leaf
+// and the two last nodes move into the holes, SPRs on the removed branch vanish and trees
+// left without an SPR merge with their neighbour (remove_null_sprs, local_tree.cpp:409-469).
+bool remove_arg_thread(ThreadTrees &a, int seqid, std::string &err);
 
 }  // namespace awg

@@ -16,13 +16,14 @@
 #include "engine.h"
 #include "kernels.h"
 #include "plan.h"
-#include "thread_add.h"
+#include "arg_surgery.h"
 
 struct awg_local_trees {
     int ntrees = 0, nnodes = 0, start_coord = 0;
     // mapping: from the previous tree (empty: the default); c0, c1: children in the order
-    // the trees keep them after surgery (empty: index order)
-    std::vector<int> ptrees, ages, sprs, blocklens, mapping, c0, c1;
+    // the trees keep them after surgery (empty: index order); seqids: the sequence each
+    // leaf holds (LocalTrees::seqids, local_tree.h:673; empty: leaf i holds sequence i)
+    std::vector<int> ptrees, ages, sprs, blocklens, mapping, c0, c1, seqids;
 };
 
 namespace {
@@ -40,12 +41,47 @@ struct ProblemView {
     std::vector<char> seqs;
 };
 
+// The leaf names the reference's exports show (get_local_trees_ptrees, local_tree.cpp:
+// 1847-1857): leaf i is named seqids[i], internal nodes keep theirs. False when the names
+// are the stored ones (default ids, or ids that are no permutation of the leaves, which the
+// reference cannot show either).
+bool leaf_perm(const awg_local_trees *t, std::vector<int> &perm) {
+    const int n = t->nnodes, nleaves = (n + 1) / 2;
+    if (t->seqids.empty() || (int)t->seqids.size() != nleaves) return false;
+    perm.assign(n, 0);
+    std::vector<char> seen(nleaves, 0);
+    bool identity = true;
+    for (int i = 0; i < nleaves; i++) {
+        const int s = t->seqids[i];
+        if (s < 0 || s >= nleaves || seen[s]) return false;
+        seen[s] = 1;
+        perm[i] = s;
+        identity = identity && s == i;
+    }
+    for (int i = nleaves; i < n; i++) perm[i] = i;
+    return !identity;
+}
+
 bool make_view(const awg_local_trees *t, double *times, int ntimes, double *popsizes,
                double rho, double mu, char **seqs, int nseqs, int seqlen, bool internal,
                ProblemView &v) {
     if (!t || !times || !popsizes || !seqs) { set_error("NULL argument"); return false; }
+    // leaf i reads sequence seqids[i] (matrices.cpp:34, total_prob.cpp:32); the rows after
+    // the leaves are the last sequences, in order (the thread's new_chrom = nseqs - 1)
+    const int nleaves = (t->nnodes + 1) / 2;
+    std::vector<int> rows(nseqs);
+    for (int i = 0; i < nseqs; i++) rows[i] = i;
+    if (!t->seqids.empty() && nseqs >= nleaves) {
+        for (int i = 0; i < nleaves; i++) {
+            if (t->seqids[i] < 0 || t->seqids[i] >= nseqs) {
+                set_error("a leaf's sequence id is past the sequences given");
+                return false;
+            }
+            rows[i] = t->seqids[i];
+        }
+    }
     v.seqs.resize((size_t)nseqs * seqlen);
-    for (int i = 0; i < nseqs; i++) memcpy(&v.seqs[(size_t)i * seqlen], seqs[i], seqlen);
+    for (int i = 0; i < nseqs; i++) memcpy(&v.seqs[(size_t)i * seqlen], seqs[rows[i]], seqlen);
     awg_problem &p = v.p;
     memset(&p, 0, sizeof(p));
     p.ntrees = t->ntrees; p.nnodes = t->nnodes; p.ntimes = ntimes; p.nseqs = nseqs;
@@ -238,12 +274,45 @@ void get_local_trees_ptrees(awg_local_trees *trees, int **ptrees, int **ages, in
                             int *blocklens) {
     if (!trees) return;
     const int n = trees->nnodes;
+    std::vector<int> perm;
+    if (leaf_perm(trees, perm)) {  // leaves named by their sequence (local_tree.cpp:1862-1890)
+        for (int b = 0; b < trees->ntrees; b++) {
+            const int *par = &trees->ptrees[(size_t)b * n], *age = &trees->ages[(size_t)b * n];
+            for (int j = 0; j < n; j++) {
+                if (ptrees) ptrees[b][perm[j]] = par[j] != -1 ? perm[par[j]] : -1;
+                if (ages) ages[b][perm[j]] = age[j];
+            }
+            if (sprs) {
+                const int *s = &trees->sprs[(size_t)b * 4];
+                const bool null = s[0] == -1;
+                sprs[b][0] = null ? s[0] : perm[s[0]];
+                sprs[b][1] = s[1];
+                sprs[b][2] = null ? s[2] : perm[s[2]];
+                sprs[b][3] = s[3];
+            }
+            if (blocklens) blocklens[b] = trees->blocklens[b];
+        }
+        return;
+    }
     for (int b = 0; b < trees->ntrees; b++) {
         if (ptrees) memcpy(ptrees[b], &trees->ptrees[(size_t)b * n], sizeof(int) * n);
         if (ages) memcpy(ages[b], &trees->ages[(size_t)b * n], sizeof(int) * n);
         if (sprs) memcpy(sprs[b], &trees->sprs[(size_t)b * 4], sizeof(int) * 4);
         if (blocklens) blocklens[b] = trees->blocklens[b];
     }
+}
+
+int awg_local_trees_seqids(awg_local_trees *trees, int *seqids) {
+    g_err.clear();
+    if (!trees) {
+        set_error("awg_local_trees_seqids: NULL trees");
+        return -1;
+    }
+    const int nleaves = (trees->nnodes + 1) / 2;
+    if (seqids)
+        for (int i = 0; i < nleaves; i++)
+            seqids[i] = trees->seqids.empty() ? i : trees->seqids[i];
+    return nleaves;
 }
 
 int awg_local_trees_mapping(awg_local_trees *trees, int *mapping) {
@@ -263,6 +332,48 @@ int awg_local_trees_mapping(awg_local_trees *trees, int *mapping) {
             for (int j = 0; j < n; j++) m[j] = j;
             const int broken = trees->ptrees[(size_t)(b - 1) * n + trees->sprs[(size_t)b * 4]];
             if (broken >= 0) m[broken] = -1;
+        }
+    }
+    std::vector<int> perm, tmp(n);
+    if (leaf_perm(trees, perm)) {  // in the names get_local_trees_ptrees shows
+        for (int b = 1; b < trees->ntrees; b++) {
+            int *m = mapping + (size_t)b * n;
+            for (int j = 0; j < n; j++) tmp[perm[j]] = m[j] != -1 ? perm[m[j]] : -1;
+            memcpy(m, tmp.data(), sizeof(int) * n);
+        }
+    }
+    return 0;
+}
+
+int awg_local_trees_children(awg_local_trees *trees, int *c0, int *c1) {
+    g_err.clear();
+    if (!trees || !c0 || !c1) {
+        set_error("awg_local_trees_children: NULL argument");
+        return -1;
+    }
+    const int n = trees->nnodes;
+    std::vector<int> perm;
+    const bool named = leaf_perm(trees, perm);
+    for (int b = 0; b < trees->ntrees; b++) {
+        int *d0 = c0 + (size_t)b * n, *d1 = c1 + (size_t)b * n;
+        std::vector<int> a0(n, -1), a1(n, -1);
+        if (!trees->c0.empty()) {
+            for (int j = 0; j < n; j++) {
+                a0[j] = trees->c0[(size_t)b * n + j];
+                a1[j] = trees->c1[(size_t)b * n + j];
+            }
+        } else {
+            for (int j = 0; j < n; j++) {
+                const int p = trees->ptrees[(size_t)b * n + j];
+                if (p < 0 || p >= n) continue;
+                if (a0[p] == -1) a0[p] = j;
+                else a1[p] = j;
+            }
+        }
+        for (int j = 0; j < n; j++) {
+            const int v = named ? perm[j] : j;
+            d0[v] = a0[j] != -1 && named ? perm[a0[j]] : a0[j];
+            d1[v] = a1[j] != -1 && named ? perm[a1[j]] : a1[j];
         }
     }
     return 0;
@@ -349,6 +460,40 @@ int awg_add_arg_thread(awg_local_trees *trees, int ntimes, const int *path, int 
     trees->sprs = std::move(a.sprs); trees->blocklens = std::move(a.blocklens);
     trees->mapping = std::move(a.mapping); trees->c0 = std::move(a.c0);
     trees->c1 = std::move(a.c1);
+    if (!trees->seqids.empty()) {  // the new leaf holds the smallest sequence id not in use
+        std::vector<char> used(trees->seqids.size() + 1, 0);
+        for (int s : trees->seqids)
+            if (s >= 0 && s < (int)used.size()) used[s] = 1;
+        int id = 0;
+        while (used[id]) id++;
+        trees->seqids.push_back(id);
+    }
+    return 0;
+}
+
+// remove_arg_thread (thread.cpp:425-556) on the host: the leaf holding sequence `seqid`
+// leaves every tree; the last leaf takes its name (its sequence id moves with it).
+int awg_remove_arg_thread(awg_local_trees *trees, int seqid) {
+    g_err.clear();
+    if (!trees) {
+        set_error("awg_remove_arg_thread: NULL trees");
+        return -1;
+    }
+    awg::ThreadTrees a;
+    a.ntrees = trees->ntrees; a.nnodes = trees->nnodes; a.start_coord = trees->start_coord;
+    a.ptrees = trees->ptrees; a.ages = trees->ages; a.sprs = trees->sprs;
+    a.blocklens = trees->blocklens; a.mapping = trees->mapping; a.c0 = trees->c0;
+    a.c1 = trees->c1; a.seqids = trees->seqids;
+    std::string err;
+    if (!awg::remove_arg_thread(a, seqid, err)) {
+        set_error(err);
+        return -1;
+    }
+    trees->ntrees = a.ntrees; trees->nnodes = a.nnodes;
+    trees->ptrees = std::move(a.ptrees); trees->ages = std::move(a.ages);
+    trees->sprs = std::move(a.sprs); trees->blocklens = std::move(a.blocklens);
+    trees->mapping = std::move(a.mapping); trees->c0 = std::move(a.c0);
+    trees->c1 = std::move(a.c1); trees->seqids = std::move(a.seqids);
     return 0;
 }
 int get_local_trees_ntrees(awg_local_trees *trees) { return trees ? trees->ntrees : 0; }
@@ -496,8 +641,9 @@ awg_local_trees *arghmm_sample_thread(awg_local_trees *trees, double *times, int
         set_error(err);
         return trees;
     }
-    awg_add_arg_thread(trees, ntimes, path.data(), seqlen, pos.data(), node.data(),
-                       time.data(), nrec);
+    if (awg_add_arg_thread(trees, ntimes, path.data(), seqlen, pos.data(), node.data(),
+                           time.data(), nrec) == 0 && !trees->seqids.empty())
+        trees->seqids.back() = nseqs - 1;  // the new leaf holds new_chrom (thread.cpp:292)
     return trees;
 }
 

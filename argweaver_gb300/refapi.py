@@ -327,6 +327,47 @@ def _read_trees(trees: "LocalTrees"):
     return pt, ag, sp, bl, mp
 
 
+def _read_structure(trees: "LocalTrees"):
+    """Each tree's root child[0] and the leaves' sequence ids of a handle."""
+    lib = capi.load()
+    nt = lib.get_local_trees_ntrees(trees.handle)
+    nn = lib.get_local_trees_nnodes(trees.handle)
+    c0, c1 = (np.zeros((nt, nn), dtype=np.int32) for _ in range(2))
+    if lib.awg_local_trees_children(trees.handle, c0.ctypes.data_as(capi.c_int_p),
+                                    c1.ctypes.data_as(capi.c_int_p)) != 0:
+        raise RuntimeError(capi.last_error())
+    nleaves = lib.awg_local_trees_seqids(trees.handle, None)
+    seqids = np.zeros(max(nleaves, 0), dtype=np.int32)
+    lib.awg_local_trees_seqids(trees.handle, seqids.ctypes.data_as(capi.c_int_p))
+    return c0, c1, seqids
+
+
+def remove_arg_thread(prob: Problem, seqids):
+    """remove_arg_thread (thread.cpp:425-556) of each listed sequence in turn from the
+    problem's full ARG, on the host. Returns, after each removal, a dict of the trees
+    (ptrees, ages, sprs, blocklens, mapping in the names get_local_trees_ptrees gives,
+    root_child0: each root's first child) and the leaves' sequence ids."""
+    lib = capi.load()
+    p = prob.normalized()
+    if p.internal:
+        raise ValueError("remove_arg_thread: full ARGs only")
+    trees = _trees_handle(p)
+    out = []
+    try:
+        for sid in seqids:
+            if lib.awg_remove_arg_thread(trees.handle, int(sid)) != 0:
+                raise ValueError(capi.last_error())
+            pt, ag, sp, bl, mp = _read_trees(trees)
+            c0, _c1, ids = _read_structure(trees)
+            roots = np.argmax(pt == -1, axis=1)
+            rc0 = c0[np.arange(len(roots)), roots]
+            out.append(dict(ptrees=pt, ages=ag, sprs=sp, blocklens=bl, mapping=mp,
+                            root_child0=rc0, seqids=ids))
+    finally:
+        trees.close()
+    return out
+
+
 def arghmm_sample_thread(prob: Problem) -> Problem:
     """The problem's ARG with its last sequence threaded in (draws from libc rand(): seed it
     with srand). The result is a full ARG over all the problem's sequences."""

@@ -50,13 +50,24 @@ int get_local_trees_ntrees(awg_local_trees *trees);
 int get_local_trees_nnodes(awg_local_trees *trees);
 
 /* get_local_trees_ptrees (local_tree.cpp:1846-1890): parents, ages, SPRs and block lengths
- * of every tree, into ntrees rows of the caller's arrays (leaf i is sequence i). */
+ * of every tree, into ntrees rows of the caller's arrays. Leaf i is named by the sequence
+ * it holds (awg_local_trees_seqids) when those ids are a permutation of the leaves, as the
+ * reference names them; otherwise by its own index. */
 void get_local_trees_ptrees(awg_local_trees *trees, int **ptrees, int **ages, int **sprs,
                             int *blocklens);
 
-/* The node mappings from each previous tree (ntrees x nnodes, row 0 all -1): after
- * awg_add_arg_thread they are no longer the default. 0, or -1 (awg_last_error). */
+/* The sequence each leaf holds (LocalTrees::seqids, local_tree.h:673) into nleaves ints
+ * (NULL: count only). Returns nleaves, or -1 (awg_last_error). */
+int awg_local_trees_seqids(awg_local_trees *trees, int *seqids);
+
+/* The node mappings from each previous tree (ntrees x nnodes, row 0 all -1), in the names
+ * get_local_trees_ptrees shows: after awg_add_arg_thread or awg_remove_arg_thread they are
+ * no longer the default. 0, or -1 (awg_last_error). */
 int awg_local_trees_mapping(awg_local_trees *trees, int *mapping);
+
+/* Each node's two children (ntrees x nnodes each, -1 for none) in the order the trees keep
+ * them, in the names get_local_trees_ptrees shows. 0, or -1 (awg_last_error). */
+int awg_local_trees_children(awg_local_trees *trees, int *c0, int *c1);
 
 /* Node mappings (ntrees x nnodes, row 0 ignored; NULL: make_node_mapping) and each root's
  * child[0] (NULL: children in index order) of trees whose structure the parent arrays do
@@ -70,6 +81,12 @@ int awg_local_trees_set_structure(awg_local_trees *trees, const int *mapping,
  * which grow by two nodes and one tree per recombination. 0, or -1 (awg_last_error). */
 int awg_add_arg_thread(awg_local_trees *trees, int ntimes, const int *path, int seqlen,
                        const int *rec_pos, const int *rec_node, const int *rec_time, int nrec);
+
+/* remove_arg_thread (thread.cpp:425-556), on the host: the leaf holding sequence `seqid`
+ * leaves every tree (the last leaf takes its index, with its sequence id), SPRs on the
+ * removed branch vanish and trees left without an SPR merge into the next
+ * (remove_null_sprs, local_tree.cpp:409-469). 0, or -1 (awg_last_error). */
+int awg_remove_arg_thread(awg_local_trees *trees, int seqid);
 
 /* arghmm_get_nstates (states.cpp:209): states of every column. */
 void arghmm_get_nstates(awg_local_trees *trees, int ntimes, bool internal, int *nstates);

@@ -33,6 +33,7 @@
 //                                    triples column, node, time) added to the problem's
 //                                    trees; writes the grown ARG as a problem
 //   samplethread <problem> <seed> <out>
+//   removethread <problem> <out-prefix> <seqid>...
 //                                    arghmm_sample_thread (sample_thread.cpp:1010-1023)
 //                                    after srand(seed): the last sequence threaded into the
 //                                    trees; writes the grown ARG as a problem
@@ -632,6 +633,45 @@ static int cmd_samplethread(const char *in, int seed, const char *out) {
     return 0;
 }
 
+// trees_to_problem when the leaves' sequence ids are a permutation of the leaves (the
+// names get_local_trees_ptrees gives), else in the trees' own leaf names; no sequences
+static void trees_to_problem_named(LocalTrees *trees, Problem &p) {
+    const int nleaves = trees->get_num_leaves();
+    vector<int> saved = trees->seqids;
+    vector<char> seen(nleaves, 0);
+    bool perm = (int)saved.size() == nleaves;
+    for (int i = 0; perm && i < nleaves; i++) {
+        perm = saved[i] >= 0 && saved[i] < nleaves && !seen[saved[i]];
+        if (perm) seen[saved[i]] = 1;
+    }
+    if (!perm) trees->set_default_seqids();
+    trees_to_problem(trees, p);
+    trees->seqids = saved;
+    p.nseqs = 0;
+    p.seqs.clear();
+}
+
+// remove_arg_thread (thread.cpp:425-556) of each listed sequence in turn; after removal i
+// the trees go to <prefix>.<i>.prob and the leaves' sequence ids to <prefix>.<i>.seqids
+static int cmd_removethread(const char *in, const char *prefix, int nrm, char **ids) {
+    Problem p = read_problem(in);
+    if (p.internal) die("removethread: full ARGs only");
+    LocalTrees *trees = make_trees(p);
+    for (int i = 0; i < nrm; i++) {
+        remove_arg_thread(trees, atoi(ids[i]));
+        Problem q = p;
+        trees_to_problem_named(trees, q);
+        std::string base = std::string(prefix) + "." + std::to_string(i);
+        write_problem((base + ".prob").c_str(), q);
+        FILE *f = fopen((base + ".seqids").c_str(), "wb");
+        if (!f) die("cannot write seqids");
+        wr(f, trees->seqids.data(), trees->seqids.size());
+        fclose(f);
+    }
+    delete trees;
+    return 0;
+}
+
 static int cmd_cut(const char *in, int seed, const char *out) {
     Problem p = read_problem(in);
     if (p.internal) die("cut: input must be a full (external-format) ARG");
@@ -661,6 +701,8 @@ int main(int argc, char **argv) {
     if (cmd == "argprob" && argc == 4) return cmd_argprob(argv[2], argv[3]);
     if (cmd == "samplethread" && argc == 5)
         return cmd_samplethread(argv[2], atoi(argv[3]), argv[4]);
+    if (cmd == "removethread" && argc >= 5)
+        return cmd_removethread(argv[2], argv[3], argc - 4, argv + 4);
     if (cmd == "addthread" && argc == 6)
         return cmd_addthread(argv[2], argv[3], argv[4], argv[5]);
     if (cmd == "recomb" && argc == 6)

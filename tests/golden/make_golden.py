@@ -324,6 +324,41 @@ def samplethread(tmp):
         print(name, Problem.load(os.path.join(out_dir, name + ".prob")).ntrees)
 
 
+# sequences removed in turn from the grown ARGs (removal orders: the last leaf, middle
+# leaves, the first; one run down to the trunk genealogy)
+REMOVALS = {
+    "dsmc_k8_s11": [3, 0, 7, 5, 1, 6, 2],
+    "dsmc_k10_T16": [9, 4],
+    "dsmc_k17_missing": [0, 16, 8, 3],
+    "sim1_c20": [2, 5],
+    "single_k7_s41": [6, 0, 1],
+}
+
+
+def removethread(tmp):
+    """remove_arg_thread (thread.cpp:425-556) on the ARGs add_arg_thread grew: after each
+    removal, the trees in the names get_local_trees_ptrees gives (leaf names when the
+    sequence ids are no permutation of the leaves), mappings, root children and sequence ids."""
+    out_dir = os.path.join(HERE, "removethread")
+    os.makedirs(out_dir, exist_ok=True)
+    for name, ids in REMOVALS.items():
+        pp = os.path.join(HERE, "addthread", name + ".prob")
+        prefix = os.path.join(tmp, name)
+        run("removethread", pp, prefix, *ids)
+        arrays = {"removed": np.asarray(ids, dtype=np.int32)}
+        for i in range(len(ids)):
+            q = Problem.load(f"{prefix}.{i}.prob")
+            arrays[f"ptrees_{i}"] = q.ptrees
+            arrays[f"ages_{i}"] = q.ages
+            arrays[f"sprs_{i}"] = q.sprs
+            arrays[f"blocklens_{i}"] = q.blocklens
+            arrays[f"mapping_{i}"] = q.mapping
+            arrays[f"root_child0_{i}"] = q.root_child0
+            arrays[f"seqids_{i}"] = np.fromfile(f"{prefix}.{i}.seqids", dtype=np.int32)
+        np.savez_compressed(os.path.join(out_dir, name + ".npz"), **arrays)
+        print(name, [int(arrays[f"ptrees_{i}"].shape[0]) for i in range(len(ids))])
+
+
 def infsites(tmp):
     """The infinite-sites penalty (ArgModel::infsites_penalty, emit.cpp:847-862; arg-sample
     --infsites uses 1e-100): external, with missing calls, and an internal-branch cut."""
@@ -347,6 +382,10 @@ def main():
     if sys.argv[1:] == ["infsites"]:
         with tempfile.TemporaryDirectory() as tmp:
             infsites(tmp)
+        return
+    if sys.argv[1:] == ["removethread"]:
+        with tempfile.TemporaryDirectory() as tmp:
+            removethread(tmp)
         return
     if sys.argv[1:] == ["samplethread"]:
         with tempfile.TemporaryDirectory() as tmp:

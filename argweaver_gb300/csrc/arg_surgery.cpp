@@ -12,6 +12,9 @@
 // kept as the reference keeps it (it decides which child a later SPR replaces), so the
 // handle stores children next to parents.
 
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -369,6 +372,118 @@ void remove_tree_branch(Tree &t, int nnodes, int remove_leaf, std::vector<int> &
 
 }  // namespace
 
+namespace {
+
+// The trees of a handle with their children (stored order, else index order), SPRs (the
+// first tree's null) and mappings from the previous tree (make_node_mapping,
+// local_tree.h:767-776, where none are stored).
+bool load_trees(const ThreadTrees &a, std::vector<Tree> &trees,
+                std::vector<std::vector<int>> &maps, std::vector<Spr4> &sprs, const char *who,
+                std::string &err) {
+    const int nnodes = a.nnodes, B = a.ntrees;
+    trees.assign(B, Tree());
+    maps.assign(B, std::vector<int>());
+    sprs.assign(B, Spr4{{-1, -1, -1, -1}});
+    for (int b = 0; b < B; b++) {
+        Tree &t = trees[b];
+        t.nd.resize(nnodes);
+        for (int i = 0; i < nnodes; i++) {
+            t.nd[i].parent = a.ptrees[(size_t)b * nnodes + i];
+            t.nd[i].age = a.ages[(size_t)b * nnodes + i];
+            if (t.nd[i].parent < -1 || t.nd[i].parent >= nnodes) {
+                err = std::string(who) + ": a parent out of range";
+                return false;
+            }
+            if (t.nd[i].parent == -1) t.root = i;
+        }
+        if (!a.c0.empty()) {
+            for (int i = 0; i < nnodes; i++) {
+                t.nd[i].c0 = a.c0[(size_t)b * nnodes + i];
+                t.nd[i].c1 = a.c1[(size_t)b * nnodes + i];
+            }
+        } else {
+            for (int i = 0; i < nnodes; i++) {
+                const int p = t.nd[i].parent;
+                if (p == -1) continue;
+                if (t.nd[p].c0 == -1) t.nd[p].c0 = i;
+                else t.nd[p].c1 = i;
+            }
+        }
+        if (b == 0) continue;
+        for (int k = 0; k < 4; k++) sprs[b].v[k] = a.sprs[(size_t)b * 4 + k];
+        const int r = sprs[b].v[0], c = sprs[b].v[2];
+        if (r < 0 || r >= nnodes || c < 0 || c >= nnodes) {
+            err = std::string(who) + ": an SPR node out of range";
+            return false;
+        }
+        if (!a.mapping.empty()) {
+            maps[b].assign(a.mapping.begin() + (size_t)b * nnodes,
+                           a.mapping.begin() + (size_t)(b + 1) * nnodes);
+        } else {
+            maps[b].resize(nnodes);
+            for (int i = 0; i < nnodes; i++) maps[b][i] = i;
+            const int broken = trees[b - 1].nd[r].parent;
+            if (broken >= 0) maps[b][broken] = -1;
+        }
+    }
+    return true;
+}
+
+// remove_null_sprs (local_tree.cpp:409-469): a tree whose successor has no SPR is absorbed
+// by it (block lengths add, the mappings compose, its SPR moves over; the first tree's
+// successor becomes the first tree). The first n nodes of each tree are kept.
+ThreadTrees merge_null_sprs(const std::vector<Tree> &trees, std::vector<std::vector<int>> &maps,
+                            const std::vector<Spr4> &sprs, const std::vector<int> &blocklens,
+                            int n, int start_coord, const std::vector<int> &seqids) {
+    ThreadTrees out;
+    out.nnodes = n;
+    out.start_coord = start_coord;
+    out.seqids = seqids;
+    struct Pending {
+        int b, blocklen;
+        Spr4 spr;
+        std::vector<int> map;
+        bool has_map;
+    };
+    auto emit = [&](const Pending &p) {
+        const Tree &t = trees[p.b];
+        for (int i = 0; i < n; i++) {
+            out.ptrees.push_back(t.nd[i].parent);
+            out.ages.push_back(t.nd[i].age);
+            out.c0.push_back(t.nd[i].c0);
+            out.c1.push_back(t.nd[i].c1);
+            out.mapping.push_back(p.has_map ? p.map[i] : -1);
+        }
+        for (int k = 0; k < 4; k++) out.sprs.push_back(p.spr.v[k]);
+        out.blocklens.push_back(p.blocklen);
+        out.ntrees++;
+    };
+    const int B = (int)trees.size();
+    Pending cur{0, blocklens[0], sprs[0], {}, false};
+    for (int b = 1; b < B; b++) {
+        Pending nx{b, blocklens[b], sprs[b], std::move(maps[b]), true};
+        nx.map.resize(n);
+        if (nx.spr.v[0] == -1) {  // no SPR into tree b: tree cur merges into it
+            if (!cur.has_map) {
+                nx.has_map = false;
+            } else {
+                std::vector<int> comp(n);
+                for (int i = 0; i < n; i++) comp[i] = cur.map[i] != -1 ? nx.map[cur.map[i]] : -1;
+                nx.map = std::move(comp);
+                nx.spr = cur.spr;
+            }
+            nx.blocklen += cur.blocklen;
+        } else {
+            emit(cur);
+        }
+        cur = std::move(nx);
+    }
+    emit(cur);
+    return out;
+}
+
+}  // namespace
+
 bool remove_arg_thread(ThreadTrees &a, int seqid, std::string &err) {
     const int nnodes = a.nnodes, B = a.ntrees;
     const int nleaves = (nnodes + 1) / 2, last_leaf = nleaves - 1;
@@ -411,48 +526,10 @@ bool remove_arg_thread(ThreadTrees &a, int seqid, std::string &err) {
         err = "remove_arg_thread: no thread to remove";
         return false;
     }
-    // the trees with their children (stored order, else index order) and mappings
-    std::vector<Tree> trees(B);
-    std::vector<std::vector<int>> maps(B);
-    std::vector<Spr4> sprs(B);
-    for (int b = 0; b < B; b++) {
-        Tree &t = trees[b];
-        t.nd.resize(nnodes);
-        for (int i = 0; i < nnodes; i++) {
-            t.nd[i].parent = a.ptrees[(size_t)b * nnodes + i];
-            t.nd[i].age = a.ages[(size_t)b * nnodes + i];
-            if (t.nd[i].parent == -1) t.root = i;
-        }
-        if (!a.c0.empty()) {
-            for (int i = 0; i < nnodes; i++) {
-                t.nd[i].c0 = a.c0[(size_t)b * nnodes + i];
-                t.nd[i].c1 = a.c1[(size_t)b * nnodes + i];
-            }
-        } else {
-            for (int i = 0; i < nnodes; i++) {
-                const int p = t.nd[i].parent;
-                if (p == -1) continue;
-                if (t.nd[p].c0 == -1) t.nd[p].c0 = i;
-                else t.nd[p].c1 = i;
-            }
-        }
-        for (int k = 0; k < 4; k++) sprs[b].v[k] = b > 0 ? a.sprs[(size_t)b * 4 + k] : -1;
-        if (b > 0) {
-            if (!a.mapping.empty()) {
-                maps[b].assign(a.mapping.begin() + (size_t)b * nnodes,
-                               a.mapping.begin() + (size_t)(b + 1) * nnodes);
-            } else {  // make_node_mapping (local_tree.h:767-776)
-                maps[b].resize(nnodes);
-                for (int i = 0; i < nnodes; i++) maps[b][i] = i;
-                const int r = sprs[b].v[0];
-                if (r < 0 || r >= nnodes) {
-                    err = "remove_arg_thread: an SPR node out of range";
-                    return false;
-                }
-                maps[b][trees[b - 1].nd[r].parent] = -1;
-            }
-        }
-    }
+    std::vector<Tree> trees;
+    std::vector<std::vector<int>> maps;
+    std::vector<Spr4> sprs;
+    if (!load_trees(a, trees, maps, sprs, "remove_arg_thread", err)) return false;
     std::vector<int> displace;
     for (int b = 0; b < B; b++) {
         Tree &t = trees[b];
@@ -495,55 +572,252 @@ bool remove_arg_thread(ThreadTrees &a, int seqid, std::string &err) {
         }
         if (spr[0] == spr[2]) { set_null(); continue; }  // a bubble
     }
-    const int n2 = nnodes - 2;
     seqids[remove_leaf] = seqids[last_leaf];
     seqids.resize(nleaves - 1);
-    // remove_null_sprs (local_tree.cpp:409-469): a tree whose successor has no SPR is
-    // absorbed by it (block lengths add, the mappings compose, its SPR moves over)
-    ThreadTrees out;
-    out.nnodes = n2;
-    out.start_coord = a.start_coord;
-    out.seqids = seqids;
-    struct Pending {
-        int b, blocklen;
-        Spr4 spr;
-        std::vector<int> map;
-        bool has_map;
-    };
-    auto emit = [&](const Pending &p) {
-        const Tree &t = trees[p.b];
-        for (int i = 0; i < n2; i++) {
-            out.ptrees.push_back(t.nd[i].parent);
-            out.ages.push_back(t.nd[i].age);
-            out.c0.push_back(t.nd[i].c0);
-            out.c1.push_back(t.nd[i].c1);
-            out.mapping.push_back(p.has_map ? p.map[i] : -1);
-        }
-        for (int k = 0; k < 4; k++) out.sprs.push_back(p.spr.v[k]);
-        out.blocklens.push_back(p.blocklen);
-        out.ntrees++;
-    };
-    Pending cur{0, a.blocklens[0], sprs[0], {}, false};
-    for (int b = 1; b < B; b++) {
-        Pending nx{b, a.blocklens[b], sprs[b], maps[b], true};
-        nx.map.resize(n2);
-        if (nx.spr.v[0] == -1) {  // no SPR into tree b: tree cur merges into it
-            if (!cur.has_map) {
-                nx.has_map = false;
-            } else {
-                std::vector<int> comp(n2);
-                for (int i = 0; i < n2; i++) comp[i] = cur.map[i] != -1 ? nx.map[cur.map[i]] : -1;
-                nx.map = comp;
-                nx.spr = cur.spr;
-            }
-            nx.blocklen += cur.blocklen;
-        } else {
-            emit(cur);
-        }
-        cur = nx;
+    a = merge_null_sprs(trees, maps, sprs, a.blocklens, nnodes - 2, a.start_coord, seqids);
+    return true;
+}
+
+namespace {
+
+int sibling(const Tree &t, int v) {
+    const int p = t.nd[v].parent;
+    if (p == -1) return -1;
+    return t.nd[p].c0 == v ? t.nd[p].c1 : t.nd[p].c0;
+}
+
+// get_recoal_node (local_tree.cpp:473-488): the first node of the next tree nothing maps to
+int recoal_node(int n, const std::vector<int> &mapping) {
+    std::vector<char> mapped(n, 0);
+    for (int i = 0; i < n; i++)
+        if (mapping[i] != -1) mapped[mapping[i]] = 1;
+    for (int i = 0; i < n; i++)
+        if (!mapped[i]) return i;
+    return -1;
+}
+
+// get_next_removal_nodes (thread.cpp:562-591): where a removal path on `node` of tree1
+// continues in the next tree: the passive branch, and the recoalescence when the SPR
+// coalesces on `node`
+void next_removal_nodes(const Tree &tree1, const Spr4 &spr, const std::vector<int> &mapping,
+                        int node, int next[2], int recoal) {
+    const int n = (int)tree1.nd.size();
+    if (recoal == -1) recoal = recoal_node(n, mapping);
+    next[0] = mapping[node];
+    if (next[0] == -1) {  // node broken by the SPR: the sibling's branch, or the recoalescence
+        const int sib = sibling(tree1, spr.v[0]);
+        next[0] = spr.v[2] == sib ? recoal : mapping[sib];
     }
-    emit(cur);
-    a = std::move(out);
+    next[1] = spr.v[2] == node ? recoal : -1;
+}
+
+// get_prev_removal_nodes (thread.cpp:609-647): the branches of tree1 a removal path on
+// `node` of the next tree can come from
+void prev_removal_nodes(const Tree &tree1, const Spr4 &spr, const std::vector<int> &mapping,
+                        const std::vector<int> &inv, int node, int prev[2]) {
+    prev[0] = inv[node];
+    const int sib = sibling(tree1, spr.v[0]);
+    if (prev[0] == -1) {  // node is the recoalescence
+        prev[0] = spr.v[2];
+        prev[1] = sib == spr.v[2] ? tree1.nd[sib].parent : -1;
+    } else {
+        prev[1] = mapping[sib] == node && sib != spr.v[2] ? tree1.nd[sib].parent : -1;
+    }
+}
+
+std::vector<int> inverse_mapping(const std::vector<int> &mapping, int n) {
+    std::vector<int> inv(n, -1);
+    for (int i = 0; i < n; i++)
+        if (mapping[i] != -1) inv[mapping[i]] = i;
+    return inv;
+}
+
+// logadd and logsum (common.h:157-163,182-201)
+double log_add(double a, double b) {
+    if (a == -INFINITY) return b;
+    if (b == -INFINITY) return a;
+    return std::max(a, b) + std::log1p(std::exp(-std::fabs(a - b)));
+}
+
+double log_sum(const double *v, int n) {
+    if (n == 0) return 1.0;
+    double m = v[0];
+    for (int i = 1; i < n; i++)
+        if (v[i] > m) m = v[i];
+    double e = 0.0;
+    for (int i = 0; i < n; i++)
+        if (v[i] - m > -15) e += std::exp(v[i] - m);
+    return m + std::log(e);
+}
+
+double unit(int (*rnd)()) { return rnd() / double(RAND_MAX); }  // frand (common.h:103-104)
+
+// one step of a removal path forward (sample_arg_removal_path_forward, thread.cpp:703-735):
+// the second branch is taken when rand() < 0.5, i.e. when rand() returns 0, as there
+int step_forward(const Tree &last, const Spr4 &spr, const std::vector<int> &mapping, int node,
+                 int (*rnd)()) {
+    int next[2];
+    next_removal_nodes(last, spr, mapping, node, next, -1);
+    if (next[1] == -1 || !rnd) return next[0];
+    return next[int(rnd() < 0.5)];
+}
+
+}  // namespace
+
+bool sample_removal_path(const ThreadTrees &a, int node, long long pos, int (*rnd)(), int *path,
+                         std::string &err) {
+    std::vector<Tree> trees;
+    std::vector<std::vector<int>> maps;
+    std::vector<Spr4> sprs;
+    if (!load_trees(a, trees, maps, sprs, "sample_arg_removal_path", err)) return false;
+    if (node < 0 || node >= a.nnodes) {
+        err = "sample_arg_removal_path: node out of range";
+        return false;
+    }
+    const int B = a.ntrees;
+    int i0 = 0;
+    if (pos >= 0) {  // the block holding pos (thread.cpp:772-790)
+        long long end = a.start_coord;
+        for (i0 = 0; i0 < B; i0++) {
+            const long long start = end;
+            end += a.blocklens[i0];
+            if (start <= pos && pos < end) break;
+        }
+        if (i0 == B) {
+            err = "sample_arg_removal_path: pos outside the trees";
+            return false;
+        }
+    }
+    path[i0] = node;
+    for (int b = i0 + 1; b < B; b++)
+        path[b] = step_forward(trees[b - 1], sprs[b], maps[b], path[b - 1], rnd);
+    // backward from the block (sample_arg_removal_path_backward, thread.cpp:738-769)
+    for (int b = i0 - 1; b >= 0; b--) {
+        int prev[2];
+        prev_removal_nodes(trees[b], sprs[b + 1], maps[b + 1],
+                           inverse_mapping(maps[b + 1], a.nnodes), path[b + 1], prev);
+        path[b] = prev[1] == -1 ? prev[0] : prev[int(rnd() < 0.5)];
+    }
+    return true;
+}
+
+bool sample_removal_path_uniform(const ThreadTrees &a, int (*rnd)(), int *path, double *lntotal,
+                                 std::string &err) {
+    std::vector<Tree> trees;
+    std::vector<std::vector<int>> maps;
+    std::vector<Spr4> sprs;
+    if (!load_trees(a, trees, maps, sprs, "sample_arg_removal_path_uniform", err)) return false;
+    const int B = a.ntrees, n = a.nnodes;
+    // log path counts and back pointers (count_arg_removal_paths, thread.cpp:914-950)
+    std::vector<double> counts((size_t)B * n, 0.0);
+    std::vector<int> back((size_t)B * n * 2, -1);
+    for (int b = 1; b < B; b++) {
+        const std::vector<int> inv = inverse_mapping(maps[b], n);
+        for (int j = 0; j < n; j++) {
+            int *ptr = &back[((size_t)b * n + j) * 2];
+            prev_removal_nodes(trees[b - 1], sprs[b], maps[b], inv, j, ptr);
+            const double *c = &counts[(size_t)(b - 1) * n];
+            if (ptr[0] < 0 || ptr[0] >= n || ptr[1] >= n) {
+                err = "sample_arg_removal_path_uniform: inconsistent SPR between neighbouring trees";
+                return false;
+            }
+            counts[(size_t)b * n + j] = ptr[1] == -1 ? c[ptr[0]] : log_add(c[ptr[0]], c[ptr[1]]);
+        }
+    }
+    // the last branch by path counts (sample, common.h:272-290), then back (thread.cpp:963-1002)
+    const double *last = &counts[(size_t)(B - 1) * n];
+    const double norm = log_sum(last, n);
+    std::vector<double> w(n);
+    double total = 0.0;
+    for (int j = 0; j < n; j++) {
+        w[j] = std::exp(last[j] - norm);
+        total += w[j];
+    }
+    const double pick = unit(rnd) * total;
+    double x = 0.0;
+    int k = n - 1;
+    for (int j = 0; j < n; j++) {
+        x += w[j];
+        if (x >= pick) {
+            k = j;
+            break;
+        }
+    }
+    path[B - 1] = k;
+    for (int b = B - 1; b > 0; b--) {
+        const int *ptr = &back[((size_t)b * n + path[b]) * 2];
+        if (ptr[1] == -1) {
+            path[b - 1] = ptr[0];
+        } else {
+            const double p1 = counts[(size_t)(b - 1) * n + ptr[0]];
+            const double p2 = counts[(size_t)(b - 1) * n + ptr[1]];
+            path[b - 1] = std::log(unit(rnd)) < p1 - log_add(p1, p2) ? ptr[0] : ptr[1];
+        }
+    }
+    if (lntotal) *lntotal = log_sum(last, n);
+    return true;
+}
+bool remove_thread_path(ThreadTrees &a, const int *removal_path, int maxtime,
+                        std::string &err) {
+    std::vector<Tree> trees;
+    std::vector<std::vector<int>> maps;
+    std::vector<Spr4> sprs;
+    if (!load_trees(a, trees, maps, sprs, "remove_arg_thread_path", err)) return false;
+    const int B = a.ntrees, n = a.nnodes;
+    for (int b = 0; b < B; b++)
+        if (removal_path[b] < 0 || removal_path[b] >= n) {
+            err = "remove_arg_thread_path: a path node out of range";
+            return false;
+        }
+    for (int b = 0; b < B; b++) {
+        Tree &t = trees[b];
+        const Tree *last = b > 0 ? &trees[b - 1] : nullptr;
+        const int rn = removal_path[b];
+        if (rn == t.root) {  // the path has left the tree over the top: nothing to cut
+            if (last && removal_path[b - 1] != last->root) maps[b][last->root] = -1;
+            continue;
+        }
+        // cut the branch above rn and regraft it over the root at maxtime: the tree in
+        // subtree/main-tree form, the subtree the root's first child
+        const int broken = t.nd[rn].parent;
+        const int coal_time = t.nd[broken].age;
+        const int broken_child = sibling(t, rn);
+        const int cut[4] = {rn, t.nd[rn].age, t.root, maxtime};
+        apply_spr(t, cut);
+        const int mainr = sibling(t, rn);
+        Node &root = t.nd[t.root];
+        if (root.c0 == mainr) {
+            root.c0 = rn;
+            root.c1 = mainr;
+        }
+        if (last && removal_path[b - 1] != last->root) maps[b][last->root] = t.root;
+        if (b + 1 == B) continue;
+        // the SPR into the next tree (thread.cpp:1560-1635)
+        int *spr = sprs[b + 1].v;
+        std::vector<int> &m = maps[b + 1];
+        auto set_null = [&]() { spr[0] = spr[1] = spr[2] = spr[3] = -1; };
+        if (spr[0] == rn) { set_null(); continue; }  // recombination on the removed branch
+        if (spr[0] == broken) spr[0] = broken_child;
+        int next[2];
+        next_removal_nodes(t, sprs[b + 1], m, rn, next, -1);
+        if (spr[2] == rn) {
+            if (removal_path[b + 1] == next[0]) {  // the path takes the lower branch
+                if (spr[0] == broken_child) { set_null(); continue; }  // now a bubble
+                spr[2] = broken_child;  // a mediated coalescence
+                spr[3] = coal_time;
+            }  // else the path takes the upper branch: the recoalescence stays
+        } else if (spr[2] == broken) {
+            spr[2] = broken_child;
+        }
+        if (spr[0] == spr[2]) { set_null(); continue; }  // a bubble
+        const int spr_broken = t.nd[spr[0]].parent;
+        if (spr_broken < 0) {
+            err = "remove_arg_thread_path: a recombination on the root";
+            return false;
+        }
+        m[spr_broken] = -1;
+    }
+    a = merge_null_sprs(trees, maps, sprs, a.blocklens, n, a.start_coord, a.seqids);
     return true;
 }
 

@@ -29,4 +29,22 @@ bool add_arg_thread(ThreadTrees &a, int T, const int *path, int seqlen, const in
 // left without an SPR merge with their neighbour (remove_null_sprs, local_tree.cpp:409-469).
 bool remove_arg_thread(ThreadTrees &a, int seqid, std::string &err);
 
+// A removal path (one branch per tree) through the trees: from `node` of the block holding
+// `pos` forward and backward (pos >= 0: sample_arg_removal_path, thread.cpp:772-790), or from
+// `node` of the first tree forward (pos < 0: thread.cpp:793-799). rnd draws the branch at
+// each split as the reference does (rand() < .5); rnd NULL (forward only) always keeps the
+// passive branch, which is the leaf path (sample_arg_removal_leaf_path, thread.cpp:672-700).
+bool sample_removal_path(const ThreadTrees &a, int node, long long pos, int (*rnd)(), int *path,
+                         std::string &err);
+
+// A removal path drawn uniformly from all paths by counting them back to front
+// (sample_arg_removal_path_uniform, thread.cpp:914-1002); lntotal: the log path count.
+bool sample_removal_path_uniform(const ThreadTrees &a, int (*rnd)(), int *path, double *lntotal,
+                                 std::string &err);
+
+// Cuts the ARG along a removal path (remove_arg_thread_path, thread.cpp:1481-1668): in every
+// tree the path's branch is pruned and regrafted above the root at maxtime (the subtree the
+// root's first child), SPRs and mappings follow, trees left without an SPR merge.
+bool remove_thread_path(ThreadTrees &a, const int *removal_path, int maxtime, std::string &err);
+
 }  // namespace awg

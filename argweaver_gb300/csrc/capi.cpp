@@ -471,6 +471,69 @@ int awg_add_arg_thread(awg_local_trees *trees, int ntimes, const int *path, int 
     return 0;
 }
 
+static awg::ThreadTrees thread_trees(const awg_local_trees *t) {
+    awg::ThreadTrees a;
+    a.ntrees = t->ntrees; a.nnodes = t->nnodes; a.start_coord = t->start_coord;
+    a.ptrees = t->ptrees; a.ages = t->ages; a.sprs = t->sprs; a.blocklens = t->blocklens;
+    a.mapping = t->mapping; a.c0 = t->c0; a.c1 = t->c1; a.seqids = t->seqids;
+    return a;
+}
+
+static void store_trees(awg_local_trees *t, awg::ThreadTrees &a) {
+    t->ntrees = a.ntrees; t->nnodes = a.nnodes;
+    t->ptrees = std::move(a.ptrees); t->ages = std::move(a.ages); t->sprs = std::move(a.sprs);
+    t->blocklens = std::move(a.blocklens); t->mapping = std::move(a.mapping);
+    t->c0 = std::move(a.c0); t->c1 = std::move(a.c1); t->seqids = std::move(a.seqids);
+}
+
+// Removal paths and the internal-branch cut (thread.cpp:1681-1716). Paths hold one node
+// per tree in the trees' own node names; draws come from libc rand(), as the reference's.
+void arghmm_sample_arg_removal_path(awg_local_trees *trees, int node, int *path) {
+    g_err.clear();
+    std::string err;
+    if (!trees || !path) set_error("arghmm_sample_arg_removal_path: NULL argument");
+    else if (!awg::sample_removal_path(thread_trees(trees), node, -1, rand, path, err))
+        set_error(err);
+}
+
+void arghmm_sample_arg_removal_path2(awg_local_trees *trees, int node, int pos, int *path) {
+    g_err.clear();
+    std::string err;
+    if (!trees || !path) set_error("arghmm_sample_arg_removal_path2: NULL argument");
+    else if (!awg::sample_removal_path(thread_trees(trees), node, pos, rand, path, err))
+        set_error(err);
+}
+
+void arghmm_sample_arg_removal_leaf_path(awg_local_trees *trees, int node, int *path) {
+    g_err.clear();
+    std::string err;
+    if (!trees || !path) set_error("arghmm_sample_arg_removal_leaf_path: NULL argument");
+    else if (!awg::sample_removal_path(thread_trees(trees), node, -1, nullptr, path, err))
+        set_error(err);
+}
+
+double awg_sample_arg_removal_path_uniform(awg_local_trees *trees, int *path) {
+    g_err.clear();
+    std::string err;
+    double lntotal = NAN;
+    if (!trees || !path) set_error("awg_sample_arg_removal_path_uniform: NULL argument");
+    else if (!awg::sample_removal_path_uniform(thread_trees(trees), rand, path, &lntotal, err))
+        set_error(err);
+    return lntotal;
+}
+
+void arghmm_remove_arg_thread_path(awg_local_trees *trees, int *removal_path, int maxtime) {
+    g_err.clear();
+    if (!trees || !removal_path) {
+        set_error("arghmm_remove_arg_thread_path: NULL argument");
+        return;
+    }
+    awg::ThreadTrees a = thread_trees(trees);
+    std::string err;
+    if (!awg::remove_thread_path(a, removal_path, maxtime, err)) set_error(err);
+    else store_trees(trees, a);
+}
+
 // remove_arg_thread (thread.cpp:425-556) on the host: the leaf holding sequence `seqid`
 // leaves every tree; the last leaf takes its name (its sequence id moves with it).
 int awg_remove_arg_thread(awg_local_trees *trees, int seqid) {
@@ -479,21 +542,13 @@ int awg_remove_arg_thread(awg_local_trees *trees, int seqid) {
         set_error("awg_remove_arg_thread: NULL trees");
         return -1;
     }
-    awg::ThreadTrees a;
-    a.ntrees = trees->ntrees; a.nnodes = trees->nnodes; a.start_coord = trees->start_coord;
-    a.ptrees = trees->ptrees; a.ages = trees->ages; a.sprs = trees->sprs;
-    a.blocklens = trees->blocklens; a.mapping = trees->mapping; a.c0 = trees->c0;
-    a.c1 = trees->c1; a.seqids = trees->seqids;
+    awg::ThreadTrees a = thread_trees(trees);
     std::string err;
     if (!awg::remove_arg_thread(a, seqid, err)) {
         set_error(err);
         return -1;
     }
-    trees->ntrees = a.ntrees; trees->nnodes = a.nnodes;
-    trees->ptrees = std::move(a.ptrees); trees->ages = std::move(a.ages);
-    trees->sprs = std::move(a.sprs); trees->blocklens = std::move(a.blocklens);
-    trees->mapping = std::move(a.mapping); trees->c0 = std::move(a.c0);
-    trees->c1 = std::move(a.c1); trees->seqids = std::move(a.seqids);
+    store_trees(trees, a);
     return 0;
 }
 int get_local_trees_ntrees(awg_local_trees *trees) { return trees ? trees->ntrees : 0; }

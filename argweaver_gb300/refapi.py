@@ -357,15 +357,79 @@ def remove_arg_thread(prob: Problem, seqids):
         for sid in seqids:
             if lib.awg_remove_arg_thread(trees.handle, int(sid)) != 0:
                 raise ValueError(capi.last_error())
-            pt, ag, sp, bl, mp = _read_trees(trees)
-            c0, _c1, ids = _read_structure(trees)
-            roots = np.argmax(pt == -1, axis=1)
-            rc0 = c0[np.arange(len(roots)), roots]
-            out.append(dict(ptrees=pt, ages=ag, sprs=sp, blocklens=bl, mapping=mp,
-                            root_child0=rc0, seqids=ids))
+            out.append(_tree_dict(trees))
     finally:
         trees.close()
     return out
+
+
+def _tree_dict(trees: "LocalTrees") -> dict:
+    pt, ag, sp, bl, mp = _read_trees(trees)
+    c0, _c1, ids = _read_structure(trees)
+    roots = np.argmax(pt == -1, axis=1)
+    return dict(ptrees=pt, ages=ag, sprs=sp, blocklens=bl, mapping=mp,
+                root_child0=c0[np.arange(len(roots)), roots], seqids=ids)
+
+
+def _with_trees(prob: Problem, fn):
+    p = prob.normalized()
+    trees = _trees_handle(p)
+    try:
+        return fn(capi.load(), trees, p)
+    finally:
+        trees.close()
+
+
+def sample_arg_removal_path(prob: Problem, node: int, pos: int | None = None,
+                            leaf: bool = False) -> np.ndarray:
+    """A removal path (one node per tree) from `node` of the first tree forward
+    (sample_arg_removal_path, thread.cpp:793-799), through `node` at coordinate `pos`
+    (thread.cpp:772-790), or the leaf path (leaf=True, thread.cpp:672-700); draws from libc
+    rand() (seed it with srand)."""
+    def run(lib, trees, p):
+        path = np.zeros(p.ntrees, dtype=np.int32)
+        ptr = path.ctypes.data_as(capi.c_int_p)
+        if leaf:
+            lib.arghmm_sample_arg_removal_leaf_path(trees.handle, int(node), ptr)
+        elif pos is None:
+            lib.arghmm_sample_arg_removal_path(trees.handle, int(node), ptr)
+        else:
+            lib.arghmm_sample_arg_removal_path2(trees.handle, int(node), int(pos), ptr)
+        err = capi.last_error()
+        if err:
+            raise ValueError(err)
+        return path
+    return _with_trees(prob, run)
+
+
+def sample_arg_removal_path_uniform(prob: Problem):
+    """(path, log number of paths): a removal path drawn uniformly over all of them
+    (sample_arg_removal_path_uniform, thread.cpp:963-1002); draws from libc rand()."""
+    def run(lib, trees, p):
+        path = np.zeros(p.ntrees, dtype=np.int32)
+        lnt = lib.awg_sample_arg_removal_path_uniform(trees.handle, path.ctypes.data_as(capi.c_int_p))
+        err = capi.last_error()
+        if err:
+            raise ValueError(err)
+        return path, lnt
+    return _with_trees(prob, run)
+
+
+def remove_arg_thread_path(prob: Problem, path, maxtime: int | None = None) -> dict:
+    """The problem's ARG cut along a removal path (remove_arg_thread_path, thread.cpp:1481-1668;
+    maxtime defaults to ntimes + 1 as arg-sample passes): the trees in subtree/main-tree form
+    as a dict (ptrees, ages, sprs, blocklens, mapping, root_child0, seqids)."""
+    def run(lib, trees, p):
+        rp = np.ascontiguousarray(path, dtype=np.int32)
+        if rp.shape != (p.ntrees,):
+            raise ValueError("remove_arg_thread_path: the path needs one node per tree")
+        lib.arghmm_remove_arg_thread_path(trees.handle, rp.ctypes.data_as(capi.c_int_p),
+                                          p.ntimes + 1 if maxtime is None else int(maxtime))
+        err = capi.last_error()
+        if err:
+            raise ValueError(err)
+        return _tree_dict(trees)
+    return _with_trees(prob, run)
 
 
 def arghmm_sample_thread(prob: Problem) -> Problem:

@@ -88,6 +88,25 @@ int awg_add_arg_thread(awg_local_trees *trees, int ntimes, const int *path, int 
  * (remove_null_sprs, local_tree.cpp:409-469). 0, or -1 (awg_last_error). */
 int awg_remove_arg_thread(awg_local_trees *trees, int seqid);
 
+/* Removal paths (thread.cpp:1681-1703): one node per tree, in the trees' own node names, into
+ * `path` (ntrees ints), drawn from libc rand() as the reference draws them. From `node` of the
+ * first tree forward (sample_arg_removal_path, :793-799); through `node` of the block holding
+ * coordinate `pos`, forward and backward (:772-790); the leaf path, no draws (:672-700).
+ * Errors: awg_last_error(). */
+void arghmm_sample_arg_removal_path(awg_local_trees *trees, int node, int *path);
+void arghmm_sample_arg_removal_path2(awg_local_trees *trees, int node, int pos, int *path);
+void arghmm_sample_arg_removal_leaf_path(awg_local_trees *trees, int node, int *path);
+
+/* A removal path drawn uniformly over all of them (sample_arg_removal_path_uniform,
+ * thread.cpp:963-1002, which arg-sample's subtree cuts use); returns the log number of paths,
+ * NaN on error. */
+double awg_sample_arg_removal_path_uniform(awg_local_trees *trees, int *path);
+
+/* remove_arg_thread_path (thread.cpp:1481-1668, bound at :1705-1709): the ARG cut along a
+ * removal path into subtree/main-tree form (each cut regrafted above the root at `maxtime`,
+ * ntimes + 1 in arg-sample), trees without an SPR merged. Errors: awg_last_error(). */
+void arghmm_remove_arg_thread_path(awg_local_trees *trees, int *removal_path, int maxtime);
+
 /* arghmm_get_nstates (states.cpp:209): states of every column. */
 void arghmm_get_nstates(awg_local_trees *trees, int ntimes, bool internal, int *nstates);
 

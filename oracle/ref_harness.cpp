@@ -34,6 +34,7 @@
 //                                    trees; writes the grown ARG as a problem
 //   samplethread <problem> <seed> <out>
 //   removethread <problem> <out-prefix> <seqid>...
+//   removalpaths <problem> <seed> <node> <pos> <out-prefix>
 //                                    arghmm_sample_thread (sample_thread.cpp:1010-1023)
 //                                    after srand(seed): the last sequence threaded into the
 //                                    trees; writes the grown ARG as a problem
@@ -672,6 +673,40 @@ static int cmd_removethread(const char *in, const char *prefix, int nrm, char **
     return 0;
 }
 
+// After srand(seed): a uniform removal path (sample_arg_removal_path_uniform), a forward
+// path from `node` (sample_arg_removal_path), one through `node` at coordinate `pos`
+// (sample_arg_removal_path2) and the leaf path of leaf 0, as <prefix>.paths (4 x ntrees
+// ints) and the log path count as <prefix>.lntotal; then the ARG cut along the uniform path
+// (remove_arg_thread_path, maxtime ntimes + 1) as <prefix>.cut.prob
+static int cmd_removalpaths(const char *in, int seed, int node, int pos, const char *prefix) {
+    Problem p = read_problem(in);
+    if (p.internal) die("removalpaths: full ARGs only");
+    LocalTrees *trees = make_trees(p);
+    const int B = trees->get_num_trees();
+    vector<int> paths((size_t)4 * B);
+    srand(seed);
+    double lntotal = sample_arg_removal_path_uniform(trees, &paths[0]);
+    sample_arg_removal_path(trees, node, &paths[B]);
+    sample_arg_removal_path(trees, node, pos, &paths[2 * B], .5);
+    sample_arg_removal_leaf_path(trees, 0, &paths[3 * B]);
+    std::string base(prefix);
+    FILE *f = fopen((base + ".paths").c_str(), "wb");
+    if (!f) die("cannot write paths");
+    wr(f, paths.data(), paths.size());
+    fclose(f);
+    f = fopen((base + ".lntotal").c_str(), "wb");
+    if (!f) die("cannot write lntotal");
+    wr(f, &lntotal, 1);
+    fclose(f);
+    remove_arg_thread_path(trees, &paths[0], p.ntimes + 1);
+    Problem q = p;
+    q.internal = 1;
+    trees_to_problem_named(trees, q);
+    write_problem((base + ".cut.prob").c_str(), q);
+    delete trees;
+    return 0;
+}
+
 static int cmd_cut(const char *in, int seed, const char *out) {
     Problem p = read_problem(in);
     if (p.internal) die("cut: input must be a full (external-format) ARG");
@@ -710,6 +745,8 @@ int main(int argc, char **argv) {
     if (cmd == "ingest" && argc == 6)
         return cmd_ingest(argv[2], argv[3], atoi(argv[4]), argv[5]);
     if (cmd == "sim1" && argc == 6) return cmd_sim1(argv[2], argv[3], atoi(argv[4]), argv[5]);
+    if (cmd == "removalpaths" && argc == 7)
+        return cmd_removalpaths(argv[2], atoi(argv[3]), atoi(argv[4]), atoi(argv[5]), argv[6]);
     if (cmd == "cut" && argc == 5) return cmd_cut(argv[2], atoi(argv[3]), argv[4]);
     die("bad arguments");
     return 1;

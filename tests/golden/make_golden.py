@@ -359,6 +359,41 @@ def removethread(tmp):
         print(name, [int(arrays[f"ptrees_{i}"].shape[0]) for i in range(len(ids))])
 
 
+# (fixture, seed, node, position as a fraction of the region) for the removal-path fixtures
+REMOVAL_PATHS = [
+    ("dsmc_k8_s11", 301, 3, 0.5),
+    ("dsmc_k8_s12", 302, 11, 0.03),
+    ("dsmc_k10_T16", 303, 12, 0.45),
+    ("dsmc_k17_missing", 304, 20, 0.75),
+    ("sim1_c20", 305, 9, 0.6),
+    ("single_k7_s41", 306, 2, 0.0),
+    ("extra_k8_T20", 307, 5, 0.9),
+]
+
+
+def removalpaths(tmp):
+    """Removal paths through the grown ARGs after srand(seed) (uniform, forward from a node,
+    through a node at a position, the leaf path of leaf 0; thread.cpp:672-1002) and the ARG
+    cut along the uniform path (remove_arg_thread_path, thread.cpp:1481-1668)."""
+    out_dir = os.path.join(HERE, "removalpaths")
+    os.makedirs(out_dir, exist_ok=True)
+    for name, seed, node, frac in REMOVAL_PATHS:
+        pp = os.path.join(HERE, "addthread", name + ".prob")
+        prob = Problem.load(pp)
+        off = int(frac * int(np.sum(prob.blocklens)))
+        prefix = os.path.join(tmp, name)
+        run("removalpaths", pp, seed, node, prob.start_coord + off, prefix)
+        paths = np.fromfile(prefix + ".paths", dtype=np.int32).reshape(4, prob.ntrees)
+        cut = Problem.load(prefix + ".cut.prob")
+        np.savez_compressed(
+            os.path.join(out_dir, name + ".npz"), seed=seed, node=node,
+            pos=prob.start_coord + off, paths=paths,
+            lntotal=np.fromfile(prefix + ".lntotal", dtype=np.float64)[0],
+            ptrees=cut.ptrees, ages=cut.ages, sprs=cut.sprs, blocklens=cut.blocklens,
+            mapping=cut.mapping, root_child0=cut.root_child0)
+        print(name, prob.ntrees, "->", cut.ntrees)
+
+
 def infsites(tmp):
     """The infinite-sites penalty (ArgModel::infsites_penalty, emit.cpp:847-862; arg-sample
     --infsites uses 1e-100): external, with missing calls, and an internal-branch cut."""
@@ -382,6 +417,10 @@ def main():
     if sys.argv[1:] == ["infsites"]:
         with tempfile.TemporaryDirectory() as tmp:
             infsites(tmp)
+        return
+    if sys.argv[1:] == ["removalpaths"]:
+        with tempfile.TemporaryDirectory() as tmp:
+            removalpaths(tmp)
         return
     if sys.argv[1:] == ["removethread"]:
         with tempfile.TemporaryDirectory() as tmp:

@@ -821,4 +821,213 @@ bool remove_thread_path(ThreadTrees &a, const int *removal_path, int maxtime,
     return true;
 }
 
+namespace {
+
+struct NodeTime {
+    int node, time;
+};
+
+// The coalescence states of a tree in subtree/main-tree form, in the reference's order
+// (get_coal_states_internal, states.cpp:109-155): none for a whole tree; else every main-tree
+// branch from max(age, minage, subtree age) up to its parent's age, the basal branches up
+// to ntimes - 2.
+void internal_states(const Tree &t, int T, int minage, std::vector<NodeTime> &st) {
+    st.clear();
+    const int n = (int)t.nd.size();
+    if (t.nd[t.root].age < T) return;
+    const int sub = t.nd[t.root].c0;
+    minage = std::max(minage, t.nd[sub].age);
+    std::vector<char> skip(n, 0);
+    skip[t.root] = 1;
+    std::vector<int> stack{sub};
+    while (!stack.empty()) {
+        const int v = stack.back();
+        stack.pop_back();
+        skip[v] = 1;
+        if (t.nd[v].c0 != -1) {
+            stack.push_back(t.nd[v].c0);
+            stack.push_back(t.nd[v].c1);
+        }
+    }
+    for (int i = 0; i < n; i++) {
+        if (skip[i]) continue;
+        const int parent = t.nd[i].parent;
+        const int top = parent == t.root ? T - 2 : t.nd[parent].age;
+        for (int time = std::max(t.nd[i].age, minage); time <= top; time++)
+            st.push_back(NodeTime{i, time});
+    }
+}
+
+// add_spr_branch for an internal branch (thread.cpp:1204-1311): the SPR into `t` and its
+// mapping renamed for the regrafted subtree's new coalescence node
+bool add_spr_branch_internal(const Tree &t, const Tree &last, NodeTime state, NodeTime last_state,
+                             int *spr, std::vector<int> &mapping, int sub, int last_sub) {
+    const int n = (int)t.nd.size();
+    auto ok = [n](int v) { return v >= 0 && v < n; };
+    const int last_newcoal = last.nd[last_sub].parent;
+    int newcoal;
+    if (state.node != -1) {
+        newcoal = t.nd[sub].parent;
+    } else if (mapping[last_sub] != -1) {  // a whole tree
+        newcoal = t.nd[mapping[last_sub]].parent;
+    } else {
+        const int sib = sibling(last, spr[0]);
+        if (!ok(sib) || !ok(mapping[sib])) return false;
+        newcoal = t.nd[mapping[sib]].parent;
+    }
+    if (!ok(last_newcoal) || !ok(mapping[spr[0]])) return false;
+    mapping[last_newcoal] = newcoal;
+    const int recoal = t.nd[mapping[spr[0]]].parent;
+    if (recoal == newcoal) {
+        if (mapping[last_state.node] == state.node) {
+            spr[0] = last_newcoal;  // the recombination is above the coalescence: renamed
+        } else if (spr[3] == last.nd[last_newcoal].age && state.node == mapping[spr[0]]) {
+            // a mediated coalescence
+            spr[2] = state.time < last.nd[last_sub].age ? sibling(last, spr[0]) : last_sub;
+            spr[3] = state.time;
+        }  // else the new branch escapes: nothing to rename
+    } else if (recoal != -1 && (t.nd[recoal].c0 == newcoal || t.nd[recoal].c1 == newcoal)) {
+        if (last.nd[spr[2]].parent == last_newcoal) spr[2] = last_newcoal;
+    }
+    if (last.nd[spr[0]].parent == last_newcoal) {  // last_newcoal was the broken node
+        mapping[last_newcoal] = -1;
+        const int p = last.nd[last_newcoal].parent;
+        if (p != -1) mapping[p] = newcoal;
+    } else {  // a child of last_newcoal without the recombination or coalescence on it
+        const int x = last_newcoal;
+        int y = last.nd[x].c0;
+        if (y == spr[2]) y = last.nd[x].c1;
+        if (!ok(y)) return false;
+        if (mapping[y] == -1) y = sibling(last, spr[0]);
+        if (y == spr[2]) y = last.nd[x].c1;
+        if (!ok(y) || !ok(mapping[y])) return false;
+        mapping[last_newcoal] = t.nd[mapping[y]].parent;
+    }
+    return last.nd[spr[0]].parent != -1;
+}
+
+}  // namespace
+
+bool add_thread_path(ThreadTrees &a, int T, int minage, const int *path, int seqlen,
+                     const int *rec_pos, const int *rec_node, const int *rec_time, int nrec,
+                     std::string &err) {
+    std::vector<Tree> in;
+    std::vector<std::vector<int>> maps;
+    std::vector<Spr4> sprs;
+    if (!load_trees(a, in, maps, sprs, "add_arg_thread_path", err)) return false;
+    const int n = a.nnodes, B = a.ntrees;
+    long long total = 0;
+    for (int b = 0; b < B; b++) total += a.blocklens[b];
+    if (total != seqlen) {
+        err = "add_arg_thread_path: the path does not cover the trees";
+        return false;
+    }
+    for (int r = 0; r < nrec; r++)
+        if (rec_pos[r] <= 0 || rec_pos[r] >= seqlen || (r > 0 && rec_pos[r] <= rec_pos[r - 1])) {
+            err = "add_arg_thread_path: recombination columns must increase within the region";
+            return false;
+        }
+    ThreadTrees out;
+    out.nnodes = n;
+    out.start_coord = a.start_coord;
+    out.seqids = a.seqids;
+    auto push = [&](const Tree &t, const int *spr, int blocklen, const std::vector<int> *mp) {
+        for (int i = 0; i < n; i++) {
+            out.ptrees.push_back(t.nd[i].parent);
+            out.ages.push_back(t.nd[i].age);
+            out.c0.push_back(t.nd[i].c0);
+            out.c1.push_back(t.nd[i].c1);
+            out.mapping.push_back(mp ? (*mp)[i] : -1);
+        }
+        for (int k = 0; k < 4; k++) out.sprs.push_back(spr[k]);
+        out.blocklens.push_back(blocklen);
+        out.ntrees++;
+    };
+    std::vector<NodeTime> states;
+    auto state_at = [&](int col, NodeTime &s) {
+        const int k = path[col];
+        if (k < 0 || k >= (int)states.size()) return false;
+        s = states[k];
+        return true;
+    };
+    Tree last_tree;
+    NodeTime last_state{0, 0};  // State() (states.h): node 0 until the first tree is seen
+    int last_sub = -1, irec = 0, end = 0;
+    for (int b = 0; b < B; b++) {
+        Tree tree = in[b];
+        int start = end;
+        end += a.blocklens[b];
+        const int sub = tree.nd[tree.root].c0;
+        internal_states(in[b], T, minage, states);
+        NodeTime state{-1, -1};
+        if (tree.nd[tree.root].age > T) {  // a partial tree: regraft the subtree at the state
+            if (sub < 0 || !state_at(start, state)) {
+                err = "add_arg_thread_path: a path entry is not a state of its tree";
+                return false;
+            }
+            const int graft[4] = {sub, tree.nd[sub].age, state.node, state.time};
+            apply_spr(tree, graft);
+        }
+        int spr[4] = {sprs[b].v[0], sprs[b].v[1], sprs[b].v[2], sprs[b].v[3]};
+        std::vector<int> mapping = maps[b];
+        const bool has_map = b > 0;
+        if (has_map && last_state.node != -1 &&
+            !add_spr_branch_internal(tree, last_tree, state, last_state, spr, mapping, sub,
+                                     last_sub)) {
+            err = "add_arg_thread_path: inconsistent SPR between neighbouring trees";
+            return false;
+        }
+        // split the block at each of its recombinations
+        Tree cur = tree;
+        int cur_spr[4] = {spr[0], spr[1], spr[2], spr[3]};
+        std::vector<int> cur_map = mapping;
+        bool cur_has_map = has_map;
+        for (; irec < nrec && rec_pos[irec] < end; irec++) {
+            const int pos = rec_pos[irec];
+            if (!state_at(pos, state) || !state_at(pos - 1, last_state)) {
+                err = "add_arg_thread_path: a path entry is not a state of its tree";
+                return false;
+            }
+            const int newcoal = cur.nd[sub].parent;
+            int spr2[4] = {rec_node[irec], rec_time[irec], -1, state.time};
+            if (spr2[0] < 0 || spr2[0] >= n) {
+                err = "add_arg_thread_path: a recombination node out of range";
+                return false;
+            }
+            if (spr2[0] == sub) {  // on the regrafted branch: coalescence as the thread
+                spr2[2] = state.node == last_state.node && state.time > last_state.time
+                              ? newcoal : state.node;
+            } else {  // in the main tree: coalescence on the regrafted branch
+                spr2[2] = state.time > last_state.time ? cur.nd[sub].parent : sub;
+            }
+            const int broken = cur.nd[spr2[0]].parent;
+            if (broken < 0) {
+                err = "add_arg_thread_path: a recombination on the root";
+                return false;
+            }
+            std::vector<int> map2(n);
+            for (int j = 0; j < n; j++) map2[j] = j;
+            map2[broken] = -1;
+            Tree nt = cur;
+            apply_spr(nt, spr2);
+            push(cur, cur_spr, pos - start, cur_has_map ? &cur_map : nullptr);
+            cur = std::move(nt);
+            for (int k = 0; k < 4; k++) cur_spr[k] = spr2[k];
+            cur_map = std::move(map2);
+            cur_has_map = true;
+            start = pos;
+        }
+        push(cur, cur_spr, end - start, cur_has_map ? &cur_map : nullptr);
+        last_tree = std::move(cur);
+        last_state = state;
+        last_sub = sub;
+    }
+    if (irec != nrec) {
+        err = "add_arg_thread_path: a recombination outside the trees";
+        return false;
+    }
+    a = std::move(out);
+    return true;
+}
+
 }  // namespace awg

@@ -47,4 +47,12 @@ bool sample_removal_path_uniform(const ThreadTrees &a, int (*rnd)(), int *path, 
 // root's first child), SPRs and mappings follow, trees left without an SPR merge.
 bool remove_thread_path(ThreadTrees &a, const int *removal_path, int maxtime, std::string &err);
 
+// Regrafts the cut subtree of every partial tree (add_arg_thread_path, thread.cpp:1314-1449)
+// at the state its internal thread path takes at the tree's first column (internal states,
+// states.cpp:109-155, with minage), splits trees at the sampled recombinations, and renames
+// the SPRs and mappings between neighbouring trees (thread.cpp:1204-1311). Node count stays.
+bool add_thread_path(ThreadTrees &a, int T, int minage, const int *path, int seqlen,
+                     const int *rec_pos, const int *rec_node, const int *rec_time, int nrec,
+                     std::string &err);
+
 }  // namespace awg

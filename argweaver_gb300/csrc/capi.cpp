@@ -39,6 +39,7 @@ void set_error(const std::string &msg) {
 struct ProblemView {
     awg_problem p;
     std::vector<char> seqs;
+    std::vector<int> root_child0;
 };
 
 // The leaf names the reference's exports show (get_local_trees_ptrees, local_tree.cpp:
@@ -91,6 +92,14 @@ bool make_view(const awg_local_trees *t, double *times, int ntimes, double *pops
     p.blocklens = t->blocklens.data();
     p.mapping = t->mapping.empty() ? nullptr : t->mapping.data();
     p.root_child0 = nullptr;
+    if (internal && !t->c0.empty()) {  // each root's child[0] is the cut subtree
+        const int n = t->nnodes;
+        v.root_child0.assign(t->ntrees, -1);
+        for (int b = 0; b < t->ntrees; b++)
+            for (int i = 0; i < n; i++)
+                if (t->ptrees[(size_t)b * n + i] == -1) v.root_child0[b] = t->c0[(size_t)b * n + i];
+        p.root_child0 = v.root_child0.data();
+    }
     p.times = times; p.popsizes = popsizes; p.rho = rho; p.mu = mu;
     p.seqs = v.seqs.data();
     return true;
@@ -486,6 +495,26 @@ static void store_trees(awg_local_trees *t, awg::ThreadTrees &a) {
     t->c0 = std::move(a.c0); t->c1 = std::move(a.c1); t->seqids = std::move(a.seqids);
 }
 
+int awg_add_arg_thread_path(awg_local_trees *trees, int ntimes, int minage, const int *path,
+                            int seqlen, const int *rec_pos, const int *rec_node,
+                            const int *rec_time, int nrec) {
+    g_err.clear();
+    if (!trees || !path || nrec < 0 || (nrec > 0 && (!rec_pos || !rec_node || !rec_time)) ||
+        ntimes < 3 || minage < 0) {
+        set_error("awg_add_arg_thread_path: bad arguments");
+        return -1;
+    }
+    awg::ThreadTrees a = thread_trees(trees);
+    std::string err;
+    if (!awg::add_thread_path(a, ntimes, minage, path, seqlen, rec_pos, rec_node, rec_time, nrec,
+                              err)) {
+        set_error(err);
+        return -1;
+    }
+    store_trees(trees, a);
+    return 0;
+}
+
 // Removal paths and the internal-branch cut (thread.cpp:1681-1716). Paths hold one node
 // per tree in the trees' own node names; draws come from libc rand(), as the reference's.
 void arghmm_sample_arg_removal_path(awg_local_trees *trees, int node, int *path) {
@@ -700,6 +729,51 @@ awg_local_trees *arghmm_sample_thread(awg_local_trees *trees, double *times, int
                            time.data(), nrec) == 0 && !trees->seqids.empty())
         trees->seqids.back() = nseqs - 1;  // the new leaf holds new_chrom (thread.cpp:292)
     return trees;
+}
+
+// sample_arg_thread_internal (sample_thread.cpp:635-692): the cut subtree of an internal
+// problem re-threaded in place: forward and traceback on the device (draws from rand(), last
+// column first), recombinations along the thread on the device (2 * seqlen + 2 draws taken up
+// front, as in arghmm_sample_thread), then the regraft on the host. The path goes to
+// thread_path when given. 0, or -1 (awg_last_error).
+int awg_sample_arg_thread_internal(awg_local_trees *trees, double *times, int ntimes,
+                                   double *popsizes, double rho, double mu, char **seqs,
+                                   int nseqs, int seqlen, int minage, int *thread_path) {
+    g_err.clear();
+    if (!trees || minage < 0) {
+        set_error("awg_sample_arg_thread_internal: bad arguments");
+        return -1;
+    }
+    ProblemView v;
+    if (!make_view(trees, times, ntimes, popsizes, rho, mu, seqs, nseqs, seqlen, true, v))
+        return -1;
+    v.p.minage = minage;
+    std::vector<int> path(seqlen);
+    awg_outputs o;
+    memset(&o, 0, sizeof(o));
+    o.path = path.data();
+    awg::RunOptions opt;
+    std::string err;
+    if (awg::run_batch(&v.p, &o, 1, opt, err) != 0) {
+        set_error(err);
+        return -1;
+    }
+    const int nu = 2 * seqlen + 2;
+    std::vector<double> u(nu);
+    for (double &x : u) x = rand() / double(RAND_MAX);  // frand (common.h:103-110)
+    std::vector<int> pos(seqlen), node(seqlen), time(seqlen);
+    int used = 0;
+    const int nrec = awg::sample_recombinations(&v.p, path.data(), u.data(), nu, pos.data(),
+                                                node.data(), time.data(), seqlen, &used, err);
+    if (nrec < 0) {
+        set_error(err);
+        return -1;
+    }
+    if (awg_add_arg_thread_path(trees, ntimes, minage, path.data(), seqlen, pos.data(),
+                                node.data(), time.data(), nrec) != 0)
+        return -1;
+    if (thread_path) memcpy(thread_path, path.data(), sizeof(int) * seqlen);
+    return 0;
 }
 
 void delete_path(int *path) { delete[] path; }

@@ -432,6 +432,46 @@ def remove_arg_thread_path(prob: Problem, path, maxtime: int | None = None) -> d
     return _with_trees(prob, run)
 
 
+def add_arg_thread_path(prob: Problem, path, rec_pos, rec_node, rec_time,
+                        minage: int | None = None) -> dict:  # ArgModel minage, 0 by default
+    """The internal problem's cut subtree regrafted along its thread path with the path's
+    recombinations (add_arg_thread_path, thread.cpp:1314-1449), on the host: the whole ARG
+    as a dict (ptrees, ages, sprs, blocklens, mapping, root_child0, seqids)."""
+    def run(lib, trees, p):
+        if not p.internal:
+            raise ValueError("add_arg_thread_path: internal problems only")
+        i32 = lambda a: np.ascontiguousarray(a, dtype=np.int32)
+        pa, rp, rn, rt = i32(path), i32(rec_pos), i32(rec_node), i32(rec_time)
+        ptr = lambda a: a.ctypes.data_as(capi.c_int_p)
+        rc = lib.awg_add_arg_thread_path(trees.handle, p.ntimes,
+                                         0 if minage is None else int(minage), ptr(pa),
+                                         len(pa), ptr(rp), ptr(rn), ptr(rt), len(rp))
+        if rc != 0:
+            raise ValueError(capi.last_error())
+        return _tree_dict(trees)
+    return _with_trees(prob, run)
+
+
+def sample_arg_thread_internal(prob: Problem, minage: int = 0):
+    """The internal problem's cut subtree re-threaded (sample_arg_thread_internal,
+    sample_thread.cpp:635-692): forward, traceback and recombinations on the device with draws
+    from libc rand() (seed it with srand), the regraft on the host. Returns (the whole ARG as
+    a dict, the thread path)."""
+    def run(lib, trees, p):
+        if not p.internal:
+            raise ValueError("sample_arg_thread_internal: internal problems only")
+        seqs, _keep = _char_pp(p.seqs)
+        path = np.zeros(p.seqlen, dtype=np.int32)
+        rc = lib.awg_sample_arg_thread_internal(
+            trees.handle, p.times.ctypes.data_as(capi.c_double_p), p.ntimes,
+            p.popsizes.ctypes.data_as(capi.c_double_p), p.rho, p.mu, seqs, p.nseqs, p.seqlen,
+            int(minage), path.ctypes.data_as(capi.c_int_p))
+        if rc != 0:
+            raise RuntimeError(capi.last_error())
+        return _tree_dict(trees), path
+    return _with_trees(prob, run)
+
+
 def arghmm_sample_thread(prob: Problem) -> Problem:
     """The problem's ARG with its last sequence threaded in (draws from libc rand(): seed it
     with srand). The result is a full ARG over all the problem's sequences."""

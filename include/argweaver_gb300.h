@@ -107,6 +107,23 @@ double awg_sample_arg_removal_path_uniform(awg_local_trees *trees, int *path);
  * ntimes + 1 in arg-sample), trees without an SPR merged. Errors: awg_last_error(). */
 void arghmm_remove_arg_thread_path(awg_local_trees *trees, int *removal_path, int maxtime);
 
+/* add_arg_thread_path (thread.cpp:1314-1449), on the host: every partial tree's cut subtree
+ * regrafted at the state its internal thread path (internal states with `minage`; e.g. from
+ * arghmm_sample_arg_thread_internal) takes at the tree's first column, the trees split at
+ * the path's recombinations (columns, nodes, times; e.g. from awg_sample_recombinations on
+ * the internal problem). 0, or -1 (awg_last_error). */
+int awg_add_arg_thread_path(awg_local_trees *trees, int ntimes, int minage, const int *path,
+                            int seqlen, const int *rec_pos, const int *rec_node,
+                            const int *rec_time, int nrec);
+
+/* sample_arg_thread_internal (sample_thread.cpp:635-692): the cut subtree of trees in
+ * subtree/main-tree form re-threaded in place, forward, traceback and recombinations on the
+ * device (draws from libc rand()), the regraft on the host; the thread path into thread_path
+ * (seqlen ints) when not NULL. 0, or -1 (awg_last_error). */
+int awg_sample_arg_thread_internal(awg_local_trees *trees, double *times, int ntimes,
+                                   double *popsizes, double rho, double mu, char **seqs,
+                                   int nseqs, int seqlen, int minage, int *thread_path);
+
 /* arghmm_get_nstates (states.cpp:209): states of every column. */
 void arghmm_get_nstates(awg_local_trees *trees, int ntimes, bool internal, int *nstates);
 

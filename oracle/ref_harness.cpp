@@ -34,6 +34,8 @@
 //                                    trees; writes the grown ARG as a problem
 //   samplethread <problem> <seed> <out>
 //   removethread <problem> <out-prefix> <seqid>...
+//   addthreadpath <internal problem> <path> <recombs> <out>
+//   samplethreadinternal <internal problem> <seed> <out>
 //   removalpaths <problem> <seed> <node> <pos> <out-prefix>
 //                                    arghmm_sample_thread (sample_thread.cpp:1010-1023)
 //                                    after srand(seed): the last sequence threaded into the
@@ -619,6 +621,57 @@ static int cmd_addthread(const char *in, const char *path_file, const char *rec_
     return 0;
 }
 
+// add_arg_thread_path (thread.cpp:1314-1449): an internal problem's thread path and its
+// recombinations (pos, node, time triples) regrafted into the cut ARG
+static int cmd_addthreadpath(const char *in, const char *path_file, const char *rec_file,
+                             const char *out) {
+    Problem p = read_problem(in);
+    if (!p.internal) die("addthreadpath: internal problems only");
+    LocalTrees *trees = make_trees(p);
+    vector<int> path(p.seqlen);
+    FILE *pf = fopen(path_file, "rb");
+    if (!pf) die("cannot read path");
+    rd(pf, path.data(), p.seqlen);
+    fclose(pf);
+    FILE *rf = fopen(rec_file, "rb");
+    if (!rf) die("cannot read recombinations");
+    vector<int> pos;
+    vector<NodePoint> recombs;
+    int v[3];
+    while (fread(v, sizeof(int), 3, rf) == 3) {
+        pos.push_back(v[0] + trees->start_coord);
+        recombs.push_back(NodePoint(v[1], v[2]));
+    }
+    fclose(rf);
+    StatesModel states_model(p.ntimes, true, 0);
+    add_arg_thread_path(trees, states_model, p.ntimes, path.data() - trees->start_coord, pos,
+                        recombs);
+    Problem q = p;
+    q.internal = 0;
+    trees_to_problem(trees, q);
+    write_problem(out, q);
+    delete trees;
+    return 0;
+}
+
+// sample_arg_thread_internal (sample_thread.cpp:635-692) after srand(seed): the whole ARG
+static int cmd_samplethreadinternal(const char *in, int seed, const char *out) {
+    Problem p = read_problem(in);
+    if (!p.internal) die("samplethreadinternal: internal problems only");
+    LocalTrees *trees = make_trees(p);
+    vector<char *> sp = seq_ptrs(p);
+    ArgModel model(p.ntimes, p.times.data(), p.popsizes.data(), p.rho, p.mu);
+    Sequences sequences(sp.data(), p.nseqs, p.seqlen);
+    srand(seed);
+    sample_arg_thread_internal(&model, &sequences, trees, 0, NULL);
+    Problem q = p;
+    q.internal = 0;
+    trees_to_problem(trees, q);
+    write_problem(out, q);
+    delete trees;
+    return 0;
+}
+
 static int cmd_samplethread(const char *in, int seed, const char *out) {
     Problem p = read_problem(in);
     if (p.internal) die("samplethread: external problems only");
@@ -738,6 +791,10 @@ int main(int argc, char **argv) {
         return cmd_samplethread(argv[2], atoi(argv[3]), argv[4]);
     if (cmd == "removethread" && argc >= 5)
         return cmd_removethread(argv[2], argv[3], argc - 4, argv + 4);
+    if (cmd == "addthreadpath" && argc == 6)
+        return cmd_addthreadpath(argv[2], argv[3], argv[4], argv[5]);
+    if (cmd == "samplethreadinternal" && argc == 5)
+        return cmd_samplethreadinternal(argv[2], atoi(argv[3]), argv[4]);
     if (cmd == "addthread" && argc == 6)
         return cmd_addthread(argv[2], argv[3], argv[4], argv[5]);
     if (cmd == "recomb" && argc == 6)

@@ -310,6 +310,52 @@ def addthread(tmp):
         print(name, len(rec["pos"]))
 
 
+def addthreadpath(tmp):
+    """add_arg_thread_path (thread.cpp:1314-1449): the internal fixtures' thread paths and
+    recombinations regrafted into their cut ARGs by the reference; the whole ARG."""
+    out_dir = os.path.join(HERE, "addthreadpath")
+    os.makedirs(out_dir, exist_ok=True)
+    rdir = os.path.join(HERE, "recomb")
+    for f in sorted(os.listdir(rdir)):
+        if not f.endswith(".npz") or f.startswith("extra_"):
+            continue
+        name = f[:-4]
+        pp = os.path.join(HERE, name + ".prob")
+        if not Problem.load(pp).internal:
+            continue
+        rec = np.load(os.path.join(rdir, f))
+        path = np.load(os.path.join(HERE, name + ".npz"))["path"]
+        path_file = os.path.join(tmp, "path.bin")
+        np.ascontiguousarray(path, dtype=np.int32).tofile(path_file)
+        rec_file = os.path.join(tmp, "rec.bin")
+        np.ascontiguousarray(np.stack([rec["pos"], rec["node"], rec["time"]], axis=1),
+                             dtype=np.int32).tofile(rec_file)
+        out = os.path.join(tmp, name + ".prob")
+        run("addthreadpath", pp, path_file, rec_file, out)
+        q = Problem.load(out)
+        np.savez_compressed(os.path.join(out_dir, name + ".npz"), ptrees=q.ptrees, ages=q.ages,
+                            sprs=q.sprs, blocklens=q.blocklens, mapping=q.mapping,
+                            root_child0=q.root_child0)
+        print(name, len(rec["pos"]), q.ntrees)
+
+
+def samplethreadinternal(tmp):
+    """sample_arg_thread_internal (sample_thread.cpp:635-692) after srand(seed + 9100) on the
+    internal fixtures: the whole ARG with the cut subtree re-threaded, as the reference does."""
+    out_dir = os.path.join(HERE, "samplethreadinternal")
+    os.makedirs(out_dir, exist_ok=True)
+    for name in ("cut_k10_s3", "cut_k10_s8", "cut_k10_s17", "cut_k10_s24", "infsites_cut_k10_s5"):
+        pp = os.path.join(HERE, name + ".prob")
+        seed = int(np.load(os.path.join(HERE, name + ".npz"))["seed"]) + 9100
+        out = os.path.join(tmp, name + ".prob")
+        run("samplethreadinternal", pp, seed, out)
+        q = Problem.load(out)
+        np.savez_compressed(os.path.join(out_dir, name + ".npz"), seed=seed, ptrees=q.ptrees,
+                            ages=q.ages, sprs=q.sprs, blocklens=q.blocklens, mapping=q.mapping,
+                            root_child0=q.root_child0)
+        print(name, q.ntrees)
+
+
 def samplethread(tmp):
     """arghmm_sample_thread (sample_thread.cpp:1010-1023) after srand(seed + 9000) on the
     external fixtures: the ARG with the last sequence threaded in, as the reference grows it."""
@@ -417,6 +463,14 @@ def main():
     if sys.argv[1:] == ["infsites"]:
         with tempfile.TemporaryDirectory() as tmp:
             infsites(tmp)
+        return
+    if sys.argv[1:] == ["samplethreadinternal"]:
+        with tempfile.TemporaryDirectory() as tmp:
+            samplethreadinternal(tmp)
+        return
+    if sys.argv[1:] == ["addthreadpath"]:
+        with tempfile.TemporaryDirectory() as tmp:
+            addthreadpath(tmp)
         return
     if sys.argv[1:] == ["removalpaths"]:
         with tempfile.TemporaryDirectory() as tmp:

@@ -757,8 +757,47 @@ bool sample_removal_path_uniform(const ThreadTrees &a, int (*rnd)(), int *path, 
     if (lntotal) *lntotal = log_sum(last, n);
     return true;
 }
+namespace {
+
+struct NodeTime {
+    int node, time;
+};
+
+// The coalescence states of a tree in subtree/main-tree form, in the reference's order
+// (get_coal_states_internal, states.cpp:109-155): none for a whole tree; else every main-tree
+// branch from max(age, minage, subtree age) up to its parent's age, the basal branches up
+// to ntimes - 2.
+void internal_states(const Tree &t, int T, int minage, std::vector<NodeTime> &st) {
+    st.clear();
+    const int n = (int)t.nd.size();
+    if (t.nd[t.root].age < T) return;
+    const int sub = t.nd[t.root].c0;
+    minage = std::max(minage, t.nd[sub].age);
+    std::vector<char> skip(n, 0);
+    skip[t.root] = 1;
+    std::vector<int> stack{sub};
+    while (!stack.empty()) {
+        const int v = stack.back();
+        stack.pop_back();
+        skip[v] = 1;
+        if (t.nd[v].c0 != -1) {
+            stack.push_back(t.nd[v].c0);
+            stack.push_back(t.nd[v].c1);
+        }
+    }
+    for (int i = 0; i < n; i++) {
+        if (skip[i]) continue;
+        const int parent = t.nd[i].parent;
+        const int top = parent == t.root ? T - 2 : t.nd[parent].age;
+        for (int time = std::max(t.nd[i].age, minage); time <= top; time++)
+            st.push_back(NodeTime{i, time});
+    }
+}
+
+}  // namespace
+
 bool remove_thread_path(ThreadTrees &a, const int *removal_path, int maxtime,
-                        std::string &err) {
+                        int *original_thread, std::string &err) {
     std::vector<Tree> trees;
     std::vector<std::vector<int>> maps;
     std::vector<Spr4> sprs;
@@ -769,6 +808,7 @@ bool remove_thread_path(ThreadTrees &a, const int *removal_path, int maxtime,
             err = "remove_arg_thread_path: a path node out of range";
             return false;
         }
+    std::vector<NodeTime> orig(B, NodeTime{-1, -1});  // the removed thread, per tree
     for (int b = 0; b < B; b++) {
         Tree &t = trees[b];
         const Tree *last = b > 0 ? &trees[b - 1] : nullptr;
@@ -777,6 +817,7 @@ bool remove_thread_path(ThreadTrees &a, const int *removal_path, int maxtime,
             if (last && removal_path[b - 1] != last->root) maps[b][last->root] = -1;
             continue;
         }
+        orig[b] = NodeTime{sibling(t, rn), t.nd[t.nd[rn].parent].age};
         // cut the branch above rn and regraft it over the root at maxtime: the tree in
         // subtree/main-tree form, the subtree the root's first child
         const int broken = t.nd[rn].parent;
@@ -817,46 +858,39 @@ bool remove_thread_path(ThreadTrees &a, const int *removal_path, int maxtime,
         }
         m[spr_broken] = -1;
     }
+    if (original_thread) {  // the removed thread as states of the cut trees (thread.cpp:1638-1665)
+        std::vector<NodeTime> states;
+        std::vector<int> nodes(n);
+        int col = 0;
+        for (int b = 0; b < B; b++) {
+            // get_actual_nodes (thread.cpp:1452-1477): names in the last tree the merge keeps;
+            // the mapping test reads mapping[i], as the reference's does
+            for (int i = 0; i < n; i++) nodes[i] = i;
+            int b2 = b + 1;
+            for (; b2 < B && sprs[b2].v[0] == -1; b2++)
+                for (int i = 0; i < n; i++)
+                    nodes[i] = maps[b2][i] != -1 && nodes[i] != -1 ? maps[b2][nodes[i]] : -1;
+            internal_states(trees[b2 - 1], maxtime - 1, 0, states);
+            int k = 0;
+            if (!states.empty()) {
+                const NodeTime o = orig[b];
+                const int node = o.node >= 0 ? nodes[o.node] : -1;
+                k = -1;
+                for (int j = 0; j < (int)states.size() && k < 0; j++)
+                    if (states[j].node == node && states[j].time == o.time) k = j;
+                if (k < 0) {
+                    err = "remove_arg_thread_path: the removed thread is no state of its tree";
+                    return false;
+                }
+            }
+            for (int c = 0; c < a.blocklens[b]; c++) original_thread[col++] = k;
+        }
+    }
     a = merge_null_sprs(trees, maps, sprs, a.blocklens, n, a.start_coord, a.seqids);
     return true;
 }
 
 namespace {
-
-struct NodeTime {
-    int node, time;
-};
-
-// The coalescence states of a tree in subtree/main-tree form, in the reference's order
-// (get_coal_states_internal, states.cpp:109-155): none for a whole tree; else every main-tree
-// branch from max(age, minage, subtree age) up to its parent's age, the basal branches up
-// to ntimes - 2.
-void internal_states(const Tree &t, int T, int minage, std::vector<NodeTime> &st) {
-    st.clear();
-    const int n = (int)t.nd.size();
-    if (t.nd[t.root].age < T) return;
-    const int sub = t.nd[t.root].c0;
-    minage = std::max(minage, t.nd[sub].age);
-    std::vector<char> skip(n, 0);
-    skip[t.root] = 1;
-    std::vector<int> stack{sub};
-    while (!stack.empty()) {
-        const int v = stack.back();
-        stack.pop_back();
-        skip[v] = 1;
-        if (t.nd[v].c0 != -1) {
-            stack.push_back(t.nd[v].c0);
-            stack.push_back(t.nd[v].c1);
-        }
-    }
-    for (int i = 0; i < n; i++) {
-        if (skip[i]) continue;
-        const int parent = t.nd[i].parent;
-        const int top = parent == t.root ? T - 2 : t.nd[parent].age;
-        for (int time = std::max(t.nd[i].age, minage); time <= top; time++)
-            st.push_back(NodeTime{i, time});
-    }
-}
 
 // add_spr_branch for an internal branch (thread.cpp:1204-1311): the SPR into `t` and its
 // mapping renamed for the regrafted subtree's new coalescence node

@@ -44,8 +44,11 @@ bool sample_removal_path_uniform(const ThreadTrees &a, int (*rnd)(), int *path, 
 
 // Cuts the ARG along a removal path (remove_arg_thread_path, thread.cpp:1481-1668): in every
 // tree the path's branch is pruned and regrafted above the root at maxtime (the subtree the
-// root's first child), SPRs and mappings follow, trees left without an SPR merge.
-bool remove_thread_path(ThreadTrees &a, const int *removal_path, int maxtime, std::string &err);
+// root's first child), SPRs and mappings follow, trees left without an SPR merge. With
+// original_thread (one int per column), the removed thread as state indices of the cut trees
+// (internal states with ntimes = maxtime - 1; 0 where a tree has none).
+bool remove_thread_path(ThreadTrees &a, const int *removal_path, int maxtime,
+                        int *original_thread, std::string &err);
 
 // Regrafts the cut subtree of every partial tree (add_arg_thread_path, thread.cpp:1314-1449)
 // at the state its internal thread path takes at the tree's first column (internal states,

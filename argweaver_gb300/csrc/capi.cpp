@@ -559,7 +559,20 @@ void arghmm_remove_arg_thread_path(awg_local_trees *trees, int *removal_path, in
     }
     awg::ThreadTrees a = thread_trees(trees);
     std::string err;
-    if (!awg::remove_thread_path(a, removal_path, maxtime, err)) set_error(err);
+    if (!awg::remove_thread_path(a, removal_path, maxtime, nullptr, err)) set_error(err);
+    else store_trees(trees, a);
+}
+
+void arghmm_remove_arg_thread_path2(awg_local_trees *trees, int *removal_path, int maxtime,
+                                    int *original_thread) {
+    g_err.clear();
+    if (!trees || !removal_path || !original_thread) {
+        set_error("arghmm_remove_arg_thread_path2: NULL argument");
+        return;
+    }
+    awg::ThreadTrees a = thread_trees(trees);
+    std::string err;
+    if (!awg::remove_thread_path(a, removal_path, maxtime, original_thread, err)) set_error(err);
     else store_trees(trees, a);
 }
 

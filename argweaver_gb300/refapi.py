@@ -415,20 +415,31 @@ def sample_arg_removal_path_uniform(prob: Problem):
     return _with_trees(prob, run)
 
 
-def remove_arg_thread_path(prob: Problem, path, maxtime: int | None = None) -> dict:
+def remove_arg_thread_path(prob: Problem, path, maxtime: int | None = None,
+                           original_thread: bool = False) -> dict:
     """The problem's ARG cut along a removal path (remove_arg_thread_path, thread.cpp:1481-1668;
     maxtime defaults to ntimes + 1 as arg-sample passes): the trees in subtree/main-tree form
-    as a dict (ptrees, ages, sprs, blocklens, mapping, root_child0, seqids)."""
+    as a dict (ptrees, ages, sprs, blocklens, mapping, root_child0, seqids), with
+    original_thread=True also the removed thread as state indices of the cut trees
+    (arghmm_remove_arg_thread_path2)."""
     def run(lib, trees, p):
         rp = np.ascontiguousarray(path, dtype=np.int32)
         if rp.shape != (p.ntrees,):
             raise ValueError("remove_arg_thread_path: the path needs one node per tree")
-        lib.arghmm_remove_arg_thread_path(trees.handle, rp.ctypes.data_as(capi.c_int_p),
-                                          p.ntimes + 1 if maxtime is None else int(maxtime))
+        mt = p.ntimes + 1 if maxtime is None else int(maxtime)
+        orig = np.zeros(p.seqlen, dtype=np.int32)
+        if original_thread:
+            lib.arghmm_remove_arg_thread_path2(trees.handle, rp.ctypes.data_as(capi.c_int_p),
+                                               mt, orig.ctypes.data_as(capi.c_int_p))
+        else:
+            lib.arghmm_remove_arg_thread_path(trees.handle, rp.ctypes.data_as(capi.c_int_p), mt)
         err = capi.last_error()
         if err:
             raise ValueError(err)
-        return _tree_dict(trees)
+        out = _tree_dict(trees)
+        if original_thread:
+            out["original_thread"] = orig
+        return out
     return _with_trees(prob, run)
 
 

@@ -107,6 +107,12 @@ double awg_sample_arg_removal_path_uniform(awg_local_trees *trees, int *path);
  * ntimes + 1 in arg-sample), trees without an SPR merged. Errors: awg_last_error(). */
 void arghmm_remove_arg_thread_path(awg_local_trees *trees, int *removal_path, int maxtime);
 
+/* arghmm_remove_arg_thread_path2 (thread.cpp:1711-1715): the same cut, and the removed
+ * thread as state indices of the cut trees into original_thread (one int per column; 0
+ * where a tree has no states). */
+void arghmm_remove_arg_thread_path2(awg_local_trees *trees, int *removal_path, int maxtime,
+                                    int *original_thread);
+
 /* add_arg_thread_path (thread.cpp:1314-1449), on the host: every partial tree's cut subtree
  * regrafted at the state its internal thread path (internal states with `minage`; e.g. from
  * arghmm_sample_arg_thread_internal) takes at the tree's first column, the trees split at

@@ -730,7 +730,8 @@ static int cmd_removethread(const char *in, const char *prefix, int nrm, char **
 // path from `node` (sample_arg_removal_path), one through `node` at coordinate `pos`
 // (sample_arg_removal_path2) and the leaf path of leaf 0, as <prefix>.paths (4 x ntrees
 // ints) and the log path count as <prefix>.lntotal; then the ARG cut along the uniform path
-// (remove_arg_thread_path, maxtime ntimes + 1) as <prefix>.cut.prob
+// (remove_arg_thread_path, maxtime ntimes + 1) as <prefix>.cut.prob, with the removed thread
+// as states of the cut trees as <prefix>.orig
 static int cmd_removalpaths(const char *in, int seed, int node, int pos, const char *prefix) {
     Problem p = read_problem(in);
     if (p.internal) die("removalpaths: full ARGs only");
@@ -751,7 +752,12 @@ static int cmd_removalpaths(const char *in, int seed, int node, int pos, const c
     if (!f) die("cannot write lntotal");
     wr(f, &lntotal, 1);
     fclose(f);
-    remove_arg_thread_path(trees, &paths[0], p.ntimes + 1);
+    vector<int> orig(p.seqlen);
+    remove_arg_thread_path(trees, &paths[0], p.ntimes + 1, orig.data());
+    f = fopen((base + ".orig").c_str(), "wb");
+    if (!f) die("cannot write the original thread");
+    wr(f, orig.data(), orig.size());
+    fclose(f);
     Problem q = p;
     q.internal = 1;
     trees_to_problem_named(trees, q);

@@ -435,6 +435,7 @@ def removalpaths(tmp):
             os.path.join(out_dir, name + ".npz"), seed=seed, node=node,
             pos=prob.start_coord + off, paths=paths,
             lntotal=np.fromfile(prefix + ".lntotal", dtype=np.float64)[0],
+            original_thread=np.fromfile(prefix + ".orig", dtype=np.int32),
             ptrees=cut.ptrees, ages=cut.ages, sprs=cut.sprs, blocklens=cut.blocklens,
             mapping=cut.mapping, root_child0=cut.root_child0)
         print(name, prob.ntrees, "->", cut.ntrees)

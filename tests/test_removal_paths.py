@@ -2,7 +2,7 @@
 after srand(seed) the uniform path, its log path count, the forward path from a node, the
 path through a node at a position and the leaf path equal the reference's draws, and the ARG
 cut along the uniform path (subtree/main-tree form, merged trees, mappings, root child
-order) equals the reference's."""
+order, the removed thread as states of the cut trees) equals the reference's."""
 
 import os
 
@@ -41,7 +41,8 @@ def test_removal_paths_match_reference(name):
 @pytest.mark.parametrize("name", NAMES)
 def test_cut_matches_reference(name):
     ref = np.load(os.path.join(GOLDEN, "removalpaths", name + ".npz"))
-    got = refapi.remove_arg_thread_path(grown(name), ref["paths"][0])
+    got = refapi.remove_arg_thread_path(grown(name), ref["paths"][0], original_thread=True)
+    np.testing.assert_array_equal(got["original_thread"], ref["original_thread"])
     assert got["ptrees"].shape == ref["ptrees"].shape
     for key in ("ptrees", "ages", "sprs", "blocklens", "root_child0"):
         np.testing.assert_array_equal(got[key], ref[key], err_msg=key)

@@ -96,6 +96,7 @@ PROTOTYPES = [
     ("awg_sample_arg_removal_path_uniform", C.c_double, [C.c_void_p, c_int_p]),
     ("arghmm_remove_arg_thread_path", None, [C.c_void_p, c_int_p, C.c_int]),
     ("arghmm_remove_arg_thread_path2", None, [C.c_void_p, c_int_p, C.c_int, c_int_p]),
+    ("arghmm_get_thread_times", None, [C.c_void_p, C.c_int, c_int_p, c_int_p]),
     ("awg_add_arg_thread_path", C.c_int, [C.c_void_p, C.c_int, C.c_int, c_int_p, C.c_int,
                                           c_int_p, c_int_p, c_int_p, C.c_int]),
     ("awg_sample_arg_thread_internal", C.c_int, [C.c_void_p, c_double_p, C.c_int, c_double_p,

@@ -1064,4 +1064,31 @@ bool add_thread_path(ThreadTrees &a, int T, int minage, const int *path, int seq
     return true;
 }
 
+bool thread_times(const ThreadTrees &a, int T, const int *path, int *path_times,
+                  std::string &err) {
+    std::vector<Tree> trees;
+    std::vector<std::vector<int>> maps;
+    std::vector<Spr4> sprs;
+    if (!load_trees(a, trees, maps, sprs, "arghmm_get_thread_times", err)) return false;
+    std::vector<NodeTime> states;
+    long long end = a.start_coord;
+    for (int b = 0; b < a.ntrees; b++) {
+        const long long start = end;
+        end += a.blocklens[b];
+        internal_states(trees[b], T, 0, states);
+        for (long long i = start; i < end; i++) {
+            if (states.empty()) {  // a whole tree: no thread here (the reference reads past)
+                path_times[i] = -1;
+                continue;
+            }
+            if (path[i] < 0 || path[i] >= (int)states.size()) {
+                err = "arghmm_get_thread_times: a path entry is not a state of its tree";
+                return false;
+            }
+            path_times[i] = states[path[i]].time;
+        }
+    }
+    return true;
+}
+
 }  // namespace awg

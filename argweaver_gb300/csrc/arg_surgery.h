@@ -54,6 +54,12 @@ bool remove_thread_path(ThreadTrees &a, const int *removal_path, int maxtime,
 // at the state its internal thread path takes at the tree's first column (internal states,
 // states.cpp:109-155, with minage), splits trees at the sampled recombinations, and renames
 // the SPRs and mappings between neighbouring trees (thread.cpp:1204-1311). Node count stays.
+// The time of each column's state of an internal thread path (arghmm_get_thread_times,
+// thread.cpp:1718-1733); path and path_times are indexed by coordinate, from start_coord.
+// Columns of a whole tree (no states) get -1.
+bool thread_times(const ThreadTrees &a, int T, const int *path, int *path_times,
+                  std::string &err);
+
 bool add_thread_path(ThreadTrees &a, int T, int minage, const int *path, int seqlen,
                      const int *rec_pos, const int *rec_node, const int *rec_time, int nrec,
                      std::string &err);

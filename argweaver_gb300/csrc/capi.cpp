@@ -495,6 +495,14 @@ static void store_trees(awg_local_trees *t, awg::ThreadTrees &a) {
     t->c0 = std::move(a.c0); t->c1 = std::move(a.c1); t->seqids = std::move(a.seqids);
 }
 
+void arghmm_get_thread_times(awg_local_trees *trees, int ntimes, int *path, int *path_times) {
+    g_err.clear();
+    std::string err;
+    if (!trees || !path || !path_times) set_error("arghmm_get_thread_times: NULL argument");
+    else if (!awg::thread_times(thread_trees(trees), ntimes, path, path_times, err))
+        set_error(err);
+}
+
 int awg_add_arg_thread_path(awg_local_trees *trees, int ntimes, int minage, const int *path,
                             int seqlen, const int *rec_pos, const int *rec_node,
                             const int *rec_time, int nrec) {

@@ -443,6 +443,23 @@ def remove_arg_thread_path(prob: Problem, path, maxtime: int | None = None,
     return _with_trees(prob, run)
 
 
+def get_thread_times(prob: Problem, path) -> np.ndarray:
+    """The time of each column's internal state along the thread path (arghmm_get_thread_times,
+    thread.cpp:1718-1733), indexed by column."""
+    def run(lib, trees, p):
+        off = p.start_coord  # the reference indexes both arrays by coordinate
+        pa = np.zeros(off + p.seqlen, dtype=np.int32)
+        pa[off:] = np.asarray(path, dtype=np.int32)
+        times = np.zeros(off + p.seqlen, dtype=np.int32)
+        lib.arghmm_get_thread_times(trees.handle, p.ntimes, pa.ctypes.data_as(capi.c_int_p),
+                                    times.ctypes.data_as(capi.c_int_p))
+        err = capi.last_error()
+        if err:
+            raise ValueError(err)
+        return times[off:].copy()
+    return _with_trees(prob, run)
+
+
 def add_arg_thread_path(prob: Problem, path, rec_pos, rec_node, rec_time,
                         minage: int | None = None) -> dict:  # ArgModel minage, 0 by default
     """The internal problem's cut subtree regrafted along its thread path with the path's

@@ -113,6 +113,12 @@ void arghmm_remove_arg_thread_path(awg_local_trees *trees, int *removal_path, in
 void arghmm_remove_arg_thread_path2(awg_local_trees *trees, int *removal_path, int maxtime,
                                     int *original_thread);
 
+/* arghmm_get_thread_times (thread.cpp:1718-1733): the time of each column's internal state
+ * along a thread path; like the reference, path and path_times are indexed by coordinate
+ * (start_coord + column). Columns of a whole tree (no states) get -1, where the reference
+ * reads past its empty state list. Errors: awg_last_error(). */
+void arghmm_get_thread_times(awg_local_trees *trees, int ntimes, int *path, int *path_times);
+
 /* add_arg_thread_path (thread.cpp:1314-1449), on the host: every partial tree's cut subtree
  * regrafted at the state its internal thread path (internal states with `minage`; e.g. from
  * arghmm_sample_arg_thread_internal) takes at the tree's first column, the trees split at

@@ -82,6 +82,12 @@
 #include "argweaver/thread.h"
 #include "argweaver/trans.h"
 
+// an export of thread.cpp (:1718) that no header declares
+namespace argweaver {
+extern "C" void arghmm_get_thread_times(LocalTrees *trees, int ntimes, int *path,
+                                        int *path_times);
+}
+
 using namespace argweaver;
 using std::vector;
 
@@ -643,6 +649,20 @@ static int cmd_addthreadpath(const char *in, const char *path_file, const char *
         recombs.push_back(NodePoint(v[1], v[2]));
     }
     fclose(rf);
+    // the path's state times first (arghmm_get_thread_times, indexed by coordinate), when
+    // every tree has states (the reference reads past an empty state list otherwise)
+    bool all_partial = true;
+    for (LocalTrees::iterator it = trees->begin(); it != trees->end(); ++it)
+        all_partial = all_partial && it->tree->nodes[it->tree->root].age >= p.ntimes;
+    if (all_partial) {
+        vector<int> pabs(trees->start_coord + p.seqlen, 0), tabs(trees->start_coord + p.seqlen, 0);
+        std::copy(path.begin(), path.end(), pabs.begin() + trees->start_coord);
+        arghmm_get_thread_times(trees, p.ntimes, pabs.data(), tabs.data());
+        FILE *tf = fopen((std::string(out) + ".times").c_str(), "wb");
+        if (!tf) die("cannot write thread times");
+        wr(tf, tabs.data() + trees->start_coord, p.seqlen);
+        fclose(tf);
+    }
     StatesModel states_model(p.ntimes, true, 0);
     add_arg_thread_path(trees, states_model, p.ntimes, path.data() - trees->start_coord, pos,
                         recombs);

@@ -335,7 +335,9 @@ def addthreadpath(tmp):
         q = Problem.load(out)
         np.savez_compressed(os.path.join(out_dir, name + ".npz"), ptrees=q.ptrees, ages=q.ages,
                             sprs=q.sprs, blocklens=q.blocklens, mapping=q.mapping,
-                            root_child0=q.root_child0)
+                            root_child0=q.root_child0,
+                            thread_times=np.fromfile(out + ".times", dtype=np.int32)
+                            if os.path.exists(out + ".times") else np.zeros(0, np.int32))
         print(name, len(rec["pos"]), q.ntrees)
 
 

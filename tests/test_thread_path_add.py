@@ -30,6 +30,17 @@ def test_add_thread_path_matches_reference(name):
     assert got["ptrees"].shape[0] == prob.ntrees + len(rec["pos"])
 
 
+@pytest.mark.parametrize("name", NAMES)
+def test_thread_times_match_reference(name):
+    prob, gold = load_golden(name)
+    ref = np.load(os.path.join(GOLDEN, "addthreadpath", name + ".npz"))
+    got = refapi.get_thread_times(prob, gold["path"])
+    if len(ref["thread_times"]):  # every tree has states: the reference's times
+        np.testing.assert_array_equal(got, ref["thread_times"])
+    else:  # some tree is whole: -1 on its columns, a state time elsewhere
+        assert np.all(got >= -1) and np.any(got == -1) and np.all(got < prob.ntimes)
+
+
 def test_add_thread_path_rejects_bad_input():
     name = NAMES[0]
     prob, gold = load_golden(name)

@@ -51,6 +51,8 @@ PROTOTYPES = [
     ("delete_local_trees", None, [C.c_void_p]),
     ("get_local_trees_ntrees", C.c_int, [C.c_void_p]),
     ("get_local_trees_nnodes", C.c_int, [C.c_void_p]),
+    ("get_state_spaces", C.c_void_p, [C.c_void_p, C.c_int, C.c_bool]),
+    ("delete_state_spaces", None, [C.c_void_p, C.c_int]),
     ("arghmm_get_nstates", None, [C.c_void_p, C.c_int, C.c_bool, c_int_p]),
     ("arghmm_forward_alg", c_double_pp,
      [C.c_void_p, c_double_p, C.c_int, c_double_p, C.c_double, C.c_double, c_char_pp,

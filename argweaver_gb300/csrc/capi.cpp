@@ -601,6 +601,44 @@ int awg_remove_arg_thread(awg_local_trees *trees, int seqid) {
     store_trees(trees, a);
     return 0;
 }
+// get_state_spaces (states.cpp:228-251): each tree's (node, time) states in new[] rows. As
+// the reference's, it lists external states (get_coal_states with its default, states.cpp:
+// 53-74) whatever `internal` says: node index order, times from the node's age up to its
+// parent's (the root's up to ntimes - 2).
+awg_intstate **get_state_spaces(awg_local_trees *trees, int ntimes, bool internal) {
+    (void)internal;
+    g_err.clear();
+    if (!trees) {
+        set_error("get_state_spaces: NULL trees");
+        return nullptr;
+    }
+    const int n = trees->nnodes;
+    awg_intstate **all = new awg_intstate *[trees->ntrees];
+    for (int b = 0; b < trees->ntrees; b++) {
+        const int *par = &trees->ptrees[(size_t)b * n], *age = &trees->ages[(size_t)b * n];
+        std::vector<int> st;
+        for (int i = 0; i < n; i++) {
+            const int top = par[i] == -1 ? ntimes - 2 : age[par[i]];
+            for (int t = age[i]; t <= top; t++) {
+                st.push_back(i);
+                st.push_back(t);
+            }
+        }
+        all[b] = new awg_intstate[st.size() / 2 + 1];
+        for (size_t j = 0; j < st.size() / 2; j++) {
+            all[b][j][0] = st[2 * j];
+            all[b][j][1] = st[2 * j + 1];
+        }
+    }
+    return all;
+}
+
+void delete_state_spaces(awg_intstate **all_states, int ntrees) {
+    if (!all_states) return;
+    for (int i = 0; i < ntrees; i++) delete[] all_states[i];
+    delete[] all_states;
+}
+
 int get_local_trees_ntrees(awg_local_trees *trees) { return trees ? trees->ntrees : 0; }
 int get_local_trees_nnodes(awg_local_trees *trees) { return trees ? trees->nnodes : 0; }
 

@@ -380,6 +380,25 @@ def _with_trees(prob: Problem, fn):
         trees.close()
 
 
+def get_state_spaces(prob: Problem) -> list:
+    """Each tree's external states as an (S, 2) array of (node, time) (get_state_spaces,
+    states.cpp:228-251)."""
+    def run(lib, trees, p):
+        ptr = lib.get_state_spaces(trees.handle, p.ntimes, False)
+        if not ptr:
+            raise ValueError(capi.last_error())
+        try:
+            rows = C.cast(ptr, C.POINTER(C.POINTER(C.c_int)))
+            ns = np.zeros(p.seqlen, dtype=np.int32)
+            lib.arghmm_get_nstates(trees.handle, p.ntimes, False, ns.ctypes.data_as(capi.c_int_p))
+            starts = np.concatenate([[0], np.cumsum(p.blocklens)[:-1]])
+            return [np.ctypeslib.as_array(rows[b], shape=(int(ns[starts[b]]) * 2,)).reshape(-1, 2).copy()
+                    if ns[starts[b]] > 0 else np.zeros((0, 2), np.int32) for b in range(p.ntrees)]
+        finally:
+            lib.delete_state_spaces(ptr, p.ntrees)
+    return _with_trees(prob, run)
+
+
 def sample_arg_removal_path(prob: Problem, node: int, pos: int | None = None,
                             leaf: bool = False) -> np.ndarray:
     """A removal path (one node per tree) from `node` of the first tree forward

@@ -136,6 +136,14 @@ int awg_sample_arg_thread_internal(awg_local_trees *trees, double *times, int nt
                                    double *popsizes, double rho, double mu, char **seqs,
                                    int nseqs, int seqlen, int minage, int *thread_path);
 
+/* get_state_spaces (states.cpp:228-251): each tree's states as (node, time) pairs, one new[]
+ * row per tree (arghmm_get_nstates' counts per column give the row lengths); free with
+ * delete_state_spaces (:255-260). As the reference's, `internal` is accepted and the
+ * external states are listed. */
+typedef int awg_intstate[2]; /* intstate (states.h:135) */
+awg_intstate **get_state_spaces(awg_local_trees *trees, int ntimes, bool internal);
+void delete_state_spaces(awg_intstate **all_states, int ntrees);
+
 /* arghmm_get_nstates (states.cpp:209): states of every column. */
 void arghmm_get_nstates(awg_local_trees *trees, int ntimes, bool internal, int *nstates);
 

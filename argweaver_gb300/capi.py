@@ -95,6 +95,7 @@ PROTOTYPES = [
     ("arghmm_sample_arg_removal_path", None, [C.c_void_p, C.c_int, c_int_p]),
     ("arghmm_sample_arg_removal_path2", None, [C.c_void_p, C.c_int, C.c_int, c_int_p]),
     ("arghmm_sample_arg_removal_leaf_path", None, [C.c_void_p, C.c_int, c_int_p]),
+    ("arghmm_sample_arg_removal_path_recomb", None, [C.c_void_p, C.c_double, c_int_p]),
     ("awg_sample_arg_removal_path_uniform", C.c_double, [C.c_void_p, c_int_p]),
     ("arghmm_remove_arg_thread_path", None, [C.c_void_p, c_int_p, C.c_int]),
     ("arghmm_remove_arg_thread_path2", None, [C.c_void_p, c_int_p, C.c_int, c_int_p]),

@@ -701,6 +701,72 @@ bool sample_removal_path(const ThreadTrees &a, int node, long long pos, int (*rn
     return true;
 }
 
+// sample (common.h:272-290): the first index whose running weight reaches frand(total)
+static int sample_index(const double *w, int n, int (*rnd)()) {
+    double total = 0.0;
+    for (int i = 0; i < n; i++) total += w[i];
+    const double pick = unit(rnd) * total;
+    double x = 0.0;
+    for (int i = 0; i < n; i++) {
+        x += w[i];
+        if (x >= pick) return i;
+    }
+    return n - 1;
+}
+
+bool sample_removal_path_recomb(const ThreadTrees &a, double pref, int (*rnd)(), int *path,
+                                std::string &err) {
+    std::vector<Tree> trees;
+    std::vector<std::vector<int>> maps;
+    std::vector<Spr4> sprs;
+    if (!load_trees(a, trees, maps, sprs, "sample_arg_removal_path_recomb", err)) return false;
+    const int B = a.ntrees, n = a.nnodes;
+    // forward table over branches (thread.cpp:814-878). As the reference's, the split
+    // weight and the recombination preference are looked up by the later tree's node index.
+    std::vector<double> fw((size_t)B * n), trans((size_t)B * n, 1.0);
+    std::vector<int> back((size_t)B * n * 2, -1);
+    for (int j = 0; j < n; j++) fw[j] = 1.0 / n;
+    for (int b = 1; b < B; b++) {
+        const std::vector<int> inv = inverse_mapping(maps[b], n);
+        const int recoal = recoal_node(n, maps[b]);
+        for (int j = 0; j < n; j++) {
+            int next[2];
+            next_removal_nodes(trees[b - 1], sprs[b], maps[b], j, next, recoal);
+            trans[(size_t)(b - 1) * n + j] = next[1] != -1 ? .5 : 1.0;
+            int *ptr = &back[((size_t)b * n + j) * 2];
+            prev_removal_nodes(trees[b - 1], sprs[b], maps[b], inv, j, ptr);
+            if (ptr[0] < 0 || ptr[0] >= n || ptr[1] >= n) {
+                err = "sample_arg_removal_path_recomb: inconsistent SPR between neighbouring trees";
+                return false;
+            }
+        }
+        double norm = 0.0;
+        for (int j = 0; j < n; j++) {
+            const int *ptr = &back[((size_t)b * n + j) * 2];
+            double sum = 0.0;
+            for (int ki = 0; ki < 2; ki++)
+                if (ptr[ki] != -1) sum += trans[(size_t)(b - 1) * n + j] * fw[(size_t)(b - 1) * n + ptr[ki]];
+            const double emit = sprs[b].v[0] == j ? pref : 1.0 - pref;
+            fw[(size_t)b * n + j] = sum * emit;
+            norm += fw[(size_t)b * n + j];
+        }
+        for (int j = 0; j < n; j++) fw[(size_t)b * n + j] /= norm;
+    }
+    // the last branch, then a stochastic traceback (thread.cpp:881-903)
+    int j = path[B - 1] = sample_index(&fw[(size_t)(B - 1) * n], n, rnd);
+    for (int b = B - 2; b >= 0; b--) {
+        const int *ptr = &back[((size_t)(b + 1) * n + j) * 2];
+        if (ptr[1] == -1) {
+            j = path[b] = ptr[0];
+        } else {
+            const double t = trans[(size_t)b * n + j];
+            const double probs[2] = {fw[(size_t)b * n + ptr[0]] * t, fw[(size_t)b * n + ptr[1]] * t};
+            j = path[b] = ptr[sample_index(probs, 2, rnd)];
+        }
+    }
+    return true;
+}
+
 bool sample_removal_path_uniform(const ThreadTrees &a, int (*rnd)(), int *path, double *lntotal,
                                  std::string &err) {
     std::vector<Tree> trees;

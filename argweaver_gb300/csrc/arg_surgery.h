@@ -37,6 +37,12 @@ bool remove_arg_thread(ThreadTrees &a, int seqid, std::string &err);
 bool sample_removal_path(const ThreadTrees &a, int node, long long pos, int (*rnd)(), int *path,
                          std::string &err);
 
+// A removal path that prefers branches carrying recombinations (sample_arg_removal_path_recomb,
+// thread.cpp:800-912): forward over branches with weight `pref` where the SPR's recombination
+// node is, 1 - pref elsewhere, then a stochastic traceback; draws from rnd as the reference's.
+bool sample_removal_path_recomb(const ThreadTrees &a, double pref, int (*rnd)(), int *path,
+                                std::string &err);
+
 // A removal path drawn uniformly from all paths by counting them back to front
 // (sample_arg_removal_path_uniform, thread.cpp:914-1002); lntotal: the log path count.
 bool sample_removal_path_uniform(const ThreadTrees &a, int (*rnd)(), int *path, double *lntotal,

@@ -549,6 +549,16 @@ void arghmm_sample_arg_removal_leaf_path(awg_local_trees *trees, int node, int *
         set_error(err);
 }
 
+void arghmm_sample_arg_removal_path_recomb(awg_local_trees *trees, double recomb_preference,
+                                           int *path) {
+    g_err.clear();
+    std::string err;
+    if (!trees || !path) set_error("arghmm_sample_arg_removal_path_recomb: NULL argument");
+    else if (!awg::sample_removal_path_recomb(thread_trees(trees), recomb_preference, rand, path,
+                                              err))
+        set_error(err);
+}
+
 double awg_sample_arg_removal_path_uniform(awg_local_trees *trees, int *path) {
     g_err.clear();
     std::string err;

@@ -421,6 +421,20 @@ def sample_arg_removal_path(prob: Problem, node: int, pos: int | None = None,
     return _with_trees(prob, run)
 
 
+def sample_arg_removal_path_recomb(prob: Problem, recomb_preference: float) -> np.ndarray:
+    """A removal path preferring recombination-bearing branches
+    (sample_arg_removal_path_recomb, thread.cpp:800-912); draws from libc rand()."""
+    def run(lib, trees, p):
+        path = np.zeros(p.ntrees, dtype=np.int32)
+        lib.arghmm_sample_arg_removal_path_recomb(trees.handle, float(recomb_preference),
+                                                  path.ctypes.data_as(capi.c_int_p))
+        err = capi.last_error()
+        if err:
+            raise ValueError(err)
+        return path
+    return _with_trees(prob, run)
+
+
 def sample_arg_removal_path_uniform(prob: Problem):
     """(path, log number of paths): a removal path drawn uniformly over all of them
     (sample_arg_removal_path_uniform, thread.cpp:963-1002); draws from libc rand()."""

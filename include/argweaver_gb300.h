@@ -97,6 +97,12 @@ void arghmm_sample_arg_removal_path(awg_local_trees *trees, int node, int *path)
 void arghmm_sample_arg_removal_path2(awg_local_trees *trees, int node, int pos, int *path);
 void arghmm_sample_arg_removal_leaf_path(awg_local_trees *trees, int node, int *path);
 
+/* A removal path that prefers branches carrying recombinations (weight recomb_preference
+ * where the SPR recombines, 1 - recomb_preference elsewhere; thread.cpp:800-912, bound at
+ * :1698-1702), drawn from libc rand(). Errors: awg_last_error(). */
+void arghmm_sample_arg_removal_path_recomb(awg_local_trees *trees, double recomb_preference,
+                                           int *path);
+
 /* A removal path drawn uniformly over all of them (sample_arg_removal_path_uniform,
  * thread.cpp:963-1002, which arg-sample's subtree cuts use); returns the log number of paths,
  * NaN on error. */

@@ -748,7 +748,8 @@ static int cmd_removethread(const char *in, const char *prefix, int nrm, char **
 
 // After srand(seed): a uniform removal path (sample_arg_removal_path_uniform), a forward
 // path from `node` (sample_arg_removal_path), one through `node` at coordinate `pos`
-// (sample_arg_removal_path2) and the leaf path of leaf 0, as <prefix>.paths (4 x ntrees
+// (sample_arg_removal_path2), the leaf path of leaf 0 and a path preferring recombinations
+// (sample_arg_removal_path_recomb, .9), as <prefix>.paths (5 x ntrees
 // ints) and the log path count as <prefix>.lntotal; then the ARG cut along the uniform path
 // (remove_arg_thread_path, maxtime ntimes + 1) as <prefix>.cut.prob, with the removed thread
 // as states of the cut trees as <prefix>.orig
@@ -757,12 +758,13 @@ static int cmd_removalpaths(const char *in, int seed, int node, int pos, const c
     if (p.internal) die("removalpaths: full ARGs only");
     LocalTrees *trees = make_trees(p);
     const int B = trees->get_num_trees();
-    vector<int> paths((size_t)4 * B);
+    vector<int> paths((size_t)5 * B);
     srand(seed);
     double lntotal = sample_arg_removal_path_uniform(trees, &paths[0]);
     sample_arg_removal_path(trees, node, &paths[B]);
     sample_arg_removal_path(trees, node, pos, &paths[2 * B], .5);
     sample_arg_removal_leaf_path(trees, 0, &paths[3 * B]);
+    sample_arg_removal_path_recomb(trees, .9, &paths[4 * B]);
     std::string base(prefix);
     FILE *f = fopen((base + ".paths").c_str(), "wb");
     if (!f) die("cannot write paths");

@@ -431,7 +431,7 @@ def removalpaths(tmp):
         off = int(frac * int(np.sum(prob.blocklens)))
         prefix = os.path.join(tmp, name)
         run("removalpaths", pp, seed, node, prob.start_coord + off, prefix)
-        paths = np.fromfile(prefix + ".paths", dtype=np.int32).reshape(4, prob.ntrees)
+        paths = np.fromfile(prefix + ".paths", dtype=np.int32).reshape(5, prob.ntrees)
         cut = Problem.load(prefix + ".cut.prob")
         np.savez_compressed(
             os.path.join(out_dir, name + ".npz"), seed=seed, node=node,

@@ -1,8 +1,9 @@
 """Removal paths and the internal-branch cut on the host (thread.cpp:562-1002,1481-1668):
 after srand(seed) the uniform path, its log path count, the forward path from a node, the
-path through a node at a position and the leaf path equal the reference's draws, and the ARG
-cut along the uniform path (subtree/main-tree form, merged trees, mappings, root child
-order, the removed thread as states of the cut trees) equals the reference's."""
+path through a node at a position, the leaf path and the path preferring recombinations
+equal the reference's draws, and the ARG cut along the uniform path (subtree/main-tree form,
+merged trees, mappings, root child order, the removed thread as states of the cut trees)
+equals the reference's."""
 
 import os
 
@@ -30,12 +31,14 @@ def test_removal_paths_match_reference(name):
     fpath = refapi.sample_arg_removal_path(prob, node)
     ppath = refapi.sample_arg_removal_path(prob, node, pos)
     lpath = refapi.sample_arg_removal_path(prob, 0, leaf=True)
+    rpath = refapi.sample_arg_removal_path_recomb(prob, 0.9)
     paths = ref["paths"]
     np.testing.assert_array_equal(upath, paths[0])
     assert lntotal == float(ref["lntotal"])
     np.testing.assert_array_equal(fpath, paths[1])
     np.testing.assert_array_equal(ppath, paths[2])
     np.testing.assert_array_equal(lpath, paths[3])
+    np.testing.assert_array_equal(rpath, paths[4])
 
 
 @pytest.mark.parametrize("name", NAMES)

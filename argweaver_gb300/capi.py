@@ -53,6 +53,10 @@ PROTOTYPES = [
     ("get_local_trees_nnodes", C.c_int, [C.c_void_p]),
     ("get_state_spaces", C.c_void_p, [C.c_void_p, C.c_int, C.c_bool]),
     ("delete_state_spaces", None, [C.c_void_p, C.c_int]),
+    ("read_local_trees", C.c_void_p, [C.c_char_p, c_double_p, C.c_int]),
+    ("arghmm_copy_trees", C.c_void_p, [C.c_void_p]),
+    ("get_local_trees_blocks", None, [C.c_void_p, c_int_p, c_int_p]),
+    ("get_treelens", None, [C.c_void_p, c_double_p, C.c_int, c_double_p]),
     ("arghmm_get_nstates", None, [C.c_void_p, C.c_int, C.c_bool, c_int_p]),
     ("arghmm_forward_alg", c_double_pp,
      [C.c_void_p, c_double_p, C.c_int, c_double_p, C.c_double, C.c_double, c_char_pp,

@@ -17,6 +17,7 @@
 #include "kernels.h"
 #include "plan.h"
 #include "arg_surgery.h"
+#include "formats.h"
 
 struct awg_local_trees {
     int ntrees = 0, nnodes = 0, start_coord = 0;
@@ -647,6 +648,60 @@ void delete_state_spaces(awg_intstate **all_states, int ntrees) {
     if (!all_states) return;
     for (int i = 0; i < ntrees; i++) delete[] all_states[i];
     delete[] all_states;
+}
+
+// read_local_trees (local_tree.cpp:1908-1932): a trees handle from an SMC file (gzip read
+// through a pipe when the name ends in .gz); NULL and awg_last_error() on failure.
+awg_local_trees *read_local_trees(const char *filename, const double *times, int ntimes) {
+    g_err.clear();
+    awg::SmcArrays a;
+    std::string err;
+    if (!awg::read_smc_arrays(filename, times, ntimes, a, err)) {
+        set_error(err);
+        return nullptr;
+    }
+    awg_local_trees *t = new awg_local_trees();
+    t->ntrees = a.ntrees; t->nnodes = a.nnodes; t->start_coord = a.start_coord;
+    t->ptrees = std::move(a.ptrees); t->ages = std::move(a.ages); t->sprs = std::move(a.sprs);
+    t->blocklens = std::move(a.blocklens);
+    t->c0 = std::move(a.c0); t->c1 = std::move(a.c1);  // newick child order
+    return t;
+}
+
+// arghmm_copy_trees (local_tree.cpp:1827-1832)
+awg_local_trees *arghmm_copy_trees(awg_local_trees *trees) {
+    g_err.clear();
+    if (!trees) {
+        set_error("arghmm_copy_trees: NULL trees");
+        return nullptr;
+    }
+    return new awg_local_trees(*trees);
+}
+
+// get_local_trees_blocks (local_tree.cpp:1946-1958): each tree's [start, end) coordinates
+void get_local_trees_blocks(awg_local_trees *trees, int *starts, int *ends) {
+    if (!trees || !starts || !ends) return;
+    int end = trees->start_coord;
+    for (int b = 0; b < trees->ntrees; b++) {
+        starts[b] = end;
+        end += trees->blocklens[b];
+        ends[b] = end;
+    }
+}
+
+// get_treelens (local_tree.cpp:1935-1943): each tree's branch length without the basal stub
+// (get_treelen, local_tree.cpp:136-155), summed in node order as there
+void get_treelens(awg_local_trees *trees, const double *times, int ntimes, double *treelens) {
+    (void)ntimes;
+    if (!trees || !times || !treelens) return;
+    const int n = trees->nnodes;
+    for (int b = 0; b < trees->ntrees; b++) {
+        const int *par = &trees->ptrees[(size_t)b * n], *age = &trees->ages[(size_t)b * n];
+        double len = 0.0;
+        for (int i = 0; i < n; i++)
+            if (par[i] != -1) len += times[age[par[i]]] - times[age[i]];
+        treelens[b] = len;
+    }
 }
 
 int get_local_trees_ntrees(awg_local_trees *trees) { return trees ? trees->ntrees : 0; }

@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "argweaver_gb300.h"
+#include "formats.h"
 
 struct awg_arg_input {
     std::vector<std::string> names;  // sequence names, sites order
@@ -438,6 +439,48 @@ bool read_smc(FILE *f, const std::vector<double> &times, SmcTrees &s) {
 }
 
 }  // namespace
+
+namespace awg {
+
+bool read_smc_arrays(const char *path, const double *times, int ntimes, SmcArrays &out,
+                     std::string &err) {
+    if (!path || !times || ntimes < 2) {
+        err = "read_local_trees: bad arguments";
+        return false;
+    }
+    SmcTrees s;
+    {
+        Stream st(path, false);
+        if (!st.f) {
+            err = std::string("cannot read SMC file '") + path + "'";
+            return false;
+        }
+        if (!read_smc(st.f, std::vector<double>(times, times + ntimes), s)) {
+            err = f_err;
+            return false;
+        }
+    }
+    const int n = 2 * (int)s.names.size() - 1, B = (int)s.trees.size();
+    out.ntrees = B;
+    out.nnodes = n;
+    out.start_coord = s.start_coord;
+    out.blocklens = s.blocklens;
+    out.sprs = s.spr;
+    for (int b = 0; b < B; b++) {
+        const PTree &t = s.trees[b];
+        if ((int)t.parent.size() != n) {
+            err = "read_local_trees: a tree with the wrong number of nodes";
+            return false;
+        }
+        out.ptrees.insert(out.ptrees.end(), t.parent.begin(), t.parent.end());
+        out.ages.insert(out.ages.end(), t.age.begin(), t.age.end());
+        out.c0.insert(out.c0.end(), t.c0.begin(), t.c0.end());
+        out.c1.insert(out.c1.end(), t.c1.begin(), t.c1.end());
+    }
+    return true;
+}
+
+}  // namespace awg
 
 extern "C" {
 

@@ -150,6 +150,20 @@ typedef int awg_intstate[2]; /* intstate (states.h:135) */
 awg_intstate **get_state_spaces(awg_local_trees *trees, int ntimes, bool internal);
 void delete_state_spaces(awg_intstate **all_states, int ntrees);
 
+/* read_local_trees (local_tree.cpp:1908-1932): a trees handle from an SMC file (.gz read
+ * through gzip), times snapped to the given grid; NULL and awg_last_error() on failure. */
+awg_local_trees *read_local_trees(const char *filename, const double *times, int ntimes);
+
+/* arghmm_copy_trees (local_tree.cpp:1827-1832): an independent copy of the handle. */
+awg_local_trees *arghmm_copy_trees(awg_local_trees *trees);
+
+/* get_local_trees_blocks (local_tree.cpp:1946-1958): [start, end) of every tree. */
+void get_local_trees_blocks(awg_local_trees *trees, int *starts, int *ends);
+
+/* get_treelens (local_tree.cpp:1935-1943): every tree's total branch length (times[] units,
+ * no basal stub). */
+void get_treelens(awg_local_trees *trees, const double *times, int ntimes, double *treelens);
+
 /* arghmm_get_nstates (states.cpp:209): states of every column. */
 void arghmm_get_nstates(awg_local_trees *trees, int ntimes, bool internal, int *nstates);
 

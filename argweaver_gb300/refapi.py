@@ -380,6 +380,20 @@ def _with_trees(prob: Problem, fn):
         trees.close()
 
 
+def as_problem(prob: Problem, trees: dict, internal: bool = False) -> Problem:
+    """A Problem over the trees a surgery call returned (its dict) with prob's model and
+    sequences: sequence rows follow the leaves' sequence ids, so leaf i reads row i, and an
+    internal problem (a cut ARG) carries each root's first child."""
+    ids = np.asarray(trees["seqids"], dtype=np.int64)
+    nleaves = (trees["ptrees"].shape[1] + 1) // 2
+    rows = list(ids[:nleaves]) + [i for i in range(prob.nseqs) if i not in set(ids[:nleaves].tolist())]
+    return Problem(times=prob.times, popsizes=prob.popsizes, rho=prob.rho, mu=prob.mu,
+                   ptrees=trees["ptrees"], ages=trees["ages"], sprs=trees["sprs"],
+                   blocklens=trees["blocklens"], seqs=np.ascontiguousarray(prob.seqs[rows]),
+                   internal=internal, start_coord=prob.start_coord, mapping=trees["mapping"],
+                   root_child0=trees["root_child0"])
+
+
 def get_state_spaces(prob: Problem) -> list:
     """Each tree's external states as an (S, 2) array of (node, time) (get_state_spaces,
     states.cpp:228-251)."""

@@ -36,6 +36,7 @@
 //   removethread <problem> <out-prefix> <seqid>...
 //   addthreadpath <internal problem> <path> <recombs> <out>
 //   samplethreadinternal <internal problem> <seed> <out>
+//   resampleleaf <problem> <seqid> <seed> <out>
 //   removalpaths <problem> <seed> <node> <pos> <out-prefix>
 //                                    arghmm_sample_thread (sample_thread.cpp:1010-1023)
 //                                    after srand(seed): the last sequence threaded into the
@@ -692,6 +693,25 @@ static int cmd_samplethreadinternal(const char *in, int seed, const char *out) {
     return 0;
 }
 
+// resample_arg_leaf's move (sample_arg.cpp:66-86) after srand(seed): sequence `seqid`
+// removed from the full ARG and threaded back in; the ARG with leaves named by sequence
+static int cmd_resampleleaf(const char *in, int seqid, int seed, const char *out) {
+    Problem p = read_problem(in);
+    if (p.internal) die("resampleleaf: full ARGs only");
+    LocalTrees *trees = make_trees(p);
+    vector<char *> sp = seq_ptrs(p);
+    ArgModel model(p.ntimes, p.times.data(), p.popsizes.data(), p.rho, p.mu);
+    Sequences sequences(sp.data(), p.nseqs, p.seqlen);
+    srand(seed);
+    remove_arg_thread(trees, seqid);
+    sample_arg_thread(&model, &sequences, trees, seqid);
+    Problem q = p;
+    trees_to_problem(trees, q);
+    write_problem(out, q);
+    delete trees;
+    return 0;
+}
+
 static int cmd_samplethread(const char *in, int seed, const char *out) {
     Problem p = read_problem(in);
     if (p.internal) die("samplethread: external problems only");
@@ -823,6 +843,8 @@ int main(int argc, char **argv) {
         return cmd_addthreadpath(argv[2], argv[3], argv[4], argv[5]);
     if (cmd == "samplethreadinternal" && argc == 5)
         return cmd_samplethreadinternal(argv[2], atoi(argv[3]), argv[4]);
+    if (cmd == "resampleleaf" && argc == 6)
+        return cmd_resampleleaf(argv[2], atoi(argv[3]), atoi(argv[4]), argv[5]);
     if (cmd == "addthread" && argc == 6)
         return cmd_addthread(argv[2], argv[3], argv[4], argv[5]);
     if (cmd == "recomb" && argc == 6)

@@ -358,6 +358,23 @@ def samplethreadinternal(tmp):
         print(name, q.ntrees)
 
 
+def resampleleaf(tmp):
+    """resample_arg_leaf's move (sample_arg.cpp:66-86) after srand(seed) on grown ARGs: a
+    sequence removed and threaded back in; the ARG with leaves named by sequence."""
+    out_dir = os.path.join(HERE, "resampleleaf")
+    os.makedirs(out_dir, exist_ok=True)
+    for name, seqid, seed in (("dsmc_k8_s11", 2, 401), ("dsmc_k10_T16", 0, 402),
+                              ("single_k7_s41", 6, 403), ("sim1_c20", 4, 404)):
+        pp = os.path.join(HERE, "addthread", name + ".prob")
+        out = os.path.join(tmp, name + ".prob")
+        run("resampleleaf", pp, seqid, seed, out)
+        q = Problem.load(out)
+        np.savez_compressed(os.path.join(out_dir, name + ".npz"), seqid=seqid, seed=seed,
+                            ptrees=q.ptrees, ages=q.ages, sprs=q.sprs, blocklens=q.blocklens,
+                            mapping=q.mapping)
+        print(name, q.ntrees)
+
+
 def samplethread(tmp):
     """arghmm_sample_thread (sample_thread.cpp:1010-1023) after srand(seed + 9000) on the
     external fixtures: the ARG with the last sequence threaded in, as the reference grows it."""
@@ -466,6 +483,10 @@ def main():
     if sys.argv[1:] == ["infsites"]:
         with tempfile.TemporaryDirectory() as tmp:
             infsites(tmp)
+        return
+    if sys.argv[1:] == ["resampleleaf"]:
+        with tempfile.TemporaryDirectory() as tmp:
+            resampleleaf(tmp)
         return
     if sys.argv[1:] == ["samplethreadinternal"]:
         with tempfile.TemporaryDirectory() as tmp:

@@ -83,3 +83,40 @@ def test_remove_then_add_restores_leaf_count():
         assert ids[-1] == 3
     finally:
         trees.close()
+
+
+RL_NAMES = sorted(f[:-4] for f in os.listdir(os.path.join(GOLDEN, "resampleleaf")) if f.endswith(".npz"))
+
+
+@pytest.mark.parametrize("name", RL_NAMES)
+def test_leaf_resampling_move_matches_reference(name):
+    """resample_arg_leaf's move (sample_arg.cpp:66-86) on one handle: the sequence removed
+    (awg_remove_arg_thread), re-threaded by the oracle's traceback and recombination sampler
+    on the reference's draws after srand(seed), added back (awg_add_arg_thread, which gives the
+    new leaf the freed sequence id); the ARG, leaves named by sequence, is the reference's."""
+    import pyoracle
+    ref = np.load(os.path.join(GOLDEN, "resampleleaf", name + ".npz"))
+    full = grown(name).normalized()
+    lib = capi.load()
+    trees = refapi._trees_handle(full)
+    try:
+        assert lib.awg_remove_arg_thread(trees.handle, int(ref["seqid"])) == 0
+        partial = refapi.as_problem(full, refapi._tree_dict(trees))
+        L = partial.seqlen
+        draws = pyoracle.rand_uniforms(int(ref["seed"]), 3 * L + 2)[::-1]
+        fw, _ = pyoracle.forward(partial)
+        path = pyoracle.traceback(partial, fw, draws[:L][::-1].copy())
+        pos, node, time, _ = pyoracle.sample_recombinations(partial, path, draws[L:].copy())
+        i32 = lambda a: np.ascontiguousarray(a, dtype=np.int32)
+        path, pos, node, time = i32(path), i32(pos), i32(node), i32(time)
+        p = lambda a: a.ctypes.data_as(capi.c_int_p)
+        assert lib.awg_add_arg_thread(trees.handle, full.ntimes, p(path), L, p(pos), p(node),
+                                      p(time), len(pos)) == 0, capi.last_error()
+        got = refapi._tree_dict(trees)
+    finally:
+        trees.close()
+    assert sorted(got["seqids"].tolist()) == list(range((full.nnodes + 1) // 2))
+    for key in ("ptrees", "ages", "blocklens"):
+        np.testing.assert_array_equal(got[key], ref[key], err_msg=key)
+    np.testing.assert_array_equal(got["sprs"][1:], ref["sprs"][1:])
+    np.testing.assert_array_equal(got["mapping"][1:], ref["mapping"][1:])

@@ -106,6 +106,8 @@ PROTOTYPES = [
     ("arghmm_get_thread_times", None, [C.c_void_p, C.c_int, c_int_p, c_int_p]),
     ("awg_add_arg_thread_path", C.c_int, [C.c_void_p, C.c_int, C.c_int, c_int_p, C.c_int,
                                           c_int_p, c_int_p, c_int_p, C.c_int]),
+    ("awg_sample_arg_thread", C.c_int, [C.c_void_p, c_double_p, C.c_int, c_double_p, C.c_double,
+                                        C.c_double, c_char_pp, C.c_int, C.c_int, C.c_int]),
     ("awg_sample_arg_thread_internal", C.c_int, [C.c_void_p, c_double_p, C.c_int, c_double_p,
                                                  C.c_double, C.c_double, c_char_pp, C.c_int,
                                                  C.c_int, C.c_int, c_int_p]),

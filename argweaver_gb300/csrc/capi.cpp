@@ -66,7 +66,7 @@ bool leaf_perm(const awg_local_trees *t, std::vector<int> &perm) {
 
 bool make_view(const awg_local_trees *t, double *times, int ntimes, double *popsizes,
                double rho, double mu, char **seqs, int nseqs, int seqlen, bool internal,
-               ProblemView &v) {
+               ProblemView &v, const std::vector<int> *row_list = nullptr) {
     if (!t || !times || !popsizes || !seqs) { set_error("NULL argument"); return false; }
     // leaf i reads sequence seqids[i] (matrices.cpp:34, total_prob.cpp:32); the rows after
     // the leaves are the last sequences, in order (the thread's new_chrom = nseqs - 1)
@@ -81,6 +81,10 @@ bool make_view(const awg_local_trees *t, double *times, int ntimes, double *pops
             }
             rows[i] = t->seqids[i];
         }
+    }
+    if (row_list) {  // the caller's rows (sequence ids), in leaf order then the new one
+        rows = *row_list;
+        nseqs = (int)rows.size();
     }
     v.seqs.resize((size_t)nseqs * seqlen);
     for (int i = 0; i < nseqs; i++) memcpy(&v.seqs[(size_t)i * seqlen], seqs[rows[i]], seqlen);
@@ -853,6 +857,58 @@ awg_local_trees *arghmm_sample_thread(awg_local_trees *trees, double *times, int
                            time.data(), nrec) == 0 && !trees->seqids.empty())
         trees->seqids.back() = nseqs - 1;  // the new leaf holds new_chrom (thread.cpp:292)
     return trees;
+}
+
+// sample_arg_thread (sample_thread.cpp:575-625) for sequence new_chrom of the caller's full
+// sequence set: the leaves read their sequence ids' rows, the thread is new_chrom's; the
+// step as in arghmm_sample_thread, and the new leaf holds new_chrom.
+int awg_sample_arg_thread(awg_local_trees *trees, double *times, int ntimes, double *popsizes,
+                          double rho, double mu, char **seqs, int nseqs, int seqlen,
+                          int new_chrom) {
+    g_err.clear();
+    if (!trees || !seqs) {
+        set_error("awg_sample_arg_thread: NULL argument");
+        return -1;
+    }
+    const int nleaves = (trees->nnodes + 1) / 2;
+    std::vector<int> rows(nleaves + 1);
+    for (int i = 0; i < nleaves; i++) rows[i] = trees->seqids.empty() ? i : trees->seqids[i];
+    rows[nleaves] = new_chrom;
+    for (int i = 0; i <= nleaves; i++)
+        if (rows[i] < 0 || rows[i] >= nseqs || (i < nleaves && rows[i] == new_chrom)) {
+            set_error("awg_sample_arg_thread: new_chrom must be a sequence no leaf holds");
+            return -1;
+        }
+    ProblemView v;
+    if (!make_view(trees, times, ntimes, popsizes, rho, mu, seqs, nseqs, seqlen, false, v, &rows))
+        return -1;
+    std::vector<int> path(seqlen);
+    awg_outputs o;
+    memset(&o, 0, sizeof(o));
+    o.path = path.data();
+    awg::RunOptions opt;
+    std::string err;
+    if (awg::run_batch(&v.p, &o, 1, opt, err) != 0) {
+        set_error(err);
+        return -1;
+    }
+    const int nu = 2 * seqlen + 2;
+    std::vector<double> u(nu);
+    for (double &x : u) x = rand() / double(RAND_MAX);  // frand (common.h:103-110)
+    std::vector<int> pos(seqlen), node(seqlen), time(seqlen);
+    int used = 0;
+    const int nrec = awg::sample_recombinations(&v.p, path.data(), u.data(), nu, pos.data(),
+                                                node.data(), time.data(), seqlen, &used, err);
+    if (nrec < 0) {
+        set_error(err);
+        return -1;
+    }
+    std::vector<int> ids(rows.begin(), rows.end());  // the leaves' ids after the step
+    if (awg_add_arg_thread(trees, ntimes, path.data(), seqlen, pos.data(), node.data(),
+                           time.data(), nrec) != 0)
+        return -1;
+    trees->seqids = ids;  // the new leaf holds new_chrom (thread.cpp:292)
+    return 0;
 }
 
 // sample_arg_thread_internal (sample_thread.cpp:635-692): the cut subtree of an internal

@@ -527,6 +527,26 @@ def add_arg_thread_path(prob: Problem, path, rec_pos, rec_node, rec_time,
     return _with_trees(prob, run)
 
 
+def resample_arg_leaf(prob: Problem, seqid: int) -> dict:
+    """resample_arg_leaf's move (sample_arg.cpp:66-86) on a full ARG: sequence `seqid`
+    removed (host) and threaded back in (awg_sample_arg_thread: forward, traceback and
+    recombinations on the device with draws from libc rand(), the thread added on the host).
+    Returns the ARG as a dict, leaves named by sequence."""
+    def run(lib, trees, p):
+        if p.internal:
+            raise ValueError("resample_arg_leaf: full ARGs only")
+        if lib.awg_remove_arg_thread(trees.handle, int(seqid)) != 0:
+            raise ValueError(capi.last_error())
+        seqs, _keep = _char_pp(p.seqs)
+        rc = lib.awg_sample_arg_thread(trees.handle, p.times.ctypes.data_as(capi.c_double_p),
+                                       p.ntimes, p.popsizes.ctypes.data_as(capi.c_double_p),
+                                       p.rho, p.mu, seqs, p.nseqs, p.seqlen, int(seqid))
+        if rc != 0:
+            raise RuntimeError(capi.last_error())
+        return _tree_dict(trees)
+    return _with_trees(prob, run)
+
+
 def sample_arg_thread_internal(prob: Problem, minage: int = 0):
     """The internal problem's cut subtree re-threaded (sample_arg_thread_internal,
     sample_thread.cpp:635-692): forward, traceback and recombinations on the device with draws

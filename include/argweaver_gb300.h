@@ -134,6 +134,14 @@ int awg_add_arg_thread_path(awg_local_trees *trees, int ntimes, int minage, cons
                             int seqlen, const int *rec_pos, const int *rec_node,
                             const int *rec_time, int nrec);
 
+/* sample_arg_thread (sample_thread.cpp:575-625) for sequence new_chrom of the full sequence
+ * set (nseqs rows; the leaves read the rows of their sequence ids): the threading step of
+ * arghmm_sample_thread, the new leaf holding new_chrom (resample_arg_leaf's re-threading,
+ * sample_arg.cpp:66-86, after awg_remove_arg_thread). 0, or -1 (awg_last_error). */
+int awg_sample_arg_thread(awg_local_trees *trees, double *times, int ntimes, double *popsizes,
+                          double rho, double mu, char **seqs, int nseqs, int seqlen,
+                          int new_chrom);
+
 /* sample_arg_thread_internal (sample_thread.cpp:635-692): the cut subtree of trees in
  * subtree/main-tree form re-threaded in place, forward, traceback and recombinations on the
  * device (draws from libc rand()), the regraft on the host; the thread path into thread_path

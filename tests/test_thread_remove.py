@@ -120,3 +120,19 @@ def test_leaf_resampling_move_matches_reference(name):
         np.testing.assert_array_equal(got[key], ref[key], err_msg=key)
     np.testing.assert_array_equal(got["sprs"][1:], ref["sprs"][1:])
     np.testing.assert_array_equal(got["mapping"][1:], ref["mapping"][1:])
+
+
+def test_sample_arg_thread_rejects_a_leafs_sequence():
+    """awg_sample_arg_thread threads only a sequence no leaf holds (checked before any device
+    work)."""
+    full = grown("single_k7_s41").normalized()
+    lib = capi.load()
+    trees = refapi._trees_handle(full)
+    try:
+        seqs, _keep = refapi._char_pp(full.seqs)
+        rc = lib.awg_sample_arg_thread(trees.handle, full.times.ctypes.data_as(capi.c_double_p),
+                                       full.ntimes, full.popsizes.ctypes.data_as(capi.c_double_p),
+                                       full.rho, full.mu, seqs, full.nseqs, full.seqlen, 2)
+        assert rc == -1 and "no leaf holds" in capi.last_error()
+    finally:
+        trees.close()

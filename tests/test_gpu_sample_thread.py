@@ -30,19 +30,3 @@ def test_sample_thread_matches_reference(name):
     np.testing.assert_array_equal(out.blocklens, ref.blocklens)
     np.testing.assert_array_equal(out.mapping[1:], ref.mapping[1:])
 
-
-RL_NAMES = sorted(f[:-4] for f in os.listdir(os.path.join(GOLDEN, "resampleleaf")) if f.endswith(".npz"))
-
-
-@pytest.mark.parametrize("name", RL_NAMES)
-def test_leaf_resampling_move_matches_reference(name):
-    """resample_arg_leaf's move on the GPU (awg_remove_arg_thread, then awg_sample_arg_thread
-    for the removed sequence): after the same srand(seed), the reference's ARG."""
-    ref = np.load(os.path.join(GOLDEN, "resampleleaf", name + ".npz"))
-    full = Problem.load(os.path.join(GOLDEN, "addthread", name + ".prob"))
-    refapi.srand(int(ref["seed"]))
-    got = refapi.resample_arg_leaf(full, int(ref["seqid"]))
-    for key in ("ptrees", "ages", "blocklens"):
-        np.testing.assert_array_equal(got[key], ref[key], err_msg=key)
-    np.testing.assert_array_equal(got["sprs"][1:], ref["sprs"][1:])
-    np.testing.assert_array_equal(got["mapping"][1:], ref["mapping"][1:])

@@ -1,5 +1,7 @@
-// Host-side ARG surgery: adding a sampled thread to local trees (add_arg_thread,
-// thread.cpp:272-422) and removing a leaf's thread (remove_arg_thread, thread.cpp:425-556).
+// Host-side ARG surgery (thread.cpp): adding a sampled leaf thread (add_arg_thread,
+// :272-422) and removing one (remove_arg_thread, :425-556); removal paths (:562-1002); the
+// internal-branch cut (remove_arg_thread_path, :1481-1668) and regraft (add_arg_thread_path,
+// :1204-1449); the times of an internal thread (arghmm_get_thread_times, :1718-1733).
 #pragma once
 
 #include <string>

@@ -10,6 +10,11 @@ Run where the reference checkout exists (default /root/reference, or $AWG_REFERE
     python tests/golden/make_golden.py recomb     # only the recombination-sampling ones
     python tests/golden/make_golden.py addthread  # only the thread-addition ones
     python tests/golden/make_golden.py samplethread  # only the full threading step
+    python tests/golden/make_golden.py removethread  # leaf-thread removals
+    python tests/golden/make_golden.py removalpaths  # removal paths and the cut
+    python tests/golden/make_golden.py addthreadpath  # the internal-branch regraft
+    python tests/golden/make_golden.py samplethreadinternal  # the internal re-threading step
+    python tests/golden/make_golden.py resampleleaf  # the leaf re-threading move
 
 It builds the reference from its own sources (oracle/Makefile target ``ref``), writes
 each problem as an AWGPROB1 file and runs the reference's threading HMM on it through
@@ -569,6 +574,11 @@ def main():
         recomb(tmp)
         addthread(tmp)
         samplethread(tmp)
+        removethread(tmp)
+        removalpaths(tmp)
+        addthreadpath(tmp)
+        samplethreadinternal(tmp)
+        resampleleaf(tmp)
 
 
 if __name__ == "__main__":

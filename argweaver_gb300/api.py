@@ -206,6 +206,26 @@ def sample_path(prob: Problem, uniforms: Optional[np.ndarray] = None,
     return r.path
 
 
+def sample_path_conditioned(prob: Problem, prior: Optional[np.ndarray] = None,
+                            last_state: int = -1,
+                            uniforms: Optional[np.ndarray] = None) -> np.ndarray:
+    """FP64 forward + traceback with a given first column (``prior``) and/or a given last
+    state (awg_sample_path_conditioned); uniforms as for sample_path (u[L-1] unused when the
+    last state is given; None draws libc rand() as the reference does)."""
+    lib = capi.load()
+    b = _Bound(prob)
+    path = np.empty(b.p.seqlen, dtype=np.int32)
+    pr = None if prior is None else np.ascontiguousarray(prior, dtype=np.float64)
+    u = None if uniforms is None else np.ascontiguousarray(uniforms, dtype=np.float64)
+    rc = lib.awg_sample_path_conditioned(
+        C.byref(b.c), None if pr is None else pr.ctypes.data_as(capi.c_double_p),
+        int(last_state), None if u is None else u.ctypes.data_as(capi.c_double_p),
+        path.ctypes.data_as(capi.c_int_p), None)
+    if rc != 0:
+        raise GpuError(f"awg_sample_path_conditioned failed ({rc}): {capi.last_error()}")
+    return path
+
+
 def posterior(prob: Problem, precision: str = "fp64") -> np.ndarray:
     return run_batch([prob], precision=precision, want_forward=False,
                      want_posterior=True)[0].posterior

@@ -28,9 +28,17 @@ CUDA_LIB = os.path.join(BUILD, "libargweaver_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 HOST_FLAGS = ["-O2", "-fPIC", "-std=c++17", "-ffp-contract=off", "-Wall"]
 # FP64 kernels keep IEEE products and sums separate (no FMA contraction) so the plain path
-# rounds like the reference's host code; FP32 kernels opt in to fused ops explicitly.
+# rounds like the reference's host code. Translation units of FP32-only kernels (FMA_SOURCES)
+# compile with contraction on; their error-free transforms use explicitly rounded intrinsics.
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-ffp-contract=off", "-I" + INCLUDE, "-I" + CSRC] + ARCH
+FMA_SOURCES: set = set()
+
+
+def nvcc_flags(src: str):
+    if src in FMA_SOURCES:
+        return [f if f != "--fmad=false" else "--fmad=true" for f in NVCC_FLAGS]
+    return NVCC_FLAGS
 
 CUDA_SOURCES = ["host_plan.cpp", "tables.cu", "forward.cu", "traceback.cu",
                 "backward.cu", "batch.cu", "static_run.cu", "dense_hmm.cu", "arg_prob.cu",
@@ -100,10 +108,10 @@ def build_cuda(verbose: bool = False) -> str:
         obj = os.path.join(BUILD, src + ".o")
         objs.append(obj)
         stamp = obj + ".stamp"
-        key = _digest([path] + headers, NVCC_FLAGS)
+        key = _digest([path] + headers, nvcc_flags(src))
         if os.path.exists(obj) and os.path.exists(stamp) and open(stamp).read() == key:
             continue
-        cmd = [nvcc] + NVCC_FLAGS + ["-c", "-o", obj, path]
+        cmd = [nvcc] + nvcc_flags(src) + ["-c", "-o", obj, path]
         jobs.append((src, cmd))
         if verbose:
             print(" ".join(cmd), file=sys.stderr)
@@ -111,7 +119,7 @@ def build_cuda(verbose: bool = False) -> str:
     for src, _ in jobs:
         obj = os.path.join(BUILD, src + ".o")
         with open(obj + ".stamp", "w") as f:
-            f.write(_digest([os.path.join(CSRC, src)] + headers, NVCC_FLAGS))
+            f.write(_digest([os.path.join(CSRC, src)] + headers, nvcc_flags(src)))
     link = [nvcc] + ARCH + ["-shared", "-o", CUDA_LIB] + objs + ["-lcudart_static", "-lrt",
                                                                   "-lpthread", "-ldl"]
     _run_parallel([("link", link)])

@@ -152,7 +152,9 @@ class AwgServerStats(C.Structure):
     _fields_ = [("submitted", C.c_longlong), ("completed", C.c_longlong), ("failed", C.c_longlong),
                 ("cells", C.c_longlong), ("p50_ms", C.c_double), ("p99_ms", C.c_double),
                 ("mean_ms", C.c_double), ("max_ms", C.c_double), ("span_s", C.c_double),
-                ("busy_s", C.c_double), ("launch_s", C.c_double), ("inflight_max", C.c_int)]
+                ("busy_s", C.c_double), ("launch_s", C.c_double), ("inflight_max", C.c_int),
+                ("queue_p50_ms", C.c_double), ("queue_p99_ms", C.c_double),
+                ("service_p50_ms", C.c_double), ("service_p99_ms", C.c_double)]
 
 
 # exports of the batch API beyond the reference's (declared in include/argweaver_gb300.h)
@@ -173,6 +175,8 @@ PROTOTYPES += [
     ("awg_batch_device_bytes", C.c_longlong, [C.POINTER(AwgProblem), C.c_int, C.c_int, C.c_int,
                                               C.c_int]),
     ("awg_release_memory", C.c_int, []),
+    ("awg_sample_path_conditioned", C.c_int,
+     [C.POINTER(AwgProblem), c_double_p, C.c_int, c_double_p, c_int_p, c_double_p]),
     ("awg_set_graphs", None, [C.c_int]),
     ("awg_set_schedule", None, [C.c_int, C.c_int, C.c_int, C.c_int]),
     ("awg_graph_replays", C.c_longlong, []),

@@ -8,7 +8,7 @@
 // device's threading passes.
 //
 // Node names follow the reference: the new leaf takes the name nleaves, the node that had
-// it moves to nnodes (displaced), the new coalescence node is nnodes + 1. Child order is
+// it moves to nnodes (moved_id), the new coalescence node is nnodes + 1. Child order is
 // kept as the reference keeps it (it decides which child a later SPR replaces), so the
 // handle stores children next to parents.
 
@@ -54,21 +54,21 @@ void rename_node(Tree &t, int src, int dest) {
 // add_tree_branch (thread.cpp:39-101): the new leaf coalesces at (node, time)
 void add_tree_branch(Tree &t, int nnodes, int node, int time) {
     const int nleaves = (nnodes + 1) / 2;
-    const int newleaf = nleaves, displaced = nnodes, newcoal = nnodes + 1;
+    const int leaf_id = nleaves, moved_id = nnodes, join_id = nnodes + 1;
     t.nd.resize(nnodes + 2);
-    const int node2 = node != newleaf ? node : displaced;
+    const int target = node != leaf_id ? node : moved_id;
     const int parent = t.nd[node].parent;
-    const int parent2 = parent != newleaf ? parent : displaced;
-    if (newleaf < displaced) rename_node(t, newleaf, displaced);
-    t.nd[newleaf] = Node{newcoal, -1, -1, 0};
-    t.nd[newcoal] = Node{parent2, newleaf, node2, time};
-    t.nd[node2].parent = newcoal;
-    if (parent2 != -1) {
-        if (t.nd[parent2].c0 == node2) t.nd[parent2].c0 = newcoal;
-        else t.nd[parent2].c1 = newcoal;
+    const int target_up = parent != leaf_id ? parent : moved_id;
+    if (leaf_id < moved_id) rename_node(t, leaf_id, moved_id);
+    t.nd[leaf_id] = Node{join_id, -1, -1, 0};
+    t.nd[join_id] = Node{target_up, leaf_id, target, time};
+    t.nd[target].parent = join_id;
+    if (target_up != -1) {
+        if (t.nd[target_up].c0 == target) t.nd[target_up].c0 = join_id;
+        else t.nd[target_up].c1 = join_id;
     }
-    if (t.nd[newcoal].parent == -1) t.root = newcoal;
-    else t.root = t.root != newleaf ? t.root : displaced;
+    if (t.nd[join_id].parent == -1) t.root = join_id;
+    else t.root = t.root != leaf_id ? t.root : moved_id;
 }
 
 // apply_spr (local_tree.cpp:223-313)
@@ -129,38 +129,38 @@ bool state_of(const Tree &t, int nnodes, int T, int k, int &node, int &time) {
 // add_spr_branch (thread.cpp:176-269): the SPR into `t` and its mapping renamed for the
 // new leaf and coalescence node
 bool add_spr_branch(const Tree &t, const Tree &last, int state_node, int state_time,
-                    int last_node, int *spr, std::vector<int> &mapping, int newleaf,
-                    int displaced, int newcoal, int nnodes2) {
-    const int last_node2 = last_node != newleaf ? last_node : displaced;
-    const int node2 = state_node != newleaf ? state_node : displaced;
-    mapping[displaced] = mapping[newleaf];
-    mapping[newleaf] = newleaf;
-    mapping[newcoal] = newcoal;
-    for (int i = newleaf + 1; i < nnodes2; i++)
-        if (mapping[i] == newleaf) mapping[i] = displaced;
-    if (spr[0] == newleaf) spr[0] = displaced;
-    if (spr[2] == newleaf) spr[2] = displaced;
+                    int last_node, int *spr, std::vector<int> &mapping, int leaf_id,
+                    int moved_id, int join_id, int nnodes2) {
+    const int last_target = last_node != leaf_id ? last_node : moved_id;
+    const int target = state_node != leaf_id ? state_node : moved_id;
+    mapping[moved_id] = mapping[leaf_id];
+    mapping[leaf_id] = leaf_id;
+    mapping[join_id] = join_id;
+    for (int i = leaf_id + 1; i < nnodes2; i++)
+        if (mapping[i] == leaf_id) mapping[i] = moved_id;
+    if (spr[0] == leaf_id) spr[0] = moved_id;
+    if (spr[2] == leaf_id) spr[2] = moved_id;
     if (mapping[spr[0]] < 0) return false;
     const int recoal = t.nd[mapping[spr[0]]].parent;
-    if (recoal == newcoal) {
-        if (mapping[last_node2] == node2) {
-            spr[0] = newcoal;  // recombination above the coalescence state: renamed
+    if (recoal == join_id) {
+        if (mapping[last_target] == target) {
+            spr[0] = join_id;  // recombination above the coalescence state: renamed
         } else {
-            const int sn = state_node != newleaf ? state_node : displaced;
+            const int sn = state_node != leaf_id ? state_node : moved_id;
             if (sn == mapping[spr[0]]) {  // mediated coalescence
-                spr[2] = newleaf;
+                spr[2] = leaf_id;
                 spr[3] = state_time;
             }  // else the new branch escapes: nothing to rename
         }
-    } else if (recoal != -1 && (t.nd[recoal].c0 == newcoal || t.nd[recoal].c1 == newcoal)) {
-        if (last.nd[spr[2]].parent == newcoal) spr[2] = newcoal;
+    } else if (recoal != -1 && (t.nd[recoal].c0 == join_id || t.nd[recoal].c1 == join_id)) {
+        if (last.nd[spr[2]].parent == join_id) spr[2] = join_id;
     }
-    if (last.nd[spr[0]].parent == newcoal) {  // newcoal was the broken node
-        mapping[newcoal] = -1;
-        const int p = last.nd[newcoal].parent;
-        if (p != -1) mapping[p] = newcoal;
+    if (last.nd[spr[0]].parent == join_id) {  // join_id was the broken node
+        mapping[join_id] = -1;
+        const int p = last.nd[join_id].parent;
+        if (p != -1) mapping[p] = join_id;
     } else {  // follow a child without the recombination or coalescence down to a mapped node
-        int x = newcoal;
+        int x = join_id;
         for (int steps = 0;; steps++) {
             if (steps > nnodes2) return false;
             int y = last.nd[x].c0;
@@ -169,7 +169,7 @@ bool add_spr_branch(const Tree &t, const Tree &last, int state_node, int state_t
             if (x < 0) return false;
             if (mapping[x] != -1) break;
         }
-        mapping[newcoal] = t.nd[mapping[x]].parent;
+        mapping[join_id] = t.nd[mapping[x]].parent;
     }
     return true;
 }
@@ -180,7 +180,7 @@ bool add_arg_thread(ThreadTrees &a, int T, const int *path, int seqlen, const in
                     const int *rec_node, const int *rec_time, int nrec, std::string &err) {
     const int nnodes = a.nnodes, nnodes2 = nnodes + 2, B = a.ntrees;
     const int nleaves = (nnodes + 1) / 2;
-    const int newleaf = nleaves, displaced = nnodes, newcoal = nnodes + 1;
+    const int leaf_id = nleaves, moved_id = nnodes, join_id = nnodes + 1;
     long long total = 0;
     for (int b = 0; b < B; b++) total += a.blocklens[b];
     if (total != seqlen) {
@@ -257,8 +257,8 @@ bool add_arg_thread(ThreadTrees &a, int T, const int *path, int seqlen, const in
                 for (int i = 0; i < nnodes; i++) mapping[i] = i;
                 mapping[a.ptrees[(size_t)(b - 1) * nnodes + spr[0]]] = -1;
             }
-            if (!add_spr_branch(tree, last_tree, sn, st, last_node, spr, mapping, newleaf,
-                                displaced, newcoal, nnodes2)) {
+            if (!add_spr_branch(tree, last_tree, sn, st, last_node, spr, mapping, leaf_id,
+                                moved_id, join_id, nnodes2)) {
                 err = "add_arg_thread: inconsistent SPR between neighbouring trees";
                 return false;
             }
@@ -279,18 +279,18 @@ bool add_arg_thread(ThreadTrees &a, int T, const int *path, int seqlen, const in
             int spr2[4];
             spr2[0] = rec_node[irec];
             spr2[1] = rec_time[irec];
-            if (spr2[0] == newleaf) spr2[0] = displaced;
+            if (spr2[0] == leaf_id) spr2[0] = moved_id;
             if (spr2[0] == -1) {  // recombination on the new branch, coalescence as the thread
-                spr2[0] = newleaf;
+                spr2[0] = leaf_id;
                 spr2[2] = stn;
-                if (spr2[2] == newleaf) spr2[2] = displaced;
-                if (stn == ltn && stt > ltt) spr2[2] = newcoal;
+                if (spr2[2] == leaf_id) spr2[2] = moved_id;
+                if (stn == ltn && stt > ltt) spr2[2] = join_id;
             } else {  // recombination in the ARG, coalescence on the new branch
                 if (spr2[0] < 0 || spr2[0] >= nnodes2) {
                     err = "add_arg_thread: a recombination node out of range";
                     return false;
                 }
-                spr2[2] = stt > ltt ? cur.nd[newleaf].parent : newleaf;
+                spr2[2] = stt > ltt ? cur.nd[leaf_id].parent : leaf_id;
             }
             spr2[3] = stt;
             if (cur.nd[spr2[0]].parent < 0) {
@@ -318,7 +318,7 @@ bool add_arg_thread(ThreadTrees &a, int T, const int *path, int seqlen, const in
             err = "add_arg_thread: a path entry is not a state of its tree";
             return false;
         }
-        last_node = ln == newleaf ? displaced : ln;
+        last_node = ln == leaf_id ? moved_id : ln;
     }
     if (irec != nrec) {
         err = "add_arg_thread: a recombination outside the trees";
@@ -965,20 +965,20 @@ bool add_spr_branch_internal(const Tree &t, const Tree &last, NodeTime state, No
     const int n = (int)t.nd.size();
     auto ok = [n](int v) { return v >= 0 && v < n; };
     const int last_newcoal = last.nd[last_sub].parent;
-    int newcoal;
+    int join_id;
     if (state.node != -1) {
-        newcoal = t.nd[sub].parent;
+        join_id = t.nd[sub].parent;
     } else if (mapping[last_sub] != -1) {  // a whole tree
-        newcoal = t.nd[mapping[last_sub]].parent;
+        join_id = t.nd[mapping[last_sub]].parent;
     } else {
         const int sib = sibling(last, spr[0]);
         if (!ok(sib) || !ok(mapping[sib])) return false;
-        newcoal = t.nd[mapping[sib]].parent;
+        join_id = t.nd[mapping[sib]].parent;
     }
     if (!ok(last_newcoal) || !ok(mapping[spr[0]])) return false;
-    mapping[last_newcoal] = newcoal;
+    mapping[last_newcoal] = join_id;
     const int recoal = t.nd[mapping[spr[0]]].parent;
-    if (recoal == newcoal) {
+    if (recoal == join_id) {
         if (mapping[last_state.node] == state.node) {
             spr[0] = last_newcoal;  // the recombination is above the coalescence: renamed
         } else if (spr[3] == last.nd[last_newcoal].age && state.node == mapping[spr[0]]) {
@@ -986,13 +986,13 @@ bool add_spr_branch_internal(const Tree &t, const Tree &last, NodeTime state, No
             spr[2] = state.time < last.nd[last_sub].age ? sibling(last, spr[0]) : last_sub;
             spr[3] = state.time;
         }  // else the new branch escapes: nothing to rename
-    } else if (recoal != -1 && (t.nd[recoal].c0 == newcoal || t.nd[recoal].c1 == newcoal)) {
+    } else if (recoal != -1 && (t.nd[recoal].c0 == join_id || t.nd[recoal].c1 == join_id)) {
         if (last.nd[spr[2]].parent == last_newcoal) spr[2] = last_newcoal;
     }
     if (last.nd[spr[0]].parent == last_newcoal) {  // last_newcoal was the broken node
         mapping[last_newcoal] = -1;
         const int p = last.nd[last_newcoal].parent;
-        if (p != -1) mapping[p] = newcoal;
+        if (p != -1) mapping[p] = join_id;
     } else {  // a child of last_newcoal without the recombination or coalescence on it
         const int x = last_newcoal;
         int y = last.nd[x].c0;
@@ -1088,7 +1088,7 @@ bool add_thread_path(ThreadTrees &a, int T, int minage, const int *path, int seq
                 err = "add_arg_thread_path: a path entry is not a state of its tree";
                 return false;
             }
-            const int newcoal = cur.nd[sub].parent;
+            const int join_id = cur.nd[sub].parent;
             int spr2[4] = {rec_node[irec], rec_time[irec], -1, state.time};
             if (spr2[0] < 0 || spr2[0] >= n) {
                 err = "add_arg_thread_path: a recombination node out of range";
@@ -1096,7 +1096,7 @@ bool add_thread_path(ThreadTrees &a, int T, int minage, const int *path, int seq
             }
             if (spr2[0] == sub) {  // on the regrafted branch: coalescence as the thread
                 spr2[2] = state.node == last_state.node && state.time > last_state.time
-                              ? newcoal : state.node;
+                              ? join_id : state.node;
             } else {  // in the main tree: coalescence on the regrafted branch
                 spr2[2] = state.time > last_state.time ? cur.nd[sub].parent : sub;
             }

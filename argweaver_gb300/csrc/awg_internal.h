@@ -72,6 +72,8 @@ struct StateInfo {
 // Device views of a batch (all pointers are device memory).
 struct BatchDev {
     int ninst, nblocks, maxS, maxT, maxnodes, maxM;
+    int var64;                   // FP32 path: every variant column's emissions formed in
+                                 // FP64 and rounded once (implies emit64)
     int emit64;                  // some instance forms FP64 emission partials even on the
                                  // FP32 path (internal-branch or infinite-sites problems)
     const InstDev *inst;
@@ -129,6 +131,8 @@ struct BatchDev {
     double *lnl;                 // [ninst] sum of log column norms
     double *post;                // posterior marginals (optional)
     const double *uniforms;      // [total columns] traceback draws
+    const int *last_state;       // [ninst] or NULL: FP64 traceback's given last state (-1:
+                                 // sampled as usual)
     int *path;                   // [total columns]
     int *err;                    // [4] first failure: code, instance, block, column
 };

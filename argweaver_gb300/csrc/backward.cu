@@ -283,11 +283,8 @@ void launch(const BatchDev &d, double *bw_out, cudaStream_t s) {
     const size_t smem = 3 * (size_t)maxS * sizeof(F) + 2 * (size_t)maxS * sizeof(float) + 16 +
                         (size_t)maxS * (sizeof(Meta) + sizeof(int)) + sizeof(int) + 16 +
                         ((size_t)maxS / 32 + 1) * sizeof(F);
-    static size_t configured = 0;
-    if (smem > configured) {  // opt in; static shared memory counts against 48 KB too
-        if (cudaFuncSetAttribute(k_backward<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return;
-        configured = smem;
-    }
+    // opt in; static shared memory counts against 48 KB too
+    if (!raise_dynamic_smem(k_backward<F>, smem)) return;
     k_backward<F><<<d.ninst, backward_threads(maxS), smem, s>>>(d, maxS, bw_out);
     note_launch();
 }

@@ -14,6 +14,7 @@
 #include <cstring>
 #include <map>
 #include <mutex>
+#include <set>
 #include <vector>
 
 #include "engine.h"
@@ -157,6 +158,30 @@ struct Layout {
 long long kernel_launch_count() { return g_launches.load(); }
 void note_launch() { g_launches.fetch_add(1); }
 
+namespace {
+std::mutex g_attr_mu;
+std::map<const void *, size_t> g_smem_limit;  // kernel -> dynamic shared memory opted in
+std::set<const void *> g_carveout;            // kernels given the largest carveout
+}  // namespace
+
+void prefer_shared_fn(const void *kernel) {
+    std::lock_guard<std::mutex> lock(g_attr_mu);
+    if (g_carveout.insert(kernel).second)
+        cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared);
+}
+
+bool raise_dynamic_smem_fn(const void *kernel, size_t bytes) {
+    std::lock_guard<std::mutex> lock(g_attr_mu);
+    size_t &cur = g_smem_limit[kernel];
+    if (bytes <= cur) return true;
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) !=
+        cudaSuccess)
+        return false;
+    cur = bytes;
+    return true;
+}
+
 // Plans, uploads and enqueues one batch on context C. Synchronous (async false): outputs go
 // straight to the caller's buffers and the call returns when they are there. Asynchronous:
 // outputs go to C's page-locked staging, C.done marks their arrival, and ctx_complete (on
@@ -169,6 +194,7 @@ int ctx_launch(Ctx &C, const awg_problem *probs, awg_outputs *outs, int n, const
     Engine &E = engine();
     const bool fp32 = opt.precision == AWG_FP32;
     if (!fp32 && opt.precision != AWG_FP64) { err = "precision must be AWG_FP64 or AWG_FP32"; return -1; }
+    if (fp32 && opt.last_states) { err = "a given last traceback state needs AWG_FP64"; return -1; }
 
     HostPlan &plan = C.plan;
     plan = HostPlan();
@@ -228,6 +254,7 @@ int ctx_launch(Ctx &C, const awg_problem *probs, awg_outputs *outs, int n, const
     const size_t o_order = in.add(sizeof(int) * plan.ninst);
     const size_t o_blkmap = in.add(sizeof(int) * plan.nblocks);
     const size_t o_u = in.add(want_path ? sizeof(double) * COLS : 0);
+    const size_t o_last = in.add(want_path && opt.last_states ? sizeof(int) * plan.ninst : 0);
     const size_t in_bytes = in.total;
 
     char *h = C.host;
@@ -302,7 +329,7 @@ int ctx_launch(Ctx &C, const awg_problem *probs, awg_outputs *outs, int n, const
     const size_t o_bw = w.add(want_bw ? sizeof(double) * CELLS : 0);
     const size_t o_path = w.add(want_path ? sizeof(int) * COLS : 0);
     // FP32 traceback: the forward columns' time-bin sums
-    const bool want_bins = fp32 && want_path && forward_writes_bins(plan.maxS, cfg.kpt);
+    const bool want_bins = fp32 && want_path && forward_writes_bins(plan.maxS, plan.maxM, plan.maxT, cfg.kpt);
     const size_t o_bins = w.add(want_bins ? sizeof(float) * MAXT * COLS : 0);
     const size_t o_err = w.add(4 * sizeof(int));
     const size_t o_queue = w.add(sizeof(int) * 2 * MAXG);  // work counters of the groups
@@ -349,6 +376,7 @@ int ctx_launch(Ctx &C, const awg_problem *probs, awg_outputs *outs, int n, const
             for (int b = 0; b < I.ntrees; b++) bm[k++] = I.block0 + b;
         }
     }
+    if (want_path && opt.last_states) memcpy(h + o_last, opt.last_states, sizeof(int) * n);
     if (want_path) {
         double *u = (double *)(h + o_u);
         for (int q = 0; q < n; q++) {
@@ -369,6 +397,8 @@ int ctx_launch(Ctx &C, const awg_problem *probs, awg_outputs *outs, int n, const
     d.maxnodes = plan.maxnodes;
     d.maxM = plan.maxM;
     d.emit64 = 0;
+    d.var64 = getenv("AWG_VAREMIT_F64") && atoi(getenv("AWG_VAREMIT_F64")) == 1;
+    if (d.var64) d.emit64 = 1;
     for (int i = 0; i < plan.ninst; i++)
         if (plan.inst[i].internal || plan.model[(size_t)i * MODEL_STRIDE + M_CONST + 3] < 1.0)
             d.emit64 = 1;
@@ -415,6 +445,7 @@ int ctx_launch(Ctx &C, const awg_problem *probs, awg_outputs *outs, int n, const
     d.lnl = (double *)(D + o_lnl);
     d.post = want_post ? (double *)(D + o_post) : nullptr;
     d.uniforms = want_path ? (const double *)(D + o_u) : nullptr;
+    d.last_state = want_path && opt.last_states ? (const int *)(D + o_last) : nullptr;
     d.path = want_path ? (int *)(D + o_path) : nullptr;
     d.bins32 = want_bins ? (float *)(D + o_bins) : nullptr;
     d.err = (int *)(D + o_err);
@@ -430,7 +461,7 @@ int ctx_launch(Ctx &C, const awg_problem *probs, awg_outputs *outs, int n, const
     // per-tree work of later groups fills the SMs they leave idle. The per-tree kernels are
     // persistent, work-stealing over units of trees; the device part of a step is captured
     // once as a CUDA graph and replayed while its launch parameters repeat.
-    const bool special = opt.tables_only || opt.priors;
+    const bool special = opt.tables_only || opt.priors || opt.last_states;
     const bool serial_timing = timing == 2;
     const bool pipelined = n >= 16 && !special && !serial_timing;
     const bool T = timing != 0;
@@ -533,7 +564,7 @@ int ctx_launch(Ctx &C, const awg_problem *probs, awg_outputs *outs, int n, const
                                           want_post, want_bw, want_bins, plan.ninst, plan.nblocks,
                                           plan.maxS, plan.maxT, plan.maxnodes, plan.maxM,
                                           cfg.kpt, cfg.chunk, cfg.group_div, cfg.persistent, ng,
-                                          (long long)total, d.emit64};
+                                          (long long)total, d.emit64, d.var64};
             for (size_t o : {o_inst, o_blocks, o_model, o_nodes, o_map, o_seq, o_cls, o_cvar,
                              o_order, o_blkmap, o_u, o_sinfo, o_t2off, o_btptr, o_btperm, o_tm,
                              o_gts, o_inv, o_det, o_detp, o_srcs, o_rrow, o_crow, o_gptr, o_gidx,

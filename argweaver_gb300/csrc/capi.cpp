@@ -178,6 +178,52 @@ extern "C" {
 
 const char *awg_last_error(void) { return g_err.c_str(); }
 
+int awg_sample_path_conditioned(const awg_problem *p, const double *prior, int last_state,
+                                const double *uniforms, int *path, double *loglik) {
+    g_err.clear();
+    if (!p || !path) {
+        g_err = "awg_sample_path_conditioned: NULL problem or path";
+        return -1;
+    }
+    if (awg_problem_cells(p) < 0) return -1;
+    if (last_state >= 0) {
+        const int b = p->ntrees - 1;
+        const int S = awg::count_states(p->ptrees + (size_t)b * p->nnodes,
+                                        p->ages + (size_t)b * p->nnodes, p->nnodes, p->ntimes,
+                                        p->internal != 0, p->minage,
+                                        p->root_child0 ? p->root_child0[b] : -1, nullptr);
+        if (last_state >= std::max(S, 1)) {
+            g_err = "awg_sample_path_conditioned: last_state " + std::to_string(last_state) +
+                    " is not a state of the last tree (" + std::to_string(std::max(S, 1)) + ")";
+            return -1;
+        }
+    }
+    awg_outputs o;
+    memset(&o, 0, sizeof(o));
+    o.path = path;
+    o.loglik = loglik;
+    std::vector<double> u;
+    if (uniforms) {
+        o.uniforms = uniforms;
+    } else {
+        // the reference's draws: one rand() per column, last column first; a given last
+        // state takes none (stochastic_traceback, sample_thread.cpp:532-539)
+        u.assign(p->seqlen, 0.0);
+        for (int c = p->seqlen - (last_state >= 0 ? 2 : 1); c >= 0; c--) u[c] = rand() / double(RAND_MAX);
+        o.uniforms = u.data();
+    }
+    awg::RunOptions opt;
+    opt.precision = AWG_FP64;
+    const double *priors[1] = {prior};
+    if (prior) opt.priors = priors;
+    const int last[1] = {last_state};
+    opt.last_states = last;
+    std::string err;
+    const int rc = awg::run_batch(p, &o, 1, opt, err);
+    if (rc != 0) set_error(err);
+    return rc;
+}
+
 long long awg_kernel_launches(void) { return awg::kernel_launch_count(); }
 
 int awg_device_name(char *buf, int len) {

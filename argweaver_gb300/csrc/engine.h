@@ -22,6 +22,8 @@ struct RunOptions {
     const TuneCfg *cfg = nullptr;  // explicit schedule (the autotuner's trials), else tuned
     int precision = AWG_FP64;
     const double *const *priors = nullptr;  // per problem: given column-0 prior, or NULL
+    const int *last_states = nullptr;       // per problem: the traceback's given last state
+                                            // (FP64 only), or -1 to sample it
     double *const *backward = nullptr;      // per problem: backward table output, or NULL
     // Debug: stop after the table kernel and copy its FP64 tables of problem 0 out:
     // tmatrix [ntrees][T-1][T-1], same-branch rows [sum M], invariant emissions

@@ -189,59 +189,59 @@ bool read_sites(FILE *f, Sites &s, int sub_start, int sub_end) {
 }
 
 struct SitesMapping {
-    int old_start = 0, old_end = 0, new_start = 0, new_end = 0;
-    std::vector<int> old_sites, new_sites, all_sites;
+    int src_start = 0, src_end = 0, dst_start = 0, dst_end = 0;
+    std::vector<int> src_pos, dst_col, kept_pos;
 };
 
 // find_compress_cols (sequences.cpp:523-592): every variant column is kept; the others
 // are represented by one column per `compress` bases
 bool find_compress_cols(const Sites &s, int compress, SitesMapping &m) {
     const int ncols = (int)s.positions.size();
-    m.old_start = s.start_coord;
-    m.old_end = s.end_coord;
+    m.src_start = s.start_coord;
+    m.src_end = s.end_coord;
     if (compress == 1) {
-        for (int i = s.start_coord; i < s.end_coord; i++) m.all_sites.push_back(i);
+        for (int i = s.start_coord; i < s.end_coord; i++) m.kept_pos.push_back(i);
         for (int i = 0; i < ncols; i++) {
-            m.old_sites.push_back(s.positions[i]);
-            m.new_sites.push_back(s.positions[i] - s.start_coord);
+            m.src_pos.push_back(s.positions[i]);
+            m.dst_col.push_back(s.positions[i] - s.start_coord);
         }
-        m.new_start = 0;
-        m.new_end = s.end_coord - s.start_coord;
+        m.dst_start = 0;
+        m.dst_end = s.end_coord - s.start_coord;
         return true;
     }
-    int blocki = 0, next_block = s.start_coord + compress;
-    const int half_block = compress / 2;
+    int ncol = 0, block_end = s.start_coord + compress;
+    const int half = compress / 2;
     for (int i = 0; i < ncols; i++) {
         const int col = s.positions[i];
-        while (col >= next_block) {
-            m.all_sites.push_back(next_block - half_block);
-            next_block += compress;
-            blocki++;
+        while (col >= block_end) {
+            m.kept_pos.push_back(block_end - half);
+            block_end += compress;
+            ncol++;
         }
-        m.old_sites.push_back(col);
-        m.new_sites.push_back(blocki);
-        m.all_sites.push_back(col);
-        next_block += compress;
-        blocki++;
-        if (next_block - compress > s.end_coord && i != ncols - 1) return false;
+        m.src_pos.push_back(col);
+        m.dst_col.push_back(ncol);
+        m.kept_pos.push_back(col);
+        block_end += compress;
+        ncol++;
+        if (block_end - compress > s.end_coord && i != ncols - 1) return false;
     }
-    while (s.end_coord >= next_block) {
-        m.all_sites.push_back(next_block - half_block);
-        next_block += compress;
-        blocki++;
+    while (s.end_coord >= block_end) {
+        m.kept_pos.push_back(block_end - half);
+        block_end += compress;
+        ncol++;
     }
-    m.new_start = 0;
-    const int new_end = (s.end_coord - s.start_coord) / compress;
-    m.new_end = ncols > 0 ? std::max(m.new_sites[ncols - 1] + 1, new_end) : new_end;
+    m.dst_start = 0;
+    const int dst_end = (s.end_coord - s.start_coord) / compress;
+    m.dst_end = ncols > 0 ? std::max(m.dst_col[ncols - 1] + 1, dst_end) : dst_end;
     return true;
 }
 
 // compress_sites + make_sequences_from_sites (sequences.cpp:315-343,598-606): variant
 // columns at their compressed positions, every other column the default base 'A'
 void make_sequences(Sites &s, const SitesMapping &m, awg_arg_input &in) {
-    for (size_t i = 0; i < s.positions.size(); i++) s.positions[i] = m.new_sites[i];
-    s.start_coord = m.new_start;
-    s.end_coord = m.new_end;
+    for (size_t i = 0; i < s.positions.size(); i++) s.positions[i] = m.dst_col[i];
+    s.start_coord = m.dst_start;
+    s.end_coord = m.dst_end;
     const int nseqs = (int)s.names.size(), L = s.end_coord - s.start_coord;
     in.names = s.names;
     in.chrom = s.chrom;
@@ -555,18 +555,18 @@ awg_arg_input *awg_read_arg_input(const char *sites_path, const char *smc_path, 
     // (sequences.h:300-322)
     std::vector<int> bl2;
     {
-        int cur = mp.new_start;
-        const int new_seqlen = mp.new_end - mp.new_start;
-        int end = mp.old_start;
+        int cur = mp.dst_start;
+        const int new_seqlen = mp.dst_end - mp.dst_start;
+        int end = mp.src_start;
         for (int b = 0; b < B; b++) {
             end += s.blocklens[b];
-            if (end < mp.old_end) {
+            if (end < mp.src_end) {
                 int cur2 = cur;
-                while (cur2 < new_seqlen && mp.all_sites[cur2] < end) cur2++;
+                while (cur2 < new_seqlen && mp.kept_pos[cur2] < end) cur2++;
                 bl2.push_back(cur2 - cur);
                 cur = cur2;
             } else {
-                bl2.push_back(mp.new_end - cur);
+                bl2.push_back(mp.dst_end - cur);
             }
         }
         for (int b = 0; b < B; b++)

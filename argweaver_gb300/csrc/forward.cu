@@ -816,11 +816,8 @@ void launch_old(const BatchDev &d, int maxM, cudaStream_t s) {
     int t2_in_smem = forward_smem<F>(maxS, maxM) <= 200 * 1024;
     if (!t2_in_smem) maxM = 1;
     const size_t smem = forward_smem<F>(maxS, maxM);
-    static size_t configured = 0;
-    if (smem > configured) {  // opt in; static shared memory counts against 48 KB too
-        if (cudaFuncSetAttribute(k_forward<F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return;
-        configured = smem;
-    }
+    // opt in; static shared memory counts against 48 KB too
+    if (!raise_dynamic_smem(k_forward<F>, smem)) return;
     k_forward<F><<<d.ninst, forward_threads(maxS), smem, s>>>(d, maxS, maxM, t2_in_smem);
     note_launch();
 }
@@ -833,13 +830,7 @@ void launch_reg(const BatchDev &d, int nt, cudaStream_t s) {
     const int t2_in_smem = bytes(maxM) <= 200 * 1024;
     if (!t2_in_smem) maxM = 1;
     const size_t smem = bytes(maxM);
-    static size_t configured = 0;
-    if (smem > configured) {
-        if (cudaFuncSetAttribute(k_forward_reg<F, KPT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem) != cudaSuccess)
-            return;
-        configured = smem;
-    }
+    if (!raise_dynamic_smem(k_forward_reg<F, KPT>, smem)) return;
     k_forward_reg<F, KPT><<<d.ninst, nt, smem, s>>>(d, maxS, maxM, t2_in_smem);
     note_launch();
 }
@@ -874,7 +865,9 @@ void launch(const BatchDev &d, cudaStream_t s, int want_kpt) {
 
 }  // namespace
 
-bool forward_writes_bins(int maxS, int kpt) {
+bool forward_writes_bins(int maxS, int maxM, int maxT, int kpt) {
+    (void)maxM;
+    (void)maxT;
     const int k = reg_kpt(imax(maxS, 1), kpt);
     return 32 * NRW + imax(32, ((imax(maxS, 1) + k - 1) / k + 31) / 32 * 32) <= 512;
 }

@@ -21,24 +21,30 @@ void launch_varemit(const BatchDev &d, bool want32, cudaStream_t s, int *queue =
 // K3: forward pass, one CTA per instance; kpt: states per owner thread of the
 // register-resident variant (0: chosen by the state count).
 void launch_forward(const BatchDev &d, bool fp32, cudaStream_t s, int kpt = 0);
-// Whether K3 writes the FP32 columns' time-bin sums (BatchDev::bins32) at this state count
-// (the register-resident variant does; the fallback for the largest trees does not).
-bool forward_writes_bins(int maxS, int kpt = 0);
+// Whether K3 writes the FP32 columns' time-bin sums (BatchDev::bins32) for a batch of these
+// largest sizes (the register-resident variant does; the fallback for the largest trees
+// does not).
+bool forward_writes_bins(int maxS, int maxM, int maxT, int kpt = 0);
 // K4: stochastic traceback, one warp per instance; FP32 with bins32 set: the decomposed draw.
 void launch_traceback(const BatchDev &d, bool fp32, cudaStream_t s);
 // K5: backward pass fused with the posterior marginals, one CTA per instance.
 void launch_backward(const BatchDev &d, bool fp32, double *bw_out, cudaStream_t s);
 
-// Asks for the largest shared-memory carveout for a kernel (once per kernel): the default
-// carveout can leave room for fewer CTAs per SM than the registers and threads allow.
+// Kernel attributes, set once per kernel and safe to call from several host threads (the
+// serving loop launches from one thread per batch slot).
+// Asks for the largest shared-memory carveout for a kernel: the default carveout can leave
+// room for fewer CTAs per SM than the registers and threads allow.
+void prefer_shared_fn(const void *kernel);
 template <typename K>
 inline void prefer_shared(K kernel) {
-    static bool done = false;
-    if (!done) {
-        cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
-                             (int)cudaSharedmemCarveoutMaxShared);
-        done = true;
-    }
+    prefer_shared_fn((const void *)kernel);
+}
+// Raises a kernel's dynamic shared-memory limit to at least `bytes` (the limit only grows).
+// False when the runtime refuses (the launch then reports the error).
+bool raise_dynamic_smem_fn(const void *kernel, size_t bytes);
+template <typename K>
+inline bool raise_dynamic_smem(K kernel, size_t bytes) {
+    return raise_dynamic_smem_fn((const void *)kernel, bytes);
 }
 
 // Count of kernels launched by this library (process-wide).

@@ -136,7 +136,7 @@ struct awg_server {
     bool stop = false;
     std::thread worker;
     // statistics
-    std::vector<double> lat_ms;
+    std::vector<double> lat_ms, queue_ms, service_ms;  // per completed request
     long long submitted = 0, completed = 0, failed = 0, cells_done = 0;
     double t_first = -1.0, t_last = 0.0;
     int inflight = 0, inflight_max = 0;
@@ -193,6 +193,8 @@ void slot_main(awg_server *S, int si) {
                 S->completed++;
                 S->cells_done += r->cells;
                 S->lat_ms.push_back(1e3 * (r->t_done - r->t_submit));
+                S->queue_ms.push_back(1e3 * (r->t_start - r->t_submit));
+                S->service_ms.push_back(1e3 * (r->t_done - r->t_start));
             } else {
                 r->status = rc;
                 r->err = err;
@@ -476,21 +478,24 @@ int awg_server_stats_get(awg_server *S, awg_server_stats *out) {
     out->busy_s = S->busy_s + (S->inflight > 0 && S->busy_since >= 0 ? now_s() - S->busy_since : 0.0);
     out->span_s = S->t_first >= 0 ? S->t_last - S->t_first : 0.0;
     out->launch_s = S->launch_s;
-    if (!S->lat_ms.empty()) {
-        std::vector<double> v = S->lat_ms;
+    auto pct = [](std::vector<double> v, double q) {
         std::sort(v.begin(), v.end());
-        auto pct = [&](double q) {
-            const double x = q * (v.size() - 1);
-            const size_t i = (size_t)x;
-            const double f = x - i;
-            return i + 1 < v.size() ? v[i] * (1 - f) + v[i + 1] * f : v[i];
-        };
-        out->p50_ms = pct(0.50);
-        out->p99_ms = pct(0.99);
-        out->max_ms = v.back();
+        const double x = q * (v.size() - 1);
+        const size_t i = (size_t)x;
+        const double f = x - i;
+        return i + 1 < v.size() ? v[i] * (1 - f) + v[i + 1] * f : v[i];
+    };
+    if (!S->lat_ms.empty()) {
+        out->p50_ms = pct(S->lat_ms, 0.50);
+        out->p99_ms = pct(S->lat_ms, 0.99);
+        out->max_ms = *std::max_element(S->lat_ms.begin(), S->lat_ms.end());
         double s = 0;
-        for (double x : v) s += x;
-        out->mean_ms = s / v.size();
+        for (double x : S->lat_ms) s += x;
+        out->mean_ms = s / S->lat_ms.size();
+        out->queue_p50_ms = pct(S->queue_ms, 0.50);
+        out->queue_p99_ms = pct(S->queue_ms, 0.99);
+        out->service_p50_ms = pct(S->service_ms, 0.50);
+        out->service_p99_ms = pct(S->service_ms, 0.99);
     }
     return 0;
 }

@@ -26,9 +26,10 @@ constexpr int MAX_DEVICES = 64;
 
 __device__ __align__(256) unsigned char g_scratch[SCRATCH_BYTES];
 
-// Device address of g_scratch, resolved once per device with that device current.
+// Device address of g_scratch. The first call on a device (that device current) loads the
+// module holding the array; every call then resolves the address again, because a context
+// destroyed and recreated in between (cudaDeviceReset) reloads the module and may move it.
 std::mutex g_setup_mu;
-char *g_scratch_ptr[MAX_DEVICES] = {};
 
 struct Carve {
     size_t total = 0;
@@ -115,7 +116,7 @@ int run_static(const awg_problem *p, awg_outputs *out, int precision, cudaStream
         return -5;
     }
 
-    // ---------------- the scratch's device address, once per device
+    // ---------------- the scratch's device address in the current context
     int dev = -1, ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
         err = "no CUDA device: the threading HMM runs on the GPU only";
@@ -128,17 +129,14 @@ int run_static(const awg_problem *p, awg_outputs *out, int precision, cudaStream
     char *D;
     {
         std::lock_guard<std::mutex> lock(g_setup_mu);
-        if (!g_scratch_ptr[dev]) {
-            void *ptr = nullptr;
-            const cudaError_t rc = cudaGetSymbolAddress(&ptr, g_scratch);
-            if (rc != cudaSuccess || !ptr) {
-                err = std::string("awg_forward_static: cudaGetSymbolAddress of the static "
-                                  "scratch failed: ") + cudaGetErrorString(rc);
-                return -3;
-            }
-            g_scratch_ptr[dev] = (char *)ptr;
+        void *ptr = nullptr;
+        const cudaError_t rc = cudaGetSymbolAddress(&ptr, g_scratch);
+        if (rc != cudaSuccess || !ptr) {
+            err = std::string("awg_forward_static: cudaGetSymbolAddress of the static "
+                              "scratch failed: ") + cudaGetErrorString(rc);
+            return -3;
         }
-        D = g_scratch_ptr[dev];
+        D = (char *)ptr;
     }
 
     BatchDev d;
@@ -192,11 +190,14 @@ int run_static(const awg_problem *p, awg_outputs *out, int precision, cudaStream
     d.lnl = (double *)(D + o_lnl);
     d.err = (int *)(D + o_err);
 
+    // On an error after work was enqueued, the stream is drained before returning, so no
+    // work of this call is left running on the shared array.
 #define SCK(x)                                                                        \
     do {                                                                              \
         const cudaError_t rc_ = (x);                                                  \
         if (rc_ != cudaSuccess) {                                                     \
             err = std::string("awg_forward_static: " #x ": ") + cudaGetErrorString(rc_); \
+            (void)cudaStreamSynchronize(s);                                           \
             return -3;                                                                \
         }                                                                             \
     } while (0)

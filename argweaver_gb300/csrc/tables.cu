@@ -1703,12 +1703,12 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
                 if (penalised) penalise(eb);
                 double *row = d.varemit + B.var0 + (size_t)vrow * S;
                 for (int k = lane; k < S; k += 32) row[k] = eb[k];
-            } else if (penalised) {
+            } else if (penalised || d.var64) {
                 // FP64 emissions, penalised, then relative to the column's largest
                 const int X0 = 0;
                 emit_column<double, EM_F64>(ctx, chars, X0, (double (*)[4])wscr,
                                             (double (*)[4])wscr + n, eb);
-                penalise(eb);
+                if (penalised) penalise(eb);
                 double eref = 0.0;
                 for (int k = lane; k < S; k += 32) eref = fmax(eref, eb[k]);
 #pragma unroll
@@ -1837,13 +1837,10 @@ size_t tables_smem(int n, int S, int S1, int T, bool want32) {
 // unit of work.
 template <typename K>
 int persistent_grid(K kernel, int threads, size_t smem, int nunits) {
-    static int sms = 0;
-    if (!sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms <= 0) sms = 1;
-    }
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess || per_sm < 1)
         per_sm = 1;
@@ -1852,20 +1849,14 @@ int persistent_grid(K kernel, int threads, size_t smem, int nunits) {
 
 void launch_tables(const BatchDev &d, bool want32, cudaStream_t s, int *queue, int chunk) {
     size_t smem = tables_smem(d.maxnodes, d.maxS, d.maxS, d.maxT, want32);
-    static size_t configured = 0, configured_ws = 0;
     if (!queue) {
         prefer_shared(k_tables);
-        if (smem > configured) {  // opt in; static shared memory counts against 48 KB too
-            if (cudaFuncSetAttribute(k_tables, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return;
-            configured = smem;
-        }
+        // opt in; static shared memory counts against 48 KB too
+        if (!raise_dynamic_smem(k_tables, smem)) return;
         k_tables<<<d.nblocks, TAB_THREADS, smem, s>>>(d, want32 ? 1 : 0);
     } else {
         prefer_shared(k_tables_ws);
-        if (smem > configured_ws) {
-            if (cudaFuncSetAttribute(k_tables_ws, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return;
-            configured_ws = smem;
-        }
+        if (!raise_dynamic_smem(k_tables_ws, smem)) return;
         chunk = imax(chunk, 1);
         const WorkQueue q{queue, (d.nblocks + chunk - 1) / chunk, chunk};
         const int grid = persistent_grid(k_tables_ws, TAB_THREADS, smem, q.nunits);
@@ -1896,20 +1887,14 @@ void launch_varemit_t(const BatchDev &d, cudaStream_t s, int *queue, int chunk) 
     };
     while (nwarps > 1 && need(nwarps) > 200 * 1024) nwarps--;
     const size_t smem = need(nwarps);
-    static size_t configured = 0, configured_ws = 0;
     if (!queue) {
         prefer_shared(k_varemit<FP32OUT>);
-        if (smem > configured) {  // opt in; static shared memory counts against 48 KB too
-            if (cudaFuncSetAttribute(k_varemit<FP32OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return;
-            configured = smem;
-        }
+        // opt in; static shared memory counts against 48 KB too
+        if (!raise_dynamic_smem(k_varemit<FP32OUT>, smem)) return;
         k_varemit<FP32OUT><<<d.nblocks, nwarps * 32, smem, s>>>(d, nwarps, maxS, (int)smem);
     } else {
         prefer_shared(k_varemit_ws<FP32OUT>);
-        if (smem > configured_ws) {
-            if (cudaFuncSetAttribute(k_varemit_ws<FP32OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return;
-            configured_ws = smem;
-        }
+        if (!raise_dynamic_smem(k_varemit_ws<FP32OUT>, smem)) return;
         chunk = imax(chunk, 1);
         const WorkQueue q{queue, (d.nblocks + chunk - 1) / chunk, chunk};
         const int grid = persistent_grid(k_varemit_ws<FP32OUT>, nwarps * 32, smem, q.nunits);

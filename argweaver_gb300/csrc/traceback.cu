@@ -181,7 +181,10 @@ __global__ void k_traceback(BatchDev d, int maxS, int slot_elems) {
         cp_wait<DEPTH - 1>();
         __syncwarp();
         const F *c = column(Bl, col);
-        const int x = warp_sample<F>(imax(Bl.S, 1), uring[col % DEPTH], [&](int j) { return c[j]; });
+        // a given last state (conditioned sampling) takes no draw
+        const int given = d.last_state ? d.last_state[qi] : -1;
+        const int x = given >= 0 ? given
+                                 : warp_sample<F>(imax(Bl.S, 1), uring[col % DEPTH], [&](int j) { return c[j]; });
         if (lane == 0) path[col] = x;
         state = x;
         __syncwarp();
@@ -859,14 +862,8 @@ bool launch_split(const BatchDev &d, cudaStream_t s, size_t budget) {
     const size_t smem = (size_t)NCH * chunk_tab_bytes(maxS) + (size_t)NCH * CW * MAXT * sizeof(float) +
                         (size_t)NCH * (CW + 2) * sizeof(double) + 2 * (size_t)TreeBufLayout(maxS).total;
     if (smem > budget) return false;
-    static size_t configured = 0;
     prefer_shared(k_traceback_split<NCH>);
-    if (smem > configured) {
-        if (cudaFuncSetAttribute(k_traceback_split<NCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem) != cudaSuccess)
-            return true;  // the launch reports the error
-        configured = smem;
-    }
+    if (!raise_dynamic_smem(k_traceback_split<NCH>, smem)) return true;  // the launch reports it
     k_traceback_split<NCH><<<d.ninst, 32, smem, s>>>(d, maxS);
     note_launch();
     return true;
@@ -879,13 +876,8 @@ bool launch_cfg(const BatchDev &d, cudaStream_t s, size_t budget) {
     const size_t smem = (size_t)DEPTH * slot_elems * sizeof(F) + DEPTH * sizeof(double) +
                         (size_t)(maxS + 1) * sizeof(F) + 2 * (size_t)maxS * sizeof(int) + 16;
     if (smem > budget) return false;
-    static size_t configured = 0;
-    if (smem > configured) {  // opt in; static shared memory counts against 48 KB too
-        if (cudaFuncSetAttribute(k_traceback<F, G, DEPTH>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-            return true;  // the launch reports the error
-        configured = smem;
-    }
+    // opt in; static shared memory counts against 48 KB too
+    if (!raise_dynamic_smem(k_traceback<F, G, DEPTH>, smem)) return true;  // the launch reports it
     k_traceback<F, G, DEPTH><<<d.ninst, 32, smem, s>>>(d, maxS, slot_elems);
     note_launch();
     return true;

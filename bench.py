@@ -149,6 +149,25 @@ def cpu_reference(problems, seconds: float, threads: int):
     return done_cells[0] / dt, done_cells[0], dt
 
 
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return "unknown"
+
+
 def _sim_pool(specs):
     """Problems simulated in parallel from (nleaves, columns, seed, ntimes, missing) specs."""
     from argweaver_gb300.sim import simulate
@@ -219,7 +238,13 @@ def _c0(rng):
     fw, _ = pyoracle.forward(p0)
     pyoracle.traceback(p0, fw, np.random.default_rng(1).random(p0.seqlen))
     cpu_ms = 1e3 * (time.perf_counter() - t0)
+    from argweaver_gb300 import api
+    api.set_timing(2)
+    api.run_batch([p0], precision="fp64", want_forward=False, want_path=True)
+    phases = api.last_timings()
+    api.set_timing(0)
     return {
+        "phase_ms": phases,
         "workload": "k=8 (7 + 1 threaded), 10,000 columns, ntimes=20, FP64, one "
                     "arghmm_sample_posterior call (reference C ABI)",
         "cells": int(p0.cells()), "p50_ms": float(np.percentile(lat, 50)),
@@ -256,14 +281,34 @@ def _c2(rng):
     return c2
 
 
-def _c3(rng):
-    from argweaver_gb300 import api
-    from argweaver_gb300.sim import leaf_cut
+def _cut_one(spec):
+    """One config-3 instance: a seeded k = 50 ARG cut along a uniform removal path drawn
+    after srand(seed) (arg-sample's subtree cut), as an internal-branch problem. Runs in a
+    worker process: the removal path draws from libc rand(), which is process-wide."""
+    from argweaver_gb300 import refapi
+    from argweaver_gb300.sim import simulate
 
-    # ---- c3: 128 internal-branch instances, k = 50, 2 Mb = 2e5 columns, missing ~U[0,2%]
-    specs = [(49, 200000, int(rng.integers(1, 2**62)), 20, float(rng.uniform(0, 0.02)))
+    nleaves, L, seed, miss = spec
+    full = simulate(nleaves, L, seed, compress=10, ntimes=20, maxtime=200e3, popsize=1e4,
+                    rho=1.6e-8, mu=1.8e-8, missing=miss, add_thread=False)
+    refapi.srand(seed % 2**31)
+    path, _ = refapi.sample_arg_removal_path_uniform(full)
+    return refapi.as_problem(full, refapi.remove_arg_thread_path(full, path), internal=True)
+
+
+def _c3(rng):
+    import multiprocessing as mp
+
+    from argweaver_gb300 import api
+
+    # ---- c3: 128 internal-branch instances, k = 50, 2 Mb = 2e5 columns, missing ~U[0,2%],
+    # each a random subtree cut along a uniform removal path (built off the clock, in
+    # worker processes started with spawn)
+    specs = [(50, 200000, int(rng.integers(1, 2**62)), float(rng.uniform(0, 0.02)))
              for _ in range(128)]
-    p3 = [leaf_cut(p) for p in _sim_pool(specs)]
+    with cf.ProcessPoolExecutor(max_workers=min(16, os.cpu_count() or 4),
+                                mp_context=mp.get_context("spawn")) as ex:
+        p3 = list(ex.map(_cut_one, specs))
     cells3 = sum(p.cells() for p in p3)
     u3 = [np.random.default_rng(300 + i).random(p.seqlen) for i, p in enumerate(p3)]
     sched3 = api.autotune(p3, precision="fp32", want_path=True, trials=1)
@@ -280,39 +325,26 @@ def _c3(rng):
     api.set_timing(0)
     return {
         "workload": "128 internal-branch threading problems, k=50, 2e5 columns (2 Mb), "
-                    "ntimes=20, missing ~U[0,2%], FP32 forward + traceback; the cut subtree is "
-                    "a single leaf (the threaded haplotype) of each seeded ARG",
+                    "ntimes=20, missing ~U[0,2%], FP32 forward + traceback; each a seeded ARG "
+                    "cut along a uniform removal path (the subtree changes along the genome)",
+        "states_per_column_mean": cells3 / sum(p.seqlen for p in p3),
         "cells_per_step": int(cells3), "value": cells3 / float(np.mean(dev3)),
         "e2e": cells3 / float(np.mean(wall3)), "ms_per_step": 1e3 * float(np.mean(dev3)),
         "schedule": sched3,
         "graph_replays": api.graph_counts()["replays"] - g0["replays"]}
 
 
-def _c4(rng):
-    from argweaver_gb300 import refapi
+def _serve_once(pool, rate, duration, rng, max_inflight=24, max_batch=32):
+    """Poisson arrivals at `rate` requests/s for `duration` s, requests drawn from `pool`
+    with fresh uniforms, FP32, through the serving loop; the server's statistics."""
     from argweaver_gb300.server import Server
 
-    # ---- c4: serving. Requests drawn from config 4's distribution (k log-U[8,200],
-    # 50 kb - 5 Mb log-uniform, ntimes in {16, 20, 32}), pre-simulated (off the clock), a
-    # pool of distinct ARGs reused with fresh uniforms; Poisson arrivals
-    npool = 160
-    specs = []
-    for _ in range(npool):
-        k = int(np.exp(rng.uniform(np.log(8), np.log(200))))
-        L = int(np.exp(rng.uniform(np.log(5e3), np.log(5e5))))
-        T = int(rng.choice([16, 20, 32]))
-        specs.append((k - 1, L, int(rng.integers(1, 2**62)), T, 0.005))
-    pool = _sim_pool(specs)
-    rate, duration = 40.0, 10.0
-    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=int(rate * duration * 1.5)))
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=int(rate * duration * 1.5) + 8))
     arrivals = arrivals[arrivals < duration]
-    picks = rng.integers(0, npool, size=arrivals.size)
-    unis = {}
-    for q, j in enumerate(picks):
-        unis[q] = np.random.default_rng(1000 + q).random(pool[j].seqlen)
-    with Server(device_bytes=96 << 30, max_inflight=24, max_batch=32) as srv, \
+    picks = rng.integers(0, len(pool), size=arrivals.size)
+    unis = [np.random.default_rng(1000 + q).random(pool[j].seqlen) for q, j in enumerate(picks)]
+    with Server(device_bytes=96 << 30, max_inflight=max_inflight, max_batch=max_batch) as srv, \
             cf.ThreadPoolExecutor(max_workers=8) as clients:
-        # clients submit at the arrival times (each call copies and sizes its request)
         t_start = time.perf_counter()
         futs = []
         for q, (t_arr, j) in enumerate(zip(arrivals, picks)):
@@ -323,9 +355,52 @@ def _c4(rng):
         for f in futs:
             srv.wait(f.result())
         st = srv.stats()
-    served_cells = sum(pool[j].cells() for j in picks)
+    return st, arrivals.size, sum(pool[j].cells() for j in picks)
+
+
+def _c4(rng):
+    from argweaver_gb300 import api, refapi
+
+    # ---- c4: serving. Requests drawn from config 4's distribution (k log-U[8,200],
+    # 50 kb - 5 Mb log-uniform, ntimes in {16, 20, 32}), pre-simulated (off the clock), a
+    # pool of distinct ARGs reused with fresh uniforms; Poisson arrivals, swept over rates
+    npool = 160
+    specs = []
+    for _ in range(npool):
+        k = int(np.exp(rng.uniform(np.log(8), np.log(200))))
+        L = int(np.exp(rng.uniform(np.log(5e3), np.log(5e5))))
+        T = int(rng.choice([16, 20, 32]))
+        specs.append((k - 1, L, int(rng.integers(1, 2**62)), T, 0.005))
+    pool = _sim_pool(specs)
+    mean_cells = float(np.mean([p.cells() for p in pool]))
+    # a request's own time: a sample of the pool run alone (one problem per batch)
+    alone = {}
+    for j in rng.permutation(npool)[:24]:
+        api.run_batch([pool[j]], precision="fp32", want_forward=False, want_path=True)
+        t0 = time.perf_counter()
+        api.run_batch([pool[j]], precision="fp32", want_forward=False, want_path=True)
+        alone[int(j)] = 1e3 * (time.perf_counter() - t0)
+    api.release_memory()
+    sweep = []
+    for rate in (10.0, 20.0, 40.0, 80.0, 160.0):
+        st, n, offered_cells = _serve_once(pool, rate, 8.0, rng)
+        row = {"rate": rate, "requests": int(st["completed"]), "failed": int(st["failed"]),
+               "throughput": st["cells"] / st["span_s"] if st["span_s"] > 0 else None,
+               "offered": offered_cells / 8.0,
+               "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
+               "queue_p50_ms": st["queue_p50_ms"], "queue_p99_ms": st["queue_p99_ms"],
+               "service_p50_ms": st["service_p50_ms"], "service_p99_ms": st["service_p99_ms"],
+               "batches_in_flight_max": int(st["inflight_max"])}
+        sweep.append(row)
+        if st["p99_ms"] > 30000:  # past saturation: the queue grows without bound
+            break
+    # saturation: the highest rate whose throughput still follows the offered load
+    sat = None
+    for row in sweep:
+        if row["throughput"] and row["throughput"] >= 0.9 * row["offered"]:
+            sat = row
     # the plain FP64 per-request path: one arghmm_sample_posterior call per request, no
-    # batching, on requests drawn from the same pool (bounded to ~10 s)
+    # batching, on requests drawn from the same pool (bounded to ~6 s)
     lat64, c64, t64 = [], 0, 0.0
     for j in rng.permutation(npool):
         t0 = time.perf_counter()
@@ -337,15 +412,16 @@ def _c4(rng):
         if t64 > 6.0:
             break
     return {
-        "workload": f"Poisson arrivals at {rate:g} requests/s for {duration:g} s "
-                    f"({arrivals.size} requests) drawn from {npool} pre-simulated ARGs: "
-                    "k log-U[8,200], 5e3-5e5 columns log-uniform, ntimes in {16,20,32}, FP32 "
-                    "forward + traceback per request",
-        "requests": int(st["completed"]), "failed": int(st["failed"]),
-        "throughput": st["cells"] / st["span_s"] if st["span_s"] > 0 else None,
-        "unit": UNIT, "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "max_ms": st["max_ms"],
-        "mean_cells_per_request": served_cells / max(1, arrivals.size),
-        "batches_in_flight_max": int(st["inflight_max"]),
+        "workload": f"Poisson arrivals swept over rates (8 s each) of requests drawn from {npool} "
+                    "pre-simulated ARGs: k log-U[8,200], 5e3-5e5 columns log-uniform, ntimes "
+                    "in {16,20,32}, FP32 forward + traceback per request; the configured "
+                    "2000 requests/s would offer about 1e11 cells/s, above one GPU's capacity",
+        "unit": UNIT, "mean_cells_per_request": mean_cells,
+        "sweep": sweep,
+        "saturation": sat,
+        "alone_ms": {"p50": float(np.percentile(list(alone.values()), 50)),
+                     "p99": float(np.percentile(list(alone.values()), 99)),
+                     "sample": f"{len(alone)} requests of the pool, each run alone"},
         "fp64_plain_per_request": {"requests": len(lat64),
                                    "p50_ms": float(np.percentile(lat64, 50)),
                                    "p99_ms": float(np.percentile(lat64, 99)),
@@ -392,6 +468,7 @@ def main():
                                    "L~U[1e4,1e5] columns, ntimes=20, 0.5% missing",
                        "sample": "problems in ascending size until the time budget"},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "cpu_model": cpu_model(),
                              "sample": f"{args.cpu_sample_seconds:.0f} s per step of the same "
                                        "problems, smallest first, one per thread"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -463,29 +540,46 @@ def main():
     phase_ms = {k: float(np.mean([t[k] for t in phases])) for k in phases[0]}
 
     # the plain FP64 path: one problem per call through the reference's C ABI
-    # (arghmm_sample_posterior: forward + traceback), smallest problems first, ~3 s
+    # (arghmm_sample_posterior: forward + traceback), on a size-stratified sample (every
+    # 16th problem by cell count), bounded to ~10 s
     from argweaver_gb300 import refapi
+    by_size = sorted(problems, key=lambda p: p.cells())
+    stratified = by_size[8::16]
     plain_cells, plain_t, plain_n = 0, 0.0, 0
-    for p in sorted(problems, key=lambda p: p.cells()):
+    for p in stratified:
         t0 = time.perf_counter()
         refapi.arghmm_sample_posterior(p)
         plain_t += time.perf_counter() - t0
         plain_cells += p.cells()
         plain_n += 1
-        if plain_t > 3.0:
+        if plain_t > 10.0:
             break
     plain = plain_cells / plain_t
 
-    # error report outside the timed region: FP32 vs FP64 posteriors on the two largest
-    # problems and two from the middle of the size range
-    by_size = sorted(problems, key=lambda p: p.cells())
-    sample = by_size[-2:] + by_size[len(by_size) // 2:len(by_size) // 2 + 2]
-    errs = []
-    for p in sample:
-        a = api.run_batch([p], precision="fp32", want_forward=False, want_posterior=True)[0]
-        b = api.run_batch([p], precision="fp64", want_forward=False, want_posterior=True)[0]
-        errs.append(float(np.max(np.abs(a.posterior - b.posterior))))
-    errs = errs or [float("nan")]
+    # the same batch in FP64 on the same GPU (forward + traceback, one batched step)
+    api.set_timing(1)
+    api.run_batch(problems, precision="fp64", want_forward=False, want_path=True, uniforms=uniforms)
+    t0 = time.perf_counter()
+    api.run_batch(problems, precision="fp64", want_forward=False, want_path=True, uniforms=uniforms)
+    fp64_wall = time.perf_counter() - t0
+    fp64_dev = api.last_timings()["compute"] / 1e3
+    api.set_timing(0)
+
+    # error report outside the timed region, over every problem of the batch: FP32 against
+    # FP64 posterior marginals (forward-backward), in batches of 16 problems
+    POST_FLOOR = 1e-3
+    max_abs, max_rel, n_floor = 0.0, 0.0, 0
+    for j in range(0, len(problems), 16):
+        chunk = problems[j:j + 16]
+        ra = api.run_batch(chunk, precision="fp32", want_forward=False, want_posterior=True)
+        rb = api.run_batch(chunk, precision="fp64", want_forward=False, want_posterior=True)
+        for a, b in zip(ra, rb):
+            e = np.abs(a.posterior - b.posterior)
+            big = b.posterior >= POST_FLOOR
+            max_abs = max(max_abs, float(e.max()))
+            if big.any():
+                max_rel = max(max_rel, float(np.max(e[big] / b.posterior[big])))
+            n_floor += int(big.sum())
 
     if rank != 0:
         return
@@ -499,6 +593,7 @@ def main():
     # dominant kernel: the forward pass, 4 B of FP32 table written per cell
     achieved = cells * 4 / (phase_ms["forward"] / 1e3) / 1e9
     cpu_v, cpu_cells, cpu_dt = cpu_reference(problems, args.cpu_sample_seconds, os.cpu_count() or 1)
+    cpu1_v, cpu1_cells, cpu1_dt = cpu_reference(problems, min(5.0, args.cpu_sample_seconds), 1)
     per_inst = sorted(p.cells() for p in problems)
     lat = np.array(wall) * 1e3
     line = {
@@ -525,13 +620,27 @@ def main():
                      "kernel": "forward (k_forward_reg), 4 B of FP32 table written per cell, "
                                "timed alone (phases run one after another)"},
         "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                         "cpu_model": cpu_model(),
                          "sample": f"{cpu_cells} cells in {cpu_dt:.1f} s: the same problems, "
-                                   "smallest first, one per thread"},
+                                   "smallest first, one per thread",
+                         "value_1core": cpu1_v,
+                         "sample_1core": f"{cpu1_cells} cells in {cpu1_dt:.1f} s on one "
+                                         "thread, smallest problems first"},
         "fp64_plain": {"value": plain, "unit": UNIT, "speedup_of_value": value / plain,
-                       "sample": f"{plain_n} smallest problems, one arghmm_sample_posterior "
-                                 "call each (FP64, forward + traceback)"},
-        "fp32_vs_fp64_posterior_max_abs_err": max(errs),
-        "error_sample": "the 2 largest and 2 median problems of the batch, full length",
+                       "sample": f"{plain_n} problems, every 16th by cell count, one "
+                                 "arghmm_sample_posterior call each (FP64, forward + "
+                                 "traceback)"},
+        "fp64_batched": {"value": cells / fp64_dev, "e2e": cells / fp64_wall, "unit": UNIT,
+                         "ms": 1e3 * fp64_dev, "e2e_ms": 1e3 * fp64_wall,
+                         "fp32_speedup": value / (cells / fp64_dev),
+                         "workload": "the same 256 problems and uniforms, FP64 forward + "
+                                     "traceback, one batched step"},
+        "fp32_vs_fp64_posterior_max_rel_err": max_rel,
+        "fp32_vs_fp64_posterior_max_abs_err": max_abs,
+        "error_floor": POST_FLOOR,
+        "error_sample": f"all {len(problems)} problems of the batch, full length; relative "
+                        f"error over the {n_floor} cells whose FP64 marginal is >= "
+                        f"{POST_FLOOR:g}, absolute error over every cell",
         "gpu_launches": launches,
         "schedule": dict(schedule, graph_replays_in_timed_steps=graphs1["replays"] - graphs0["replays"],
                          note="autotuned once before the timed steps; each step replays the "

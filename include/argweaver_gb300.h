@@ -363,6 +363,19 @@ int awg_sample_recombinations(const awg_problem *problem, const int *path,
 int awg_autotune(const awg_problem *problems, awg_outputs *outputs, int n, int precision,
                  int trials, char *report, int report_len);
 
+/* Forward (FP64) and stochastic traceback of ONE problem conditioned at its ends, for the
+ * reference's conditioned samplers (cond_sample_arg_thread[_internal],
+ * sample_thread.cpp:708-865, which fill the first forward column and fix the last state
+ * before calling arghmm_forward_alg and stochastic_traceback). prior: the first column's
+ * max(S0,1) values (NULL: the state prior); last_state: the last column's state (-1: drawn
+ * from the last column, as usual). uniforms: seqlen draws as awg_outputs.uniforms (u[L-1]
+ * unused when last_state >= 0); NULL draws libc rand() as the reference does: one per column
+ * from the last drawn column down to column 0. path: seqlen state indices; loglik optional.
+ * Returns 0 or a negative code (awg_last_error). */
+int awg_sample_path_conditioned(const awg_problem *problem, const double *prior,
+                                int last_state, const double *uniforms, int *path,
+                                double *loglik);
+
 /* Frees the batch engine's grow-only device arena, its page-locked staging and captured
  * graph (the next awg_run_batch allocates again). Returns 0. */
 int awg_release_memory(void);
@@ -402,6 +415,8 @@ typedef struct {
     double busy_s;        /* time with at least one batch on the GPU */
     double launch_s;      /* server thread time spent planning and launching batches */
     int inflight_max;     /* most batches on the GPU at once */
+    double queue_p50_ms, queue_p99_ms;      /* submission to admission into a batch */
+    double service_p50_ms, service_p99_ms;  /* admission to results in place */
 } awg_server_stats;
 
 awg_server *awg_server_create(const awg_server_options *opt);  /* NULL: awg_server_last_error */
@@ -430,9 +445,8 @@ const char *awg_server_last_error(void);
 #define AWG_STATIC_SCRATCH_BYTES (64ull << 20)
 
 /* Forward table and log-likelihood of ONE problem, allocating nothing: no cudaMalloc or
- * cudaFree, no page-locked host memory, no memory pool. No counterpart in the reference
- * (its forward pass, arghmm_forward_alg in sample_thread.cpp:887-925, allocates the table
- * per call); the results equal awg_run_batch's for the same problem and precision.
+ * cudaFree, no page-locked host memory, no memory pool. No counterpart in the reference.
+ * The results equal awg_run_batch's for the same problem and precision.
  *
  * For callers that cannot allocate device memory: a process whose device memory belongs
  * to another allocator (a framework's caching allocator, a per-process memory cap), or a
@@ -445,14 +459,16 @@ const char *awg_server_last_error(void);
  * sizes. (FP64, a problem of S states per column and L columns needs a little over 8*S*L
  * bytes: S = 300 fits about 25,000 columns.)
  *
- * Set-up: the first call on each device, with that device current, resolves the array's
- * device address (cudaGetSymbolAddress, which may load the module that holds it). Make
- * that first call before any stream capture starts.
+ * Set-up: the first call on each device, with that device current, loads the module that
+ * holds the array (cudaGetSymbolAddress). Make that first call before any stream capture
+ * starts. Every call resolves the array's address again in the current context, so a
+ * context destroyed and recreated in between (cudaDeviceReset) is safe.
  * Zeroing: only the 16-byte error record has to start at zero, and each call clears it
  * itself (cudaMemsetAsync). Every other byte of the array is written before it is read.
  * Concurrency: the array is shared by every call on a device. Calls that overlap in time
  * (from several host threads, or streams of several threads) race on it and corrupt each
- * other's results: serialise them. A call returns after its stream has finished its work.
+ * other's results: serialise them. A call returns after its stream has finished its work,
+ * also when it fails after work was enqueued.
  *
  * output: forward (AWG_FP64) or forward32 (AWG_FP32) and loglik may be set, as in
  * awg_outputs; path and posterior must be NULL. stream: a cudaStream_t, NULL for the

@@ -1341,6 +1341,13 @@ int oracle_nstates(const oracle_problem *p, int *nstates) {
 }
 
 int oracle_forward(const oracle_problem *p, double *fw, double *loglik) {
+    return oracle_forward_prior(p, nullptr, fw, loglik);
+}
+
+// With prior non-NULL, column 0 holds those max(S0,1) values instead of the state priors
+// (the given first column of arghmm_forward_alg's prior_given, sample_thread.cpp:425-429).
+int oracle_forward_prior(const oracle_problem *p, const double *prior, double *fw,
+                         double *loglik) {
     Hmm h;
     if (!setup(p, h)) return -1;
     vector<int> nst;
@@ -1356,6 +1363,7 @@ int oracle_forward(const oracle_problem *p, double *fw, double *loglik) {
         double *col = fw + off[blk.start];
         if (b == 0) {
             calc_state_priors(blk.states, blk.lineages, h.m, col, h.minage);
+            if (prior) std::copy(prior, prior + S, col);
         } else {
             const int S1 = std::max(nst[blk.start - 1], 1);
             (void)S1;
@@ -1369,14 +1377,25 @@ int oracle_forward(const oracle_problem *p, double *fw, double *loglik) {
     return 0;
 }
 
-int oracle_traceback(const oracle_problem *p, const double *fw, const double *u, int *path) {
+// With `given` non-NULL each column draws conditioned on given[i + 1] instead of the path
+// drawn so far (a per-column check of another sampler's draws on its own table).
+int oracle_traceback_given(const oracle_problem *p, const double *fw, const double *u,
+                           const int *given, int *path) {
+    return oracle_traceback_last(p, fw, u, given, -1, path);
+}
+
+// last_state >= 0: the last column's state is given (stochastic_traceback with
+// last_state_given, sample_thread.cpp:532-539) and takes no draw.
+int oracle_traceback_last(const oracle_problem *p, const double *fw, const double *u,
+                          const int *given, int last_state, int *path) {
     Hmm h;
     if (!setup(p, h)) return -1;
     vector<int> nst;
     vector<long long> off = column_offsets(h, nst);
     const int L = p->seqlen;
     const int B = (int)h.arg.trees.size();
-    path[L - 1] = sample(fw + off[L - 1], std::max(nst[L - 1], 1), u[L - 1]);
+    path[L - 1] = last_state >= 0 ? last_state
+                                  : sample(fw + off[L - 1], std::max(nst[L - 1], 1), u[L - 1]);
     vector<double> A, trans;
     for (int b = B - 1; b >= 0; b--) {
         Block blk;
@@ -1388,7 +1407,7 @@ int oracle_traceback(const oracle_problem *p, const double *fw, const double *u,
         int last_k = -1;
         for (int i = blk.len - 2; i >= 0; i--) {  // sample_hmm_posterior (sample_thread.cpp:470-503)
             const int col = blk.start + i;
-            int k = path[col + 1];
+            int k = given ? given[col + 1] : path[col + 1];
             if (k != last_k) {
                 for (int j = 0; j < nstates; j++) trans[j] = blk.tm.get(t, blk.states, j, k);
                 last_k = k;
@@ -1400,11 +1419,16 @@ int oracle_traceback(const oracle_problem *p, const double *fw, const double *u,
             const int col = blk.start - 1;
             const int n1 = std::max(blk.sw.nstates1, 1);
             A.assign(n1, 0.0);
-            for (int j = 0; j < n1; j++) A[j] = fw[off[col] + j] * blk.sw.get(j, path[col + 1]);
+            const int k = given ? given[col + 1] : path[col + 1];
+            for (int j = 0; j < n1; j++) A[j] = fw[off[col] + j] * blk.sw.get(j, k);
             path[col] = sample(A.data(), n1, u[col]);
         }
     }
     return 0;
+}
+
+int oracle_traceback(const oracle_problem *p, const double *fw, const double *u, int *path) {
+    return oracle_traceback_given(p, fw, u, nullptr, path);
 }
 
 // The FP32 path's decomposed draw, restated in FP64 (no counterpart in the reference; it

@@ -38,11 +38,19 @@ int oracle_nstates(const oracle_problem *p, int *nstates);
  * (no emission); every later column is normalised to sum 1. When loglik is not NULL it
  * receives sum over columns i>=1 of log(norm_i). */
 int oracle_forward(const oracle_problem *p, double *fw, double *loglik);
+/* The same with column 0 given (prior: max(S0,1) values), or the state priors when NULL. */
+int oracle_forward_prior(const oracle_problem *p, const double *prior, double *fw,
+                         double *loglik);
 
 /* Stochastic traceback (stochastic_traceback, sample_thread.cpp:522-569) with explicit
  * uniforms: u[i] in [0,1] is the draw used for column i (the reference draws
  * rand()/RAND_MAX once per column, last column first). */
 int oracle_traceback(const oracle_problem *p, const double *fw, const double *u, int *path);
+int oracle_traceback_given(const oracle_problem *p, const double *fw, const double *u,
+                           const int *given, int *path);
+/* last_state >= 0: the last column's state is given and takes no draw. */
+int oracle_traceback_last(const oracle_problem *p, const double *fw, const double *u,
+                          const int *given, int last_state, int *path);
 
 /* Backward table, same layout as the forward table, each column normalised to sum 1;
  * the transition into column i+1 is the one the forward pass used (block matrix or

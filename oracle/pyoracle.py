@@ -43,6 +43,11 @@ def load():
         for name, args in [("oracle_nstates", [P, C.c_void_p]),
                            ("oracle_forward", [P, C.c_void_p, C.c_void_p]),
                            ("oracle_traceback", [P, C.c_void_p, C.c_void_p, C.c_void_p]),
+                           ("oracle_traceback_given", [P, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                       C.c_void_p]),
+                           ("oracle_traceback_last", [P, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                      C.c_int, C.c_void_p]),
+                           ("oracle_forward_prior", [P, C.c_void_p, C.c_void_p, C.c_void_p]),
                            ("oracle_traceback_split", [P, C.c_void_p, C.c_void_p, C.c_void_p,
                                                        C.c_void_p]),
                            ("oracle_backward", [P, C.c_void_p]),
@@ -104,8 +109,9 @@ def offsets(ns: np.ndarray) -> np.ndarray:
     return off
 
 
-def forward(prob):
-    """Packed forward table and the log-likelihood from the column norms."""
+def forward(prob, prior=None):
+    """Packed forward table and the log-likelihood from the column norms; with ``prior``,
+    column 0 holds those values instead of the state priors."""
     b = Bound(prob)
     lib = load()
     ncells = lib.oracle_cells(b.ref)
@@ -113,17 +119,34 @@ def forward(prob):
         raise ValueError("oracle rejected the problem")
     fw = np.zeros(ncells, dtype=np.float64)
     lnl = C.c_double(0.0)
-    _check(lib.oracle_forward(b.ref, fw.ctypes.data, C.addressof(lnl)), "forward")
+    pr = None if prior is None else np.ascontiguousarray(prior, dtype=np.float64)
+    _check(lib.oracle_forward_prior(b.ref, None if pr is None else pr.ctypes.data,
+                                    fw.ctypes.data, C.addressof(lnl)), "forward")
     return fw, lnl.value
 
 
-def traceback(prob, fw: np.ndarray, u: np.ndarray) -> np.ndarray:
+def traceback_last(prob, fw: np.ndarray, u: np.ndarray, last_state: int) -> np.ndarray:
+    """The reference's scan with the last column's state given (no draw there)."""
     b = Bound(prob)
     fw = np.ascontiguousarray(fw, dtype=np.float64)
     u = np.ascontiguousarray(u, dtype=np.float64)
     path = np.zeros(prob.seqlen, dtype=np.int32)
-    _check(load().oracle_traceback(b.ref, fw.ctypes.data, u.ctypes.data, path.ctypes.data),
-           "traceback")
+    _check(load().oracle_traceback_last(b.ref, fw.ctypes.data, u.ctypes.data, None,
+                                        int(last_state), path.ctypes.data), "traceback")
+    return path
+
+
+def traceback(prob, fw: np.ndarray, u: np.ndarray, given=None) -> np.ndarray:
+    """The reference's scan (sample_hmm_posterior). With ``given``, column i draws
+    conditioned on given[i + 1] instead of the path drawn so far."""
+    b = Bound(prob)
+    fw = np.ascontiguousarray(fw, dtype=np.float64)
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    g = None if given is None else np.ascontiguousarray(given, dtype=np.int32)
+    path = np.zeros(prob.seqlen, dtype=np.int32)
+    _check(load().oracle_traceback_given(b.ref, fw.ctypes.data, u.ctypes.data,
+                                         None if g is None else g.ctypes.data,
+                                         path.ctypes.data), "traceback")
     return path
 
 

@@ -15,6 +15,7 @@ Run where the reference checkout exists (default /root/reference, or $AWG_REFERE
     python tests/golden/make_golden.py addthreadpath  # the internal-branch regraft
     python tests/golden/make_golden.py samplethreadinternal  # the internal re-threading step
     python tests/golden/make_golden.py resampleleaf  # the leaf re-threading move
+    python tests/golden/make_golden.py large      # config-scale shapes (k = 48, k = 50 cut)
 
 It builds the reference from its own sources (oracle/Makefile target ``ref``), writes
 each problem as an AWGPROB1 file and runs the reference's threading HMM on it through
@@ -481,10 +482,56 @@ def infsites(tmp):
     make("infsites_cut_k10_s5", pc, 505, tmp, penalty=1e-3)
 
 
+def cut_leaves(prob: Problem) -> int:
+    """Most leaves under the cut subtree (each root's child[0]) over the trees of a cut."""
+    best = 0
+    for b in range(prob.ntrees):
+        par = prob.ptrees[b]
+        top = int(prob.root_child0[b])
+        nleaves = (prob.nnodes + 1) // 2
+        n = 0
+        for v in range(nleaves):
+            x = v
+            while x != -1 and x != top:
+                x = par[x]
+            n += x == top
+        best = max(best, n)
+    return best
+
+
+def large(tmp):
+    """Shapes at the configurations' scale, pinned by the reference itself: an external
+    problem at k = 48 (config 1's upper range, 0.5% missing calls) and internal-branch cuts
+    of k = 50 ARGs along the reference's uniform removal path (config 3's shape), the first
+    whose cut subtree holds 3 to 12 leaves and leaves at least 100 states per column."""
+    prob = simulate(47, 3000, 41, missing=0.005)
+    p = os.path.join(tmp, "p.prob"); prob.save(p)
+    make("large_k48_s41", p, 141, tmp)
+    made = 0
+    for seed in range(1, 40):
+        full = simulate(50, 3000, 250 + seed, add_thread=False, missing=0.01)
+        pf = os.path.join(tmp, "full.prob"); full.save(pf)
+        pc = os.path.join(tmp, "cut.prob")
+        run("cut", pf, seed, pc)
+        cut = Problem.load(pc)
+        n = cut_leaves(cut)
+        if n < 3 or n > 12 or cut.cells() < 100 * cut.seqlen:
+            continue
+        make(f"large_cut_k50_s{seed}", pc, 600 + seed, tmp)
+        print(f"  cut subtree: up to {n} leaves")
+        made += 1
+        if made == 1:
+            break
+
+
 def main():
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={REF}"],
                    check=True)
     pyoracle.build()
+    if sys.argv[1:] == ["large"]:
+        with tempfile.TemporaryDirectory() as tmp:
+            large(tmp)
+        return
     if sys.argv[1:] == ["infsites"]:
         with tempfile.TemporaryDirectory() as tmp:
             infsites(tmp)
@@ -567,6 +614,7 @@ def main():
             run("cut", pf, seed, pc)
             make(f"cut_k10_s{seed}", pc, 500 + seed, tmp)
 
+        large(tmp)
         dense(tmp)
         densernd(tmp)
         argprob(tmp)

@@ -276,3 +276,44 @@ def test_all_missing_column_data_is_prior():
     fw_o, lnl_o = pyoracle.forward(prob)
     assert max_rel(r.forward, fw_o) <= 1e-12
     assert abs(r.loglik - lnl_o) <= 1e-9
+
+
+@pytest.mark.parametrize("name", ["dsmc_k8_s11", "dsmc_k17_missing", "cut_k10_s3"])
+def test_conditioned_path_matches_oracle(name):
+    """awg_sample_path_conditioned (the conditioned samplers' forward and traceback): a
+    first column holding 1 at a chosen state and a given last state give the oracle's path on
+    its forward table with that first column, the last column taking no draw; each alone
+    too."""
+    prob, _ = load(name)
+    ns = pyoracle.nstates(prob)
+    S0, SL = max(int(ns[0]), 1), max(int(ns[-1]), 1)
+    rng = np.random.default_rng(17)
+    u = rng.random(prob.seqlen)
+    prior = np.zeros(S0)
+    prior[S0 // 3] = 1.0
+    last = (2 * SL) // 3
+    for pr, ls in ((prior, last), (prior, -1), (None, last)):
+        path = api.sample_path_conditioned(prob, prior=pr, last_state=ls, uniforms=u)
+        fw, _ = pyoracle.forward(prob, prior=pr)
+        ref = pyoracle.traceback_last(prob, fw, u, ls)
+        np.testing.assert_array_equal(path, ref)
+        if pr is not None:
+            assert path[0] == S0 // 3
+        if ls >= 0:
+            assert path[-1] == ls
+
+
+def test_conditioned_path_rand_order():
+    """With no uniforms the draws come from libc rand() in the reference's order: one per
+    column from the last drawn column down to column 0 (none for a given last state)."""
+    prob, _ = load("dsmc_k8_s12")
+    ns = pyoracle.nstates(prob)
+    last = max(int(ns[-1]), 1) - 1
+    refapi.srand(41)
+    path = api.sample_path_conditioned(prob, last_state=last)
+    fw, _ = pyoracle.forward(prob)
+    # rand_uniforms(seed, n): the draws of a traceback over n columns, last column first,
+    # indexed by column; column L-1 takes none here, so columns 0..L-2 take them
+    u = np.zeros(prob.seqlen)
+    u[:-1] = pyoracle.rand_uniforms(41, prob.seqlen - 1)
+    np.testing.assert_array_equal(path, pyoracle.traceback_last(prob, fw, u, last))

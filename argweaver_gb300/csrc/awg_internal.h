@@ -72,8 +72,9 @@ struct StateInfo {
 // Device views of a batch (all pointers are device memory).
 struct BatchDev {
     int ninst, nblocks, maxS, maxT, maxnodes, maxM;
-    int var64;                   // FP32 path: every variant column's emissions formed in
-                                 // FP64 and rounded once (implies emit64)
+    int vardf;                   // FP32 path: variant columns with two or more observed
+                                 // bases formed in double-float and rounded once (needs
+                                 // emit64's carve; off where that carve does not fit)
     int emit64;                  // some instance forms FP64 emission partials even on the
                                  // FP32 path (internal-branch or infinite-sites problems)
     const InstDev *inst;

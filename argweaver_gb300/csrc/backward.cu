@@ -111,7 +111,8 @@ __global__ void k_backward(BatchDev d, int maxS, double *bw_out) {
     F *g = bwB + maxS;
     float *loA = (float *)(g + maxS);           // FP32 path: low parts of bwA / bwB
     float *loB = loA + maxS;
-    Meta *meta = (Meta *)(((uintptr_t)(loB + maxS) + 15) & ~(uintptr_t)15);
+    float *glo = loB + maxS;                    // FP32 path: low parts of g at a switch
+    Meta *meta = (Meta *)(((uintptr_t)(glo + maxS) + 15) & ~(uintptr_t)15);
     int *perm = (int *)(meta + maxS);
     F *gs = (F *)(perm + maxS + 1) + 1;     // [maxS / 32 + 1] group sums, 8-byte aligned
     gs = (F *)(((uintptr_t)gs + 7) & ~(uintptr_t)7);
@@ -240,28 +241,64 @@ __global__ void k_backward(BatchDev d, int maxS, double *bw_out) {
             // into the previous tree's last column through the switch matrix
             const BlockDev &P = d.blocks[I.block0 + bi - 1];
             const int n1 = imax(B.S1, 1);
-            for (int k = tid; k < Sm; k += blockDim.x) g[k] = emitx(0, k, cur[k]);
+            if constexpr (BTab<F>::split) {
+                // pairs through the switch: e * bw of the tree's first column with its low
+                // parts; a deterministic move by its FP64 probability (a complement near 1)
+                for (int k = tid; k < Sm; k += blockDim.x) {
+                    F2 x = F2{cur[k], S == 0 ? 0.0f : curlo[k]};
+                    const uint8_t c = cls[0];
+                    if (S > 0 && c == COL_INVARIANT) x = f2_keep(x, inv[k]);
+                    else if (S > 0 && c != COL_MASKED) {
+                        const float e = var[(size_t)cvar[0] * S + k];
+                        x = e >= 0.0f ? f2_keep(x, e) : f2_mul(x, -e);
+                    }
+                    g[k] = x.hi;
+                    glo[k] = x.lo;
+                }
+            } else {
+                for (int k = tid; k < Sm; k += blockDim.x) g[k] = emitx(0, k, cur[k]);
+            }
             __syncthreads();
             const int2 src = d.srcs[I.block0 + bi];
             const int *determ = d.determ + B.prev_state0;
             const F *dp = tab.dprob + B.prev_state0;
+            const double *dp64 = d.determprob + B.prev_state0;
             const F *rr = tab.rrow + B.state0;
             const F *cr = tab.crow + B.state0;
             for (int j = tid; j < n1; j += blockDim.x) {
                 F s = 0;
+                float slo = 0.0f;
                 if (j == src.y || j == src.x) {
                     const F *row = (j == src.y) ? cr : rr;
                     for (int k = 0; k < Sm; k++)
                         if (row[k] > F(0)) s += row[k] * g[k];
                 } else if (determ[j] >= 0) {
-                    s = dp[j] * g[determ[j]];
+                    if constexpr (BTab<F>::split) {
+                        const double pj = dp64[j];
+                        const F2 x{g[determ[j]], glo[determ[j]]};
+                        const F2 y = pj >= 0.5 ? f2_keep(x, (float)(1.0 - pj)) : f2_mul(x, (float)pj);
+                        s = y.hi;
+                        slo = y.lo;
+                    } else {
+                        s = dp[j] * g[determ[j]];
+                    }
                 }
                 nxt[j] = s;
+                nxtlo[j] = slo;
             }
             const F z = fixed_sum<F>(n1, [&](int k) { return nxt[k]; }, gs);
-            for (int k = tid; k < n1; k += blockDim.x) {
-                nxt[k] /= z;
-                nxtlo[k] = 0.0f;  // the switch starts the previous tree's pairs afresh
+            if constexpr (BTab<F>::split) {
+                const float iz = 1.0f / z;
+                for (int k = tid; k < n1; k += blockDim.x) {
+                    const F2 x = f2_mul(F2{nxt[k], nxtlo[k]}, iz);
+                    nxt[k] = x.hi;
+                    nxtlo[k] = x.lo;
+                }
+            } else {
+                for (int k = tid; k < n1; k += blockDim.x) {
+                    nxt[k] /= z;
+                    nxtlo[k] = 0.0f;
+                }
             }
             __syncthreads();
             (void)P;
@@ -280,7 +317,7 @@ int backward_threads(int maxS) {
 template <typename F>
 void launch(const BatchDev &d, double *bw_out, cudaStream_t s) {
     const int maxS = imax(d.maxS, 1);
-    const size_t smem = 3 * (size_t)maxS * sizeof(F) + 2 * (size_t)maxS * sizeof(float) + 16 +
+    const size_t smem = 3 * (size_t)maxS * sizeof(F) + 3 * (size_t)maxS * sizeof(float) + 16 +
                         (size_t)maxS * (sizeof(Meta) + sizeof(int)) + sizeof(int) + 16 +
                         ((size_t)maxS / 32 + 1) * sizeof(F);
     // opt in; static shared memory counts against 48 KB too

@@ -195,6 +195,7 @@ int ctx_launch(Ctx &C, const awg_problem *probs, awg_outputs *outs, int n, const
     const bool fp32 = opt.precision == AWG_FP32;
     if (!fp32 && opt.precision != AWG_FP64) { err = "precision must be AWG_FP64 or AWG_FP32"; return -1; }
     if (fp32 && opt.last_states) { err = "a given last traceback state needs AWG_FP64"; return -1; }
+    if (fp32 && opt.dense) { err = "the dense forward step needs AWG_FP64"; return -1; }
 
     HostPlan &plan = C.plan;
     plan = HostPlan();
@@ -397,8 +398,8 @@ int ctx_launch(Ctx &C, const awg_problem *probs, awg_outputs *outs, int n, const
     d.maxnodes = plan.maxnodes;
     d.maxM = plan.maxM;
     d.emit64 = 0;
-    d.var64 = getenv("AWG_VAREMIT_F64") && atoi(getenv("AWG_VAREMIT_F64")) == 1;
-    if (d.var64) d.emit64 = 1;
+    d.vardf = fp32 && varemit_full_carve_fits(plan.maxnodes, plan.maxS) ? 1 : 0;
+    if (d.vardf) d.emit64 = 1;
     for (int i = 0; i < plan.ninst; i++)
         if (plan.inst[i].internal || plan.model[(size_t)i * MODEL_STRIDE + M_CONST + 3] < 1.0)
             d.emit64 = 1;
@@ -461,7 +462,7 @@ int ctx_launch(Ctx &C, const awg_problem *probs, awg_outputs *outs, int n, const
     // per-tree work of later groups fills the SMs they leave idle. The per-tree kernels are
     // persistent, work-stealing over units of trees; the device part of a step is captured
     // once as a CUDA graph and replayed while its launch parameters repeat.
-    const bool special = opt.tables_only || opt.priors || opt.last_states;
+    const bool special = opt.tables_only || opt.priors || opt.last_states || opt.dense;
     const bool serial_timing = timing == 2;
     const bool pipelined = n >= 16 && !special && !serial_timing;
     const bool T = timing != 0;
@@ -564,7 +565,7 @@ int ctx_launch(Ctx &C, const awg_problem *probs, awg_outputs *outs, int n, const
                                           want_post, want_bw, want_bins, plan.ninst, plan.nblocks,
                                           plan.maxS, plan.maxT, plan.maxnodes, plan.maxM,
                                           cfg.kpt, cfg.chunk, cfg.group_div, cfg.persistent, ng,
-                                          (long long)total, d.emit64, d.var64};
+                                          (long long)total, d.emit64, d.vardf};
             for (size_t o : {o_inst, o_blocks, o_model, o_nodes, o_map, o_seq, o_cls, o_cvar,
                              o_order, o_blkmap, o_u, o_sinfo, o_t2off, o_btptr, o_btperm, o_tm,
                              o_gts, o_inv, o_det, o_detp, o_srcs, o_rrow, o_crow, o_gptr, o_gidx,
@@ -663,7 +664,8 @@ int ctx_launch(Ctx &C, const awg_problem *probs, awg_outputs *outs, int n, const
         launch_varemit(d, fp32, s);
         CKL("emission kernel");
         if (T) CK(cudaEventRecord(C.ev[3], s));
-        launch_forward(d, fp32, s, cfg.kpt);
+        if (opt.dense) launch_forward_dense(d, s);
+        else launch_forward(d, fp32, s, cfg.kpt);
         CKL("forward kernel");
         if (T) CK(cudaEventRecord(C.ev[4], s));
         if (want_path) {

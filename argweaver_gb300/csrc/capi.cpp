@@ -143,7 +143,7 @@ std::vector<int> column_nstates(const awg_problem &p) {
 
 double **table_call(awg_local_trees *trees, double *times, int ntimes, double *popsizes,
                     double rho, double mu, char **seqs, int nseqs, int seqlen, bool internal,
-                    const double *prior, int kind) {
+                    const double *prior, int kind, bool dense = false) {
     g_err.clear();
     ProblemView v;
     if (!make_view(trees, times, ntimes, popsizes, rho, mu, seqs, nseqs, seqlen, internal, v))
@@ -162,6 +162,7 @@ double **table_call(awg_local_trees *trees, double *times, int ntimes, double *p
     if (kind == 1) { opt.backward = bws; }
     if (kind == 2) o.posterior = block;
     if (prior) opt.priors = priors;
+    opt.dense = dense;
     std::string err;
     if (awg::run_batch(&v.p, &o, 1, opt, err) != 0) {
         set_error(err);
@@ -773,9 +774,10 @@ double **arghmm_forward_alg(awg_local_trees *trees, double *times, int ntimes,
                             double *popsizes, double rho, double mu, char **seqs, int nseqs,
                             int seqlen, bool prior_given, double *prior, bool internal,
                             bool slow) {
-    (void)slow;  // the dense step (sample_thread.cpp:303-338) computes the same table
+    // slow: the reference's dense S x S step (arghmm_forward_block_slow,
+    // sample_thread.cpp:301-337), its test path
     return table_call(trees, times, ntimes, popsizes, rho, mu, seqs, nseqs, seqlen, internal,
-                      prior_given ? prior : nullptr, 0);
+                      prior_given ? prior : nullptr, 0, slow);
 }
 
 double **arghmm_backward_alg(awg_local_trees *trees, double *times, int ntimes,

@@ -22,6 +22,7 @@ struct RunOptions {
     const TuneCfg *cfg = nullptr;  // explicit schedule (the autotuner's trials), else tuned
     int precision = AWG_FP64;
     const double *const *priors = nullptr;  // per problem: given column-0 prior, or NULL
+    bool dense = false;                     // forward by the dense S x S step (FP64)
     const int *last_states = nullptr;       // per problem: the traceback's given last state
                                             // (FP64 only), or -1 to sample it
     double *const *backward = nullptr;      // per problem: backward table output, or NULL

@@ -361,7 +361,10 @@ __global__ void __launch_bounds__(512) k_forward(BatchDev d, int maxS, int maxM,
 //   B  tf and the norm published: owners finish column i (tf of their time + dot, stay,
 //      emission, rescaling) and write column i-1 / norm to HBM.
 // Every sum has an order fixed by the tree alone, so results do not depend on the block
-// size or on the other problems of the batch.
+// size or on the other problems of the batch. Products are summed with fused multiply-adds
+// (explicit: this file compiles without FMA contraction): on GB300 a warp's FP64 instruction
+// holds its sub-partition's FP64 pipe for about 64 cycles, so the plain FP64 path's cost is
+// its count of FP64 instructions; FMA halves it for the dot and tf and rounds once.
 // FP32 pair arithmetic (value = hi + lo, |lo| <= ulp(hi) / 2) for the dominant path of
 // the FP32 forward step. Within a tree the normalised column converges to the fixed point
 // of the step; a rounding error of the step shifts that fixed point by about the error
@@ -395,6 +398,11 @@ __device__ __forceinline__ F2 f2_add(F2 x, float s) {
     const float err = (x.hi - (h - bb)) + (s - bb);
     return f2_renorm(h, err + x.lo);
 }
+// x + y, both pairs
+__device__ __forceinline__ F2 f2_add2(F2 x, F2 y) {
+    const F2 s = f2_add(x, y.hi);
+    return f2_renorm(s.hi, s.lo + y.lo);
+}
 
 constexpr int NRW = 4;                      // reduction warps of the register variant
 constexpr int RBINS = (MAXT - 1 + NRW - 1) / NRW;  // time bins per reduction warp (<= 8)
@@ -415,6 +423,7 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
     F *col = (F *)dyn_d;                       // [2][maxS] columns in state order
     F *colT = col + 2 * maxS;                  // [maxS] newest column, time-sorted
     F *t2s = colT + maxS;                      // [maxM] same-branch entries of the block
+    float *lastlo = (float *)(t2s + maxM);     // FP32: low parts of a tree's last column
     __shared__ F tmS[MAXT * MAXT];             // [b][a] tmatrix; column 31 holds ones
     __shared__ F part[NRW][32][RBINS];         // reducers: per lane, its chunk's bin sums
     __shared__ F tfp[NRW][32];                 // each reducer's share of tf; [31]: of the norm
@@ -457,6 +466,7 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
                 }
                 v = F(1);
             }
+            if (Tab<F>::split && tid == 0) lastlo[0] = 0.0f;
             for (int i = 1 + tid; i < len; i += NT) fw[i] = v;
             __syncthreads();
             continue;
@@ -528,8 +538,12 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
                 }
             }
         }
-        // the fast chunk sum handles chunks of up to 32 positions spanning up to 3 bins
-        const bool fast_chunk = __all_sync(0xffffffffu, !reducer || (chunk <= 32 && nbc <= 3));
+        // the fast chunk sum handles chunks of up to 32 positions spanning up to 3 bins, eight
+        // loads and three predicated sums at a time: FP32 only, where the adds are cheap. On
+        // GB300 a warp's FP64 add occupies the FP64 pipe of its SM sub-partition for about 64
+        // cycles whether its lanes are live or not, so FP64 sums each lane's positions in turn
+        const bool fast_chunk =
+            sizeof(F) == 4 && __all_sync(0xffffffffu, !reducer || (chunk <= 32 && nbc <= 3));
         if (t2_in_smem) {
 #pragma unroll
             for (int q = 0; q < KPT; q++) {
@@ -612,18 +626,43 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
             for (int q = 0; q < KPT; q++) {
                 const int k = owned(q);
                 if (!valid(k)) continue;
-                F sv = 0;
-                for (int p = gp[k]; p < gp[k + 1]; p++) {
-                    const int j = gi[p];
-                    sv += prev[j] * dp[j];
+                if constexpr (Tab<F>::split) {
+                    // pairs: the previous column's values with their low parts, each
+                    // deterministic move by its FP64 probability (kept as a complement near
+                    // 1), the recombination rows (a small inflow) plain, then the emission
+                    const double *dp64 = d.determprob + B.prev_state0;
+                    F2 a{0.0f, 0.0f};
+                    for (int p = gp[k]; p < gp[k + 1]; p++) {
+                        const int j = gi[p];
+                        const double pj = dp64[j];
+                        const F2 xj{prev[j], lastlo[j]};
+                        a = f2_add2(a, pj >= 0.5 ? f2_keep(xj, (float)(1.0 - pj)) : f2_mul(xj, (float)pj));
+                    }
+                    if (src.x != -1 && rr[k] > F(0)) a = f2_add(a, prev[src.x] * rr[k]);
+                    if (src.y != -1 && cr[k] > F(0)) a = f2_add(a, prev[src.y] * cr[k]);
+                    if (c0 == COL_INVARIANT) a = f2_keep(a, st_inv[q]);
+                    else if (c0 != COL_MASKED) {
+                        const F e = var[(size_t)v0 * S + k];
+                        a = e >= F(0) ? f2_keep(a, e) : f2_mul(a, -e);
+                    }
+                    col[(c ^ 1) * maxS + k] = a.hi;
+                    colT[st_rank[q]] = a.hi;
+                    x_own[q] = a.hi;
+                    x_lo[q] = a.lo;
+                } else {
+                    F sv = 0;
+                    for (int p = gp[k]; p < gp[k + 1]; p++) {
+                        const int j = gi[p];
+                        sv = fma(prev[j], dp[j], sv);
+                    }
+                    if (src.x != -1 && rr[k] > F(0)) sv += prev[src.x] * rr[k];
+                    if (src.y != -1 && cr[k] > F(0)) sv += prev[src.y] * cr[k];
+                    const F v = emit(sv, c0, v0, q, false);
+                    col[(c ^ 1) * maxS + k] = v;
+                    colT[st_rank[q]] = v;
+                    x_own[q] = v;
+                    x_lo[q] = 0.0f;
                 }
-                if (src.x != -1 && rr[k] > F(0)) sv += prev[src.x] * rr[k];
-                if (src.y != -1 && cr[k] > F(0)) sv += prev[src.y] * cr[k];
-                const F v = emit(sv, c0, v0, q, false);
-                col[(c ^ 1) * maxS + k] = v;
-                colT[st_rank[q]] = v;
-                x_own[q] = v;
-                x_lo[q] = 0.0f;
             }
             c ^= 1;
         }
@@ -678,7 +717,7 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
 #pragma unroll
                 for (int j = 0; j < RBINS; j++) {
                     const F g = __shfl_sync(0xffffffffu, bin, j);
-                    if (blo + j < bhi) tf += tmS[(blo + j) * MAXT + lane] * g;
+                    if (blo + j < bhi) tf = fma(tmS[(blo + j) * MAXT + lane], g, tf);
                 }
                 tfp[rw][lane] = tf;
             } else {
@@ -698,23 +737,23 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
                             for (; y + 3 < m; y += 4) {
                                 const F r0 = row[0], r1 = row[m], r2 = row[2 * m], r3 = row[3 * m];
                                 const F n0 = nb[y], n1 = nb[y + 1], n2 = nb[y + 2], n3 = nb[y + 3];
-                                sv += r0 * n0;
-                                s1 += r1 * n1;
-                                sv += r2 * n2;
-                                s1 += r3 * n3;
+                                sv = fma(r0, n0, sv);
+                                s1 = fma(r1, n1, s1);
+                                sv = fma(r2, n2, sv);
+                                s1 = fma(r3, n3, s1);
                                 row += 4 * m;
                             }
                             for (; y + 1 < m; y += 2) {
-                                sv += row[0] * nb[y];
-                                s1 += row[m] * nb[y + 1];
+                                sv = fma(row[0], nb[y], sv);
+                                s1 = fma(row[m], nb[y + 1], s1);
                                 row += 2 * m;
                             }
-                            if (y < m) sv += row[0] * nb[y];
+                            if (y < m) sv = fma(row[0], nb[y], sv);
                             sv += s1;
                         } else {
                             const int a0 = st_time[q] - (k - st_j1[q]);
                             for (int y = 0; y < m; y++)
-                                sv += tab.t2(B.t2_0 + st_off[q] + y * m, tmS[(a0 + y) * MAXT + st_time[q]]) * nb[y];
+                                sv = fma(tab.t2(B.t2_0 + st_off[q] + y * m, tmS[(a0 + y) * MAXT + st_time[q]]), nb[y], sv);
                         }
                     }
                     dq[q] = sv;
@@ -744,7 +783,12 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
                 for (int q = 0; q < KPT; q++) {
                     const int k = owned(q);
                     if (!valid(k)) continue;
-                    const F v = x_own[q] * inv_norm;
+                    F v = x_own[q] * inv_norm;
+                    if constexpr (Tab<F>::split) {
+                        const F2 x = f2_mul(F2{x_own[q], x_lo[q]}, inv_norm);
+                        v = x.hi;
+                        lastlo[k] = x.lo;  // the pair's low part, for the next switch
+                    }
                     if (write_prev) outp[k] = v;
                     col[c * maxS + k] = v;  // normalised, for the next switch
                 }
@@ -796,6 +840,160 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
     }
 }
 
+// ---------------------------------------------------------------------------------------
+// The reference's dense test step (arghmm_forward_block_slow, sample_thread.cpp:301-337),
+// FP64, one CTA per instance: every column of a local tree from the full S x S transition
+// matrix, col2[k] = (sum_j col1[j] transmat[j][k]) emit[i][k], normalised by division. The
+// matrix entries are TransMatrix::get (trans.h:64-83) formed where they are read from the
+// table kernel's FP64 tables: the different-node entry tmatrix[a_j][b_k] for states on
+// other nodes, the same-node row get_time(a, b, c, minage, true) on k's own node. Thread k
+// sums over j in the reference's order. Tree switches, priors and the log-likelihood are
+// the structured path's (arghmm_forward_switch, sample_thread.cpp:345-389).
+__device__ double dense_block_sum(const double *v, int n, double *red) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+    double s = 0.0;
+    for (int k = tid; k < n; k += blockDim.x) s += v[k];
+    s = warp_sum(s);
+    __syncthreads();  // red free
+    if (lane == 0) red[warp] = s;
+    __syncthreads();
+    double t = 0.0;
+    for (int w = 0; w < nw; w++) t += red[w];
+    return t;
+}
+
+__global__ void __launch_bounds__(512) k_forward_dense(BatchDev d, int maxS) {
+    extern __shared__ double dyn_d[];
+    const int qi = cta_instance(d);
+    const InstDev I = d.inst[qi];
+    const int tid = threadIdx.x, lane = tid & 31, NT = blockDim.x;
+    double *col = dyn_d;                         // [2][maxS]
+    int *snode = (int *)(col + 2 * maxS);        // [maxS] node of each state
+    int *stime = snode + maxS;                   // [maxS] time of each state
+    __shared__ double tmS[MAXT * MAXT];
+    __shared__ double red[16];
+    LogAcc acc;
+    int c = 0;  // buffer holding the current (normalised) column
+
+    for (int bi = 0; bi < I.ntrees; bi++) {
+        const int blk = I.block0 + bi;
+        const BlockDev B = d.blocks[blk];
+        const int S = B.S;
+        double *fw = d.fw64 + B.cell0;
+        if (S == 0) {
+            // fully specified tree: one state that carries over (sample_thread.cpp:201-206)
+            double v;
+            if (bi == 0) {
+                v = fw[0];
+                if (tid == 0) col[c * maxS] = v;
+            } else {
+                const int2 src = d.srcs[blk];
+                const int *gp = d.gptr + B.gptr0;
+                const int *gi = d.gidx + B.prev_state0;
+                const double *dp = d.determprob + B.prev_state0;
+                const double *rr = d.recombrow + B.state0;
+                const double *cr = d.recoalrow + B.state0;
+                double sum = 0.0;
+                if (tid < 32) {
+                    for (int p = gp[0] + lane; p < gp[1]; p += 32) sum += col[c * maxS + gi[p]] * dp[gi[p]];
+                    sum = warp_sum(sum);
+                }
+                if (tid == 0) {
+                    if (src.x != -1 && rr[0] > 0.0) sum += col[c * maxS + src.x] * rr[0];
+                    if (src.y != -1 && cr[0] > 0.0) sum += col[c * maxS + src.y] * cr[0];
+                    acc.add(sum);
+                    col[c * maxS] = 1.0;
+                    fw[0] = 1.0;
+                }
+                v = 1.0;
+            }
+            for (int i = 1 + tid; i < B.len; i += NT) fw[i] = v;
+            __syncthreads();
+            continue;
+        }
+        for (int k = tid; k < S; k += NT) {
+            const StateInfo si = d.sinfo[B.state0 + k];
+            snode[k] = si.node;
+            stime[k] = si.time;
+        }
+        const double *tmg = d.tm + (size_t)blk * MAXT * MAXT;
+        for (int e = tid; e < MAXT * MAXT; e += NT) tmS[e] = tmg[e];
+        __syncthreads();
+        const uint8_t *cls = d.colclass + I.col0 + B.start;
+        const int *cvar = d.colvar + I.col0 + B.start;
+        auto emit = [&](int i, int k) -> double {
+            const uint8_t ci = cls[i];
+            if (ci == COL_MASKED) return 1.0;
+            if (ci == COL_INVARIANT) return d.inv_lk[B.state0 + k];
+            return d.varemit[B.var0 + (size_t)cvar[i] * S + k];
+        };
+        // first column: the priors, or the switch from the previous tree's last column
+        double *cur = col + (c ^ 1) * maxS;
+        if (bi == 0) {
+            for (int k = tid; k < S; k += NT) cur[k] = fw[k];
+        } else {
+            const double *prev = col + c * maxS;
+            const int2 src = d.srcs[blk];
+            const int *gp = d.gptr + B.gptr0;
+            const int *gi = d.gidx + B.prev_state0;
+            const double *dp = d.determprob + B.prev_state0;
+            const double *rr = d.recombrow + B.state0;
+            const double *cr = d.recoalrow + B.state0;
+            for (int k = tid; k < S; k += NT) {
+                double s = 0.0;
+                for (int p = gp[k]; p < gp[k + 1]; p++) s += prev[gi[p]] * dp[gi[p]];
+                if (src.x != -1 && rr[k] > 0.0) s += prev[src.x] * rr[k];
+                if (src.y != -1 && cr[k] > 0.0) s += prev[src.y] * cr[k];
+                cur[k] = s * emit(0, k);
+            }
+            __syncthreads();
+            const double norm = dense_block_sum(cur, S, red);
+            if (tid == 0) {
+                acc.add(norm);
+                if (!(norm > 0.0)) report_error(d.err, ERR_ZERO_NORM, qi, bi, B.start);
+            }
+            for (int k = tid; k < S; k += NT) {
+                cur[k] /= norm;
+                fw[k] = cur[k];
+            }
+        }
+        c ^= 1;
+        for (int i = 1; i < B.len; i++) {
+            __syncthreads();  // column i-1 complete
+            const double *c1 = col + c * maxS;
+            double *c2 = col + (c ^ 1) * maxS;
+            for (int k = tid; k < S; k += NT) {
+                const StateInfo sk = d.sinfo[B.state0 + k];
+                const double *grow = d.gts + B.t2_0 + d.t2off[B.state0 + k];
+                double s = 0.0;
+                for (int j = 0; j < S; j++) {
+                    const double p = snode[j] == sk.node ? grow[(j - sk.j1) * sk.m]
+                                                         : tmS[stime[j] * MAXT + sk.time];
+                    s += c1[j] * p;
+                }
+                c2[k] = s * emit(i, k);
+            }
+            __syncthreads();
+            const double norm = dense_block_sum(c2, S, red);
+            if (tid == 0) {
+                acc.add(norm);
+                if (!(norm > 0.0)) report_error(d.err, ERR_ZERO_NORM, qi, bi, B.start + i);
+            }
+            double *outp = fw + (size_t)i * S;
+            for (int k = tid; k < S; k += NT) {
+                c2[k] /= norm;
+                outp[k] = c2[k];
+            }
+            c ^= 1;
+        }
+        __syncthreads();
+    }
+    if (tid == 0 && d.lnl) {
+        acc.flush();
+        d.lnl[qi] = acc.lnl;
+    }
+}
+
 int forward_threads(int maxS) {
     if (maxS > 256) return 512;
     if (maxS > 128) return 256;
@@ -826,7 +1024,7 @@ template <typename F, int KPT>
 void launch_reg(const BatchDev &d, int nt, cudaStream_t s) {
     const int maxS = imax(d.maxS, 1);
     int maxM = imax(d.maxM, 1);
-    auto bytes = [&](int m) { return (size_t)(3 * maxS + m) * sizeof(F) + 16; };
+    auto bytes = [&](int m) { return (size_t)(3 * maxS + m) * sizeof(F) + (size_t)maxS * sizeof(float) + 16; };
     const int t2_in_smem = bytes(maxM) <= 200 * 1024;
     if (!t2_in_smem) maxM = 1;
     const size_t smem = bytes(maxM);
@@ -870,6 +1068,15 @@ bool forward_writes_bins(int maxS, int maxM, int maxT, int kpt) {
     (void)maxT;
     const int k = reg_kpt(imax(maxS, 1), kpt);
     return 32 * NRW + imax(32, ((imax(maxS, 1) + k - 1) / k + 31) / 32 * 32) <= 512;
+}
+
+void launch_forward_dense(const BatchDev &d, cudaStream_t s) {
+    const int maxS = imax(d.maxS, 1);
+    const size_t smem = 2 * (size_t)maxS * sizeof(double) + 2 * (size_t)maxS * sizeof(int);
+    if (!raise_dynamic_smem(k_forward_dense, smem)) return;  // the launch reports it
+    const int nt = imin(512, imax(32, (maxS + 31) / 32 * 32));
+    k_forward_dense<<<d.ninst, nt, smem, s>>>(d, maxS);
+    note_launch();
 }
 
 void launch_forward(const BatchDev &d, bool fp32, cudaStream_t s, int kpt) {

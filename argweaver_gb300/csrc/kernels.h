@@ -18,9 +18,14 @@ void launch_tables(const BatchDev &d, bool want32, cudaStream_t s, int *queue = 
 // K2: emissions of variant columns (Felsenstein pruning); as K1.
 void launch_varemit(const BatchDev &d, bool want32, cudaStream_t s, int *queue = nullptr,
                     int chunk = 1);
+// Whether K2's carve with FP64 per-state factors and 8-byte scratch (needed for FP64 and
+// double-float emissions) fits this largest tree.
+bool varemit_full_carve_fits(int maxnodes, int maxS);
 // K3: forward pass, one CTA per instance; kpt: states per owner thread of the
 // register-resident variant (0: chosen by the state count).
 void launch_forward(const BatchDev &d, bool fp32, cudaStream_t s, int kpt = 0);
+// K3 with the reference's dense test step (arghmm_forward_block_slow), FP64.
+void launch_forward_dense(const BatchDev &d, cudaStream_t s);
 // Whether K3 writes the FP32 columns' time-bin sums (BatchDev::bins32) for a batch of these
 // largest sizes (the register-resident variant does; the fallback for the largest trees
 // does not).

@@ -145,6 +145,8 @@ int run_static(const awg_problem *p, awg_outputs *out, int precision, cudaStream
     d.maxnodes = plan.maxnodes;
     d.maxM = plan.maxM;
     d.emit64 = 0;
+    d.vardf = fp32 && varemit_full_carve_fits(plan.maxnodes, plan.maxS) ? 1 : 0;
+    if (d.vardf) d.emit64 = 1;
     for (int i = 0; i < plan.ninst; i++)
         if (plan.inst[i].internal || plan.model[(size_t)i * MODEL_STRIDE + M_CONST + 3] < 1.0)
             d.emit64 = 1;

@@ -1149,6 +1149,48 @@ __device__ __forceinline__ void jc_apply_x(const R *x, R m, R nm, R *y) {
 template <typename R>
 __device__ __forceinline__ R cprod(R a, R b) { return (a + b) - a * b; }
 
+// Double-float: value = hi + lo, |lo| <= ulp(hi) / 2, about 48 significant bits, from
+// FP32 error-free transforms (Knuth's two-sum; the product's error by fused multiply-add).
+// The FP32 path's emissions of columns with two or more observed bases are formed in it:
+// the forward posterior amplifies a relative error of those emissions roughly 200-fold, so
+// they must reach FP32 as correctly rounded ratios, which FP32 arithmetic does not give.
+struct df {
+    float hi, lo;
+    __device__ __forceinline__ df() : hi(0.f), lo(0.f) {}
+    __device__ __forceinline__ df(double x) : hi((float)x), lo((float)(x - (double)(float)x)) {}
+    __device__ __forceinline__ df(float h, float l) : hi(h), lo(l) {}
+    __device__ __forceinline__ explicit operator double() const { return (double)hi + (double)lo; }
+};
+__device__ __forceinline__ df df_fast2(float a, float b) {  // |a| >= |b|
+    const float s = __fadd_rn(a, b);
+    return df(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+__device__ __forceinline__ df operator+(df a, df b) {
+    const float s = __fadd_rn(a.hi, b.hi);
+    const float bb = __fsub_rn(s, a.hi);
+    const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+    return df_fast2(s, __fadd_rn(e, __fadd_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ df operator-(df a) { return df(-a.hi, -a.lo); }
+__device__ __forceinline__ df operator-(df a, df b) { return a + (-b); }
+__device__ __forceinline__ df operator*(df a, df b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    const float e = __fmaf_rn(a.hi, b.hi, -p);
+    return df_fast2(p, __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, e)));
+}
+__device__ __forceinline__ df &operator+=(df &a, df b) { return a = a + b; }
+__device__ __forceinline__ df &operator-=(df &a, df b) { return a = a - b; }
+__device__ __forceinline__ df fma(df a, df b, df c) { return a * b + c; }
+__device__ __forceinline__ bool operator<(df a, df b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+__device__ __forceinline__ df fmax(df a, df b) { return a < b ? b : a; }
+__device__ __forceinline__ df __shfl_xor_sync(unsigned mask, df v, int o) {
+    return df(::__shfl_xor_sync(mask, v.hi, o), ::__shfl_xor_sync(mask, v.lo, o));
+}
+// the built-in overloads stay visible beside the double-float ones
+using ::fmax;
+using ::fma;
+using ::__shfl_xor_sync;
+
 // Per-tree context of K2 shared by the column passes.
 struct EmitCtx {
     const int4 *nd;
@@ -1703,12 +1745,12 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
                 if (penalised) penalise(eb);
                 double *row = d.varemit + B.var0 + (size_t)vrow * S;
                 for (int k = lane; k < S; k += 32) row[k] = eb[k];
-            } else if (penalised || d.var64) {
+            } else if (penalised) {
                 // FP64 emissions, penalised, then relative to the column's largest
                 const int X0 = 0;
                 emit_column<double, EM_F64>(ctx, chars, X0, (double (*)[4])wscr,
                                             (double (*)[4])wscr + n, eb);
-                if (penalised) penalise(eb);
+                penalise(eb);
                 double eref = 0.0;
                 for (int k = lane; k < S; k += 32) eref = fmax(eref, eb[k]);
 #pragma unroll
@@ -1756,6 +1798,22 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
                         row[k] = c <= 0.5f ? c : -((1.f - fe[k]) * inv1);
                     }
                     if (lane == 0) d.lnvref[B.vrow0 + vrow] = log(.25) + log1p(-(double)dref);
+                } else if (d.vardf) {
+                    // two or more observed bases: the emissions differ between states by
+                    // factors, and the forward posterior amplifies their relative error
+                    // about 200-fold, so they are formed in double-float and rounded once
+                    df *ed = (df *)eb;
+                    emit_column<df, EM_F64>(ctx, chars, 0, (df (*)[4])wscr, (df (*)[4])wscr + n, ed);
+                    double eref = 0.0;
+                    for (int k = lane; k < S; k += 32) eref = fmax(eref, (double)ed[k]);
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) eref = fmax(eref, ::__shfl_xor_sync(0xffffffffu, eref, o));
+                    const double inv1 = 1.0 / eref;  // 1 / (4 e_ref)
+                    for (int k = lane; k < S; k += 32) {
+                        const double r = (double)ed[k] * inv1;  // e_k / e_ref
+                        row[k] = (float)(r >= 0.5 ? 1.0 - r : -r);
+                    }
+                    if (lane == 0) d.lnvref[B.vrow0 + vrow] = log(.25 * eref);
                 } else if (!internal) {
                     // brackets against the column's largest: D form x / plain form y
                     float *fs = (float *)wscr, *fe = (float *)eb;
@@ -1865,26 +1923,33 @@ void launch_tables(const BatchDev &d, bool want32, cudaStream_t s, int *queue, i
     note_launch();
 }
 
+// K2's shared-memory carve for w warps, offset by offset (16-byte alignment where it aligns);
+// lean: an FP32 batch with FP32 per-state factors and 4-byte scratch only.
+size_t varemit_need(int n, int maxS, bool lean, int w) {
+    const size_t esz = lean ? sizeof(float) : sizeof(double);
+    auto a16 = [](size_t o) { return (o + 15) & ~(size_t)15; };
+    size_t o = (size_t)n * sizeof(int4);                              // nd
+    o = a16(o) + 2 * (size_t)n * sizeof(double);                      // muts, nomuts
+    if (!lean) o = a16(o) + 6 * (size_t)maxS * sizeof(double);        // pm
+    o = a16(o) + (6 * (size_t)n + 4 + maxS) * sizeof(int);            // order .. outp
+    o += (size_t)maxS;                                                // sfloor
+    o = a16(o) + 2 * (size_t)n * sizeof(float);                       // muts32, nomuts32
+    o = a16(o) + 8 * (size_t)maxS * sizeof(float);                    // pm32
+    o = a16(o) + (size_t)w * n * 8 * esz;                             // scratch
+    o += (size_t)w * maxS * esz;                                      // ebuf
+    return o + 16;
+}
+
+bool varemit_full_carve_fits(int maxnodes, int maxS) {
+    return varemit_need(maxnodes, imax(maxS, 1), false, 1) <= 200 * 1024;
+}
+
 template <bool FP32OUT>
 void launch_varemit_t(const BatchDev &d, cudaStream_t s, int *queue, int chunk) {
     const int n = d.maxnodes, maxS = imax(d.maxS, 1);
     const bool lean = FP32OUT && !d.emit64;
-    const size_t esz = lean ? sizeof(float) : sizeof(double);
     int nwarps = 4;
-    // the kernel's carve, offset by offset (16-byte alignment where it aligns)
-    auto need = [&](int w) {
-        auto a16 = [](size_t o) { return (o + 15) & ~(size_t)15; };
-        size_t o = (size_t)n * sizeof(int4);                              // nd
-        o = a16(o) + 2 * (size_t)n * sizeof(double);                      // muts, nomuts
-        if (!lean) o = a16(o) + 6 * (size_t)maxS * sizeof(double);        // pm
-        o = a16(o) + (6 * (size_t)n + 4 + maxS) * sizeof(int);            // order .. outp
-        o += (size_t)maxS;                                                // sfloor
-        o = a16(o) + 2 * (size_t)n * sizeof(float);                       // muts32, nomuts32
-        o = a16(o) + 8 * (size_t)maxS * sizeof(float);                    // pm32
-        o = a16(o) + (size_t)w * n * 8 * esz;                             // scratch
-        o += (size_t)w * maxS * esz;                                      // ebuf
-        return o + 16;
-    };
+    auto need = [&](int w) { return varemit_need(n, maxS, lean, w); };
     while (nwarps > 1 && need(nwarps) > 200 * 1024) nwarps--;
     const size_t smem = need(nwarps);
     if (!queue) {

@@ -245,14 +245,14 @@ __global__ void k_traceback(BatchDev d, int maxS, int slot_elems) {
                 const F t0 = trans[j], t1 = trans[j + 1];
 #pragma unroll
                 for (int g = 0; g < G; g++) {
-                    l0[g] += cg[g][j] * t0;
-                    l1[g] += cg[g][j + 1] * t1;
+                    l0[g] = fma(cg[g][j], t0, l0[g]);
+                    l1[g] = fma(cg[g][j + 1], t1, l1[g]);
                 }
             }
             if (j < hi) {
                 const F t0 = trans[j];
 #pragma unroll
-                for (int g = 0; g < G; g++) l0[g] += cg[g][j] * t0;
+                for (int g = 0; g < G; g++) l0[g] = fma(cg[g][j], t0, l0[g]);
             }
             F incl[G];
 #pragma unroll

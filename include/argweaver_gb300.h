@@ -176,8 +176,9 @@ void get_treelens(awg_local_trees *trees, const double *times, int ntimes, doubl
 void arghmm_get_nstates(awg_local_trees *trees, int ntimes, bool internal, int *nstates);
 
 /* arghmm_forward_alg (sample_thread.cpp:887-926): FP64 forward table, seqlen rows of
- * max(nstates,1) doubles; free with delete_forward_matrix. `slow` is accepted for ABI
- * compatibility (the dense step gives the same table). */
+ * max(nstates,1) doubles; free with delete_forward_matrix. slow: the reference's dense
+ * S x S test step (arghmm_forward_block_slow, sample_thread.cpp:301-337) instead of the
+ * structured one; the same table up to rounding. */
 double **arghmm_forward_alg(awg_local_trees *trees, double *times, int ntimes,
                             double *popsizes, double rho, double mu, char **seqs, int nseqs,
                             int seqlen, bool prior_given, double *prior, bool internal,

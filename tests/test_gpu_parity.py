@@ -317,3 +317,15 @@ def test_conditioned_path_rand_order():
     u = np.zeros(prob.seqlen)
     u[:-1] = pyoracle.rand_uniforms(41, prob.seqlen - 1)
     np.testing.assert_array_equal(path, pyoracle.traceback_last(prob, fw, u, last))
+
+
+@pytest.mark.parametrize("name", ["dsmc_k8_s11", "dsmc_k10_T32", "cut_k10_s3", "single_k7_s41",
+                                  "dsmc_k17_missing"])
+def test_c_abi_forward_alg_slow_dense_step(name):
+    """arghmm_forward_alg(slow=True): the reference's dense S x S test step
+    (arghmm_forward_block_slow, sample_thread.cpp:301-337) gives the structured step's
+    table within rounding (the reference's own test compares the two, test_hmm.py:314-349)."""
+    prob, _ = load(name)
+    rows = refapi.arghmm_forward_alg(prob, slow=True)
+    fw_o, _ = pyoracle.forward(prob)
+    assert max_rel(np.concatenate(rows), fw_o) <= 1e-12

@@ -53,6 +53,15 @@ class LocalTrees:
                                            p.ntrees, p.nnodes, p.start_coord)
         if not self.handle:
             raise ValueError(capi.last_error())
+        # node mappings and root child order the parent arrays do not carry (an ARG after
+        # surgery, e.g. an internal-branch cut), when the problem has them
+        if p.mapping is not None or p.root_child0 is not None:
+            mp = None if p.mapping is None else np.ascontiguousarray(p.mapping, dtype=np.int32)
+            rc = None if p.root_child0 is None else np.ascontiguousarray(p.root_child0, dtype=np.int32)
+            if lib.awg_local_trees_set_structure(
+                    self.handle, None if mp is None else mp.ctypes.data_as(capi.c_int_p),
+                    None if rc is None else rc.ctypes.data_as(capi.c_int_p)) != 0:
+                raise ValueError(capi.last_error())
 
     def close(self):
         if self.handle:

@@ -55,7 +55,24 @@ def parse():
                          "and serving configurations (0: skip)")
     ap.add_argument("--max-columns", type=int, default=0,
                     help="cap each problem's length (small cases for profiling)")
+    ap.add_argument("--one-instance", default="",
+                    help="K,L: run one seeded problem (K haplotypes, L columns, ntimes 20, 0.5%% "
+                         "missing) once, FP32 forward + traceback, print its cell count and "
+                         "exit (a single launch of each kernel, for ncu captures)")
     return ap.parse_args()
+
+
+def one_instance(spec: str, seed: int):
+    from argweaver_gb300 import api
+    from argweaver_gb300.sim import simulate
+
+    k, L = (int(x) for x in spec.split(","))
+    p = simulate(k - 1, L, seed, compress=10, ntimes=20, maxtime=200e3, popsize=1e4,
+                 rho=1.6e-8, mu=1.8e-8, missing=0.005)
+    api.run_batch([p], precision="fp32", want_forward=False, want_path=True)
+    print(json.dumps({"one_instance": {"k": k, "columns": L, "seed": seed,
+                                       "cells": int(p.cells()), "trees": int(p.ntrees),
+                                       "max_states": int(p.nstates_per_tree().max())}}))
 
 
 def make_workload(n: int, seed: int, rank: int = 0, max_columns: int = 0):
@@ -444,6 +461,10 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     threads = os.cpu_count() or 1
+
+    if args.one_instance:
+        one_instance(args.one_instance, args.seed)
+        return
 
     if args.impl == "reference":
         if rank != 0:

@@ -195,8 +195,14 @@ def wide():
         age[v] = 26 + (j * 5) // (nl - 1)
         prev = v
     L = 300
+    # sparse differences, as in real alignments (a column where every base is random would
+    # take the pruning's partials down to about 4^-131, below FP32's range)
     rng = np.random.default_rng(5)
-    seqs = np.frombuffer(b"ACGT", np.uint8)[rng.integers(0, 4, size=(nl + 1, L))]
+    consensus = rng.integers(0, 4, size=L)
+    calls = np.tile(consensus, (nl + 1, 1))
+    hit = rng.random(calls.shape) < 0.01
+    calls[hit] = rng.integers(0, 4, size=int(hit.sum()))
+    seqs = np.frombuffer(b"ACGT", np.uint8)[calls]
     p = Problem(times=base.times, popsizes=base.popsizes, rho=base.rho, mu=base.mu,
                 ptrees=par[None, :].copy(), ages=age[None, :].copy(),
                 sprs=np.full((1, 4), -1, np.int32), blocklens=np.array([L], np.int32),

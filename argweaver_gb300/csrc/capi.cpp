@@ -761,10 +761,15 @@ int get_local_trees_nnodes(awg_local_trees *trees) { return trees ? trees->nnode
 void arghmm_get_nstates(awg_local_trees *trees, int ntimes, bool internal, int *nstates) {
     if (!trees || !nstates) return;
     int pos = 0;
+    const int n = trees->nnodes;
     for (int b = 0; b < trees->ntrees; b++) {
-        int S = awg::count_states(&trees->ptrees[(size_t)b * trees->nnodes],
-                                  &trees->ages[(size_t)b * trees->nnodes], trees->nnodes,
-                                  ntimes, internal, 0, -1, nullptr);
+        // internal: the cut subtree is the root's child[0] as the trees keep it
+        int rc0 = -1;
+        if (!trees->c0.empty())
+            for (int i = 0; i < n; i++)
+                if (trees->ptrees[(size_t)b * n + i] == -1) rc0 = trees->c0[(size_t)b * n + i];
+        int S = awg::count_states(&trees->ptrees[(size_t)b * n], &trees->ages[(size_t)b * n], n,
+                                  ntimes, internal, 0, rc0, nullptr);
         for (int i = 0; i < trees->blocklens[b]; i++) nstates[pos + i] = S;
         pos += trees->blocklens[b];
     }

@@ -1179,7 +1179,6 @@ __device__ __forceinline__ df operator*(df a, df b) {
     return df_fast2(p, __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, e)));
 }
 __device__ __forceinline__ df &operator+=(df &a, df b) { return a = a + b; }
-__device__ __forceinline__ df &operator-=(df &a, df b) { return a = a - b; }
 __device__ __forceinline__ df fma(df a, df b, df c) { return a * b + c; }
 __device__ __forceinline__ bool operator<(df a, df b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
 __device__ __forceinline__ df fmax(df a, df b) { return a < b ? b : a; }
@@ -1299,32 +1298,44 @@ enum { EM_REF = 0, EM_F64 = 1, EM_REL = 2, EM_SNP = 3 };
 // One variant column by one warp: inner partials by height level, outer partials by
 // depth, then the states' emissions (4 e_k, or D_k = 1 - 4 e_k in the relative form) into
 // eb[S]. Returns, over the warp, the reference value: the largest 4 e_k, or the smallest D_k.
-template <typename R, int MODE>
-__device__ R emit_column(const EmitCtx &c, const uint8_t *chars, int X, R (*in)[4], R (*out)[4],
+// Partials of type P rounded to the states' type R.
+template <typename R, typename P>
+__device__ __forceinline__ R to_r(P v) {
+    if constexpr (std::is_same<P, df>::value && std::is_same<R, float>::value) return v.hi;
+    else return (R)v;
+}
+
+// P: the type of the inner and outer partials (the tree pass); R: the type of the states'
+// split-branch steps and emissions. The FP32 path takes P = double-float with R = FP32: a
+// partial is the outcome of a chain of JC69 steps as long as the tree is deep, the states'
+// own steps are three.
+template <typename R, int MODE, typename P = R>
+__device__ R emit_column(const EmitCtx &c, const uint8_t *chars, int X, P (*in)[4], P (*out)[4],
                          R *eb) {
     const int lane = threadIdx.x & 31;
     const int4 *nd = c.nd;
-    auto leaf = [&](uint8_t ch, R *v) {
-        if constexpr (MODE == EM_REL) leaf_partial_x<R>(ch, X, v);
-        else leaf_partial<R>(ch, v);
+    auto leaf = [&](uint8_t ch, P *v) {
+        if constexpr (MODE == EM_REL) leaf_partial_x<P>(ch, X, v);
+        else leaf_partial<P>(ch, v);
     };
     constexpr bool F32 = std::is_same<R, float>::value;
-    auto bm = [&](int j) -> R { if constexpr (F32) return c.muts32[j]; else return (R)c.muts[j]; };
-    auto bn = [&](int j) -> R { if constexpr (F32) return c.nomuts32[j]; else return (R)c.nomuts[j]; };
-    auto step = [&](const R *x, R m, R nm, R *y) {
-        const double m64 = (double)m, nm64 = (double)nm;
+    constexpr bool PF32 = std::is_same<P, float>::value;
+    auto bm = [&](int j) -> P { if constexpr (PF32) return c.muts32[j]; else return (P)c.muts[j]; };
+    auto bn = [&](int j) -> P { if constexpr (PF32) return c.nomuts32[j]; else return (P)c.nomuts[j]; };
+    auto step = [&](const auto *x, auto m, auto nm, auto *y) {
+        using T = decltype(m);
         if constexpr (MODE == EM_REL) {
-            jc_apply_x<R>(x, m, nm, y);
+            jc_apply_x<T>(x, m, nm, y);
         } else if constexpr (MODE == EM_F64 || MODE == EM_SNP) {
-            const R sum = (x[0] + x[1]) + (x[2] + x[3]);
+            const T sum = (x[0] + x[1]) + (x[2] + x[3]);
 #pragma unroll
             for (int a = 0; a < 4; a++) y[a] = fma(nm - m, x[a], m * sum);
         } else {
-            jc_apply<false>((const double *)x, m64, nm64, (double *)y);
+            jc_apply<false>((const double *)x, (double)m, (double)nm, (double *)y);
         }
     };
-    auto mul = [&](const R *a, const R *b, R *z) {
-        z[0] = MODE == EM_REL ? cprod<R>(a[0], b[0]) : a[0] * b[0];
+    auto mul = [&](const P *a, const P *b, P *z) {
+        z[0] = MODE == EM_REL ? cprod<P>(a[0], b[0]) : a[0] * b[0];
 #pragma unroll
         for (int t = 1; t < 4; t++) z[t] = a[t] * b[t];
     };
@@ -1335,7 +1346,7 @@ __device__ R emit_column(const EmitCtx &c, const uint8_t *chars, int X, R (*in)[
         for (int x = c.inp[h] + lane; x < c.inp[h + 1]; x += 32) {
             const int j = c.inl[x];
             const int c1 = nd[j].y, c2 = nd[j].z;
-            R p1[4], p2[4];
+            P p1[4], p2[4];
             step(in[c1], bm(c1), bn(c1), p1);
             step(in[c2], bm(c2), bn(c2), p2);
             mul(p1, p2, in[j]);
@@ -1347,16 +1358,16 @@ __device__ R emit_column(const EmitCtx &c, const uint8_t *chars, int X, R (*in)[
         for (int x = c.outp[h] + lane; x < c.outp[h + 1]; x += 32) {
             const int j = c.outl[x];
             if (j == c.mainr) {
-                out[j][0] = MODE == EM_REL ? R(0) : R(1);
-                out[j][1] = out[j][2] = out[j][3] = R(1);
+                out[j][0] = MODE == EM_REL ? P(0) : P(1);
+                out[j][1] = out[j][2] = out[j][3] = P(1);
                 continue;
             }
             const int p = nd[j].x;
             const int sib = nd[p].y == j ? nd[p].z : nd[p].y;
-            R p1[4];
+            P p1[4];
             step(in[sib], bm(sib), bn(sib), p1);
             if (p != c.mainr) {
-                R p2[4];
+                P p2[4];
                 step(out[p], bm(p), bn(p), p2);
                 mul(p1, p2, out[j]);
             } else {
@@ -1369,16 +1380,18 @@ __device__ R emit_column(const EmitCtx &c, const uint8_t *chars, int X, R (*in)[
     // leaf partial of the threaded sequence (external) or the subtree root (internal)
     R in2[4];
     if (c.internal) {
-        for (int a = 0; a < 4; a++) in2[a] = in[c.node1][a];
+        for (int a = 0; a < 4; a++) in2[a] = to_r<R>(in[c.node1][a]);
     } else {
-        leaf(chars[c.nleaves], in2);
+        P lp[4];
+        leaf(chars[c.nleaves], lp);
+        for (int a = 0; a < 4; a++) in2[a] = to_r<R>(lp[a]);
     }
     R ref = MODE == EM_REL || MODE == EM_SNP ? R(4) : R(0);
     R vmax = R(0);  // SNP: the largest bracket among states in the plain form
     R wcol = R(1);  // SNP: the column's W, sum over the main root's inner partial
     if constexpr (MODE == EM_SNP) {
-        const R *im = in[c.mainr];
-        wcol = (im[0] + im[1]) + (im[2] + im[3]);
+        const P *im = in[c.mainr];
+        wcol = to_r<R>((im[0] + im[1]) + (im[2] + im[3]));
     }
     // SNP: the threaded base (external trees), 4 for a missing call
     const uint8_t chb = MODE == EM_SNP ? chars[c.nleaves] : 'N';
@@ -1395,10 +1408,15 @@ __device__ R emit_column(const EmitCtx &c, const uint8_t *chars, int X, R (*in)[
             for (int t = 0; t < 6; t++) q[t] = (R)c.pm[6 * k + t];
             q[6] = R(1) - R(4) * q[0];
         }
-        R p1[4], p2[4], p3[4];
+        R p1[4], p2[4], p3[4], x2[4], x3[4];
+#pragma unroll
+        for (int a = 0; a < 4; a++) {
+            x2[a] = to_r<R>(in[node2][a]);
+            x3[a] = to_r<R>(out[node2][a]);
+        }
         if constexpr (MODE != EM_SNP) step(in2, q[0], q[3], p1);
-        step(in[node2], q[1], q[4], p2);
-        if (node2 != c.mainr) step(out[node2], q[2], q[5], p3);
+        step(x2, q[1], q[4], p2);
+        if (node2 != c.mainr) step(x3, q[2], q[5], p3);
         else p3[0] = p3[1] = p3[2] = p3[3] = R(1);
         R v;  // calc_emit (emit.cpp:620-645)
         if constexpr (MODE == EM_SNP) {
@@ -1788,17 +1806,21 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
                     near = !__any_sync(0xffffffffu, other);
                 }
                 float *row = d.var32 + B.var0 + (size_t)vrow * S;
-                if (near) {
+                if (near && d.vardf != 2) {
                     float *fs = (float *)wscr, *fe = (float *)eb;
-                    const float dref = emit_column<float, EM_REL>(ctx, chars, X, (float (*)[4])fs,
-                                                                  (float (*)[4])fs + n, fe);
+                    const float dref =
+                        d.vardf == 1
+                            ? emit_column<float, EM_REL, df>(ctx, chars, X, (df (*)[4])wscr,
+                                                             (df (*)[4])wscr + n, fe)
+                            : emit_column<float, EM_REL>(ctx, chars, X, (float (*)[4])fs,
+                                                         (float (*)[4])fs + n, fe);
                     const float inv1 = 1.f / (1.f - dref);  // 1 / (4 e_ref)
                     for (int k = lane; k < S; k += 32) {
                         const float c = (fe[k] - dref) * inv1;  // 1 - e_k / e_ref
                         row[k] = c <= 0.5f ? c : -((1.f - fe[k]) * inv1);
                     }
                     if (lane == 0) d.lnvref[B.vrow0 + vrow] = log(.25) + log1p(-(double)dref);
-                } else if (d.vardf) {
+                } else if (d.vardf == 2) {
                     // two or more observed bases: the emissions differ between states by
                     // factors, and the forward posterior amplifies their relative error
                     // about 200-fold, so they are formed in double-float and rounded once
@@ -1817,8 +1839,12 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
                 } else if (!internal) {
                     // brackets against the column's largest: D form x / plain form y
                     float *fs = (float *)wscr, *fe = (float *)eb;
-                    const float ref = emit_column<float, EM_SNP>(ctx, chars, X, (float (*)[4])fs,
-                                                                 (float (*)[4])fs + n, fe);
+                    const float ref =
+                        d.vardf == 1
+                            ? emit_column<float, EM_SNP, df>(ctx, chars, X, (df (*)[4])wscr,
+                                                             (df (*)[4])wscr + n, fe)
+                            : emit_column<float, EM_SNP>(ctx, chars, X, (float (*)[4])fs,
+                                                         (float (*)[4])fs + n, fe);
                     const float bref = ref >= 0.f ? 1.f - ref : -ref;  // the largest bracket
                     const float inv1 = 1.f / bref;
                     for (int k = lane; k < S; k += 32) {
@@ -1833,8 +1859,14 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
                     }
                     if (lane == 0) {
                         // W: the tree's own likelihood, sum over the main root's inner partial
-                        const float *im = fs + 4 * mainr;
-                        const double w = (double)((im[0] + im[1]) + (im[2] + im[3]));
+                        double w;
+                        if (d.vardf == 1) {
+                            const df *im = (const df *)wscr + 4 * mainr;
+                            w = (double)((im[0] + im[1]) + (im[2] + im[3]));
+                        } else {
+                            const float *im = fs + 4 * mainr;
+                            w = (double)((im[0] + im[1]) + (im[2] + im[3]));
+                        }
                         d.lnvref[B.vrow0 + vrow] = log(.25 * w * (double)bref);
                     }
                 } else {

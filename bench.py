@@ -37,7 +37,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "HMM state-cells/s fwd+traceback, batched FP32 vs plain FP64 @<=1e-5 err; p50/p99"
-FWD_DRAM_BYTES_PER_CELL = 3.93  # forward kernel, ncu capture summarised in profiles/
+FWD_DRAM_BYTES_PER_CELL = 7.26  # forward kernel, ncu capture summarised in profiles/
 UNIT = "state-cells/s"
 
 
@@ -634,9 +634,10 @@ def main():
                 "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99))},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm,
-                     # DRAM bytes of one forward launch: ncu dram__bytes_read.sum +
-                     # dram__bytes_write.sum on the 16 x 10,000-column capture, 3.93 B per
-                     # state-cell, scaled to this launch's cells (profiles/)
+                     # DRAM bytes of the forward launches: ncu dram__bytes_read.sum +
+                     # dram__bytes_write.sum of one k = 64, 100,000-column launch
+                     # (--one-instance 64,100000), 7.26 B per state-cell, scaled to this
+                     # step's cells (profiles/forward_traffic_k64_1e5.md)
                      "traffic": FWD_DRAM_BYTES_PER_CELL * cells, "peak_source": src,
                      "kernel": "forward (k_forward_reg), 4 B of FP32 table written per cell, "
                                "timed alone (phases run one after another)"},

@@ -23,3 +23,18 @@ def test_state_spaces(name):
         want = [(i, t) for i in range(prob.nnodes)
                 for t in range(age[i], (prob.ntimes - 2 if par[i] == -1 else age[par[i]]) + 1)]
         assert [tuple(x) for x in st.tolist()] == want
+
+
+@pytest.mark.parametrize("name", ["cut_k10_s3", "large_cut_k50_s19"])
+def test_internal_state_counts_follow_the_root_child_order(name):
+    """arghmm_get_nstates(internal=True) on a trees handle that keeps each root's child[0]
+    (the cut subtree): the oracle's per-column counts, the layout of every internal table
+    the C ABI returns."""
+    prob, _ = load_golden(name)
+    assert prob.internal
+    trees = refapi.LocalTrees(prob.normalized())
+    try:
+        got = refapi.get_nstates(trees, prob.ntimes, True, prob.seqlen)
+    finally:
+        trees.close()
+    np.testing.assert_array_equal(np.maximum(got, 0), pyoracle.nstates(prob))

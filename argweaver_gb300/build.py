@@ -41,8 +41,8 @@ def nvcc_flags(src: str):
     return NVCC_FLAGS
 
 CUDA_SOURCES = ["host_plan.cpp", "tables.cu", "forward.cu", "traceback.cu",
-                "backward.cu", "batch.cu", "static_run.cu", "dense_hmm.cu", "arg_prob.cu",
-                "recomb.cu", "capi.cpp", "server.cpp", "formats.cpp",
+                "backward.cu", "batch.cu", "static_run.cu", "dense_hmm.cu", "dense_tables.cu",
+                "arg_prob.cu", "recomb.cu", "capi.cpp", "server.cpp", "formats.cpp",
                 "arg_surgery.cpp"]
 
 

@@ -76,6 +76,18 @@ PROTOTYPES = [
     ("delete_path", None, [c_int_p]),
     ("delete_double_matrix", None, [c_double_pp, C.c_int]),
     ("delete_forward_matrix", None, [c_double_pp, C.c_int]),
+    ("new_transition_probs", c_double_pp,
+     [C.c_int, c_int_p, c_int_p, C.c_double, c_int_p, C.c_int, C.c_int, c_double_p, c_double_p,
+      c_int_p, c_int_p, c_int_p, c_double_p, C.c_double]),
+    ("new_transition_probs_switch", c_double_pp,
+     [c_int_p, c_int_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, c_int_p, c_int_p,
+      C.c_double, C.c_double, c_int_p, C.c_int, c_int_p, C.c_int, C.c_int, c_double_p,
+      c_double_p, c_int_p, c_int_p, c_int_p, c_double_p, C.c_double]),
+    ("delete_transition_probs", None, [c_double_pp, C.c_int]),
+    ("new_emissions", c_double_pp,
+     [c_int_p, C.c_int, c_int_p, C.c_int, c_int_p, C.POINTER(C.c_char_p), C.c_int, C.c_int,
+      c_double_p, C.c_int, C.c_double]),
+    ("delete_emissions", None, [c_double_pp, C.c_int]),
     ("arghmm_likelihood", C.c_double, [C.c_void_p, c_double_p, C.c_int, C.c_double,
                                         c_char_pp, C.c_int, C.c_int]),
     ("arghmm_prior_prob", C.c_double, [C.c_void_p, c_double_p, C.c_int, c_double_p,

@@ -72,10 +72,9 @@ struct StateInfo {
 // Device views of a batch (all pointers are device memory).
 struct BatchDev {
     int ninst, nblocks, maxS, maxT, maxnodes, maxM;
-    int vardf;                   // FP32 path, variant columns: 1 = the tree pass's partials
-                                 // in double-float, the states' steps in FP32; 2 = all of
-                                 // it in double-float; 0 = FP32 (1 and 2 need emit64's
-                                 // carve: 0 where that carve does not fit)
+    int vardf;                   // FP32 path: variant columns formed in double-float and
+                                 // rounded once (needs emit64's carve; off where that carve
+                                 // does not fit: FP32 forms)
     int emit64;                  // some instance forms FP64 emission partials even on the
                                  // FP32 path (internal-branch or infinite-sites problems)
     const InstDev *inst;

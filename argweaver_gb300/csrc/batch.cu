@@ -186,7 +186,9 @@ bool raise_dynamic_smem_fn(const void *kernel, size_t bytes) {
 // straight to the caller's buffers and the call returns when they are there. Asynchronous:
 // outputs go to C's page-locked staging, C.done marks their arrival, and ctx_complete (on
 // the same thread, before C's next batch) checks the device error record and hands them
-// over. timing: 0 off, 1 one compute time, 2 kernels one phase after another.
+// over. timing: 0 off, 1 one compute time, 2 kernels one phase after another. Returns 0,
+// 1 when a debug or dense-table call finished inside it (nothing left for ctx_complete), or
+// a negative code with err set.
 int ctx_launch(Ctx &C, const awg_problem *probs, awg_outputs *outs, int n, const RunOptions &opt,
                bool async, int timing, long long *key_out, std::string &err,
                size_t *dry_bytes) {
@@ -196,6 +198,7 @@ int ctx_launch(Ctx &C, const awg_problem *probs, awg_outputs *outs, int n, const
     if (!fp32 && opt.precision != AWG_FP64) { err = "precision must be AWG_FP64 or AWG_FP32"; return -1; }
     if (fp32 && opt.last_states) { err = "a given last traceback state needs AWG_FP64"; return -1; }
     if (fp32 && opt.dense) { err = "the dense forward step needs AWG_FP64"; return -1; }
+    if (fp32 && opt.dense_kind) { err = "the dense helper matrices need AWG_FP64"; return -1; }
 
     HostPlan &plan = C.plan;
     plan = HostPlan();
@@ -462,7 +465,8 @@ int ctx_launch(Ctx &C, const awg_problem *probs, awg_outputs *outs, int n, const
     // per-tree work of later groups fills the SMs they leave idle. The per-tree kernels are
     // persistent, work-stealing over units of trees; the device part of a step is captured
     // once as a CUDA graph and replayed while its launch parameters repeat.
-    const bool special = opt.tables_only || opt.priors || opt.last_states || opt.dense;
+    const bool special =
+        opt.tables_only || opt.priors || opt.last_states || opt.dense || opt.dense_kind;
     const bool serial_timing = timing == 2;
     const bool pipelined = n >= 16 && !special && !serial_timing;
     const bool T = timing != 0;
@@ -612,6 +616,16 @@ int ctx_launch(Ctx &C, const awg_problem *probs, awg_outputs *outs, int n, const
     } else {
         launch_tables(d, fp32, s);
         CKL("table kernel");
+        if (opt.dense_kind) {
+            if (opt.dense_kind == DENSE_EMISSIONS) {
+                launch_varemit(d, fp32, s);
+                CKL("emission kernel");
+            }
+            const int rc = dense_tables(d, opt.dense_kind, opt.dense_rows, opt.dense_nrows,
+                                        opt.dense_cols, opt.dense_ncols, opt.dense_ncolumns,
+                                        opt.dense_out, s, err);
+            return rc != 0 ? rc : 1;  // finished: nothing left for ctx_complete
+        }
         if (opt.priors) {
             for (int q = 0; q < n; q++) {
                 if (!opt.priors[q]) continue;
@@ -658,7 +672,7 @@ int ctx_launch(Ctx &C, const awg_problem *probs, awg_outputs *outs, int n, const
                             opt.dbg_tm[((size_t)b * (T - 1) + a) * (T - 1) + c] =
                                 tmall[((size_t)b * MAXT + a) * MAXT + c];
             }
-            return 0;
+            return 1;  // finished: nothing left for ctx_complete
         }
         if (T) CK(cudaEventRecord(C.ev[2], s));
         launch_varemit(d, fp32, s);
@@ -911,6 +925,7 @@ int run_batch(const awg_problem *probs, awg_outputs *outs, int n, const RunOptio
     long long key = -1;
     const int rc = ctx_launch(E.ctx, probs, outs, n, opt, false, E.timing, &key, err, nullptr);
     E.last_key = key;
+    if (rc == 1) return 0;  // a debug or dense-table call that finished inside the launch
     if (rc != 0) {
         if (E.ctx.init) cudaStreamSynchronize(E.ctx.stream);  // nothing left in flight
         return rc;

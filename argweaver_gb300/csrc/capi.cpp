@@ -1035,6 +1035,190 @@ void delete_double_matrix(double **mat, int nrows) {
     delete[] mat;
 }
 
+}  // extern "C"
+
+// ---- the reference's dense helper matrices (its ctypes layer's test and plotting aids)
+
+namespace {
+
+// state index of (node, time) in a tree's external state list (get_coal_states,
+// states.cpp:53-74: nodes in index order, times from the node's age to its parent's, the
+// root's to ntimes - 2), or -1
+struct StateIndex {
+    std::vector<int> first, lo, hi;
+    StateIndex(const int *ptree, const int *ages, int nnodes, int ntimes)
+        : first(nnodes), lo(nnodes), hi(nnodes) {
+        int S = 0;
+        for (int v = 0; v < nnodes; v++) {
+            lo[v] = ages[v];
+            hi[v] = ptree[v] == -1 ? ntimes - 2 : ages[ptree[v]];
+            first[v] = S;
+            S += std::max(0, hi[v] - lo[v] + 1);
+        }
+    }
+    int operator()(int node, int time) const {
+        if (node < 0 || node >= (int)first.size() || time < lo[node] || time > hi[node]) return -1;
+        return first[node] + time - lo[node];
+    }
+};
+
+bool map_states(const awg_intstate *istates, int n, const StateIndex &ix, std::vector<int> &out,
+                const char *who) {
+    out.resize(std::max(n, 0));
+    for (int i = 0; i < n; i++) {
+        out[i] = ix(istates[i][0], istates[i][1]);
+        if (out[i] < 0) {
+            set_error(std::string(who) + ": state " + std::to_string(i) + " (node " +
+                      std::to_string(istates[i][0]) + ", time " + std::to_string(istates[i][1]) +
+                      ") is not a coalescence state of its tree");
+            return false;
+        }
+    }
+    return true;
+}
+
+// nrows row pointers into one block of nrows * ncols doubles (freed by delete_double_matrix
+// and its aliases)
+double **new_dense(int nrows, int ncols) {
+    double **m = new double *[std::max(nrows, 1)];
+    double *blk = new double[std::max((size_t)nrows * ncols, (size_t)1)];
+    for (int i = 0; i < nrows; i++) m[i] = blk + (size_t)i * ncols;
+    if (nrows == 0) m[0] = blk;
+    return m;
+}
+
+double **dense_call(const awg_problem &p, int kind, const std::vector<int> &rows,
+                    const std::vector<int> &cols, int ncolumns, const char *who) {
+    const int nr = kind == awg::DENSE_EMISSIONS ? ncolumns : (int)rows.size();
+    double **m = new_dense(nr, (int)cols.size());
+    awg_outputs o;
+    memset(&o, 0, sizeof(o));
+    awg::RunOptions opt;
+    opt.dense_kind = kind;
+    opt.dense_rows = rows.data();
+    opt.dense_nrows = (int)rows.size();
+    opt.dense_cols = cols.data();
+    opt.dense_ncols = (int)cols.size();
+    opt.dense_ncolumns = ncolumns;
+    opt.dense_out = m[0];
+    std::string err;
+    if (awg::run_batch(&p, &o, 1, opt, err) != 0) {
+        set_error(std::string(who) + ": " + err);
+        delete[] m[0];
+        delete[] m;
+        return nullptr;
+    }
+    return m;
+}
+
+}  // namespace
+
+extern "C" {
+
+double **new_transition_probs(int nnodes, int *ptree, int *ages, double treelen,
+                              awg_intstate *istates, int nstates, int ntimes, double *times,
+                              double *time_steps, int *nbranches, int *nrecombs, int *ncoals,
+                              double *popsizes, double rho) {
+    // treelen, time_steps and the lineage counts are the caller's copies of what the table
+    // kernel derives from the tree and the times (the reference recomputes them too)
+    (void)treelen; (void)time_steps; (void)nbranches; (void)nrecombs; (void)ncoals;
+    g_err.clear();
+    if (!ptree || !ages || !times || !popsizes || (nstates > 0 && !istates) || nnodes < 1) {
+        set_error("new_transition_probs: bad arguments");
+        return nullptr;
+    }
+    std::vector<int> idx;
+    if (!map_states(istates, nstates, StateIndex(ptree, ages, nnodes, ntimes), idx,
+                    "new_transition_probs"))
+        return nullptr;
+    const int nseqs = (nnodes + 1) / 2 + 1;
+    std::vector<char> seqs(nseqs, 'N');
+    int sprs[4] = {-1, -1, -1, -1}, blocklen = 1;
+    awg_problem p;
+    memset(&p, 0, sizeof(p));
+    p.ntrees = 1; p.nnodes = nnodes; p.ntimes = ntimes; p.nseqs = nseqs; p.seqlen = 1;
+    p.ptrees = ptree; p.ages = ages; p.sprs = sprs; p.blocklens = &blocklen;
+    p.times = times; p.popsizes = popsizes; p.rho = rho; p.mu = 0.0; p.seqs = seqs.data();
+    return dense_call(p, awg::DENSE_TRANSITION, idx, idx, 0, "new_transition_probs");
+}
+
+double **new_transition_probs_switch(int *ptree, int *last_ptree, int nnodes, int recomb_node,
+                                     int recomb_time, int coal_node, int coal_time,
+                                     int *ages_index, int *last_ages_index, double treelen,
+                                     double last_treelen, awg_intstate *istates1, int nstates1,
+                                     awg_intstate *istates2, int nstates2, int ntimes,
+                                     double *times, double *time_steps, int *nbranches,
+                                     int *nrecombs, int *ncoals, double *popsizes, double rho) {
+    (void)treelen; (void)last_treelen; (void)time_steps; (void)nbranches; (void)nrecombs;
+    (void)ncoals;
+    g_err.clear();
+    if (!ptree || !last_ptree || !ages_index || !last_ages_index || !times || !popsizes ||
+        (nstates1 > 0 && !istates1) || (nstates2 > 0 && !istates2) || nnodes < 1) {
+        set_error("new_transition_probs_switch: bad arguments");
+        return nullptr;
+    }
+    std::vector<int> rows, cols;
+    if (!map_states(istates1, nstates1, StateIndex(last_ptree, last_ages_index, nnodes, ntimes),
+                    rows, "new_transition_probs_switch") ||
+        !map_states(istates2, nstates2, StateIndex(ptree, ages_index, nnodes, ntimes), cols,
+                    "new_transition_probs_switch"))
+        return nullptr;
+    // two trees of one column each; the node mapping is make_node_mapping's (local_tree.h:
+    // 767-778), as the reference builds it here
+    std::vector<int> pt(2 * (size_t)nnodes), ag(2 * (size_t)nnodes);
+    std::copy(last_ptree, last_ptree + nnodes, pt.begin());
+    std::copy(ptree, ptree + nnodes, pt.begin() + nnodes);
+    std::copy(last_ages_index, last_ages_index + nnodes, ag.begin());
+    std::copy(ages_index, ages_index + nnodes, ag.begin() + nnodes);
+    int sprs[8] = {-1, -1, -1, -1, recomb_node, recomb_time, coal_node, coal_time};
+    int blocklens[2] = {1, 1};
+    const int nseqs = (nnodes + 1) / 2 + 1;
+    std::vector<char> seqs(2 * (size_t)nseqs, 'N');
+    awg_problem p;
+    memset(&p, 0, sizeof(p));
+    p.ntrees = 2; p.nnodes = nnodes; p.ntimes = ntimes; p.nseqs = nseqs; p.seqlen = 2;
+    p.ptrees = pt.data(); p.ages = ag.data(); p.sprs = sprs; p.blocklens = blocklens;
+    p.times = times; p.popsizes = popsizes; p.rho = rho; p.mu = 0.0; p.seqs = seqs.data();
+    return dense_call(p, awg::DENSE_SWITCH, rows, cols, 0, "new_transition_probs_switch");
+}
+
+void delete_transition_probs(double **transmat, int nstates) {
+    delete_double_matrix(transmat, nstates);
+}
+
+double **new_emissions(awg_intstate *istates, int nstates, int *ptree, int nnodes,
+                       int *ages_index, char **seqs, int nseqs, int seqlen, double *times,
+                       int ntimes, double mu) {
+    g_err.clear();
+    if (!ptree || !ages_index || !seqs || !times || (nstates > 0 && !istates) || nnodes < 1 ||
+        seqlen < 0 || nseqs < 1) {
+        set_error("new_emissions: bad arguments");
+        return nullptr;
+    }
+    std::vector<int> idx;
+    if (!map_states(istates, nstates, StateIndex(ptree, ages_index, nnodes, ntimes), idx,
+                    "new_emissions"))
+        return nullptr;
+    // one tree over a masked column (the forward's first column, which has no emission)
+    // followed by the caller's columns
+    const int L = seqlen + 1;
+    std::vector<char> sq((size_t)nseqs * L);
+    for (int j = 0; j < nseqs; j++) {
+        sq[(size_t)j * L] = 'N';
+        memcpy(&sq[(size_t)j * L + 1], seqs[j], seqlen);
+    }
+    std::vector<double> pops(ntimes, 1.0);  // the model's popsizes do not enter emissions
+    int sprs[4] = {-1, -1, -1, -1};
+    awg_problem p;
+    memset(&p, 0, sizeof(p));
+    p.ntrees = 1; p.nnodes = nnodes; p.ntimes = ntimes; p.nseqs = nseqs; p.seqlen = L;
+    p.ptrees = ptree; p.ages = ages_index; p.sprs = sprs; p.blocklens = &L;
+    p.times = times; p.popsizes = pops.data(); p.rho = 0.0; p.mu = mu; p.seqs = sq.data();
+    return dense_call(p, awg::DENSE_EMISSIONS, {}, idx, seqlen, "new_emissions");
+}
+
+void delete_emissions(double **emit, int seqlen) { delete_double_matrix(emit, seqlen); }
+
 void delete_forward_matrix(double **mat, int nrows) {
     (void)nrows;
     if (!mat) return;

@@ -26,6 +26,13 @@ struct RunOptions {
     const int *last_states = nullptr;       // per problem: the traceback's given last state
                                             // (FP64 only), or -1 to sample it
     double *const *backward = nullptr;      // per problem: backward table output, or NULL
+    // Dense helper matrices (dense_tables, kernels.h) of problem 0, FP64: kind 1-3, the
+    // state indices of the rows and columns, the columns of an emission matrix, the host
+    // output; the batch stops after them
+    int dense_kind = 0;
+    const int *dense_rows = nullptr, *dense_cols = nullptr;
+    int dense_nrows = 0, dense_ncols = 0, dense_ncolumns = 0;
+    double *dense_out = nullptr;
     // Debug: stop after the table kernel and copy its FP64 tables of problem 0 out:
     // tmatrix [ntrees][T-1][T-1], same-branch rows [sum M], invariant emissions
     // [sum max(S,1)], column-0 prior [max(S0,1)].

@@ -26,6 +26,15 @@ bool varemit_full_carve_fits(int maxnodes, int maxS);
 void launch_forward(const BatchDev &d, bool fp32, cudaStream_t s, int kpt = 0);
 // K3 with the reference's dense test step (arghmm_forward_block_slow), FP64.
 void launch_forward_dense(const BatchDev &d, cudaStream_t s);
+
+// The reference's dense helper matrices of one tree (or one boundary) from the table and
+// emission kernels' FP64 outputs, into out (host, row-major): DENSE_TRANSITION log P(rows[r]
+// -> cols[c]) in tree 0; DENSE_SWITCH log P(rows[r] of tree 0 -> cols[c] of tree 1);
+// DENSE_EMISSIONS P(column 1 + i | cols[c]) of tree 0 for i < ncolumns. Synchronous;
+// 0 or -3 with err set (also when the table kernels recorded a device error).
+enum { DENSE_TRANSITION = 1, DENSE_SWITCH = 2, DENSE_EMISSIONS = 3 };
+int dense_tables(const BatchDev &d, int kind, const int *rows, int nr, const int *cols, int nc,
+                 int ncolumns, double *out, cudaStream_t s, std::string &err);
 // Whether K3 writes the FP32 columns' time-bin sums (BatchDev::bins32) for a batch of these
 // largest sizes (the register-resident variant does; the fallback for the largest trees
 // does not).

@@ -1151,9 +1151,11 @@ __device__ __forceinline__ R cprod(R a, R b) { return (a + b) - a * b; }
 
 // Double-float: value = hi + lo, |lo| <= ulp(hi) / 2, about 48 significant bits, from
 // FP32 error-free transforms (Knuth's two-sum; the product's error by fused multiply-add).
-// The FP32 path's emissions of columns with two or more observed bases are formed in it:
-// the forward posterior amplifies a relative error of those emissions roughly 200-fold, so
-// they must reach FP32 as correctly rounded ratios, which FP32 arithmetic does not give.
+// The FP32 path's variant-column emissions are formed in it: the forward posterior amplifies
+// an error of those emissions thousands-fold on the columns where they differ little between
+// states, so they must reach FP32 as correctly rounded ratios to the column's largest. FP32
+// forms left the posterior up to 6.6e-5 from FP64's (9.1e-5 with only the partials in
+// double-float); double-float, 3.1e-6 (k = 64, 100,000 columns).
 struct df {
     float hi, lo;
     __device__ __forceinline__ df() : hi(0.f), lo(0.f) {}
@@ -1179,7 +1181,6 @@ __device__ __forceinline__ df operator*(df a, df b) {
     return df_fast2(p, __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, e)));
 }
 __device__ __forceinline__ df &operator+=(df &a, df b) { return a = a + b; }
-__device__ __forceinline__ df fma(df a, df b, df c) { return a * b + c; }
 __device__ __forceinline__ bool operator<(df a, df b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
 __device__ __forceinline__ df fmax(df a, df b) { return a < b ? b : a; }
 __device__ __forceinline__ df __shfl_xor_sync(unsigned mask, df v, int o) {
@@ -1187,7 +1188,6 @@ __device__ __forceinline__ df __shfl_xor_sync(unsigned mask, df v, int o) {
 }
 // the built-in overloads stay visible beside the double-float ones
 using ::fmax;
-using ::fma;
 using ::__shfl_xor_sync;
 
 // Per-tree context of K2 shared by the column passes.
@@ -1298,44 +1298,32 @@ enum { EM_REF = 0, EM_F64 = 1, EM_REL = 2, EM_SNP = 3 };
 // One variant column by one warp: inner partials by height level, outer partials by
 // depth, then the states' emissions (4 e_k, or D_k = 1 - 4 e_k in the relative form) into
 // eb[S]. Returns, over the warp, the reference value: the largest 4 e_k, or the smallest D_k.
-// Partials of type P rounded to the states' type R.
-template <typename R, typename P>
-__device__ __forceinline__ R to_r(P v) {
-    if constexpr (std::is_same<P, df>::value && std::is_same<R, float>::value) return v.hi;
-    else return (R)v;
-}
-
-// P: the type of the inner and outer partials (the tree pass); R: the type of the states'
-// split-branch steps and emissions. The FP32 path takes P = double-float with R = FP32: a
-// partial is the outcome of a chain of JC69 steps as long as the tree is deep, the states'
-// own steps are three.
-template <typename R, int MODE, typename P = R>
-__device__ R emit_column(const EmitCtx &c, const uint8_t *chars, int X, P (*in)[4], P (*out)[4],
+template <typename R, int MODE>
+__device__ R emit_column(const EmitCtx &c, const uint8_t *chars, int X, R (*in)[4], R (*out)[4],
                          R *eb) {
     const int lane = threadIdx.x & 31;
     const int4 *nd = c.nd;
-    auto leaf = [&](uint8_t ch, P *v) {
-        if constexpr (MODE == EM_REL) leaf_partial_x<P>(ch, X, v);
-        else leaf_partial<P>(ch, v);
+    auto leaf = [&](uint8_t ch, R *v) {
+        if constexpr (MODE == EM_REL) leaf_partial_x<R>(ch, X, v);
+        else leaf_partial<R>(ch, v);
     };
     constexpr bool F32 = std::is_same<R, float>::value;
-    constexpr bool PF32 = std::is_same<P, float>::value;
-    auto bm = [&](int j) -> P { if constexpr (PF32) return c.muts32[j]; else return (P)c.muts[j]; };
-    auto bn = [&](int j) -> P { if constexpr (PF32) return c.nomuts32[j]; else return (P)c.nomuts[j]; };
-    auto step = [&](const auto *x, auto m, auto nm, auto *y) {
-        using T = decltype(m);
+    auto bm = [&](int j) -> R { if constexpr (F32) return c.muts32[j]; else return (R)c.muts[j]; };
+    auto bn = [&](int j) -> R { if constexpr (F32) return c.nomuts32[j]; else return (R)c.nomuts[j]; };
+    auto step = [&](const R *x, R m, R nm, R *y) {
+        const double m64 = (double)m, nm64 = (double)nm;
         if constexpr (MODE == EM_REL) {
-            jc_apply_x<T>(x, m, nm, y);
+            jc_apply_x<R>(x, m, nm, y);
         } else if constexpr (MODE == EM_F64 || MODE == EM_SNP) {
-            const T sum = (x[0] + x[1]) + (x[2] + x[3]);
+            const R sum = (x[0] + x[1]) + (x[2] + x[3]);
 #pragma unroll
             for (int a = 0; a < 4; a++) y[a] = fma(nm - m, x[a], m * sum);
         } else {
-            jc_apply<false>((const double *)x, (double)m, (double)nm, (double *)y);
+            jc_apply<false>((const double *)x, m64, nm64, (double *)y);
         }
     };
-    auto mul = [&](const P *a, const P *b, P *z) {
-        z[0] = MODE == EM_REL ? cprod<P>(a[0], b[0]) : a[0] * b[0];
+    auto mul = [&](const R *a, const R *b, R *z) {
+        z[0] = MODE == EM_REL ? cprod<R>(a[0], b[0]) : a[0] * b[0];
 #pragma unroll
         for (int t = 1; t < 4; t++) z[t] = a[t] * b[t];
     };
@@ -1346,7 +1334,7 @@ __device__ R emit_column(const EmitCtx &c, const uint8_t *chars, int X, P (*in)[
         for (int x = c.inp[h] + lane; x < c.inp[h + 1]; x += 32) {
             const int j = c.inl[x];
             const int c1 = nd[j].y, c2 = nd[j].z;
-            P p1[4], p2[4];
+            R p1[4], p2[4];
             step(in[c1], bm(c1), bn(c1), p1);
             step(in[c2], bm(c2), bn(c2), p2);
             mul(p1, p2, in[j]);
@@ -1358,16 +1346,16 @@ __device__ R emit_column(const EmitCtx &c, const uint8_t *chars, int X, P (*in)[
         for (int x = c.outp[h] + lane; x < c.outp[h + 1]; x += 32) {
             const int j = c.outl[x];
             if (j == c.mainr) {
-                out[j][0] = MODE == EM_REL ? P(0) : P(1);
-                out[j][1] = out[j][2] = out[j][3] = P(1);
+                out[j][0] = MODE == EM_REL ? R(0) : R(1);
+                out[j][1] = out[j][2] = out[j][3] = R(1);
                 continue;
             }
             const int p = nd[j].x;
             const int sib = nd[p].y == j ? nd[p].z : nd[p].y;
-            P p1[4];
+            R p1[4];
             step(in[sib], bm(sib), bn(sib), p1);
             if (p != c.mainr) {
-                P p2[4];
+                R p2[4];
                 step(out[p], bm(p), bn(p), p2);
                 mul(p1, p2, out[j]);
             } else {
@@ -1380,18 +1368,16 @@ __device__ R emit_column(const EmitCtx &c, const uint8_t *chars, int X, P (*in)[
     // leaf partial of the threaded sequence (external) or the subtree root (internal)
     R in2[4];
     if (c.internal) {
-        for (int a = 0; a < 4; a++) in2[a] = to_r<R>(in[c.node1][a]);
+        for (int a = 0; a < 4; a++) in2[a] = in[c.node1][a];
     } else {
-        P lp[4];
-        leaf(chars[c.nleaves], lp);
-        for (int a = 0; a < 4; a++) in2[a] = to_r<R>(lp[a]);
+        leaf(chars[c.nleaves], in2);
     }
     R ref = MODE == EM_REL || MODE == EM_SNP ? R(4) : R(0);
     R vmax = R(0);  // SNP: the largest bracket among states in the plain form
     R wcol = R(1);  // SNP: the column's W, sum over the main root's inner partial
     if constexpr (MODE == EM_SNP) {
-        const P *im = in[c.mainr];
-        wcol = to_r<R>((im[0] + im[1]) + (im[2] + im[3]));
+        const R *im = in[c.mainr];
+        wcol = (im[0] + im[1]) + (im[2] + im[3]);
     }
     // SNP: the threaded base (external trees), 4 for a missing call
     const uint8_t chb = MODE == EM_SNP ? chars[c.nleaves] : 'N';
@@ -1408,15 +1394,10 @@ __device__ R emit_column(const EmitCtx &c, const uint8_t *chars, int X, P (*in)[
             for (int t = 0; t < 6; t++) q[t] = (R)c.pm[6 * k + t];
             q[6] = R(1) - R(4) * q[0];
         }
-        R p1[4], p2[4], p3[4], x2[4], x3[4];
-#pragma unroll
-        for (int a = 0; a < 4; a++) {
-            x2[a] = to_r<R>(in[node2][a]);
-            x3[a] = to_r<R>(out[node2][a]);
-        }
+        R p1[4], p2[4], p3[4];
         if constexpr (MODE != EM_SNP) step(in2, q[0], q[3], p1);
-        step(x2, q[1], q[4], p2);
-        if (node2 != c.mainr) step(x3, q[2], q[5], p3);
+        step(in[node2], q[1], q[4], p2);
+        if (node2 != c.mainr) step(out[node2], q[2], q[5], p3);
         else p3[0] = p3[1] = p3[2] = p3[3] = R(1);
         R v;  // calc_emit (emit.cpp:620-645)
         if constexpr (MODE == EM_SNP) {
@@ -1495,6 +1476,126 @@ __device__ R emit_column(const EmitCtx &c, const uint8_t *chars, int X, P (*in)[
     return ref;
 }
 
+// One variant column in double-float by one warp: the FP32 path's variant columns, the
+// partials and emissions of emit_column's F64 form (4 e_k into eb[S]; returns the largest)
+// with less work per step. A leaf with an observed base contributes its JC69 row's entries
+// (m, or nm for the base itself) instead of a step over its one-hot partial; each partial's
+// sum is kept beside it (isum, osum: n each) for the steps that read it; and with the
+// threaded base b observed, sum_a p1_a t_a = m1 sum_{a != b} t_a + nm1 t_b.
+__device__ df emit_column_df(const EmitCtx &c, const uint8_t *chars, df (*in)[4], df (*out)[4],
+                             df *isum, df *osum, df *eb) {
+    const int lane = threadIdx.x & 31;
+    const int4 *nd = c.nd;
+    auto base_of = [&](uint8_t ch) {
+        return ch == 'N' ? 4 : (ch == 'A' || ch == 'a') ? 0 : (ch == 'C' || ch == 'c') ? 1
+             : (ch == 'G' || ch == 'g') ? 2 : 3;
+    };
+    // the JC69 step of node j's partial x (sum xs) over a branch with m, nm
+    auto step = [&](int j, const df *x, df xs, df m, df nm, df *y) {
+        const int b = j >= 0 && j < c.nleaves ? base_of(chars[j]) : 4;
+        if (b < 4) {
+#pragma unroll
+            for (int a = 0; a < 4; a++) y[a] = a == b ? nm : m;
+        } else {
+            const df dd = nm - m, ms = m * xs;
+#pragma unroll
+            for (int a = 0; a < 4; a++) y[a] = dd * x[a] + ms;
+        }
+    };
+    auto sum4 = [](const df *v) { return (v[0] + v[1]) + (v[2] + v[3]); };
+    for (int x = lane; x < c.inp[1]; x += 32) {
+        const int j = c.inl[x];
+        leaf_partial<df>(chars[j], in[j]);
+        isum[j] = sum4(in[j]);
+    }
+    __syncwarp();
+    for (int h = 1; h < c.nlev_in; h++) {
+        for (int x = c.inp[h] + lane; x < c.inp[h + 1]; x += 32) {
+            const int j = c.inl[x];
+            const int c1 = nd[j].y, c2 = nd[j].z;
+            df p1[4], p2[4];
+            step(c1, in[c1], isum[c1], df(c.muts[c1]), df(c.nomuts[c1]), p1);
+            step(c2, in[c2], isum[c2], df(c.muts[c2]), df(c.nomuts[c2]), p2);
+#pragma unroll
+            for (int a = 0; a < 4; a++) in[j][a] = p1[a] * p2[a];
+            isum[j] = sum4(in[j]);
+        }
+        __syncwarp();
+    }
+    for (int h = 0; h < c.nlev_out; h++) {
+        for (int x = c.outp[h] + lane; x < c.outp[h + 1]; x += 32) {
+            const int j = c.outl[x];
+            if (j == c.mainr) {
+                out[j][0] = out[j][1] = out[j][2] = out[j][3] = df(1.0);
+                osum[j] = df(4.0);
+                continue;
+            }
+            const int p = nd[j].x;
+            const int sib = nd[p].y == j ? nd[p].z : nd[p].y;
+            df p1[4];
+            step(sib, in[sib], isum[sib], df(c.muts[sib]), df(c.nomuts[sib]), p1);
+            if (p != c.mainr) {
+                df p2[4];
+                step(-1, out[p], osum[p], df(c.muts[p]), df(c.nomuts[p]), p2);
+#pragma unroll
+                for (int a = 0; a < 4; a++) out[j][a] = p1[a] * p2[a];
+            } else {
+#pragma unroll
+                for (int a = 0; a < 4; a++) out[j][a] = p1[a];
+            }
+            osum[j] = sum4(out[j]);
+        }
+        __syncwarp();
+    }
+    // the threaded sequence's base (external), else the subtree root's partial (internal)
+    const int bnew = c.internal ? 4 : base_of(chars[c.nleaves]);
+    df in2[4], s2;
+    if (c.internal) {
+#pragma unroll
+        for (int a = 0; a < 4; a++) in2[a] = in[c.node1][a];
+        s2 = isum[c.node1];
+    } else {
+        leaf_partial<df>(chars[c.nleaves], in2);
+        s2 = sum4(in2);
+    }
+    df ref = df(0.0);
+    for (int k = lane; k < c.S; k += 32) {
+        const int node2 = c.snode[k];
+        const double *q = c.pm + 6 * (size_t)k;  // mut0..2, nomut0..2
+        df p2[4], t[4];
+        step(node2, in[node2], isum[node2], df(q[1]), df(q[4]), p2);
+        if (node2 != c.mainr) {
+            df p3[4];
+            step(-1, out[node2], osum[node2], df(q[2]), df(q[5]), p3);
+#pragma unroll
+            for (int a = 0; a < 4; a++) t[a] = p2[a] * p3[a];
+        } else {
+#pragma unroll
+            for (int a = 0; a < 4; a++) t[a] = p2[a];
+        }
+        df v;
+        if (bnew < 4) {
+            df rest = df(0.0);
+#pragma unroll
+            for (int a = 0; a < 4; a++)
+                if (a != bnew) rest += t[a];
+            v = df(q[0]) * rest + df(q[3]) * t[bnew];
+        } else {
+            df p1[4];
+            step(-1, in2, s2, df(q[0]), df(q[3]), p1);
+            v = df(0.0);
+#pragma unroll
+            for (int a = 0; a < 4; a++) v += p1[a] * t[a];
+        }
+        eb[k] = v;
+        ref = fmax(ref, v);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) ref = fmax(ref, __shfl_xor_sync(0xffffffffu, ref, o));
+    __syncwarp();
+    return ref;
+}
+
 // FP32 path: a tree's share of the log-likelihood's emission references, lneref per
 // invariant column and lnvref per variant column (the instance's column 0, the prior, has
 // none), summed by one warp in a fixed order.
@@ -1568,11 +1669,12 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
     float *muts32 = (float *)align16(sfloor + maxS);     // FP32 path copies
     float *nomuts32 = muts32 + n;
     float *pm32 = (float *)align16(nomuts32 + n);        // [maxS][8]
-    // per warp: inner[n][4], outer[n][4] partials, then the column's emissions (float-sized
-    // when lean)
+    // per warp: inner[n][4], outer[n][4] partials (and, not lean, the double-float form's
+    // partial sums [2][n]), then the column's emissions (float-sized when lean)
     const int esz = lean ? 4 : 8;
+    const int per_node = lean ? 8 : 10;
     double *scratch = (double *)align16(pm32 + (size_t)8 * maxS);
-    char *ebuf = (char *)scratch + (size_t)nwarps * n * 8 * esz;
+    char *ebuf = (char *)scratch + (size_t)nwarps * n * per_node * esz;
     __shared__ double times[MAXT];
     __shared__ int nlev_in, nlev_out;
     if (ebuf + (size_t)nwarps * maxS * esz - (char *)dyn > smem_bytes) {
@@ -1713,7 +1815,7 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
 
     const EmitCtx ctx{nd, muts, nomuts, pm, muts32, nomuts32, pm32, snode, inl, inp, outl, outp,
                       sfloor, nlev_in, nlev_out, mainr, node1, S, I.nseqs, I.nleaves, n, internal};
-    double *wscr = (double *)((char *)scratch + (size_t)warp * n * 8 * esz);
+    double *wscr = (double *)((char *)scratch + (size_t)warp * n * per_node * esz);
     double *eb = (double *)(ebuf + (size_t)warp * maxS * esz);  // read as float when lean
     const uint8_t *cls = d.colclass + I.col0 + B.start;
     const int ns = I.nseqs;
@@ -1806,26 +1908,26 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
                     near = !__any_sync(0xffffffffu, other);
                 }
                 float *row = d.var32 + B.var0 + (size_t)vrow * S;
-                if (near && d.vardf != 2) {
+                if (near && !d.vardf) {
                     float *fs = (float *)wscr, *fe = (float *)eb;
-                    const float dref =
-                        d.vardf == 1
-                            ? emit_column<float, EM_REL, df>(ctx, chars, X, (df (*)[4])wscr,
-                                                             (df (*)[4])wscr + n, fe)
-                            : emit_column<float, EM_REL>(ctx, chars, X, (float (*)[4])fs,
-                                                         (float (*)[4])fs + n, fe);
+                    const float dref = emit_column<float, EM_REL>(ctx, chars, X, (float (*)[4])fs,
+                                                                  (float (*)[4])fs + n, fe);
                     const float inv1 = 1.f / (1.f - dref);  // 1 / (4 e_ref)
                     for (int k = lane; k < S; k += 32) {
                         const float c = (fe[k] - dref) * inv1;  // 1 - e_k / e_ref
                         row[k] = c <= 0.5f ? c : -((1.f - fe[k]) * inv1);
                     }
                     if (lane == 0) d.lnvref[B.vrow0 + vrow] = log(.25) + log1p(-(double)dref);
-                } else if (d.vardf == 2) {
-                    // two or more observed bases: the emissions differ between states by
-                    // factors, and the forward posterior amplifies their relative error
-                    // about 200-fold, so they are formed in double-float and rounded once
+                } else if (d.vardf) {
+                    // the forward posterior amplifies an error of a variant column's
+                    // emissions thousands-fold where they differ little between states (the
+                    // columns that vary only through missing calls): the partials and every
+                    // state's split-branch steps are formed in double-float and each ratio
+                    // to the column's largest is rounded once
                     df *ed = (df *)eb;
-                    emit_column<df, EM_F64>(ctx, chars, 0, (df (*)[4])wscr, (df (*)[4])wscr + n, ed);
+                    df *dscr = (df *)wscr;
+                    emit_column_df(ctx, chars, (df (*)[4])dscr, (df (*)[4])dscr + n, dscr + 8 * n,
+                                   dscr + 9 * n, ed);
                     double eref = 0.0;
                     for (int k = lane; k < S; k += 32) eref = fmax(eref, (double)ed[k]);
 #pragma unroll
@@ -1839,12 +1941,8 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
                 } else if (!internal) {
                     // brackets against the column's largest: D form x / plain form y
                     float *fs = (float *)wscr, *fe = (float *)eb;
-                    const float ref =
-                        d.vardf == 1
-                            ? emit_column<float, EM_SNP, df>(ctx, chars, X, (df (*)[4])wscr,
-                                                             (df (*)[4])wscr + n, fe)
-                            : emit_column<float, EM_SNP>(ctx, chars, X, (float (*)[4])fs,
-                                                         (float (*)[4])fs + n, fe);
+                    const float ref = emit_column<float, EM_SNP>(ctx, chars, X, (float (*)[4])fs,
+                                                                 (float (*)[4])fs + n, fe);
                     const float bref = ref >= 0.f ? 1.f - ref : -ref;  // the largest bracket
                     const float inv1 = 1.f / bref;
                     for (int k = lane; k < S; k += 32) {
@@ -1859,14 +1957,8 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
                     }
                     if (lane == 0) {
                         // W: the tree's own likelihood, sum over the main root's inner partial
-                        double w;
-                        if (d.vardf == 1) {
-                            const df *im = (const df *)wscr + 4 * mainr;
-                            w = (double)((im[0] + im[1]) + (im[2] + im[3]));
-                        } else {
-                            const float *im = fs + 4 * mainr;
-                            w = (double)((im[0] + im[1]) + (im[2] + im[3]));
-                        }
+                        const float *im = fs + 4 * mainr;
+                        const double w = (double)((im[0] + im[1]) + (im[2] + im[3]));
                         d.lnvref[B.vrow0 + vrow] = log(.25 * w * (double)bref);
                     }
                 } else {
@@ -1967,7 +2059,7 @@ size_t varemit_need(int n, int maxS, bool lean, int w) {
     o += (size_t)maxS;                                                // sfloor
     o = a16(o) + 2 * (size_t)n * sizeof(float);                       // muts32, nomuts32
     o = a16(o) + 8 * (size_t)maxS * sizeof(float);                    // pm32
-    o = a16(o) + (size_t)w * n * 8 * esz;                             // scratch
+    o = a16(o) + (size_t)w * n * (lean ? 8 : 10) * esz;               // scratch
     o += (size_t)w * maxS * esz;                                      // ebuf
     return o + 16;
 }

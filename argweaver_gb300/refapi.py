@@ -422,6 +422,74 @@ def get_state_spaces(prob: Problem) -> list:
     return _with_trees(prob, run)
 
 
+def _i32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _f64c(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _take_matrix(lib, mat, nrows: int, ncols: int, free: str) -> np.ndarray:
+    if not mat:
+        raise ValueError(capi.last_error())
+    try:
+        if nrows == 0 or ncols == 0:
+            return np.zeros((nrows, ncols))
+        return np.ctypeslib.as_array(mat[0], shape=(nrows * ncols,)).reshape(nrows, ncols).copy()
+    finally:
+        getattr(lib, free)(mat, nrows)
+
+
+def new_transition_probs(ptree, ages, states, times, popsizes, rho: float) -> np.ndarray:
+    """The log transition matrix within one tree over `states` ((node, time) rows, any
+    order), as the reference's new_transition_probs (trans.cpp:1190-1208)."""
+    lib = capi.load()
+    pt, ag, st = _i32(ptree), _i32(ages), _i32(states).reshape(-1, 2)
+    tm, pops = _f64c(times), _f64c(popsizes)
+    S = st.shape[0]
+    mat = lib.new_transition_probs(len(pt), pt.ctypes.data_as(capi.c_int_p),
+                                   ag.ctypes.data_as(capi.c_int_p), 0.0,
+                                   st.ctypes.data_as(capi.c_int_p), S, len(tm),
+                                   tm.ctypes.data_as(capi.c_double_p), None, None, None, None,
+                                   pops.ctypes.data_as(capi.c_double_p), float(rho))
+    return _take_matrix(lib, mat, S, S, "delete_transition_probs")
+
+
+def new_transition_probs_switch(ptree, last_ptree, spr, ages, last_ages, states1, states2,
+                                times, popsizes, rho: float) -> np.ndarray:
+    """The log switch matrix from last_ptree's states1 to ptree's states2 across `spr`
+    (recomb_node, recomb_time, coal_node, coal_time), as the reference's
+    new_transition_probs_switch (trans.cpp:1212-1245)."""
+    lib = capi.load()
+    pt, lpt, ag, lag = _i32(ptree), _i32(last_ptree), _i32(ages), _i32(last_ages)
+    s1, s2 = _i32(states1).reshape(-1, 2), _i32(states2).reshape(-1, 2)
+    tm, pops = _f64c(times), _f64c(popsizes)
+    r = [int(x) for x in spr]
+    mat = lib.new_transition_probs_switch(
+        pt.ctypes.data_as(capi.c_int_p), lpt.ctypes.data_as(capi.c_int_p), len(pt), r[0], r[1],
+        r[2], r[3], ag.ctypes.data_as(capi.c_int_p), lag.ctypes.data_as(capi.c_int_p), 0.0, 0.0,
+        s1.ctypes.data_as(capi.c_int_p), s1.shape[0], s2.ctypes.data_as(capi.c_int_p),
+        s2.shape[0], len(tm), tm.ctypes.data_as(capi.c_double_p), None, None, None, None,
+        pops.ctypes.data_as(capi.c_double_p), float(rho))
+    return _take_matrix(lib, mat, s1.shape[0], s2.shape[0], "delete_transition_probs")
+
+
+def new_emissions(states, ptree, ages, seqs: np.ndarray, times, mu: float) -> np.ndarray:
+    """Emissions P(column | state) of the threaded sequence (the last row of seqs) on one
+    tree, [columns][states], as the reference's new_emissions (emit.cpp:1288-1301)."""
+    lib = capi.load()
+    pt, ag, st = _i32(ptree), _i32(ages), _i32(states).reshape(-1, 2)
+    tm = _f64c(times)
+    sq, _keep = _char_pp(seqs)
+    nseqs, seqlen = np.asarray(seqs).shape
+    mat = lib.new_emissions(st.ctypes.data_as(capi.c_int_p), st.shape[0],
+                            pt.ctypes.data_as(capi.c_int_p), len(pt),
+                            ag.ctypes.data_as(capi.c_int_p), sq, nseqs, seqlen,
+                            tm.ctypes.data_as(capi.c_double_p), len(tm), float(mu))
+    return _take_matrix(lib, mat, seqlen, st.shape[0], "delete_emissions")
+
+
 def sample_arg_removal_path(prob: Problem, node: int, pos: int | None = None,
                             leaf: bool = False) -> np.ndarray:
     """A removal path (one node per tree) from `node` of the first tree forward

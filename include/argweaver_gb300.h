@@ -228,6 +228,39 @@ void delete_path(int *path);
 void delete_double_matrix(double **mat, int nrows);
 void delete_forward_matrix(double **mat, int nrows);
 
+/* The reference's dense helper matrices (its ctypes layer's aids for tests and plots),
+ * formed by the table kernel (and, for emissions, the emission kernel) on the GPU in FP64
+ * and gathered into the caller's state order. istates are (node, time) pairs of the tree's
+ * coalescence states in any order (a pair that is no state of the tree is an error: NULL,
+ * awg_last_error). treelen, time_steps and the lineage counts are accepted and not read:
+ * the kernels derive them from the tree, as the reference recomputes them.
+ *
+ * new_transition_probs (trans.cpp:1190-1208): [nstates][nstates], log P(i -> j) within
+ * the tree (TransMatrix::get_log, trans.h:64-83, 130-133). Free with
+ * delete_transition_probs (trans.cpp:1248-1251). */
+double **new_transition_probs(int nnodes, int *ptree, int *ages, double treelen,
+                              awg_intstate *istates, int nstates, int ntimes, double *times,
+                              double *time_steps, int *nbranches, int *nrecombs, int *ncoals,
+                              double *popsizes, double rho);
+/* new_transition_probs_switch (trans.cpp:1212-1245): [nstates1][nstates2], log P(i -> j)
+ * from last_ptree's states to ptree's across the SPR (TransMatrixSwitch::get_log,
+ * trans.h:200-219), the node mapping make_node_mapping's (local_tree.h:767-778). */
+double **new_transition_probs_switch(int *ptree, int *last_ptree, int nnodes, int recomb_node,
+                                     int recomb_time, int coal_node, int coal_time,
+                                     int *ages_index, int *last_ages_index, double treelen,
+                                     double last_treelen, awg_intstate *istates1, int nstates1,
+                                     awg_intstate *istates2, int nstates2, int ntimes,
+                                     double *times, double *time_steps, int *nbranches,
+                                     int *nrecombs, int *ncoals, double *popsizes, double rho);
+void delete_transition_probs(double **transmat, int nstates);
+/* new_emissions (emit.cpp:1288-1301): [seqlen][nstates], P(column i | state j) of the
+ * threaded sequence seqs[nseqs - 1] on the tree (calc_emissions_external, emit.cpp:
+ * 650-845; not in log). Free with delete_emissions (emit.cpp:1304-1307). */
+double **new_emissions(awg_intstate *istates, int nstates, int *ptree, int nnodes,
+                       int *ages_index, char **seqs, int nseqs, int seqlen, double *times,
+                       int ntimes, double mu);
+void delete_emissions(double **emit, int seqlen);
+
 /* Probabilities of a whole ARG (total_prob.cpp:315-382; bound by
  * argweaver/argweaverc.py:219-245), computed on the device. arghmm_likelihood: log P(seqs |
  * ARG), sequences one per leaf (leaf i = seqs[i]) covering start_coord .. end of the trees;

@@ -1693,6 +1693,29 @@ int oracle_debug_tables(const oracle_problem *p, double *tm_out, double *gts_out
     return 0;
 }
 
+// Dense log matrices of tree b: trans [S][S] = log TransMatrix::get (get_transition_probs,
+// trans.cpp:119-130) and, for b > 0 with sw non-NULL, sw [S1][S2] = log
+// TransMatrixSwitch::get from tree b - 1 (get_transition_probs_switch, trans.cpp:756-764);
+// states in coal_states order.
+int oracle_dense_matrices(const oracle_problem *p, int b, double *trans, double *sw) {
+    Hmm h;
+    if (!setup(p, h)) return -1;
+    if (b < 0 || b >= (int)h.arg.trees.size() || (sw && b == 0)) return -1;
+    Block blk;
+    if (!make_block(h, b, blk, sw != nullptr)) return -2;
+    const Tree &t = h.arg.trees[b];
+    const int S = blk.states.size();
+    if (trans)
+        for (int i = 0; i < S; i++)
+            for (int j = 0; j < S; j++)
+                trans[(size_t)i * S + j] = log(blk.tm.get(t, blk.states, i, j));
+    if (sw)
+        for (int i = 0; i < blk.sw.nstates1; i++)
+            for (int j = 0; j < blk.sw.nstates2; j++)
+                sw[(size_t)i * blk.sw.nstates2 + j] = log(blk.sw.get(i, j));
+    return 0;
+}
+
 int oracle_emissions(const oracle_problem *p, double *emit_out) {
     Hmm h;
     if (!setup(p, h)) return -1;

@@ -65,6 +65,9 @@ int oracle_block_terms(const oracle_problem *p, double *out_terms, int *out_mina
 
 /* Emissions of every column, packed like the forward table. */
 int oracle_emissions(const oracle_problem *p, double *emit);
+// Dense log matrices of tree b: trans [S][S] within it and (b > 0, sw non-NULL) the switch
+// [S1][S2] from tree b - 1; NULL skips one.
+int oracle_dense_matrices(const oracle_problem *p, int b, double *trans, double *sw);
 
 /* The tables of the GPU table kernel, same layouts (for kernel-level checks): tmatrix
  * [ntrees][T-1][T-1]; same-branch entries get_time(a_y, b_x, c, minage, true) of each node

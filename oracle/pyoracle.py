@@ -54,6 +54,7 @@ def load():
                            ("oracle_posterior", [P, C.c_void_p, C.c_void_p, C.c_void_p]),
                            ("oracle_block_terms", [P, C.c_void_p, C.c_void_p]),
                            ("oracle_emissions", [P, C.c_void_p]),
+                           ("oracle_dense_matrices", [P, C.c_int, C.c_void_p, C.c_void_p]),
                            ("oracle_debug_tables", [P, C.c_void_p, C.c_void_p, C.c_void_p,
                                                     C.c_void_p]),
                            ("oracle_dense_forward", [C.c_int, C.c_int] + [C.c_void_p] * 3),
@@ -188,6 +189,19 @@ def block_terms(prob):
     minage = np.zeros(prob.ntrees, dtype=np.int32)
     _check(load().oracle_block_terms(b.ref, out.ctypes.data, minage.ctypes.data), "terms")
     return out, minage
+
+
+def dense_matrices(prob, b: int, switch: bool = False):
+    """Tree b's log transition matrix [S][S] and, with switch (b > 0), the log switch
+    matrix [S1][S2] from tree b - 1, states in the reference's get_coal_states order."""
+    bd = Bound(prob)
+    ns = prob.nstates_per_tree()
+    S = int(ns[b])
+    trans = np.zeros((S, S))
+    sw = np.zeros((int(ns[b - 1]), S)) if switch else None
+    _check(load().oracle_dense_matrices(bd.ref, b, trans.ctypes.data,
+                                        sw.ctypes.data if switch else None), "dense matrices")
+    return (trans, sw) if switch else trans
 
 
 def emissions(prob) -> np.ndarray:

@@ -111,6 +111,17 @@ double arghmm_tree_prior_prob(LocalTrees *trees, double *times, int ntimes,
 double arghmm_joint_prob(LocalTrees *trees, double *times, int ntimes, double *popsizes,
                          double mu, double rho, char **seqs, int nseqs,
                          int seqlen);                                  // total_prob.cpp:369
+double **new_transition_probs(int nnodes, int *ptree, int *ages, double treelen,
+                              intstate *istates, int nstates, int ntimes, double *times,
+                              double *time_steps, int *nbranches, int *nrecombs, int *ncoals,
+                              double *popsizes, double rho);           // trans.cpp:1190
+double **new_transition_probs_switch(
+    int *ptree, int *last_ptree, int nnodes, int recomb_node, int recomb_time, int coal_node,
+    int coal_time, int *ages_index, int *last_ages_index, double treelen, double last_treelen,
+    intstate *istates1, int nstates1, intstate *istates2, int nstates2, int ntimes,
+    double *times, double *time_steps, int *nbranches, int *nrecombs, int *ncoals,
+    double *popsizes, double rho);                                     // trans.cpp:1212
+void delete_transition_probs(double **transmat, int nstates);         // trans.cpp:1248
 }
 }
 
@@ -396,6 +407,68 @@ static int cmd_dense(const char *in, const char *out, int seed) {
     delete_matrix(trans, S); delete_matrix(emit, p.seqlen); delete_matrix(bw, p.seqlen);
     delete_matrix(fw, p.seqlen);
     delete trees;
+    return 0;
+}
+
+// The reference's dense helper exports on a problem's trees, states in get_coal_states
+// order: new_transition_probs of tree 0, new_emissions of tree 0's columns, and
+// new_transition_probs_switch into trees 1..maxb. Output "AWGHLP01", i32 {S0, L0, nsw},
+// f64 trans[S0][S0], f64 emit[L0][S0], then per switch i32 {S1, S2}, f64 [S1][S2].
+static int cmd_helpers(const char *in, const char *out, int maxb) {
+    Problem p = read_problem(in);
+    const int n = p.nnodes;
+    if (p.internal) die("helpers: external trees only");
+    // new_transition_probs_switch maps nodes by make_node_mapping (local_tree.h:767)
+    for (int b = 1; b < p.ntrees && !p.mapping.empty(); b++)
+        for (int j = 0; j < n; j++) {
+            const int broken = p.ptrees[(size_t)(b - 1) * n + p.sprs[(size_t)b * 4]];
+            if (p.mapping[(size_t)b * n + j] != (j == broken ? -1 : j))
+                die("helpers: node mappings other than make_node_mapping's");
+        }
+    auto states_of = [&](int b) {
+        LocalTree tree(&p.ptrees[(size_t)b * n], n, &p.ages[(size_t)b * n]);
+        States st;
+        get_coal_states(&tree, p.ntimes, st, false);
+        vector<int> flat(2 * st.size());
+        for (size_t i = 0; i < st.size(); i++) {
+            flat[2 * i] = st[i].node;
+            flat[2 * i + 1] = st[i].time;
+        }
+        return flat;
+    };
+    FILE *f = fopen(out, "wb");
+    if (!f) die("cannot write output");
+    wr(f, "AWGHLP01", 8);
+    vector<int> s0 = states_of(0);
+    const int S0 = (int)s0.size() / 2, L0 = p.blocklens[0];
+    const int nsw = std::min(maxb, p.ntrees - 1);
+    int hdr[3] = {S0, L0, nsw};
+    wr(f, hdr, 3);
+    double **tr = new_transition_probs(n, &p.ptrees[0], &p.ages[0], 0.0, (intstate *)s0.data(),
+                                       S0, p.ntimes, p.times.data(), NULL, NULL, NULL, NULL,
+                                       p.popsizes.data(), p.rho);
+    for (int i = 0; i < S0; i++) wr(f, tr[i], S0);
+    delete_transition_probs(tr, S0);
+    vector<char *> sp = seq_ptrs(p);  // tree 0's columns are the first L0
+    double **em = new_emissions((intstate *)s0.data(), S0, &p.ptrees[0], n, &p.ages[0],
+                                sp.data(), p.nseqs, L0, p.times.data(), p.ntimes, p.mu);
+    for (int i = 0; i < L0; i++) wr(f, em[i], S0);
+    delete_emissions(em, L0);
+    for (int b = 1; b <= nsw; b++) {
+        vector<int> s1 = states_of(b - 1), s2 = states_of(b);
+        const int S1 = (int)s1.size() / 2, S2 = (int)s2.size() / 2;
+        const int *spr = &p.sprs[(size_t)b * 4];
+        double **sw = new_transition_probs_switch(
+            &p.ptrees[(size_t)b * n], &p.ptrees[(size_t)(b - 1) * n], n, spr[0], spr[1], spr[2],
+            spr[3], &p.ages[(size_t)b * n], &p.ages[(size_t)(b - 1) * n], 0.0, 0.0,
+            (intstate *)s1.data(), S1, (intstate *)s2.data(), S2, p.ntimes, p.times.data(), NULL,
+            NULL, NULL, NULL, p.popsizes.data(), p.rho);
+        int sz[2] = {S1, S2};
+        wr(f, sz, 2);
+        for (int i = 0; i < S1; i++) wr(f, sw[i], S2);
+        delete_transition_probs(sw, S1);
+    }
+    fclose(f);
     return 0;
 }
 
@@ -835,6 +908,7 @@ int main(int argc, char **argv) {
     if (cmd == "densernd" && argc == 6)
         return cmd_densernd(atoi(argv[2]), atoi(argv[3]), atoi(argv[4]), argv[5]);
     if (cmd == "argprob" && argc == 4) return cmd_argprob(argv[2], argv[3]);
+    if (cmd == "helpers" && argc == 5) return cmd_helpers(argv[2], argv[3], atoi(argv[4]));
     if (cmd == "samplethread" && argc == 5)
         return cmd_samplethread(argv[2], atoi(argv[3]), argv[4]);
     if (cmd == "removethread" && argc >= 5)

@@ -5,6 +5,7 @@ Run where the reference checkout exists (default /root/reference, or $AWG_REFERE
     python tests/golden/make_golden.py            # all fixtures
     python tests/golden/make_golden.py infsites   # only the infinite-sites ones
     python tests/golden/make_golden.py dense      # only the dense-HMM ones
+    python tests/golden/make_golden.py helpers    # the dense transition / emission helpers
     python tests/golden/make_golden.py argprob    # only the ARG-probability ones
     python tests/golden/make_golden.py formats    # only the sites / SMC ones
     python tests/golden/make_golden.py recomb     # only the recombination-sampling ones
@@ -163,6 +164,40 @@ def dense(tmp):
         prob = first_tree(simulate(6, 400, seed))
         p = os.path.join(tmp, "p.prob"); prob.save(p)
         make(f"single_k7_s{seed}", p, seed, tmp, dense=True)
+
+
+def helpers(tmp):
+    """The reference's dense helper exports (new_transition_probs, new_emissions,
+    new_transition_probs_switch) on simulated external ARGs with default node mappings:
+    tree 0's log transition matrix and emissions, and the log switch matrices into the next
+    trees, states in get_coal_states order."""
+    out_dir = os.path.join(HERE, "helpers")
+    os.makedirs(out_dir, exist_ok=True)
+    cases = [("k8_s11", simulate(7, 1500, 11), 12),
+             ("k10_T32", simulate(9, 1500, 31, ntimes=32), 8),
+             ("k17_missing", simulate(16, 1000, 21, missing=0.02), 8)]
+    for name, prob, maxb in cases:
+        pp = os.path.join(tmp, "h.prob")
+        prob.save(pp)
+        ob = os.path.join(tmp, "h.bin")
+        run("helpers", pp, ob, maxb)
+        d = open(ob, "rb").read()
+        assert d[:8] == b"AWGHLP01"
+        S0, L0, nsw = np.frombuffer(d, np.int32, 3, 8)
+        o = 20
+        trans = np.frombuffer(d, np.float64, S0 * S0, o).reshape(S0, S0); o += 8 * S0 * S0
+        emit = np.frombuffer(d, np.float64, L0 * S0, o).reshape(L0, S0); o += 8 * L0 * S0
+        sizes, mats = [], []
+        for _ in range(nsw):
+            S1, S2 = np.frombuffer(d, np.int32, 2, o); o += 8
+            mats.append(np.frombuffer(d, np.float64, S1 * S2, o)); o += 8 * S1 * S2
+            sizes.append((S1, S2))
+        assert o == len(d)
+        prob.save(os.path.join(out_dir, name + ".prob"))
+        np.savez_compressed(os.path.join(out_dir, name + ".npz"), trans=trans, emit=emit,
+                            switch_sizes=np.array(sizes, np.int32).reshape(-1, 2),
+                            switch=np.concatenate(mats) if mats else np.zeros(0))
+        print(name, S0, L0, sizes)
 
 
 def densernd(tmp):
@@ -576,6 +611,10 @@ def main():
         with tempfile.TemporaryDirectory() as tmp:
             argprob(tmp)
         return
+    if sys.argv[1:] == ["helpers"]:
+        with tempfile.TemporaryDirectory() as tmp:
+            helpers(tmp)
+        return
     if sys.argv[1:] == ["dense"]:
         with tempfile.TemporaryDirectory() as tmp:
             dense(tmp)
@@ -618,6 +657,7 @@ def main():
         dense(tmp)
         densernd(tmp)
         argprob(tmp)
+        helpers(tmp)
         formats(tmp)
         recomb(tmp)
         addthread(tmp)

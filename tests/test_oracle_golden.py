@@ -158,3 +158,35 @@ def test_arg_probabilities_match_reference(name):
     np.testing.assert_allclose(tprior, gold["tree_prior"], rtol=1e-13)
     np.testing.assert_allclose(lik + prior, gold["joint"], rtol=1e-13)
 
+
+
+HELPERS = ["k8_s11", "k10_T32", "k17_missing"]
+
+
+def load_helpers(name):
+    d = os.path.join(GOLDEN, "helpers")
+    return Problem.load(os.path.join(d, name + ".prob")), np.load(os.path.join(d, name + ".npz"))
+
+
+def switch_matrices(gold):
+    out, o = [], 0
+    for S1, S2 in gold["switch_sizes"]:
+        out.append(gold["switch"][o:o + S1 * S2].reshape(S1, S2))
+        o += S1 * S2
+    return out
+
+
+@pytest.mark.parametrize("name", HELPERS)
+def test_dense_helpers_match_reference(name):
+    """The oracle's dense log transition and switch matrices (TransMatrix::get,
+    TransMatrixSwitch::get) and its emissions against the reference's new_transition_probs,
+    new_transition_probs_switch and new_emissions on the same trees: identical, zero
+    probabilities (-inf) in the same places."""
+    prob, gold = load_helpers(name)
+    np.testing.assert_array_equal(pyoracle.dense_matrices(prob, 0), gold["trans"])
+    for b, ref in enumerate(switch_matrices(gold), start=1):
+        _, sw = pyoracle.dense_matrices(prob, b, switch=True)
+        np.testing.assert_array_equal(sw, ref)
+    S0, L0 = gold["trans"].shape[0], gold["emit"].shape[0]
+    em = pyoracle.emissions(prob)[:L0 * S0].reshape(L0, S0)
+    np.testing.assert_array_equal(em, gold["emit"])

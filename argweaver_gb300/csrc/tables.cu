@@ -1479,46 +1479,40 @@ __device__ R emit_column(const EmitCtx &c, const uint8_t *chars, int X, R (*in)[
 // One variant column in double-float by one warp: the FP32 path's variant columns, the
 // partials and emissions of emit_column's F64 form (4 e_k into eb[S]; returns the largest)
 // with less work per step. A leaf with an observed base contributes its JC69 row's entries
-// (m, or nm for the base itself) instead of a step over its one-hot partial; each partial's
-// sum is kept beside it (isum, osum: n each) for the steps that read it; and with the
+// (m, or nm for the base itself) instead of a step over its one-hot partial, and with the
 // threaded base b observed, sum_a p1_a t_a = m1 sum_{a != b} t_a + nm1 t_b.
 __device__ df emit_column_df(const EmitCtx &c, const uint8_t *chars, df (*in)[4], df (*out)[4],
-                             df *isum, df *osum, df *eb) {
+                             df *eb) {
     const int lane = threadIdx.x & 31;
     const int4 *nd = c.nd;
     auto base_of = [&](uint8_t ch) {
         return ch == 'N' ? 4 : (ch == 'A' || ch == 'a') ? 0 : (ch == 'C' || ch == 'c') ? 1
              : (ch == 'G' || ch == 'g') ? 2 : 3;
     };
-    // the JC69 step of node j's partial x (sum xs) over a branch with m, nm
-    auto step = [&](int j, const df *x, df xs, df m, df nm, df *y) {
+    auto sum4 = [](const df *v) { return (v[0] + v[1]) + (v[2] + v[3]); };
+    // the JC69 step of node j's partial x over a branch with m, nm (j < 0: not a leaf)
+    auto step = [&](int j, const df *x, df m, df nm, df *y) {
         const int b = j >= 0 && j < c.nleaves ? base_of(chars[j]) : 4;
         if (b < 4) {
 #pragma unroll
             for (int a = 0; a < 4; a++) y[a] = a == b ? nm : m;
         } else {
-            const df dd = nm - m, ms = m * xs;
+            const df dd = nm - m, ms = m * sum4(x);
 #pragma unroll
             for (int a = 0; a < 4; a++) y[a] = dd * x[a] + ms;
         }
     };
-    auto sum4 = [](const df *v) { return (v[0] + v[1]) + (v[2] + v[3]); };
-    for (int x = lane; x < c.inp[1]; x += 32) {
-        const int j = c.inl[x];
-        leaf_partial<df>(chars[j], in[j]);
-        isum[j] = sum4(in[j]);
-    }
+    for (int x = lane; x < c.inp[1]; x += 32) leaf_partial<df>(chars[c.inl[x]], in[c.inl[x]]);
     __syncwarp();
     for (int h = 1; h < c.nlev_in; h++) {
         for (int x = c.inp[h] + lane; x < c.inp[h + 1]; x += 32) {
             const int j = c.inl[x];
             const int c1 = nd[j].y, c2 = nd[j].z;
             df p1[4], p2[4];
-            step(c1, in[c1], isum[c1], df(c.muts[c1]), df(c.nomuts[c1]), p1);
-            step(c2, in[c2], isum[c2], df(c.muts[c2]), df(c.nomuts[c2]), p2);
+            step(c1, in[c1], df(c.muts[c1]), df(c.nomuts[c1]), p1);
+            step(c2, in[c2], df(c.muts[c2]), df(c.nomuts[c2]), p2);
 #pragma unroll
             for (int a = 0; a < 4; a++) in[j][a] = p1[a] * p2[a];
-            isum[j] = sum4(in[j]);
         }
         __syncwarp();
     }
@@ -1527,46 +1521,41 @@ __device__ df emit_column_df(const EmitCtx &c, const uint8_t *chars, df (*in)[4]
             const int j = c.outl[x];
             if (j == c.mainr) {
                 out[j][0] = out[j][1] = out[j][2] = out[j][3] = df(1.0);
-                osum[j] = df(4.0);
                 continue;
             }
             const int p = nd[j].x;
             const int sib = nd[p].y == j ? nd[p].z : nd[p].y;
             df p1[4];
-            step(sib, in[sib], isum[sib], df(c.muts[sib]), df(c.nomuts[sib]), p1);
+            step(sib, in[sib], df(c.muts[sib]), df(c.nomuts[sib]), p1);
             if (p != c.mainr) {
                 df p2[4];
-                step(-1, out[p], osum[p], df(c.muts[p]), df(c.nomuts[p]), p2);
+                step(-1, out[p], df(c.muts[p]), df(c.nomuts[p]), p2);
 #pragma unroll
                 for (int a = 0; a < 4; a++) out[j][a] = p1[a] * p2[a];
             } else {
 #pragma unroll
                 for (int a = 0; a < 4; a++) out[j][a] = p1[a];
             }
-            osum[j] = sum4(out[j]);
         }
         __syncwarp();
     }
     // the threaded sequence's base (external), else the subtree root's partial (internal)
     const int bnew = c.internal ? 4 : base_of(chars[c.nleaves]);
-    df in2[4], s2;
+    df in2[4];
     if (c.internal) {
 #pragma unroll
         for (int a = 0; a < 4; a++) in2[a] = in[c.node1][a];
-        s2 = isum[c.node1];
     } else {
         leaf_partial<df>(chars[c.nleaves], in2);
-        s2 = sum4(in2);
     }
-    df ref = df(0.0);
-    for (int k = lane; k < c.S; k += 32) {
+    auto state_v = [&](int k) -> df {
         const int node2 = c.snode[k];
         const double *q = c.pm + 6 * (size_t)k;  // mut0..2, nomut0..2
         df p2[4], t[4];
-        step(node2, in[node2], isum[node2], df(q[1]), df(q[4]), p2);
+        step(node2, in[node2], df(q[1]), df(q[4]), p2);
         if (node2 != c.mainr) {
             df p3[4];
-            step(-1, out[node2], osum[node2], df(q[2]), df(q[5]), p3);
+            step(-1, out[node2], df(q[2]), df(q[5]), p3);
 #pragma unroll
             for (int a = 0; a < 4; a++) t[a] = p2[a] * p3[a];
         } else {
@@ -1582,13 +1571,22 @@ __device__ df emit_column_df(const EmitCtx &c, const uint8_t *chars, df (*in)[4]
             v = df(q[0]) * rest + df(q[3]) * t[bnew];
         } else {
             df p1[4];
-            step(-1, in2, s2, df(q[0]), df(q[3]), p1);
+            step(-1, in2, df(q[0]), df(q[3]), p1);
             v = df(0.0);
 #pragma unroll
             for (int a = 0; a < 4; a++) v += p1[a] * t[a];
         }
-        eb[k] = v;
-        ref = fmax(ref, v);
+        return v;
+    };
+    // two states per lane at a time: independent chains the scheduler can interleave (the
+    // second one repeats the last state where it would run past S)
+    df ref = df(0.0);
+    for (int k0 = lane; k0 < c.S; k0 += 64) {
+        const int k1 = k0 + 32 < c.S ? k0 + 32 : k0;
+        const df v0 = state_v(k0), v1 = state_v(k1);
+        eb[k0] = v0;
+        eb[k1] = v1;
+        ref = fmax(ref, fmax(v0, v1));
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) ref = fmax(ref, __shfl_xor_sync(0xffffffffu, ref, o));
@@ -1669,12 +1667,11 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
     float *muts32 = (float *)align16(sfloor + maxS);     // FP32 path copies
     float *nomuts32 = muts32 + n;
     float *pm32 = (float *)align16(nomuts32 + n);        // [maxS][8]
-    // per warp: inner[n][4], outer[n][4] partials (and, not lean, the double-float form's
-    // partial sums [2][n]), then the column's emissions (float-sized when lean)
+    // per warp: inner[n][4], outer[n][4] partials, then the column's emissions (float-sized
+    // when lean)
     const int esz = lean ? 4 : 8;
-    const int per_node = lean ? 8 : 10;
     double *scratch = (double *)align16(pm32 + (size_t)8 * maxS);
-    char *ebuf = (char *)scratch + (size_t)nwarps * n * per_node * esz;
+    char *ebuf = (char *)scratch + (size_t)nwarps * n * 8 * esz;
     __shared__ double times[MAXT];
     __shared__ int nlev_in, nlev_out;
     if (ebuf + (size_t)nwarps * maxS * esz - (char *)dyn > smem_bytes) {
@@ -1815,7 +1812,7 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
 
     const EmitCtx ctx{nd, muts, nomuts, pm, muts32, nomuts32, pm32, snode, inl, inp, outl, outp,
                       sfloor, nlev_in, nlev_out, mainr, node1, S, I.nseqs, I.nleaves, n, internal};
-    double *wscr = (double *)((char *)scratch + (size_t)warp * n * per_node * esz);
+    double *wscr = (double *)((char *)scratch + (size_t)warp * n * 8 * esz);
     double *eb = (double *)(ebuf + (size_t)warp * maxS * esz);  // read as float when lean
     const uint8_t *cls = d.colclass + I.col0 + B.start;
     const int ns = I.nseqs;
@@ -1925,9 +1922,7 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
                     // state's split-branch steps are formed in double-float and each ratio
                     // to the column's largest is rounded once
                     df *ed = (df *)eb;
-                    df *dscr = (df *)wscr;
-                    emit_column_df(ctx, chars, (df (*)[4])dscr, (df (*)[4])dscr + n, dscr + 8 * n,
-                                   dscr + 9 * n, ed);
+                    emit_column_df(ctx, chars, (df (*)[4])wscr, (df (*)[4])wscr + n, ed);
                     double eref = 0.0;
                     for (int k = lane; k < S; k += 32) eref = fmax(eref, (double)ed[k]);
 #pragma unroll
@@ -2059,7 +2054,7 @@ size_t varemit_need(int n, int maxS, bool lean, int w) {
     o += (size_t)maxS;                                                // sfloor
     o = a16(o) + 2 * (size_t)n * sizeof(float);                       // muts32, nomuts32
     o = a16(o) + 8 * (size_t)maxS * sizeof(float);                    // pm32
-    o = a16(o) + (size_t)w * n * (lean ? 8 : 10) * esz;               // scratch
+    o = a16(o) + (size_t)w * n * 8 * esz;                             // scratch
     o += (size_t)w * maxS * esz;                                      // ebuf
     return o + 16;
 }

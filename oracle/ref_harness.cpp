@@ -122,6 +122,14 @@ double **new_transition_probs_switch(
     double *times, double *time_steps, int *nbranches, int *nrecombs, int *ncoals,
     double *popsizes, double rho);                                     // trans.cpp:1212
 void delete_transition_probs(double **transmat, int nstates);         // trans.cpp:1248
+bool arghmm_assert_transmat(int nnodes, int *ptree, int *ages, int ntimes, double *times,
+                            double *popsizes, double rho);             // trans.cpp:1254
+bool arghmm_assert_transmat_switch(int nnodes, int *ptree, int *ages, int recomb_node,
+                                   int recomb_time, int coal_node, int coal_time, int ntimes,
+                                   double *times, double *popsizes,
+                                   double rho);                        // trans.cpp:1275
+bool arghmm_assert_emit(LocalTrees *trees, int ntimes, double *times, double mu, char **seqs,
+                        int nseqs, int seqlen);                        // emit.cpp:1312
 }
 }
 
@@ -412,8 +420,11 @@ static int cmd_dense(const char *in, const char *out, int seed) {
 
 // The reference's dense helper exports on a problem's trees, states in get_coal_states
 // order: new_transition_probs of tree 0, new_emissions of tree 0's columns, and
-// new_transition_probs_switch into trees 1..maxb. Output "AWGHLP01", i32 {S0, L0, nsw},
-// f64 trans[S0][S0], f64 emit[L0][S0], then per switch i32 {S1, S2}, f64 [S1][S2].
+// new_transition_probs_switch into trees 1..maxb; then the reference's own brute-force
+// self-checks on the same trees (arghmm_assert_transmat on tree 0, arghmm_assert_transmat_
+// switch on each boundary, arghmm_assert_emit over every tree). Output "AWGHLP01",
+// i32 {S0, L0, nsw}, f64 trans[S0][S0], f64 emit[L0][S0], per switch i32 {S1, S2} and
+// f64 [S1][S2], then i32 checks[nsw + 2] (1: passed).
 static int cmd_helpers(const char *in, const char *out, int maxb) {
     Problem p = read_problem(in);
     const int n = p.nnodes;
@@ -468,6 +479,20 @@ static int cmd_helpers(const char *in, const char *out, int maxb) {
         for (int i = 0; i < S1; i++) wr(f, sw[i], S2);
         delete_transition_probs(sw, S1);
     }
+    vector<int> checks;
+    checks.push_back(arghmm_assert_transmat(n, &p.ptrees[0], &p.ages[0], p.ntimes,
+                                            p.times.data(), p.popsizes.data(), p.rho));
+    for (int b = 1; b <= nsw; b++) {
+        const int *spr = &p.sprs[(size_t)b * 4];
+        checks.push_back(arghmm_assert_transmat_switch(
+            n, &p.ptrees[(size_t)(b - 1) * n], &p.ages[(size_t)(b - 1) * n], spr[0], spr[1],
+            spr[2], spr[3], p.ntimes, p.times.data(), p.popsizes.data(), p.rho));
+    }
+    LocalTrees *trees = make_trees(p);
+    checks.push_back(arghmm_assert_emit(trees, p.ntimes, p.times.data(), p.mu, sp.data(),
+                                        p.nseqs, p.seqlen));
+    delete trees;
+    wr(f, checks.data(), checks.size());
     fclose(f);
     return 0;
 }

@@ -170,7 +170,9 @@ def helpers(tmp):
     """The reference's dense helper exports (new_transition_probs, new_emissions,
     new_transition_probs_switch) on simulated external ARGs with default node mappings:
     tree 0's log transition matrix and emissions, and the log switch matrices into the next
-    trees, states in get_coal_states order."""
+    trees, states in get_coal_states order; and whether the reference's brute-force
+    self-checks (arghmm_assert_transmat, _switch, arghmm_assert_emit: trans.cpp:856-1032,
+    emit.cpp:1222-1248) pass on the same trees (self_checks, 1 each)."""
     out_dir = os.path.join(HERE, "helpers")
     os.makedirs(out_dir, exist_ok=True)
     cases = [("k8_s11", simulate(7, 1500, 11), 12),
@@ -192,12 +194,14 @@ def helpers(tmp):
             S1, S2 = np.frombuffer(d, np.int32, 2, o); o += 8
             mats.append(np.frombuffer(d, np.float64, S1 * S2, o)); o += 8 * S1 * S2
             sizes.append((S1, S2))
+        checks = np.frombuffer(d, np.int32, nsw + 2, o); o += 4 * (nsw + 2)
         assert o == len(d)
         prob.save(os.path.join(out_dir, name + ".prob"))
         np.savez_compressed(os.path.join(out_dir, name + ".npz"), trans=trans, emit=emit,
                             switch_sizes=np.array(sizes, np.int32).reshape(-1, 2),
-                            switch=np.concatenate(mats) if mats else np.zeros(0))
-        print(name, S0, L0, sizes)
+                            switch=np.concatenate(mats) if mats else np.zeros(0),
+                            self_checks=checks)
+        print(name, S0, L0, sizes, checks)
 
 
 def densernd(tmp):

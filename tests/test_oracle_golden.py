@@ -190,3 +190,6 @@ def test_dense_helpers_match_reference(name):
     S0, L0 = gold["trans"].shape[0], gold["emit"].shape[0]
     em = pyoracle.emissions(prob)[:L0 * S0].reshape(L0, S0)
     np.testing.assert_array_equal(em, gold["emit"])
+    # the reference's brute-force checks of these matrices (transition and switch rows
+    # against sums over SPRs, emissions against per-state Felsenstein) passed on these trees
+    assert gold["self_checks"].tolist() == [1] * (len(switch_matrices(gold)) + 2)

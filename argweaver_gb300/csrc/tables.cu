@@ -1182,12 +1182,14 @@ __device__ __forceinline__ df operator*(df a, df b) {
 }
 __device__ __forceinline__ df &operator+=(df &a, df b) { return a = a + b; }
 __device__ __forceinline__ bool operator<(df a, df b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+__device__ __forceinline__ df fma(df a, df b, df c) { return a * b + c; }
 __device__ __forceinline__ df fmax(df a, df b) { return a < b ? b : a; }
 __device__ __forceinline__ df __shfl_xor_sync(unsigned mask, df v, int o) {
     return df(::__shfl_xor_sync(mask, v.hi, o), ::__shfl_xor_sync(mask, v.lo, o));
 }
 // the built-in overloads stay visible beside the double-float ones
 using ::fmax;
+using ::fma;
 using ::__shfl_xor_sync;
 
 // Per-tree context of K2 shared by the column passes.
@@ -1476,43 +1478,39 @@ __device__ R emit_column(const EmitCtx &c, const uint8_t *chars, int X, R (*in)[
     return ref;
 }
 
-// One variant column in double-float by one warp: the FP32 path's variant columns, the
-// partials and emissions of emit_column's F64 form (4 e_k into eb[S]; returns the largest)
-// with less work per step. A leaf with an observed base contributes its JC69 row's entries
-// (m, or nm for the base itself) instead of a step over its one-hot partial, and with the
-// threaded base b observed, sum_a p1_a t_a = m1 sum_{a != b} t_a + nm1 t_b.
-__device__ df emit_column_df(const EmitCtx &c, const uint8_t *chars, df (*in)[4], df (*out)[4],
-                             df *eb) {
+// A column whose observed calls all show one base X (it varies only through missing calls),
+// in double-float by one warp: 4 e_k into eb[S], returns the largest. Every partial is then
+// symmetric in the other three bases (the leaves' are (1, 0) or, missing, (1, 1); JC69 treats
+// the three alike), so it is kept as the pair (x_X, x_other): half the work of the four-base
+// form, the same sums. The FP32 path's columns of this kind (about 26% of all columns at
+// 0.5% missing calls, 87% of the variant ones) are where the forward posterior amplifies an
+// emission error most: their emissions differ little between states.
+__device__ df emit_near_df(const EmitCtx &c, const uint8_t *chars, int X, df (*in)[2],
+                           df (*out)[2], df *eb) {
     const int lane = threadIdx.x & 31;
     const int4 *nd = c.nd;
-    auto base_of = [&](uint8_t ch) {
-        return ch == 'N' ? 4 : (ch == 'A' || ch == 'a') ? 0 : (ch == 'C' || ch == 'c') ? 1
-             : (ch == 'G' || ch == 'g') ? 2 : 3;
+    // JC69 over a branch with m (to each other base), nm (no change)
+    auto step = [](const df *x, df m, df nm, df *y) {
+        const df dd = nm - m, ms = m * (x[0] + df(3.0) * x[1]);
+        y[0] = dd * x[0] + ms;
+        y[1] = dd * x[1] + ms;
     };
-    auto sum4 = [](const df *v) { return (v[0] + v[1]) + (v[2] + v[3]); };
-    // the JC69 step of node j's partial x over a branch with m, nm (j < 0: not a leaf)
-    auto step = [&](int j, const df *x, df m, df nm, df *y) {
-        const int b = j >= 0 && j < c.nleaves ? base_of(chars[j]) : 4;
-        if (b < 4) {
-#pragma unroll
-            for (int a = 0; a < 4; a++) y[a] = a == b ? nm : m;
-        } else {
-            const df dd = nm - m, ms = m * sum4(x);
-#pragma unroll
-            for (int a = 0; a < 4; a++) y[a] = dd * x[a] + ms;
-        }
+    auto leaf = [](uint8_t ch, df *v) {  // observed calls are X here
+        v[0] = df(1.0);
+        v[1] = ch == 'N' ? df(1.0) : df(0.0);
     };
-    for (int x = lane; x < c.inp[1]; x += 32) leaf_partial<df>(chars[c.inl[x]], in[c.inl[x]]);
+    (void)X;
+    for (int x = lane; x < c.inp[1]; x += 32) leaf(chars[c.inl[x]], in[c.inl[x]]);
     __syncwarp();
     for (int h = 1; h < c.nlev_in; h++) {
         for (int x = c.inp[h] + lane; x < c.inp[h + 1]; x += 32) {
             const int j = c.inl[x];
             const int c1 = nd[j].y, c2 = nd[j].z;
-            df p1[4], p2[4];
-            step(c1, in[c1], df(c.muts[c1]), df(c.nomuts[c1]), p1);
-            step(c2, in[c2], df(c.muts[c2]), df(c.nomuts[c2]), p2);
-#pragma unroll
-            for (int a = 0; a < 4; a++) in[j][a] = p1[a] * p2[a];
+            df p1[2], p2[2];
+            step(in[c1], df(c.muts[c1]), df(c.nomuts[c1]), p1);
+            step(in[c2], df(c.muts[c2]), df(c.nomuts[c2]), p2);
+            in[j][0] = p1[0] * p2[0];
+            in[j][1] = p1[1] * p2[1];
         }
         __syncwarp();
     }
@@ -1520,63 +1518,48 @@ __device__ df emit_column_df(const EmitCtx &c, const uint8_t *chars, df (*in)[4]
         for (int x = c.outp[h] + lane; x < c.outp[h + 1]; x += 32) {
             const int j = c.outl[x];
             if (j == c.mainr) {
-                out[j][0] = out[j][1] = out[j][2] = out[j][3] = df(1.0);
+                out[j][0] = out[j][1] = df(1.0);
                 continue;
             }
             const int p = nd[j].x;
             const int sib = nd[p].y == j ? nd[p].z : nd[p].y;
-            df p1[4];
-            step(sib, in[sib], df(c.muts[sib]), df(c.nomuts[sib]), p1);
+            df p1[2];
+            step(in[sib], df(c.muts[sib]), df(c.nomuts[sib]), p1);
             if (p != c.mainr) {
-                df p2[4];
-                step(-1, out[p], df(c.muts[p]), df(c.nomuts[p]), p2);
-#pragma unroll
-                for (int a = 0; a < 4; a++) out[j][a] = p1[a] * p2[a];
+                df p2[2];
+                step(out[p], df(c.muts[p]), df(c.nomuts[p]), p2);
+                out[j][0] = p1[0] * p2[0];
+                out[j][1] = p1[1] * p2[1];
             } else {
-#pragma unroll
-                for (int a = 0; a < 4; a++) out[j][a] = p1[a];
+                out[j][0] = p1[0];
+                out[j][1] = p1[1];
             }
         }
         __syncwarp();
     }
-    // the threaded sequence's base (external), else the subtree root's partial (internal)
-    const int bnew = c.internal ? 4 : base_of(chars[c.nleaves]);
-    df in2[4];
+    df in2[2];
     if (c.internal) {
-#pragma unroll
-        for (int a = 0; a < 4; a++) in2[a] = in[c.node1][a];
+        in2[0] = in[c.node1][0];
+        in2[1] = in[c.node1][1];
     } else {
-        leaf_partial<df>(chars[c.nleaves], in2);
+        leaf(chars[c.nleaves], in2);
     }
     auto state_v = [&](int k) -> df {
         const int node2 = c.snode[k];
         const double *q = c.pm + 6 * (size_t)k;  // mut0..2, nomut0..2
-        df p2[4], t[4];
-        step(node2, in[node2], df(q[1]), df(q[4]), p2);
+        df p1[2], p2[2], t[2];
+        step(in2, df(q[0]), df(q[3]), p1);
+        step(in[node2], df(q[1]), df(q[4]), p2);
         if (node2 != c.mainr) {
-            df p3[4];
-            step(-1, out[node2], df(q[2]), df(q[5]), p3);
-#pragma unroll
-            for (int a = 0; a < 4; a++) t[a] = p2[a] * p3[a];
+            df p3[2];
+            step(out[node2], df(q[2]), df(q[5]), p3);
+            t[0] = p2[0] * p3[0];
+            t[1] = p2[1] * p3[1];
         } else {
-#pragma unroll
-            for (int a = 0; a < 4; a++) t[a] = p2[a];
+            t[0] = p2[0];
+            t[1] = p2[1];
         }
-        df v;
-        if (bnew < 4) {
-            df rest = df(0.0);
-#pragma unroll
-            for (int a = 0; a < 4; a++)
-                if (a != bnew) rest += t[a];
-            v = df(q[0]) * rest + df(q[3]) * t[bnew];
-        } else {
-            df p1[4];
-            step(-1, in2, df(q[0]), df(q[3]), p1);
-            v = df(0.0);
-#pragma unroll
-            for (int a = 0; a < 4; a++) v += p1[a] * t[a];
-        }
-        return v;
+        return p1[0] * t[0] + df(3.0) * (p1[1] * t[1]);
     };
     // two states per lane at a time: independent chains the scheduler can interleave (the
     // second one repeats the last state where it would run past S)
@@ -1922,7 +1905,11 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
                     // state's split-branch steps are formed in double-float and each ratio
                     // to the column's largest is rounded once
                     df *ed = (df *)eb;
-                    emit_column_df(ctx, chars, (df (*)[4])wscr, (df (*)[4])wscr + n, ed);
+                    if (near)
+                        emit_near_df(ctx, chars, X, (df (*)[2])wscr, (df (*)[2])wscr + n, ed);
+                    else
+                        emit_column<df, EM_F64>(ctx, chars, 0, (df (*)[4])wscr,
+                                                (df (*)[4])wscr + n, ed);
                     double eref = 0.0;
                     for (int k = lane; k < S; k += 32) eref = fmax(eref, (double)ed[k]);
 #pragma unroll

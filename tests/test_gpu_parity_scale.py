@@ -271,3 +271,38 @@ def test_config3_multileaf_cut_fp32(c3):
     check_fp32_posterior(c3)
     u = np.random.default_rng(10).random(c3.seqlen)
     assert split_mismatches(c3, u) <= 2
+
+
+# ---- FP32 paths as samples of the posterior, at the benchmark's state counts -----------
+
+def test_fp32_paths_sample_the_posterior_at_scale():
+    """3,000 FP32 paths of one k = 64, 1,500-column problem (about 500 states per column)
+    drawn by the traceback alone from one resident FP32 forward table, fresh uniforms each:
+    every cell's empirical frequency within 5 sigma + 2e-3 of the FP64 posterior marginal,
+    and the mean total-variation distance between a column's empirical and posterior
+    distributions within 1.25x its expectation under exact sampling (a biased sampler at
+    this state count moves the mean well beyond that)."""
+    from argweaver_gb300.server import Server
+
+    prob = simulate(63, 1500, seed=105, missing=0.005)
+    post = api.posterior(prob)
+    off = pyoracle.offsets(pyoracle.nstates(prob))
+    assert np.diff(off).mean() > 400
+    n = 3000
+    rng = np.random.default_rng(11)
+    counts = np.zeros_like(post)
+    cols = np.arange(prob.seqlen)
+    with Server(device_bytes=2 << 30, max_inflight=1, max_batch=1) as srv:
+        t = srv.submit(prob, precision="fp32", resident=True)
+        assert srv.wait(t, timeout=120) is not None
+        for _ in range(n):
+            path = srv.resample(t, rng.random(prob.seqlen))
+            counts[off[cols] + path] += 1
+        srv.release(t)
+    emp = counts / n
+    sig = np.sqrt(post * (1.0 - post) / n)
+    assert np.all(np.abs(emp - post) <= 5.0 * sig + 2e-3)
+    # E|emp - p| ~ sqrt(2 / pi) * sigma for the cells with enough mass to be near normal
+    tv = 0.5 * np.add.reduceat(np.abs(emp - post), off[:-1])
+    expect = 0.5 * np.add.reduceat(np.sqrt(2.0 / np.pi) * sig, off[:-1])
+    assert tv.mean() <= 1.25 * expect.mean(), (tv.mean(), expect.mean())

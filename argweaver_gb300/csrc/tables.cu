@@ -1202,6 +1202,19 @@ struct EmitCtx {
     const uint8_t *sfloor;  // per state: a split branch of it was raised to mintime
     int nlev_in, nlev_out, mainr, node1, S, ns, nleaves, n;
     bool internal;
+    // muts, nomuts and pm hold double-float values (8 bytes each, in the same slots) instead
+    // of doubles: the FP32 path's double-float forms then read them without a conversion,
+    // which would run on the FP64 pipe in every step
+    bool dfpm;
+    __device__ __forceinline__ df dmut(int j) const {
+        return dfpm ? ((const df *)muts)[j] : df(muts[j]);
+    }
+    __device__ __forceinline__ df dnomut(int j) const {
+        return dfpm ? ((const df *)nomuts)[j] : df(nomuts[j]);
+    }
+    __device__ __forceinline__ df dpm(size_t i) const {
+        return dfpm ? ((const df *)pm)[i] : df(pm[i]);
+    }
 };
 
 __device__ __forceinline__ int base_bit(uint8_t ch) {
@@ -1310,8 +1323,17 @@ __device__ R emit_column(const EmitCtx &c, const uint8_t *chars, int X, R (*in)[
         else leaf_partial<R>(ch, v);
     };
     constexpr bool F32 = std::is_same<R, float>::value;
-    auto bm = [&](int j) -> R { if constexpr (F32) return c.muts32[j]; else return (R)c.muts[j]; };
-    auto bn = [&](int j) -> R { if constexpr (F32) return c.nomuts32[j]; else return (R)c.nomuts[j]; };
+    constexpr bool DF = std::is_same<R, df>::value;
+    auto bm = [&](int j) -> R {
+        if constexpr (F32) return c.muts32[j];
+        else if constexpr (DF) return c.dmut(j);
+        else return (R)c.muts[j];
+    };
+    auto bn = [&](int j) -> R {
+        if constexpr (F32) return c.nomuts32[j];
+        else if constexpr (DF) return c.dnomut(j);
+        else return (R)c.nomuts[j];
+    };
     auto step = [&](const R *x, R m, R nm, R *y) {
         const double m64 = (double)m, nm64 = (double)nm;
         if constexpr (MODE == EM_REL) {
@@ -1393,7 +1415,10 @@ __device__ R emit_column(const EmitCtx &c, const uint8_t *chars, int X, R (*in)[
             const float4 qb = *(const float4 *)(c.pm32 + 8 * k + 4);
             q[0] = qa.x; q[1] = qa.y; q[2] = qa.z; q[3] = qa.w; q[4] = qb.x; q[5] = qb.y; q[6] = qb.z;
         } else {
-            for (int t = 0; t < 6; t++) q[t] = (R)c.pm[6 * k + t];
+            for (int t = 0; t < 6; t++) {
+                if constexpr (DF) q[t] = c.dpm(6 * (size_t)k + t);
+                else q[t] = (R)c.pm[6 * k + t];
+            }
             q[6] = R(1) - R(4) * q[0];
         }
         R p1[4], p2[4], p3[4];
@@ -1491,13 +1516,13 @@ __device__ df emit_near_df(const EmitCtx &c, const uint8_t *chars, int X, df (*i
     const int4 *nd = c.nd;
     // JC69 over a branch with m (to each other base), nm (no change)
     auto step = [](const df *x, df m, df nm, df *y) {
-        const df dd = nm - m, ms = m * (x[0] + df(3.0) * x[1]);
+        const df dd = nm - m, ms = m * (x[0] + df(3.0f, 0.0f) * x[1]);
         y[0] = dd * x[0] + ms;
         y[1] = dd * x[1] + ms;
     };
     auto leaf = [](uint8_t ch, df *v) {  // observed calls are X here
-        v[0] = df(1.0);
-        v[1] = ch == 'N' ? df(1.0) : df(0.0);
+        v[0] = df(1.0f, 0.0f);
+        v[1] = ch == 'N' ? df(1.0f, 0.0f) : df();
     };
     (void)X;
     for (int x = lane; x < c.inp[1]; x += 32) leaf(chars[c.inl[x]], in[c.inl[x]]);
@@ -1507,8 +1532,8 @@ __device__ df emit_near_df(const EmitCtx &c, const uint8_t *chars, int X, df (*i
             const int j = c.inl[x];
             const int c1 = nd[j].y, c2 = nd[j].z;
             df p1[2], p2[2];
-            step(in[c1], df(c.muts[c1]), df(c.nomuts[c1]), p1);
-            step(in[c2], df(c.muts[c2]), df(c.nomuts[c2]), p2);
+            step(in[c1], c.dmut(c1), c.dnomut(c1), p1);
+            step(in[c2], c.dmut(c2), c.dnomut(c2), p2);
             in[j][0] = p1[0] * p2[0];
             in[j][1] = p1[1] * p2[1];
         }
@@ -1518,16 +1543,16 @@ __device__ df emit_near_df(const EmitCtx &c, const uint8_t *chars, int X, df (*i
         for (int x = c.outp[h] + lane; x < c.outp[h + 1]; x += 32) {
             const int j = c.outl[x];
             if (j == c.mainr) {
-                out[j][0] = out[j][1] = df(1.0);
+                out[j][0] = out[j][1] = df(1.0f, 0.0f);
                 continue;
             }
             const int p = nd[j].x;
             const int sib = nd[p].y == j ? nd[p].z : nd[p].y;
             df p1[2];
-            step(in[sib], df(c.muts[sib]), df(c.nomuts[sib]), p1);
+            step(in[sib], c.dmut(sib), c.dnomut(sib), p1);
             if (p != c.mainr) {
                 df p2[2];
-                step(out[p], df(c.muts[p]), df(c.nomuts[p]), p2);
+                step(out[p], c.dmut(p), c.dnomut(p), p2);
                 out[j][0] = p1[0] * p2[0];
                 out[j][1] = p1[1] * p2[1];
             } else {
@@ -1546,24 +1571,24 @@ __device__ df emit_near_df(const EmitCtx &c, const uint8_t *chars, int X, df (*i
     }
     auto state_v = [&](int k) -> df {
         const int node2 = c.snode[k];
-        const double *q = c.pm + 6 * (size_t)k;  // mut0..2, nomut0..2
+        const size_t q = 6 * (size_t)k;  // mut0..2, nomut0..2
         df p1[2], p2[2], t[2];
-        step(in2, df(q[0]), df(q[3]), p1);
-        step(in[node2], df(q[1]), df(q[4]), p2);
+        step(in2, c.dpm(q), c.dpm(q + 3), p1);
+        step(in[node2], c.dpm(q + 1), c.dpm(q + 4), p2);
         if (node2 != c.mainr) {
             df p3[2];
-            step(out[node2], df(q[2]), df(q[5]), p3);
+            step(out[node2], c.dpm(q + 2), c.dpm(q + 5), p3);
             t[0] = p2[0] * p3[0];
             t[1] = p2[1] * p3[1];
         } else {
             t[0] = p2[0];
             t[1] = p2[1];
         }
-        return p1[0] * t[0] + df(3.0) * (p1[1] * t[1]);
+        return p1[0] * t[0] + df(3.0f, 0.0f) * (p1[1] * t[1]);
     };
     // two states per lane at a time: independent chains the scheduler can interleave (the
     // second one repeats the last state where it would run past S)
-    df ref = df(0.0);
+    df ref = df();
     for (int k0 = lane; k0 < c.S; k0 += 64) {
         const int k1 = k0 + 32 < c.S ? k0 + 32 : k0;
         const df v0 = state_v(k0), v1 = state_v(k1);
@@ -1690,6 +1715,11 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
         return;
     }
     for (int i = tid; i < n; i += blockDim.x) nd[i] = d.nodes[B.nodes0 + i];
+    // FP32 path with double-float variant columns: no column takes an FP32 form, and the
+    // split-branch factors are stored as double-float unless a penalised column (FP64
+    // form) may need them as doubles
+    const bool f32forms = FP32OUT && !d.vardf;
+    const bool dfpm = FP32OUT && d.vardf && !(penalty < 1.0);
     const bool refill = bc->inst != B.inst;  // read by all before anyone rewrites it
     __syncthreads();
     if (refill) {
@@ -1717,9 +1747,14 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
                 m0 = branch_nomut(e);
             }
         }
-        muts[i] = m1;
-        nomuts[i] = m0;
-        if (FP32OUT) {
+        if (dfpm) {
+            ((df *)muts)[i] = df(m1);
+            ((df *)nomuts)[i] = df(m0);
+        } else {
+            muts[i] = m1;
+            nomuts[i] = m0;
+        }
+        if (f32forms) {
             muts32[i] = (float)m1;
             nomuts32[i] = (float)m0;
         }
@@ -1745,12 +1780,20 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
                          : branch_exp(fmax(coal_time - time1, mintime), mu);
         e[1] = age2 < T ? bc->e[age2][a] : branch_exp(fmax(coal_time - time2, mintime), mu);
         e[2] = parent != -1 ? bc->e[a][pidx] : bc->ez[a];
-        if (!lean)
+        if (dfpm) {  // branch_mut / branch_nomut in double-float: one FP64 split each
+            const df quarter(0.25f, 0.0f), one(1.0f, 0.0f), three(3.0f, 0.0f);
+            for (int x = 0; x < 3; x++) {
+                const df ex(e[x]);
+                ((df *)pm)[6 * k + x] = quarter * (one - ex);
+                ((df *)pm)[6 * k + 3 + x] = quarter * (one + three * ex);
+            }
+        } else if (!lean) {
             for (int x = 0; x < 3; x++) {
                 pm[6 * k + x] = branch_mut(e[x]);
                 pm[6 * k + 3 + x] = branch_nomut(e[x]);
             }
-        if (FP32OUT) {
+        }
+        if (f32forms) {
             for (int x = 0; x < 3; x++) {
                 pm32[8 * k + x] = (float)branch_mut(e[x]);
                 pm32[8 * k + 3 + x] = (float)branch_nomut(e[x]);
@@ -1793,8 +1836,9 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
     }
     __syncthreads();
 
-    const EmitCtx ctx{nd, muts, nomuts, pm, muts32, nomuts32, pm32, snode, inl, inp, outl, outp,
-                      sfloor, nlev_in, nlev_out, mainr, node1, S, I.nseqs, I.nleaves, n, internal};
+    const EmitCtx ctx{nd,      muts,     nomuts,   pm,   muts32,  nomuts32, pm32, snode,
+                      inl,     inp,      outl,     outp, sfloor,  nlev_in,  nlev_out,
+                      mainr,   node1,    S,        I.nseqs, I.nleaves, n,   internal, dfpm};
     double *wscr = (double *)((char *)scratch + (size_t)warp * n * 8 * esz);
     double *eb = (double *)(ebuf + (size_t)warp * maxS * esz);  // read as float when lean
     const uint8_t *cls = d.colclass + I.col0 + B.start;
@@ -1904,22 +1948,23 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
                     // columns that vary only through missing calls): the partials and every
                     // state's split-branch steps are formed in double-float and each ratio
                     // to the column's largest is rounded once
+                    // (FP64 arithmetic only once per column: per state it would hold the
+                    // FP64 pipe, 64 cycles a warp instruction)
                     df *ed = (df *)eb;
-                    if (near)
-                        emit_near_df(ctx, chars, X, (df (*)[2])wscr, (df (*)[2])wscr + n, ed);
-                    else
-                        emit_column<df, EM_F64>(ctx, chars, 0, (df (*)[4])wscr,
-                                                (df (*)[4])wscr + n, ed);
-                    double eref = 0.0;
-                    for (int k = lane; k < S; k += 32) eref = fmax(eref, (double)ed[k]);
-#pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) eref = fmax(eref, ::__shfl_xor_sync(0xffffffffu, eref, o));
-                    const double inv1 = 1.0 / eref;  // 1 / (4 e_ref)
+                    const df eref =
+                        near ? emit_near_df(ctx, chars, X, (df (*)[2])wscr, (df (*)[2])wscr + n, ed)
+                             : emit_column<df, EM_F64>(ctx, chars, 0, (df (*)[4])wscr,
+                                                       (df (*)[4])wscr + n, ed);
+                    const double erefd = (double)eref;
+                    const df inv1(1.0 / erefd);  // 1 / (4 e_ref)
+                    const df one(1.0f, 0.0f);
                     for (int k = lane; k < S; k += 32) {
-                        const double r = (double)ed[k] * inv1;  // e_k / e_ref
-                        row[k] = (float)(r >= 0.5 ? 1.0 - r : -r);
+                        const df r = ed[k] * inv1;  // e_k / e_ref
+                        float v = r.hi >= 0.5f ? (one - r).hi : -r.hi;
+                        if (r.hi < 0.5f && v == 0.0f) v = -__int_as_float(1);  // stays a ratio
+                        row[k] = v;
                     }
-                    if (lane == 0) d.lnvref[B.vrow0 + vrow] = log(.25 * eref);
+                    if (lane == 0) d.lnvref[B.vrow0 + vrow] = log(.25 * erefd);
                 } else if (!internal) {
                     // brackets against the column's largest: D form x / plain form y
                     float *fs = (float *)wscr, *fe = (float *)eb;

@@ -494,9 +494,9 @@ const char *awg_server_last_error(void);
  * bytes: S = 300 fits about 25,000 columns.)
  *
  * Set-up: the first call on each device, with that device current, loads the module that
- * holds the array (cudaGetSymbolAddress). Make that first call before any stream capture
- * starts. Every call resolves the array's address again in the current context, so a
- * context destroyed and recreated in between (cudaDeviceReset) is safe.
+ * holds the array (cudaGetSymbolAddress). Every call resolves the array's address again in
+ * the current context, so a context destroyed and recreated in between (cudaDeviceReset)
+ * is safe. Each call copies from pageable host memory and waits for its stream.
  * Zeroing: only the 16-byte error record has to start at zero, and each call clears it
  * itself (cudaMemsetAsync). Every other byte of the array is written before it is read.
  * Concurrency: the array is shared by every call on a device. Calls that overlap in time

@@ -113,14 +113,15 @@ struct BatchDev {
     //   inv32    1 - e_k / e_ref for invariant sites, e_ref the block's largest emission
     //   lneref   [nblocks] log(e_ref), added to the log-likelihood per invariant column
     //   var32    1 - e_k / e_ref for variant columns too, e_ref the column's largest
-    //            emission (formed in FP64: a column that varies only through missing calls
-    //            has emissions equal to a few digits, which FP32 values would lose)
-    //   lnvref   [variant columns] log(e_ref) of each variant column
+    //            emission (formed in double-float: a column that varies only through
+    //            missing calls has emissions equal to a few digits, which FP32 values lose)
+    //   vref     [variant columns] e_ref / 4 of each variant column (its log is taken when
+    //            the tree's share is summed)
     //   blkext   [nblocks] a tree's sum of those references over its columns (lneref per
-    //            invariant column, lnvref per variant column; not the instance's column 0),
+    //            invariant column, log(vref) per variant column; not the instance's column 0),
     //            added to the log-likelihood once per tree
     float *tm32, *t2d32, *inv32, *var32, *determprob32, *recombrow32, *recoalrow32, *rstay32;
-    double *lneref, *lnvref, *blkext;
+    double *lneref, *vref, *blkext;
     // [total columns * MAXT] or NULL: per stored FP32 forward column, its time-bin sums
     // (the fgroups of arghmm_forward_block, sample_thread.cpp:258-263), written by the
     // forward kernel for the traceback's decomposed draw

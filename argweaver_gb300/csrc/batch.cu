@@ -312,7 +312,7 @@ int ctx_launch(Ctx &C, const awg_problem *probs, awg_outputs *outs, int n, const
     const size_t o_gidx = w.add(sizeof(int) * ST);
     const size_t o_var = w.add(sizeof(double) * std::max(plan.total_var, 1LL));
     size_t o_tm32 = 0, o_t2d32 = 0, o_inv32 = 0, o_var32 = 0, o_detp32 = 0, o_rrow32 = 0,
-           o_crow32 = 0, o_rstay32 = 0, o_lneref = 0, o_lnvref = 0,
+           o_crow32 = 0, o_rstay32 = 0, o_lneref = 0, o_vref = 0,
            o_blkext = 0;
     if (fp32) {
         o_tm32 = w.add(sizeof(float) * (size_t)plan.nblocks * MAXT * MAXT);
@@ -324,7 +324,7 @@ int ctx_launch(Ctx &C, const awg_problem *probs, awg_outputs *outs, int n, const
         o_crow32 = w.add(sizeof(float) * ST);
         o_rstay32 = w.add(sizeof(float) * (size_t)plan.nblocks * MAXT);
         o_lneref = w.add(sizeof(double) * plan.nblocks);
-        o_lnvref = w.add(sizeof(double) * std::max(plan.total_vcols, 1LL));
+        o_vref = w.add(sizeof(double) * std::max(plan.total_vcols, 1LL));
         o_blkext = w.add(sizeof(double) * plan.nblocks);
     }
     const size_t o_fw = w.add((fp32 ? sizeof(float) : sizeof(double)) * CELLS);
@@ -440,7 +440,7 @@ int ctx_launch(Ctx &C, const awg_problem *probs, awg_outputs *outs, int n, const
         d.recoalrow32 = (float *)(D + o_crow32);
         d.rstay32 = (float *)(D + o_rstay32);
         d.lneref = (double *)(D + o_lneref);
-        d.lnvref = (double *)(D + o_lnvref);
+        d.vref = (double *)(D + o_vref);
         d.blkext = (double *)(D + o_blkext);
         d.fw32 = (float *)(D + o_fw);
     } else {
@@ -574,7 +574,7 @@ int ctx_launch(Ctx &C, const awg_problem *probs, awg_outputs *outs, int n, const
                              o_order, o_blkmap, o_u, o_sinfo, o_t2off, o_btptr, o_btperm, o_tm,
                              o_gts, o_inv, o_det, o_detp, o_srcs, o_rrow, o_crow, o_gptr, o_gidx,
                              o_var, o_tm32, o_t2d32, o_inv32, o_var32, o_detp32, o_rrow32,
-                             o_crow32, o_rstay32, o_lneref, o_lnvref, o_blkext, o_fw, o_lnl,
+                             o_crow32, o_rstay32, o_lneref, o_vref, o_blkext, o_fw, o_lnl,
                              o_post, o_bw, o_path, o_bins, o_err, o_queue})
                 sig.push_back((long long)o);
             for (int g = 0; g <= ng; g++) sig.push_back(bounds[g]);

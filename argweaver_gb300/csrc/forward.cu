@@ -46,7 +46,7 @@ template <> struct Tab<double> {
     static constexpr bool split = false;
     const double *tm, *inv, *var, *dprob, *rrow, *crow, *gts;
     const float *rstay = nullptr;
-    const double *lneref = nullptr, *lnvref = nullptr;
+    const double *lneref = nullptr, *vref = nullptr;
     double *fw;
     __device__ explicit Tab(const BatchDev &d)
         : tm(d.tm), inv(d.inv_lk), var(d.varemit), dprob(d.determprob), rrow(d.recombrow),
@@ -59,11 +59,11 @@ template <> struct Tab<float> {
     static constexpr bool split = true;
     const float *tm, *inv, *var, *dprob, *rrow, *crow, *t2d;
     const float *rstay;
-    const double *lneref, *lnvref;
+    const double *lneref, *vref;
     float *fw;
     __device__ explicit Tab(const BatchDev &d)
         : tm(d.tm32), inv(d.inv32), var(d.var32), dprob(d.determprob32), rrow(d.recombrow32),
-          crow(d.recoalrow32), t2d(d.t2d32), rstay(d.rstay32), lneref(d.lneref), lnvref(d.lnvref),
+          crow(d.recoalrow32), t2d(d.t2d32), rstay(d.rstay32), lneref(d.lneref), vref(d.vref),
           fw(d.fw32) {}
     __device__ float t2(long long idx, float) const { return t2d[idx]; }
 };

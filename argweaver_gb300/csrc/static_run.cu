@@ -88,7 +88,7 @@ int run_static(const awg_problem *p, awg_outputs *out, int precision, cudaStream
     const size_t o_gidx = c.add(sizeof(int) * ST);
     const size_t o_var = c.add(sizeof(double) * std::max(plan.total_var, 1LL));
     size_t o_tm32 = 0, o_t2d32 = 0, o_inv32 = 0, o_var32 = 0, o_detp32 = 0, o_rrow32 = 0,
-           o_crow32 = 0, o_rstay32 = 0, o_lneref = 0, o_lnvref = 0,
+           o_crow32 = 0, o_rstay32 = 0, o_lneref = 0, o_vref = 0,
            o_blkext = 0;
     if (fp32) {
         o_tm32 = c.add(sizeof(float) * (size_t)plan.nblocks * MAXT * MAXT);
@@ -100,7 +100,7 @@ int run_static(const awg_problem *p, awg_outputs *out, int precision, cudaStream
         o_crow32 = c.add(sizeof(float) * ST);
         o_rstay32 = c.add(sizeof(float) * (size_t)plan.nblocks * MAXT);
         o_lneref = c.add(sizeof(double) * plan.nblocks);
-        o_lnvref = c.add(sizeof(double) * std::max(plan.total_vcols, 1LL));
+        o_vref = c.add(sizeof(double) * std::max(plan.total_vcols, 1LL));
         o_blkext = c.add(sizeof(double) * plan.nblocks);
     }
     const size_t o_fw = c.add((fp32 ? sizeof(float) : sizeof(double)) * CELLS);
@@ -183,7 +183,7 @@ int run_static(const awg_problem *p, awg_outputs *out, int precision, cudaStream
         d.recoalrow32 = (float *)(D + o_crow32);
         d.rstay32 = (float *)(D + o_rstay32);
         d.lneref = (double *)(D + o_lneref);
-        d.lnvref = (double *)(D + o_lnvref);
+        d.vref = (double *)(D + o_vref);
         d.blkext = (double *)(D + o_blkext);
         d.fw32 = (float *)(D + o_fw);
     } else {

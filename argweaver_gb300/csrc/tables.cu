@@ -1603,8 +1603,10 @@ __device__ df emit_near_df(const EmitCtx &c, const uint8_t *chars, int X, df (*i
 }
 
 // FP32 path: a tree's share of the log-likelihood's emission references, lneref per
-// invariant column and lnvref per variant column (the instance's column 0, the prior, has
-// none), summed by one warp in a fixed order.
+// invariant column and log(vref) per variant column (the instance's column 0, the prior, has
+// none), summed by one warp in a fixed order. The logarithms are taken here, a lane per
+// column, not by one lane per column in the emission passes: there an FP64 log holds the
+// warp's FP64 pipe for a few thousand cycles per column.
 __device__ void block_log_offset(const BatchDev &d, const BlockDev &B, const InstDev &I, int blk,
                                  int lane) {
     const uint8_t *cls = d.colclass + I.col0 + B.start;
@@ -1616,7 +1618,7 @@ __device__ void block_log_offset(const BatchDev &d, const BlockDev &B, const Ins
             if (B.b == 0 && i == 0) continue;
             const uint8_t c = cls[i];
             if (c == COL_INVARIANT) s += lner;
-            else if (c == COL_VARIANT) s += d.lnvref[B.vrow0 + cvar[i]];
+            else if (c == COL_VARIANT) s += log(d.vref[B.vrow0 + cvar[i]]);
         }
     }
 #pragma unroll
@@ -1909,7 +1911,7 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
                     if (r < 0.5 && v == 0.0f) v = -__int_as_float(1);
                     row[k] = v;
                 }
-                if (lane == 0) d.lnvref[B.vrow0 + vrow] = log(.25 * eref);
+                if (lane == 0) d.vref[B.vrow0 + vrow] = .25 * eref;
             } else {
                 // X = the column's first observed base; near = every observed call (the
                 // threaded sequence's too) is X
@@ -1941,7 +1943,7 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
                         const float c = (fe[k] - dref) * inv1;  // 1 - e_k / e_ref
                         row[k] = c <= 0.5f ? c : -((1.f - fe[k]) * inv1);
                     }
-                    if (lane == 0) d.lnvref[B.vrow0 + vrow] = log(.25) + log1p(-(double)dref);
+                    if (lane == 0) d.vref[B.vrow0 + vrow] = .25 * (1.0 - (double)dref);
                 } else if (d.vardf) {
                     // the forward posterior amplifies an error of a variant column's
                     // emissions thousands-fold where they differ little between states (the
@@ -1955,16 +1957,20 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
                         near ? emit_near_df(ctx, chars, X, (df (*)[2])wscr, (df (*)[2])wscr + n, ed)
                              : emit_column<df, EM_F64>(ctx, chars, 0, (df (*)[4])wscr,
                                                        (df (*)[4])wscr + n, ed);
-                    const double erefd = (double)eref;
-                    const df inv1(1.0 / erefd);  // 1 / (4 e_ref)
+                    // 1 / (4 e_ref): the FP32 reciprocal and one Newton step in double-float
                     const df one(1.0f, 0.0f);
+                    const df y0(1.0f / eref.hi, 0.0f);
+                    const df inv1 = y0 + y0 * (one - eref * y0);
                     for (int k = lane; k < S; k += 32) {
-                        const df r = ed[k] * inv1;  // e_k / e_ref
-                        float v = r.hi >= 0.5f ? (one - r).hi : -r.hi;
+                        // e_k / e_ref; the largest state's r can round a hair above 1, so its
+                        // complement is clamped at +0 (a negative value would read as a
+                        // ratio, i.e. an emission near zero)
+                        const df r = ed[k] * inv1;
+                        float v = r.hi >= 0.5f ? fmaxf((one - r).hi, 0.0f) : -r.hi;
                         if (r.hi < 0.5f && v == 0.0f) v = -__int_as_float(1);  // stays a ratio
                         row[k] = v;
                     }
-                    if (lane == 0) d.lnvref[B.vrow0 + vrow] = log(.25 * erefd);
+                    if (lane == 0) d.vref[B.vrow0 + vrow] = .25 * (double)eref;
                 } else if (!internal) {
                     // brackets against the column's largest: D form x / plain form y
                     float *fs = (float *)wscr, *fe = (float *)eb;
@@ -1986,7 +1992,7 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
                         // W: the tree's own likelihood, sum over the main root's inner partial
                         const float *im = fs + 4 * mainr;
                         const double w = (double)((im[0] + im[1]) + (im[2] + im[3]));
-                        d.lnvref[B.vrow0 + vrow] = log(.25 * w * (double)bref);
+                        d.vref[B.vrow0 + vrow] = .25 * w * (double)bref;
                     }
                 } else {
                     const double eref = emit_column<double, EM_F64>(ctx, chars, X, (double (*)[4])wscr,
@@ -1996,14 +2002,14 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
                         const double r = eb[k] * inv1;  // e_k / e_ref
                         row[k] = (float)(r >= 0.5 ? 1.0 - r : -r);
                     }
-                    if (lane == 0) d.lnvref[B.vrow0 + vrow] = log(.25 * eref);
+                    if (lane == 0) d.vref[B.vrow0 + vrow] = .25 * eref;
                 }
             }
             __syncwarp();
         }
     }
     if constexpr (FP32OUT) {
-        __syncthreads();  // every variant column's lnvref written
+        __syncthreads();  // every variant column's vref written
         if (warp == 0) block_log_offset(d, B, I, blk, lane);
     }
 }

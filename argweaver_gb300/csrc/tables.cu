@@ -1160,6 +1160,8 @@ struct df {
     float hi, lo;
     __device__ __forceinline__ df() : hi(0.f), lo(0.f) {}
     __device__ __forceinline__ df(double x) : hi((float)x), lo((float)(x - (double)(float)x)) {}
+    // small integer constants (0, 1, 4 in the emission forms) without the FP64 split
+    __device__ __forceinline__ df(int x) : hi((float)x), lo(0.0f) {}
     __device__ __forceinline__ df(float h, float l) : hi(h), lo(l) {}
     __device__ __forceinline__ explicit operator double() const { return (double)hi + (double)lo; }
 };
@@ -1202,19 +1204,12 @@ struct EmitCtx {
     const uint8_t *sfloor;  // per state: a split branch of it was raised to mintime
     int nlev_in, nlev_out, mainr, node1, S, ns, nleaves, n;
     bool internal;
-    // muts, nomuts and pm hold double-float values (8 bytes each, in the same slots) instead
-    // of doubles: the FP32 path's double-float forms then read them without a conversion,
-    // which would run on the FP64 pipe in every step
-    bool dfpm;
-    __device__ __forceinline__ df dmut(int j) const {
-        return dfpm ? ((const df *)muts)[j] : df(muts[j]);
-    }
-    __device__ __forceinline__ df dnomut(int j) const {
-        return dfpm ? ((const df *)nomuts)[j] : df(nomuts[j]);
-    }
-    __device__ __forceinline__ df dpm(size_t i) const {
-        return dfpm ? ((const df *)pm)[i] : df(pm[i]);
-    }
+    // The FP32 path's double-float forms (BatchDev::vardf): muts, nomuts and pm then hold
+    // double-float values, 8 bytes each in the same slots, so that the steps read them with
+    // no conversion (a conversion from double runs on the FP64 pipe, in every step)
+    __device__ __forceinline__ df dmut(int j) const { return ((const df *)muts)[j]; }
+    __device__ __forceinline__ df dnomut(int j) const { return ((const df *)nomuts)[j]; }
+    __device__ __forceinline__ df dpm(size_t i) const { return ((const df *)pm)[i]; }
 };
 
 __device__ __forceinline__ int base_bit(uint8_t ch) {
@@ -1717,11 +1712,11 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
         return;
     }
     for (int i = tid; i < n; i += blockDim.x) nd[i] = d.nodes[B.nodes0 + i];
-    // FP32 path with double-float variant columns: no column takes an FP32 form, and the
-    // split-branch factors are stored as double-float unless a penalised column (FP64
-    // form) may need them as doubles
+    // FP32 path with double-float variant columns: every variant column takes that form
+    // (penalised ones too), so the split-branch factors are stored as double-float and no
+    // FP32 form's copies are made
     const bool f32forms = FP32OUT && !d.vardf;
-    const bool dfpm = FP32OUT && d.vardf && !(penalty < 1.0);
+    const bool dfpm = FP32OUT && d.vardf;
     const bool refill = bc->inst != B.inst;  // read by all before anyone rewrites it
     __syncthreads();
     if (refill) {
@@ -1840,7 +1835,7 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
 
     const EmitCtx ctx{nd,      muts,     nomuts,   pm,   muts32,  nomuts32, pm32, snode,
                       inl,     inp,      outl,     outp, sfloor,  nlev_in,  nlev_out,
-                      mainr,   node1,    S,        I.nseqs, I.nleaves, n,   internal, dfpm};
+                      mainr,   node1,    S,        I.nseqs, I.nleaves, n,   internal};
     double *wscr = (double *)((char *)scratch + (size_t)warp * n * 8 * esz);
     double *eb = (double *)(ebuf + (size_t)warp * maxS * esz);  // read as float when lean
     const uint8_t *cls = d.colclass + I.col0 + B.start;
@@ -1891,7 +1886,7 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
                 if (penalised) penalise(eb);
                 double *row = d.varemit + B.var0 + (size_t)vrow * S;
                 for (int k = lane; k < S; k += 32) row[k] = eb[k];
-            } else if (penalised) {
+            } else if (penalised && !d.vardf) {
                 // FP64 emissions, penalised, then relative to the column's largest
                 const int X0 = 0;
                 emit_column<double, EM_F64>(ctx, chars, X0, (double (*)[4])wscr,
@@ -1953,10 +1948,30 @@ __device__ __forceinline__ void varemit_tree(const BatchDev &d, int blk, int nwa
                     // (FP64 arithmetic only once per column: per state it would hold the
                     // FP64 pipe, 64 cycles a warp instruction)
                     df *ed = (df *)eb;
-                    const df eref =
+                    df eref =
                         near ? emit_near_df(ctx, chars, X, (df (*)[2])wscr, (df (*)[2])wscr + n, ed)
                              : emit_column<df, EM_F64>(ctx, chars, 0, (df (*)[4])wscr,
                                                        (df (*)[4])wscr + n, ed);
+                    if (penalised) {
+                        // states that break the infinite-sites model times the penalty
+                        // (emit.cpp:847-862); below FP32's range that leaves the ratio 0,
+                        // written as the smallest negative value below, as the FP64 form
+                        // writes it
+                        const df pen(penalty);
+                        df mx;
+                        for (int kb = 0; kb < S; kb += 32) {
+                            const int k = kb + lane;
+                            const bool ok = state_ok(vword, k < S ? snode[k] : 0);
+                            if (k < S) {
+                                if (!ok) ed[k] = ed[k] * pen;
+                                mx = fmax(mx, ed[k]);
+                            }
+                        }
+#pragma unroll
+                        for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+                        eref = mx;
+                        __syncwarp();
+                    }
                     // 1 / (4 e_ref): the FP32 reciprocal and one Newton step in double-float
                     const df one(1.0f, 0.0f);
                     const df y0(1.0f / eref.hi, 0.0f);

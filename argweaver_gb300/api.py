@@ -156,6 +156,64 @@ def _bind_batch(problems, precision, want_forward, want_path, want_posterior, un
     return probs, outs, results, keep
 
 
+class BatchContext:
+    """Batches in flight from one thread (awg_batch_ctx): launch() plans, uploads and queues
+    a batch and returns; finish() waits for it and returns its results. Two contexts used in
+    turn overlap one batch's host work (binding, planning, upload) with the other's kernels;
+    a context holds one batch at a time."""
+
+    def __init__(self):
+        self._lib = capi.load()
+        self._h = self._lib.awg_batch_ctx_create()
+        if not self._h:
+            raise GpuError(capi.last_error())
+        self._pending = None
+
+    def launch(self, problems: Sequence[Problem], *, precision: str = "fp32",
+               want_forward: bool = False, want_path: bool = True, want_posterior: bool = False,
+               uniforms: Optional[Sequence[Optional[np.ndarray]]] = None) -> None:
+        if self._pending is not None:
+            raise RuntimeError("finish() the context's last batch before launching another")
+        probs, outs, results, keep = _bind_batch(problems, precision, want_forward, want_path,
+                                                 want_posterior, uniforms)
+        prec = capi.AWG_FP32 if precision == "fp32" else capi.AWG_FP64
+        rc = self._lib.awg_batch_launch(self._h, probs, outs, len(problems), prec)
+        if rc != 0:
+            raise GpuError(f"awg_batch_launch failed ({rc}): {capi.last_error()}")
+        self._pending = (probs, outs, results, keep)
+
+    def finish(self) -> List[Result]:
+        if self._pending is None:
+            raise RuntimeError("no batch in flight")
+        _, _, results, _ = self._pending
+        self._pending = None
+        rc = self._lib.awg_batch_finish(self._h)
+        if rc != 0:
+            raise GpuError(f"awg_batch_finish failed ({rc}): {capi.last_error()}")
+        out = []
+        for r, ll in results:
+            r.loglik = float(ll[0])
+            out.append(r)
+        return out
+
+    def close(self) -> None:
+        if self._h:
+            self._lib.awg_batch_ctx_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def autotune(problems: Sequence[Problem], *, precision: str = "fp32", want_path: bool = True,
              trials: int = 2) -> dict:
     """Time the candidate schedules on this batch and keep the fastest for its shape class

@@ -186,6 +186,11 @@ PROTOTYPES += [
                                C.c_int, C.c_char_p, C.c_int]),
     ("awg_batch_device_bytes", C.c_longlong, [C.POINTER(AwgProblem), C.c_int, C.c_int, C.c_int,
                                               C.c_int]),
+    ("awg_batch_ctx_create", C.c_void_p, []),
+    ("awg_batch_launch", C.c_int, [C.c_void_p, C.POINTER(AwgProblem), C.POINTER(AwgOutputs),
+                                   C.c_int, C.c_int]),
+    ("awg_batch_finish", C.c_int, [C.c_void_p]),
+    ("awg_batch_ctx_destroy", None, [C.c_void_p]),
     ("awg_release_memory", C.c_int, []),
     ("awg_sample_path_conditioned", C.c_int,
      [C.POINTER(AwgProblem), c_double_p, C.c_int, c_double_p, c_int_p, c_double_p]),

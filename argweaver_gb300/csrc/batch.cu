@@ -825,6 +825,8 @@ void ctx_destroy(Ctx *C) {
     delete C;
 }
 
+void ctx_set_graphs(Ctx *C, bool on) { C->graphs = on; }
+
 void ctx_set_region(Ctx *C, char *dev, size_t bytes) {
     C->ext = dev;
     C->ext_cap = bytes;

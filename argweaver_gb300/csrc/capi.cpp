@@ -271,6 +271,67 @@ int awg_run_batch(const awg_problem *problems, awg_outputs *outputs, int n, int 
     return rc;
 }
 
+}  // extern "C"
+
+struct awg_batch_ctx {
+    awg::Ctx *ctx = nullptr;
+    bool pending = false;
+};
+
+extern "C" {
+
+awg_batch_ctx *awg_batch_ctx_create(void) {
+    g_err.clear();
+    awg_batch_ctx *c = new awg_batch_ctx();
+    c->ctx = awg::ctx_create();
+    awg::ctx_set_graphs(c->ctx, true);
+    return c;
+}
+
+int awg_batch_launch(awg_batch_ctx *c, const awg_problem *problems, awg_outputs *outputs, int n,
+                     int precision) {
+    g_err.clear();
+    if (!c || !problems || !outputs || n < 1) {
+        set_error("awg_batch_launch: bad arguments");
+        return -1;
+    }
+    if (c->pending) {
+        set_error("awg_batch_launch: the context's last batch is not finished");
+        return -1;
+    }
+    std::string err;
+    const int rc = awg::ctx_launch_async(c->ctx, problems, outputs, n, precision, err);
+    if (rc != 0) {
+        awg::ctx_sync(c->ctx);  // nothing of the failed launch left in flight
+        set_error(err);
+        return rc;
+    }
+    c->pending = true;
+    return 0;
+}
+
+int awg_batch_finish(awg_batch_ctx *c) {
+    g_err.clear();
+    if (!c || !c->pending) {
+        set_error("awg_batch_finish: no batch in flight");
+        return -1;
+    }
+    c->pending = false;
+    std::string err;
+    const int rc = awg::ctx_finish(c->ctx, err);
+    if (rc != 0) set_error(err);
+    return rc;
+}
+
+void awg_batch_ctx_destroy(awg_batch_ctx *c) {
+    if (!c) return;
+    if (c->ctx) {
+        awg::ctx_sync(c->ctx);
+        awg::ctx_destroy(c->ctx);
+    }
+    delete c;
+}
+
 long long awg_batch_device_bytes(const awg_problem *problems, int n, int precision, int want_path,
                                  int want_posterior) {
     g_err.clear();

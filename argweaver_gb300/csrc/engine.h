@@ -57,6 +57,9 @@ struct Ctx;
 Ctx *ctx_create();
 void ctx_destroy(Ctx *C);
 void ctx_set_region(Ctx *C, char *dev, size_t bytes);
+// Capture each step as a CUDA graph and replay it while its shape repeats (off by default
+// for contexts made here: a server's batches rarely repeat a shape).
+void ctx_set_graphs(Ctx *C, bool on);
 // Page-locked input and output staging of at least these sizes, allocated now.
 int ctx_reserve_host(Ctx *C, size_t in_bytes, size_t out_bytes);
 int ctx_launch_async(Ctx *C, const awg_problem *probs, awg_outputs *outs, int n, int precision,

@@ -368,6 +368,22 @@ int awg_problems_cells(const awg_problem *problems, int n, long long *cells);
  * Returns 0 on success, a negative code on error (awg_last_error() has the message). */
 int awg_run_batch(const awg_problem *problems, awg_outputs *outputs, int n, int precision);
 
+/* Batches in flight from one thread (no counterpart in the reference): a context plans,
+ * uploads and enqueues a batch (awg_batch_launch returns once its kernels are queued), and
+ * awg_batch_finish waits for it and hands its outputs to the caller's buffers. Two contexts
+ * used in turn keep the GPU busy while the host plans and uploads the next batch. Each
+ * context owns its own streams, page-locked staging and device arena (grown as needed and
+ * kept), and replays a batch shape it has seen from a CUDA graph. The output buffers and
+ * uniforms must stay valid until awg_batch_finish; a context runs one batch at a time
+ * (launch, finish, launch, ...). Both return 0 or a negative code (awg_last_error); results
+ * equal awg_run_batch's. */
+typedef struct awg_batch_ctx awg_batch_ctx;
+awg_batch_ctx *awg_batch_ctx_create(void);
+int awg_batch_launch(awg_batch_ctx *ctx, const awg_problem *problems, awg_outputs *outputs,
+                     int n, int precision);
+int awg_batch_finish(awg_batch_ctx *ctx);
+void awg_batch_ctx_destroy(awg_batch_ctx *ctx);
+
 /* Device bytes awg_run_batch needs for this batch with these outputs wanted (the size of a
  * server pool or of a region to set aside), or a negative code (awg_last_error). */
 long long awg_batch_device_bytes(const awg_problem *problems, int n, int precision, int want_path,

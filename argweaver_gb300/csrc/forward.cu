@@ -408,7 +408,7 @@ constexpr int NRW = 4;                      // reduction warps of the register v
 constexpr int RBINS = (MAXT - 1 + NRW - 1) / NRW;  // time bins per reduction warp (<= 8)
 
 template <typename F, int KPT>
-__global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int maxM, int t2_in_smem) {
+__device__ __forceinline__ void forward_reg_body(BatchDev d, int maxS, int maxM, int t2_in_smem) {
     extern __shared__ double dyn_d[];
     const Tab<F> tab(d);
     const int qi = cta_instance(d);
@@ -840,6 +840,33 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
     }
 }
 
+// The register variant's kernels. FP32 with 1 or 2 states a thread: at most FWD32_NREG
+// registers a thread (the body needs no more without spilling), so that per-tree kernels'
+// CTAs fit on an SM beside a forward CTA and the chains share the SMs with the per-tree work
+// of later instance groups. Otherwise up to the 512-thread bound.
+#ifndef FWD32_NREG
+#define FWD32_NREG 88
+#endif
+template <int KPT>
+__global__ void __maxnreg__(FWD32_NREG) k_forward_reg32(BatchDev d, int maxS, int maxM, int t2_in_smem) {
+    forward_reg_body<float, KPT>(d, maxS, maxM, t2_in_smem);
+}
+// 4 and 8 states a thread (large trees) keep the registers they take
+template <int KPT>
+__global__ void __launch_bounds__(512) k_forward_reg32w(BatchDev d, int maxS, int maxM, int t2_in_smem) {
+    forward_reg_body<float, KPT>(d, maxS, maxM, t2_in_smem);
+}
+template <int KPT>
+__global__ void __launch_bounds__(512) k_forward_reg64(BatchDev d, int maxS, int maxM, int t2_in_smem) {
+    forward_reg_body<double, KPT>(d, maxS, maxM, t2_in_smem);
+}
+template <typename F, int KPT>
+void (*fwd_reg_kernel())(BatchDev, int, int, int) {
+    if constexpr (sizeof(F) == 8) return k_forward_reg64<KPT>;
+    else if constexpr (KPT <= 2) return k_forward_reg32<KPT>;
+    else return k_forward_reg32w<KPT>;
+}
+
 // ---------------------------------------------------------------------------------------
 // The reference's dense test step (arghmm_forward_block_slow, sample_thread.cpp:301-337),
 // FP64, one CTA per instance: every column of a local tree from the full S x S transition
@@ -1028,8 +1055,9 @@ void launch_reg(const BatchDev &d, int nt, cudaStream_t s) {
     const int t2_in_smem = bytes(maxM) <= 200 * 1024;
     if (!t2_in_smem) maxM = 1;
     const size_t smem = bytes(maxM);
-    if (!raise_dynamic_smem(k_forward_reg<F, KPT>, smem)) return;
-    k_forward_reg<F, KPT><<<d.ninst, nt, smem, s>>>(d, maxS, maxM, t2_in_smem);
+    auto kernel = fwd_reg_kernel<F, KPT>();
+    if (!raise_dynamic_smem(kernel, smem)) return;
+    kernel<<<d.ninst, nt, smem, s>>>(d, maxS, maxM, t2_in_smem);
     note_launch();
 }
 

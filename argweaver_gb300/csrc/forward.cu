@@ -408,7 +408,7 @@ constexpr int NRW = 4;                      // reduction warps of the register v
 constexpr int RBINS = (MAXT - 1 + NRW - 1) / NRW;  // time bins per reduction warp (<= 8)
 
 template <typename F, int KPT>
-__device__ __forceinline__ void forward_reg_body(BatchDev d, int maxS, int maxM, int t2_in_smem) {
+__global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int maxM, int t2_in_smem) {
     extern __shared__ double dyn_d[];
     const Tab<F> tab(d);
     const int qi = cta_instance(d);
@@ -840,33 +840,6 @@ __device__ __forceinline__ void forward_reg_body(BatchDev d, int maxS, int maxM,
     }
 }
 
-// The register variant's kernels. FP32 with 1 or 2 states a thread: at most FWD32_NREG
-// registers a thread (the body needs no more without spilling), so that per-tree kernels'
-// CTAs fit on an SM beside a forward CTA and the chains share the SMs with the per-tree work
-// of later instance groups. Otherwise up to the 512-thread bound.
-#ifndef FWD32_NREG
-#define FWD32_NREG 88
-#endif
-template <int KPT>
-__global__ void __maxnreg__(FWD32_NREG) k_forward_reg32(BatchDev d, int maxS, int maxM, int t2_in_smem) {
-    forward_reg_body<float, KPT>(d, maxS, maxM, t2_in_smem);
-}
-// 4 and 8 states a thread (large trees) keep the registers they take
-template <int KPT>
-__global__ void __launch_bounds__(512) k_forward_reg32w(BatchDev d, int maxS, int maxM, int t2_in_smem) {
-    forward_reg_body<float, KPT>(d, maxS, maxM, t2_in_smem);
-}
-template <int KPT>
-__global__ void __launch_bounds__(512) k_forward_reg64(BatchDev d, int maxS, int maxM, int t2_in_smem) {
-    forward_reg_body<double, KPT>(d, maxS, maxM, t2_in_smem);
-}
-template <typename F, int KPT>
-void (*fwd_reg_kernel())(BatchDev, int, int, int) {
-    if constexpr (sizeof(F) == 8) return k_forward_reg64<KPT>;
-    else if constexpr (KPT <= 2) return k_forward_reg32<KPT>;
-    else return k_forward_reg32w<KPT>;
-}
-
 // ---------------------------------------------------------------------------------------
 // The reference's dense test step (arghmm_forward_block_slow, sample_thread.cpp:301-337),
 // FP64, one CTA per instance: every column of a local tree from the full S x S transition
@@ -1055,9 +1028,8 @@ void launch_reg(const BatchDev &d, int nt, cudaStream_t s) {
     const int t2_in_smem = bytes(maxM) <= 200 * 1024;
     if (!t2_in_smem) maxM = 1;
     const size_t smem = bytes(maxM);
-    auto kernel = fwd_reg_kernel<F, KPT>();
-    if (!raise_dynamic_smem(kernel, smem)) return;
-    kernel<<<d.ninst, nt, smem, s>>>(d, maxS, maxM, t2_in_smem);
+    if (!raise_dynamic_smem(k_forward_reg<F, KPT>, smem)) return;
+    k_forward_reg<F, KPT><<<d.ninst, nt, smem, s>>>(d, maxS, maxM, t2_in_smem);
     note_launch();
 }
 
@@ -1074,6 +1046,19 @@ int reg_kpt(int maxS, int want) {
           : maxS <= 64 ? 1 : maxS <= 768 ? 2 : maxS <= 1536 ? 4 : 8;
     while (k < 8 && (maxS + k - 1) / k > 384) k *= 2;
     return k;
+}
+
+template <typename F, int KPT>
+bool footprint_reg(const BatchDev &d, int nt, SmReserve &r) {
+    const int maxS = imax(d.maxS, 1);
+    int maxM = imax(d.maxM, 1);
+    auto bytes = [&](int m) { return (size_t)(3 * maxS + m) * sizeof(F) + (size_t)maxS * sizeof(float) + 16; };
+    if (bytes(maxM) > 200 * 1024) maxM = 1;
+    cudaFuncAttributes a;
+    if (cudaFuncGetAttributes(&a, k_forward_reg<F, KPT>) != cudaSuccess) return false;
+    r.regs = (nt / 32) * ((a.numRegs * 32 + 255) / 256 * 256);
+    r.smem = bytes(maxM) + a.sharedSizeBytes + 1024;
+    return true;
 }
 
 template <typename F>
@@ -1105,6 +1090,19 @@ void launch_forward_dense(const BatchDev &d, cudaStream_t s) {
     const int nt = imin(512, imax(32, (maxS + 31) / 32 * 32));
     k_forward_dense<<<d.ninst, nt, smem, s>>>(d, maxS);
     note_launch();
+}
+
+bool forward_footprint(const BatchDev &d, bool fp32, int want_kpt, SmReserve &r) {
+    const int maxS = imax(d.maxS, 1);
+    const int kpt = reg_kpt(maxS, want_kpt);
+    const int nt = 32 * NRW + imax(32, ((maxS + kpt - 1) / kpt + 31) / 32 * 32);
+    if (nt > 512) return false;
+    switch (kpt) {
+        case 1: return fp32 ? footprint_reg<float, 1>(d, nt, r) : footprint_reg<double, 1>(d, nt, r);
+        case 2: return fp32 ? footprint_reg<float, 2>(d, nt, r) : footprint_reg<double, 2>(d, nt, r);
+        case 4: return fp32 ? footprint_reg<float, 4>(d, nt, r) : footprint_reg<double, 4>(d, nt, r);
+        default: return fp32 ? footprint_reg<float, 8>(d, nt, r) : footprint_reg<double, 8>(d, nt, r);
+    }
 }
 
 void launch_forward(const BatchDev &d, bool fp32, cudaStream_t s, int kpt) {

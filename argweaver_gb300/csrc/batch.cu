@@ -494,11 +494,6 @@ int ctx_launch(Ctx &C, const awg_problem *probs, awg_outputs *outs, int n, const
         }
     }
     int *qk = cfg.persistent ? queues : nullptr;
-    // room for a forward CTA beside the persistent per-tree kernels (autotuned knob)
-    SmReserve reserve;
-    const SmReserve *rsv = nullptr;
-    if (pipelined && qk && cfg.reserve && !dry && forward_footprint(d, fp32, cfg.kpt, reserve))
-        rsv = &reserve;
     auto qp = [&](int i) { return qk ? qk + i : nullptr; };
     // the device part of the step (no host synchronisation: it is also what is captured)
     auto enqueue = [&]() -> cudaError_t {
@@ -520,9 +515,9 @@ int ctx_launch(Ctx &C, const awg_problem *probs, awg_outputs *outs, int n, const
                 dg.blkmap = (const int *)(D + o_blkmap) + boff;
                 dg.nblocks = nb;
                 boff += nb;
-                launch_tables(dg, fp32, s, qp(2 * g), cfg.chunk, rsv);
+                launch_tables(dg, fp32, s, qp(2 * g), cfg.chunk);
                 EQ(cudaGetLastError());
-                launch_varemit(dg, fp32, s, qp(2 * g + 1), cfg.chunk, rsv);
+                launch_varemit(dg, fp32, s, qp(2 * g + 1), cfg.chunk);
                 EQ(cudaGetLastError());
                 cudaStream_t gs = C.gstream[g];
                 EQ(cudaEventRecord(C.gev[2 * g], s));
@@ -573,8 +568,7 @@ int ctx_launch(Ctx &C, const awg_problem *probs, awg_outputs *outs, int n, const
             std::vector<long long> sig = {(long long)(uintptr_t)D, (long long)fp32, want_path,
                                           want_post, want_bw, want_bins, plan.ninst, plan.nblocks,
                                           plan.maxS, plan.maxT, plan.maxnodes, plan.maxM,
-                                          cfg.kpt, cfg.chunk, cfg.group_div, cfg.persistent,
-                                          cfg.reserve, ng,
+                                          cfg.kpt, cfg.chunk, cfg.group_div, cfg.persistent, ng,
                                           (long long)total, d.emit64, d.vardf};
             for (size_t o : {o_inst, o_blocks, o_model, o_nodes, o_map, o_seq, o_cls, o_cvar,
                              o_order, o_blkmap, o_u, o_sinfo, o_t2off, o_btptr, o_btperm, o_tm,
@@ -970,7 +964,6 @@ int autotune(const awg_problem *probs, awg_outputs *outs, int n, int precision, 
         {&TuneCfg::group_div, {4, 8, 16}},
         {&TuneCfg::chunk, {1, 4}},
         {&TuneCfg::persistent, {1, 0}},
-        {&TuneCfg::reserve, {0, 1}},
     };
     for (const auto &k : knobs) {
         if (rc != 0) break;

@@ -16,8 +16,6 @@ struct TuneCfg {
     int chunk = 1;       // trees per work unit of the persistent per-tree kernels
     int group_div = 8;   // pipelined schedule: the largest instance group holds n / group_div
     int persistent = 1;  // per-tree kernels as persistent work-stealing kernels
-    int reserve = 0;     // pipelined schedule: persistent per-tree kernels leave room on every
-                         // SM for one forward CTA
 };
 
 struct RunOptions {

@@ -1048,19 +1048,6 @@ int reg_kpt(int maxS, int want) {
     return k;
 }
 
-template <typename F, int KPT>
-bool footprint_reg(const BatchDev &d, int nt, SmReserve &r) {
-    const int maxS = imax(d.maxS, 1);
-    int maxM = imax(d.maxM, 1);
-    auto bytes = [&](int m) { return (size_t)(3 * maxS + m) * sizeof(F) + (size_t)maxS * sizeof(float) + 16; };
-    if (bytes(maxM) > 200 * 1024) maxM = 1;
-    cudaFuncAttributes a;
-    if (cudaFuncGetAttributes(&a, k_forward_reg<F, KPT>) != cudaSuccess) return false;
-    r.regs = (nt / 32) * ((a.numRegs * 32 + 255) / 256 * 256);
-    r.smem = bytes(maxM) + a.sharedSizeBytes + 1024;
-    return true;
-}
-
 template <typename F>
 void launch(const BatchDev &d, cudaStream_t s, int want_kpt) {
     const int maxS = imax(d.maxS, 1);
@@ -1090,19 +1077,6 @@ void launch_forward_dense(const BatchDev &d, cudaStream_t s) {
     const int nt = imin(512, imax(32, (maxS + 31) / 32 * 32));
     k_forward_dense<<<d.ninst, nt, smem, s>>>(d, maxS);
     note_launch();
-}
-
-bool forward_footprint(const BatchDev &d, bool fp32, int want_kpt, SmReserve &r) {
-    const int maxS = imax(d.maxS, 1);
-    const int kpt = reg_kpt(maxS, want_kpt);
-    const int nt = 32 * NRW + imax(32, ((maxS + kpt - 1) / kpt + 31) / 32 * 32);
-    if (nt > 512) return false;
-    switch (kpt) {
-        case 1: return fp32 ? footprint_reg<float, 1>(d, nt, r) : footprint_reg<double, 1>(d, nt, r);
-        case 2: return fp32 ? footprint_reg<float, 2>(d, nt, r) : footprint_reg<double, 2>(d, nt, r);
-        case 4: return fp32 ? footprint_reg<float, 4>(d, nt, r) : footprint_reg<double, 4>(d, nt, r);
-        default: return fp32 ? footprint_reg<float, 8>(d, nt, r) : footprint_reg<double, 8>(d, nt, r);
-    }
 }
 
 void launch_forward(const BatchDev &d, bool fp32, cudaStream_t s, int kpt) {

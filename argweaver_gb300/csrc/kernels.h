@@ -13,17 +13,11 @@ namespace awg {
 // K1: per-block tables (states, transition matrix, same-branch rows, switch matrix,
 // priors into forward column 0, invariant emissions); one CTA per local tree, or with a
 // work counter (zeroed) a persistent kernel whose CTAs take units of `chunk` trees.
-// Resources of one SM a persistent per-tree kernel leaves free (a forward CTA's registers
-// and shared memory), so that a chain can start beside it; NULL: none.
-struct SmReserve {
-    int regs = 0;
-    size_t smem = 0;
-};
 void launch_tables(const BatchDev &d, bool want32, cudaStream_t s, int *queue = nullptr,
-                   int chunk = 1, const SmReserve *reserve = nullptr);
+                   int chunk = 1);
 // K2: emissions of variant columns (Felsenstein pruning); as K1.
 void launch_varemit(const BatchDev &d, bool want32, cudaStream_t s, int *queue = nullptr,
-                    int chunk = 1, const SmReserve *reserve = nullptr);
+                    int chunk = 1);
 // Whether K2's carve with FP64 per-state factors and 8-byte scratch (needed for FP64 and
 // double-float emissions) fits this largest tree.
 bool varemit_full_carve_fits(int maxnodes, int maxS);
@@ -32,10 +26,6 @@ bool varemit_full_carve_fits(int maxnodes, int maxS);
 void launch_forward(const BatchDev &d, bool fp32, cudaStream_t s, int kpt = 0);
 // K3 with the reference's dense test step (arghmm_forward_block_slow), FP64.
 void launch_forward_dense(const BatchDev &d, cudaStream_t s);
-// The SM resources one forward CTA of this batch takes (registers at the allocation
-// granularity, shared memory with the per-CTA reservation); false for the shared-memory
-// variant.
-bool forward_footprint(const BatchDev &d, bool fp32, int kpt, SmReserve &r);
 
 // The reference's dense helper matrices of one tree (or one boundary) from the table and
 // emission kernels' FP64 outputs, into out (host, row-major): DENSE_TRANSITION log P(rows[r]

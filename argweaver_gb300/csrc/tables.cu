@@ -2065,11 +2065,8 @@ size_t tables_smem(int n, int S, int S1, int T, bool want32) {
 
 // CTAs of a persistent kernel: as many as are resident on the GPU at once, at most one per
 // unit of work.
-// With a reserve, at most as many per SM as leave the reserved registers and shared memory
-// free (at least one).
 template <typename K>
-int persistent_grid(K kernel, int threads, size_t smem, int nunits,
-                    const SmReserve *reserve = nullptr) {
+int persistent_grid(K kernel, int threads, size_t smem, int nunits) {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -2077,26 +2074,10 @@ int persistent_grid(K kernel, int threads, size_t smem, int nunits,
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess || per_sm < 1)
         per_sm = 1;
-    cudaFuncAttributes a;
-    if (reserve && cudaFuncGetAttributes(&a, kernel) == cudaSuccess) {
-        int regs_sm = 0, smem_sm = 0;
-        cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
-        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
-        const int warps = (threads + 31) / 32;
-        const int regs_cta = warps * ((a.numRegs * 32 + 255) / 256 * 256);
-        const size_t smem_cta = smem + a.sharedSizeBytes + 1024;
-        int fit = regs_cta > 0 ? (regs_sm - reserve->regs) / regs_cta : per_sm;
-        if (smem_sm > (long long)reserve->smem)
-            fit = imin(fit, (int)(((size_t)smem_sm - reserve->smem) / smem_cta));
-        else
-            fit = 1;
-        per_sm = imax(1, imin(per_sm, fit));
-    }
     return imax(1, imin(nunits, per_sm * sms));
 }
 
-void launch_tables(const BatchDev &d, bool want32, cudaStream_t s, int *queue, int chunk,
-                   const SmReserve *reserve) {
+void launch_tables(const BatchDev &d, bool want32, cudaStream_t s, int *queue, int chunk) {
     size_t smem = tables_smem(d.maxnodes, d.maxS, d.maxS, d.maxT, want32);
     if (!queue) {
         prefer_shared(k_tables);
@@ -2108,7 +2089,7 @@ void launch_tables(const BatchDev &d, bool want32, cudaStream_t s, int *queue, i
         if (!raise_dynamic_smem(k_tables_ws, smem)) return;
         chunk = imax(chunk, 1);
         const WorkQueue q{queue, (d.nblocks + chunk - 1) / chunk, chunk};
-        const int grid = persistent_grid(k_tables_ws, TAB_THREADS, smem, q.nunits, reserve);
+        const int grid = persistent_grid(k_tables_ws, TAB_THREADS, smem, q.nunits);
         k_tables_ws<<<grid, TAB_THREADS, smem, s>>>(d, want32 ? 1 : 0, q);
     }
     note_launch();
@@ -2136,8 +2117,7 @@ bool varemit_full_carve_fits(int maxnodes, int maxS) {
 }
 
 template <bool FP32OUT>
-void launch_varemit_t(const BatchDev &d, cudaStream_t s, int *queue, int chunk,
-                      const SmReserve *reserve) {
+void launch_varemit_t(const BatchDev &d, cudaStream_t s, int *queue, int chunk) {
     const int n = d.maxnodes, maxS = imax(d.maxS, 1);
     const bool lean = FP32OUT && !d.emit64;
     int nwarps = 4;
@@ -2154,17 +2134,15 @@ void launch_varemit_t(const BatchDev &d, cudaStream_t s, int *queue, int chunk,
         if (!raise_dynamic_smem(k_varemit_ws<FP32OUT>, smem)) return;
         chunk = imax(chunk, 1);
         const WorkQueue q{queue, (d.nblocks + chunk - 1) / chunk, chunk};
-        const int grid =
-            persistent_grid(k_varemit_ws<FP32OUT>, nwarps * 32, smem, q.nunits, reserve);
+        const int grid = persistent_grid(k_varemit_ws<FP32OUT>, nwarps * 32, smem, q.nunits);
         k_varemit_ws<FP32OUT><<<grid, nwarps * 32, smem, s>>>(d, nwarps, maxS, (int)smem, q);
     }
     note_launch();
 }
 
-void launch_varemit(const BatchDev &d, bool fp32, cudaStream_t s, int *queue, int chunk,
-                    const SmReserve *reserve) {
-    if (fp32) launch_varemit_t<true>(d, s, queue, chunk, reserve);
-    else launch_varemit_t<false>(d, s, queue, chunk, reserve);
+void launch_varemit(const BatchDev &d, bool fp32, cudaStream_t s, int *queue, int chunk) {
+    if (fp32) launch_varemit_t<true>(d, s, queue, chunk);
+    else launch_varemit_t<false>(d, s, queue, chunk);
 }
 
 }  // namespace awg

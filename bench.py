@@ -413,10 +413,12 @@ def _c4(rng):
         sweep.append(row)
         if st["p99_ms"] > 30000:  # past saturation: the queue grows without bound
             break
-    # saturation: the highest rate whose throughput still follows the offered load
+    # saturation: the highest rate whose throughput still follows the offered load (80% of
+    # it: the measured span runs past the 8 s of arrivals by the last requests' own time, up
+    # to a few seconds for the largest, so even an idle server shows less than the offered)
     sat = None
     for row in sweep:
-        if row["throughput"] and row["throughput"] >= 0.9 * row["offered"]:
+        if row["throughput"] and row["throughput"] >= 0.8 * row["offered"]:
             sat = row
     # the plain FP64 per-request path: one arghmm_sample_posterior call per request, no
     # batching, on requests drawn from the same pool (bounded to ~6 s)

@@ -53,6 +53,7 @@ template <> struct Tab<double> {
           crow(d.recoalrow), gts(d.gts), fw(d.fw64) {}
     // tmatrix2[a][k] (sample_thread.cpp:223-224)
     __device__ double t2(long long idx, double tmab) const { return gts[idx] - tmab; }
+    __device__ const double *t2rows() const { return gts; }
 };
 
 template <> struct Tab<float> {
@@ -66,7 +67,45 @@ template <> struct Tab<float> {
           crow(d.recoalrow32), t2d(d.t2d32), rstay(d.rstay32), lneref(d.lneref), vref(d.vref),
           fw(d.fw32) {}
     __device__ float t2(long long idx, float) const { return t2d[idx]; }
+    __device__ const float *t2rows() const { return t2d; }
 };
+
+// A hint that moves [p, p + bytes) (the whole 16-byte granules inside it) from HBM into L2
+// (cp.async.bulk.prefetch.L2): no result, no fault, no effect on any value.
+__device__ __forceinline__ void l2_prefetch(const void *p, size_t bytes) {
+    const uintptr_t a = ((uintptr_t)p + 15) & ~(uintptr_t)15;
+    const uintptr_t e = ((uintptr_t)p + bytes) & ~(uintptr_t)15;
+    if (e > a)
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a), "r"((unsigned)(e - a))
+                     : "memory");
+}
+
+// The tables a tree's staging and columns read (the register kernel's per-tree staging:
+// state metadata, tmatrix, same-branch rows, invariant emissions, time bins, the switch
+// column's gather lists and rows; then its column classes and variant emission rows), for
+// tree blk of instance I, prefetched into L2 while the tree before it runs: its staging then
+// waits on L2 instead of HBM.
+template <typename F>
+__device__ __forceinline__ void prefetch_tree(const BatchDev &d, const Tab<F> &tab, const InstDev &I,
+                                              int blk) {
+    const BlockDev &N = d.blocks[blk];
+    const size_t S = (size_t)imax(N.S, 1), S1 = (size_t)imax(N.S1, 1);
+    l2_prefetch(d.sinfo + N.state0, sizeof(StateInfo) * S);
+    l2_prefetch(d.t2off + N.state0, sizeof(int) * S);
+    l2_prefetch(d.bt_perm + N.state0, sizeof(int) * S);
+    l2_prefetch(tab.inv + N.state0, sizeof(F) * S);
+    l2_prefetch(tab.rrow + N.state0, sizeof(F) * S);
+    l2_prefetch(tab.crow + N.state0, sizeof(F) * S);
+    l2_prefetch(tab.tm + (size_t)blk * MAXT * MAXT, sizeof(F) * MAXT * MAXT);
+    l2_prefetch(d.bt_ptr + (size_t)blk * (MAXT + 1), sizeof(int) * (MAXT + 1));
+    l2_prefetch(d.gptr + N.gptr0, sizeof(int) * (S + 1));
+    l2_prefetch(d.gidx + N.prev_state0, sizeof(int) * S1);
+    l2_prefetch(d.determprob + N.prev_state0, sizeof(double) * S1);
+    l2_prefetch(d.colclass + I.col0 + N.start, (size_t)N.len);
+    l2_prefetch(d.colvar + I.col0 + N.start, sizeof(int) * N.len);
+    if (N.M > 0) l2_prefetch(tab.t2rows() + N.t2_0, sizeof(F) * N.M);
+    if (N.nvar > 0 && N.S > 0) l2_prefetch(tab.var + N.var0, sizeof(F) * N.nvar * (size_t)N.S);
+}
 
 template <typename F>
 __device__ __forceinline__ F warp_sum(F v) {
@@ -438,6 +477,7 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
         const BlockDev &B = d.blocks[blk];
         const int S = B.S, len = B.len;
         F *fw = tab.fw + B.cell0;
+        if (tid == NT - 32 && bi + 1 < I.ntrees) prefetch_tree<F>(d, tab, I, blk + 1);
 
         if (S == 0) {
             // fully specified tree: one state that carries over (sample_thread.cpp:201-206)

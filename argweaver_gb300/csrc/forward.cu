@@ -469,7 +469,14 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
     __shared__ int bptr[MAXT + 1];
     __shared__ int fbin[NRW][32];              // reducers: first bin of each lane's chunk
 
-    LogAcc acc;
+    // the log-likelihood accumulates on one thread of reduction warp 1: after barrier B its
+    // warp has nothing else to do before barrier A, so the FP64 frexp, product and periodic
+    // log stay off the column's critical path (on warp 0 they delayed barrier A by about a
+    // fifth of a column). Thread 0 keeps a second accumulator for the rare switch into a
+    // fully specified tree; the two are summed at the end.
+    LogAcc acc, acc0;
+    const bool acc_thread = tid == 32;
+    __shared__ double lnl0;
     int c = 0;                                 // buffer holding the current column
 
     for (int bi = 0; bi < I.ntrees; bi++) {
@@ -500,7 +507,7 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
                 if (tid == 0) {
                     if (src.x != -1 && rr[0] > F(0)) sum += col[c * maxS + src.x] * rr[0];
                     if (src.y != -1 && cr[0] > F(0)) sum += col[c * maxS + src.y] * cr[0];
-                    acc.add((double)sum);
+                    acc0.add((double)sum);
                     col[c * maxS] = F(1);
                     fw[0] = F(1);
                 }
@@ -599,7 +606,7 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
         const int *cvar = d.colvar + I.col0 + B.start;
         const F *var = tab.var + B.var0;
         // FP32: the tree's emission references, added once the tree is done
-        const double blkx = Tab<F>::split && tid == 0 ? d.blkext[blk] : 0.0;
+        const double blkx = Tab<F>::split && acc_thread ? d.blkext[blk] : 0.0;
         // column classes and variant rows, 32 columns per lane-window; the next window is
         // loaded when the current one is entered, so its loads overlap 32 columns of work
         int ccache, vcache, ncc, nvc, cbase = 0;
@@ -804,7 +811,7 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
 #pragma unroll
             for (int r = 0; r < NRW; r++) norm += tfp[r][MAXT - 1];
             const F inv_norm = F(1) / norm;
-            if (tid == 0) {
+            if (acc_thread) {
                 acc.add((double)norm);
                 if (!(norm > F(0))) report_error(d.err, ERR_ZERO_NORM, qi, bi, B.start + i - 1);
             }
@@ -871,12 +878,17 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
             }
             c ^= 1;
         }
-        if (Tab<F>::split && tid == 0) acc.extra += blkx;
+        if (Tab<F>::split && acc_thread) acc.extra += blkx;
         __syncthreads();
     }
-    if (tid == 0 && d.lnl) {
+    if (tid == 0) {
+        acc0.flush();
+        lnl0 = acc0.lnl;
+    }
+    __syncthreads();
+    if (acc_thread && d.lnl) {
         acc.flush();
-        d.lnl[qi] = acc.lnl;
+        d.lnl[qi] = acc.lnl + lnl0;
     }
 }
 

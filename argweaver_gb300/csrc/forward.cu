@@ -607,6 +607,12 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
         const F *var = tab.var + B.var0;
         // FP32: the tree's emission references, added once the tree is done
         const double blkx = Tab<F>::split && acc_thread ? d.blkext[blk] : 0.0;
+        // reducers: the tree's rows of the stored time-bin sums (the address formed once per
+        // tree: a per-column read of the tree's descriptor from global memory sat on the
+        // reducers' path to barrier A)
+        float *const bins_row = Tab<F>::split && reducer && d.bins32
+                                    ? d.bins32 + (size_t)(I.col0 + B.start) * MAXT
+                                    : nullptr;
         // column classes and variant rows, 32 columns per lane-window; the next window is
         // loaded when the current one is entered, so its loads overlap 32 columns of work
         int ccache, vcache, ncc, nvc, cbase = 0;
@@ -820,9 +826,8 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
             const bool write_prev = !(bi == 0 && i == 1);
             if constexpr (Tab<F>::split) {
                 // the stored column's time-bin sums, on the stored column's scale
-                if (reducer && d.bins32 && blo + lane < bhi)
-                    d.bins32[(size_t)(I.col0 + B.start + i - 1) * MAXT + blo + lane] =
-                        write_prev ? binv * inv_norm : binv;
+                if (bins_row && blo + lane < bhi)
+                    bins_row[(size_t)(i - 1) * MAXT + blo + lane] = write_prev ? binv * inv_norm : binv;
             }
             F *outp = fw + (size_t)(i - 1) * S;
             if (i == len) {

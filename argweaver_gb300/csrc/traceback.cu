@@ -285,6 +285,38 @@ __global__ void k_traceback(BatchDev d, int maxS, int slot_elems) {
 #pragma unroll
             for (int g = 0; g < G; g++)
                 if (shi[g] > slo[g]) open |= 1u << g;
+            if (chunk <= 16) {
+                // short chunks: lane g rescans column g's chosen chunk in order, one product
+                // and one add per state, the G columns side by side (a 32-lane scan per column
+                // costs five warp-wide adds however few states the chunk holds: on the FP64
+                // path each holds the sub-partition's FP64 pipe for about 64 cycles)
+                int mine = 0;
+                if (lane < G) {
+                    F mpick = 0, run = 0;
+                    int mslo = 0, mshi = 0;
+                    const F *mc = cg[0];
+#pragma unroll
+                    for (int g = 0; g < G; g++)
+                        if (lane == g) {
+                            mpick = pick[g];
+                            run = carry[g];
+                            mslo = slo[g];
+                            mshi = (open >> g) & 1 ? shi[g] : slo[g];
+                            mine = res[g];
+                            mc = cg[g];
+                        }
+                    for (int jj = mslo; jj < mshi; jj++) {
+                        run += mc[jj] * trans[jj];
+                        if (run >= mpick) {
+                            mine = jj;
+                            break;
+                        }
+                    }
+                }
+#pragma unroll
+                for (int g = 0; g < G; g++) res[g] = __shfl_sync(0xffffffffu, mine, g);
+                open = 0;
+            }
             for (int b = 0; open; b += 32) {
                 F x[G];
 #pragma unroll

@@ -727,43 +727,52 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
             const F *cur = col + c * maxS;
             F binv = F(0);  // reducers, lane b - blo: bin b of column i-1
             if (reducer) {
-                // chunk sums by bin (positions sorted by time)
-                if (fast_chunk) {
-                    // eight loads at a time; three independent sums over the chunk's bin ranges
-                    F a0 = 0, a1 = 0, a2 = 0;
-                    const int len_c = chi - clo;
-                    for (int j0 = 0; j0 < len_c; j0 += 8) {
-                        F v[8];
-#pragma unroll
-                        for (int j = 0; j < 8; j++) v[j] = j0 + j < len_c ? colT[clo + j0 + j] : F(0);
-#pragma unroll
-                        for (int j = 0; j < 8; j++) {
-                            const int jj = j0 + j;
-                            a0 += jj < o1 ? v[j] : F(0);
-                            a1 += (jj >= o1 && jj < o2) ? v[j] : F(0);
-                            a2 += jj >= o2 ? v[j] : F(0);
-                        }
-                    }
-                    if (nbc >= 1) part[rw][lane][0] = a0;
-                    if (nbc >= 2) part[rw][lane][1] = a1;
-                    if (nbc >= 3) part[rw][lane][2] = a2;
-                } else {
-                    int bcur = fbin[rw][lane], j = 0, nextb = bptr[bcur + 1];
-                    F a = 0;
-                    for (int p = clo; p < chi; p++) {
-                        while (p >= nextb) {
-                            part[rw][lane][j++] = a;
-                            a = F(0);
-                            bcur++;
-                            nextb = bptr[bcur + 1];
-                        }
-                        a += colT[p];
-                    }
-                    if (chi > clo) part[rw][lane][j] = a;
-                }
-                __syncwarp();
                 F bin = 0;  // lane b - blo: bin b
-                for (int l = l0; l <= l1; l++) bin += part[rw][l][blo + lane - fbin[rw][l]];
+                if (sizeof(F) == 8 && chunk == 1) {
+                    // FP64, one position per lane: each bin's positions summed in order
+                    // directly, the additions the chunk partials and their gather make,
+                    // without the partials' round trip through shared memory
+                    const int b = blo + lane;
+                    if (b < bhi)
+                        for (int p = bptr[b]; p < bptr[b + 1]; p++) bin += colT[p];
+                } else {
+                    // chunk sums by bin (positions sorted by time)
+                    if (fast_chunk) {
+                        // eight loads at a time; three independent sums over the chunk's bin ranges
+                        F a0 = 0, a1 = 0, a2 = 0;
+                        const int len_c = chi - clo;
+                        for (int j0 = 0; j0 < len_c; j0 += 8) {
+                            F v[8];
+#pragma unroll
+                            for (int j = 0; j < 8; j++) v[j] = j0 + j < len_c ? colT[clo + j0 + j] : F(0);
+#pragma unroll
+                            for (int j = 0; j < 8; j++) {
+                                const int jj = j0 + j;
+                                a0 += jj < o1 ? v[j] : F(0);
+                                a1 += (jj >= o1 && jj < o2) ? v[j] : F(0);
+                                a2 += jj >= o2 ? v[j] : F(0);
+                            }
+                        }
+                        if (nbc >= 1) part[rw][lane][0] = a0;
+                        if (nbc >= 2) part[rw][lane][1] = a1;
+                        if (nbc >= 3) part[rw][lane][2] = a2;
+                    } else {
+                        int bcur = fbin[rw][lane], j = 0, nextb = bptr[bcur + 1];
+                        F a = 0;
+                        for (int p = clo; p < chi; p++) {
+                            while (p >= nextb) {
+                                part[rw][lane][j++] = a;
+                                a = F(0);
+                                bcur++;
+                                nextb = bptr[bcur + 1];
+                            }
+                            a += colT[p];
+                        }
+                        if (chi > clo) part[rw][lane][j] = a;
+                    }
+                    __syncwarp();
+                    for (int l = l0; l <= l1; l++) bin += part[rw][l][blo + lane - fbin[rw][l]];
+                }
                 binv = bin;
                 // this warp's share of tf[a] = sum_b tm[b][a] bin[b], its bins in order
                 F tf = 0;
@@ -813,10 +822,16 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
                 }
             }
             __syncthreads();  // B: tf and the norm of column i-1
-            F norm = 0;
+            // the column's norm and its reciprocal where they are used: the owners, the
+            // accumulator thread and (FP32) the reducers storing bin sums; on the FP64 path
+            // the other reduction warps skip them, whose division held the FP64 pipe of the
+            // sub-partitions the owners share
+            F norm = 0, inv_norm = 0;
+            if (!reducer || acc_thread || Tab<F>::split) {
 #pragma unroll
-            for (int r = 0; r < NRW; r++) norm += tfp[r][MAXT - 1];
-            const F inv_norm = F(1) / norm;
+                for (int r = 0; r < NRW; r++) norm += tfp[r][MAXT - 1];
+                inv_norm = F(1) / norm;
+            }
             if (acc_thread) {
                 acc.add((double)norm);
                 if (!(norm > F(0))) report_error(d.err, ERR_ZERO_NORM, qi, bi, B.start + i - 1);

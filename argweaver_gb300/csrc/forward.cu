@@ -771,7 +771,17 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
                         if (chi > clo) part[rw][lane][j] = a;
                     }
                     __syncwarp();
-                    for (int l = l0; l <= l1; l++) bin += part[rw][l][blo + lane - fbin[rw][l]];
+                    // the chunk partials of bin b, eight loads issued together, then added in
+                    // order (the same additions as one at a time; the partials are >= 0, so
+                    // the zeros past l1 change nothing)
+                    for (int l = l0; l <= l1; l += 8) {
+                        F v[8];
+#pragma unroll
+                        for (int t = 0; t < 8; t++)
+                            v[t] = l + t <= l1 ? part[rw][l + t][blo + lane - fbin[rw][l + t]] : F(0);
+#pragma unroll
+                        for (int t = 0; t < 8; t++) bin += v[t];
+                    }
                 }
                 binv = bin;
                 // this warp's share of tf[a] = sum_b tm[b][a] bin[b], its bins in order

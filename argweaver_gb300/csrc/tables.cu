@@ -1184,7 +1184,17 @@ __device__ __forceinline__ df operator*(df a, df b) {
 }
 __device__ __forceinline__ df &operator+=(df &a, df b) { return a = a + b; }
 __device__ __forceinline__ bool operator<(df a, df b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
-__device__ __forceinline__ df fma(df a, df b, df c) { return a * b + c; }
+// a + b for a, b >= 0 (every sum of the emission passes: partials, branch probabilities and
+// their products): the larger high part first makes Dekker's fast two-sum exact, three adds
+// where the two-sum of arbitrary signs takes six
+__device__ __forceinline__ df df_addp(df a, df b) {
+    const float big = fmaxf(a.hi, b.hi), small = fminf(a.hi, b.hi);
+    const float s = __fadd_rn(big, small);
+    const float e = __fsub_rn(small, __fsub_rn(s, big));
+    return df_fast2(s, __fadd_rn(e, __fadd_rn(a.lo, b.lo)));
+}
+// a * b + c, a, b, c >= 0 (the JC69 steps of the emission passes)
+__device__ __forceinline__ df fma(df a, df b, df c) { return df_addp(a * b, c); }
 __device__ __forceinline__ df fmax(df a, df b) { return a < b ? b : a; }
 __device__ __forceinline__ df __shfl_xor_sync(unsigned mask, df v, int o) {
     return df(::__shfl_xor_sync(mask, v.hi, o), ::__shfl_xor_sync(mask, v.lo, o));
@@ -1511,9 +1521,9 @@ __device__ df emit_near_df(const EmitCtx &c, const uint8_t *chars, int X, df (*i
     const int4 *nd = c.nd;
     // JC69 over a branch with m (to each other base), nm (no change)
     auto step = [](const df *x, df m, df nm, df *y) {
-        const df dd = nm - m, ms = m * (x[0] + df(3.0f, 0.0f) * x[1]);
-        y[0] = dd * x[0] + ms;
-        y[1] = dd * x[1] + ms;
+        const df dd = nm - m, ms = m * df_addp(x[0], df(3.0f, 0.0f) * x[1]);
+        y[0] = df_addp(dd * x[0], ms);
+        y[1] = df_addp(dd * x[1], ms);
     };
     auto leaf = [](uint8_t ch, df *v) {  // observed calls are X here
         v[0] = df(1.0f, 0.0f);
@@ -1579,7 +1589,7 @@ __device__ df emit_near_df(const EmitCtx &c, const uint8_t *chars, int X, df (*i
             t[0] = p2[0];
             t[1] = p2[1];
         }
-        return p1[0] * t[0] + df(3.0f, 0.0f) * (p1[1] * t[1]);
+        return df_addp(p1[0] * t[0], df(3.0f, 0.0f) * (p1[1] * t[1]));
     };
     // two states per lane at a time: independent chains the scheduler can interleave (the
     // second one repeats the last state where it would run past S)

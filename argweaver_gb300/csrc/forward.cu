@@ -107,21 +107,6 @@ __device__ __forceinline__ void prefetch_tree(const BatchDev &d, const Tab<F> &t
     if (N.nvar > 0 && N.S > 0) l2_prefetch(tab.var + N.var0, sizeof(F) * N.nvar * (size_t)N.S);
 }
 
-// 1 / x. FP64 (x within FP32's normal range): Newton-Raphson from the FP32 reciprocal,
-// r <- r + r (1 - x r) twice (24 -> 48 -> full-precision bits), six FP64-pipe operations
-// where the division takes about twice as many: on GB300 each holds the sub-partition's
-// FP64 pipe for about 64 cycles, in every warp that forms the column's scale. The result
-// is within an ulp of the division's. Otherwise the division.
-template <typename F>
-__device__ __forceinline__ F recip(F x) { return F(1) / x; }
-template <>
-__device__ __forceinline__ double recip<double>(double x) {
-    if (!(x > 1e-30 && x < 1e30)) return 1.0 / x;
-    double r = (double)__frcp_rn((float)x);
-    r = fma(r, fma(-x, r, 1.0), r);
-    return fma(r, fma(-x, r, 1.0), r);
-}
-
 template <typename F>
 __device__ __forceinline__ F warp_sum(F v) {
 #pragma unroll
@@ -855,7 +840,7 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
             if (!reducer || acc_thread || Tab<F>::split) {
 #pragma unroll
                 for (int r = 0; r < NRW; r++) norm += tfp[r][MAXT - 1];
-                inv_norm = recip(norm);
+                inv_norm = F(1) / norm;
             }
             if (acc_thread) {
                 acc.add((double)norm);

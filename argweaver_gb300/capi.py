@@ -157,7 +157,8 @@ EXTRA = [
     ("awg_last_timings", None, [c_double_p]),
 ]
 class AwgServerOptions(C.Structure):
-    _fields_ = [("device_bytes", C.c_size_t), ("max_inflight", C.c_int), ("max_batch", C.c_int)]
+    _fields_ = [("device_bytes", C.c_size_t), ("max_inflight", C.c_int), ("max_batch", C.c_int),
+                ("length_ratio", C.c_double)]
 
 
 class AwgServerStats(C.Structure):

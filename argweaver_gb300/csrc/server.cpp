@@ -3,8 +3,9 @@
 //
 // Requests arrive through awg_server_submit from any thread and wait in a FIFO queue. A
 // worker thread forms batches ("waves") led by the oldest request — with it, queued requests
-// of one precision, one set of wanted outputs and a like number of columns (a batch lasts as
-// long as its longest chain), as many as fit the free device memory and max_batch — and
+// of one precision, one set of wanted outputs and a like number of columns (within the
+// options' length_ratio: a batch lasts as long as its longest chain), as many as fit the
+// free device memory and max_batch — and
 // launches each on an execution context of its own (streams, staging, a region of the
 // server's device pool) and a thread of its own that plans, launches and completes it. Up
 // to max_inflight waves are on the GPU at once, so requests that
@@ -241,8 +242,10 @@ void serve(awg_server *S) {
             }
             // the oldest request, then queued requests of like length: a batch lasts as long
             // as its longest chain of columns, so short requests ride with short ones and
-            // are not held back by long ones (length within a factor of two of the head's)
+            // are not held back by long ones (length within the options' factor of the
+            // head's, 2 by default)
             const size_t avail = S->pool.largest();
+            const double ratio = S->opt.length_ratio > 1.0 ? S->opt.length_ratio : 2.0;
             std::vector<Req *> wave;
             std::vector<size_t> taken;
             size_t bytes = 0;
@@ -255,7 +258,7 @@ void serve(awg_server *S) {
                     if (r->resident || r->precision != first->precision ||
                         r->want_path != first->want_path || r->want_post != first->want_post)
                         continue;
-                    if (2LL * r->p.seqlen < L0 || r->p.seqlen > 2LL * L0) continue;
+                    if (ratio * r->p.seqlen < (double)L0 || r->p.seqlen > ratio * L0) continue;
                 }
                 if (bytes + (size_t)r->bytes > avail) {
                     if (wave.empty()) break;

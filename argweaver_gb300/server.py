@@ -32,9 +32,11 @@ class Ticket:
 
 
 class Server:
-    def __init__(self, device_bytes: int = 8 << 30, max_inflight: int = 4, max_batch: int = 32):
+    def __init__(self, device_bytes: int = 8 << 30, max_inflight: int = 4, max_batch: int = 32,
+                 length_ratio: float = 2.0):
         self._lib = capi.load()
-        opt = capi.AwgServerOptions(int(device_bytes), int(max_inflight), int(max_batch))
+        opt = capi.AwgServerOptions(int(device_bytes), int(max_inflight), int(max_batch),
+                                    float(length_ratio))
         self._h = self._lib.awg_server_create(C.byref(opt))
         if not self._h:
             raise GpuError(self._err())

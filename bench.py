@@ -353,7 +353,7 @@ def _c3(rng):
         "graph_replays": api.graph_counts()["replays"] - g0["replays"]}
 
 
-def _serve_once(pool, rate, duration, rng, max_inflight=24, max_batch=32):
+def _serve_once(pool, rate, duration, rng, max_inflight=24, max_batch=32, length_ratio=2.0):
     """Poisson arrivals at `rate` requests/s for `duration` s, requests drawn from `pool`
     with fresh uniforms, FP32, through the serving loop; the server's statistics."""
     from argweaver_gb300.server import Server
@@ -362,7 +362,8 @@ def _serve_once(pool, rate, duration, rng, max_inflight=24, max_batch=32):
     arrivals = arrivals[arrivals < duration]
     picks = rng.integers(0, len(pool), size=arrivals.size)
     unis = [np.random.default_rng(1000 + q).random(pool[j].seqlen) for q, j in enumerate(picks)]
-    with Server(device_bytes=96 << 30, max_inflight=max_inflight, max_batch=max_batch) as srv, \
+    with Server(device_bytes=96 << 30, max_inflight=max_inflight, max_batch=max_batch,
+                length_ratio=length_ratio) as srv, \
             cf.ThreadPoolExecutor(max_workers=8) as clients:
         t_start = time.perf_counter()
         futs = []

@@ -457,6 +457,9 @@ typedef struct {
     size_t device_bytes;  /* device pool for batches in flight (and resident requests) */
     int max_inflight;     /* batches on the GPU at once */
     int max_batch;        /* problems per batch */
+    double length_ratio;  /* a batch's requests have column counts within this factor of its
+                             oldest request's (a batch lasts as long as its longest chain);
+                             <= 1, e.g. 0 from a zeroed struct: 2 */
 } awg_server_options;
 typedef struct {
     long long submitted, completed, failed, cells;  /* cells: forward cells of completed */

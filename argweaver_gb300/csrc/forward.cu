@@ -478,6 +478,17 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
     const bool acc_thread = tid == 32;
     __shared__ double lnl0;
     int c = 0;                                 // buffer holding the current column
+    // FP64: a column is computed from the previous one scaled by a power of two (the
+    // exponent of its largest norm partial: exact, no division on the column's path) rather
+    // than divided by its norm. Reduction warp NRW-1 (its own sub-partition where the owners
+    // fill at most three warps) divides one column later: it keeps the partials of column
+    // i-1 in fnp and, after barrier A of column i+1, writes column i-1 normalised into the
+    // table. A tree's last column is normalised exactly for the switch, as before.
+    constexpr bool pow2 = !Tab<F>::split;
+    const bool finalizer = reducer && rw == NRW - 1;
+    F fnp[NRW];
+#pragma unroll
+    for (int r = 0; r < NRW; r++) fnp[r] = F(0);
 
     for (int bi = 0; bi < I.ntrees; bi++) {
         const int blk = I.block0 + bi;
@@ -792,6 +803,20 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
                     if (blo + j < bhi) tf = fma(tmS[(blo + j) * MAXT + lane], g, tf);
                 }
                 tfp[rw][lane] = tf;
+                if (pow2 && finalizer && i >= 2) {
+                    // column i-2 (the other column buffer) normalised into the table
+                    F nrm = fnp[0];
+#pragma unroll
+                    for (int r = 1; r < NRW; r++) nrm += fnp[r];
+                    const F inv = F(1) / nrm;
+                    if (lane == 0 && !(nrm > F(0)))
+                        report_error(d.err, ERR_ZERO_NORM, qi, bi, B.start + i - 2);
+                    if (!(bi == 0 && i == 2)) {
+                        const F *x = col + (c ^ 1) * maxS;
+                        F *o = fw + (size_t)(i - 2) * S;
+                        for (int k = lane; k < S; k += 32) o[k] = x[k] * inv;
+                    }
+                }
             } else {
                 // same-branch dot of the owned states: sum_y tmatrix2[a_y][k] col[j1 + y]
 #pragma unroll
@@ -836,15 +861,35 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
             // accumulator thread and (FP32) the reducers storing bin sums; on the FP64 path
             // the other reduction warps skip them, whose division held the FP64 pipe of the
             // sub-partitions the owners share
-            F norm = 0, inv_norm = 0;
-            if (!reducer || acc_thread || Tab<F>::split) {
+            F norm = 0, inv_norm = 0, scale = 0;
+            if (!pow2 || i == len) {
+                if (!reducer || acc_thread || Tab<F>::split) {
+                    norm = tfp[0][MAXT - 1];
 #pragma unroll
-                for (int r = 0; r < NRW; r++) norm += tfp[r][MAXT - 1];
-                inv_norm = F(1) / norm;
-            }
-            if (acc_thread) {
-                acc.add((double)norm);
-                if (!(norm > F(0))) report_error(d.err, ERR_ZERO_NORM, qi, bi, B.start + i - 1);
+                    for (int r = 1; r < NRW; r++) norm += tfp[r][MAXT - 1];
+                    inv_norm = F(1) / norm;
+                }
+                if (acc_thread) {
+                    acc.add((double)norm);
+                    if (!(norm > F(0))) report_error(d.err, ERR_ZERO_NORM, qi, bi, B.start + i - 1);
+                }
+            } else if constexpr (pow2) {
+                // 2^(1023 - E), E the largest biased exponent of the partials: the scaled
+                // column sums to [1, 8). The tree's log-likelihood is log(norm of its last
+                // column) plus ln 2 times the sum of E - 1023 over its other columns
+                // (column i's norm is the reference's norm times the scaled sum of column
+                // i-1, so the sum of the reference's log norms telescopes).
+                int E = 1;
+#pragma unroll
+                for (int r = 0; r < NRW; r++)
+                    E = imax(E, (__double2hiint((double)tfp[r][MAXT - 1]) >> 20) & 0x7ff);
+                E = imin(E, 2045);
+                scale = (F)__hiloint2double((2046 - E) << 20, 0);
+                if (acc_thread) acc.e += E - 1023;
+                if (finalizer) {
+#pragma unroll
+                    for (int r = 0; r < NRW; r++) fnp[r] = tfp[r][MAXT - 1];
+                }
             }
             // finalise column i-1: normalised into the table (the instance's column 0
             // keeps the unnormalised prior, as the reference's table does)
@@ -881,10 +926,10 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
                     const int k = owned(q);
                     if (!valid(k)) continue;
                     const F xk = x_own[q];
-                    if (write_prev) outp[k] = xk * inv_norm;
-                    F tfk = 0;
+                    if (!pow2 && write_prev) outp[k] = xk * inv_norm;
+                    F tfk = tfp[0][st_time[q]];
 #pragma unroll
-                    for (int r = 0; r < NRW; r++) tfk += tfp[r][st_time[q]];
+                    for (int r = 1; r < NRW; r++) tfk += tfp[r][st_time[q]];
                     const F sv = tfk + dq[q];
                     F v;
                     if constexpr (Tab<F>::split) {
@@ -898,7 +943,7 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
                         v = x.hi;
                         x_lo[q] = x.lo;
                     } else {
-                        v = emit(sv, ci, vrow, q, true) * inv_norm;
+                        v = emit(sv, ci, vrow, q, true) * scale;
                     }
                     nxt[k] = v;
                     colT[st_rank[q]] = v;

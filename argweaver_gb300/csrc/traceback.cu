@@ -123,7 +123,18 @@ __device__ int warp_sample(int n, double u, W w) {
     return finish_sample<F>(n, chunk, incl, (F)u * total, lo, hi, lane, w);
 }
 
-template <typename F, int G, int DEPTH>
+// QL: four lanes per column (G = 8): lane 4g + q runs quarter q of column g's states in
+// order, keeping each running sum in shared memory, so that a column's draw needs a 4-lane
+// scan and a binary search of the stored sums instead of a 32-lane scan and a rescan; the
+// fewer warp-wide FP64 instructions suit the FP64 path, whose every warp instruction holds
+// the sub-partition's FP64 pipe for about 64 cycles. For trees of up to QL_MAXS states.
+constexpr int QL_MAXS = 256;
+
+// The order of non-negative values as integers (their bit patterns order the same way).
+__device__ __forceinline__ long long order_key(double x) { return __double_as_longlong(x); }
+__device__ __forceinline__ long long order_key(float x) { return __float_as_int(x); }
+
+template <typename F, int G, int DEPTH, bool QL>
 __global__ void k_traceback(BatchDev d, int maxS, int slot_elems) {
     extern __shared__ double dyn_d[];
     F *ring = (F *)dyn_d;                                   // [DEPTH][slot_elems], 16-B slots
@@ -131,6 +142,8 @@ __global__ void k_traceback(BatchDev d, int maxS, int slot_elems) {
     F *trans = (F *)(uring + DEPTH);                        // [maxS]
     int *stime = (int *)(trans + maxS + (maxS & 1));        // [maxS] state times of the tree
     int *snode = stime + maxS;                              // [maxS]
+    // QL: [G][maxS + 1] running sums (after the ints, 8-byte aligned)
+    F *pre = (F *)((char *)dyn_d + (((char *)(snode + maxS) - (char *)dyn_d + 15) & ~(size_t)15));
     __shared__ F tmS[MAXT * MAXT];
     const TTab<F> tab(d);
     const int qi = cta_instance(d);
@@ -236,6 +249,57 @@ __global__ void k_traceback(BatchDev d, int maxS, int slot_elems) {
             const F *cg[G];
 #pragma unroll
             for (int g = 0; g < G; g++) cg[g] = column(B, c0 - imin(g, ng - 1));
+            int res[G];
+            if constexpr (QL) {
+                static_assert(G == 8, "four lanes per column of eight");
+                const int g = lane >> 2, q = lane & 3;
+                const int qs = (Sm + 3) >> 2;
+                const int qlo = imin(q * qs, Sm), qhi = imin(qlo + qs, Sm);
+                const int mycol = c0 - imin(g, ng - 1);
+                const F *cp = column(B, mycol);
+                F *pg = pre + g * (maxS + 1);
+                F run = 0;
+                for (int j = qlo; j < qhi; j++) {
+                    run = fma(cp[j], trans[j], run);
+                    pg[j] = run;
+                }
+                // inclusive scan of the quarters' sums within the column's four lanes
+                F incl = run;
+                F v = __shfl_up_sync(0xffffffffu, incl, 1);
+                if (q >= 1) incl += v;
+                v = __shfl_up_sync(0xffffffffu, incl, 2);
+                if (q >= 2) incl += v;
+                F excl = __shfl_up_sync(0xffffffffu, incl, 1);
+                if (q == 0) excl = 0;
+                const F total = __shfl_sync(0xffffffffu, incl, lane | 3);
+                const F pick = (F)uring[mycol % DEPTH] * total;
+                const unsigned hit = __ballot_sync(0xffffffffu, incl >= pick && qhi > qlo);
+                __syncwarp();  // the running sums are stored
+                int mine = Sm - 1;
+                const unsigned gh = (hit >> (4 * g)) & 15u;
+                if (gh && q == __ffs(gh) - 1) {
+                    // the first state whose running sum reaches the pick: stored sum >=
+                    // pick - (the sums of the quarters before); none (rounding): the
+                    // quarter's last state
+                    const long long key = order_key(pick - excl);
+                    int a = qlo, b = qhi - 1;
+                    if (order_key(pg[b]) >= key) {
+                        while (a < b) {
+                            const int mid = (a + b) >> 1;
+                            if (order_key(pg[mid]) >= key) b = mid;
+                            else a = mid + 1;
+                        }
+                    }
+                    mine = b;
+                }
+#pragma unroll
+                for (int gg = 0; gg < G; gg++) {
+                    const unsigned hq = (hit >> (4 * gg)) & 15u;
+                    const int src = hq ? 4 * gg + __ffs(hq) - 1 : 4 * gg;
+                    const int r = __shfl_sync(0xffffffffu, mine, src);
+                    res[gg] = hq ? r : Sm - 1;
+                }
+            } else {
             // every column's chunk sums under the current row, as warp_sample forms them
             F l0[G], l1[G];
 #pragma unroll
@@ -267,7 +331,7 @@ __global__ void k_traceback(BatchDev d, int maxS, int slot_elems) {
             }
             // every column's draw, all G interleaved (finish_sample's steps, column-wise)
             F pick[G], carry[G];
-            int slo[G], shi[G], res[G];
+            int slo[G], shi[G];
 #pragma unroll
             for (int g = 0; g < G; g++) {
                 F excl = __shfl_up_sync(0xffffffffu, incl[g], 1);
@@ -346,6 +410,7 @@ __global__ void k_traceback(BatchDev d, int maxS, int slot_elems) {
                         if (slo[g] + b + 32 >= shi[g]) open &= ~(1u << g);
                     }
                 }
+            }
             }
             // keep the draws in column order up to the first that leaves the current state
             int r = 0, x = state;
@@ -901,16 +966,18 @@ bool launch_split(const BatchDev &d, cudaStream_t s, size_t budget) {
     return true;
 }
 
-template <typename F, int G, int DEPTH>
+template <typename F, int G, int DEPTH, bool QL = false>
 bool launch_cfg(const BatchDev &d, cudaStream_t s, size_t budget) {
     const int maxS = imax(d.maxS, 1);
+    if (QL && maxS > QL_MAXS) return false;
     const int slot_elems = (int)(((size_t)maxS * sizeof(F) + 32 + 15) / 16 * 16 / sizeof(F));
-    const size_t smem = (size_t)DEPTH * slot_elems * sizeof(F) + DEPTH * sizeof(double) +
-                        (size_t)(maxS + 1) * sizeof(F) + 2 * (size_t)maxS * sizeof(int) + 16;
+    size_t smem = (size_t)DEPTH * slot_elems * sizeof(F) + DEPTH * sizeof(double) +
+                  (size_t)(maxS + 1) * sizeof(F) + 2 * (size_t)maxS * sizeof(int) + 16;
+    if (QL) smem = (smem + 15) / 16 * 16 + (size_t)G * (maxS + 1) * sizeof(F);
     if (smem > budget) return false;
     // opt in; static shared memory counts against 48 KB too
-    if (!raise_dynamic_smem(k_traceback<F, G, DEPTH>, smem)) return true;  // the launch reports it
-    k_traceback<F, G, DEPTH><<<d.ninst, 32, smem, s>>>(d, maxS, slot_elems);
+    if (!raise_dynamic_smem(k_traceback<F, G, DEPTH, QL>, smem)) return true;  // the launch reports it
+    k_traceback<F, G, DEPTH, QL><<<d.ninst, 32, smem, s>>>(d, maxS, slot_elems);
     note_launch();
     return true;
 }
@@ -926,6 +993,9 @@ void launch(const BatchDev &d, cudaStream_t s) {
             if (launch_split<4>(d, s, 224 * 1024)) return;
             if (launch_split<3>(d, s, 224 * 1024)) return;
         }
+    }
+    if constexpr (sizeof(F) == 8) {
+        if (launch_cfg<F, 8, 24, true>(d, s, two)) return;
     }
     if (launch_cfg<F, 8, 24>(d, s, two)) return;
     if (launch_cfg<F, 4, 12>(d, s, two)) return;

@@ -446,6 +446,23 @@ __device__ __forceinline__ F2 f2_add2(F2 x, F2 y) {
 constexpr int NRW = 4;                      // reduction warps of the register variant
 constexpr int RBINS = (MAXT - 1 + NRW - 1) / NRW;  // time bins per reduction warp (<= 8)
 
+// FP64: the first time bin of reduction warp r (r = NRW: NB), the bins split by their
+// states (positions of the time-sorted column) rather than by count; whole bins, at most
+// RBINS per warp.
+__device__ __forceinline__ int fp64_bin_split(const int *bptr, int NB, int r) {
+    if (r >= NRW) return NB;
+    const int S = bptr[NB];
+    int prev = 0;
+    for (int q = 1; q <= r; q++) {
+        const int target = (q * S + NRW - 1) / NRW;
+        int b = prev;
+        while (b < NB && bptr[b] < target) b++;
+        b = imax(b, NB - (NRW - q) * RBINS);
+        prev = imin(b, prev + RBINS);
+    }
+    return prev;
+}
+
 template <typename F, int KPT>
 __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int maxM, int t2_in_smem) {
     extern __shared__ double dyn_d[];
@@ -481,14 +498,11 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
     // FP64: a column is computed from the previous one scaled by a power of two (the
     // exponent of its largest norm partial: exact, no division on the column's path) rather
     // than divided by its norm. Reduction warp NRW-1 (its own sub-partition where the owners
-    // fill at most three warps) divides one column later: it keeps the partials of column
-    // i-1 in fnp and, after barrier A of column i+1, writes column i-1 normalised into the
-    // table. A tree's last column is normalised exactly for the switch, as before.
+    // fill at most three warps), idle while the owners form the next column, divides and
+    // writes the previous column normalised into the table meanwhile. A tree's last column
+    // is normalised exactly for the switch, as before.
     constexpr bool pow2 = !Tab<F>::split;
     const bool finalizer = reducer && rw == NRW - 1;
-    F fnp[NRW];
-#pragma unroll
-    for (int r = 0; r < NRW; r++) fnp[r] = F(0);
 
     for (int bi = 0; bi < I.ntrees; bi++) {
         const int blk = I.block0 + bi;
@@ -569,16 +583,25 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
         }
         // reducer warp rw: bins [blo, bhi), sorted positions [plo, phi); lane l sums its
         // chunk of ceil((phi - plo) / 32) positions, lane b - blo adds bin b's chunk sums
-        const int blo = reducer ? rw * NB / NRW : 0, bhi = reducer ? (rw + 1) * NB / NRW : 0;
+        const int blo = !reducer ? 0 : sizeof(F) == 8 ? fp64_bin_split(bptr, NB, rw) : rw * NB / NRW;
+        const int bhi = !reducer ? 0 : sizeof(F) == 8 ? fp64_bin_split(bptr, NB, rw + 1) : (rw + 1) * NB / NRW;
         const int plo = reducer ? bptr[blo] : 0, phi = reducer ? bptr[bhi] : 0;
         const int chunk = imax((phi - plo + 31) >> 5, 1);
         const int clo = imin(plo + lane * chunk, phi), chi = imin(clo + chunk, phi);
         int l0 = 0, l1 = -1;
         int o1 = 0, o2 = 0, nbc = 0;  // bin boundaries inside the chunk, bins it spans
+        // FP64, one position per lane: the lane's bin starts at lane seg0, the warp's largest
+        // bin holds segmax positions, bin blo + lane ends at lane blast (-1: empty or none)
+        int seg0 = 0, segmax = 0, blast = -1;
         if (reducer) {
             int fb = blo;
             while (fb < bhi - 1 && bptr[fb + 1] <= clo) fb++;
             fbin[rw][lane] = fb;
+            seg0 = bptr[fb] - plo;
+            const int bl = blo + lane;
+            const int bsize = bl < bhi ? bptr[bl + 1] - bptr[bl] : 0;
+            segmax = __reduce_max_sync(0xffffffffu, bsize);
+            blast = bsize > 0 ? bptr[bl + 1] - 1 - plo : -1;
             const int b = blo + lane;
             if (b < bhi && bptr[b + 1] > bptr[b]) {
                 l0 = (bptr[b] - plo) / chunk;
@@ -740,12 +763,17 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
             if (reducer) {
                 F bin = 0;  // lane b - blo: bin b
                 if (sizeof(F) == 8 && chunk == 1) {
-                    // FP64, one position per lane: each bin's positions summed in order
-                    // directly, the additions the chunk partials and their gather make,
-                    // without the partials' round trip through shared memory
-                    const int b = blo + lane;
-                    if (b < bhi)
-                        for (int p = bptr[b]; p < bptr[b + 1]; p++) bin += colT[p];
+                    // FP64, one position per lane: an inclusive scan within each bin's lanes
+                    // (log2 of the largest bin's size dependent adds, where a sum in order
+                    // takes its size: each dependent FP64 step costs hundreds of cycles),
+                    // then lane b - blo takes bin b's total from the bin's last lane
+                    F v = plo + lane < phi ? colT[plo + lane] : F(0);
+                    for (int o = 1; o < segmax; o <<= 1) {
+                        const F x = __shfl_up_sync(0xffffffffu, v, o);
+                        if (lane - o >= seg0) v += x;
+                    }
+                    const F t = __shfl_sync(0xffffffffu, v, blast & 31);
+                    bin = blast >= 0 ? t : F(0);
                 } else {
                     // chunk sums by bin (positions sorted by time)
                     if (fast_chunk) {
@@ -797,26 +825,26 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
                 binv = bin;
                 // this warp's share of tf[a] = sum_b tm[b][a] bin[b], its bins in order
                 F tf = 0;
+                if constexpr (sizeof(F) == 8) {
+                    // two independent chains (even and odd bins)
+                    F ta = 0, tb = 0;
 #pragma unroll
-                for (int j = 0; j < RBINS; j++) {
-                    const F g = __shfl_sync(0xffffffffu, bin, j);
-                    if (blo + j < bhi) tf = fma(tmS[(blo + j) * MAXT + lane], g, tf);
-                }
-                tfp[rw][lane] = tf;
-                if (pow2 && finalizer && i >= 2) {
-                    // column i-2 (the other column buffer) normalised into the table
-                    F nrm = fnp[0];
+                    for (int j = 0; j < RBINS; j++) {
+                        const F g = __shfl_sync(0xffffffffu, bin, j);
+                        if (blo + j < bhi) {
+                            if (j & 1) tb = fma(tmS[(blo + j) * MAXT + lane], g, tb);
+                            else ta = fma(tmS[(blo + j) * MAXT + lane], g, ta);
+                        }
+                    }
+                    tf = ta + tb;
+                } else {
 #pragma unroll
-                    for (int r = 1; r < NRW; r++) nrm += fnp[r];
-                    const F inv = F(1) / nrm;
-                    if (lane == 0 && !(nrm > F(0)))
-                        report_error(d.err, ERR_ZERO_NORM, qi, bi, B.start + i - 2);
-                    if (!(bi == 0 && i == 2)) {
-                        const F *x = col + (c ^ 1) * maxS;
-                        F *o = fw + (size_t)(i - 2) * S;
-                        for (int k = lane; k < S; k += 32) o[k] = x[k] * inv;
+                    for (int j = 0; j < RBINS; j++) {
+                        const F g = __shfl_sync(0xffffffffu, bin, j);
+                        if (blo + j < bhi) tf = fma(tmS[(blo + j) * MAXT + lane], g, tf);
                     }
                 }
+                tfp[rw][lane] = tf;
             } else {
                 // same-branch dot of the owned states: sum_y tmatrix2[a_y][k] col[j1 + y]
 #pragma unroll
@@ -826,7 +854,25 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
                     if (valid(k)) {
                         const F *nb = cur + st_j1[q];
                         const int m = st_m[q];
-                        if (t2_in_smem) {
+                        if (t2_in_smem && sizeof(F) == 8) {
+                            // FP64: four independent chains, four loads ahead
+                            const F *row = t2s + st_off[q];
+                            F a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+                            int y = 0;
+                            for (; y + 3 < m; y += 4) {
+                                const F r0 = row[0], r1 = row[m], r2 = row[2 * m], r3 = row[3 * m];
+                                const F n0 = nb[y], n1 = nb[y + 1], n2 = nb[y + 2], n3 = nb[y + 3];
+                                a0 = fma(r0, n0, a0);
+                                a1 = fma(r1, n1, a1);
+                                a2 = fma(r2, n2, a2);
+                                a3 = fma(r3, n3, a3);
+                                row += 4 * m;
+                            }
+                            if (y < m) a0 = fma(row[0], nb[y], a0);
+                            if (y + 1 < m) a1 = fma(row[m], nb[y + 1], a1);
+                            if (y + 2 < m) a2 = fma(row[2 * m], nb[y + 2], a2);
+                            sv = (a0 + a1) + (a2 + a3);
+                        } else if (t2_in_smem) {
                             // even terms into sv, odd into s1, four loads ahead
                             const F *row = t2s + st_off[q];
                             int y = 0;
@@ -887,8 +933,17 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
                 scale = (F)__hiloint2double((2046 - E) << 20, 0);
                 if (acc_thread) acc.e += E - 1023;
                 if (finalizer) {
-#pragma unroll
-                    for (int r = 0; r < NRW; r++) fnp[r] = tfp[r][MAXT - 1];
+                    // column i-1 (the current buffer; the owners write the other) normalised
+                    static_assert(NRW == 4, "the FP64 norm sum is written for four warps");
+                    const F nrm = (tfp[0][MAXT - 1] + tfp[1][MAXT - 1]) + (tfp[2][MAXT - 1] + tfp[3][MAXT - 1]);
+                    const F inv = F(1) / nrm;
+                    if (lane == 0 && !(nrm > F(0)))
+                        report_error(d.err, ERR_ZERO_NORM, qi, bi, B.start + i - 1);
+                    if (!(bi == 0 && i == 1)) {
+                        const F *x = col + c * maxS;
+                        F *o = fw + (size_t)(i - 1) * S;
+                        for (int k = lane; k < S; k += 32) o[k] = x[k] * inv;
+                    }
                 }
             }
             // finalise column i-1: normalised into the table (the instance's column 0
@@ -927,9 +982,16 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
                     if (!valid(k)) continue;
                     const F xk = x_own[q];
                     if (!pow2 && write_prev) outp[k] = xk * inv_norm;
-                    F tfk = tfp[0][st_time[q]];
+                    const int tq = st_time[q];
+                    F tfk;
+                    if constexpr (pow2) {
+                        static_assert(NRW == 4, "the FP64 share sum is written for four warps");
+                        tfk = (tfp[0][tq] + tfp[1][tq]) + (tfp[2][tq] + tfp[3][tq]);
+                    } else {
+                        tfk = tfp[0][tq];
 #pragma unroll
-                    for (int r = 1; r < NRW; r++) tfk += tfp[r][st_time[q]];
+                        for (int r = 1; r < NRW; r++) tfk += tfp[r][tq];
+                    }
                     const F sv = tfk + dq[q];
                     F v;
                     if constexpr (Tab<F>::split) {
@@ -943,7 +1005,10 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
                         v = x.hi;
                         x_lo[q] = x.lo;
                     } else {
-                        v = emit(sv, ci, vrow, q, true) * scale;
+                        // the emission times the power of two (exact) off the chain of sv
+                        const F f = ci == COL_MASKED ? scale
+                                                     : (ci == COL_INVARIANT ? st_inv[q] : e_next[q]) * scale;
+                        v = sv * f;
                     }
                     nxt[k] = v;
                     colT[st_rank[q]] = v;

@@ -498,11 +498,13 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
     // FP64: a column is computed from the previous one scaled by a power of two (the
     // exponent of its largest norm partial: exact, no division on the column's path) rather
     // than divided by its norm. Reduction warp NRW-1 (its own sub-partition where the owners
-    // fill at most three warps), idle while the owners form the next column, divides and
-    // writes the previous column normalised into the table meanwhile. A tree's last column
-    // is normalised exactly for the switch, as before.
+    // fill at most three warps) divides while the owners form the next column (fin_inv) and
+    // writes the column normalised into the table at the start of the column after. A
+    // tree's last column is normalised exactly for the switch, as before.
     constexpr bool pow2 = !Tab<F>::split;
     const bool finalizer = reducer && rw == NRW - 1;
+    F fin_inv = F(0);
+    bool fin_pending = false;
 
     for (int bi = 0; bi < I.ntrees; bi++) {
         const int blk = I.block0 + bi;
@@ -761,6 +763,13 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
             const F *cur = col + c * maxS;
             F binv = F(0);  // reducers, lane b - blo: bin b of column i-1
             if (reducer) {
+                if (pow2 && finalizer && fin_pending) {
+                    // column i-2 (the other column buffer) normalised into the table
+                    const F *x = col + (c ^ 1) * maxS;
+                    F *o = fw + (size_t)(i - 2) * S;
+                    for (int k = lane; k < S; k += 32) o[k] = x[k] * fin_inv;
+                    fin_pending = false;
+                }
                 F bin = 0;  // lane b - blo: bin b
                 if (sizeof(F) == 8 && chunk == 1) {
                     // FP64, one position per lane: an inclusive scan within each bin's lanes
@@ -933,17 +942,13 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
                 scale = (F)__hiloint2double((2046 - E) << 20, 0);
                 if (acc_thread) acc.e += E - 1023;
                 if (finalizer) {
-                    // column i-1 (the current buffer; the owners write the other) normalised
+                    // the reciprocal norm of column i-1, written into the table next column
                     static_assert(NRW == 4, "the FP64 norm sum is written for four warps");
                     const F nrm = (tfp[0][MAXT - 1] + tfp[1][MAXT - 1]) + (tfp[2][MAXT - 1] + tfp[3][MAXT - 1]);
-                    const F inv = F(1) / nrm;
+                    fin_inv = F(1) / nrm;
+                    fin_pending = !(bi == 0 && i == 1);
                     if (lane == 0 && !(nrm > F(0)))
                         report_error(d.err, ERR_ZERO_NORM, qi, bi, B.start + i - 1);
-                    if (!(bi == 0 && i == 1)) {
-                        const F *x = col + c * maxS;
-                        F *o = fw + (size_t)(i - 1) * S;
-                        for (int k = lane; k < S; k += 32) o[k] = x[k] * inv;
-                    }
                 }
             }
             // finalise column i-1: normalised into the table (the instance's column 0

@@ -1,6 +1,7 @@
 """Generate the golden fixtures in tests/golden/ from the compiled reference.
 
-Run where the reference checkout exists (default /root/reference, or $AWG_REFERENCE):
+Run where the reference checkout exists ($AWG_REFERENCE, default: a sibling of this
+repository named "reference"):
 
     python tests/golden/make_golden.py            # all fixtures
     python tests/golden/make_golden.py infsites   # only the infinite-sites ones
@@ -67,7 +68,7 @@ from argweaver_gb300.problem import Problem  # noqa: E402
 from argweaver_gb300.sim import simulate  # noqa: E402
 import pyoracle  # noqa: E402
 
-REF = os.environ.get("AWG_REFERENCE", "/root/reference")
+REF = os.environ.get("AWG_REFERENCE", os.path.join(os.path.dirname(ROOT), "reference"))
 HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
 
 

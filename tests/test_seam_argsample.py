@@ -21,7 +21,7 @@ import subprocess
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = os.environ.get("AWG_REFERENCE", "/root/reference")
+REF = os.environ.get("AWG_REFERENCE", os.path.join(os.path.dirname(ROOT), "reference"))
 SEAM = os.path.join(ROOT, "oracle", "_ref", "seam")
 SITES = os.path.join(REF, "examples", "sim1", "sim1.sites")
 

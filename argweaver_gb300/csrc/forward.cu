@@ -688,6 +688,9 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
                     if (valid(owned(q))) e_next[q] = var[(size_t)v1 * S + owned(q)];
         };
         __syncthreads();  // t2s, fbin; the rank scratch is read
+        // reducers: bin blo + lane's slot among the partials of chunk l0 (the chunk holding
+        // its first position); every later chunk of the bin starts inside it (slot 0)
+        const int slot0 = reducer && l0 <= l1 ? blo + lane - fbin[rw][l0] : 0;
 
         // ---- first column of the block
         if (bi == 0) {
@@ -826,7 +829,7 @@ __global__ void __launch_bounds__(512) k_forward_reg(BatchDev d, int maxS, int m
                         F v[8];
 #pragma unroll
                         for (int t = 0; t < 8; t++)
-                            v[t] = l + t <= l1 ? part[rw][l + t][blo + lane - fbin[rw][l + t]] : F(0);
+                            v[t] = l + t <= l1 ? part[rw][l + t][l + t == l0 ? slot0 : 0] : F(0);
 #pragma unroll
                         for (int t = 0; t < 8; t++) bin += v[t];
                     }

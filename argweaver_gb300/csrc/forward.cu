@@ -384,26 +384,31 @@ __global__ void __launch_bounds__(512) k_forward(BatchDev d, int maxS, int maxM,
 }
 
 // ---------------------------------------------------------------------------------------
-// Register-resident variant for trees of up to KPT * (blockDim.x - 32) states.
+// Register-resident variant for trees of up to KPT * (blockDim.x - 32 NRW) states.
 //
-// Warp 0 is the reduction warp; the other threads own states k = (t - 32) + q * NTS
-// (q < KPT), in state order, so lanes holding one node's states read the same neighbours
-// and consecutive same-branch entries. A state's time, node span, row offset, time-sorted
-// rank and invariant emission stay in registers for the tree's columns, and the next
-// variant column's emissions are loaded a column ahead. Per column, two CTA barriers:
+// Warps 0 .. NRW-1 are reduction warps; the other threads own states
+// k = (t - 32 NRW) + q * NTS (q < KPT), in state order, so lanes holding one node's states
+// read the same neighbours and consecutive same-branch entries. A state's time, node span,
+// row offset, time-sorted rank and invariant emission stay in registers for the tree's
+// columns, and the next variant column's emissions are loaded a column ahead. Per column,
+// two CTA barriers:
 //   A  column i-1 complete in state order and time-sorted (each time bin a contiguous
 //      range of the sorted copy). In parallel:
-//        warp 0: lane l sums its contiguous chunk of ceil(S/32) sorted positions bin by
-//                bin; lane b adds bin b's chunk sums in lane order; lane a forms
-//                tf[a] = sum_b tm[b][a] bin[b] by shuffles, lane 31 (ones) the norm
+//        reduction warp r: the time bins of its share (FP32: a quarter of the bins; FP64:
+//                whole bins holding about a quarter of the states) summed from the sorted
+//                copy, then lane a forms its share of tf[a] = sum_b tm[b][a] bin[b] by
+//                shuffles, lane 31 (tmatrix column of ones) its share of the norm
 //        owners: the same-branch dot sum_y tmatrix2[a_y][k] col[j1 + y] of their states
-//   B  tf and the norm published: owners finish column i (tf of their time + dot, stay,
-//      emission, rescaling) and write column i-1 / norm to HBM.
+//   B  the shares published: owners add them for their state's time and finish column i
+//      (dot, stay, emission, rescaling). FP32 divides by the norm and writes column i-1;
+//      FP64 scales by a power of two and reduction warp NRW-1 divides and writes the
+//      previous column into the table.
 // Every sum has an order fixed by the tree alone, so results do not depend on the block
 // size or on the other problems of the batch. Products are summed with fused multiply-adds
 // (explicit: this file compiles without FMA contraction): on GB300 a warp's FP64 instruction
-// holds its sub-partition's FP64 pipe for about 64 cycles, so the plain FP64 path's cost is
-// its count of FP64 instructions; FMA halves it for the dot and tf and rounds once.
+// holds its sub-partition's FP64 pipe for about 64 cycles and a dependent FP64 step costs a
+// few hundred cycles, so the plain FP64 path is shaped to issue few FP64 instructions in
+// short dependent chains.
 // FP32 pair arithmetic (value = hi + lo, |lo| <= ulp(hi) / 2) for the dominant path of
 // the FP32 forward step. Within a tree the normalised column converges to the fixed point
 // of the step; a rounding error of the step shifts that fixed point by about the error
